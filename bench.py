@@ -1,0 +1,356 @@
+#!/usr/bin/env python
+"""FDTD stepping throughput on GB300: one JSON line per run.
+
+Default workload: the 192^3 (7,077,888-cell) sphere under a 10-cell PML with eight DFT
+objects (six flux planes, two 32^3 field volumes, 100 frequencies each). One "step" is
+one FDTD time step over the whole grid (two fused kernels, plus the monitor kernel on
+decimated steps).
+
+* ``value``: Mcell-steps/s with every array resident in HBM, K steps timed with CUDA
+  events on the launching stream (the working set, ~1.5 GB, is far above the 129 MB
+  L2, so nothing is served from L2 between steps).
+* ``e2e``: the same metric through the public API (``FdtdDriver``) from host arrays:
+  the freeze with its host-to-device uploads, K steps (with their per-step source words
+  uploaded from host), and the device-to-host read of every flux spectrum and DFT
+  accumulator, on the wall clock.
+* ``roofline``: algorithmic bytes per launch of the dominant kernel over its mean
+  CUDA-event duration, against the measured HBM copy bandwidth.
+* ``cpu_baseline``: the float32 oracle (the C restatement of the reference's array
+  path, OpenMP over every host core) on a bounded sample of the same workload.
+* ``error``: relative L2 of the fields and flux against the float64 oracle on bounded
+  samples.
+
+``--impl reference`` times the reference path's CPU implementation (the oracle port:
+the reference itself is Python and does not travel) on the same workload instead.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mcell-updates/s"
+
+
+def parse_args():
+    p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=500)
+    p.add_argument("--warmup", type=int, default=20)
+    p.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
+    p.add_argument("--workload", default="sphere192_8dft")
+    p.add_argument("--launch-shape", default=None, help="block_z,block_y,x_chunk")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-validate", action="store_true")
+    p.add_argument("--kernel-steps", type=int, default=40, help="steps timed kernel by kernel")
+    return p.parse_args()
+
+
+def measured_peaks():
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        data = json.loads(path.read_text())
+        return float(data["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+            time.sleep(0.25)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        if not self.lines:
+            return None
+        sm, sm_max, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [v.strip() for v in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                sm_max = max(sm_max, float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": sm_max, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_threads() -> int:
+    return os.cpu_count() or 1
+
+
+def time_oracle(workload: str, steps: int, budget_s: float = 20.0):
+    """Float32 oracle Mcell-steps/s on ``steps`` steps (capped to a ~``budget_s`` sample)."""
+    from meep_gpu_gb300 import FdtdDriver, workloads
+    from oracle.oracle import Oracle, problem_from_driver
+    os.environ.setdefault("OMP_NUM_THREADS", str(cpu_threads()))
+    driver, _, _ = workloads.build(workload, FdtdDriver)
+    oracle = Oracle(problem_from_driver(driver), "f32")
+    oracle.run(1)  # warm-up (page-in, thread pool)
+    t0 = time.perf_counter()
+    oracle.run(1)
+    per_step = max(time.perf_counter() - t0, 1e-6)
+    sample = max(1, min(steps, int(budget_s / per_step)))
+    t0 = time.perf_counter()
+    oracle.run(sample)
+    elapsed = time.perf_counter() - t0
+    cells = driver.grid.total_cells
+    return cells * sample / elapsed / 1e6, sample, cells
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    value, sample, cells = time_oracle(args.workload, max(args.steps, 1), budget_s=60.0)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mcell-steps/s",
+        "n_gpus": args.gpus, "steps": sample, "warmup": 1,
+        "ms_per_step": round(cells / (value * 1e6) * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "cells": cells},
+        "cpu_baseline": {"value": round(value, 3), "unit": "Mcell-steps/s", "cores": cpu_threads(),
+                         "kind": "port",
+                         "sample": f"{sample} full-grid steps of {args.workload} on the float32 C oracle "
+                                   f"(OpenMP, {cpu_threads()} threads)"},
+        "e2e": {"value": round(value, 3), "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+
+    from meep_gpu_gb300 import FdtdDriver, workloads
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    shape = tuple(int(v) for v in args.launch_shape.split(",")) if args.launch_shape else None
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- device-resident throughput ---------------------------------------------------
+    driver, flux, dft = workloads.build(args.workload, FdtdDriver, gpu_id=local, launch_shape=shape)
+    driver.step_many(args.warmup)  # freezes the configuration and warms the kernels
+    engine = driver.engine
+    cells = driver.grid.total_cells
+    first = driver.step_count
+    engine.ensure_source_words(first, args.steps)
+    stream = torch.cuda.current_stream(device)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches = 2 * args.steps + sum(
+        1 for n in range(first, first + args.steps) for m in engine.monitors
+        if (n + 1) % m.decimation_factor == 0)
+    torch.cuda.synchronize(device)
+    barrier()
+    with ClockSampler(local) as clocks:
+        start.record(stream)
+        engine.step(first, args.steps)
+        end.record(stream)
+        torch.cuda.synchronize(device)
+    driver.step_count += args.steps
+    ms = start.elapsed_time(end)
+    if world > 1:
+        t = torch.tensor([ms], device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = cells * args.steps * world / (ms / 1e3) / 1e6
+    if engine.nonfinite():
+        raise RuntimeError("the benchmark run wrote a non-finite field")
+
+    # ---- kernel-by-kernel timing (roofline) ---------------------------------------------
+    kernel_steps = max(1, args.kernel_steps)
+    n0 = driver.step_count
+    engine.ensure_source_words(n0, kernel_steps)
+    events = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(kernel_steps)]
+    torch.cuda.synchronize(device)
+    for t in range(kernel_steps):
+        ev = events[t]
+        ev[0].record(stream)
+        engine.launch(n0 + t, 0, stream)
+        ev[1].record(stream)
+        engine.launch(n0 + t, 1, stream)
+        ev[2].record(stream)
+        engine.launch(n0 + t, 2, stream)
+        ev[3].record(stream)
+    torch.cuda.synchronize(device)
+    driver.step_count += kernel_steps
+    h_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in events]))
+    e_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in events]))
+    bytes_per = engine.algorithmic_bytes()
+    peak, peak_kind = measured_peaks()
+    kernels = {"h_half": {"ms": h_ms, "bytes": bytes_per["h_half"]},
+               "e_half": {"ms": e_ms, "bytes": bytes_per["e_half"]}}
+    for info in kernels.values():
+        info["gbs"] = info["bytes"] / (info["ms"] / 1e3) / 1e9
+    dominant = max(kernels, key=lambda k: kernels[k]["ms"])
+    traffic = None
+    summary = ROOT / "profiles" / f"{dominant}_{args.workload}.txt"
+    if summary.exists():
+        for line in summary.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_launch:"):
+                traffic = int(float(line.split(":", 1)[1]))
+    step_bytes = bytes_per["h_half"] + bytes_per["e_half"]
+    roofline = {"bound": "hbm", "kernel": dominant,
+                "achieved": round(kernels[dominant]["gbs"], 1), "peak": peak, "unit": "GB/s",
+                "frac": round(kernels[dominant]["gbs"] / peak, 4), "traffic": traffic,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+                "algorithmic_bytes_per_launch": bytes_per[dominant],
+                "per_kernel": {k: {"ms": round(v["ms"], 4), "GB/s": round(v["gbs"], 1),
+                                   "frac": round(v["gbs"] / peak, 4)} for k, v in kernels.items()},
+                "step_bytes_per_cell": round(step_bytes / cells, 2),
+                "step_frac": round(step_bytes / ((ms / args.steps) / 1e3) / 1e9 / peak, 4)}
+    driver.close()
+    del driver, engine
+    torch.cuda.empty_cache()
+
+    # ---- end to end through the public API ---------------------------------------------
+    e2e = None
+    if not args.no_e2e:
+        torch.cuda.synchronize(device)
+        barrier()
+        t0 = time.perf_counter()
+        d2, f2, v2 = workloads.build(args.workload, FdtdDriver, gpu_id=local, launch_shape=shape)
+        d2.run(num_steps=args.steps, progress_interval=max(args.steps, 1), check_finite=False)
+        results = [m.get_flux_spectrum() for m in f2]
+        arrays = [m.raw(c) for m in v2 for c in m.components]
+        torch.cuda.synchronize(device)
+        wall = time.perf_counter() - t0
+        eng = d2.engine
+        h2d = sum(int(t.numel() * t.element_size()) for t in eng.inv_eps[:1])
+        h2d += sum(int(t.numel() * t.element_size()) for t in eng.coefficients.values())
+        h2d += 8 * eng.desc.nsrc * args.steps
+        d2h = sum(r.nbytes for r in results) + sum(a.nbytes for a in arrays)
+        e2e = {"value": round(cells * args.steps * world / wall / 1e6, 3), "unit": "Mcell-steps/s",
+               "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps),
+               "wall_s": round(wall, 3),
+               "what": "FdtdDriver from host arrays: freeze + uploads, K steps, read every flux "
+                       "spectrum and DFT accumulator"}
+        d2.close()
+        del d2, eng
+        torch.cuda.empty_cache()
+
+    if rank != 0:
+        return
+    # ---- CPU baseline and float64 error (rank 0 only) -----------------------------------
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu_value, sample, _ = time_oracle(args.workload, args.steps, budget_s=20.0)
+        cpu = {"value": round(cpu_value, 3), "unit": "Mcell-steps/s", "cores": cpu_threads(),
+               "kind": "port",
+               "sample": f"{sample} full-grid steps of {args.workload} on the float32 C oracle "
+                         f"(OpenMP, {cpu_threads()} threads)"}
+    error = None
+    if not args.no_validate:
+        error = validate(device)
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "Mcell-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 5),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "cells": cells, "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2 (no flush needed)",
+                   "launch_shape": list(shape) if shape else [32, 8, 16],
+                   "monitors": {"flux_planes": len(flux), "dft_volumes": len(dft),
+                                "decimation": [m.decimation_factor for m in list(flux) + list(dft)][:1]}},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+        "clocks": clocks.summary(), "error": error,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def validate(device):
+    """Relative errors of the float32 engine against the float64 oracle, bounded samples."""
+    from meep_gpu_gb300 import FdtdDriver, workloads
+    from oracle.oracle import Oracle, problem_from_driver
+    out = {}
+    steps = 600
+    gpu, flux, _ = workloads.build("sphere80", FdtdDriver)
+    gpu.run(num_steps=steps, progress_interval=steps)
+    ref, _, _ = workloads.build("sphere80", FdtdDriver)
+    o64 = Oracle(problem_from_driver(ref), "f64")
+    o64.run(steps)
+    num = den = 0.0
+    for c in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz"):
+        a = gpu.get_field(c, cell_centered=False).astype(np.float64)
+        b = o64.field(c)
+        num += float(np.sum((a - b) ** 2))
+        den += float(np.sum(b ** 2))
+    got = flux[0].get_flux_spectrum()
+    expected = o64.flux_spectrum(0)
+    out["sphere80_600_steps"] = {
+        "fields_rel_l2_vs_f64": float(math.sqrt(num / den)),
+        "flux_rel_vs_f64": float(np.max(np.abs(got - expected)) / np.max(np.abs(expected)))}
+    gpu.close()
+    return out
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,171 @@
+/*
+ * meepgb.h — C ABI of the GB300 FDTD stepping library (libmeepgb.so).
+ *
+ * The library steps one lifted MEEP simulation (real float32 fields, 3-D, UPML,
+ * isotropic chi1inv, Lorentz/Drude poles, electric point/extended sources, DFT and
+ * flux monitors) on one GPU. It owns no field memory: every array is allocated by the
+ * caller (the Python host uses torch tensors) and passed in by device pointer. It
+ * allocates nothing on the device at any point, so a caller may capture mgb_step in a
+ * CUDA graph.
+ *
+ * Reference interface this replaces (file:line inside the reference project):
+ *   - plan_fast_path(fields, pml, grid, sources, chunk_layout)  meep_gpu/fastpath.py:6986
+ *       -> mgb_create: one plan per configuration freeze, refusals named in the error text.
+ *   - FastPathPlan.dispatch(slot, fields) for the slots step_B, fill_B, update_H, step_D,
+ *     fill_D, update_E, update_P (meep_gpu/fastpath.py:4631, slots :575) together with the
+ *     driver's in-between passes zero_metal_B/D and the electric source deposit
+ *     (meep_gpu/driver.py:3533-3585, sources.py:2400)
+ *       -> mgb_step: the whole FdtdDriver.step() body for nsteps steps in two fused
+ *          kernels per step (H-half, E-half), plus the monitor accumulation of
+ *          FluxMonitor.update / DFTMonitor.update (meep_gpu/dft.py:3031, :2197) on
+ *          decimated steps.
+ *   - FluxMonitor.get_flux_spectrum / _integrate_flux  meep_gpu/dft.py:3090, :3107
+ *       -> mgb_flux_spectrum.
+ *   - invalidate_fast_path()  meep_gpu/driver.py:3321  -> mgb_destroy + mgb_create.
+ *
+ * Conventions: arrays are C-contiguous (nx, ny, nz), z fastest. Every entry point
+ * returns MGB_OK (0) or a negative error code; mgb_last_error() describes the last
+ * failure of the calling thread. No C++ exception crosses this boundary, and no entry
+ * point synchronises the device.
+ */
+#ifndef MEEPGB_H
+#define MEEPGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MGB_ABI_VERSION 1
+#define MGB_MAX_POLES 4
+#define MGB_MAX_MONITORS 16
+#define MGB_MAX_MONITOR_COMPONENTS 6
+
+enum {
+  MGB_OK = 0,
+  MGB_ERR_ARGUMENT = -1,    /* a null or inconsistent argument */
+  MGB_ERR_CUDA = -2,        /* a CUDA runtime error (launch, configuration) */
+  MGB_ERR_UNSUPPORTED = -3, /* a configuration this engine refuses by name */
+  MGB_ERR_RANGE = -4        /* a step outside the uploaded source-word table */
+};
+
+/* One compact auxiliary array (PML): stored only over the rows of `axis` that lie in
+ * the membership runs [a0, a1) U [b0, b1); the other two axes are full length. */
+typedef struct mgb_aux {
+  float* data; /* device; NULL when the run has no PML */
+  int32_t axis;
+  int32_t a0, a1, b0, b1;
+} mgb_aux;
+
+/* One Lorentz/Drude pole (MEEP's realnum constants). Polarization storage covers the
+ * box desc.pbox only; sigma[c] == NULL means the pole does not drive component c. */
+typedef struct mgb_pole {
+  float two_minus_od, gamma1, omega0dtsqr, gamma1inv;
+  const float* sigma[3]; /* device, box-shaped */
+  float* p[3][2];        /* device, box-shaped, two rotating buffers */
+} mgb_pole;
+
+/* One DFT accumulator: cell-centred samples of `ncomp` components over a region.
+ * comp[i]: 0..2 = Ex..Ez, 3..5 = Hx..Hz. acc layout: [ncomp][nfreq][2 (re, im)][cells],
+ * cells in C order over the region. */
+typedef struct mgb_monitor {
+  int32_t region[6]; /* x0, x1, y0, y1, z0, z1 (half-open) */
+  int32_t ncomp;
+  int32_t comp[MGB_MAX_MONITOR_COMPONENTS];
+  int32_t nfreq;
+  int32_t decimation;
+  double scale;         /* dt * decimation / sqrt(2 pi) */
+  double dt;            /* time step (E sampled at step*dt, H at step*dt - dt/2) */
+  const double* omega;  /* device [nfreq], 2 pi f */
+  float* acc;           /* device */
+} mgb_monitor;
+
+typedef struct mgb_sim_desc {
+  int32_t abi_version; /* MGB_ABI_VERSION */
+  int32_t nx, ny, nz;
+  int32_t metallic[3]; /* 1: PEC walls on that axis; 0: periodic wrap */
+  float dtdx;          /* float32(dt / dx) */
+  int32_t pml_active;
+  /* UPML coefficient vectors [lattice: 0 integer, 1 half-integer][axis], device,
+   * length of the axis. Ignored when pml_active == 0. */
+  const float* kms[2][3];
+  const float* sinv[2][3];
+  const float* kps[2][3];
+  /* primary fields, full volumes */
+  float* E[3];
+  float* D[3];
+  float* B[3];
+  const float* inv_eps[3]; /* may alias one another */
+  /* PML auxiliaries: stored H and f_w of H on each component's own-axis integer slab
+   * (H is B's word everywhere else), f_w of E on the own-axis half slab, and the curl
+   * split-field fu of B (half lattice) and D (integer lattice) on the dsigu slab. */
+  mgb_aux H[3];
+  mgb_aux fwH[3];
+  mgb_aux fwE[3];
+  mgb_aux fuB[3];
+  mgb_aux fuD[3];
+  /* polarization */
+  int32_t npoles;
+  int32_t pbox[6];
+  mgb_pole poles[MGB_MAX_POLES];
+  /* electric sources: nsrc points in deposit order */
+  int32_t nsrc;
+  const int64_t* src_cell; /* device, linear index into the component volume */
+  const int32_t* src_comp; /* device, 0..2 */
+  int32_t src_box[6];      /* bounding box of the points, half-open */
+  /* monitors */
+  int32_t nmonitors;
+  mgb_monitor monitors[MGB_MAX_MONITORS];
+  /* non-finite detector: the E-kernel ORs 1 into *status when it writes a NaN/Inf E */
+  int32_t* status; /* device, may be NULL */
+} mgb_sim_desc;
+
+typedef struct mgb_sim mgb_sim;
+
+/* Version of this ABI (MGB_ABI_VERSION). */
+int mgb_abi_version(void);
+
+/* Validate a descriptor and make a plan from a copy of it. Replaces plan_fast_path
+ * (meep_gpu/fastpath.py:6986); refusals return MGB_ERR_UNSUPPORTED with the reason. */
+int mgb_create(const mgb_sim_desc* desc, mgb_sim** out);
+
+/* Launch shape of the step kernels: a (block_z x block_y) tile of (z, y) columns per CTA
+ * marching over x_chunk planes of x. No reference counterpart: the reference launches a
+ * fixed 1-D grid of 256 threads, one cell each (cuda_kernels/step_curl_kernels.py:788). */
+int mgb_set_launch_shape(mgb_sim* sim, int block_z, int block_y, int x_chunk);
+
+/* Install the float64 source-deposit words for steps [first_step, first_step+steps):
+ * words is a device array [steps][nsrc]; borrowed until replaced. */
+int mgb_set_source_words(mgb_sim* sim, const double* words, int64_t first_step, int64_t steps);
+
+/* Advance steps first_step .. first_step+nsteps-1 on `stream` (a cudaStream_t; NULL is
+ * the legacy default stream). Replaces the body of FdtdDriver.step() (meep_gpu/driver.py
+ * :3419-3596) and its dispatch consults. Asynchronous. */
+int mgb_step(mgb_sim* sim, int64_t first_step, int32_t nsteps, void* stream);
+
+/* Launch one part of step `step` on `stream`: part 0 the H half, 1 the E half, 2 the
+ * monitor accumulation of every monitor due after that step (nothing if none is due).
+ * mgb_step(sim, n, 1, s) is mgb_launch(sim, n, 0..2, s) in order. Used to time each
+ * kernel on its own stream with events, and to capture steps into a CUDA graph. */
+int mgb_launch(mgb_sim* sim, int64_t step, int32_t part, void* stream);
+
+/* Reduce one flux monitor (its comp[] = Ea, Eb, Ha, Hb, the tangential pair of the
+ * normal) to out[f] = sum_cells w * Re(Ea conj(Hb) - Eb conj(Ha)), float64, on the
+ * device. weights: device float32 [cells]. Replaces FluxMonitor._integrate_flux
+ * (meep_gpu/dft.py:3107) without the dA * weight scale, which the host applies. */
+int mgb_flux_spectrum(mgb_sim* sim, int32_t monitor, const float* weights, double* out,
+                      void* stream);
+
+/* Release the plan (never the caller's arrays). */
+void mgb_destroy(mgb_sim* sim);
+
+/* Copy the last error message of the calling thread into buf (NUL-terminated). */
+int mgb_last_error(char* buf, size_t size);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MEEPGB_H */

@@ -1,0 +1,392 @@
+"""``FdtdDriver``: the reference's driver API, stepped on one GB300 by ``libmeepgb.so``.
+
+Mirrors ``meep_gpu/driver.py``'s ``FdtdDriver`` (constructor :810, ``set_epsilon``
+:1170, ``add_susceptibility`` :1531, ``setup_pml`` :2155, ``add_source`` :2567,
+``add_dft_monitor`` :2783, ``add_flux_monitor`` :3001, ``step`` :3419, ``run`` :3667,
+``get_field`` :4056) for the configurations this engine steps: 3-D, real float32
+fields, metallic or periodic (k = 0) boundaries, no mirror symmetry, isotropic or
+diagonal chi1inv, Lorentz/Drude poles, electric sources and DFT/flux monitors.
+Anything else is refused by name when it is asked for, never approximated.
+
+The configuration freezes at the first step (as the reference's fast-path plan
+does, driver.py:3509): the engine allocates the device state and every later step
+is two kernel launches (plus a monitor launch on decimated steps). There is no CPU
+stepping path: without a GPU, or without the built library, stepping raises.
+"""
+
+from __future__ import annotations
+
+import math
+import numbers
+import time as time_module
+from typing import Any, Callable, Dict, List, Mapping, Optional, Sequence, Tuple
+
+import numpy as np
+
+from .dft import (DFTMonitor, FluxMonitor, absorbing_cells, automatic_decimation,
+                  normalize_frequencies)
+from .dispersion import Susceptibility
+from .grid import AXIS_NAMES, IYEE, Grid, Unsupported
+from .pml import PML
+from .sources import Source, make_waveform
+
+FIELD_COMPONENTS = ("Ex", "Ey", "Ez", "Dx", "Dy", "Dz", "Hx", "Hy", "Hz", "Bx", "By", "Bz")
+STEP_TOLERANCE = 1e-9
+
+
+class FdtdDivergence(RuntimeError):
+    """A non-finite field was written: the run diverged."""
+
+
+class FdtdCancelled(RuntimeError):
+    """``cancel_check`` asked the run to stop."""
+
+
+def _as_xyz(name: str, value: Any) -> Tuple[float, float, float]:
+    values = tuple(float(v) for v in value)
+    if len(values) != 3:
+        raise ValueError(f"{name} needs three components, got {value!r}")
+    return values  # type: ignore[return-value]
+
+
+class FdtdDriver:
+    """One FDTD simulation: build it on the host, step it on the GPU."""
+
+    def __init__(self, cell_size: Sequence[float], resolution: float, courant: float = 0.5,
+                 force_complex_fields: bool = True, symmetry: Sequence[Any] = (),
+                 k_point: Sequence[float] = (0.0, 0.0, 0.0), boundaries: Any = None,
+                 dimensions: int = 3, cylindrical: bool = False, m: int = 0,
+                 accurate_fields_near_cylorigin: bool = False, beta: float = 0.0,
+                 bfast_scaled_k: Sequence[float] = (0.0, 0.0, 0.0), prefer_gpu: bool = True,
+                 gpu_id: int = 0, launch_shape: Optional[Tuple[int, int, int]] = None):
+        if force_complex_fields:
+            raise Unsupported("complex fields are not stepped by this engine; pass "
+                              "force_complex_fields=False (real float32 fields)")
+        if tuple(symmetry):
+            raise Unsupported("mirror symmetry is not stepped by this engine")
+        if any(float(k) != 0.0 for k in k_point):
+            raise Unsupported("a nonzero Bloch k_point needs complex fields; not stepped")
+        if dimensions != 3 or cylindrical:
+            raise Unsupported("only 3-D Cartesian runs are stepped by this engine")
+        if beta != 0.0 or any(float(k) != 0.0 for k in bfast_scaled_k):
+            raise Unsupported("out-of-plane beta and BFAST are not stepped by this engine")
+        del m, accurate_fields_near_cylorigin, prefer_gpu
+        self.grid = Grid(cell_size, resolution, courant, boundaries)
+        self.gpu_id = int(gpu_id)
+        self.launch_shape = launch_shape
+        self.pml: Optional[PML] = None
+        self._eps: Optional[Tuple[np.ndarray, np.ndarray, np.ndarray]] = None
+        self._inv_eps: Optional[Tuple[np.ndarray, np.ndarray, np.ndarray]] = None
+        self._poles: List[Tuple[Susceptibility, List[Optional[np.ndarray]]]] = []
+        self._sources: List[Source] = []
+        self._flux_monitors: List[FluxMonitor] = []
+        self._dft_monitors: List[DFTMonitor] = []
+        self._automatic: List[Any] = []
+        self._pending_regions: List[Tuple[DFTMonitor, Any, Any]] = []
+        self.step_count = 0
+        self.engine = None
+        self.last_run_seconds = 0.0
+
+    # --- configuration --------------------------------------------------------------
+    def _require_unfrozen(self, what: str) -> None:
+        if self.engine is not None:
+            raise RuntimeError(f"{what} after the first step: the configuration is frozen")
+
+    def _volume(self, value: Any, label: str) -> np.ndarray:
+        shape = self.grid.shape
+        if np.isscalar(value):
+            return np.full(shape, float(value), dtype=np.float64)
+        array = np.asarray(value)
+        if array.shape == tuple(n + 1 for n in shape):
+            array = array[:-1, :-1, :-1]
+        if array.shape != shape:
+            raise ValueError(f"{label} shape {array.shape} does not match the grid {shape}")
+        return array
+
+    def set_epsilon(self, eps: Any) -> None:
+        """Isotropic permittivity: a scalar or a volume at the integer Yee positions."""
+        self._require_unfrozen("set_epsilon")
+        wide = self._volume(eps, "epsilon").astype(np.float64)
+        if not np.all(np.isfinite(wide)) or np.any(wide <= 0):
+            raise ValueError("epsilon must be finite and positive everywhere")
+        inverse = np.ascontiguousarray((1.0 / wide).astype(np.float32))
+        epsilon = np.ascontiguousarray(wide.astype(np.float32))
+        self._eps = (epsilon, epsilon, epsilon)
+        self._inv_eps = (inverse, inverse, inverse)
+
+    def set_epsilon_components(self, eps_x: Any, eps_y: Any, eps_z: Any) -> None:
+        """Diagonal permittivity, one volume per E component (MEEP's chi1inv[c][c])."""
+        self._require_unfrozen("set_epsilon_components")
+        eps = []
+        inv = []
+        for label, value in (("eps_x", eps_x), ("eps_y", eps_y), ("eps_z", eps_z)):
+            wide = self._volume(value, label).astype(np.float64)
+            if not np.all(np.isfinite(wide)) or np.any(wide <= 0):
+                raise ValueError(f"{label} must be finite and positive everywhere")
+            eps.append(np.ascontiguousarray(wide.astype(np.float32)))
+            inv.append(np.ascontiguousarray((1.0 / wide).astype(np.float32)))
+        self._eps = tuple(eps)  # type: ignore[assignment]
+        self._inv_eps = tuple(inv)  # type: ignore[assignment]
+
+    def setup_pml(self, thickness_cells: Any, order: int = 2) -> PML:
+        self._require_unfrozen("setup_pml")
+        self.pml = PML(self.grid, thickness_cells, order=order)
+        return self.pml
+
+    def add_susceptibility(self, susceptibility: Susceptibility, sigma: Any) -> None:
+        """One Lorentz/Drude term of ``eps_inf + sum_n sigma_n chi_n`` (scalar, volume or per component)."""
+        self._require_unfrozen("add_susceptibility")
+        if not isinstance(susceptibility, Susceptibility):
+            raise TypeError("add_susceptibility takes a meep_gpu_gb300.Susceptibility")
+        if isinstance(sigma, Mapping):
+            unknown = set(sigma) - {"Ex", "Ey", "Ez"}
+            if unknown:
+                raise Unsupported(f"sigma components {sorted(unknown)} are not stepped")
+            raw = [sigma.get(c) for c in ("Ex", "Ey", "Ez")]
+        else:
+            raw = [sigma, sigma, sigma]
+        volumes: List[Optional[np.ndarray]] = []
+        for value in raw:
+            if value is None:
+                volumes.append(None)
+                continue
+            volume = np.ascontiguousarray(self._volume(value, "sigma").astype(np.float32))
+            if not np.all(np.isfinite(volume)):
+                raise ValueError("sigma must be finite")
+            volumes.append(volume if np.any(volume != 0) else None)
+        radius = susceptibility.stability_radius(self.grid.dt)
+        if radius > 1.0 + 1e-12:
+            raise ValueError(f"susceptibility {susceptibility} is unstable at dt={self.grid.dt} "
+                             f"(root modulus {radius:.6f})")
+        self._poles.append((susceptibility, volumes))
+
+    def add_source(self, source_data: Mapping[str, Any]) -> Source:
+        """A source from the reference's boundary-protocol dict (driver.py:2567)."""
+        self._require_unfrozen("add_source")
+        spec = dict(source_data)
+        unknown = set(spec) - {"component", "center", "size", "amplitude", "amp_func",
+                               "is_integrated", "source_type", "frequency", "fwidth",
+                               "start_time", "end_time", "cutoff", "width", "slowness",
+                               "src_func"}
+        if unknown:
+            raise ValueError(f"unknown source keys {sorted(unknown)}")
+        waveform = make_waveform(spec)
+        source = Source(self.grid, spec.get("component", "Ez"),
+                        _as_xyz("center", spec.get("center", (0.0, 0.0, 0.0))),
+                        _as_xyz("size", spec.get("size", (0.0, 0.0, 0.0))),
+                        waveform, complex(spec.get("amplitude", 1.0)), spec.get("amp_func"))
+        if complex(spec.get("amplitude", 1.0)).imag != 0.0:
+            raise Unsupported("a complex source amplitude needs complex fields")
+        self._sources.append(source)
+        return source
+
+    def _decimation(self, request: int, frequencies) -> int:
+        request = int(request)
+        if request < 0:
+            raise ValueError(f"decimation_factor must be >= 0, got {request}")
+        if request == 0:
+            return automatic_decimation(self.grid.dt, frequencies, self._sources)
+        return request
+
+    def add_flux_monitor(self, frequencies: Any = None, center: Optional[Sequence[float]] = None,
+                         size: Optional[Sequence[float]] = None, direction: Optional[int] = None, *,
+                         frequency: Any = None, fcen: Optional[float] = None, df: Optional[float] = None,
+                         nfreq: Optional[int] = None, decimation_factor: int = 1,
+                         weight: float = 1.0) -> FluxMonitor:
+        self._require_unfrozen("add_flux_monitor")
+        freqs = normalize_frequencies(frequencies, frequency, fcen, df, nfreq)
+        if center is None or size is None:
+            raise ValueError("a flux monitor needs a center and a size")
+        monitor = FluxMonitor(self.grid, freqs, _as_xyz("center", center), _as_xyz("size", size),
+                              direction, weight, self._decimation(decimation_factor, freqs))
+        if int(decimation_factor) == 0:
+            self._automatic.append(monitor)
+        self._flux_monitors.append(monitor)
+        return monitor
+
+    def add_dft_monitor(self, frequencies: Any = None, components: Sequence[str] = ("Ex", "Ey", "Ez"),
+                        center: Optional[Sequence[float]] = None, size: Optional[Sequence[float]] = None,
+                        *, frequency: Any = None, fcen: Optional[float] = None, df: Optional[float] = None,
+                        nfreq: Optional[int] = None, decimation_factor: int = 1) -> DFTMonitor:
+        self._require_unfrozen("add_dft_monitor")
+        freqs = normalize_frequencies(frequencies, frequency, fcen, df, nfreq)
+        monitor = DFTMonitor(self.grid, freqs, tuple(components), self._decimation(decimation_factor, freqs))
+        if int(decimation_factor) == 0:
+            self._automatic.append(monitor)
+        self._pending_regions.append((monitor, center, size))
+        self._dft_monitors.append(monitor)
+        return monitor
+
+    # --- freeze ---------------------------------------------------------------------
+    def _resolve_regions(self) -> None:
+        for monitor, center, size in self._pending_regions:
+            if center is not None and size is not None:
+                monitor.set_region_from_volume(_as_xyz("center", center), _as_xyz("size", size))
+                continue
+            region = []
+            for axis in range(3):
+                n = self.grid.shape[axis]
+                low, high = self.pml.faces[axis] if self.pml is not None else (0, 0)
+                region += [absorbing_cells(low) if low > 0 else 0,
+                           n - (absorbing_cells(high) if high > 0 else 0)]
+            monitor.set_region(region)
+        self._pending_regions = []
+
+    def prepare(self) -> None:
+        """Resolve what the first step fixes (automatic decimation, default monitor
+        regions, vacuum epsilon) without touching the GPU."""
+        for monitor in self._automatic:
+            monitor._configure_decimation(automatic_decimation(self.grid.dt, monitor.frequencies,
+                                                               self._sources))
+        self._automatic = []
+        self._resolve_regions()
+        if self._inv_eps is None:
+            self.set_epsilon(1.0)
+
+    def _freeze(self) -> None:
+        import torch
+
+        from .engine import Engine
+        self.prepare()
+        device = torch.device("cuda", self.gpu_id)
+        self.engine = Engine(self.grid, self.pml, self._inv_eps, self._poles, self._sources,
+                             list(self._flux_monitors) + list(self._dft_monitors), device=device,
+                             launch_shape=self.launch_shape)
+
+    # --- stepping -------------------------------------------------------------------
+    @property
+    def time(self) -> float:
+        return self.step_count * self.grid.dt
+
+    @property
+    def dt(self) -> float:
+        return self.grid.dt
+
+    @property
+    def dx(self) -> float:
+        return self.grid.dx
+
+    @property
+    def shape(self) -> Tuple[int, int, int]:
+        return self.grid.shape
+
+    def step(self) -> None:
+        """One FDTD step in MEEP's ``fields::step()`` order (two fused kernels)."""
+        self.step_many(1)
+
+    def step_many(self, nsteps: int) -> None:
+        if self.engine is None:
+            self._freeze()
+        self.engine.step(self.step_count, int(nsteps))
+        self.step_count += int(nsteps)
+
+    def sources_end_time(self) -> float:
+        """Last time any source is on (Gaussian: peak + cutoff), MEEP's ``last_source_time``."""
+        latest = 0.0
+        for source in self._sources:
+            waveform = source.waveform
+            if hasattr(waveform, "peak_time"):
+                latest = max(latest, waveform.peak_time + waveform.cutoff_time)
+            elif getattr(waveform, "end_time", None) is not None:
+                latest = max(latest, float(waveform.end_time))
+        return latest
+
+    def run(self, num_steps: Optional[int] = None, until: Optional[float] = None,
+            progress_cb: Optional[Callable[[int, int], None]] = None,
+            cancel_check: Optional[Callable[[], bool]] = None, progress_interval: int = 100, *,
+            until_after_sources: Optional[float] = None, check_finite: bool = True, **unsupported) -> int:
+        """Advance ``num_steps`` steps, or until a simulation time (reference driver.py:3667).
+
+        Steps are queued in chunks of ``progress_interval``; between chunks the
+        non-finite detector is read (one small device-to-host read) and the cancel
+        and progress callbacks run. Returns the number of steps taken.
+        """
+        if unsupported:
+            raise Unsupported(f"run options {sorted(unsupported)} are not supported by this engine")
+        given = [x is not None for x in (num_steps, until, until_after_sources)]
+        if sum(given) != 1:
+            raise ValueError("give exactly one of num_steps, until, until_after_sources")
+        if until_after_sources is not None:
+            until = self.sources_end_time() + float(until_after_sources)
+        if until is not None:
+            end_time = float(until)
+            if not math.isfinite(end_time) or end_time <= self.time:
+                raise ValueError(f"until={until!r} is not beyond the current time {self.time}")
+            total = int(math.ceil((end_time - self.time) / self.grid.dt - STEP_TOLERANCE))
+        else:
+            total = int(num_steps)
+            if total != num_steps or total < 1:
+                raise ValueError(f"num_steps must be a positive whole number, got {num_steps!r}")
+        interval = max(1, int(progress_interval))
+        started = time_module.perf_counter()
+        completed = 0
+        while completed < total:
+            chunk = min(interval, total - completed)
+            self.step_many(chunk)
+            completed += chunk
+            if check_finite and self.engine.nonfinite():
+                raise FdtdDivergence(f"a non-finite E was written by step {self.step_count}")
+            if cancel_check is not None and cancel_check():
+                raise FdtdCancelled(f"FDTD run cancelled after {self.step_count} steps")
+            if progress_cb is not None:
+                progress_cb(completed, total)
+        if self.engine is not None:
+            import torch
+            torch.cuda.synchronize(self.engine.device)
+        self.last_run_seconds = time_module.perf_counter() - started
+        return total
+
+    # --- read-out -------------------------------------------------------------------
+    def get_field(self, component: str, cell_centered: bool = True) -> np.ndarray:
+        """Host copy of one component: the stored Yee words, or their cell-centre values.
+
+        The centred value is MEEP's ``get_array`` sum ``0.25 * (((a + b) + c) + d)``
+        over the shift-0 neighbours (``0.5 * (a + b)`` with one such axis), with the
+        PEC zero (or the periodic image) past the high face.
+        """
+        if component not in FIELD_COMPONENTS:
+            raise ValueError(f"unknown component {component!r}; supported {FIELD_COMPONENTS}")
+        if self.engine is None:
+            return np.zeros(self.grid.shape, dtype=np.float32)
+        name = {"D": "D", "E": "E", "B": "B", "H": "H"}[component[0]] + component[1]
+        raw = self.engine.field(name).detach().cpu().numpy().copy()
+        if not cell_centered:
+            return raw
+        shifts = IYEE[component]
+        axes = [a for a in range(3) if shifts[a] == 0]
+        padded = raw
+        for axis in axes:
+            pad = [(0, 0)] * 3
+            pad[axis] = (0, 1)
+            if self.grid.is_metallic(axis):
+                padded = np.pad(padded, pad)
+            else:
+                padded = np.pad(padded, pad, mode="wrap")
+        n = self.grid.shape
+        def view(offsets):
+            return padded[tuple(slice(o, o + n[a]) for a, o in enumerate(offsets))]
+        if not axes:
+            return raw
+        if len(axes) == 1:
+            o = [0, 0, 0]
+            o[axes[0]] = 1
+            return (np.float32(0.5) * (view((0, 0, 0)) + view(o))).astype(np.float32)
+        a0, a1 = axes
+        o1 = [0, 0, 0]; o1[a0] = 1
+        o2 = [0, 0, 0]; o2[a1] = 1
+        o3 = [0, 0, 0]; o3[a0] = 1; o3[a1] = 1
+        total = ((view((0, 0, 0)) + view(o1)) + view(o2)) + view(o3)
+        return (np.float32(0.25) * total).astype(np.float32)
+
+    def get_flux_spectrum(self, monitor: FluxMonitor) -> np.ndarray:
+        return monitor.get_flux_spectrum()
+
+    def close(self) -> None:
+        if self.engine is not None:
+            self.engine.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

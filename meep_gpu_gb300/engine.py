@@ -1,0 +1,338 @@
+"""Device state of one frozen simulation and the calls into ``libmeepgb.so``.
+
+The engine allocates every device array (as torch tensors: torch is the allocator and
+the stream provider here, nothing more), fills the ``mgb_sim_desc`` the C ABI takes,
+and drives ``mgb_step``. Layout in HBM, all float32 and C-ordered ``(nx, ny, nz)``:
+
+* E, D, B: three full volumes each; one inverse-epsilon volume per distinct array
+  (the isotropic case aliases one volume for all three components);
+* PML auxiliaries, compact over their membership runs only (one axis shortened to the
+  run length): stored H and its ``f_w`` on each H component's own-axis integer runs
+  (H is B's word everywhere else), ``f_w`` of E on the own-axis half runs, and the
+  split-field ``fu`` of B (half lattice) and D (integer lattice) on the dsigu runs;
+* polarization: two rotating buffers per pole and driven component, over the bounding
+  box of the cells where any pole's sigma is nonzero (P stays zero elsewhere);
+* DFT accumulators ``[ncomp][nfreq][re, im][cells]`` per monitor.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+import torch
+
+from . import _lib
+from .dft import COMPONENTS, FluxMonitor, _Monitor
+from .grid import Grid
+from .pml import (HALF, INTEGER, PML, aux_shape, constitutive_aux_key, curl_aux_key,
+                  identity_tables, no_pml_records, slab_index)
+from .sources import Source, deposit_words
+
+FIELD_NAMES = ("E", "D", "B")
+# Source words are uploaded in windows of this many steps.
+SOURCE_WINDOW = 4096
+
+
+def _ptr(t: Optional[torch.Tensor]) -> Optional[int]:
+    return None if t is None else t.data_ptr()
+
+
+class Engine:
+    """One simulation resident on one GPU."""
+
+    def __init__(self, grid: Grid, pml: Optional[PML], inv_eps: Sequence[np.ndarray],
+                 poles: Sequence[Tuple[object, Sequence[Optional[np.ndarray]]]],
+                 sources: Sequence[Source], monitors: Sequence[_Monitor],
+                 device: Optional[torch.device] = None, stream: Optional[torch.cuda.Stream] = None,
+                 launch_shape: Optional[Tuple[int, int, int]] = None):
+        if not torch.cuda.is_available():
+            raise RuntimeError("meep_gpu_gb300 steps on a CUDA GPU and none is visible")
+        self.lib = _lib.load()
+        self.grid = grid
+        self.pml = pml if (pml is not None and pml.is_active) else None
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.stream = stream
+        self.sources = list(sources)
+        self.monitors = list(monitors)
+        shape = grid.shape
+        dev = self.device
+        zeros = lambda s: torch.zeros(s, dtype=torch.float32, device=dev)  # noqa: E731
+        self.fields: Dict[str, torch.Tensor] = {}
+        for family in FIELD_NAMES:
+            for q, axis in enumerate("xyz"):
+                self.fields[family + axis] = zeros(shape)
+        # inverse epsilon: one device volume per distinct host array
+        self.inv_eps: List[torch.Tensor] = []
+        seen: Dict[int, torch.Tensor] = {}
+        for array in inv_eps:
+            key = id(array)
+            if key not in seen:
+                seen[key] = torch.from_numpy(np.ascontiguousarray(array, dtype=np.float32)).to(dev)
+            self.inv_eps.append(seen[key])
+        self.desc = _lib.MgbSimDesc()
+        d = self.desc
+        d.abi_version = _lib.MGB_ABI_VERSION
+        d.nx, d.ny, d.nz = shape
+        for axis in range(3):
+            d.metallic[axis] = 1 if grid.is_metallic(axis) else 0
+        d.dtdx = float(np.float32(grid.dt / grid.dx))
+        for q, axis in enumerate("xyz"):
+            d.E[q] = self.fields["E" + axis].data_ptr()
+            d.D[q] = self.fields["D" + axis].data_ptr()
+            d.B[q] = self.fields["B" + axis].data_ptr()
+            d.inv_eps[q] = self.inv_eps[q].data_ptr()
+        self.aux: Dict[str, torch.Tensor] = {}
+        self.coefficients: Dict[Tuple[str, int, int], torch.Tensor] = {}
+        if self.pml is not None:
+            d.pml_active = 1
+            for (lattice, axis), table in self.pml.tables.items():
+                for name in ("kms", "sinv", "kps"):
+                    t = torch.from_numpy(getattr(table, name).copy()).to(dev)
+                    self.coefficients[(name, lattice, axis)] = t
+                    getattr(d, name)[lattice][axis] = t.data_ptr()
+            self.records = self.pml.records
+            for q in range(3):
+                self._aux(d.H, "H", q, constitutive_aux_key("H", q))
+                self._aux(d.fwH, "fwH", q, constitutive_aux_key("H", q))
+                self._aux(d.fwE, "fwE", q, constitutive_aux_key("E", q))
+                self._aux(d.fuB, "fuB", q, curl_aux_key("B", q))
+                self._aux(d.fuD, "fuD", q, curl_aux_key("D", q))
+        else:
+            d.pml_active = 0
+            self.records = no_pml_records(grid)
+        self._setup_poles(poles)
+        self._setup_sources()
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        d.status = self.status.data_ptr()
+        self._setup_monitors()
+        handle = ctypes.c_void_p()
+        _lib.check(self.lib, self.lib.mgb_create(ctypes.byref(d), ctypes.byref(handle)))
+        self.handle = handle
+        if launch_shape is not None:
+            self.set_launch_shape(*launch_shape)
+        self._words: Optional[torch.Tensor] = None
+        self._words_first = 0
+        self._words_steps = 0
+
+    # --- setup --------------------------------------------------------------------------
+    def _aux(self, slot, name: str, q: int, key: Tuple[int, int]) -> None:
+        lattice, axis = key
+        record = self.records[key]
+        tensor = torch.zeros(aux_shape(self.grid, record, axis), dtype=torch.float32, device=self.device)
+        if tensor.numel() == 0:
+            # An empty membership still needs a valid pointer; the kernels never touch it.
+            tensor = torch.zeros(1, dtype=torch.float32, device=self.device)
+        self.aux[f"{name}{'xyz'[q]}"] = tensor
+        entry = slot[q]
+        entry.data = tensor.data_ptr()
+        entry.axis = axis
+        entry.a0, entry.a1, entry.b0, entry.b1 = record
+
+    def _setup_poles(self, poles) -> None:
+        d = self.desc
+        self.pole_tensors: List[dict] = []
+        d.npoles = len(poles)
+        if not poles:
+            return
+        if len(poles) > _lib.MGB_MAX_POLES:
+            raise _lib.MeepGBError(-3, f"at most {_lib.MGB_MAX_POLES} susceptibility poles are stepped")
+        support = np.zeros(self.grid.shape, dtype=bool)
+        for _, sigmas in poles:
+            for sigma in sigmas:
+                if sigma is not None:
+                    support |= (sigma != 0)
+        box = []
+        for axis in range(3):
+            other = tuple(a for a in range(3) if a != axis)
+            line = support.any(axis=other)
+            idx = np.flatnonzero(line)
+            if idx.size == 0:
+                idx = np.array([0])
+            box += [int(idx[0]), int(idx[-1]) + 1]
+        self.pbox = tuple(box)
+        d.pbox[:] = box
+        slices = (slice(box[0], box[1]), slice(box[2], box[3]), slice(box[4], box[5]))
+        bshape = (box[1] - box[0], box[3] - box[2], box[5] - box[4])
+        for m, (susceptibility, sigmas) in enumerate(poles):
+            const = susceptibility.realnum_constants(self.grid.dt)
+            pole = d.poles[m]
+            pole.two_minus_od = float(const.two_minus_od)
+            pole.gamma1 = float(const.gamma1)
+            pole.omega0dtsqr = float(const.omega0dtsqr)
+            pole.gamma1inv = float(const.gamma1inv)
+            kept = {}
+            for q in range(3):
+                sigma = sigmas[q]
+                if sigma is None:
+                    pole.sigma[q] = None
+                    continue
+                s = torch.from_numpy(np.ascontiguousarray(sigma[slices], dtype=np.float32)).to(self.device)
+                p0 = torch.zeros(bshape, dtype=torch.float32, device=self.device)
+                p1 = torch.zeros(bshape, dtype=torch.float32, device=self.device)
+                kept[q] = (s, p0, p1)
+                pole.sigma[q] = s.data_ptr()
+                pole.p[q][0] = p0.data_ptr()
+                pole.p[q][1] = p1.data_ptr()
+            self.pole_tensors.append(kept)
+
+    def _setup_sources(self) -> None:
+        d = self.desc
+        cells: List[int] = []
+        comps: List[int] = []
+        ny, nz = self.grid.ny, self.grid.nz
+        for source in self.sources:
+            for (i, j, k) in source.cells:
+                cells.append((i * ny + j) * nz + k)
+                comps.append(source.comp_index)
+        d.nsrc = len(cells)
+        if not cells:
+            return
+        self.src_cell = torch.tensor(cells, dtype=torch.int64, device=self.device)
+        self.src_comp = torch.tensor(comps, dtype=torch.int32, device=self.device)
+        d.src_cell = self.src_cell.data_ptr()
+        d.src_comp = self.src_comp.data_ptr()
+        ijk = np.array([c for s in self.sources for c in s.cells])
+        lo, hi = ijk.min(axis=0), ijk.max(axis=0) + 1
+        d.src_box[:] = [int(lo[0]), int(hi[0]), int(lo[1]), int(hi[1]), int(lo[2]), int(hi[2])]
+
+    def _setup_monitors(self) -> None:
+        d = self.desc
+        if len(self.monitors) > _lib.MGB_MAX_MONITORS:
+            raise _lib.MeepGBError(-3, f"at most {_lib.MGB_MAX_MONITORS} monitors per simulation")
+        d.nmonitors = len(self.monitors)
+        self.monitor_tensors = []
+        for index, monitor in enumerate(self.monitors):
+            entry = d.monitors[index]
+            entry.region[:] = list(monitor.region)
+            entry.ncomp = len(monitor.components)
+            for q, comp in enumerate(monitor.components):
+                entry.comp[q] = COMPONENTS.index(comp)
+            entry.nfreq = monitor.num_frequencies
+            entry.decimation = monitor.decimation_factor
+            entry.scale = monitor.scale
+            entry.dt = self.grid.dt
+            omega = torch.from_numpy(monitor.omegas.copy()).to(self.device)
+            acc = torch.zeros((entry.ncomp, entry.nfreq, 2, monitor.cells), dtype=torch.float32,
+                              device=self.device)
+            entry.omega = omega.data_ptr()
+            entry.acc = acc.data_ptr()
+            weights = None
+            if isinstance(monitor, FluxMonitor):
+                weights = torch.from_numpy(monitor.weights.reshape(-1).copy()).to(self.device)
+            self.monitor_tensors.append((omega, acc, weights))
+            monitor.accumulator = acc
+            monitor._engine = self
+
+    # --- stepping -----------------------------------------------------------------------
+    def set_launch_shape(self, block_z: int, block_y: int, x_chunk: int) -> None:
+        _lib.check(self.lib, self.lib.mgb_set_launch_shape(self.handle, block_z, block_y, x_chunk))
+
+    def _stream_handle(self) -> int:
+        stream = self.stream if self.stream is not None else torch.cuda.current_stream(self.device)
+        return stream.cuda_stream
+
+    def ensure_source_words(self, first_step: int, steps: int) -> None:
+        """Upload the float64 deposit words covering ``[first_step, first_step + steps)``."""
+        if self.desc.nsrc == 0 or steps <= 0:
+            return
+        if (self._words is not None and first_step >= self._words_first
+                and first_step + steps <= self._words_first + self._words_steps):
+            return
+        count = max(steps, SOURCE_WINDOW)
+        host = deposit_words(self.sources, first_step, count, self.grid.dt)
+        # The previous table may still be read by queued kernels: keep it alive until
+        # the stream has passed them.
+        stream = self.stream if self.stream is not None else torch.cuda.current_stream(self.device)
+        words = torch.from_numpy(host).to(self.device, non_blocking=False)
+        if self._words is not None:
+            self._words.record_stream(stream)
+        self._words = words
+        self._words_first = first_step
+        self._words_steps = count
+        _lib.check(self.lib, self.lib.mgb_set_source_words(self.handle, words.data_ptr(),
+                                                             first_step, count))
+
+    def step(self, first_step: int, nsteps: int) -> None:
+        """Queue steps ``first_step .. first_step + nsteps - 1`` (asynchronous)."""
+        done = 0
+        while done < nsteps:
+            chunk = min(nsteps - done, SOURCE_WINDOW)
+            self.ensure_source_words(first_step + done, chunk)
+            _lib.check(self.lib, self.lib.mgb_step(self.handle, first_step + done, chunk,
+                                                   self._stream_handle()))
+            done += chunk
+
+    def launch(self, step: int, part: int, stream=None) -> None:
+        """Launch one kernel of one step: 0 the H half, 1 the E half, 2 the monitors."""
+        if part < 2:
+            self.ensure_source_words(step, 1)
+        handle = (stream if stream is not None else
+                  (self.stream if self.stream is not None else torch.cuda.current_stream(self.device)))
+        _lib.check(self.lib, self.lib.mgb_launch(self.handle, step, part, handle.cuda_stream))
+
+    def algorithmic_bytes(self) -> Dict[str, int]:
+        """Minimum HBM bytes one launch of each step kernel must move.
+
+        H half: read E (3 volumes) and B (3), write B (3); on the PML slabs read and
+        write ``fu`` of B, and read H and ``f_w`` of H and write both.
+        E half: read H (3 volumes: the slab word or B's) and D (3) and each distinct
+        inverse-epsilon volume, write D (3) and E (3); on the slabs read and write ``fu``
+        of D, read and write ``f_w`` of E and read E; per pole and driven component read
+        P, P_prev and sigma and write P' over the polarization box.
+        """
+        cells = self.grid.total_cells
+        word = 4
+        aux = lambda name: sum(int(self.aux[f"{name}{a}"].numel()) for a in "xyz") if self.pml is not None else 0  # noqa: E731
+        h = 9 * cells + 2 * aux("fuB") + 2 * aux("H") + 2 * aux("fwH")
+        distinct_inv = len({t.data_ptr() for t in self.inv_eps})
+        e = (12 + distinct_inv) * cells + 2 * aux("fuD") + 3 * aux("fwE")
+        for kept in getattr(self, "pole_tensors", []):
+            for _, (s, p0, _p1) in kept.items():
+                e += 4 * int(p0.numel())
+        return {"h_half": word * h, "e_half": word * e}
+
+    def nonfinite(self) -> bool:
+        return bool(self.status.item() != 0)
+
+    # --- read-out -----------------------------------------------------------------------
+    def field(self, name: str) -> torch.Tensor:
+        """Device tensor of one component's stored Yee words (H composed from B and slab)."""
+        if name[0] in "EDB":
+            return self.fields[name]
+        if name[0] == "H":
+            q = "xyz".index(name[1])
+            b = self.fields["B" + name[1]]
+            if self.pml is None:
+                return b
+            h = b.clone()
+            record = self.records[(INTEGER, q)]
+            rows = np.flatnonzero(slab_index(record, np.arange(self.grid.shape[q])) >= 0)
+            if rows.size:
+                index = [slice(None)] * 3
+                index[q] = torch.from_numpy(rows).to(self.device)
+                h[tuple(index)] = self.aux["H" + name[1]]
+            return h
+        raise ValueError(f"unknown component {name!r}")
+
+    def flux_spectrum(self, monitor: FluxMonitor) -> np.ndarray:
+        index = self.monitors.index(monitor)
+        _, _, weights = self.monitor_tensors[index]
+        out = torch.zeros(monitor.num_frequencies, dtype=torch.float64, device=self.device)
+        _lib.check(self.lib, self.lib.mgb_flux_spectrum(self.handle, index, weights.data_ptr(),
+                                                        out.data_ptr(), self._stream_handle()))
+        sums = out.cpu().numpy()
+        return sums * monitor.measure * monitor.weight
+
+    def close(self) -> None:
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            self.lib.mgb_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order varies
+        try:
+            self.close()
+        except Exception:
+            pass

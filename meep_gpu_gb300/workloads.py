@@ -1,0 +1,82 @@
+"""Synthetic workloads with the shapes of the benchmarked configurations.
+
+Each builder configures an ``FdtdDriver`` (or any class with the same API) and
+returns ``(driver, flux_monitors, dft_monitors)``. Geometry is point-sampled on the
+grid's cell centres, as the configurations specify; there is no dataset.
+
+* ``sphere80``: 80^3 cells at resolution 10 (8-unit cube), 10-cell PML, eps-4 sphere of
+  radius 2, Ez Gaussian (fcen 0.15, df 0.1) at x = -2, one x-normal flux plane at
+  x = 2.5 of size 6 x 6 with 50 frequencies; 2000 steps.
+* ``sphere192_8dft``: the same physical case at resolution 24 (192^3 = 7,077,888 cells),
+  with eight DFT objects: flux planes one cell inside the PML on all six faces and two
+  32^3 field-DFT volumes (Ex, Ey, Ez) centred at (+-1.6, 0, 0), 100 frequencies each;
+  5000 steps.
+* ``lorentz192``: 192^3 at resolution 20 (9.6-unit cube), slab |x| < 0.5 with
+  eps_inf 2.25 and one Lorentz pole (f0 1.1, gamma 0.05, sigma 1.5), 10-cell PML,
+  Ez Gaussian (fcen 0.8, df 1.0) at x = -2.4, transmission/reflection planes at x = +-2
+  of size 7.6 x 7.6 with 200 frequencies; 10,000 steps.
+* ``sphere128``: a 128^3 sphere case with one flux plane, the size used for detailed
+  profiles (working set above the L2 size, a few hundred MB).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+WORKLOADS = ("sphere80", "sphere192_8dft", "lorentz192", "sphere128")
+STEPS = {"sphere80": 2000, "sphere192_8dft": 5000, "lorentz192": 10000, "sphere128": 1000}
+
+
+def build(name: str, driver_cls=None, susceptibility_cls=None, **driver_kwargs):
+    if driver_cls is None:
+        from .driver import FdtdDriver as driver_cls  # noqa: N813
+    if susceptibility_cls is None:
+        from .dispersion import Susceptibility as susceptibility_cls  # noqa: N813
+    if name in ("sphere80", "sphere192_8dft", "sphere128"):
+        res = {"sphere80": 10, "sphere192_8dft": 24, "sphere128": 16}[name]
+        length = 8.0
+        d = driver_cls(cell_size=(length, length, length), resolution=res, courant=0.5,
+                       force_complex_fields=False, boundaries="metallic", **driver_kwargs)
+        d.setup_pml(10)
+        x, y, z = d.grid.meshgrid()
+        d.set_epsilon(np.where(x ** 2 + y ** 2 + z ** 2 < 2.0 ** 2, 4.0, 1.0).astype(np.float32))
+        d.add_source({"source_type": "gaussian", "component": "Ez", "center": (-2.0, 0.0, 0.0),
+                      "size": (0, 0, 0), "frequency": 0.15, "fwidth": 0.1})
+        flux, dft = [], []
+        if name != "sphere192_8dft":
+            flux.append(d.add_flux_monitor(fcen=0.15, df=0.1, nfreq=50, center=(2.5, 0, 0),
+                                           size=(0, 6, 6), decimation_factor=0))
+            return d, flux, dft
+        inset = 4.0 - 11 * d.grid.dx           # one cell inside the 10-cell PML
+        span = 2 * inset
+        for axis in range(3):
+            for sign in (-1.0, 1.0):
+                center = [0.0, 0.0, 0.0]
+                center[axis] = sign * inset
+                size = [span, span, span]
+                size[axis] = 0.0
+                flux.append(d.add_flux_monitor(fcen=0.15, df=0.1, nfreq=100, center=tuple(center),
+                                               size=tuple(size), decimation_factor=0))
+        side = 32 * d.grid.dx
+        for sign in (-1.0, 1.0):
+            dft.append(d.add_dft_monitor(fcen=0.15, df=0.1, nfreq=100, components=("Ex", "Ey", "Ez"),
+                                         center=(sign * 1.6, 0.0, 0.0), size=(side, side, side),
+                                         decimation_factor=0))
+        return d, flux, dft
+    if name == "lorentz192":
+        res = 20
+        length = 9.6
+        d = driver_cls(cell_size=(length, length, length), resolution=res, courant=0.5,
+                       force_complex_fields=False, boundaries="metallic", **driver_kwargs)
+        d.setup_pml(10)
+        x, y, z = d.grid.meshgrid()
+        slab = np.abs(x) < 0.5
+        d.set_epsilon(np.where(slab, 2.25, 1.0).astype(np.float32))
+        d.add_susceptibility(susceptibility_cls(frequency=1.1, gamma=0.05),
+                             np.where(slab, 1.5, 0.0).astype(np.float32))
+        d.add_source({"source_type": "gaussian", "component": "Ez", "center": (-2.4, 0.0, 0.0),
+                      "size": (0, 0, 0), "frequency": 0.8, "fwidth": 1.0})
+        flux = [d.add_flux_monitor(fcen=0.8, df=1.0, nfreq=200, center=(sign * 2.0, 0, 0),
+                                   size=(0, 7.6, 7.6), decimation_factor=0) for sign in (1.0, -1.0)]
+        return d, flux, []
+    raise ValueError(f"unknown workload {name!r}; choose from {WORKLOADS}")

@@ -1,0 +1,77 @@
+"""Small seeded cases shared by the golden-vector script and the tests.
+
+Each case is built through whichever driver class is passed in (the reference's
+``meep_gpu.FdtdDriver`` when recording, ``meep_gpu_gb300.FdtdDriver`` when testing), with
+the same calls, so both sides configure the same simulation.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+CASES = {
+    "sphere_pml": dict(n=(14, 12, 16), pml=3, steps=60),
+    "lorentz_slab": dict(n=(16, 12, 14), pml=3, steps=60, lorentz=True),
+    "nopml_metallic": dict(n=(12, 14, 13), pml=0, steps=50),
+    "periodic": dict(n=(12, 13, 14), pml=0, steps=50, boundaries="periodic"),
+    "periodic_pml": dict(n=(14, 12, 13), pml=3, steps=50, boundaries="periodic"),
+    "mixed": dict(n=(13, 15, 12), pml={"x": 3, "y": {"low": 2, "high": 4}, "z": 2.5}, steps=45,
+                  mixed=True),
+}
+
+# The 80^3 sphere-under-PML workload (resolution 10, 10-cell PML, eps 4 sphere of radius
+# 2, Ez Gaussian at x = -2, one 50-frequency x-normal flux plane at x = 2.5).
+SPHERE80 = dict(n=(80, 80, 80), pml=10, steps=200, sphere80=True)
+
+
+def build_case(driver_cls, susceptibility_cls, case: dict, reference: bool = False):
+    """Configure one case; returns (driver, flux monitors, DFT monitors)."""
+    res = 10
+    n = case["n"]
+    lengths = tuple(v / res for v in n)
+    boundaries = case.get("boundaries", "metallic")
+    d = driver_cls(cell_size=lengths, resolution=res, courant=0.5, force_complex_fields=False,
+                   boundaries=boundaries, **({"prefer_gpu": False} if reference else {}))
+    if case["pml"]:
+        d.setup_pml(case["pml"])
+    x, y, z = d.grid.meshgrid()
+    flux, dft = [], []
+    if case.get("sphere80"):
+        d.set_epsilon(np.where(x ** 2 + y ** 2 + z ** 2 < 2.0 ** 2, 4.0, 1.0).astype(np.float32))
+        d.add_source({"source_type": "gaussian", "component": "Ez", "center": (-2.0, 0, 0),
+                      "size": (0, 0, 0), "frequency": 0.15, "fwidth": 0.1})
+        flux.append(d.add_flux_monitor(fcen=0.15, df=0.1, nfreq=50, center=(2.5, 0, 0),
+                                       size=(0, 6, 6), decimation_factor=0))
+        return d, flux, dft
+    if case.get("lorentz"):
+        inside = np.abs(x) < 0.2
+        d.set_epsilon(np.where(inside, 2.25, 1.0).astype(np.float32))
+        d.add_susceptibility(susceptibility_cls(frequency=1.1, gamma=0.05),
+                             np.where(inside, 1.5, 0.0).astype(np.float32))
+        fcen, fwidth = 0.8, 1.0
+    else:
+        d.set_epsilon(np.where(x ** 2 + y ** 2 + z ** 2 < 0.35 ** 2, 4.0, 1.0).astype(np.float32))
+        fcen, fwidth = 0.15, 0.1
+    d.add_source({"source_type": "gaussian", "component": "Ez",
+                  "center": (-lengths[0] / 4, 0.03, 0.0), "size": (0, 0, 0),
+                  "frequency": fcen, "fwidth": fwidth})
+    if case.get("mixed"):
+        block = (np.abs(x - 0.2) < 0.15) & (np.abs(y) < 0.3)
+        d.add_susceptibility(susceptibility_cls(frequency=0.9, gamma=0.1),
+                             np.where(block, 0.8, 0.0).astype(np.float32))
+        d.add_susceptibility(susceptibility_cls(frequency=0.5, gamma=0.2, kind="drude"),
+                             np.where(block, 0.3, 0.0).astype(np.float32))
+        d.add_source({"source_type": "gaussian", "component": "Ex", "center": (0.1, 0.0, 0.05),
+                      "size": (0, 0.4, 0), "frequency": 0.5, "fwidth": 0.4})
+        d.add_source({"source_type": "continuous", "component": "Ey", "center": (-0.2, 0.21, -0.1),
+                      "size": (0, 0, 0), "frequency": 0.3, "amplitude": 0.5})
+        flux.append(d.add_flux_monitor(fcen=0.3, df=0.2, nfreq=3, center=(0, 0.4, 0),
+                                       size=(0.8, 0, 0.7), decimation_factor=0))
+        flux.append(d.add_flux_monitor(frequencies=[0.2, 0.35], center=(0.05, -0.05, 0.25),
+                                       size=(0.9, 0.8, 0), decimation_factor=2))
+        dft.append(d.add_dft_monitor(frequencies=[0.25, 0.4], components=("Ex", "Ey", "Hz", "Hx"),
+                                     center=(0.0, 0.1, 0.0), size=(0.6, 0.5, 0.4),
+                                     decimation_factor=1))
+    flux.append(d.add_flux_monitor(fcen=fcen, df=fwidth / 2, nfreq=4, center=(lengths[0] / 4, 0, 0),
+                                   size=(0, lengths[1] - 0.5, lengths[2] - 0.5), decimation_factor=0))
+    return d, flux, dft

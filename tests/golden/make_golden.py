@@ -1,0 +1,140 @@
+"""Record golden vectors from the reference implementation (run in the build container).
+
+Imports the reference's NumPy array path (``meep_gpu.FdtdDriver`` with
+``prefer_gpu=False``) from ``$MEEPGB_REFERENCE`` (default: the reference checkout
+beside the repository) and writes small fixtures into this directory:
+
+* ``fields_<case>.npz``: every stored float32 field word (E, D, B, H and, for a
+  dispersive case, P) after N steps of a small seeded case, plus its flux spectra and
+  DFT accumulators;
+* ``digest_sphere80.json``: SHA-256 of every field component after 200 steps of the
+  80^3 sphere-under-PML workload (the full-size configuration), plus its flux spectrum;
+* ``tables.npz``: PML coefficient vectors, source deposition tables, flux-plane
+  regions and weights and automatic decimation factors for a sweep of requests.
+
+The fixtures are committed; this script is how they were made. It is not run by the
+tests (the reference is not available where the GPU tests run).
+"""
+
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REFERENCE = os.environ.get("MEEPGB_REFERENCE", "/root/reference")
+sys.path.insert(0, REFERENCE)
+
+from meep_gpu import FdtdDriver  # noqa: E402
+from meep_gpu.dispersion import Susceptibility  # noqa: E402
+
+sys.path.insert(0, str(HERE.parent.parent))
+from tests.golden.cases import CASES, SPHERE80, build_case  # noqa: E402
+
+COMPONENTS = ("Ex", "Ey", "Ez", "Dx", "Dy", "Dz", "Bx", "By", "Bz", "Hx", "Hy", "Hz")
+
+
+def reference_driver(case):
+    return build_case(FdtdDriver, Susceptibility, case, reference=True)
+
+
+def record_fields(name: str, case: dict) -> None:
+    driver, flux, dft = reference_driver(case)
+    driver.run(num_steps=case["steps"])
+    out = {}
+    for c in COMPONENTS:
+        out[c] = np.asarray(driver.get_field(c, cell_centered=False), dtype=np.float32)
+    for index, monitor in enumerate(flux):
+        out[f"flux{index}"] = np.asarray(monitor.get_flux_spectrum(), dtype=np.float64)
+    for index, monitor in enumerate(dft):
+        for c in monitor.components:
+            out[f"dft{index}_{c}"] = np.asarray(monitor._dft[c], dtype=np.complex64)
+    for m, state in enumerate(driver.fields.polarizations):
+        for c, array in state.P.items():
+            out[f"P{m}_{c}"] = np.asarray(array, dtype=np.float32)
+    np.savez_compressed(HERE / f"fields_{name}.npz", **out)
+    print(name, "written")
+
+
+def record_digest() -> None:
+    driver, flux, _ = reference_driver(SPHERE80)
+    driver.run(num_steps=SPHERE80["steps"])
+    digests = {}
+    for c in COMPONENTS:
+        words = np.ascontiguousarray(driver.get_field(c, cell_centered=False), dtype=np.float32)
+        digests[c] = hashlib.sha256(words.tobytes()).hexdigest()
+    payload = {"case": "sphere80", "steps": SPHERE80["steps"], "sha256": digests,
+               "flux": [float(v) for v in flux[0].get_flux_spectrum()],
+               "decimation": int(flux[0].decimation_factor)}
+    (HERE / "digest_sphere80.json").write_text(json.dumps(payload, indent=1) + "\n")
+    print("digest written")
+
+
+def record_tables() -> None:
+    from meep_gpu.grid import Grid
+    from meep_gpu.pml import PML
+    from meep_gpu.sources import _build_source_points
+    from meep_gpu.dft import FluxMonitor
+
+    out = {}
+    grid = Grid(cell_size=(2.4, 2.0, 2.8), resolution=10, boundaries="metallic")
+    for thickness in (3, 4, 2.5, 5.2):
+        pml = PML(grid, thickness)
+        for axis in "xyz":
+            for half in ("", "_h"):
+                for name in ("kms", "sinv", "kps"):
+                    key = f"pml_{thickness}_{name}_{axis}{half}"
+                    out[key] = np.asarray(getattr(pml, f"{name}_{axis}{half}")).ravel()
+    rng = np.random.default_rng(7)
+    requests = []
+    for t in range(24):
+        component = ["Ex", "Ey", "Ez"][t % 3]
+        center = tuple(float(v) for v in np.round(rng.uniform(-0.9, 0.9, 3), 3))
+        size = [0.0, 0.0, 0.0]
+        if t % 4 == 1:
+            size[1] = float(np.round(rng.uniform(0.05, 0.9), 3))
+        if t % 4 == 2:
+            size[0] = float(np.round(rng.uniform(0.05, 0.9), 3))
+            size[2] = float(np.round(rng.uniform(0.05, 0.9), 3))
+        if t % 6 == 5:
+            center = (round(-0.6 + 0.1 * (t % 3), 10), 0.0, 0.05 * t)
+        cells, amps = _build_source_points(grid, component, center, tuple(size), 1.0, None)
+        out[f"src{t}_cells"] = np.asarray(cells, dtype=np.int64).reshape(-1, 3)
+        out[f"src{t}_amps"] = np.asarray(amps, dtype=np.complex128)
+        requests.append({"component": component, "center": center, "size": size})
+    planes = []
+    for t in range(12):
+        direction = t % 3
+        center = [float(v) for v in np.round(rng.uniform(-0.7, 0.7, 3), 3)]
+        size = [float(np.round(rng.uniform(0.2, 1.4), 3)) for _ in range(3)]
+        size[direction] = 0.0
+        if t % 4 == 0:
+            center[direction] = round(0.1 * (t - 5), 10)
+        monitor = FluxMonitor(grid, frequencies=(0.1, 0.2), center=tuple(center), size=tuple(size),
+                              periodic=(False, False, False))
+        out[f"plane{t}_region"] = np.asarray(monitor._region, dtype=np.int64)
+        out[f"plane{t}_weights"] = np.asarray(monitor._weights, dtype=np.float32)
+        out[f"plane{t}_measure"] = np.float64(monitor._measure)
+        planes.append({"center": center, "size": size, "direction": direction})
+    np.savez_compressed(HERE / "tables.npz", **out)
+    (HERE / "tables.json").write_text(json.dumps({"grid": {"cell_size": [2.4, 2.0, 2.8], "resolution": 10,
+                                                            "boundaries": "metallic"},
+                                                   "pml_thicknesses": [3, 4, 2.5, 5.2],
+                                                   "sources": requests, "planes": planes}, indent=1) + "\n")
+    print("tables written")
+
+
+if __name__ == "__main__":
+    which = sys.argv[1:] or ["fields", "digest", "tables"]
+    if "fields" in which:
+        for name, case in CASES.items():
+            record_fields(name, case)
+    if "tables" in which:
+        record_tables()
+    if "digest" in which:
+        record_digest()

@@ -1,0 +1,80 @@
+"""The C ABI: libmeepgb.so builds, loads, exports every declared symbol, and the
+ctypes mirror of ``include/meepgb.h`` has the header's layout (no GPU needed)."""
+
+import ctypes
+import re
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from meep_gpu_gb300 import _lib
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "meepgb.h"
+
+
+def declared_symbols():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|void)\s+(mgb_\w+)\s*\(", text, re.M)))
+
+
+def test_library_loads_and_exports_every_declared_symbol():
+    lib = _lib.load()
+    symbols = declared_symbols()
+    assert symbols, "no entry points found in the header"
+    for name in symbols:
+        assert hasattr(lib, name), f"libmeepgb.so does not export {name}"
+    assert set(symbols) == set(_lib.SIGNATURES), "binding and header disagree on the entry points"
+    assert lib.mgb_abi_version() == _lib.MGB_ABI_VERSION
+
+
+def test_create_refuses_bad_descriptors_without_a_gpu():
+    lib = _lib.load()
+    desc = _lib.MgbSimDesc()
+    desc.abi_version = _lib.MGB_ABI_VERSION + 7
+    handle = ctypes.c_void_p()
+    code = lib.mgb_create(ctypes.byref(desc), ctypes.byref(handle))
+    assert code == -1 and "ABI version" in _lib.last_error(lib)
+    desc.abi_version = _lib.MGB_ABI_VERSION
+    desc.nx, desc.ny, desc.nz = 1, 8, 8
+    assert lib.mgb_create(ctypes.byref(desc), ctypes.byref(handle)) == -3
+    assert "at least 2 cells" in _lib.last_error(lib)
+
+
+PROBE = r"""
+#include <stdio.h>
+#include <stddef.h>
+#include "meepgb.h"
+#define F(T, m) printf(#T "." #m " %zu\n", offsetof(T, m));
+int main(void) {
+  printf("sizeof.mgb_sim_desc %zu\n", sizeof(mgb_sim_desc));
+  printf("sizeof.mgb_monitor %zu\n", sizeof(mgb_monitor));
+  printf("sizeof.mgb_pole %zu\n", sizeof(mgb_pole));
+  printf("sizeof.mgb_aux %zu\n", sizeof(mgb_aux));
+  F(mgb_sim_desc, dtdx) F(mgb_sim_desc, kms) F(mgb_sim_desc, E) F(mgb_sim_desc, H)
+  F(mgb_sim_desc, fuD) F(mgb_sim_desc, npoles) F(mgb_sim_desc, poles) F(mgb_sim_desc, nsrc)
+  F(mgb_sim_desc, src_box) F(mgb_sim_desc, nmonitors) F(mgb_sim_desc, monitors)
+  F(mgb_sim_desc, status) F(mgb_monitor, scale) F(mgb_monitor, omega) F(mgb_monitor, acc)
+  F(mgb_pole, sigma) F(mgb_pole, p)
+  return 0;
+}
+"""
+
+
+def test_ctypes_layout_matches_the_header(tmp_path):
+    source = tmp_path / "probe.c"
+    source.write_text(PROBE)
+    exe = tmp_path / "probe"
+    subprocess.run(["gcc", "-std=c11", "-I", str(ROOT / "include"), "-o", str(exe), str(source)],
+                   check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    layout = dict(line.split() for line in out.strip().splitlines())
+    types = {"mgb_sim_desc": _lib.MgbSimDesc, "mgb_monitor": _lib.MgbMonitor,
+             "mgb_pole": _lib.MgbPole, "mgb_aux": _lib.MgbAux}
+    for key, value in layout.items():
+        kind, member = key.split(".")
+        if kind == "sizeof":
+            assert ctypes.sizeof(types[member]) == int(value), key
+        else:
+            assert getattr(types[kind], member).offset == int(value), key

@@ -1,0 +1,128 @@
+"""CUDA engine parity: libmeepgb.so against the reference's recorded words and the oracle.
+
+Every stepping kernel is compiled with -fmad=false and follows the reference's
+operation order, so the bar for fields is bit-exactness (zero differing float32 words)
+against the reference's own words (golden fixtures) and against the float32 oracle.
+Monitors form their phases on the device in float64 (CUDA sincos), which may round a
+phase word differently from the host's libm once in a while, so DFT accumulators and
+flux spectra are held to tolerances: relative 1e-5 of the spectrum's peak against the
+reference (a float32-rounding bound), and 1e-4 against the float64 oracle (the stated
+flux tolerance).
+"""
+
+import hashlib
+
+import numpy as np
+import pytest
+
+from meep_gpu_gb300 import FdtdDriver, Susceptibility
+from oracle.oracle import Oracle, problem_from_driver
+from tests import golden_io
+from tests.golden.cases import CASES, SPHERE80, build_case
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("Ex", "Ey", "Ez", "Dx", "Dy", "Dz", "Bx", "By", "Bz", "Hx", "Hy", "Hz")
+
+
+def gpu_case(case, steps=None, launch_shape=None, chunks=None):
+    driver, flux, dft = build_case(FdtdDriver, Susceptibility, case)
+    driver.launch_shape = launch_shape
+    total = steps if steps is not None else case["steps"]
+    if chunks:
+        done = 0
+        for chunk in chunks:
+            driver.run(num_steps=chunk)
+            done += chunk
+        assert done == total
+    else:
+        driver.run(num_steps=total)
+    return driver, flux, dft
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_fields_are_the_reference_words(gpu, name):
+    case = CASES[name]
+    gold = golden_io.fields(name)
+    driver, flux, dft = gpu_case(case)
+    for c in FIELDS:
+        got = driver.get_field(c, cell_centered=False)
+        mismatched = int(np.sum(got != gold[c]))
+        assert mismatched == 0, f"{name} {c}: {mismatched} words differ from the reference"
+    for index, monitor in enumerate(flux):
+        expected = gold[f"flux{index}"]
+        got = monitor.get_flux_spectrum()
+        assert np.max(np.abs(got - expected)) <= 1e-5 * np.max(np.abs(expected)), f"{name} flux {index}"
+    for index, monitor in enumerate(dft):
+        for c in monitor.components:
+            expected = gold[f"dft{index}_{c}"]
+            got = monitor.raw(c)
+            scale = np.max(np.abs(expected))
+            assert np.max(np.abs(got - expected)) <= 1e-5 * scale, f"{name} dft {c}"
+    for m, pole in enumerate(driver.engine.pole_tensors):
+        box = driver.engine.pbox
+        for q, (_, p0, p1) in pole.items():
+            current = (p0 if driver.step_count % 2 == 0 else p1).cpu().numpy()
+            expected = gold[f"P{m}_{'Ex Ey Ez'.split()[q]}"][box[0]:box[1], box[2]:box[3], box[4]:box[5]]
+            assert np.array_equal(current, expected), f"{name} P{m}"
+    driver.close()
+
+
+@pytest.mark.parametrize("shape", [(32, 8, 16), (64, 4, 7), (16, 16, 200), (128, 2, 1)])
+def test_launch_shape_does_not_change_a_word(gpu, shape):
+    case = CASES["mixed"]
+    gold = golden_io.fields("mixed")
+    driver, _, _ = gpu_case(case, launch_shape=shape)
+    for c in FIELDS:
+        assert np.array_equal(driver.get_field(c, cell_centered=False), gold[c]), (shape, c)
+    driver.close()
+
+
+def test_chunked_runs_equal_one_run(gpu):
+    case = CASES["lorentz_slab"]
+    gold = golden_io.fields("lorentz_slab")
+    driver, _, _ = gpu_case(case, chunks=[1, 2, 17, 40])
+    for c in FIELDS:
+        assert np.array_equal(driver.get_field(c, cell_centered=False), gold[c]), c
+    driver.close()
+
+
+def test_sphere80_words_after_200_steps(gpu):
+    gold = golden_io.digest()
+    driver, flux, _ = gpu_case(SPHERE80, steps=gold["steps"])
+    for c, expected in gold["sha256"].items():
+        words = np.ascontiguousarray(driver.get_field(c, cell_centered=False), dtype=np.float32)
+        assert hashlib.sha256(words.tobytes()).hexdigest() == expected, c
+    got = flux[0].get_flux_spectrum()
+    expected = np.asarray(gold["flux"])
+    assert np.max(np.abs(got - expected)) <= 1e-5 * np.max(np.abs(expected))
+    driver.close()
+
+
+def test_flux_against_float64_oracle(gpu):
+    """Flux after the pulse has crossed the plane: float32 engine vs float64 oracle."""
+    case = dict(CASES["sphere_pml"], steps=400)
+    driver, flux, _ = gpu_case(case)
+    mine, _, _ = build_case(FdtdDriver, Susceptibility, case)
+    oracle = Oracle(problem_from_driver(mine), "f64")
+    oracle.run(case["steps"])
+    expected = oracle.flux_spectrum(0)
+    got = flux[0].get_flux_spectrum()
+    rel = np.max(np.abs(got - expected)) / np.max(np.abs(expected))
+    assert rel <= 1e-4, f"flux vs float64 oracle {rel:.2e}"
+    for c in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz"):
+        a = driver.get_field(c, cell_centered=False).astype(np.float64)
+        b = oracle.field(c)
+        assert np.linalg.norm(a - b) <= 1e-4 * np.linalg.norm(b), c
+    driver.close()
+
+
+def test_nonfinite_detector_raises(gpu):
+    """A current large enough to overflow float32 is reported by the run, not returned."""
+    from meep_gpu_gb300 import FdtdDivergence
+    driver = FdtdDriver((1.2, 1.2, 1.2), 10, force_complex_fields=False, boundaries="metallic")
+    driver.add_source({"source_type": "continuous", "component": "Ez", "center": (0, 0, 0),
+                       "size": (0, 0, 0), "frequency": 0.5, "amplitude": 1e36})
+    with pytest.raises(FdtdDivergence):
+        driver.run(num_steps=40, progress_interval=10)
+    driver.close()

@@ -1,0 +1,59 @@
+"""Host-side setup tables against the reference's, recorded in tests/golden/tables.npz."""
+
+import numpy as np
+import pytest
+
+from meep_gpu_gb300.dft import FluxMonitor
+from meep_gpu_gb300.grid import Grid
+from meep_gpu_gb300.pml import PML, one_rank_line, runs_of, slab_index
+from meep_gpu_gb300.sources import deposition_table
+from tests import golden_io
+
+GOLD, META = golden_io.tables()
+GRID = Grid(tuple(META["grid"]["cell_size"]), META["grid"]["resolution"],
+            boundaries=META["grid"]["boundaries"])
+
+
+@pytest.mark.parametrize("thickness", META["pml_thicknesses"])
+def test_pml_coefficients_are_the_reference_words(thickness):
+    pml = PML(GRID, thickness)
+    for axis, name_axis in enumerate("xyz"):
+        for lattice, suffix in ((0, ""), (1, "_h")):
+            table = pml.tables[(lattice, axis)]
+            for name in ("kms", "sinv", "kps"):
+                expected = GOLD[f"pml_{thickness}_{name}_{name_axis}{suffix}"]
+                assert np.array_equal(getattr(table, name), expected), (thickness, name, name_axis, suffix)
+
+
+@pytest.mark.parametrize("index", range(len(META["sources"])))
+def test_source_tables_are_the_reference_tables(index):
+    request = META["sources"][index]
+    cells, amps = deposition_table(GRID, request["component"], tuple(request["center"]),
+                                   tuple(request["size"]))
+    expected_cells = [tuple(int(v) for v in row) for row in GOLD[f"src{index}_cells"]]
+    assert cells == expected_cells
+    assert np.array_equal(np.asarray(amps, dtype=np.complex128), GOLD[f"src{index}_amps"])
+
+
+@pytest.mark.parametrize("index", range(len(META["planes"])))
+def test_flux_plane_registration_is_the_reference(index):
+    plane = META["planes"][index]
+    monitor = FluxMonitor(GRID, (0.1, 0.2), tuple(plane["center"]), tuple(plane["size"]),
+                          None, 1.0, 1)
+    assert tuple(monitor.region) == tuple(int(v) for v in GOLD[f"plane{index}_region"])
+    assert np.array_equal(monitor.weights, GOLD[f"plane{index}_weights"])
+    assert monitor.measure == float(GOLD[f"plane{index}_measure"])
+
+
+def test_one_rank_membership_runs():
+    # 4-cell faces: span int(4 + 1.5) = 5; integer cells 1..5 low, n-4..n-1 high.
+    line = one_rank_line(24, (4, 4), 0, wraps=False)
+    assert runs_of(line) == (1, 6, 20, 24)
+    line = one_rank_line(24, (4, 4), 1, wraps=False)
+    assert runs_of(line) == (0, 5, 19, 24)
+    wrapped = one_rank_line(24, (0, 4), 0, wraps=True)
+    assert runs_of(wrapped) == (0, 1, 20, 24)
+    record = (1, 6, 20, 24)
+    rows = slab_index(record, np.arange(24))
+    assert list(rows[:7]) == [-1, 0, 1, 2, 3, 4, -1]
+    assert list(rows[19:]) == [-1, 5, 6, 7, 8]

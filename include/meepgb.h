@@ -93,15 +93,17 @@ typedef struct mgb_sim_desc {
   const float* kms[2][3];
   const float* sinv[2][3];
   const float* kps[2][3];
-  /* primary fields, full volumes */
+  /* primary fields, full volumes. H holds every cell: outside each component's
+   * own-axis integer PML membership MEEP's H is B's word (mu = 1), so B needs no
+   * storage of its own there. */
   float* E[3];
   float* D[3];
-  float* B[3];
+  float* H[3];
   const float* inv_eps[3]; /* may alias one another */
-  /* PML auxiliaries: stored H and f_w of H on each component's own-axis integer slab
-   * (H is B's word everywhere else), f_w of E on the own-axis half slab, and the curl
-   * split-field fu of B (half lattice) and D (integer lattice) on the dsigu slab. */
-  mgb_aux H[3];
+  /* PML auxiliaries: B and f_w of H on each H component's own-axis integer slab, f_w of
+   * E on the own-axis half slab, and the curl split-field fu of B (half lattice) and D
+   * (integer lattice) on the dsigu slab. */
+  mgb_aux B[3];
   mgb_aux fwH[3];
   mgb_aux fwE[3];
   mgb_aux fuB[3];
@@ -118,7 +120,9 @@ typedef struct mgb_sim_desc {
   /* monitors */
   int32_t nmonitors;
   mgb_monitor monitors[MGB_MAX_MONITORS];
-  /* non-finite detector: the E-kernel ORs 1 into *status when it writes a NaN/Inf E */
+  /* status word: the E half ORs 1 into it when it writes a NaN/Inf E; a tile kernel ORs
+   * 2 when a wait for its own shared-memory copies exceeds its time limit (the kernel
+   * then stops stepping instead of spinning). */
   int32_t* status; /* device, may be NULL */
 } mgb_sim_desc;
 
@@ -157,6 +161,10 @@ int mgb_launch(mgb_sim* sim, int64_t step, int32_t part, void* stream);
  * (meep_gpu/dft.py:3107) without the dA * weight scale, which the host applies. */
 int mgb_flux_spectrum(mgb_sim* sim, int32_t monitor, const float* weights, double* out,
                       void* stream);
+
+/* 1 when the plan steps with the TMA tile kernels, 0 when with the generic kernels (a z
+ * extent that is not a multiple of 4, or MEEPGB_TILES=0 in the environment). */
+int mgb_uses_tiles(mgb_sim* sim);
 
 /* Release the plan (never the caller's arrays). */
 void mgb_destroy(mgb_sim* sim);

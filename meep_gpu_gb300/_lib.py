@@ -62,9 +62,9 @@ class MgbSimDesc(ctypes.Structure):
         ("kps", (ctypes.c_void_p * 3) * 2),
         ("E", ctypes.c_void_p * 3),
         ("D", ctypes.c_void_p * 3),
-        ("B", ctypes.c_void_p * 3),
+        ("H", ctypes.c_void_p * 3),
         ("inv_eps", ctypes.c_void_p * 3),
-        ("H", MgbAux * 3),
+        ("B", MgbAux * 3),
         ("fwH", MgbAux * 3),
         ("fwE", MgbAux * 3),
         ("fuB", MgbAux * 3),
@@ -93,6 +93,7 @@ SIGNATURES = {
     "mgb_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p]),
     "mgb_flux_spectrum": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.c_void_p]),
+    "mgb_uses_tiles": (ctypes.c_int, [ctypes.c_void_p]),
     "mgb_destroy": (None, [ctypes.c_void_p]),
     "mgb_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
 }

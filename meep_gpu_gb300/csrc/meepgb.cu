@@ -1,11 +1,11 @@
 // meepgb.cu — GB300 (sm_103a) FDTD stepping kernels and the C ABI of libmeepgb.so.
 //
 // One step is two fused kernels:
-//   h_half: MEEP's step_B (curl E with the split-field UPML), zero_metal_B and
-//           update_H (own-axis constitutive accumulation, H aliased to B outside it);
-//   e_half: step_D, the electric source deposit in double, zero_metal_D, update_E
+//   H half: MEEP's step_B (curl E with the split-field UPML), zero_metal_B and
+//           update_H (own-axis constitutive accumulation);
+//   E half: step_D, the electric source deposit in double, zero_metal_D, update_E
 //           (chi1inv of D minus every polarization, own-axis accumulation) and update_P
-//           (Lorentz/Drude ADE), all on registers of one cell.
+//           (Lorentz/Drude ADE), all on the registers of one cell;
 // followed on decimated steps by dft_accumulate for every monitor.
 //
 // Arithmetic follows the reference array path operation for operation (meep_gpu/
@@ -13,20 +13,34 @@
 // _apply_dsig_only_update :2662, _apply_constitutive_pml :2991, separate_h_from_b
 // :2789, _mask_non_owned_cells :2589, _zero_metal :3135; dispersion.py
 // PolarizationState.update :689; sources.py _deposit :1357). The file is compiled
-// with -fmad=false so no multiply-add is contracted, which keeps every float32 word
-// equal to the reference's separately rounded operations.
+// with -fmad=false so no multiply-add is contracted: every float32 word equals the
+// reference's separately rounded operations.
 //
-// Work decomposition: a CTA covers a (BZ x BY) tile of (z, y) columns and marches
-// along x over a chunk of planes; the x-neighbour a stencil needs (E at i+1 for the H
-// half, H at i-1 for the E half) is carried in registers from the previous plane, and
-// the y/z neighbours are re-read through L1. Each cell's word is read from HBM once
-// per half step. PML auxiliaries live in compact slab arrays over the membership runs.
+// Storage: E, D and H are full volumes. MEEP's H is B's own word outside each H
+// component's own-axis PML membership, so B is stored only on that membership (a
+// compact slab) and H carries it everywhere else. Every PML auxiliary is a compact slab
+// over its membership runs.
+//
+// Two kernel families share that layout:
+//   tile kernels (h_tile, e_tile): a CTA owns a 64 (z) x 8 (y) tile and marches over a
+//     chunk of x planes. One thread issues TMA bulk-tensor loads (cp.async.bulk.tensor)
+//     of each plane's tiles (the stencil operand with its one-cell halo, the cell's own
+//     fields) into a ring of shared-memory stages guarded by mbarriers, several planes
+//     ahead of the 256 threads computing from shared memory; the x neighbour is the
+//     previous (or next) stage of the ring. Waits are bounded: a wait that outlives its
+//     limit sets status bit 2 and the CTA stops stepping.
+//   generic kernels (h_generic, e_generic): one thread per (y, z) column marching over
+//     x with plain loads, for grids whose z extent is not a multiple of 4 (TMA needs
+//     16-byte row strides).
 
 #include "meepgb.h"
 
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 
@@ -39,8 +53,17 @@ int fail(int code, const std::string& message) {
   return code;
 }
 
+constexpr int kInteger = 0;
+constexpr int kHalf = 1;
+constexpr int kTileZ = 64;          // cells per tile along z (innermost)
+constexpr int kTileY = 8;           // cells per tile along y
+constexpr int kHaloZ = kTileZ + 4;  // z extent of a halo box (16-byte multiple)
+constexpr int kHaloY = kTileY + 1;
+constexpr int kThreads = 256;
+constexpr int kBoxHalo = 2560;      // bytes of one halo box buffer (68 x 9 floats, 128-aligned)
+constexpr int kBoxOwn = kTileZ * kTileY * 4;  // 2048 bytes
+
 // ------------------------------------------------------------------------------------
-// Parameters passed by value (__grid_constant__) to the step kernels.
 struct StepParams {
   int nx, ny, nz;
   int met[3];
@@ -50,9 +73,9 @@ struct StepParams {
   const float* kps[2][3];
   float* E[3];
   float* D[3];
-  float* B[3];
+  float* H[3];
   const float* inv_eps[3];
-  mgb_aux H[3], fwH[3], fwE[3], fuB[3], fuD[3];
+  mgb_aux B[3], fwH[3], fwE[3], fuB[3], fuD[3];
   int npoles;
   int pbox[6];
   mgb_pole poles[MGB_MAX_POLES];
@@ -64,18 +87,25 @@ struct StepParams {
   int32_t* status;
 };
 
+// Tensor maps of the tile kernels (each 64-byte aligned, passed as __grid_constant__).
+struct TileMaps {
+  CUtensorMap E[3];     // box 68 x 9 x 1 (halo above in z and y)
+  CUtensorMap Hown[3];  // box 64 x 8 x 1
+  CUtensorMap Hhalo[3]; // box 68 x 9 x 1 (halo below in z and y)
+  CUtensorMap D[3];     // box 64 x 8 x 1
+  CUtensorMap inv[3];   // box 64 x 8 x 1
+  int ninv;             // distinct inverse-epsilon volumes (1 or 3)
+  int inv_of[3];        // which of inv[] serves each component
+  int stages;
+};
+
 struct DftParams {
   int nx, ny, nz;
   int met[3];
-  int pml;
   const float* E[3];
-  const float* B[3];
-  mgb_aux H[3];
+  const float* H[3];
   mgb_monitor mon;
 };
-
-constexpr int kInteger = 0;
-constexpr int kHalf = 1;
 
 __device__ __forceinline__ int slab_row(const mgb_aux& a, int i) {
   if (i >= a.a0 && i < a.a1) return i - a.a0;
@@ -117,11 +147,153 @@ __device__ __forceinline__ float curl_update(const StepParams& p, int lattice, i
   return (kms * f - curl) * sinv;
 }
 
-// ------------------------------------------------------------------------------------
-// H half: B -= curl E (split-field UPML), zero_metal_B, H from B.
+// B update of one cell from its curls, zero_metal_B, and H from B (update_H). `h_old`
+// is the stored H word, which is the old B outside the own-axis membership.
 template <bool PML>
-__global__ void __launch_bounds__(256) h_half(const __grid_constant__ StepParams p,
-                                              int first_step, int xchunk) {
+__device__ __forceinline__ void b_and_h(const StepParams& p, int first_step, int i, int j, int k,
+                                        float cx, float cy, float cz, const float h_old[3],
+                                        float h_new[3]) {
+  if (p.met[0] && i == 0) cx = 0.f;
+  if (p.met[1] && j == 0) cy = 0.f;
+  if (p.met[2] && k == 0) cz = 0.f;
+  if (!PML) {
+    h_new[0] = h_old[0] - cx;
+    h_new[1] = h_old[1] - cy;
+    h_new[2] = h_old[2] - cz;
+    if (p.met[0] && i == 0) h_new[0] = 0.f;
+    if (p.met[1] && j == 0) h_new[1] = 0.f;
+    if (p.met[2] && k == 0) h_new[2] = 0.f;
+    return;
+  }
+  const int at[3] = {i, j, k};
+  const float curls[3] = {cx, cy, cz};
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    const int row = slab_row(p.B[q], at[q]);
+    long long a = 0;
+    if (row >= 0) {
+      if (q == 0) a = aux_index<0>(p.B[0], row, i, j, k, p.ny, p.nz);
+      else if (q == 1) a = aux_index<1>(p.B[1], row, i, j, k, p.ny, p.nz);
+      else a = aux_index<2>(p.B[2], row, i, j, k, p.ny, p.nz);
+    }
+    float b = row >= 0 ? p.B[q].data[a] : h_old[q];
+    // Bx: dsig y, dsigu z; By: dsig z, dsigu x; Bz: dsig x, dsigu y (half lattice).
+    if (q == 0) b = curl_update<2>(p, kHalf, 1, p.fuB[0], b, curls[0], i, j, k);
+    else if (q == 1) b = curl_update<0>(p, kHalf, 2, p.fuB[1], b, curls[1], i, j, k);
+    else b = curl_update<1>(p, kHalf, 0, p.fuB[2], b, curls[2], i, j, k);
+    if (p.met[q] && at[q] == 0) b = 0.f;  // zero_metal_B: shift 0 only on its own axis
+    if (row >= 0) {
+      // update_H on the own-axis integer membership: fw' = B, H' = H + ((kps*B) - (kms*fw)).
+      const float fw_prev = first_step ? b : p.fwH[q].data[a];
+      const float h_prev = first_step ? b : h_old[q];
+      const float kps = __ldg(p.kps[kInteger][q] + at[q]);
+      const float kms = __ldg(p.kms[kInteger][q] + at[q]);
+      p.B[q].data[a] = b;
+      p.fwH[q].data[a] = b;
+      h_new[q] = h_prev + (kps * b - kms * fw_prev);
+    } else {
+      h_new[q] = b;
+    }
+  }
+}
+
+// D update of one cell from its curls, the source deposit, zero_metal_D, E and P.
+template <bool PML>
+__device__ __forceinline__ void d_e_p(const StepParams& p, int parity, int i, int j, int k,
+                                      long long c, float cx, float cy, float cz, float d[3],
+                                      const float inv[3]) {
+  const bool wx = p.met[0] && i == 0, wy = p.met[1] && j == 0, wz = p.met[2] && k == 0;
+  if (wy || wz) cx = 0.f;
+  if (wx || wz) cy = 0.f;
+  if (wx || wy) cz = 0.f;
+  if (PML) {
+    // Dx: dsig y, dsigu z; Dy: dsig z, dsigu x; Dz: dsig x, dsigu y (integer lattice).
+    d[0] = curl_update<2>(p, kInteger, 1, p.fuD[0], d[0], cx, i, j, k);
+    d[1] = curl_update<0>(p, kInteger, 2, p.fuD[1], d[1], cy, i, j, k);
+    d[2] = curl_update<1>(p, kInteger, 0, p.fuD[2], d[2], cz, i, j, k);
+  } else {
+    d[0] = d[0] - cx;
+    d[1] = d[1] - cy;
+    d[2] = d[2] - cz;
+  }
+  // Electric sources at t + dt/2: f = float(double(f) - A), point by point in order.
+  if (p.nsrc > 0 && i >= p.src_box[0] && i < p.src_box[1] && j >= p.src_box[2] &&
+      j < p.src_box[3] && k >= p.src_box[4] && k < p.src_box[5]) {
+    for (int s = 0; s < p.nsrc; ++s) {
+      if (p.src_cell[s] != c) continue;
+      const int q = p.src_comp[s];
+      const double a = p.src_words[s];
+      if (q == 0) d[0] = __double2float_rn(__dsub_rn((double)d[0], a));
+      else if (q == 1) d[1] = __double2float_rn(__dsub_rn((double)d[1], a));
+      else d[2] = __double2float_rn(__dsub_rn((double)d[2], a));
+    }
+  }
+  // zero_metal_D: shift 0 on both transverse axes.
+  if (wy || wz) d[0] = 0.f;
+  if (wx || wz) d[1] = 0.f;
+  if (wx || wy) d[2] = 0.f;
+  p.D[0][c] = d[0];
+  p.D[1][c] = d[1];
+  p.D[2][c] = d[2];
+  const bool in_box = p.npoles > 0 && i >= p.pbox[0] && i < p.pbox[1] && j >= p.pbox[2] &&
+                      j < p.pbox[3] && k >= p.pbox[4] && k < p.pbox[5];
+  long long pb = 0;
+  if (in_box) {
+    const int bny = p.pbox[3] - p.pbox[2], bnz = p.pbox[5] - p.pbox[4];
+    pb = ((long long)(i - p.pbox[0]) * bny + (j - p.pbox[2])) * bnz + (k - p.pbox[4]);
+  }
+  const int at[3] = {i, j, k};
+  bool bad = false;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    float dmp = d[q];
+    if (in_box) {
+      for (int m = 0; m < p.npoles; ++m) {
+        const mgb_pole& pole = p.poles[m];
+        if (pole.sigma[q] != nullptr) dmp = dmp - (parity ? pole.p[q][1] : pole.p[q][0])[pb];
+      }
+    }
+    const float w = inv[q] * dmp;
+    float e = w;
+    if (PML) {
+      const int row = slab_row(p.fwE[q], at[q]);
+      if (row >= 0) {
+        long long a;
+        if (q == 0) a = aux_index<0>(p.fwE[0], row, i, j, k, p.ny, p.nz);
+        else if (q == 1) a = aux_index<1>(p.fwE[1], row, i, j, k, p.ny, p.nz);
+        else a = aux_index<2>(p.fwE[2], row, i, j, k, p.ny, p.nz);
+        const float fw_prev = p.fwE[q].data[a];
+        p.fwE[q].data[a] = w;
+        const float kps = __ldg(p.kps[kHalf][q] + at[q]);
+        const float kms = __ldg(p.kms[kHalf][q] + at[q]);
+        e = p.E[q][c] + (kps * w - kms * fw_prev);
+      }
+    }
+    p.E[q][c] = e;
+    bad |= !isfinite(e);
+    if (in_box) {
+      // update_P: P' = g1inv*(((P*A) - (g1*Pp)) + (w0dt2*(s*W))), written over Pp.
+      for (int m = 0; m < p.npoles; ++m) {
+        const mgb_pole& pole = p.poles[m];
+        if (pole.sigma[q] == nullptr) continue;
+        const float* cur = parity ? pole.p[q][1] : pole.p[q][0];
+        float* prv = parity ? pole.p[q][0] : pole.p[q][1];
+        const float pc = cur[pb];
+        const float pp = prv[pb];
+        const float s = __ldg(pole.sigma[q] + pb);
+        const float drive = pole.omega0dtsqr * (s * w);
+        prv[pb] = pole.gamma1inv * ((pc * pole.two_minus_od - pole.gamma1 * pp) + drive);
+      }
+    }
+  }
+  if (bad && p.status != nullptr) atomicOr(p.status, 1);
+}
+
+// ------------------------------------------------------------------------------------
+// Generic kernels: plain loads, one thread per (y, z) column marching over x.
+template <bool PML>
+__global__ void __launch_bounds__(256) h_generic(const __grid_constant__ StepParams p,
+                                                 int first_step, int xchunk) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
@@ -129,11 +301,10 @@ __global__ void __launch_bounds__(256) h_half(const __grid_constant__ StepParams
   const int i1 = min(i0 + xchunk, p.nx);
   const long long sx = (long long)p.ny * p.nz;
   const long long sy = p.nz;
-  const float* __restrict__ Ex = p.E[0];
-  const float* __restrict__ Ey = p.E[1];
-  const float* __restrict__ Ez = p.E[2];
+  const float* Ex = p.E[0];
+  const float* Ey = p.E[1];
+  const float* Ez = p.E[2];
   const float dtdx = p.dtdx;
-  // Offsets of the +1 neighbours; a metallic far face reads the zero ghost instead.
   const bool ytop = (j + 1 == p.ny), ztop = (k + 1 == p.nz);
   const bool ywall = ytop && p.met[1], zwall = ztop && p.met[2];
   const long long oy = ytop ? -(long long)(p.ny - 1) * sy : sy;
@@ -160,72 +331,23 @@ __global__ void __launch_bounds__(256) h_half(const __grid_constant__ StepParams
     const float ey_zp = zwall ? 0.f : Ey[c + oz];
     const float ex_zp = zwall ? 0.f : Ex[c + oz];
     // MEEP's association ((g1s - g1) + g2) - g2s, then the dtdx scale.
-    float cx = dtdx * (((ez_yp - ez) + ey) - ey_zp);
-    float cy = dtdx * (((ex_zp - ex) + ez) - ez_xp);
-    float cz = dtdx * (((ey_xp - ey) + ex) - ex_yp);
-    // Owned-cell masks: a shift-0 axis on a metallic wall does not step cell 0.
-    if (p.met[0] && i == 0) cx = 0.f;
-    if (p.met[1] && j == 0) cy = 0.f;
-    if (p.met[2] && k == 0) cz = 0.f;
-    float bx = p.B[0][c], by = p.B[1][c], bz = p.B[2][c];
-    if (PML) {
-      // Bx: dsig y, dsigu z; By: dsig z, dsigu x; Bz: dsig x, dsigu y (half lattice).
-      bx = curl_update<2>(p, kHalf, 1, p.fuB[0], bx, cx, i, j, k);
-      by = curl_update<0>(p, kHalf, 2, p.fuB[1], by, cy, i, j, k);
-      bz = curl_update<1>(p, kHalf, 0, p.fuB[2], bz, cz, i, j, k);
-    } else {
-      bx = bx - cx;
-      by = by - cy;
-      bz = bz - cz;
-    }
-    // zero_metal_B: the component sits on the wall of every axis where its shift is 0.
-    if (p.met[0] && i == 0) bx = 0.f;
-    if (p.met[1] && j == 0) by = 0.f;
-    if (p.met[2] && k == 0) bz = 0.f;
-    p.B[0][c] = bx;
-    p.B[1][c] = by;
-    p.B[2][c] = bz;
-    if (PML) {
-      // update_H on the own-axis integer membership: fw' = B, H' = H + ((kps*B) - (kms*fw)).
-      const float bs[3] = {bx, by, bz};
-      const int at[3] = {i, j, k};
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        const int row = slab_row(p.H[q], at[q]);
-        if (row < 0) continue;
-        long long a;
-        if (q == 0) a = aux_index<0>(p.H[0], row, i, j, k, p.ny, p.nz);
-        else if (q == 1) a = aux_index<1>(p.H[1], row, i, j, k, p.ny, p.nz);
-        else a = aux_index<2>(p.H[2], row, i, j, k, p.ny, p.nz);
-        const float fw_prev = first_step ? bs[q] : p.fwH[q].data[a];
-        const float h_prev = first_step ? bs[q] : p.H[q].data[a];
-        const float kps = __ldg(p.kps[kInteger][q] + at[q]);
-        const float kms = __ldg(p.kms[kInteger][q] + at[q]);
-        p.fwH[q].data[a] = bs[q];
-        p.H[q].data[a] = h_prev + (kps * bs[q] - kms * fw_prev);
-      }
-    }
+    const float cx = dtdx * (((ez_yp - ez) + ey) - ey_zp);
+    const float cy = dtdx * (((ex_zp - ex) + ez) - ez_xp);
+    const float cz = dtdx * (((ey_xp - ey) + ex) - ex_yp);
+    const float h_old[3] = {p.H[0][c], p.H[1][c], p.H[2][c]};
+    float h_new[3];
+    b_and_h<PML>(p, first_step, i, j, k, cx, cy, cz, h_old, h_new);
+    p.H[0][c] = h_new[0];
+    p.H[1][c] = h_new[1];
+    p.H[2][c] = h_new[2];
     ey = ey_xp;
     ez = ez_xp;
   }
 }
 
-// H component q at (i, j, k): the stored own-axis slab word, or B's word outside it.
-template <bool PML, int Q>
-__device__ __forceinline__ float read_h(const StepParams& p, long long c, int i, int j, int k) {
-  if (PML) {
-    const int at = Q == 0 ? i : (Q == 1 ? j : k);
-    const int row = slab_row(p.H[Q], at);
-    if (row >= 0) return p.H[Q].data[aux_index<Q>(p.H[Q], row, i, j, k, p.ny, p.nz)];
-  }
-  return p.B[Q][c];
-}
-
-// ------------------------------------------------------------------------------------
-// E half: D += curl H (negated strides), source deposit, zero_metal_D, E, P.
 template <bool PML>
-__global__ void __launch_bounds__(256) e_half(const __grid_constant__ StepParams p, int parity,
-                                              int xchunk) {
+__global__ void __launch_bounds__(256) e_generic(const __grid_constant__ StepParams p, int parity,
+                                                 int xchunk) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
@@ -234,161 +356,361 @@ __global__ void __launch_bounds__(256) e_half(const __grid_constant__ StepParams
   const long long sx = (long long)p.ny * p.nz;
   const long long sy = p.nz;
   const float dtdx = p.dtdx;
-  const bool ybot = (j == 0), zbot = (k == 0);
-  const int jm = ybot ? (p.met[1] ? -1 : p.ny - 1) : j - 1;
-  const int km = zbot ? (p.met[2] ? -1 : p.nz - 1) : k - 1;
+  const float* Hx = p.H[0];
+  const float* Hy = p.H[1];
+  const float* Hz = p.H[2];
+  const int jm = j == 0 ? (p.met[1] ? -1 : p.ny - 1) : j - 1;
+  const int km = k == 0 ? (p.met[2] ? -1 : p.nz - 1) : k - 1;
   const long long col = (long long)j * sy + k;
   long long c = (long long)i0 * sx + col;
-  // H at i0 - 1 (x-neighbour below) for Hy and Hz.
   float hy_xm = 0.f, hz_xm = 0.f;
   {
     int im = i0 - 1;
     if (im < 0) im = p.met[0] ? -1 : p.nx - 1;
     if (im >= 0) {
-      const long long cm = (long long)im * sx + col;
-      hy_xm = read_h<PML, 1>(p, cm, im, j, k);
-      hz_xm = read_h<PML, 2>(p, cm, im, j, k);
+      hy_xm = Hy[(long long)im * sx + col];
+      hz_xm = Hz[(long long)im * sx + col];
     }
   }
-  const bool src_cols = p.nsrc > 0 && j >= p.src_box[2] && j < p.src_box[3] &&
-                        k >= p.src_box[4] && k < p.src_box[5];
   for (int i = i0; i < i1; ++i, c += sx) {
-    const float hx = read_h<PML, 0>(p, c, i, j, k);
-    const float hy = read_h<PML, 1>(p, c, i, j, k);
-    const float hz = read_h<PML, 2>(p, c, i, j, k);
+    const float hx = Hx[c], hy = Hy[c], hz = Hz[c];
     float hz_ym = 0.f, hx_ym = 0.f, hy_zm = 0.f, hx_zm = 0.f;
     if (jm >= 0) {
       const long long cm = (long long)i * sx + (long long)jm * sy + k;
-      hz_ym = read_h<PML, 2>(p, cm, i, jm, k);
-      hx_ym = read_h<PML, 0>(p, cm, i, jm, k);
+      hz_ym = Hz[cm];
+      hx_ym = Hx[cm];
     }
     if (km >= 0) {
       const long long cm = (long long)i * sx + (long long)j * sy + km;
-      hy_zm = read_h<PML, 1>(p, cm, i, j, km);
-      hx_zm = read_h<PML, 0>(p, cm, i, j, km);
+      hy_zm = Hy[cm];
+      hx_zm = Hx[cm];
     }
-    float cx = dtdx * (((hz_ym - hz) + hy) - hy_zm);
-    float cy = dtdx * (((hx_zm - hx) + hz) - hz_xm);
-    float cz = dtdx * (((hy_xm - hy) + hx) - hx_ym);
-    const bool wx = p.met[0] && i == 0, wy = p.met[1] && j == 0, wz = p.met[2] && k == 0;
-    if (wy || wz) cx = 0.f;
-    if (wx || wz) cy = 0.f;
-    if (wx || wy) cz = 0.f;
+    const float cx = dtdx * (((hz_ym - hz) + hy) - hy_zm);
+    const float cy = dtdx * (((hx_zm - hx) + hz) - hz_xm);
+    const float cz = dtdx * (((hy_xm - hy) + hx) - hx_ym);
     float d[3] = {p.D[0][c], p.D[1][c], p.D[2][c]};
-    if (PML) {
-      // Dx: dsig y, dsigu z; Dy: dsig z, dsigu x; Dz: dsig x, dsigu y (integer lattice).
-      d[0] = curl_update<2>(p, kInteger, 1, p.fuD[0], d[0], cx, i, j, k);
-      d[1] = curl_update<0>(p, kInteger, 2, p.fuD[1], d[1], cy, i, j, k);
-      d[2] = curl_update<1>(p, kInteger, 0, p.fuD[2], d[2], cz, i, j, k);
-    } else {
-      d[0] = d[0] - cx;
-      d[1] = d[1] - cy;
-      d[2] = d[2] - cz;
-    }
-    // Electric sources at t + dt/2: f = float(double(f) - A), point by point in order.
-    if (src_cols && i >= p.src_box[0] && i < p.src_box[1]) {
-      for (int s = 0; s < p.nsrc; ++s) {
-        if (p.src_cell[s] != c) continue;
-        const int q = p.src_comp[s];
-        const double a = p.src_words[s];
-        if (q == 0) d[0] = __double2float_rn(__dsub_rn((double)d[0], a));
-        else if (q == 1) d[1] = __double2float_rn(__dsub_rn((double)d[1], a));
-        else d[2] = __double2float_rn(__dsub_rn((double)d[2], a));
-      }
-    }
-    // zero_metal_D.
-    if (wy || wz) d[0] = 0.f;
-    if (wx || wz) d[1] = 0.f;
-    if (wx || wy) d[2] = 0.f;
-    p.D[0][c] = d[0];
-    p.D[1][c] = d[1];
-    p.D[2][c] = d[2];
-    // Polarization box position of this cell.
-    const bool in_box = p.npoles > 0 && i >= p.pbox[0] && i < p.pbox[1] && j >= p.pbox[2] &&
-                        j < p.pbox[3] && k >= p.pbox[4] && k < p.pbox[5];
-    long long pb = 0;
-    if (in_box) {
-      const int bny = p.pbox[3] - p.pbox[2], bnz = p.pbox[5] - p.pbox[4];
-      pb = ((long long)(i - p.pbox[0]) * bny + (j - p.pbox[2])) * bnz + (k - p.pbox[4]);
-    }
-    const int at[3] = {i, j, k};
-    bool bad = false;
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      float dmp = d[q];
-      if (in_box) {
-        for (int m = 0; m < p.npoles; ++m) {
-          if (p.poles[m].sigma[q] != nullptr) dmp = dmp - p.poles[m].p[q][parity][pb];
-        }
-      }
-      const float w = __ldg(p.inv_eps[q] + c) * dmp;
-      float e = w;
-      if (PML) {
-        const int row = slab_row(p.fwE[q], at[q]);
-        if (row >= 0) {
-          long long a;
-          if (q == 0) a = aux_index<0>(p.fwE[0], row, i, j, k, p.ny, p.nz);
-          else if (q == 1) a = aux_index<1>(p.fwE[1], row, i, j, k, p.ny, p.nz);
-          else a = aux_index<2>(p.fwE[2], row, i, j, k, p.ny, p.nz);
-          const float fw_prev = p.fwE[q].data[a];
-          p.fwE[q].data[a] = w;
-          const float kps = __ldg(p.kps[kHalf][q] + at[q]);
-          const float kms = __ldg(p.kms[kHalf][q] + at[q]);
-          e = p.E[q][c] + (kps * w - kms * fw_prev);
-        }
-      }
-      p.E[q][c] = e;
-      bad |= !isfinite(e);
-      if (in_box) {
-        // update_P: P' = g1inv*(((P*A) - (g1*Pp)) + (w0dt2*(s*W))), written over Pp.
-        for (int m = 0; m < p.npoles; ++m) {
-          const mgb_pole& pole = p.poles[m];
-          if (pole.sigma[q] == nullptr) continue;
-          float* cur = pole.p[q][parity];
-          float* prv = pole.p[q][parity ^ 1];
-          const float pc = cur[pb];
-          const float pp = prv[pb];
-          const float s = __ldg(pole.sigma[q] + pb);
-          const float drive = pole.omega0dtsqr * (s * w);
-          prv[pb] = pole.gamma1inv * ((pc * pole.two_minus_od - pole.gamma1 * pp) + drive);
-        }
-      }
-    }
-    if (bad && p.status != nullptr) atomicOr(p.status, 1);
+    const float inv[3] = {__ldg(p.inv_eps[0] + c), __ldg(p.inv_eps[1] + c), __ldg(p.inv_eps[2] + c)};
+    d_e_p<PML>(p, parity, i, j, k, c, cx, cy, cz, d, inv);
     hy_xm = hy;
     hz_xm = hz;
   }
 }
 
 // ------------------------------------------------------------------------------------
-// DFT accumulation on one monitor: cell-centred samples times float64-formed phases.
-template <bool PML, int Q>
-__device__ __forceinline__ float read_h_dft(const DftParams& p, long long c, int i, int j,
-                                            int k) {
-  if (PML) {
-    const int at = Q == 0 ? i : (Q == 1 ? j : k);
-    const int row = slab_row(p.H[Q], at);
-    if (row >= 0) return p.H[Q].data[aux_index<Q>(p.H[Q], row, i, j, k, p.ny, p.nz)];
-  }
-  return p.B[Q][c];
+// TMA + mbarrier primitives (inline PTX).
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
 }
 
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wait for phase `parity` of a stage barrier, for at most ~2 s of wall time.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long start = global_ns();
+  for (;;) {
+    for (int spin = 0; spin < 256; ++spin)
+      if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - start > 2000000000ull) return false;
+  }
+}
+
+__device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* map,
+                                         unsigned long long* bar, int z, int y, int x) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(smem_addr(bar)), "r"(z), "r"(y), "r"(x)
+      : "memory");
+}
+
+// ------------------------------------------------------------------------------------
+// Tile kernels.
+//
+// H half. Ring stage of chain index c (plane i0 + c): the E box (68 x 9, z from k0 and
+// y from j0, so the +1 halo of the forward differences) and, for planes below i1, the
+// cell's own H box. Plane i1 (the chunk's x neighbour above) carries E only; past the
+// high x face it is the zero fill of a metallic wall or plane 0 of a periodic axis.
 template <bool PML>
-__device__ float field_at(const DftParams& p, int comp, int i, int j, int k) {
+__global__ void __launch_bounds__(kThreads) h_tile(const __grid_constant__ StepParams p,
+                                                  const __grid_constant__ TileMaps maps,
+                                                  int first_step, int xchunk) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int S = maps.stages;
+  const int stage_bytes = 3 * kBoxHalo + 3 * kBoxOwn;
+  unsigned long long* full = reinterpret_cast<unsigned long long*>(smem + S * stage_bytes);
+  __shared__ int abort_flag;
+  const int tid = threadIdx.x;
+  const int k0 = blockIdx.x * kTileZ, j0 = blockIdx.y * kTileY;
+  const int i0 = blockIdx.z * xchunk;
+  const int i1 = min(i0 + xchunk, p.nx);
+  const int nchain = i1 - i0 + 1;  // planes i0 .. i1
+  auto e_box = [&](int st, int q) { return reinterpret_cast<float*>(smem + st * stage_bytes + q * kBoxHalo); };
+  auto h_box = [&](int st, int q) { return reinterpret_cast<float*>(smem + st * stage_bytes + 3 * kBoxHalo + q * kBoxOwn); };
+  auto issue = [&](int chain) {
+    const int st = chain % S;
+    const int plane = i0 + chain;
+    const bool own = plane < i1;
+    const int xplane = (plane >= p.nx && !p.met[0]) ? plane - p.nx : plane;
+    mbar_expect_tx(&full[st], 3 * (kHaloZ * kHaloY * 4) + (own ? 3 * kBoxOwn : 0));
+    for (int q = 0; q < 3; ++q) tma_load(e_box(st, q), &maps.E[q], &full[st], k0, j0, xplane);
+    if (own)
+      for (int q = 0; q < 3; ++q) tma_load(h_box(st, q), &maps.Hown[q], &full[st], k0, j0, plane);
+  };
+  if (tid == 0) {
+    abort_flag = 0;
+    for (int s = 0; s < S; ++s) mbar_init(&full[s], 1);
+    mbar_fence_init();
+    for (int c = 0; c < S && c < nchain; ++c) issue(c);
+  }
+  __syncthreads();
+  const int lane = tid & 31, ty = tid >> 5;
+  const int j = j0 + ty;
+  // Periodic faces: the halo row/column past the far face is row/column 0, which the
+  // box's zero fill does not supply.
+  const bool patch_y = !p.met[1] && j0 + kTileY >= p.ny;
+  const bool patch_z = !p.met[2] && k0 + kTileZ >= p.nz;
+  const long long sx = (long long)p.ny * p.nz;
+  auto wait_chain = [&](int chain) {
+    const int st = chain % S;
+    if (!mbar_wait(&full[st], (unsigned)((chain / S) & 1))) {
+      abort_flag = 1;
+      if (p.status != nullptr) atomicOr(p.status, 2);
+    }
+    __syncthreads();  // the abort decision is uniform; the stage is complete for everyone
+    if (!abort_flag && (patch_y || patch_z)) {
+      const int plane = i0 + chain;
+      const int xplane = (plane >= p.nx && !p.met[0]) ? plane - p.nx : plane;
+      const bool in_x = xplane < p.nx;
+      if (patch_y) {
+        const int ry = p.ny - j0;  // halo row standing for y = ny
+        for (int t = tid; t < 3 * kHaloZ; t += kThreads) {
+          const int q = t / kHaloZ, z = t % kHaloZ, kk = k0 + z;
+          float v = 0.f;
+          if (in_x && kk < p.nz) v = p.E[q][(long long)xplane * sx + kk];
+          e_box(st, q)[ry * kHaloZ + z] = v;
+        }
+      }
+      if (patch_z) {
+        const int rz = p.nz - k0;  // halo column standing for z = nz
+        for (int t = tid; t < 3 * kHaloY; t += kThreads) {
+          const int q = t / kHaloY, y = t % kHaloY;
+          int jj = j0 + y;
+          if (jj >= p.ny) jj = p.met[1] ? -1 : jj - p.ny;
+          float v = 0.f;
+          if (in_x && jj >= 0) v = p.E[q][(long long)xplane * sx + (long long)jj * p.nz];
+          e_box(st, q)[y * kHaloZ + rz] = v;
+        }
+      }
+      __syncthreads();
+    }
+  };
+  wait_chain(0);
+  const float dtdx = p.dtdx;
+  for (int i = i0; i < i1; ++i) {
+    const int chain = i - i0;
+    wait_chain(chain + 1);
+    if (abort_flag) break;
+    const int s0 = chain % S, s1 = (chain + 1) % S;
+    const float* Ex0 = e_box(s0, 0);
+    const float* Ey0 = e_box(s0, 1);
+    const float* Ez0 = e_box(s0, 2);
+    const float* Ey1 = e_box(s1, 1);
+    const float* Ez1 = e_box(s1, 2);
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int tz = lane + 32 * half;
+      const int k = k0 + tz;
+      if (j < p.ny && k < p.nz) {
+        const int e = ty * kHaloZ + tz;
+        const float ex = Ex0[e], ey = Ey0[e], ez = Ez0[e];
+        const float cx = dtdx * (((Ez0[e + kHaloZ] - ez) + ey) - Ey0[e + 1]);
+        const float cy = dtdx * (((Ex0[e + 1] - ex) + ez) - Ez1[e]);
+        const float cz = dtdx * (((Ey1[e] - ey) + ex) - Ex0[e + kHaloZ]);
+        const int o = ty * kTileZ + tz;
+        const float h_old[3] = {h_box(s0, 0)[o], h_box(s0, 1)[o], h_box(s0, 2)[o]};
+        float h_new[3];
+        b_and_h<PML>(p, first_step, i, j, k, cx, cy, cz, h_old, h_new);
+        const long long c = (long long)i * sx + (long long)j * p.nz + k;
+        p.H[0][c] = h_new[0];
+        p.H[1][c] = h_new[1];
+        p.H[2][c] = h_new[2];
+      }
+    }
+    __syncthreads();  // stage s0 is read by everyone: refill it
+    if (tid == 0 && chain + S < nchain) {
+      fence_proxy_async_smem();
+      issue(chain + S);
+    }
+  }
+}
+
+// E half. Ring stage of chain index c (plane i0 - 1 + c): the H box (68 x 9, z from
+// k0 - 4 and y from j0 - 1, so the -1 halo of the backward differences) and, for planes
+// at or above i0, the cell's own D and inverse-epsilon boxes. Plane i0 - 1 (the chunk's
+// x neighbour below) carries H only; below the low x face it is the zero fill of a
+// metallic wall or plane nx - 1 of a periodic axis.
+template <bool PML>
+__global__ void __launch_bounds__(kThreads) e_tile(const __grid_constant__ StepParams p,
+                                                  const __grid_constant__ TileMaps maps,
+                                                  int parity, int xchunk) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int S = maps.stages;
+  const int stage_bytes = 3 * kBoxHalo + (3 + maps.ninv) * kBoxOwn;
+  unsigned long long* full = reinterpret_cast<unsigned long long*>(smem + S * stage_bytes);
+  __shared__ int abort_flag;
+  const int tid = threadIdx.x;
+  const int k0 = blockIdx.x * kTileZ, j0 = blockIdx.y * kTileY;
+  const int i0 = blockIdx.z * xchunk;
+  const int i1 = min(i0 + xchunk, p.nx);
+  const int nchain = i1 - i0 + 1;  // planes i0-1 .. i1-1
+  auto h_box = [&](int st, int q) { return reinterpret_cast<float*>(smem + st * stage_bytes + q * kBoxHalo); };
+  auto own_box = [&](int st, int slot) { return reinterpret_cast<float*>(smem + st * stage_bytes + 3 * kBoxHalo + slot * kBoxOwn); };
+  auto issue = [&](int chain) {
+    const int st = chain % S;
+    const int plane = i0 - 1 + chain;
+    const bool own = plane >= i0;
+    const int xplane = (plane < 0 && !p.met[0]) ? plane + p.nx : plane;
+    mbar_expect_tx(&full[st], 3 * (kHaloZ * kHaloY * 4) + (own ? (3 + maps.ninv) * kBoxOwn : 0));
+    for (int q = 0; q < 3; ++q) tma_load(h_box(st, q), &maps.Hhalo[q], &full[st], k0 - 4, j0 - 1, xplane);
+    if (own) {
+      for (int q = 0; q < 3; ++q) tma_load(own_box(st, q), &maps.D[q], &full[st], k0, j0, plane);
+      for (int q = 0; q < maps.ninv; ++q) tma_load(own_box(st, 3 + q), &maps.inv[q], &full[st], k0, j0, plane);
+    }
+  };
+  if (tid == 0) {
+    abort_flag = 0;
+    for (int s = 0; s < S; ++s) mbar_init(&full[s], 1);
+    mbar_fence_init();
+    for (int c = 0; c < S && c < nchain; ++c) issue(c);
+  }
+  __syncthreads();
+  const int lane = tid & 31, ty = tid >> 5;
+  const int j = j0 + ty;
+  const bool patch_y = !p.met[1] && j0 == 0;
+  const bool patch_z = !p.met[2] && k0 == 0;
+  const long long sx = (long long)p.ny * p.nz;
+  auto wait_chain = [&](int chain) {
+    const int st = chain % S;
+    if (!mbar_wait(&full[st], (unsigned)((chain / S) & 1))) {
+      abort_flag = 1;
+      if (p.status != nullptr) atomicOr(p.status, 2);
+    }
+    __syncthreads();  // the abort decision is uniform; the stage is complete for everyone
+    if (!abort_flag && (patch_y || patch_z)) {
+      const int plane = i0 - 1 + chain;
+      const int xplane = (plane < 0 && !p.met[0]) ? plane + p.nx : plane;
+      const bool in_x = xplane >= 0;
+      if (patch_y) {  // halo row 0 stands for y = -1, i.e. y = ny - 1
+        for (int t = tid; t < 3 * kHaloZ; t += kThreads) {
+          const int q = t / kHaloZ, z = t % kHaloZ;
+          int kk = k0 - 4 + z;
+          if (kk < 0) kk = p.met[2] ? -1 : kk + p.nz;
+          float v = 0.f;
+          if (in_x && kk >= 0 && kk < p.nz)
+            v = p.H[q][(long long)xplane * sx + (long long)(p.ny - 1) * p.nz + kk];
+          h_box(st, q)[z] = v;
+        }
+      }
+      if (patch_z) {  // halo column 3 stands for z = -1, i.e. z = nz - 1
+        for (int t = tid; t < 3 * kHaloY; t += kThreads) {
+          const int q = t / kHaloY, y = t % kHaloY;
+          int jj = j0 - 1 + y;
+          if (jj < 0) jj = p.met[1] ? -1 : jj + p.ny;
+          float v = 0.f;
+          if (in_x && jj >= 0 && jj < p.ny)
+            v = p.H[q][(long long)xplane * sx + (long long)jj * p.nz + (p.nz - 1)];
+          h_box(st, q)[y * kHaloZ + 3] = v;
+        }
+      }
+      __syncthreads();
+    }
+  };
+  wait_chain(0);
+  const float dtdx = p.dtdx;
+  for (int i = i0; i < i1; ++i) {
+    const int chain = i - i0 + 1;
+    wait_chain(chain);
+    if (abort_flag) break;
+    const int s1 = chain % S, s0 = (chain - 1) % S;
+    const float* Hx = h_box(s1, 0);
+    const float* Hy = h_box(s1, 1);
+    const float* Hz = h_box(s1, 2);
+    const float* Hy0 = h_box(s0, 1);
+    const float* Hz0 = h_box(s0, 2);
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int tz = lane + 32 * half;
+      const int k = k0 + tz;
+      if (j < p.ny && k < p.nz) {
+        const int h = (ty + 1) * kHaloZ + tz + 4;
+        const float hx = Hx[h], hy = Hy[h], hz = Hz[h];
+        const float cx = dtdx * (((Hz[h - kHaloZ] - hz) + hy) - Hy[h - 1]);
+        const float cy = dtdx * (((Hx[h - 1] - hx) + hz) - Hz0[h]);
+        const float cz = dtdx * (((Hy0[h] - hy) + hx) - Hx[h - kHaloZ]);
+        const int o = ty * kTileZ + tz;
+        float d[3] = {own_box(s1, 0)[o], own_box(s1, 1)[o], own_box(s1, 2)[o]};
+        const float inv[3] = {own_box(s1, 3 + maps.inv_of[0])[o], own_box(s1, 3 + maps.inv_of[1])[o],
+                              own_box(s1, 3 + maps.inv_of[2])[o]};
+        const long long c = (long long)i * sx + (long long)j * p.nz + k;
+        d_e_p<PML>(p, parity, i, j, k, c, cx, cy, cz, d, inv);
+      }
+    }
+    __syncthreads();
+    if (tid == 0 && chain - 1 + S < nchain) {
+      fence_proxy_async_smem();
+      issue(chain - 1 + S);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// DFT accumulation on one monitor: cell-centred samples times float64-formed phases.
+__device__ __forceinline__ float field_at(const DftParams& p, int comp, int i, int j, int k) {
   // Past a face: metallic walls hold zero, periodic axes wrap.
   if (i >= p.nx) { if (p.met[0]) return 0.f; i -= p.nx; }
   if (j >= p.ny) { if (p.met[1]) return 0.f; j -= p.ny; }
   if (k >= p.nz) { if (p.met[2]) return 0.f; k -= p.nz; }
   const long long c = ((long long)i * p.ny + j) * p.nz + k;
-  if (comp < 3) return p.E[comp][c];
-  if (comp == 3) return read_h_dft<PML, 0>(p, c, i, j, k);
-  if (comp == 4) return read_h_dft<PML, 1>(p, c, i, j, k);
-  return read_h_dft<PML, 2>(p, c, i, j, k);
+  return comp < 3 ? p.E[comp][c] : p.H[comp - 3][c];
 }
 
 // Yee-to-centre average along every axis where the component's shift is 0, x then y
 // then z, each 0.5*(f[i] + f[i+1]) in float32 (reference dft.py:352).
-template <bool PML>
 __device__ float centred(const DftParams& p, int comp, int i, int j, int k) {
   // Yee shifts: Ex (1,0,0) Ey (0,1,0) Ez (0,0,1) Hx (0,1,1) Hy (1,0,1) Hz (1,1,0).
   const int q = comp % 3;
@@ -402,8 +724,8 @@ __device__ float centred(const DftParams& p, int comp, int i, int j, int k) {
 #pragma unroll
     for (int a = 0; a < 2; ++a) {
       if ((a && !ay) || (b && !az)) { v[b][a] = 0.f; continue; }
-      const float f0 = field_at<PML>(p, comp, i, j + a, k + b);
-      v[b][a] = ax ? 0.5f * (f0 + field_at<PML>(p, comp, i + 1, j + a, k + b)) : f0;
+      const float f0 = field_at(p, comp, i, j + a, k + b);
+      v[b][a] = ax ? 0.5f * (f0 + field_at(p, comp, i + 1, j + a, k + b)) : f0;
     }
   }
   float r0 = ay ? 0.5f * (v[0][0] + v[0][1]) : v[0][0];
@@ -412,7 +734,6 @@ __device__ float centred(const DftParams& p, int comp, int i, int j, int k) {
   return 0.5f * (r0 + r1);
 }
 
-template <bool PML>
 __global__ void __launch_bounds__(256) dft_accumulate(const __grid_constant__ DftParams p,
                                                       long long step) {
   extern __shared__ float2 phase[];  // [0, nf): E phases, [nf, 2nf): H phases
@@ -440,7 +761,7 @@ __global__ void __launch_bounds__(256) dft_accumulate(const __grid_constant__ Df
   const int i = m.region[0] + ri, j = m.region[2] + rj, k = m.region[4] + rk;
   for (int q = 0; q < m.ncomp; ++q) {
     const int comp = m.comp[q];
-    const float s = centred<PML>(p, comp, i, j, k);
+    const float s = centred(p, comp, i, j, k);
     const float2* ph = comp < 3 ? phase : phase + nf;
     float* acc = m.acc + (long long)q * nf * 2 * cells + cell;
     for (int f = 0; f < nf; ++f) {
@@ -488,12 +809,16 @@ __global__ void __launch_bounds__(256) flux_reduce(const __grid_constant__ mgb_m
 struct mgb_sim {
   mgb_sim_desc desc;
   StepParams step;
+  TileMaps maps;
+  bool tiles = false;
+  size_t h_smem = 0, e_smem = 0;
   const double* words = nullptr;
   long long words_first = 0;
   long long words_steps = 0;
   int block_z = 32;
   int block_y = 8;
-  int xchunk = 16;
+  int xchunk = 16;       // generic kernels
+  int tile_xchunk = 24;  // tile kernels
 };
 
 namespace {
@@ -516,6 +841,81 @@ int launch_error(const char* what) {
     return fail(MGB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(err));
   }
   return MGB_OK;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (fn == nullptr) {
+    void* ptr = nullptr;
+    cudaDriverEntryPointQueryResult status;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault,
+                                         &status) == cudaSuccess &&
+        status == cudaDriverEntryPointSuccess) {
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+    }
+  }
+  return fn;
+}
+
+// A 3-D float32 tensor map over an (nx, ny, nz) volume with a (bz, by, 1) box.
+bool make_map(CUtensorMap* map, const void* base, int nx, int ny, int nz, int bz, int by) {
+  auto fn = encode_fn();
+  if (fn == nullptr) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)nz, (cuuint64_t)ny, (cuuint64_t)nx};
+  const cuuint64_t strides[2] = {(cuuint64_t)nz * 4, (cuuint64_t)ny * nz * 4};
+  const cuuint32_t box[3] = {(cuuint32_t)bz, (cuuint32_t)by, 1};
+  const cuuint32_t estride[3] = {1, 1, 1};
+  const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(base), dims,
+                        strides, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// Set up the tile path when the grid allows it (z rows a multiple of 16 bytes, 16-byte
+// aligned volumes) and it is not switched off with MEEPGB_TILES=0.
+void setup_tiles(mgb_sim* sim) {
+  const char* env = getenv("MEEPGB_TILES");
+  if (env != nullptr && env[0] == '0') return;
+  const StepParams& p = sim->step;
+  if (p.nz % 4 != 0) return;
+  for (int q = 0; q < 3; ++q)
+    if (!aligned16(p.E[q]) || !aligned16(p.D[q]) || !aligned16(p.H[q]) || !aligned16(p.inv_eps[q]))
+      return;
+  TileMaps& m = sim->maps;
+  memset(&m, 0, sizeof m);
+  bool ok = true;
+  for (int q = 0; q < 3; ++q) {
+    ok = ok && make_map(&m.E[q], p.E[q], p.nx, p.ny, p.nz, kHaloZ, kHaloY);
+    ok = ok && make_map(&m.Hown[q], p.H[q], p.nx, p.ny, p.nz, kTileZ, kTileY);
+    ok = ok && make_map(&m.Hhalo[q], p.H[q], p.nx, p.ny, p.nz, kHaloZ, kHaloY);
+    ok = ok && make_map(&m.D[q], p.D[q], p.nx, p.ny, p.nz, kTileZ, kTileY);
+  }
+  const bool alias = p.inv_eps[0] == p.inv_eps[1] && p.inv_eps[1] == p.inv_eps[2];
+  m.ninv = alias ? 1 : 3;
+  for (int q = 0; q < m.ninv; ++q) ok = ok && make_map(&m.inv[q], p.inv_eps[q], p.nx, p.ny, p.nz, kTileZ, kTileY);
+  for (int q = 0; q < 3; ++q) m.inv_of[q] = alias ? 0 : q;
+  if (!ok) return;
+  m.stages = 4;
+  const char* st = getenv("MEEPGB_STAGES");
+  if (st != nullptr && atoi(st) >= 2 && atoi(st) <= 8) m.stages = atoi(st);
+  sim->h_smem = (size_t)m.stages * (3 * kBoxHalo + 3 * kBoxOwn) + 8 * m.stages;
+  sim->e_smem = (size_t)m.stages * (3 * kBoxHalo + (3 + m.ninv) * kBoxOwn) + 8 * m.stages;
+  const void* kernels[4] = {(const void*)h_tile<true>, (const void*)h_tile<false>,
+                            (const void*)e_tile<true>, (const void*)e_tile<false>};
+  for (int t = 0; t < 4; ++t) {
+    const size_t bytes = t < 2 ? sim->h_smem : sim->e_smem;
+    if (cudaFuncSetAttribute(kernels[t], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+  }
+  const char* xc = getenv("MEEPGB_TILE_XCHUNK");
+  if (xc != nullptr && atoi(xc) >= 1) sim->tile_xchunk = atoi(xc);
+  sim->tiles = true;
 }
 
 }  // namespace
@@ -546,7 +946,7 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
   }
   const int n[3] = {d.nx, d.ny, d.nz};
   for (int q = 0; q < 3; ++q) {
-    if (d.E[q] == nullptr || d.D[q] == nullptr || d.B[q] == nullptr || d.inv_eps[q] == nullptr) {
+    if (d.E[q] == nullptr || d.D[q] == nullptr || d.H[q] == nullptr || d.inv_eps[q] == nullptr) {
       return fail(MGB_ERR_ARGUMENT, "a primary field or inverse-epsilon pointer is null");
     }
   }
@@ -558,7 +958,7 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
           return fail(MGB_ERR_ARGUMENT, "a PML coefficient vector is null");
     const int uaxis[3] = {2, 0, 1};
     for (int q = 0; q < 3; ++q) {
-      if (!aux_ok(d.H[q], q, n[q], &why, "H", q) || !aux_ok(d.fwH[q], q, n[q], &why, "fwH", q) ||
+      if (!aux_ok(d.B[q], q, n[q], &why, "B", q) || !aux_ok(d.fwH[q], q, n[q], &why, "fwH", q) ||
           !aux_ok(d.fwE[q], q, n[q], &why, "fwE", q) ||
           !aux_ok(d.fuB[q], uaxis[q], n[uaxis[q]], &why, "fuB", q) ||
           !aux_ok(d.fuD[q], uaxis[q], n[uaxis[q]], &why, "fuD", q)) {
@@ -618,8 +1018,8 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
       p.kps[l][a] = d.kps[l][a];
     }
   for (int q = 0; q < 3; ++q) {
-    p.E[q] = d.E[q]; p.D[q] = d.D[q]; p.B[q] = d.B[q]; p.inv_eps[q] = d.inv_eps[q];
-    p.H[q] = d.H[q]; p.fwH[q] = d.fwH[q]; p.fwE[q] = d.fwE[q]; p.fuB[q] = d.fuB[q]; p.fuD[q] = d.fuD[q];
+    p.E[q] = d.E[q]; p.D[q] = d.D[q]; p.H[q] = d.H[q]; p.inv_eps[q] = d.inv_eps[q];
+    p.B[q] = d.B[q]; p.fwH[q] = d.fwH[q]; p.fwE[q] = d.fwE[q]; p.fuB[q] = d.fuB[q]; p.fuD[q] = d.fuD[q];
   }
   p.npoles = d.npoles;
   for (int a = 0; a < 6; ++a) { p.pbox[a] = d.pbox[a]; p.src_box[a] = d.src_box[a]; }
@@ -629,6 +1029,7 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
   p.src_comp = d.src_comp;
   p.src_words = nullptr;
   p.status = d.status;
+  setup_tiles(sim);
   *out = sim;
   return MGB_OK;
 }
@@ -641,6 +1042,7 @@ int mgb_set_launch_shape(mgb_sim* sim, int block_z, int block_y, int xchunk) {
   sim->block_z = block_z;
   sim->block_y = block_y;
   sim->xchunk = xchunk;
+  sim->tile_xchunk = xchunk;
   return MGB_OK;
 }
 
@@ -663,15 +1065,28 @@ int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s) {
   const bool pml = sim->desc.pml_active != 0;
   if (part == 0 || part == 1) {
     if (p.nsrc > 0) p.src_words = sim->words + (n - sim->words_first) * p.nsrc;
+    if (sim->tiles) {
+      const int xc = sim->tile_xchunk;
+      const dim3 grid((p.nz + kTileZ - 1) / kTileZ, (p.ny + kTileY - 1) / kTileY,
+                      (p.nx + xc - 1) / xc);
+      if (part == 0) {
+        if (pml) h_tile<true><<<grid, kThreads, sim->h_smem, s>>>(p, sim->maps, n == 0, xc);
+        else h_tile<false><<<grid, kThreads, sim->h_smem, s>>>(p, sim->maps, n == 0, xc);
+      } else {
+        if (pml) e_tile<true><<<grid, kThreads, sim->e_smem, s>>>(p, sim->maps, (int)(n & 1), xc);
+        else e_tile<false><<<grid, kThreads, sim->e_smem, s>>>(p, sim->maps, (int)(n & 1), xc);
+      }
+      return MGB_OK;
+    }
     const dim3 block(sim->block_z, sim->block_y, 1);
     const dim3 grid((p.nz + block.x - 1) / block.x, (p.ny + block.y - 1) / block.y,
                     (p.nx + sim->xchunk - 1) / sim->xchunk);
     if (part == 0) {
-      if (pml) h_half<true><<<grid, block, 0, s>>>(p, n == 0, sim->xchunk);
-      else h_half<false><<<grid, block, 0, s>>>(p, n == 0, sim->xchunk);
+      if (pml) h_generic<true><<<grid, block, 0, s>>>(p, n == 0, sim->xchunk);
+      else h_generic<false><<<grid, block, 0, s>>>(p, n == 0, sim->xchunk);
     } else {
-      if (pml) e_half<true><<<grid, block, 0, s>>>(p, (int)(n & 1), sim->xchunk);
-      else e_half<false><<<grid, block, 0, s>>>(p, (int)(n & 1), sim->xchunk);
+      if (pml) e_generic<true><<<grid, block, 0, s>>>(p, (int)(n & 1), sim->xchunk);
+      else e_generic<false><<<grid, block, 0, s>>>(p, (int)(n & 1), sim->xchunk);
     }
     return MGB_OK;
   }
@@ -682,15 +1097,13 @@ int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s) {
     DftParams q;
     q.nx = p.nx; q.ny = p.ny; q.nz = p.nz;
     for (int a = 0; a < 3; ++a) q.met[a] = p.met[a];
-    q.pml = pml;
-    for (int c = 0; c < 3; ++c) { q.E[c] = p.E[c]; q.B[c] = p.B[c]; q.H[c] = p.H[c]; }
+    for (int c = 0; c < 3; ++c) { q.E[c] = p.E[c]; q.H[c] = p.H[c]; }
     q.mon = mon;
     const long long cells = (long long)(mon.region[1] - mon.region[0]) *
                             (mon.region[3] - mon.region[2]) * (mon.region[5] - mon.region[4]);
     const unsigned blocks = (unsigned)((cells + 255) / 256);
     const size_t smem = (size_t)mon.nfreq * 2 * sizeof(float2);
-    if (pml) dft_accumulate<true><<<blocks, 256, smem, s>>>(q, post);
-    else dft_accumulate<false><<<blocks, 256, smem, s>>>(q, post);
+    dft_accumulate<<<blocks, 256, smem, s>>>(q, post);
   }
   return MGB_OK;
 }
@@ -750,6 +1163,8 @@ int mgb_flux_spectrum(mgb_sim* sim, int32_t monitor, const float* weights, doubl
   flux_reduce<<<m.nfreq, 256, 0, static_cast<cudaStream_t>(stream)>>>(m, weights, out);
   return launch_error("flux reduction launch");
 }
+
+int mgb_uses_tiles(mgb_sim* sim) { return sim != nullptr && sim->tiles ? 1 : 0; }
 
 void mgb_destroy(mgb_sim* sim) { delete sim; }
 

@@ -4,12 +4,13 @@ The engine allocates every device array (as torch tensors: torch is the allocato
 the stream provider here, nothing more), fills the ``mgb_sim_desc`` the C ABI takes,
 and drives ``mgb_step``. Layout in HBM, all float32 and C-ordered ``(nx, ny, nz)``:
 
-* E, D, B: three full volumes each; one inverse-epsilon volume per distinct array
-  (the isotropic case aliases one volume for all three components);
+* E, D, H: three full volumes each; one inverse-epsilon volume per distinct array
+  (the isotropic case aliases one volume for all three components). Outside each H
+  component's own-axis integer PML runs MEEP's H is B's word, so H carries B there;
 * PML auxiliaries, compact over their membership runs only (one axis shortened to the
-  run length): stored H and its ``f_w`` on each H component's own-axis integer runs
-  (H is B's word everywhere else), ``f_w`` of E on the own-axis half runs, and the
-  split-field ``fu`` of B (half lattice) and D (integer lattice) on the dsigu runs;
+  run length): B and the ``f_w`` of H on each H component's own-axis integer runs,
+  ``f_w`` of E on the own-axis half runs, and the split-field ``fu`` of B (half
+  lattice) and D (integer lattice) on the dsigu runs;
 * polarization: two rotating buffers per pole and driven component, over the bounding
   box of the cells where any pole's sigma is nonzero (P stays zero elsewhere);
 * DFT accumulators ``[ncomp][nfreq][re, im][cells]`` per monitor.
@@ -31,7 +32,7 @@ from .pml import (HALF, INTEGER, PML, aux_shape, constitutive_aux_key, curl_aux_
                   identity_tables, no_pml_records, slab_index)
 from .sources import Source, deposit_words
 
-FIELD_NAMES = ("E", "D", "B")
+FIELD_NAMES = ("E", "D", "H")
 # Source words are uploaded in windows of this many steps.
 SOURCE_WINDOW = 4096
 
@@ -82,7 +83,7 @@ class Engine:
         for q, axis in enumerate("xyz"):
             d.E[q] = self.fields["E" + axis].data_ptr()
             d.D[q] = self.fields["D" + axis].data_ptr()
-            d.B[q] = self.fields["B" + axis].data_ptr()
+            d.H[q] = self.fields["H" + axis].data_ptr()
             d.inv_eps[q] = self.inv_eps[q].data_ptr()
         self.aux: Dict[str, torch.Tensor] = {}
         self.coefficients: Dict[Tuple[str, int, int], torch.Tensor] = {}
@@ -95,7 +96,7 @@ class Engine:
                     getattr(d, name)[lattice][axis] = t.data_ptr()
             self.records = self.pml.records
             for q in range(3):
-                self._aux(d.H, "H", q, constitutive_aux_key("H", q))
+                self._aux(d.B, "B", q, constitutive_aux_key("H", q))
                 self._aux(d.fwH, "fwH", q, constitutive_aux_key("H", q))
                 self._aux(d.fwE, "fwE", q, constitutive_aux_key("E", q))
                 self._aux(d.fuB, "fuB", q, curl_aux_key("B", q))
@@ -265,6 +266,11 @@ class Engine:
                                                    self._stream_handle()))
             done += chunk
 
+    @property
+    def uses_tiles(self) -> bool:
+        """Whether the plan steps with the TMA tile kernels (else the generic ones)."""
+        return bool(self.lib.mgb_uses_tiles(self.handle))
+
     def launch(self, step: int, part: int, stream=None) -> None:
         """Launch one kernel of one step: 0 the H half, 1 the E half, 2 the monitors."""
         if part < 2:
@@ -276,8 +282,8 @@ class Engine:
     def algorithmic_bytes(self) -> Dict[str, int]:
         """Minimum HBM bytes one launch of each step kernel must move.
 
-        H half: read E (3 volumes) and B (3), write B (3); on the PML slabs read and
-        write ``fu`` of B, and read H and ``f_w`` of H and write both.
+        H half: read E (3 volumes) and H (3), write H (3); on the PML slabs read and
+        write ``fu`` of B, and read and write the slab B and ``f_w`` of H.
         E half: read H (3 volumes: the slab word or B's) and D (3) and each distinct
         inverse-epsilon volume, write D (3) and E (3); on the slabs read and write ``fu``
         of D, read and write ``f_w`` of E and read E; per pole and driven component read
@@ -286,7 +292,7 @@ class Engine:
         cells = self.grid.total_cells
         word = 4
         aux = lambda name: sum(int(self.aux[f"{name}{a}"].numel()) for a in "xyz") if self.pml is not None else 0  # noqa: E731
-        h = 9 * cells + 2 * aux("fuB") + 2 * aux("H") + 2 * aux("fwH")
+        h = 9 * cells + 2 * aux("fuB") + 2 * aux("B") + 2 * aux("fwH")
         distinct_inv = len({t.data_ptr() for t in self.inv_eps})
         e = (12 + distinct_inv) * cells + 2 * aux("fuD") + 3 * aux("fwE")
         for kept in getattr(self, "pole_tensors", []):
@@ -300,21 +306,21 @@ class Engine:
     # --- read-out -----------------------------------------------------------------------
     def field(self, name: str) -> torch.Tensor:
         """Device tensor of one component's stored Yee words (H composed from B and slab)."""
-        if name[0] in "EDB":
+        if name[0] in "EDH":
             return self.fields[name]
-        if name[0] == "H":
+        if name[0] == "B":
             q = "xyz".index(name[1])
-            b = self.fields["B" + name[1]]
+            h = self.fields["H" + name[1]]
             if self.pml is None:
-                return b
-            h = b.clone()
+                return h
+            b = h.clone()
             record = self.records[(INTEGER, q)]
             rows = np.flatnonzero(slab_index(record, np.arange(self.grid.shape[q])) >= 0)
             if rows.size:
                 index = [slice(None)] * 3
                 index[q] = torch.from_numpy(rows).to(self.device)
-                h[tuple(index)] = self.aux["H" + name[1]]
-            return h
+                b[tuple(index)] = self.aux["B" + name[1]]
+            return b
         raise ValueError(f"unknown component {name!r}")
 
     def flux_spectrum(self, monitor: FluxMonitor) -> np.ndarray:

@@ -15,16 +15,18 @@ grid's cell centres, as the configurations specify; there is no dataset.
   eps_inf 2.25 and one Lorentz pole (f0 1.1, gamma 0.05, sigma 1.5), 10-cell PML,
   Ez Gaussian (fcen 0.8, df 1.0) at x = -2.4, transmission/reflection planes at x = +-2
   of size 7.6 x 7.6 with 200 frequencies; 10,000 steps.
-* ``sphere128``: a 128^3 sphere case with one flux plane, the size used for detailed
-  profiles (working set above the L2 size, a few hundred MB).
+* ``sphere128``: a 128^3 sphere case with one flux plane.
+* ``sphere192``: the 192^3 sphere case with one 50-frequency flux plane (working set
+  ~0.4 GB, above the L2 size): the case detailed kernel profiles are taken on.
 """
 
 from __future__ import annotations
 
 import numpy as np
 
-WORKLOADS = ("sphere80", "sphere192_8dft", "lorentz192", "sphere128")
-STEPS = {"sphere80": 2000, "sphere192_8dft": 5000, "lorentz192": 10000, "sphere128": 1000}
+WORKLOADS = ("sphere80", "sphere192_8dft", "lorentz192", "sphere128", "sphere192")
+STEPS = {"sphere80": 2000, "sphere192_8dft": 5000, "lorentz192": 10000, "sphere128": 1000,
+         "sphere192": 5000}
 
 
 def build(name: str, driver_cls=None, susceptibility_cls=None, **driver_kwargs):
@@ -32,8 +34,8 @@ def build(name: str, driver_cls=None, susceptibility_cls=None, **driver_kwargs):
         from .driver import FdtdDriver as driver_cls  # noqa: N813
     if susceptibility_cls is None:
         from .dispersion import Susceptibility as susceptibility_cls  # noqa: N813
-    if name in ("sphere80", "sphere192_8dft", "sphere128"):
-        res = {"sphere80": 10, "sphere192_8dft": 24, "sphere128": 16}[name]
+    if name in ("sphere80", "sphere192_8dft", "sphere128", "sphere192"):
+        res = {"sphere80": 10, "sphere192_8dft": 24, "sphere128": 16, "sphere192": 24}[name]
         length = 8.0
         d = driver_cls(cell_size=(length, length, length), resolution=res, courant=0.5,
                        force_complex_fields=False, boundaries="metallic", **driver_kwargs)

@@ -17,6 +17,13 @@ CASES = {
     "periodic_pml": dict(n=(14, 12, 13), pml=3, steps=50, boundaries="periodic"),
     "mixed": dict(n=(13, 15, 12), pml={"x": 3, "y": {"low": 2, "high": 4}, "z": 2.5}, steps=45,
                   mixed=True),
+    # z extents that are multiples of 4 (the shared-memory tile path), with partial tiles
+    # in y and z, a z extent spanning two tiles, and periodic faces in every axis.
+    "tile_periodic_pml": dict(n=(12, 14, 20), pml=3, steps=50, boundaries="periodic"),
+    "tile_lorentz": dict(n=(16, 10, 24), pml=3, steps=50, lorentz=True),
+    "tile_periodic": dict(n=(10, 12, 16), pml=0, steps=40, boundaries="periodic"),
+    "tile_mixed": dict(n=(11, 18, 68), pml={"x": 2, "y": {"low": 3, "high": 2}, "z": 4}, steps=40,
+                       mixed=True),
 }
 
 # The 80^3 sphere-under-PML workload (resolution 10, 10-cell PML, eps 4 sphere of radius

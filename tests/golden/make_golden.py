@@ -131,9 +131,10 @@ def record_tables() -> None:
 
 if __name__ == "__main__":
     which = sys.argv[1:] or ["fields", "digest", "tables"]
-    if "fields" in which:
-        for name, case in CASES.items():
-            record_fields(name, case)
+    if "fields" in which or any(w in CASES for w in which):
+        names = [w for w in which if w in CASES] or list(CASES)
+        for name in names:
+            record_fields(name, CASES[name])
     if "tables" in which:
         record_tables()
     if "digest" in which:

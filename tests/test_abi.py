@@ -52,7 +52,7 @@ int main(void) {
   printf("sizeof.mgb_monitor %zu\n", sizeof(mgb_monitor));
   printf("sizeof.mgb_pole %zu\n", sizeof(mgb_pole));
   printf("sizeof.mgb_aux %zu\n", sizeof(mgb_aux));
-  F(mgb_sim_desc, dtdx) F(mgb_sim_desc, kms) F(mgb_sim_desc, E) F(mgb_sim_desc, H)
+  F(mgb_sim_desc, dtdx) F(mgb_sim_desc, kms) F(mgb_sim_desc, E) F(mgb_sim_desc, H) F(mgb_sim_desc, B)
   F(mgb_sim_desc, fuD) F(mgb_sim_desc, npoles) F(mgb_sim_desc, poles) F(mgb_sim_desc, nsrc)
   F(mgb_sim_desc, src_box) F(mgb_sim_desc, nmonitors) F(mgb_sim_desc, monitors)
   F(mgb_sim_desc, status) F(mgb_monitor, scale) F(mgb_monitor, omega) F(mgb_monitor, acc)

@@ -40,11 +40,16 @@ def gpu_case(case, steps=None, launch_shape=None, chunks=None):
     return driver, flux, dft
 
 
+@pytest.mark.parametrize("mode", ["tiles", "generic"])
 @pytest.mark.parametrize("name", sorted(CASES))
-def test_fields_are_the_reference_words(gpu, name):
+def test_fields_are_the_reference_words(gpu, name, mode, monkeypatch):
+    """Both kernel families: the TMA tile kernels (z extent a multiple of 4) and the
+    generic plain-load kernels (forced with MEEPGB_TILES=0, or any other z extent)."""
     case = CASES[name]
     gold = golden_io.fields(name)
+    monkeypatch.setenv("MEEPGB_TILES", "1" if mode == "tiles" else "0")
     driver, flux, dft = gpu_case(case)
+    assert driver.engine.uses_tiles == (mode == "tiles" and case["n"][2] % 4 == 0)
     for c in FIELDS:
         got = driver.get_field(c, cell_centered=False)
         mismatched = int(np.sum(got != gold[c]))
@@ -68,13 +73,28 @@ def test_fields_are_the_reference_words(gpu, name):
     driver.close()
 
 
-@pytest.mark.parametrize("shape", [(32, 8, 16), (64, 4, 7), (16, 16, 200), (128, 2, 1)])
-def test_launch_shape_does_not_change_a_word(gpu, shape):
-    case = CASES["mixed"]
-    gold = golden_io.fields("mixed")
+@pytest.mark.parametrize("name", ["mixed", "tile_mixed", "tile_periodic_pml"])
+@pytest.mark.parametrize("shape", [(32, 8, 16), (64, 4, 7), (16, 16, 200), (128, 2, 1), (32, 8, 3)])
+def test_launch_shape_does_not_change_a_word(gpu, shape, name):
+    """The x chunk (both families) and block shape (generic family) change no word."""
+    case = CASES[name]
+    gold = golden_io.fields(name)
     driver, _, _ = gpu_case(case, launch_shape=shape)
     for c in FIELDS:
         assert np.array_equal(driver.get_field(c, cell_centered=False), gold[c]), (shape, c)
+    driver.close()
+
+
+@pytest.mark.parametrize("stages", ["2", "3", "6"])
+def test_ring_depth_does_not_change_a_word(gpu, stages, monkeypatch):
+    monkeypatch.setenv("MEEPGB_STAGES", stages)
+    case = CASES["tile_lorentz"]
+    gold = golden_io.fields("tile_lorentz")
+    driver, _, _ = gpu_case(case)
+    assert driver.engine.uses_tiles
+    for c in FIELDS:
+        assert np.array_equal(driver.get_field(c, cell_centered=False), gold[c]), (stages, c)
+    assert driver.engine.status.item() == 0
     driver.close()
 
 
@@ -87,9 +107,12 @@ def test_chunked_runs_equal_one_run(gpu):
     driver.close()
 
 
-def test_sphere80_words_after_200_steps(gpu):
+@pytest.mark.parametrize("mode", ["tiles", "generic"])
+def test_sphere80_words_after_200_steps(gpu, mode, monkeypatch):
     gold = golden_io.digest()
+    monkeypatch.setenv("MEEPGB_TILES", "1" if mode == "tiles" else "0")
     driver, flux, _ = gpu_case(SPHERE80, steps=gold["steps"])
+    assert driver.engine.uses_tiles == (mode == "tiles")
     for c, expected in gold["sha256"].items():
         words = np.ascontiguousarray(driver.get_field(c, cell_centered=False), dtype=np.float32)
         assert hashlib.sha256(words.tobytes()).hexdigest() == expected, c
@@ -122,7 +145,7 @@ def test_nonfinite_detector_raises(gpu):
     from meep_gpu_gb300 import FdtdDivergence
     driver = FdtdDriver((1.2, 1.2, 1.2), 10, force_complex_fields=False, boundaries="metallic")
     driver.add_source({"source_type": "continuous", "component": "Ez", "center": (0, 0, 0),
-                       "size": (0, 0, 0), "frequency": 0.5, "amplitude": 1e36})
+                       "size": (0, 0, 0), "frequency": 0.5, "amplitude": 1e40})
     with pytest.raises(FdtdDivergence):
         driver.run(num_steps=40, progress_interval=10)
     driver.close()

@@ -51,8 +51,10 @@ enum {
   MGB_ERR_RANGE = -4        /* a step outside the uploaded source-word table */
 };
 
-/* One compact auxiliary array (PML): stored only over the rows of `axis` that lie in
- * the membership runs [a0, a1) U [b0, b1); the other two axes are full length. */
+/* One PML auxiliary array: a full (nx, ny, nz) volume of which only the cells whose
+ * coordinate along `axis` lies in the membership runs [a0, a1) U [b0, b1) are ever read
+ * or written (the rest is never touched, so it moves no bytes); full-volume storage
+ * keeps its index the cell's own linear index. */
 typedef struct mgb_aux {
   float* data; /* device; NULL when the run has no PML */
   int32_t axis;
@@ -100,9 +102,9 @@ typedef struct mgb_sim_desc {
   float* D[3];
   float* H[3];
   const float* inv_eps[3]; /* may alias one another */
-  /* PML auxiliaries: B and f_w of H on each H component's own-axis integer slab, f_w of
-   * E on the own-axis half slab, and the curl split-field fu of B (half lattice) and D
-   * (integer lattice) on the dsigu slab. */
+  /* PML auxiliaries: B and f_w of H on each H component's own-axis integer membership,
+   * f_w of E on the own-axis half membership, and the curl split-field fu of B (half
+   * lattice) and D (integer lattice) on the dsigu membership. */
   mgb_aux B[3];
   mgb_aux fwH[3];
   mgb_aux fwE[3];
@@ -134,6 +136,9 @@ int mgb_abi_version(void);
 /* Validate a descriptor and make a plan from a copy of it. Replaces plan_fast_path
  * (meep_gpu/fastpath.py:6986); refusals return MGB_ERR_UNSUPPORTED with the reason. */
 int mgb_create(const mgb_sim_desc* desc, mgb_sim** out);
+
+/* Largest grid the kernels index (32-bit cell offsets): nx * ny * nz < 2^31. */
+#define MGB_MAX_CELLS 2147483647LL
 
 /* Launch shape of the step kernels: a (block_z x block_y) tile of (z, y) columns per CTA
  * marching over x_chunk planes of x. No reference counterpart: the reference launches a

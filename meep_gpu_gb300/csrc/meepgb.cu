@@ -26,8 +26,8 @@
 //     chunk of x planes. One thread issues TMA bulk-tensor loads (cp.async.bulk.tensor)
 //     of each plane's tiles (the stencil operand with its one-cell halo, the cell's own
 //     fields) into a ring of shared-memory stages guarded by mbarriers, several planes
-//     ahead of the 256 threads computing from shared memory; the x neighbour is the
-//     previous (or next) stage of the ring. Waits are bounded: a wait that outlives its
+//     ahead of the 512 threads (one per tile cell) computing from shared memory; the x
+//     neighbour is the previous (or next) stage of the ring. Waits are bounded: a wait that outlives its
 //     limit sets status bit 2 and the CTA stops stepping.
 //   generic kernels (h_generic, e_generic): one thread per (y, z) column marching over
 //     x with plain loads, for grids whose z extent is not a multiple of 4 (TMA needs
@@ -59,7 +59,7 @@ constexpr int kTileZ = 64;          // cells per tile along z (innermost)
 constexpr int kTileY = 8;           // cells per tile along y
 constexpr int kHaloZ = kTileZ + 4;  // z extent of a halo box (16-byte multiple)
 constexpr int kHaloY = kTileY + 1;
-constexpr int kThreads = 256;
+constexpr int kThreads = 512;         // one thread per tile cell
 constexpr int kBoxHalo = 2560;      // bytes of one halo box buffer (68 x 9 floats, 128-aligned)
 constexpr int kBoxOwn = kTileZ * kTileY * 4;  // 2048 bytes
 
@@ -107,56 +107,72 @@ struct DftParams {
   mgb_monitor mon;
 };
 
-__device__ __forceinline__ int slab_row(const mgb_aux& a, int i) {
-  if (i >= a.a0 && i < a.a1) return i - a.a0;
-  if (i >= a.b0 && i < a.b1) return (a.a1 - a.a0) + (i - a.b0);
-  return -1;
+__device__ __forceinline__ bool in_runs(const mgb_aux& a, int x) {
+  return (x >= a.a0 && x < a.a1) || (x >= a.b0 && x < a.b1);
 }
 
-template <int AXIS>
-__device__ __forceinline__ long long aux_index(const mgb_aux& a, int row, int i, int j, int k,
-                                               int ny, int nz) {
-  const int m = (a.a1 - a.a0) + (a.b1 - a.b0);
-  if (AXIS == 0) return ((long long)row * ny + j) * nz + k;
-  if (AXIS == 1) return ((long long)i * m + row) * nz + k;
-  return ((long long)i * ny + j) * m + row;
+__device__ __forceinline__ float ldgf(const float* base, int at) { return __ldg(base + at); }
+
+// ---- per-cell updates ----------------------------------------------------------------
+//
+// Component q's curl update uses the split-field recurrence where its dsigu membership
+// holds (dsig = axis q+1, dsigu = axis q+2, MEEP's cycle X -> Y -> Z):
+//   fu' = ((kms*fu) - curl)*sinv;  f' = (((kms_u*f) + fu') - fu)*sinv_u
+// and f' = ((kms*f) - curl)*sinv elsewhere. The constitutive accumulation on the own-
+// axis membership is f_w' = src, f' = f + ((kps*src) - (kms*f_w)).
+//
+// Every PML coefficient outside its membership is exactly 1 (checked when the tables are
+// built), so a cell outside all six memberships steps f - curl and H = B: the same
+// words. A warp takes that fast path when none of its lanes is in a membership (the
+// lanes of a warp share y and the plane, so only the z lanes can differ).
+//
+// Coefficients and membership flags depend on one coordinate each. A thread keeps y and
+// z fixed while it marches over x, so everything indexed by j or k is formed once per
+// thread (a "column") and everything indexed by i once per plane.
+
+// H half: B lives on the half lattice transversally (curl tables), H on the integer
+// lattice of its own axis (constitutive tables).
+struct HColumn {
+  bool f0, f2, b1, b2;                  // fuB[0] (z), fuB[2] (y), B[1] (y), B[2] (z)
+  float kms_yh, sinv_yh, kps_y, kms_y;  // j-indexed
+  float kms_zh, sinv_zh, kps_z, kms_z;  // k-indexed
+};
+struct HPlane {
+  bool f1, b0;                          // fuB[1] (x), B[0] (x)
+  float kms_xh, sinv_xh, kps_x, kms_x;
+};
+
+__device__ __forceinline__ HColumn h_column(const StepParams& p, int j, int k) {
+  HColumn c;
+  c.f0 = in_runs(p.fuB[0], k); c.f2 = in_runs(p.fuB[2], j);
+  c.b1 = in_runs(p.B[1], j); c.b2 = in_runs(p.B[2], k);
+  c.kms_yh = ldgf(p.kms[kHalf][1], j); c.sinv_yh = ldgf(p.sinv[kHalf][1], j);
+  c.kps_y = ldgf(p.kps[kInteger][1], j); c.kms_y = ldgf(p.kms[kInteger][1], j);
+  c.kms_zh = ldgf(p.kms[kHalf][2], k); c.sinv_zh = ldgf(p.sinv[kHalf][2], k);
+  c.kps_z = ldgf(p.kps[kInteger][2], k); c.kms_z = ldgf(p.kms[kInteger][2], k);
+  return c;
 }
 
-// The split-field curl update of one B/D component (MEEP step_curl, both forms).
-//   inside the dsigu membership: fu' = ((kms*fu) - curl)*sinv;
-//                                f'  = (((kms_u*f) + fu') - fu)*sinv_u
-//   elsewhere:                   f'  = ((kms*f) - curl)*sinv
-template <int UAXIS>
-__device__ __forceinline__ float curl_update(const StepParams& p, int lattice, int sig_axis,
-                                             const mgb_aux& fu, float f, float curl, int i,
-                                             int j, int k) {
-  const int sig_at = sig_axis == 0 ? i : (sig_axis == 1 ? j : k);
-  const int u_at = UAXIS == 0 ? i : (UAXIS == 1 ? j : k);
-  const float kms = __ldg(p.kms[lattice][sig_axis] + sig_at);
-  const float sinv = __ldg(p.sinv[lattice][sig_axis] + sig_at);
-  const int row = slab_row(fu, u_at);
-  if (row >= 0) {
-    const long long a = aux_index<UAXIS>(fu, row, i, j, k, p.ny, p.nz);
-    const float prev = fu.data[a];
-    const float next = (kms * prev - curl) * sinv;
-    fu.data[a] = next;
-    const float kms_u = __ldg(p.kms[lattice][UAXIS] + u_at);
-    const float sinv_u = __ldg(p.sinv[lattice][UAXIS] + u_at);
-    return ((kms_u * f + next) - prev) * sinv_u;
-  }
-  return (kms * f - curl) * sinv;
+__device__ __forceinline__ HPlane h_plane(const StepParams& p, int i) {
+  HPlane c;
+  c.f1 = in_runs(p.fuB[1], i); c.b0 = in_runs(p.B[0], i);
+  c.kms_xh = ldgf(p.kms[kHalf][0], i); c.sinv_xh = ldgf(p.sinv[kHalf][0], i);
+  c.kps_x = ldgf(p.kps[kInteger][0], i); c.kms_x = ldgf(p.kms[kInteger][0], i);
+  return c;
 }
 
-// B update of one cell from its curls, zero_metal_B, and H from B (update_H). `h_old`
-// is the stored H word, which is the old B outside the own-axis membership.
+// B from its curls, zero_metal_B, H from B (update_H) for one cell at offset c, and the
+// auxiliary stores. `h_old` is the stored H word (the old B outside the own-axis
+// membership). `slow` selects the PML arithmetic.
 template <bool PML>
-__device__ __forceinline__ void b_and_h(const StepParams& p, int first_step, int i, int j, int k,
-                                        float cx, float cy, float cz, const float h_old[3],
-                                        float h_new[3]) {
+__device__ __forceinline__ void h_cell(const StepParams& p, const HColumn& col, const HPlane& pl,
+                                       bool slow, int first_step, int i, int j, int k, int c,
+                                       float cx, float cy, float cz, const float h_old[3],
+                                       float h_new[3]) {
   if (p.met[0] && i == 0) cx = 0.f;
   if (p.met[1] && j == 0) cy = 0.f;
   if (p.met[2] && k == 0) cz = 0.f;
-  if (!PML) {
+  if (!PML || !slow) {
     h_new[0] = h_old[0] - cx;
     h_new[1] = h_old[1] - cy;
     h_new[2] = h_old[2] - cz;
@@ -165,52 +181,106 @@ __device__ __forceinline__ void b_and_h(const StepParams& p, int first_step, int
     if (p.met[2] && k == 0) h_new[2] = 0.f;
     return;
   }
-  const int at[3] = {i, j, k};
-  const float curls[3] = {cx, cy, cz};
-#pragma unroll
-  for (int q = 0; q < 3; ++q) {
-    const int row = slab_row(p.B[q], at[q]);
-    long long a = 0;
-    if (row >= 0) {
-      if (q == 0) a = aux_index<0>(p.B[0], row, i, j, k, p.ny, p.nz);
-      else if (q == 1) a = aux_index<1>(p.B[1], row, i, j, k, p.ny, p.nz);
-      else a = aux_index<2>(p.B[2], row, i, j, k, p.ny, p.nz);
-    }
-    float b = row >= 0 ? p.B[q].data[a] : h_old[q];
-    // Bx: dsig y, dsigu z; By: dsig z, dsigu x; Bz: dsig x, dsigu y (half lattice).
-    if (q == 0) b = curl_update<2>(p, kHalf, 1, p.fuB[0], b, curls[0], i, j, k);
-    else if (q == 1) b = curl_update<0>(p, kHalf, 2, p.fuB[1], b, curls[1], i, j, k);
-    else b = curl_update<1>(p, kHalf, 0, p.fuB[2], b, curls[2], i, j, k);
-    if (p.met[q] && at[q] == 0) b = 0.f;  // zero_metal_B: shift 0 only on its own axis
-    if (row >= 0) {
-      // update_H on the own-axis integer membership: fw' = B, H' = H + ((kps*B) - (kms*fw)).
-      const float fw_prev = first_step ? b : p.fwH[q].data[a];
-      const float h_prev = first_step ? b : h_old[q];
-      const float kps = __ldg(p.kps[kInteger][q] + at[q]);
-      const float kms = __ldg(p.kms[kInteger][q] + at[q]);
-      p.B[q].data[a] = b;
-      p.fwH[q].data[a] = b;
-      h_new[q] = h_prev + (kps * b - kms * fw_prev);
-    } else {
-      h_new[q] = b;
-    }
-  }
+  const bool sb0 = pl.b0, sb1 = col.b1, sb2 = col.b2;
+  const bool sf0 = col.f0, sf1 = pl.f1, sf2 = col.f2;
+  // Loads: every auxiliary word of the cell, before any store.
+  float b0 = sb0 ? p.B[0].data[c] : h_old[0];
+  float b1 = sb1 ? p.B[1].data[c] : h_old[1];
+  float b2 = sb2 ? p.B[2].data[c] : h_old[2];
+  const float w0 = sb0 ? p.fwH[0].data[c] : 0.f;
+  const float w1 = sb1 ? p.fwH[1].data[c] : 0.f;
+  const float w2 = sb2 ? p.fwH[2].data[c] : 0.f;
+  const float u0 = sf0 ? p.fuB[0].data[c] : 0.f;
+  const float u1 = sf1 ? p.fuB[1].data[c] : 0.f;
+  const float u2 = sf2 ? p.fuB[2].data[c] : 0.f;
+  // Bx: dsig y, dsigu z; By: dsig z, dsigu x; Bz: dsig x, dsigu y.
+  float n0 = 0.f, n1 = 0.f, n2 = 0.f;
+  if (sf0) { n0 = (col.kms_yh * u0 - cx) * col.sinv_yh; b0 = ((col.kms_zh * b0 + n0) - u0) * col.sinv_zh; }
+  else b0 = (col.kms_yh * b0 - cx) * col.sinv_yh;
+  if (sf1) { n1 = (col.kms_zh * u1 - cy) * col.sinv_zh; b1 = ((pl.kms_xh * b1 + n1) - u1) * pl.sinv_xh; }
+  else b1 = (col.kms_zh * b1 - cy) * col.sinv_zh;
+  if (sf2) { n2 = (pl.kms_xh * u2 - cz) * pl.sinv_xh; b2 = ((col.kms_yh * b2 + n2) - u2) * col.sinv_yh; }
+  else b2 = (pl.kms_xh * b2 - cz) * pl.sinv_xh;
+  // zero_metal_B: each component sits on the wall of its own axis.
+  if (p.met[0] && i == 0) b0 = 0.f;
+  if (p.met[1] && j == 0) b1 = 0.f;
+  if (p.met[2] && k == 0) b2 = 0.f;
+  // update_H on the own-axis integer membership (MEEP starts H and f_w from B once).
+  h_new[0] = sb0 ? (first_step ? b0 : h_old[0]) + (pl.kps_x * b0 - pl.kms_x * (first_step ? b0 : w0)) : b0;
+  h_new[1] = sb1 ? (first_step ? b1 : h_old[1]) + (col.kps_y * b1 - col.kms_y * (first_step ? b1 : w1)) : b1;
+  h_new[2] = sb2 ? (first_step ? b2 : h_old[2]) + (col.kps_z * b2 - col.kms_z * (first_step ? b2 : w2)) : b2;
+  if (sf0) p.fuB[0].data[c] = n0;
+  if (sf1) p.fuB[1].data[c] = n1;
+  if (sf2) p.fuB[2].data[c] = n2;
+  if (sb0) { p.B[0].data[c] = b0; p.fwH[0].data[c] = b0; }
+  if (sb1) { p.B[1].data[c] = b1; p.fwH[1].data[c] = b1; }
+  if (sb2) { p.B[2].data[c] = b2; p.fwH[2].data[c] = b2; }
 }
 
-// D update of one cell from its curls, the source deposit, zero_metal_D, E and P.
+// E half: D lives on the integer lattice transversally (curl tables), E on the half
+// lattice of its own axis (constitutive tables).
+struct EColumn {
+  bool f0, f2, w1, w2;                  // fuD[0] (z), fuD[2] (y), fwE[1] (y), fwE[2] (z)
+  float kms_y, sinv_y, kps_yh, kms_yh;  // j-indexed
+  float kms_z, sinv_z, kps_zh, kms_zh;  // k-indexed
+};
+struct EPlane {
+  bool f1, w0;                          // fuD[1] (x), fwE[0] (x)
+  float kms_x, sinv_x, kps_xh, kms_xh;
+};
+
+__device__ __forceinline__ EColumn e_column(const StepParams& p, int j, int k) {
+  EColumn c;
+  c.f0 = in_runs(p.fuD[0], k); c.f2 = in_runs(p.fuD[2], j);
+  c.w1 = in_runs(p.fwE[1], j); c.w2 = in_runs(p.fwE[2], k);
+  c.kms_y = ldgf(p.kms[kInteger][1], j); c.sinv_y = ldgf(p.sinv[kInteger][1], j);
+  c.kps_yh = ldgf(p.kps[kHalf][1], j); c.kms_yh = ldgf(p.kms[kHalf][1], j);
+  c.kms_z = ldgf(p.kms[kInteger][2], k); c.sinv_z = ldgf(p.sinv[kInteger][2], k);
+  c.kps_zh = ldgf(p.kps[kHalf][2], k); c.kms_zh = ldgf(p.kms[kHalf][2], k);
+  return c;
+}
+
+__device__ __forceinline__ EPlane e_plane(const StepParams& p, int i) {
+  EPlane c;
+  c.f1 = in_runs(p.fuD[1], i); c.w0 = in_runs(p.fwE[0], i);
+  c.kms_x = ldgf(p.kms[kInteger][0], i); c.sinv_x = ldgf(p.sinv[kInteger][0], i);
+  c.kps_xh = ldgf(p.kps[kHalf][0], i); c.kms_xh = ldgf(p.kms[kHalf][0], i);
+  return c;
+}
+
+// D from its curls, the source deposit, zero_metal_D, E (update_E) and P (update_P)
+// for one cell at offset c. `slow` selects the PML arithmetic.
 template <bool PML>
-__device__ __forceinline__ void d_e_p(const StepParams& p, int parity, int i, int j, int k,
-                                      long long c, float cx, float cy, float cz, float d[3],
-                                      const float inv[3]) {
+__device__ __forceinline__ void e_cell(const StepParams& p, const EColumn& col, const EPlane& pl,
+                                       bool slow, int parity, int i, int j, int k, int c,
+                                       float cx, float cy, float cz, float d[3], const float inv[3]) {
   const bool wx = p.met[0] && i == 0, wy = p.met[1] && j == 0, wz = p.met[2] && k == 0;
   if (wy || wz) cx = 0.f;
   if (wx || wz) cy = 0.f;
   if (wx || wy) cz = 0.f;
-  if (PML) {
-    // Dx: dsig y, dsigu z; Dy: dsig z, dsigu x; Dz: dsig x, dsigu y (integer lattice).
-    d[0] = curl_update<2>(p, kInteger, 1, p.fuD[0], d[0], cx, i, j, k);
-    d[1] = curl_update<0>(p, kInteger, 2, p.fuD[1], d[1], cy, i, j, k);
-    d[2] = curl_update<1>(p, kInteger, 0, p.fuD[2], d[2], cz, i, j, k);
+  bool sf0 = false, sf1 = false, sf2 = false, sw0 = false, sw1 = false, sw2 = false;
+  float fw0 = 0.f, fw1 = 0.f, fw2 = 0.f, e0 = 0.f, e1 = 0.f, e2 = 0.f;
+  float n0 = 0.f, n1 = 0.f, n2 = 0.f;
+  if (PML && slow) {
+    sf0 = col.f0; sf1 = pl.f1; sf2 = col.f2;
+    sw0 = pl.w0; sw1 = col.w1; sw2 = col.w2;
+    // Loads: every auxiliary word of the cell, before any store.
+    const float u0 = sf0 ? p.fuD[0].data[c] : 0.f;
+    const float u1 = sf1 ? p.fuD[1].data[c] : 0.f;
+    const float u2 = sf2 ? p.fuD[2].data[c] : 0.f;
+    fw0 = sw0 ? p.fwE[0].data[c] : 0.f;
+    fw1 = sw1 ? p.fwE[1].data[c] : 0.f;
+    fw2 = sw2 ? p.fwE[2].data[c] : 0.f;
+    e0 = sw0 ? p.E[0][c] : 0.f;
+    e1 = sw1 ? p.E[1][c] : 0.f;
+    e2 = sw2 ? p.E[2][c] : 0.f;
+    // Dx: dsig y, dsigu z; Dy: dsig z, dsigu x; Dz: dsig x, dsigu y.
+    if (sf0) { n0 = (col.kms_y * u0 - cx) * col.sinv_y; d[0] = ((col.kms_z * d[0] + n0) - u0) * col.sinv_z; }
+    else d[0] = (col.kms_y * d[0] - cx) * col.sinv_y;
+    if (sf1) { n1 = (col.kms_z * u1 - cy) * col.sinv_z; d[1] = ((pl.kms_x * d[1] + n1) - u1) * pl.sinv_x; }
+    else d[1] = (col.kms_z * d[1] - cy) * col.sinv_z;
+    if (sf2) { n2 = (pl.kms_x * u2 - cz) * pl.sinv_x; d[2] = ((col.kms_y * d[2] + n2) - u2) * col.sinv_y; }
+    else d[2] = (pl.kms_x * d[2] - cz) * pl.sinv_x;
   } else {
     d[0] = d[0] - cx;
     d[1] = d[1] - cy;
@@ -222,66 +292,65 @@ __device__ __forceinline__ void d_e_p(const StepParams& p, int parity, int i, in
     for (int s = 0; s < p.nsrc; ++s) {
       if (p.src_cell[s] != c) continue;
       const int q = p.src_comp[s];
-      const double a = p.src_words[s];
-      if (q == 0) d[0] = __double2float_rn(__dsub_rn((double)d[0], a));
-      else if (q == 1) d[1] = __double2float_rn(__dsub_rn((double)d[1], a));
-      else d[2] = __double2float_rn(__dsub_rn((double)d[2], a));
+      const double w = p.src_words[s];
+      if (q == 0) d[0] = __double2float_rn(__dsub_rn((double)d[0], w));
+      else if (q == 1) d[1] = __double2float_rn(__dsub_rn((double)d[1], w));
+      else d[2] = __double2float_rn(__dsub_rn((double)d[2], w));
     }
   }
   // zero_metal_D: shift 0 on both transverse axes.
   if (wy || wz) d[0] = 0.f;
   if (wx || wz) d[1] = 0.f;
   if (wx || wy) d[2] = 0.f;
-  p.D[0][c] = d[0];
-  p.D[1][c] = d[1];
-  p.D[2][c] = d[2];
   const bool in_box = p.npoles > 0 && i >= p.pbox[0] && i < p.pbox[1] && j >= p.pbox[2] &&
                       j < p.pbox[3] && k >= p.pbox[4] && k < p.pbox[5];
   long long pb = 0;
+  float w[3] = {d[0], d[1], d[2]};
   if (in_box) {
     const int bny = p.pbox[3] - p.pbox[2], bnz = p.pbox[5] - p.pbox[4];
     pb = ((long long)(i - p.pbox[0]) * bny + (j - p.pbox[2])) * bnz + (k - p.pbox[4]);
-  }
-  const int at[3] = {i, j, k};
-  bool bad = false;
+    for (int m = 0; m < p.npoles; ++m) {
+      const mgb_pole& pole = p.poles[m];
 #pragma unroll
-  for (int q = 0; q < 3; ++q) {
-    float dmp = d[q];
-    if (in_box) {
-      for (int m = 0; m < p.npoles; ++m) {
-        const mgb_pole& pole = p.poles[m];
-        if (pole.sigma[q] != nullptr) dmp = dmp - (parity ? pole.p[q][1] : pole.p[q][0])[pb];
-      }
+      for (int q = 0; q < 3; ++q)
+        if (pole.sigma[q] != nullptr) w[q] = w[q] - (parity ? pole.p[q][1] : pole.p[q][0])[pb];
     }
-    const float w = inv[q] * dmp;
-    float e = w;
-    if (PML) {
-      const int row = slab_row(p.fwE[q], at[q]);
-      if (row >= 0) {
-        long long a;
-        if (q == 0) a = aux_index<0>(p.fwE[0], row, i, j, k, p.ny, p.nz);
-        else if (q == 1) a = aux_index<1>(p.fwE[1], row, i, j, k, p.ny, p.nz);
-        else a = aux_index<2>(p.fwE[2], row, i, j, k, p.ny, p.nz);
-        const float fw_prev = p.fwE[q].data[a];
-        p.fwE[q].data[a] = w;
-        const float kps = __ldg(p.kps[kHalf][q] + at[q]);
-        const float kms = __ldg(p.kms[kHalf][q] + at[q]);
-        e = p.E[q][c] + (kps * w - kms * fw_prev);
-      }
-    }
-    p.E[q][c] = e;
-    bad |= !isfinite(e);
-    if (in_box) {
-      // update_P: P' = g1inv*(((P*A) - (g1*Pp)) + (w0dt2*(s*W))), written over Pp.
-      for (int m = 0; m < p.npoles; ++m) {
-        const mgb_pole& pole = p.poles[m];
+  }
+  w[0] = inv[0] * w[0];
+  w[1] = inv[1] * w[1];
+  w[2] = inv[2] * w[2];
+  float e[3] = {w[0], w[1], w[2]};
+  if (PML && slow) {
+    if (sw0) e[0] = e0 + (pl.kps_xh * w[0] - pl.kms_xh * fw0);
+    if (sw1) e[1] = e1 + (col.kps_yh * w[1] - col.kms_yh * fw1);
+    if (sw2) e[2] = e2 + (col.kps_zh * w[2] - col.kms_zh * fw2);
+    if (sf0) p.fuD[0].data[c] = n0;
+    if (sf1) p.fuD[1].data[c] = n1;
+    if (sf2) p.fuD[2].data[c] = n2;
+    if (sw0) p.fwE[0].data[c] = w[0];
+    if (sw1) p.fwE[1].data[c] = w[1];
+    if (sw2) p.fwE[2].data[c] = w[2];
+  }
+  p.D[0][c] = d[0];
+  p.D[1][c] = d[1];
+  p.D[2][c] = d[2];
+  p.E[0][c] = e[0];
+  p.E[1][c] = e[1];
+  p.E[2][c] = e[2];
+  const bool bad = !isfinite(e[0]) || !isfinite(e[1]) || !isfinite(e[2]);
+  if (in_box) {
+    // update_P: P' = g1inv*(((P*A) - (g1*Pp)) + (w0dt2*(s*W))), written over Pp.
+    for (int m = 0; m < p.npoles; ++m) {
+      const mgb_pole& pole = p.poles[m];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
         if (pole.sigma[q] == nullptr) continue;
         const float* cur = parity ? pole.p[q][1] : pole.p[q][0];
         float* prv = parity ? pole.p[q][0] : pole.p[q][1];
         const float pc = cur[pb];
         const float pp = prv[pb];
         const float s = __ldg(pole.sigma[q] + pb);
-        const float drive = pole.omega0dtsqr * (s * w);
+        const float drive = pole.omega0dtsqr * (s * w[q]);
         prv[pb] = pole.gamma1inv * ((pc * pole.two_minus_od - pole.gamma1 * pp) + drive);
       }
     }
@@ -299,18 +368,24 @@ __global__ void __launch_bounds__(256) h_generic(const __grid_constant__ StepPar
   if (k >= p.nz || j >= p.ny) return;
   const int i0 = blockIdx.z * xchunk;
   const int i1 = min(i0 + xchunk, p.nx);
-  const long long sx = (long long)p.ny * p.nz;
-  const long long sy = p.nz;
+  const int sx = p.ny * p.nz;
+  const int sy = p.nz;
   const float* Ex = p.E[0];
   const float* Ey = p.E[1];
   const float* Ez = p.E[2];
   const float dtdx = p.dtdx;
   const bool ytop = (j + 1 == p.ny), ztop = (k + 1 == p.nz);
   const bool ywall = ytop && p.met[1], zwall = ztop && p.met[2];
-  const long long oy = ytop ? -(long long)(p.ny - 1) * sy : sy;
-  const long long oz = ztop ? -(long long)(p.nz - 1) : 1;
-  const long long col = (long long)j * sy + k;
-  long long c = (long long)i0 * sx + col;
+  const int oy = ytop ? -(p.ny - 1) * sy : sy;
+  const int oz = ztop ? -(p.nz - 1) : 1;
+  const int col = j * sy + k;
+  int c = i0 * sx + col;
+  HColumn hcol = {};
+  bool warp_slow = false;
+  if (PML) {
+    hcol = h_column(p, j, k);
+    warp_slow = __any_sync(__activemask(), hcol.f0 || hcol.f2 || hcol.b1 || hcol.b2);
+  }
   float ey = Ey[c];
   float ez = Ez[c];
   for (int i = i0; i < i1; ++i, c += sx) {
@@ -336,7 +411,13 @@ __global__ void __launch_bounds__(256) h_generic(const __grid_constant__ StepPar
     const float cz = dtdx * (((ey_xp - ey) + ex) - ex_yp);
     const float h_old[3] = {p.H[0][c], p.H[1][c], p.H[2][c]};
     float h_new[3];
-    b_and_h<PML>(p, first_step, i, j, k, cx, cy, cz, h_old, h_new);
+    HPlane pl = {};
+    bool slow = false;
+    if (PML) {
+      pl = h_plane(p, i);
+      slow = warp_slow || pl.f1 || pl.b0;
+    }
+    h_cell<PML>(p, hcol, pl, slow, first_step, i, j, k, c, cx, cy, cz, h_old, h_new);
     p.H[0][c] = h_new[0];
     p.H[1][c] = h_new[1];
     p.H[2][c] = h_new[2];
@@ -353,35 +434,41 @@ __global__ void __launch_bounds__(256) e_generic(const __grid_constant__ StepPar
   if (k >= p.nz || j >= p.ny) return;
   const int i0 = blockIdx.z * xchunk;
   const int i1 = min(i0 + xchunk, p.nx);
-  const long long sx = (long long)p.ny * p.nz;
-  const long long sy = p.nz;
+  const int sx = p.ny * p.nz;
+  const int sy = p.nz;
   const float dtdx = p.dtdx;
   const float* Hx = p.H[0];
   const float* Hy = p.H[1];
   const float* Hz = p.H[2];
   const int jm = j == 0 ? (p.met[1] ? -1 : p.ny - 1) : j - 1;
   const int km = k == 0 ? (p.met[2] ? -1 : p.nz - 1) : k - 1;
-  const long long col = (long long)j * sy + k;
-  long long c = (long long)i0 * sx + col;
+  const int col = j * sy + k;
+  int c = i0 * sx + col;
+  EColumn ecol = {};
+  bool warp_slow = false;
+  if (PML) {
+    ecol = e_column(p, j, k);
+    warp_slow = __any_sync(__activemask(), ecol.f0 || ecol.f2 || ecol.w1 || ecol.w2);
+  }
   float hy_xm = 0.f, hz_xm = 0.f;
   {
     int im = i0 - 1;
     if (im < 0) im = p.met[0] ? -1 : p.nx - 1;
     if (im >= 0) {
-      hy_xm = Hy[(long long)im * sx + col];
-      hz_xm = Hz[(long long)im * sx + col];
+      hy_xm = Hy[im * sx + col];
+      hz_xm = Hz[im * sx + col];
     }
   }
   for (int i = i0; i < i1; ++i, c += sx) {
     const float hx = Hx[c], hy = Hy[c], hz = Hz[c];
     float hz_ym = 0.f, hx_ym = 0.f, hy_zm = 0.f, hx_zm = 0.f;
     if (jm >= 0) {
-      const long long cm = (long long)i * sx + (long long)jm * sy + k;
+      const int cm = i * sx + jm * sy + k;
       hz_ym = Hz[cm];
       hx_ym = Hx[cm];
     }
     if (km >= 0) {
-      const long long cm = (long long)i * sx + (long long)j * sy + km;
+      const int cm = i * sx + j * sy + km;
       hy_zm = Hy[cm];
       hx_zm = Hx[cm];
     }
@@ -390,7 +477,13 @@ __global__ void __launch_bounds__(256) e_generic(const __grid_constant__ StepPar
     const float cz = dtdx * (((hy_xm - hy) + hx) - hx_ym);
     float d[3] = {p.D[0][c], p.D[1][c], p.D[2][c]};
     const float inv[3] = {__ldg(p.inv_eps[0] + c), __ldg(p.inv_eps[1] + c), __ldg(p.inv_eps[2] + c)};
-    d_e_p<PML>(p, parity, i, j, k, c, cx, cy, cz, d, inv);
+    EPlane pl = {};
+    bool slow = false;
+    if (PML) {
+      pl = e_plane(p, i);
+      slow = warp_slow || pl.f1 || pl.w0;
+    }
+    e_cell<PML>(p, ecol, pl, slow, parity, i, j, k, c, cx, cy, cz, d, inv);
     hy_xm = hy;
     hz_xm = hz;
   }
@@ -458,17 +551,31 @@ __device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* map,
       : "memory");
 }
 
+// After an aborted wait: thread 0 lets this CTA's copies still in flight land (each
+// wait bounded) before the CTA exits and its shared memory is reused.
+__device__ __noinline__ void drain_copies(unsigned long long* full, int S, int from, int issued,
+                                          int tid) {
+  if (tid != 0) return;
+  for (int c = from; c < issued; ++c) mbar_wait(&full[c % S], (unsigned)((c / S) & 1));
+}
+
 // ------------------------------------------------------------------------------------
-// Tile kernels.
+// Tile kernels. Per plane: every thread waits (bounded) for the plane's stage, computes
+// its cell from shared memory, and the CTA meets at one barrier, after which thread 0
+// refills the stage the CTA has finished with. A wait that times out makes its thread
+// skip the cell and raise the shared abort flag, which every thread reads after the
+// barrier, so the whole CTA leaves together.
 //
 // H half. Ring stage of chain index c (plane i0 + c): the E box (68 x 9, z from k0 and
 // y from j0, so the +1 halo of the forward differences) and, for planes below i1, the
 // cell's own H box. Plane i1 (the chunk's x neighbour above) carries E only; past the
 // high x face it is the zero fill of a metallic wall or plane 0 of a periodic axis.
+// Past the high y or z face of a periodic axis the halo is row or column 0, which the
+// box does not hold: those cells read it from global memory.
 template <bool PML>
-__global__ void __launch_bounds__(kThreads) h_tile(const __grid_constant__ StepParams p,
-                                                  const __grid_constant__ TileMaps maps,
-                                                  int first_step, int xchunk) {
+__global__ void __launch_bounds__(kThreads, 2) h_tile(const __grid_constant__ StepParams p,
+                                                     const __grid_constant__ TileMaps maps,
+                                                     int first_step, int xchunk) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int S = maps.stages;
   const int stage_bytes = 3 * kBoxHalo + 3 * kBoxOwn;
@@ -479,102 +586,88 @@ __global__ void __launch_bounds__(kThreads) h_tile(const __grid_constant__ StepP
   const int i0 = blockIdx.z * xchunk;
   const int i1 = min(i0 + xchunk, p.nx);
   const int nchain = i1 - i0 + 1;  // planes i0 .. i1
-  auto e_box = [&](int st, int q) { return reinterpret_cast<float*>(smem + st * stage_bytes + q * kBoxHalo); };
-  auto h_box = [&](int st, int q) { return reinterpret_cast<float*>(smem + st * stage_bytes + 3 * kBoxHalo + q * kBoxOwn); };
   auto issue = [&](int chain) {
     const int st = chain % S;
+    unsigned char* base = smem + st * stage_bytes;
     const int plane = i0 + chain;
     const bool own = plane < i1;
     const int xplane = (plane >= p.nx && !p.met[0]) ? plane - p.nx : plane;
     mbar_expect_tx(&full[st], 3 * (kHaloZ * kHaloY * 4) + (own ? 3 * kBoxOwn : 0));
-    for (int q = 0; q < 3; ++q) tma_load(e_box(st, q), &maps.E[q], &full[st], k0, j0, xplane);
+    for (int q = 0; q < 3; ++q) tma_load(base + q * kBoxHalo, &maps.E[q], &full[st], k0, j0, xplane);
     if (own)
-      for (int q = 0; q < 3; ++q) tma_load(h_box(st, q), &maps.Hown[q], &full[st], k0, j0, plane);
+      for (int q = 0; q < 3; ++q)
+        tma_load(base + 3 * kBoxHalo + q * kBoxOwn, &maps.Hown[q], &full[st], k0, j0, plane);
   };
+  int issued = 0;  // chains issued so far (meaningful in thread 0)
   if (tid == 0) {
     abort_flag = 0;
-    for (int s = 0; s < S; ++s) mbar_init(&full[s], 1);
+    for (int st = 0; st < S; ++st) mbar_init(&full[st], 1);
     mbar_fence_init();
     for (int c = 0; c < S && c < nchain; ++c) issue(c);
+    issued = S < nchain ? S : nchain;
   }
   __syncthreads();
-  const int lane = tid & 31, ty = tid >> 5;
-  const int j = j0 + ty;
-  // Periodic faces: the halo row/column past the far face is row/column 0, which the
-  // box's zero fill does not supply.
-  const bool patch_y = !p.met[1] && j0 + kTileY >= p.ny;
-  const bool patch_z = !p.met[2] && k0 + kTileZ >= p.nz;
-  const long long sx = (long long)p.ny * p.nz;
-  auto wait_chain = [&](int chain) {
-    const int st = chain % S;
-    if (!mbar_wait(&full[st], (unsigned)((chain / S) & 1))) {
-      abort_flag = 1;
-      if (p.status != nullptr) atomicOr(p.status, 2);
-    }
-    __syncthreads();  // the abort decision is uniform; the stage is complete for everyone
-    if (!abort_flag && (patch_y || patch_z)) {
-      const int plane = i0 + chain;
-      const int xplane = (plane >= p.nx && !p.met[0]) ? plane - p.nx : plane;
-      const bool in_x = xplane < p.nx;
-      if (patch_y) {
-        const int ry = p.ny - j0;  // halo row standing for y = ny
-        for (int t = tid; t < 3 * kHaloZ; t += kThreads) {
-          const int q = t / kHaloZ, z = t % kHaloZ, kk = k0 + z;
-          float v = 0.f;
-          if (in_x && kk < p.nz) v = p.E[q][(long long)xplane * sx + kk];
-          e_box(st, q)[ry * kHaloZ + z] = v;
-        }
-      }
-      if (patch_z) {
-        const int rz = p.nz - k0;  // halo column standing for z = nz
-        for (int t = tid; t < 3 * kHaloY; t += kThreads) {
-          const int q = t / kHaloY, y = t % kHaloY;
-          int jj = j0 + y;
-          if (jj >= p.ny) jj = p.met[1] ? -1 : jj - p.ny;
-          float v = 0.f;
-          if (in_x && jj >= 0) v = p.E[q][(long long)xplane * sx + (long long)jj * p.nz];
-          e_box(st, q)[y * kHaloZ + rz] = v;
-        }
-      }
-      __syncthreads();
-    }
-  };
-  wait_chain(0);
+  const int tz = tid & (kTileZ - 1), ty = tid / kTileZ;
+  const int j = j0 + ty, k = k0 + tz;
+  const bool live = j < p.ny && k < p.nz;
+  HColumn hcol = {};
+  bool warp_slow = false;
+  if (PML) {
+    if (live) hcol = h_column(p, j, k);
+    warp_slow = __any_sync(0xffffffffu, live && (hcol.f0 || hcol.f2 || hcol.b1 || hcol.b2));
+  }
+  const bool wrap_y = live && !p.met[1] && j + 1 == p.ny;
+  const bool wrap_z = live && !p.met[2] && k + 1 == p.nz;
+  const int sx = p.ny * p.nz;
+  const int col = j * p.nz + k;
+  const int e = ty * kHaloZ + tz;  // this cell in an E box
+  const int o = ty * kTileZ + tz;  // this cell in an own box
   const float dtdx = p.dtdx;
+  bool ok = mbar_wait(&full[0], 0);
   for (int i = i0; i < i1; ++i) {
     const int chain = i - i0;
-    wait_chain(chain + 1);
-    if (abort_flag) break;
-    const int s0 = chain % S, s1 = (chain + 1) % S;
-    const float* Ex0 = e_box(s0, 0);
-    const float* Ey0 = e_box(s0, 1);
-    const float* Ez0 = e_box(s0, 2);
-    const float* Ey1 = e_box(s1, 1);
-    const float* Ez1 = e_box(s1, 2);
-#pragma unroll
-    for (int half = 0; half < 2; ++half) {
-      const int tz = lane + 32 * half;
-      const int k = k0 + tz;
-      if (j < p.ny && k < p.nz) {
-        const int e = ty * kHaloZ + tz;
-        const float ex = Ex0[e], ey = Ey0[e], ez = Ez0[e];
-        const float cx = dtdx * (((Ez0[e + kHaloZ] - ez) + ey) - Ey0[e + 1]);
-        const float cy = dtdx * (((Ex0[e + 1] - ex) + ez) - Ez1[e]);
-        const float cz = dtdx * (((Ey1[e] - ey) + ex) - Ex0[e + kHaloZ]);
-        const int o = ty * kTileZ + tz;
-        const float h_old[3] = {h_box(s0, 0)[o], h_box(s0, 1)[o], h_box(s0, 2)[o]};
-        float h_new[3];
-        b_and_h<PML>(p, first_step, i, j, k, cx, cy, cz, h_old, h_new);
-        const long long c = (long long)i * sx + (long long)j * p.nz + k;
-        p.H[0][c] = h_new[0];
-        p.H[1][c] = h_new[1];
-        p.H[2][c] = h_new[2];
+    ok = ok && mbar_wait(&full[(chain + 1) % S], (unsigned)(((chain + 1) / S) & 1));
+    if (!ok) {
+      abort_flag = 1;
+    } else if (live) {
+      const float* st0 = reinterpret_cast<const float*>(smem + (chain % S) * stage_bytes);
+      const float* st1 = reinterpret_cast<const float*>(smem + ((chain + 1) % S) * stage_bytes);
+      const float* Ex0 = st0;
+      const float* Ey0 = st0 + kBoxHalo / 4;
+      const float* Ez0 = st0 + 2 * kBoxHalo / 4;
+      const float* Hown = st0 + 3 * kBoxHalo / 4;
+      const int c = i * sx + col;
+      const float ex = Ex0[e], ey = Ey0[e], ez = Ez0[e];
+      float ez_yp = Ez0[e + kHaloZ], ex_yp = Ex0[e + kHaloZ];
+      float ey_zp = Ey0[e + 1], ex_zp = Ex0[e + 1];
+      if (wrap_y) { ez_yp = p.E[2][c - (p.ny - 1) * p.nz]; ex_yp = p.E[0][c - (p.ny - 1) * p.nz]; }
+      if (wrap_z) { ey_zp = p.E[1][c - (p.nz - 1)]; ex_zp = p.E[0][c - (p.nz - 1)]; }
+      const float cx = dtdx * (((ez_yp - ez) + ey) - ey_zp);
+      const float cy = dtdx * (((ex_zp - ex) + ez) - (st1 + 2 * kBoxHalo / 4)[e]);
+      const float cz = dtdx * ((((st1 + kBoxHalo / 4)[e] - ey) + ex) - ex_yp);
+      const float h_old[3] = {Hown[o], Hown[kBoxOwn / 4 + o], Hown[2 * kBoxOwn / 4 + o]};
+      float h_new[3];
+      HPlane pl = {};
+      bool slow = false;
+      if (PML) {
+        pl = h_plane(p, i);
+        slow = warp_slow || pl.f1 || pl.b0;
       }
+      h_cell<PML>(p, hcol, pl, slow, first_step, i, j, k, c, cx, cy, cz, h_old, h_new);
+      p.H[0][c] = h_new[0];
+      p.H[1][c] = h_new[1];
+      p.H[2][c] = h_new[2];
     }
-    __syncthreads();  // stage s0 is read by everyone: refill it
+    __syncthreads();  // the stage of plane i is read by everyone
+    if (abort_flag) {
+      if (p.status != nullptr && tid == 0) atomicOr(p.status, 2);
+      drain_copies(full, S, chain + 1, issued, tid);
+      return;
+    }
     if (tid == 0 && chain + S < nchain) {
       fence_proxy_async_smem();
       issue(chain + S);
+      issued = chain + S + 1;
     }
   }
 }
@@ -583,11 +676,13 @@ __global__ void __launch_bounds__(kThreads) h_tile(const __grid_constant__ StepP
 // k0 - 4 and y from j0 - 1, so the -1 halo of the backward differences) and, for planes
 // at or above i0, the cell's own D and inverse-epsilon boxes. Plane i0 - 1 (the chunk's
 // x neighbour below) carries H only; below the low x face it is the zero fill of a
-// metallic wall or plane nx - 1 of a periodic axis.
+// metallic wall or plane nx - 1 of a periodic axis. Below the low y or z face of a
+// periodic axis the halo is row ny - 1 or column nz - 1: those cells read it from
+// global memory.
 template <bool PML>
-__global__ void __launch_bounds__(kThreads) e_tile(const __grid_constant__ StepParams p,
-                                                  const __grid_constant__ TileMaps maps,
-                                                  int parity, int xchunk) {
+__global__ void __launch_bounds__(kThreads, 2) e_tile(const __grid_constant__ StepParams p,
+                                                     const __grid_constant__ TileMaps maps,
+                                                     int parity, int xchunk) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int S = maps.stages;
   const int stage_bytes = 3 * kBoxHalo + (3 + maps.ninv) * kBoxOwn;
@@ -598,102 +693,91 @@ __global__ void __launch_bounds__(kThreads) e_tile(const __grid_constant__ StepP
   const int i0 = blockIdx.z * xchunk;
   const int i1 = min(i0 + xchunk, p.nx);
   const int nchain = i1 - i0 + 1;  // planes i0-1 .. i1-1
-  auto h_box = [&](int st, int q) { return reinterpret_cast<float*>(smem + st * stage_bytes + q * kBoxHalo); };
-  auto own_box = [&](int st, int slot) { return reinterpret_cast<float*>(smem + st * stage_bytes + 3 * kBoxHalo + slot * kBoxOwn); };
   auto issue = [&](int chain) {
     const int st = chain % S;
+    unsigned char* base = smem + st * stage_bytes;
     const int plane = i0 - 1 + chain;
     const bool own = plane >= i0;
     const int xplane = (plane < 0 && !p.met[0]) ? plane + p.nx : plane;
     mbar_expect_tx(&full[st], 3 * (kHaloZ * kHaloY * 4) + (own ? (3 + maps.ninv) * kBoxOwn : 0));
-    for (int q = 0; q < 3; ++q) tma_load(h_box(st, q), &maps.Hhalo[q], &full[st], k0 - 4, j0 - 1, xplane);
+    for (int q = 0; q < 3; ++q)
+      tma_load(base + q * kBoxHalo, &maps.Hhalo[q], &full[st], k0 - 4, j0 - 1, xplane);
     if (own) {
-      for (int q = 0; q < 3; ++q) tma_load(own_box(st, q), &maps.D[q], &full[st], k0, j0, plane);
-      for (int q = 0; q < maps.ninv; ++q) tma_load(own_box(st, 3 + q), &maps.inv[q], &full[st], k0, j0, plane);
+      for (int q = 0; q < 3; ++q)
+        tma_load(base + 3 * kBoxHalo + q * kBoxOwn, &maps.D[q], &full[st], k0, j0, plane);
+      for (int q = 0; q < maps.ninv; ++q)
+        tma_load(base + 3 * kBoxHalo + (3 + q) * kBoxOwn, &maps.inv[q], &full[st], k0, j0, plane);
     }
   };
+  int issued = 0;  // chains issued so far (meaningful in thread 0)
   if (tid == 0) {
     abort_flag = 0;
-    for (int s = 0; s < S; ++s) mbar_init(&full[s], 1);
+    for (int st = 0; st < S; ++st) mbar_init(&full[st], 1);
     mbar_fence_init();
     for (int c = 0; c < S && c < nchain; ++c) issue(c);
+    issued = S < nchain ? S : nchain;
   }
   __syncthreads();
-  const int lane = tid & 31, ty = tid >> 5;
-  const int j = j0 + ty;
-  const bool patch_y = !p.met[1] && j0 == 0;
-  const bool patch_z = !p.met[2] && k0 == 0;
-  const long long sx = (long long)p.ny * p.nz;
-  auto wait_chain = [&](int chain) {
-    const int st = chain % S;
-    if (!mbar_wait(&full[st], (unsigned)((chain / S) & 1))) {
-      abort_flag = 1;
-      if (p.status != nullptr) atomicOr(p.status, 2);
-    }
-    __syncthreads();  // the abort decision is uniform; the stage is complete for everyone
-    if (!abort_flag && (patch_y || patch_z)) {
-      const int plane = i0 - 1 + chain;
-      const int xplane = (plane < 0 && !p.met[0]) ? plane + p.nx : plane;
-      const bool in_x = xplane >= 0;
-      if (patch_y) {  // halo row 0 stands for y = -1, i.e. y = ny - 1
-        for (int t = tid; t < 3 * kHaloZ; t += kThreads) {
-          const int q = t / kHaloZ, z = t % kHaloZ;
-          int kk = k0 - 4 + z;
-          if (kk < 0) kk = p.met[2] ? -1 : kk + p.nz;
-          float v = 0.f;
-          if (in_x && kk >= 0 && kk < p.nz)
-            v = p.H[q][(long long)xplane * sx + (long long)(p.ny - 1) * p.nz + kk];
-          h_box(st, q)[z] = v;
-        }
-      }
-      if (patch_z) {  // halo column 3 stands for z = -1, i.e. z = nz - 1
-        for (int t = tid; t < 3 * kHaloY; t += kThreads) {
-          const int q = t / kHaloY, y = t % kHaloY;
-          int jj = j0 - 1 + y;
-          if (jj < 0) jj = p.met[1] ? -1 : jj + p.ny;
-          float v = 0.f;
-          if (in_x && jj >= 0 && jj < p.ny)
-            v = p.H[q][(long long)xplane * sx + (long long)jj * p.nz + (p.nz - 1)];
-          h_box(st, q)[y * kHaloZ + 3] = v;
-        }
-      }
-      __syncthreads();
-    }
-  };
-  wait_chain(0);
+  const int tz = tid & (kTileZ - 1), ty = tid / kTileZ;
+  const int j = j0 + ty, k = k0 + tz;
+  const bool live = j < p.ny && k < p.nz;
+  EColumn ecol = {};
+  bool warp_slow = false;
+  if (PML) {
+    if (live) ecol = e_column(p, j, k);
+    warp_slow = __any_sync(0xffffffffu, live && (ecol.f0 || ecol.f2 || ecol.w1 || ecol.w2));
+  }
+  const bool wrap_y = live && !p.met[1] && j == 0;
+  const bool wrap_z = live && !p.met[2] && k == 0;
+  const int sx = p.ny * p.nz;
+  const int col = j * p.nz + k;
+  const int h = (ty + 1) * kHaloZ + tz + 4;  // this cell in an H box
+  const int o = ty * kTileZ + tz;            // this cell in an own box
+  const int inv0 = 3 + maps.inv_of[0], inv1 = 3 + maps.inv_of[1], inv2 = 3 + maps.inv_of[2];
   const float dtdx = p.dtdx;
+  bool ok = mbar_wait(&full[0], 0);
   for (int i = i0; i < i1; ++i) {
     const int chain = i - i0 + 1;
-    wait_chain(chain);
-    if (abort_flag) break;
-    const int s1 = chain % S, s0 = (chain - 1) % S;
-    const float* Hx = h_box(s1, 0);
-    const float* Hy = h_box(s1, 1);
-    const float* Hz = h_box(s1, 2);
-    const float* Hy0 = h_box(s0, 1);
-    const float* Hz0 = h_box(s0, 2);
-#pragma unroll
-    for (int half = 0; half < 2; ++half) {
-      const int tz = lane + 32 * half;
-      const int k = k0 + tz;
-      if (j < p.ny && k < p.nz) {
-        const int h = (ty + 1) * kHaloZ + tz + 4;
-        const float hx = Hx[h], hy = Hy[h], hz = Hz[h];
-        const float cx = dtdx * (((Hz[h - kHaloZ] - hz) + hy) - Hy[h - 1]);
-        const float cy = dtdx * (((Hx[h - 1] - hx) + hz) - Hz0[h]);
-        const float cz = dtdx * (((Hy0[h] - hy) + hx) - Hx[h - kHaloZ]);
-        const int o = ty * kTileZ + tz;
-        float d[3] = {own_box(s1, 0)[o], own_box(s1, 1)[o], own_box(s1, 2)[o]};
-        const float inv[3] = {own_box(s1, 3 + maps.inv_of[0])[o], own_box(s1, 3 + maps.inv_of[1])[o],
-                              own_box(s1, 3 + maps.inv_of[2])[o]};
-        const long long c = (long long)i * sx + (long long)j * p.nz + k;
-        d_e_p<PML>(p, parity, i, j, k, c, cx, cy, cz, d, inv);
+    ok = ok && mbar_wait(&full[chain % S], (unsigned)((chain / S) & 1));
+    if (!ok) {
+      abort_flag = 1;
+    } else if (live) {
+      const float* st1 = reinterpret_cast<const float*>(smem + (chain % S) * stage_bytes);
+      const float* st0 = reinterpret_cast<const float*>(smem + ((chain - 1) % S) * stage_bytes);
+      const float* Hx = st1;
+      const float* Hy = st1 + kBoxHalo / 4;
+      const float* Hz = st1 + 2 * kBoxHalo / 4;
+      const float* own = st1 + 3 * kBoxHalo / 4;
+      const int c = i * sx + col;
+      const float hx = Hx[h], hy = Hy[h], hz = Hz[h];
+      float hz_ym = Hz[h - kHaloZ], hx_ym = Hx[h - kHaloZ];
+      float hy_zm = Hy[h - 1], hx_zm = Hx[h - 1];
+      if (wrap_y) { hz_ym = p.H[2][c + (p.ny - 1) * p.nz]; hx_ym = p.H[0][c + (p.ny - 1) * p.nz]; }
+      if (wrap_z) { hy_zm = p.H[1][c + (p.nz - 1)]; hx_zm = p.H[0][c + (p.nz - 1)]; }
+      const float cx = dtdx * (((hz_ym - hz) + hy) - hy_zm);
+      const float cy = dtdx * (((hx_zm - hx) + hz) - (st0 + 2 * kBoxHalo / 4)[h]);
+      const float cz = dtdx * ((((st0 + kBoxHalo / 4)[h] - hy) + hx) - hx_ym);
+      float d[3] = {own[o], own[kBoxOwn / 4 + o], own[2 * kBoxOwn / 4 + o]};
+      const float inv[3] = {own[inv0 * (kBoxOwn / 4) + o], own[inv1 * (kBoxOwn / 4) + o],
+                            own[inv2 * (kBoxOwn / 4) + o]};
+      EPlane pl = {};
+      bool slow = false;
+      if (PML) {
+        pl = e_plane(p, i);
+        slow = warp_slow || pl.f1 || pl.w0;
       }
+      e_cell<PML>(p, ecol, pl, slow, parity, i, j, k, c, cx, cy, cz, d, inv);
     }
-    __syncthreads();
+    __syncthreads();  // the stage of plane i - 1 is read by everyone
+    if (abort_flag) {
+      if (p.status != nullptr && tid == 0) atomicOr(p.status, 2);
+      drain_copies(full, S, chain, issued, tid);
+      return;
+    }
     if (tid == 0 && chain - 1 + S < nchain) {
       fence_proxy_async_smem();
       issue(chain - 1 + S);
+      issued = chain - 1 + S + 1;
     }
   }
 }
@@ -818,7 +902,7 @@ struct mgb_sim {
   int block_z = 32;
   int block_y = 8;
   int xchunk = 16;       // generic kernels
-  int tile_xchunk = 24;  // tile kernels
+  int tile_xchunk = 8;   // tile kernels
 };
 
 namespace {

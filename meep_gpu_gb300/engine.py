@@ -7,10 +7,12 @@ and drives ``mgb_step``. Layout in HBM, all float32 and C-ordered ``(nx, ny, nz)
 * E, D, H: three full volumes each; one inverse-epsilon volume per distinct array
   (the isotropic case aliases one volume for all three components). Outside each H
   component's own-axis integer PML runs MEEP's H is B's word, so H carries B there;
-* PML auxiliaries, compact over their membership runs only (one axis shortened to the
-  run length): B and the ``f_w`` of H on each H component's own-axis integer runs,
-  ``f_w`` of E on the own-axis half runs, and the split-field ``fu`` of B (half
-  lattice) and D (integer lattice) on the dsigu runs;
+* PML auxiliaries, read and written only on their membership runs: B and the ``f_w`` of
+  H on each H component's own-axis integer runs, ``f_w`` of E on the own-axis half
+  runs, and the split-field ``fu`` of B (half lattice) and D (integer lattice) on the
+  dsigu runs. Each is allocated as a full volume (HBM is plentiful) so a cell's
+  auxiliary word sits at the cell's own offset and needs no index arithmetic; the cells
+  outside the runs are never touched and move no bytes;
 * polarization: two rotating buffers per pole and driven component, over the bounding
   box of the cells where any pole's sigma is nonzero (P stays zero elsewhere);
 * DFT accumulators ``[ncomp][nfreq][re, im][cells]`` per monitor.
@@ -86,6 +88,7 @@ class Engine:
             d.H[q] = self.fields["H" + axis].data_ptr()
             d.inv_eps[q] = self.inv_eps[q].data_ptr()
         self.aux: Dict[str, torch.Tensor] = {}
+        self.aux_cells: Dict[str, int] = {}  # membership cells each auxiliary touches
         self.coefficients: Dict[Tuple[str, int, int], torch.Tensor] = {}
         if self.pml is not None:
             d.pml_active = 1
@@ -122,11 +125,12 @@ class Engine:
     def _aux(self, slot, name: str, q: int, key: Tuple[int, int]) -> None:
         lattice, axis = key
         record = self.records[key]
-        tensor = torch.zeros(aux_shape(self.grid, record, axis), dtype=torch.float32, device=self.device)
-        if tensor.numel() == 0:
-            # An empty membership still needs a valid pointer; the kernels never touch it.
-            tensor = torch.zeros(1, dtype=torch.float32, device=self.device)
+        # A full volume, of which the kernels touch only the membership cells: the
+        # auxiliary word of a cell sits at the cell's own offset.
+        tensor = torch.zeros(self.grid.shape, dtype=torch.float32, device=self.device)
         self.aux[f"{name}{'xyz'[q]}"] = tensor
+        self.aux_cells[f"{name}{'xyz'[q]}"] = (
+            int(np.prod(aux_shape(self.grid, record, axis))))
         entry = slot[q]
         entry.data = tensor.data_ptr()
         entry.axis = axis
@@ -291,7 +295,7 @@ class Engine:
         """
         cells = self.grid.total_cells
         word = 4
-        aux = lambda name: sum(int(self.aux[f"{name}{a}"].numel()) for a in "xyz") if self.pml is not None else 0  # noqa: E731
+        aux = lambda name: sum(self.aux_cells[f"{name}{a}"] for a in "xyz") if self.pml is not None else 0  # noqa: E731
         h = 9 * cells + 2 * aux("fuB") + 2 * aux("B") + 2 * aux("fwH")
         distinct_inv = len({t.data_ptr() for t in self.inv_eps})
         e = (12 + distinct_inv) * cells + 2 * aux("fuD") + 3 * aux("fwE")
@@ -319,7 +323,7 @@ class Engine:
             if rows.size:
                 index = [slice(None)] * 3
                 index[q] = torch.from_numpy(rows).to(self.device)
-                b[tuple(index)] = self.aux["B" + name[1]]
+                b[tuple(index)] = self.aux["B" + name[1]][tuple(index)]
             return b
         raise ValueError(f"unknown component {name!r}")
 

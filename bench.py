@@ -51,7 +51,9 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     p.add_argument("--workload", default="sphere192_8dft")
-    p.add_argument("--launch-shape", default=None, help="block_z,block_y,x_chunk")
+    p.add_argument("--kernels", default=None,
+                   help="family,block_z,block_y,x_chunk (family 1: TMA tiles, 0: generic); "
+                        "default: the autotuner's choice")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-validate", action="store_true")
@@ -190,16 +192,17 @@ def main():
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     device = torch.device("cuda", local)
-    shape = tuple(int(v) for v in args.launch_shape.split(",")) if args.launch_shape else None
+    kernels = tuple(int(v) for v in args.kernels.split(",")) if args.kernels else None
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
 
     # ---- device-resident throughput ---------------------------------------------------
-    driver, flux, dft = workloads.build(args.workload, FdtdDriver, gpu_id=local, launch_shape=shape)
+    driver, flux, dft = workloads.build(args.workload, FdtdDriver, gpu_id=local, kernels=kernels)
     driver.step_many(args.warmup)  # freezes the configuration and warms the kernels
     engine = driver.engine
+    choice = list(engine.choice) if engine.choice is not None else None
     cells = driver.grid.total_cells
     first = driver.step_count
     engine.ensure_source_words(first, args.steps)
@@ -246,11 +249,11 @@ def main():
     e_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in events]))
     bytes_per = engine.algorithmic_bytes()
     peak, peak_kind = measured_peaks()
-    kernels = {"h_half": {"ms": h_ms, "bytes": bytes_per["h_half"]},
-               "e_half": {"ms": e_ms, "bytes": bytes_per["e_half"]}}
-    for info in kernels.values():
+    timed = {"h_half": {"ms": h_ms, "bytes": bytes_per["h_half"]},
+             "e_half": {"ms": e_ms, "bytes": bytes_per["e_half"]}}
+    for info in timed.values():
         info["gbs"] = info["bytes"] / (info["ms"] / 1e3) / 1e9
-    dominant = max(kernels, key=lambda k: kernels[k]["ms"])
+    dominant = max(timed, key=lambda k: timed[k]["ms"])
     traffic = None
     summary = ROOT / "profiles" / f"{dominant}_{args.workload}.txt"
     if summary.exists():
@@ -259,12 +262,12 @@ def main():
                 traffic = int(float(line.split(":", 1)[1]))
     step_bytes = bytes_per["h_half"] + bytes_per["e_half"]
     roofline = {"bound": "hbm", "kernel": dominant,
-                "achieved": round(kernels[dominant]["gbs"], 1), "peak": peak, "unit": "GB/s",
-                "frac": round(kernels[dominant]["gbs"] / peak, 4), "traffic": traffic,
+                "achieved": round(timed[dominant]["gbs"], 1), "peak": peak, "unit": "GB/s",
+                "frac": round(timed[dominant]["gbs"] / peak, 4), "traffic": traffic,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
                 "algorithmic_bytes_per_launch": bytes_per[dominant],
                 "per_kernel": {k: {"ms": round(v["ms"], 4), "GB/s": round(v["gbs"], 1),
-                                   "frac": round(v["gbs"] / peak, 4)} for k, v in kernels.items()},
+                                   "frac": round(v["gbs"] / peak, 4)} for k, v in timed.items()},
                 "step_bytes_per_cell": round(step_bytes / cells, 2),
                 "step_frac": round(step_bytes / ((ms / args.steps) / 1e3) / 1e9 / peak, 4)}
     driver.close()
@@ -277,7 +280,7 @@ def main():
         torch.cuda.synchronize(device)
         barrier()
         t0 = time.perf_counter()
-        d2, f2, v2 = workloads.build(args.workload, FdtdDriver, gpu_id=local, launch_shape=shape)
+        d2, f2, v2 = workloads.build(args.workload, FdtdDriver, gpu_id=local, kernels=kernels)
         d2.run(num_steps=args.steps, progress_interval=max(args.steps, 1), check_finite=False)
         results = [m.get_flux_spectrum() for m in f2]
         arrays = [m.raw(c) for m in v2 for c in m.components]
@@ -317,7 +320,8 @@ def main():
         "data": "synthetic",
         "config": {"workload": args.workload, "cells": cells, "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 (no flush needed)",
-                   "launch_shape": list(shape) if shape else [32, 8, 16],
+                   "kernels": {"family": ("tiles" if choice and choice[0] == 1 else "generic"),
+                               "choice": choice, "chosen_by": "argument" if kernels else "autotuner"},
                    "monitors": {"flux_planes": len(flux), "dft_volumes": len(dft),
                                 "decimation": [m.decimation_factor for m in list(flux) + list(dft)][:1]}},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,

@@ -171,6 +171,13 @@ int mgb_flux_spectrum(mgb_sim* sim, int32_t monitor, const float* weights, doubl
  * extent that is not a multiple of 4, or MEEPGB_TILES=0 in the environment). */
 int mgb_uses_tiles(mgb_sim* sim);
 
+/* Choose the kernel family: 0 the generic kernels (plain loads), 1 the tile kernels
+ * (TMA-staged shared-memory planes; needs a z extent that is a multiple of 4). Both
+ * compute the same words; the autotuner picks the faster for a grid. No reference
+ * counterpart (the reference's dispatch arbiter picks among its own kernel tables,
+ * meep_gpu/dispatch_preference.py). */
+int mgb_select_kernels(mgb_sim* sim, int32_t family);
+
 /* Release the plan (never the caller's arrays). */
 void mgb_destroy(mgb_sim* sim);
 

@@ -94,6 +94,7 @@ SIGNATURES = {
     "mgb_flux_spectrum": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.c_void_p]),
     "mgb_uses_tiles": (ctypes.c_int, [ctypes.c_void_p]),
+    "mgb_select_kernels": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "mgb_destroy": (None, [ctypes.c_void_p]),
     "mgb_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
 }

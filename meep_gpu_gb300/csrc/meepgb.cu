@@ -154,11 +154,15 @@ __device__ __forceinline__ HColumn h_column(const StepParams& p, int j, int k) {
 }
 
 __device__ __forceinline__ HPlane h_plane(const StepParams& p, int i) {
-  HPlane c;
+  HPlane c = {};
   c.f1 = in_runs(p.fuB[1], i); c.b0 = in_runs(p.B[0], i);
+  return c;
+}
+
+// The plane's coefficients, needed only on the PML path.
+__device__ __forceinline__ void h_plane_coefficients(const StepParams& p, int i, HPlane& c) {
   c.kms_xh = ldgf(p.kms[kHalf][0], i); c.sinv_xh = ldgf(p.sinv[kHalf][0], i);
   c.kps_x = ldgf(p.kps[kInteger][0], i); c.kms_x = ldgf(p.kms[kInteger][0], i);
-  return c;
 }
 
 // B from its curls, zero_metal_B, H from B (update_H) for one cell at offset c, and the
@@ -241,11 +245,15 @@ __device__ __forceinline__ EColumn e_column(const StepParams& p, int j, int k) {
 }
 
 __device__ __forceinline__ EPlane e_plane(const StepParams& p, int i) {
-  EPlane c;
+  EPlane c = {};
   c.f1 = in_runs(p.fuD[1], i); c.w0 = in_runs(p.fwE[0], i);
+  return c;
+}
+
+// The plane's coefficients, needed only on the PML path.
+__device__ __forceinline__ void e_plane_coefficients(const StepParams& p, int i, EPlane& c) {
   c.kms_x = ldgf(p.kms[kInteger][0], i); c.sinv_x = ldgf(p.sinv[kInteger][0], i);
   c.kps_xh = ldgf(p.kps[kHalf][0], i); c.kms_xh = ldgf(p.kms[kHalf][0], i);
-  return c;
 }
 
 // D from its curls, the source deposit, zero_metal_D, E (update_E) and P (update_P)
@@ -361,7 +369,7 @@ __device__ __forceinline__ void e_cell(const StepParams& p, const EColumn& col, 
 // ------------------------------------------------------------------------------------
 // Generic kernels: plain loads, one thread per (y, z) column marching over x.
 template <bool PML>
-__global__ void __launch_bounds__(256) h_generic(const __grid_constant__ StepParams p,
+__global__ void __launch_bounds__(256, 5) h_generic(const __grid_constant__ StepParams p,
                                                  int first_step, int xchunk) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -416,6 +424,7 @@ __global__ void __launch_bounds__(256) h_generic(const __grid_constant__ StepPar
     if (PML) {
       pl = h_plane(p, i);
       slow = warp_slow || pl.f1 || pl.b0;
+      if (slow) h_plane_coefficients(p, i, pl);
     }
     h_cell<PML>(p, hcol, pl, slow, first_step, i, j, k, c, cx, cy, cz, h_old, h_new);
     p.H[0][c] = h_new[0];
@@ -427,7 +436,7 @@ __global__ void __launch_bounds__(256) h_generic(const __grid_constant__ StepPar
 }
 
 template <bool PML>
-__global__ void __launch_bounds__(256) e_generic(const __grid_constant__ StepParams p, int parity,
+__global__ void __launch_bounds__(256, 5) e_generic(const __grid_constant__ StepParams p, int parity,
                                                  int xchunk) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -482,6 +491,7 @@ __global__ void __launch_bounds__(256) e_generic(const __grid_constant__ StepPar
     if (PML) {
       pl = e_plane(p, i);
       slow = warp_slow || pl.f1 || pl.w0;
+      if (slow) e_plane_coefficients(p, i, pl);
     }
     e_cell<PML>(p, ecol, pl, slow, parity, i, j, k, c, cx, cy, cz, d, inv);
     hy_xm = hy;
@@ -652,6 +662,7 @@ __global__ void __launch_bounds__(kThreads, 2) h_tile(const __grid_constant__ St
       if (PML) {
         pl = h_plane(p, i);
         slow = warp_slow || pl.f1 || pl.b0;
+        if (slow) h_plane_coefficients(p, i, pl);
       }
       h_cell<PML>(p, hcol, pl, slow, first_step, i, j, k, c, cx, cy, cz, h_old, h_new);
       p.H[0][c] = h_new[0];
@@ -765,6 +776,7 @@ __global__ void __launch_bounds__(kThreads, 2) e_tile(const __grid_constant__ St
       if (PML) {
         pl = e_plane(p, i);
         slow = warp_slow || pl.f1 || pl.w0;
+        if (slow) e_plane_coefficients(p, i, pl);
       }
       e_cell<PML>(p, ecol, pl, slow, parity, i, j, k, c, cx, cy, cz, d, inv);
     }
@@ -894,14 +906,15 @@ struct mgb_sim {
   mgb_sim_desc desc;
   StepParams step;
   TileMaps maps;
-  bool tiles = false;
+  bool tiles = false;        // step with the tile kernels
+  bool tiles_ready = false;  // their tensor maps are built
   size_t h_smem = 0, e_smem = 0;
   const double* words = nullptr;
   long long words_first = 0;
   long long words_steps = 0;
   int block_z = 32;
-  int block_y = 8;
-  int xchunk = 16;       // generic kernels
+  int block_y = 4;
+  int xchunk = 4;        // generic kernels
   int tile_xchunk = 8;   // tile kernels
 };
 
@@ -999,6 +1012,7 @@ void setup_tiles(mgb_sim* sim) {
   }
   const char* xc = getenv("MEEPGB_TILE_XCHUNK");
   if (xc != nullptr && atoi(xc) >= 1) sim->tile_xchunk = atoi(xc);
+  sim->tiles_ready = true;
   sim->tiles = true;
 }
 
@@ -1120,8 +1134,10 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
 
 int mgb_set_launch_shape(mgb_sim* sim, int block_z, int block_y, int xchunk) {
   if (sim == nullptr) return fail(MGB_ERR_ARGUMENT, "null plan");
-  if (block_z < 1 || block_y < 1 || block_z * block_y > 256 || xchunk < 1) {
-    return fail(MGB_ERR_ARGUMENT, "launch shape needs block_z*block_y <= 256 and x_chunk >= 1");
+  if (block_z < 1 || block_y < 1 || block_z * block_y > 256 || (block_z * block_y) % 32 != 0 ||
+      xchunk < 1) {
+    return fail(MGB_ERR_ARGUMENT,
+                "launch shape needs block_z*block_y a multiple of 32 up to 256 and x_chunk >= 1");
   }
   sim->block_z = block_z;
   sim->block_y = block_y;
@@ -1249,6 +1265,20 @@ int mgb_flux_spectrum(mgb_sim* sim, int32_t monitor, const float* weights, doubl
 }
 
 int mgb_uses_tiles(mgb_sim* sim) { return sim != nullptr && sim->tiles ? 1 : 0; }
+
+int mgb_select_kernels(mgb_sim* sim, int32_t family) {
+  if (sim == nullptr) return fail(MGB_ERR_ARGUMENT, "null plan");
+  if (family == 0) {
+    sim->tiles = false;
+    return MGB_OK;
+  }
+  if (family == 1) {
+    if (!sim->tiles_ready) return fail(MGB_ERR_UNSUPPORTED, "the tile kernels need a z extent that is a multiple of 4");
+    sim->tiles = true;
+    return MGB_OK;
+  }
+  return fail(MGB_ERR_ARGUMENT, "kernel family is 0 (generic) or 1 (tiles)");
+}
 
 void mgb_destroy(mgb_sim* sim) { delete sim; }
 

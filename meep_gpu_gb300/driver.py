@@ -58,7 +58,8 @@ class FdtdDriver:
                  dimensions: int = 3, cylindrical: bool = False, m: int = 0,
                  accurate_fields_near_cylorigin: bool = False, beta: float = 0.0,
                  bfast_scaled_k: Sequence[float] = (0.0, 0.0, 0.0), prefer_gpu: bool = True,
-                 gpu_id: int = 0, launch_shape: Optional[Tuple[int, int, int]] = None):
+                 gpu_id: int = 0, launch_shape: Optional[Tuple[int, int, int]] = None,
+                 kernels: Optional[Tuple[int, int, int, int]] = None):
         if force_complex_fields:
             raise Unsupported("complex fields are not stepped by this engine; pass "
                               "force_complex_fields=False (real float32 fields)")
@@ -74,6 +75,9 @@ class FdtdDriver:
         self.grid = Grid(cell_size, resolution, courant, boundaries)
         self.gpu_id = int(gpu_id)
         self.launch_shape = launch_shape
+        # (family, block_z, block_y, x_chunk): 1 the TMA tile kernels, 0 the generic ones;
+        # None lets the autotuner time both on this grid and keep the faster.
+        self.kernels = kernels
         self.pml: Optional[PML] = None
         self._eps: Optional[Tuple[np.ndarray, np.ndarray, np.ndarray]] = None
         self._inv_eps: Optional[Tuple[np.ndarray, np.ndarray, np.ndarray]] = None
@@ -251,7 +255,7 @@ class FdtdDriver:
         device = torch.device("cuda", self.gpu_id)
         self.engine = Engine(self.grid, self.pml, self._inv_eps, self._poles, self._sources,
                              list(self._flux_monitors) + list(self._dft_monitors), device=device,
-                             launch_shape=self.launch_shape)
+                             launch_shape=self.launch_shape, kernels=self.kernels)
 
     # --- stepping -------------------------------------------------------------------
     @property

@@ -22,6 +22,7 @@ from __future__ import annotations
 
 import ctypes
 import math
+import os
 from typing import Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
@@ -38,6 +39,17 @@ FIELD_NAMES = ("E", "D", "H")
 # Source words are uploaded in windows of this many steps.
 SOURCE_WINDOW = 4096
 
+# Kernel choices the autotuner times: (family, block_z, block_y, x_chunk); family 1 is
+# the tile kernels (block shape fixed at 64 x 8, x_chunk used), family 0 the generic ones.
+AUTOTUNE_CANDIDATES = ((0, 32, 4, 4), (0, 32, 8, 4), (0, 32, 4, 8), (0, 64, 2, 8),
+                       (1, 64, 8, 4), (1, 64, 8, 8))
+_AUTOTUNE_CACHE: Dict[tuple, Tuple[int, int, int, int]] = {}
+
+
+def autotune_key(grid: Grid, pml: Optional[PML], npoles: int, ninv: int) -> tuple:
+    faces = pml.faces if (pml is not None and pml.is_active) else None
+    return (grid.shape, grid.boundaries, faces, npoles, ninv)
+
 
 def _ptr(t: Optional[torch.Tensor]) -> Optional[int]:
     return None if t is None else t.data_ptr()
@@ -50,7 +62,8 @@ class Engine:
                  poles: Sequence[Tuple[object, Sequence[Optional[np.ndarray]]]],
                  sources: Sequence[Source], monitors: Sequence[_Monitor],
                  device: Optional[torch.device] = None, stream: Optional[torch.cuda.Stream] = None,
-                 launch_shape: Optional[Tuple[int, int, int]] = None):
+                 launch_shape: Optional[Tuple[int, int, int]] = None, autotune: bool = True,
+                 kernels: Optional[Tuple[int, int, int, int]] = None):
         if not torch.cuda.is_available():
             raise RuntimeError("meep_gpu_gb300 steps on a CUDA GPU and none is visible")
         self.lib = _lib.load()
@@ -115,8 +128,14 @@ class Engine:
         handle = ctypes.c_void_p()
         _lib.check(self.lib, self.lib.mgb_create(ctypes.byref(d), ctypes.byref(handle)))
         self.handle = handle
-        if launch_shape is not None:
+        self._pole_specs = list(poles)
+        self.choice = None
+        if kernels is not None:
+            self.select(tuple(kernels))
+        elif launch_shape is not None:
             self.set_launch_shape(*launch_shape)
+        elif autotune and os.environ.get("MEEPGB_AUTOTUNE", "1") != "0":
+            self.autotune()
         self._words: Optional[torch.Tensor] = None
         self._words_first = 0
         self._words_steps = 0
@@ -274,6 +293,59 @@ class Engine:
     def uses_tiles(self) -> bool:
         """Whether the plan steps with the TMA tile kernels (else the generic ones)."""
         return bool(self.lib.mgb_uses_tiles(self.handle))
+
+    def select(self, choice: Tuple[int, int, int, int]) -> None:
+        """Apply a kernel choice (family, block_z, block_y, x_chunk)."""
+        family, bz, by, xc = choice
+        _lib.check(self.lib, self.lib.mgb_select_kernels(self.handle, family))
+        if family == 0:
+            self.set_launch_shape(bz, by, xc)
+        else:
+            self.set_launch_shape(32, 8, xc)
+        self.choice = choice
+
+    def autotune(self, steps: int = 4) -> Tuple[int, int, int, int]:
+        """Pick the fastest kernel choice for this grid and apply it.
+
+        Candidates are timed (CUDA events, H and E halves) on a scratch engine with the
+        same grid, absorber, materials and poles but zero fields and no sources or
+        monitors, so this simulation's state is untouched; the result is cached per
+        configuration for the life of the process.
+        """
+        key = autotune_key(self.grid, self.pml, len(getattr(self, "pole_tensors", [])),
+                           len({t.data_ptr() for t in self.inv_eps}))
+        if key in _AUTOTUNE_CACHE:
+            self.select(_AUTOTUNE_CACHE[key])
+            return self.choice
+        scratch = Engine(self.grid, self.pml, [t.cpu().numpy() for t in self.inv_eps],
+                         self._pole_specs, [], [], device=self.device, autotune=False)
+        stream = torch.cuda.current_stream(self.device)
+        best, best_ms = None, float("inf")
+        for choice in AUTOTUNE_CANDIDATES:
+            try:
+                scratch.select(choice)
+            except _lib.MeepGBError:
+                continue
+            for n in range(2):
+                scratch.launch(n, 0, stream)
+                scratch.launch(n, 1, stream)
+            start = torch.cuda.Event(enable_timing=True)
+            end = torch.cuda.Event(enable_timing=True)
+            start.record(stream)
+            for n in range(2, 2 + steps):
+                scratch.launch(n, 0, stream)
+                scratch.launch(n, 1, stream)
+            end.record(stream)
+            end.synchronize()
+            ms = start.elapsed_time(end) / steps
+            if ms < best_ms:
+                best, best_ms = choice, ms
+        scratch.close()
+        del scratch
+        _AUTOTUNE_CACHE[key] = best
+        self.select(best)
+        self.autotune_ms = best_ms
+        return best
 
     def launch(self, step: int, part: int, stream=None) -> None:
         """Launch one kernel of one step: 0 the H half, 1 the E half, 2 the monitors."""

@@ -165,28 +165,32 @@ __device__ __forceinline__ void h_plane_coefficients(const StepParams& p, int i,
   c.kps_x = ldgf(p.kps[kInteger][0], i); c.kms_x = ldgf(p.kms[kInteger][0], i);
 }
 
-// B from its curls, zero_metal_B, H from B (update_H) for one cell at offset c, and the
-// auxiliary stores. `h_old` is the stored H word (the old B outside the own-axis
-// membership). `slow` selects the PML arithmetic.
-template <bool PML>
-__device__ __forceinline__ void h_cell(const StepParams& p, const HColumn& col, const HPlane& pl,
-                                       bool slow, int first_step, int i, int j, int k, int c,
-                                       float cx, float cy, float cz, const float h_old[3],
-                                       float h_new[3]) {
-  if (p.met[0] && i == 0) cx = 0.f;
-  if (p.met[1] && j == 0) cy = 0.f;
-  if (p.met[2] && k == 0) cz = 0.f;
-  if (!PML || !slow) {
-    h_new[0] = h_old[0] - cx;
-    h_new[1] = h_old[1] - cy;
-    h_new[2] = h_old[2] - cz;
-    if (p.met[0] && i == 0) h_new[0] = 0.f;
-    if (p.met[1] && j == 0) h_new[1] = 0.f;
-    if (p.met[2] && k == 0) h_new[2] = 0.f;
-    return;
+// One curl component. DSIG: a lane of the warp may sit in the dsig membership (else the
+// dsig coefficients are exactly 1 for the whole warp and drop out); DSIGU: a lane may sit
+// in the dsigu membership (`member` says whether this one does), which selects the
+// split-field recurrence and its auxiliary `u` (the new one returned in `n`).
+template <bool DSIG, bool DSIGU>
+__device__ __forceinline__ float curl_form(float f, float curl, bool member, float u, float kms,
+                                           float sinv, float kms_u, float sinv_u, float& n) {
+  if (DSIGU && member) {
+    n = DSIG ? (kms * u - curl) * sinv : u - curl;
+    return ((kms_u * f + n) - u) * sinv_u;
   }
-  const bool sb0 = pl.b0, sb1 = col.b1, sb2 = col.b2;
-  const bool sf0 = col.f0, sf1 = pl.f1, sf2 = col.f2;
+  return DSIG ? (kms * f - curl) * sinv : f - curl;
+}
+
+// B from its curls, zero_metal_B, H from B (update_H) for one cell at offset c, and the
+// auxiliary stores, for a warp that may touch the x (SX), y (SY) and z (SZ) memberships.
+// Each axis switches on one feature per component (x: Bx own, By dsigu, Bz dsig;
+// y: Bx dsig, By own, Bz dsigu; z: Bx dsigu, By dsig, Bz own). `h_old` is the stored H
+// word (the old B outside the own-axis membership).
+template <bool SX, bool SY, bool SZ>
+__device__ __forceinline__ void h_cell_v(const StepParams& p, const HColumn& col,
+                                         const HPlane& pl, int first_step, int c, float cx,
+                                         float cy, float cz, const float h_old[3],
+                                         float h_new[3]) {
+  const bool sb0 = SX && pl.b0, sb1 = SY && col.b1, sb2 = SZ && col.b2;
+  const bool sf0 = SZ && col.f0, sf1 = SX && pl.f1, sf2 = SY && col.f2;
   // Loads: every auxiliary word of the cell, before any store.
   float b0 = sb0 ? p.B[0].data[c] : h_old[0];
   float b1 = sb1 ? p.B[1].data[c] : h_old[1];
@@ -199,26 +203,51 @@ __device__ __forceinline__ void h_cell(const StepParams& p, const HColumn& col, 
   const float u2 = sf2 ? p.fuB[2].data[c] : 0.f;
   // Bx: dsig y, dsigu z; By: dsig z, dsigu x; Bz: dsig x, dsigu y.
   float n0 = 0.f, n1 = 0.f, n2 = 0.f;
-  if (sf0) { n0 = (col.kms_yh * u0 - cx) * col.sinv_yh; b0 = ((col.kms_zh * b0 + n0) - u0) * col.sinv_zh; }
-  else b0 = (col.kms_yh * b0 - cx) * col.sinv_yh;
-  if (sf1) { n1 = (col.kms_zh * u1 - cy) * col.sinv_zh; b1 = ((pl.kms_xh * b1 + n1) - u1) * pl.sinv_xh; }
-  else b1 = (col.kms_zh * b1 - cy) * col.sinv_zh;
-  if (sf2) { n2 = (pl.kms_xh * u2 - cz) * pl.sinv_xh; b2 = ((col.kms_yh * b2 + n2) - u2) * col.sinv_yh; }
-  else b2 = (pl.kms_xh * b2 - cz) * pl.sinv_xh;
-  // zero_metal_B: each component sits on the wall of its own axis.
-  if (p.met[0] && i == 0) b0 = 0.f;
-  if (p.met[1] && j == 0) b1 = 0.f;
-  if (p.met[2] && k == 0) b2 = 0.f;
+  b0 = curl_form<SY, SZ>(b0, cx, sf0, u0, col.kms_yh, col.sinv_yh, col.kms_zh, col.sinv_zh, n0);
+  b1 = curl_form<SZ, SX>(b1, cy, sf1, u1, col.kms_zh, col.sinv_zh, pl.kms_xh, pl.sinv_xh, n1);
+  b2 = curl_form<SX, SY>(b2, cz, sf2, u2, pl.kms_xh, pl.sinv_xh, col.kms_yh, col.sinv_yh, n2);
+  // zero_metal_B happens in the caller before this returns its words (masks above).
+  h_new[0] = b0; h_new[1] = b1; h_new[2] = b2;
   // update_H on the own-axis integer membership (MEEP starts H and f_w from B once).
-  h_new[0] = sb0 ? (first_step ? b0 : h_old[0]) + (pl.kps_x * b0 - pl.kms_x * (first_step ? b0 : w0)) : b0;
-  h_new[1] = sb1 ? (first_step ? b1 : h_old[1]) + (col.kps_y * b1 - col.kms_y * (first_step ? b1 : w1)) : b1;
-  h_new[2] = sb2 ? (first_step ? b2 : h_old[2]) + (col.kps_z * b2 - col.kms_z * (first_step ? b2 : w2)) : b2;
+  if (SX && sb0) h_new[0] = (first_step ? b0 : h_old[0]) + (pl.kps_x * b0 - pl.kms_x * (first_step ? b0 : w0));
+  if (SY && sb1) h_new[1] = (first_step ? b1 : h_old[1]) + (col.kps_y * b1 - col.kms_y * (first_step ? b1 : w1));
+  if (SZ && sb2) h_new[2] = (first_step ? b2 : h_old[2]) + (col.kps_z * b2 - col.kms_z * (first_step ? b2 : w2));
   if (sf0) p.fuB[0].data[c] = n0;
   if (sf1) p.fuB[1].data[c] = n1;
   if (sf2) p.fuB[2].data[c] = n2;
   if (sb0) { p.B[0].data[c] = b0; p.fwH[0].data[c] = b0; }
   if (sb1) { p.B[1].data[c] = b1; p.fwH[1].data[c] = b1; }
   if (sb2) { p.B[2].data[c] = b2; p.fwH[2].data[c] = b2; }
+}
+
+// Whether the H variant chosen for `axes` reads the plane's x coefficients (every
+// variant but the plain one and the z-only one does).
+__device__ __forceinline__ bool h_needs_plane(int axes) { return axes != 0 && axes != 4; }
+
+// One cell of the H half: masks, the variant for the warp's memberships, zero_metal_B.
+// `axes` bit 0/1/2: the warp touches the x/y/z memberships (0 on the fast path).
+template <bool PML>
+__device__ __forceinline__ void h_cell(const StepParams& p, const HColumn& col, const HPlane& pl,
+                                       int axes, int first_step, int i, int j, int k, int c,
+                                       float cx, float cy, float cz, const float h_old[3],
+                                       float h_new[3]) {
+  if (p.met[0] && i == 0) cx = 0.f;
+  if (p.met[1] && j == 0) cy = 0.f;
+  if (p.met[2] && k == 0) cz = 0.f;
+  // zero_metal_B clears the wall samples after the curl update; a wall cell is never
+  // in its component's own-axis membership, so there H is B and clearing H_new after
+  // the accumulation is the same word.
+  if (!PML || axes == 0) {
+    h_cell_v<false, false, false>(p, col, pl, first_step, c, cx, cy, cz, h_old, h_new);
+  } else {
+    // The z-only edge (the two z-edge warps of every interior row) is the commonest slow
+    // case; every other mix takes the general variant.
+    if (axes == 4) h_cell_v<false, false, true>(p, col, pl, first_step, c, cx, cy, cz, h_old, h_new);
+    else h_cell_v<true, true, true>(p, col, pl, first_step, c, cx, cy, cz, h_old, h_new);
+  }
+  if (p.met[0] && i == 0) h_new[0] = 0.f;
+  if (p.met[1] && j == 0) h_new[1] = 0.f;
+  if (p.met[2] && k == 0) h_new[2] = 0.f;
 }
 
 // E half: D lives on the integer lattice transversally (curl tables), E on the half
@@ -257,43 +286,34 @@ __device__ __forceinline__ void e_plane_coefficients(const StepParams& p, int i,
 }
 
 // D from its curls, the source deposit, zero_metal_D, E (update_E) and P (update_P)
-// for one cell at offset c. `slow` selects the PML arithmetic.
-template <bool PML>
-__device__ __forceinline__ void e_cell(const StepParams& p, const EColumn& col, const EPlane& pl,
-                                       bool slow, int parity, int i, int j, int k, int c,
-                                       float cx, float cy, float cz, float d[3], const float inv[3]) {
+// for one cell at offset c, for a warp that may touch the x (SX), y (SY) and z (SZ)
+// memberships (x: Dx own, Dy dsigu, Dz dsig; y: Dx dsig, Dy own, Dz dsigu; z: Dx dsigu,
+// Dy dsig, Dz own). <false, false, false> is the plain update.
+template <bool SX, bool SY, bool SZ>
+__device__ __forceinline__ void e_cell_v(const StepParams& p, const EColumn& col, const EPlane& pl,
+                                         int parity, int i, int j, int k, int c, float cx,
+                                         float cy, float cz, float d[3], const float inv[3]) {
   const bool wx = p.met[0] && i == 0, wy = p.met[1] && j == 0, wz = p.met[2] && k == 0;
   if (wy || wz) cx = 0.f;
   if (wx || wz) cy = 0.f;
   if (wx || wy) cz = 0.f;
-  bool sf0 = false, sf1 = false, sf2 = false, sw0 = false, sw1 = false, sw2 = false;
-  float fw0 = 0.f, fw1 = 0.f, fw2 = 0.f, e0 = 0.f, e1 = 0.f, e2 = 0.f;
+  const bool sf0 = SZ && col.f0, sf1 = SX && pl.f1, sf2 = SY && col.f2;
+  const bool sw0 = SX && pl.w0, sw1 = SY && col.w1, sw2 = SZ && col.w2;
+  // Loads: every auxiliary word of the cell, before any store.
+  const float u0 = sf0 ? p.fuD[0].data[c] : 0.f;
+  const float u1 = sf1 ? p.fuD[1].data[c] : 0.f;
+  const float u2 = sf2 ? p.fuD[2].data[c] : 0.f;
+  const float fw0 = sw0 ? p.fwE[0].data[c] : 0.f;
+  const float fw1 = sw1 ? p.fwE[1].data[c] : 0.f;
+  const float fw2 = sw2 ? p.fwE[2].data[c] : 0.f;
+  const float e0 = sw0 ? p.E[0][c] : 0.f;
+  const float e1 = sw1 ? p.E[1][c] : 0.f;
+  const float e2 = sw2 ? p.E[2][c] : 0.f;
+  // Dx: dsig y, dsigu z; Dy: dsig z, dsigu x; Dz: dsig x, dsigu y.
   float n0 = 0.f, n1 = 0.f, n2 = 0.f;
-  if (PML && slow) {
-    sf0 = col.f0; sf1 = pl.f1; sf2 = col.f2;
-    sw0 = pl.w0; sw1 = col.w1; sw2 = col.w2;
-    // Loads: every auxiliary word of the cell, before any store.
-    const float u0 = sf0 ? p.fuD[0].data[c] : 0.f;
-    const float u1 = sf1 ? p.fuD[1].data[c] : 0.f;
-    const float u2 = sf2 ? p.fuD[2].data[c] : 0.f;
-    fw0 = sw0 ? p.fwE[0].data[c] : 0.f;
-    fw1 = sw1 ? p.fwE[1].data[c] : 0.f;
-    fw2 = sw2 ? p.fwE[2].data[c] : 0.f;
-    e0 = sw0 ? p.E[0][c] : 0.f;
-    e1 = sw1 ? p.E[1][c] : 0.f;
-    e2 = sw2 ? p.E[2][c] : 0.f;
-    // Dx: dsig y, dsigu z; Dy: dsig z, dsigu x; Dz: dsig x, dsigu y.
-    if (sf0) { n0 = (col.kms_y * u0 - cx) * col.sinv_y; d[0] = ((col.kms_z * d[0] + n0) - u0) * col.sinv_z; }
-    else d[0] = (col.kms_y * d[0] - cx) * col.sinv_y;
-    if (sf1) { n1 = (col.kms_z * u1 - cy) * col.sinv_z; d[1] = ((pl.kms_x * d[1] + n1) - u1) * pl.sinv_x; }
-    else d[1] = (col.kms_z * d[1] - cy) * col.sinv_z;
-    if (sf2) { n2 = (pl.kms_x * u2 - cz) * pl.sinv_x; d[2] = ((col.kms_y * d[2] + n2) - u2) * col.sinv_y; }
-    else d[2] = (pl.kms_x * d[2] - cz) * pl.sinv_x;
-  } else {
-    d[0] = d[0] - cx;
-    d[1] = d[1] - cy;
-    d[2] = d[2] - cz;
-  }
+  d[0] = curl_form<SY, SZ>(d[0], cx, sf0, u0, col.kms_y, col.sinv_y, col.kms_z, col.sinv_z, n0);
+  d[1] = curl_form<SZ, SX>(d[1], cy, sf1, u1, col.kms_z, col.sinv_z, pl.kms_x, pl.sinv_x, n1);
+  d[2] = curl_form<SX, SY>(d[2], cz, sf2, u2, pl.kms_x, pl.sinv_x, col.kms_y, col.sinv_y, n2);
   // Electric sources at t + dt/2: f = float(double(f) - A), point by point in order.
   if (p.nsrc > 0 && i >= p.src_box[0] && i < p.src_box[1] && j >= p.src_box[2] &&
       j < p.src_box[3] && k >= p.src_box[4] && k < p.src_box[5]) {
@@ -328,17 +348,15 @@ __device__ __forceinline__ void e_cell(const StepParams& p, const EColumn& col, 
   w[1] = inv[1] * w[1];
   w[2] = inv[2] * w[2];
   float e[3] = {w[0], w[1], w[2]};
-  if (PML && slow) {
-    if (sw0) e[0] = e0 + (pl.kps_xh * w[0] - pl.kms_xh * fw0);
-    if (sw1) e[1] = e1 + (col.kps_yh * w[1] - col.kms_yh * fw1);
-    if (sw2) e[2] = e2 + (col.kps_zh * w[2] - col.kms_zh * fw2);
-    if (sf0) p.fuD[0].data[c] = n0;
-    if (sf1) p.fuD[1].data[c] = n1;
-    if (sf2) p.fuD[2].data[c] = n2;
-    if (sw0) p.fwE[0].data[c] = w[0];
-    if (sw1) p.fwE[1].data[c] = w[1];
-    if (sw2) p.fwE[2].data[c] = w[2];
-  }
+  if (sw0) e[0] = e0 + (pl.kps_xh * w[0] - pl.kms_xh * fw0);
+  if (sw1) e[1] = e1 + (col.kps_yh * w[1] - col.kms_yh * fw1);
+  if (sw2) e[2] = e2 + (col.kps_zh * w[2] - col.kms_zh * fw2);
+  if (sf0) p.fuD[0].data[c] = n0;
+  if (sf1) p.fuD[1].data[c] = n1;
+  if (sf2) p.fuD[2].data[c] = n2;
+  if (sw0) p.fwE[0].data[c] = w[0];
+  if (sw1) p.fwE[1].data[c] = w[1];
+  if (sw2) p.fwE[2].data[c] = w[2];
   p.D[0][c] = d[0];
   p.D[1][c] = d[1];
   p.D[2][c] = d[2];
@@ -366,6 +384,23 @@ __device__ __forceinline__ void e_cell(const StepParams& p, const EColumn& col, 
   if (bad && p.status != nullptr) atomicOr(p.status, 1);
 }
 
+template <bool PML>
+__device__ __forceinline__ void e_cell(const StepParams& p, const EColumn& col, const EPlane& pl,
+                                       int axes, int parity, int i, int j, int k, int c, float cx,
+                                       float cy, float cz, float d[3], const float inv[3]) {
+  if (!PML) axes = 0;
+  switch (axes) {
+    case 0: e_cell_v<false, false, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv); break;
+    case 1: e_cell_v<true, false, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv); break;
+    case 2: e_cell_v<false, true, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv); break;
+    case 3: e_cell_v<true, true, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv); break;
+    case 4: e_cell_v<false, false, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv); break;
+    case 5: e_cell_v<true, false, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv); break;
+    case 6: e_cell_v<false, true, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv); break;
+    default: e_cell_v<true, true, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv); break;
+  }
+}
+
 // ------------------------------------------------------------------------------------
 // Generic kernels: plain loads, one thread per (y, z) column marching over x.
 template <bool PML>
@@ -389,10 +424,12 @@ __global__ void __launch_bounds__(256, 5) h_generic(const __grid_constant__ Step
   const int col = j * sy + k;
   int c = i0 * sx + col;
   HColumn hcol = {};
-  bool warp_slow = false;
+  int col_axes = 0;  // bit 1: the warp touches the y memberships, bit 2: the z ones
   if (PML) {
     hcol = h_column(p, j, k);
-    warp_slow = __any_sync(__activemask(), hcol.f0 || hcol.f2 || hcol.b1 || hcol.b2);
+    const unsigned lanes = __activemask();
+    col_axes = (__any_sync(lanes, hcol.f2 || hcol.b1) ? 2 : 0) |
+               (__any_sync(lanes, hcol.f0 || hcol.b2) ? 4 : 0);
   }
   float ey = Ey[c];
   float ez = Ez[c];
@@ -420,13 +457,13 @@ __global__ void __launch_bounds__(256, 5) h_generic(const __grid_constant__ Step
     const float h_old[3] = {p.H[0][c], p.H[1][c], p.H[2][c]};
     float h_new[3];
     HPlane pl = {};
-    bool slow = false;
+    int axes = 0;
     if (PML) {
       pl = h_plane(p, i);
-      slow = warp_slow || pl.f1 || pl.b0;
-      if (slow) h_plane_coefficients(p, i, pl);
+      axes = col_axes | ((pl.f1 || pl.b0) ? 1 : 0);
+      if (h_needs_plane(axes)) h_plane_coefficients(p, i, pl);
     }
-    h_cell<PML>(p, hcol, pl, slow, first_step, i, j, k, c, cx, cy, cz, h_old, h_new);
+    h_cell<PML>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, h_old, h_new);
     p.H[0][c] = h_new[0];
     p.H[1][c] = h_new[1];
     p.H[2][c] = h_new[2];
@@ -454,10 +491,12 @@ __global__ void __launch_bounds__(256, 5) e_generic(const __grid_constant__ Step
   const int col = j * sy + k;
   int c = i0 * sx + col;
   EColumn ecol = {};
-  bool warp_slow = false;
+  int col_axes = 0;  // bit 1: the warp touches the y memberships, bit 2: the z ones
   if (PML) {
     ecol = e_column(p, j, k);
-    warp_slow = __any_sync(__activemask(), ecol.f0 || ecol.f2 || ecol.w1 || ecol.w2);
+    const unsigned lanes = __activemask();
+    col_axes = (__any_sync(lanes, ecol.f2 || ecol.w1) ? 2 : 0) |
+               (__any_sync(lanes, ecol.f0 || ecol.w2) ? 4 : 0);
   }
   float hy_xm = 0.f, hz_xm = 0.f;
   {
@@ -487,13 +526,13 @@ __global__ void __launch_bounds__(256, 5) e_generic(const __grid_constant__ Step
     float d[3] = {p.D[0][c], p.D[1][c], p.D[2][c]};
     const float inv[3] = {__ldg(p.inv_eps[0] + c), __ldg(p.inv_eps[1] + c), __ldg(p.inv_eps[2] + c)};
     EPlane pl = {};
-    bool slow = false;
+    int axes = 0;
     if (PML) {
       pl = e_plane(p, i);
-      slow = warp_slow || pl.f1 || pl.w0;
-      if (slow) e_plane_coefficients(p, i, pl);
+      axes = col_axes | ((pl.f1 || pl.w0) ? 1 : 0);
+      if (axes & 1) e_plane_coefficients(p, i, pl);
     }
-    e_cell<PML>(p, ecol, pl, slow, parity, i, j, k, c, cx, cy, cz, d, inv);
+    e_cell<PML>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, d, inv);
     hy_xm = hy;
     hz_xm = hz;
   }
@@ -621,10 +660,11 @@ __global__ void __launch_bounds__(kThreads, 2) h_tile(const __grid_constant__ St
   const int j = j0 + ty, k = k0 + tz;
   const bool live = j < p.ny && k < p.nz;
   HColumn hcol = {};
-  bool warp_slow = false;
+  int col_axes = 0;  // bit 1: the warp touches the y memberships, bit 2: the z ones
   if (PML) {
     if (live) hcol = h_column(p, j, k);
-    warp_slow = __any_sync(0xffffffffu, live && (hcol.f0 || hcol.f2 || hcol.b1 || hcol.b2));
+    col_axes = (__any_sync(0xffffffffu, live && (hcol.f2 || hcol.b1)) ? 2 : 0) |
+               (__any_sync(0xffffffffu, live && (hcol.f0 || hcol.b2)) ? 4 : 0);
   }
   const bool wrap_y = live && !p.met[1] && j + 1 == p.ny;
   const bool wrap_z = live && !p.met[2] && k + 1 == p.nz;
@@ -658,13 +698,13 @@ __global__ void __launch_bounds__(kThreads, 2) h_tile(const __grid_constant__ St
       const float h_old[3] = {Hown[o], Hown[kBoxOwn / 4 + o], Hown[2 * kBoxOwn / 4 + o]};
       float h_new[3];
       HPlane pl = {};
-      bool slow = false;
+      int axes = 0;
       if (PML) {
         pl = h_plane(p, i);
-        slow = warp_slow || pl.f1 || pl.b0;
-        if (slow) h_plane_coefficients(p, i, pl);
+        axes = col_axes | ((pl.f1 || pl.b0) ? 1 : 0);
+        if (h_needs_plane(axes)) h_plane_coefficients(p, i, pl);
       }
-      h_cell<PML>(p, hcol, pl, slow, first_step, i, j, k, c, cx, cy, cz, h_old, h_new);
+      h_cell<PML>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, h_old, h_new);
       p.H[0][c] = h_new[0];
       p.H[1][c] = h_new[1];
       p.H[2][c] = h_new[2];
@@ -733,10 +773,11 @@ __global__ void __launch_bounds__(kThreads, 2) e_tile(const __grid_constant__ St
   const int j = j0 + ty, k = k0 + tz;
   const bool live = j < p.ny && k < p.nz;
   EColumn ecol = {};
-  bool warp_slow = false;
+  int col_axes = 0;  // bit 1: the warp touches the y memberships, bit 2: the z ones
   if (PML) {
     if (live) ecol = e_column(p, j, k);
-    warp_slow = __any_sync(0xffffffffu, live && (ecol.f0 || ecol.f2 || ecol.w1 || ecol.w2));
+    col_axes = (__any_sync(0xffffffffu, live && (ecol.f2 || ecol.w1)) ? 2 : 0) |
+               (__any_sync(0xffffffffu, live && (ecol.f0 || ecol.w2)) ? 4 : 0);
   }
   const bool wrap_y = live && !p.met[1] && j == 0;
   const bool wrap_z = live && !p.met[2] && k == 0;
@@ -772,13 +813,13 @@ __global__ void __launch_bounds__(kThreads, 2) e_tile(const __grid_constant__ St
       const float inv[3] = {own[inv0 * (kBoxOwn / 4) + o], own[inv1 * (kBoxOwn / 4) + o],
                             own[inv2 * (kBoxOwn / 4) + o]};
       EPlane pl = {};
-      bool slow = false;
+      int axes = 0;
       if (PML) {
         pl = e_plane(p, i);
-        slow = warp_slow || pl.f1 || pl.w0;
-        if (slow) e_plane_coefficients(p, i, pl);
+        axes = col_axes | ((pl.f1 || pl.w0) ? 1 : 0);
+        if (axes & 1) e_plane_coefficients(p, i, pl);
       }
-      e_cell<PML>(p, ecol, pl, slow, parity, i, j, k, c, cx, cy, cz, d, inv);
+      e_cell<PML>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, d, inv);
     }
     __syncthreads();  // the stage of plane i - 1 is read by everyone
     if (abort_flag) {

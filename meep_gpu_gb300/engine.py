@@ -42,7 +42,7 @@ SOURCE_WINDOW = 4096
 # Kernel choices the autotuner times: (family, block_z, block_y, x_chunk); family 1 is
 # the tile kernels (block shape fixed at 64 x 8, x_chunk used), family 0 the generic ones.
 AUTOTUNE_CANDIDATES = ((0, 32, 4, 4), (0, 32, 8, 4), (0, 32, 4, 8), (0, 64, 2, 8),
-                       (1, 64, 8, 4), (1, 64, 8, 8))
+                       (0, 16, 8, 4), (0, 16, 16, 4), (1, 64, 8, 4), (1, 64, 8, 8))
 _AUTOTUNE_CACHE: Dict[tuple, Tuple[int, int, int, int]] = {}
 
 

@@ -184,6 +184,64 @@ void mgb_destroy(mgb_sim* sim);
 /* Copy the last error message of the calling thread into buf (NUL-terminated). */
 int mgb_last_error(char* buf, size_t size);
 
+/* ---- Batched stepping of independent simulations (serving) ---------------------------
+ * No reference counterpart: the reference steps one simulation per process
+ * (meep_gpu/driver.py:3419, one FdtdDriver per GPU, README.md:127). A batch is a slot
+ * table over plans created with mgb_create; every step of mgb_batch_step advances each
+ * active slot that has steps left by one, in kernels shared by all slots (one CTA per
+ * work item), so simulations of different sizes step together. A slot's words equal
+ * those of the same plan stepped alone. The caller owns every device array, the batch's
+ * tables included. */
+typedef struct mgb_batch mgb_batch;
+
+/* Bytes of the device buffer that holds a batch's tables: max_slots slots, max_work step
+ * items and max_dft_work monitor items (256 cells each). */
+size_t mgb_batch_bytes(int32_t max_slots, int32_t max_work, int32_t max_dft_work);
+
+/* Create a batch over a caller-allocated, 256-byte aligned device buffer of at least
+ * mgb_batch_bytes() bytes. */
+int mgb_batch_create(int32_t max_slots, int32_t max_work, int32_t max_dft_work,
+                     void* device_buffer, size_t bytes, mgb_batch** out);
+
+/* Set the batch's launch shape: block_z (a multiple of 32) x block_y cells per CTA,
+ * block_z * block_y <= 256, x_chunk x cells per step item. Takes effect at the next
+ * mgb_batch_commit. The default is 32 x 4 x 4. */
+int mgb_batch_set_shape(mgb_batch* batch, int32_t block_z, int32_t block_y, int32_t x_chunk);
+
+/* Put a plan in a slot, to run steps 0 .. end_step-1 from its arrays' current words
+ * (normally zero). words: device float64 [end_step][points] deposit words of its electric
+ * sources from step 0 (NULL if it has none); the plan's own mgb_set_source_words table is
+ * not used. At most 2 monitors of at most 512 frequencies. Takes effect at the next
+ * mgb_batch_commit; the plan and its arrays must outlive the slot's last queued step. */
+int mgb_batch_set_slot(mgb_batch* batch, int32_t slot, mgb_sim* sim, int64_t end_step,
+                       const double* words);
+
+/* Empty a slot (takes effect at the next mgb_batch_commit). */
+int mgb_batch_clear_slot(mgb_batch* batch, int32_t slot);
+
+/* Upload the changed slots and the rebuilt work lists on `stream` (stream-ordered after
+ * the batch steps queued before). */
+int mgb_batch_commit(mgb_batch* batch, void* stream);
+
+/* Queue nsteps batch steps on `stream`: plain launches (use_graph 0) or one replay of a
+ * CUDA graph of nsteps steps (use_graph 1), captured on first use and again only when
+ * nsteps, the stream or the launch shape change. Slots coming and going need no
+ * recapture: the captured launches' grid sizes are updated in the executable graph.
+ * Asynchronous; the slots' step counters advance on the host at once. */
+int mgb_batch_step(mgb_batch* batch, int32_t nsteps, int32_t use_graph, void* stream);
+
+/* Every slot's step once the queued batch steps have run (-1 for an empty slot) into
+ * steps[max_slots]. A slot has run all its steps when this equals its end_step; its
+ * results are in its arrays once the stream has passed the queued steps. No device
+ * access. */
+int mgb_batch_steps(mgb_batch* batch, int64_t* steps);
+
+/* Committed step items (which = 0) or monitor items (which = 1). */
+int64_t mgb_batch_items(mgb_batch* batch, int32_t which);
+
+/* Release the batch (never the caller's buffer or plans). */
+void mgb_batch_destroy(mgb_batch* batch);
+
 #ifdef __cplusplus
 }
 #endif

@@ -97,6 +97,21 @@ SIGNATURES = {
     "mgb_select_kernels": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "mgb_destroy": (None, [ctypes.c_void_p]),
     "mgb_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
+    "mgb_batch_bytes": (ctypes.c_size_t, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+    "mgb_batch_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                        ctypes.c_void_p, ctypes.c_size_t,
+                                        ctypes.POINTER(ctypes.c_void_p)]),
+    "mgb_batch_set_shape": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                           ctypes.c_int32]),
+    "mgb_batch_set_slot": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                                          ctypes.c_int64, ctypes.c_void_p]),
+    "mgb_batch_clear_slot": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "mgb_batch_commit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "mgb_batch_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                      ctypes.c_void_p]),
+    "mgb_batch_steps": (ctypes.c_int, [ctypes.c_void_p, c_int64_p]),
+    "mgb_batch_items": (ctypes.c_int64, [ctypes.c_void_p, ctypes.c_int32]),
+    "mgb_batch_destroy": (None, [ctypes.c_void_p]),
 }
 
 _LIB: Optional[ctypes.CDLL] = None

@@ -39,10 +39,12 @@
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <vector>
 
 namespace {
 
@@ -66,6 +68,7 @@ constexpr int kBoxOwn = kTileZ * kTileY * 4;  // 2048 bytes
 // ------------------------------------------------------------------------------------
 struct StepParams {
   int nx, ny, nz;
+  int pml;  // 1 when the run has an absorber (the PML memberships below are live)
   int met[3];
   float dtdx;
   const float* kms[2][3];
@@ -292,7 +295,8 @@ __device__ __forceinline__ void e_plane_coefficients(const StepParams& p, int i,
 template <bool SX, bool SY, bool SZ>
 __device__ __forceinline__ void e_cell_v(const StepParams& p, const EColumn& col, const EPlane& pl,
                                          int parity, int i, int j, int k, int c, float cx,
-                                         float cy, float cz, float d[3], const float inv[3]) {
+                                         float cy, float cz, float d[3], const float inv[3],
+                                         const double* words) {
   const bool wx = p.met[0] && i == 0, wy = p.met[1] && j == 0, wz = p.met[2] && k == 0;
   if (wy || wz) cx = 0.f;
   if (wx || wz) cy = 0.f;
@@ -320,7 +324,7 @@ __device__ __forceinline__ void e_cell_v(const StepParams& p, const EColumn& col
     for (int s = 0; s < p.nsrc; ++s) {
       if (p.src_cell[s] != c) continue;
       const int q = p.src_comp[s];
-      const double w = p.src_words[s];
+      const double w = words[s];
       if (q == 0) d[0] = __double2float_rn(__dsub_rn((double)d[0], w));
       else if (q == 1) d[1] = __double2float_rn(__dsub_rn((double)d[1], w));
       else d[2] = __double2float_rn(__dsub_rn((double)d[2], w));
@@ -387,30 +391,27 @@ __device__ __forceinline__ void e_cell_v(const StepParams& p, const EColumn& col
 template <bool PML>
 __device__ __forceinline__ void e_cell(const StepParams& p, const EColumn& col, const EPlane& pl,
                                        int axes, int parity, int i, int j, int k, int c, float cx,
-                                       float cy, float cz, float d[3], const float inv[3]) {
+                                       float cy, float cz, float d[3], const float inv[3],
+                                       const double* words) {
   if (!PML) axes = 0;
   switch (axes) {
-    case 0: e_cell_v<false, false, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv); break;
-    case 1: e_cell_v<true, false, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv); break;
-    case 2: e_cell_v<false, true, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv); break;
-    case 3: e_cell_v<true, true, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv); break;
-    case 4: e_cell_v<false, false, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv); break;
-    case 5: e_cell_v<true, false, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv); break;
-    case 6: e_cell_v<false, true, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv); break;
-    default: e_cell_v<true, true, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv); break;
+    case 0: e_cell_v<false, false, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words); break;
+    case 1: e_cell_v<true, false, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words); break;
+    case 2: e_cell_v<false, true, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words); break;
+    case 3: e_cell_v<true, true, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words); break;
+    case 4: e_cell_v<false, false, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words); break;
+    case 5: e_cell_v<true, false, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words); break;
+    case 6: e_cell_v<false, true, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words); break;
+    default: e_cell_v<true, true, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words); break;
   }
 }
 
 // ------------------------------------------------------------------------------------
 // Generic kernels: plain loads, one thread per (y, z) column marching over x.
+// One thread's column (j, k) of the H half over planes [i0, i1).
 template <bool PML>
-__global__ void __launch_bounds__(256, 5) h_generic(const __grid_constant__ StepParams p,
-                                                 int first_step, int xchunk) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  if (k >= p.nz || j >= p.ny) return;
-  const int i0 = blockIdx.z * xchunk;
-  const int i1 = min(i0 + xchunk, p.nx);
+__device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i0, int i1,
+                                        int first_step) {
   const int sx = p.ny * p.nz;
   const int sy = p.nz;
   const float* Ex = p.E[0];
@@ -472,14 +473,10 @@ __global__ void __launch_bounds__(256, 5) h_generic(const __grid_constant__ Step
   }
 }
 
+// One thread's column (j, k) of the E half over planes [i0, i1).
 template <bool PML>
-__global__ void __launch_bounds__(256, 5) e_generic(const __grid_constant__ StepParams p, int parity,
-                                                 int xchunk) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  if (k >= p.nz || j >= p.ny) return;
-  const int i0 = blockIdx.z * xchunk;
-  const int i1 = min(i0 + xchunk, p.nx);
+__device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i0, int i1,
+                                        int parity, const double* words) {
   const int sx = p.ny * p.nz;
   const int sy = p.nz;
   const float dtdx = p.dtdx;
@@ -532,10 +529,31 @@ __global__ void __launch_bounds__(256, 5) e_generic(const __grid_constant__ Step
       axes = col_axes | ((pl.f1 || pl.w0) ? 1 : 0);
       if (axes & 1) e_plane_coefficients(p, i, pl);
     }
-    e_cell<PML>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, d, inv);
+    e_cell<PML>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, d, inv, words);
     hy_xm = hy;
     hz_xm = hz;
   }
+}
+
+// Generic kernels: plain loads, one thread per (y, z) column marching over an x chunk.
+template <bool PML>
+__global__ void __launch_bounds__(256, 5) h_generic(const __grid_constant__ StepParams p,
+                                                    int first_step, int xchunk) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (k >= p.nz || j >= p.ny) return;
+  const int i0 = blockIdx.z * xchunk;
+  h_march<PML>(p, j, k, i0, min(i0 + xchunk, p.nx), first_step);
+}
+
+template <bool PML>
+__global__ void __launch_bounds__(256, 5) e_generic(const __grid_constant__ StepParams p, int parity,
+                                                    int xchunk) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (k >= p.nz || j >= p.ny) return;
+  const int i0 = blockIdx.z * xchunk;
+  e_march<PML>(p, j, k, i0, min(i0 + xchunk, p.nx), parity, p.src_words);
 }
 
 // ------------------------------------------------------------------------------------
@@ -819,7 +837,7 @@ __global__ void __launch_bounds__(kThreads, 2) e_tile(const __grid_constant__ St
         axes = col_axes | ((pl.f1 || pl.w0) ? 1 : 0);
         if (axes & 1) e_plane_coefficients(p, i, pl);
       }
-      e_cell<PML>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, d, inv);
+      e_cell<PML>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, d, inv, p.src_words);
     }
     __syncthreads();  // the stage of plane i - 1 is read by everyone
     if (abort_flag) {
@@ -871,10 +889,9 @@ __device__ float centred(const DftParams& p, int comp, int i, int j, int k) {
   return 0.5f * (r0 + r1);
 }
 
-__global__ void __launch_bounds__(256) dft_accumulate(const __grid_constant__ DftParams p,
-                                                      long long step) {
-  extern __shared__ float2 phase[];  // [0, nf): E phases, [nf, 2nf): H phases
-  const mgb_monitor& m = p.mon;
+// The float64-formed phases of one accumulation into shared memory: [0, nf) for E at
+// t = step*dt, [nf, 2nf) for H at t - dt/2 (the caller synchronises).
+__device__ __forceinline__ void dft_phases(const mgb_monitor& m, long long step, float2* phase) {
   const int nf = m.nfreq;
   const double t_e = (double)step * m.dt;
   const double t_h = t_e - 0.5 * m.dt;
@@ -886,11 +903,15 @@ __global__ void __launch_bounds__(256) dft_accumulate(const __grid_constant__ Df
     sincos(t_h * w, &s, &co);
     phase[nf + f] = make_float2((float)(co * m.scale), (float)(s * m.scale));
   }
-  __syncthreads();
+}
+
+// Accumulate one region cell of one monitor.
+__device__ __forceinline__ void dft_cell(const DftParams& p, const float2* phase, long long cell) {
+  const mgb_monitor& m = p.mon;
+  const int nf = m.nfreq;
   const int rx = m.region[1] - m.region[0], ry = m.region[3] - m.region[2],
             rz = m.region[5] - m.region[4];
   const long long cells = (long long)rx * ry * rz;
-  const long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (cell >= cells) return;
   const int rk = (int)(cell % rz);
   const int rj = (int)((cell / rz) % ry);
@@ -908,6 +929,14 @@ __global__ void __launch_bounds__(256) dft_accumulate(const __grid_constant__ Df
       *im = *im + ph[f].y * s;
     }
   }
+}
+
+__global__ void __launch_bounds__(256) dft_accumulate(const __grid_constant__ DftParams p,
+                                                      long long step) {
+  extern __shared__ float2 phase[];  // [0, nf): E phases, [nf, 2nf): H phases
+  dft_phases(p.mon, step, phase);
+  __syncthreads();
+  dft_cell(p, phase, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // Flux reduction, one block per frequency, float64 sums.
@@ -937,6 +966,104 @@ __global__ void __launch_bounds__(256) flux_reduce(const __grid_constant__ mgb_m
     __syncthreads();
   }
   if (threadIdx.x == 0) out[f] = part[0];
+}
+
+// ------------------------------------------------------------------------------------
+// Batched stepping of many independent simulations (serving). A slot table holds every
+// admitted simulation's step parameters; a work list cuts every active slot's grid into
+// (slot, z tile, y tile, x chunk) items of the batch's launch shape, one CTA each. A CTA
+// copies its slot's parameters into shared memory and runs the generic column march on
+// them, so a slot computes the words of the same simulation stepped alone.
+//
+// Step counters live on the host: every running slot advances exactly one step per batch
+// step, so before each call of G steps the host uploads each slot's step at the start
+// (n0), and launch t of the G computes n = n0 + t. A slot whose n has reached its end is
+// skipped by every kernel, so one captured graph of G steps is replayed while slots
+// finish at different steps, and slots coming and going change only the tables, the lists
+// and the launches' grid sizes. Three launches per step: H half, E half, monitors.
+//
+// (Measured on GB300 against two other layouts of the same march: a resident grid
+// looping over the list needs 78-80 registers a thread and loses occupancy; the slot
+// table in constant memory, indexed by the CTA's slot, misses the constant cache. Both
+// stepped a 128^3 slot 10-15 % slower than this one.)
+constexpr int kSlotMonitors = 2;
+constexpr int kBatchMaxFreq = 512;
+constexpr int kDftItemCells = 256;
+
+struct SlotState {
+  long long end;        // the slot has run all its steps when n reaches end
+  const double* words;  // deposit words [end][nsrc] from step 0
+  int active;
+  int nmon;
+};
+
+struct BatchTables {
+  StepParams* params;  // [max_slots]
+  SlotState* state;    // [max_slots]
+  long long* n0;       // [max_slots] step of each slot at the first launch of a batch step call
+  DftParams* dft;      // [max_slots * kSlotMonitors]
+  int4* work;          // step items (slot, z tile, y tile, x chunk)
+  int4* dft_work;      // monitor items (slot * kSlotMonitors + monitor, cell block)
+  int* counts;         // [0] step items, [1] monitor items
+  int max_slots;
+  int xchunk;          // x cells per step item; the block is (z, y) cells
+};
+
+template <typename T>
+__device__ __forceinline__ void copy_to_shared(T* dst, const T* src) {
+  static_assert(sizeof(T) % 4 == 0, "copied as 32-bit words");
+  const int* from = reinterpret_cast<const int*>(src);
+  int* to = reinterpret_cast<int*>(dst);
+  const int n = (int)(sizeof(T) / 4);
+  const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+  for (int i = tid; i < n; i += blockDim.x * blockDim.y) to[i] = from[i];
+}
+
+// Register budget as the generic kernels' (48 per thread): more costs occupancy the
+// column march needs. `t` is the launch's step within the batch step call.
+template <int PART>
+__global__ void __launch_bounds__(256, 5) step_batched(const __grid_constant__ BatchTables tb, int t) {
+  __shared__ StepParams sp;
+  if ((int)blockIdx.x >= tb.counts[0]) return;
+  const int4 w = tb.work[blockIdx.x];
+  // The parameter copy and the slot's state are fetched together (one round trip).
+  copy_to_shared(&sp, &tb.params[w.x]);
+  const SlotState st = tb.state[w.x];
+  const long long n = tb.n0[w.x] + t;
+  if (!st.active || n >= st.end) return;  // uniform over the CTA
+  __syncthreads();
+  const int k = w.y * (int)blockDim.x + (int)threadIdx.x;
+  const int j = w.z * (int)blockDim.y + (int)threadIdx.y;
+  if (k >= sp.nz || j >= sp.ny) return;
+  const int i0 = w.w * tb.xchunk;
+  const int i1 = min(i0 + tb.xchunk, sp.nx);
+  if (PART == 0) {
+    if (sp.pml) h_march<true>(sp, j, k, i0, i1, n == 0);
+    else h_march<false>(sp, j, k, i0, i1, n == 0);
+  } else {
+    const double* words = st.words + n * sp.nsrc;
+    if (sp.pml) e_march<true>(sp, j, k, i0, i1, (int)(n & 1), words);
+    else e_march<false>(sp, j, k, i0, i1, (int)(n & 1), words);
+  }
+}
+
+__global__ void __launch_bounds__(kDftItemCells) dft_batched(const __grid_constant__ BatchTables tb, int t) {
+  __shared__ float2 phase[2 * kBatchMaxFreq];
+  __shared__ DftParams dp;
+  if ((int)blockIdx.x >= tb.counts[1]) return;
+  const int4 w = tb.dft_work[blockIdx.x];
+  const int slot = w.x / kSlotMonitors;
+  copy_to_shared(&dp, &tb.dft[w.x]);
+  const SlotState st = tb.state[slot];
+  const long long n = tb.n0[slot] + t;
+  if (!st.active || n >= st.end) return;
+  __syncthreads();
+  // Monitors are due after step n when (n + 1) is a multiple of their decimation.
+  const long long post = n + 1;
+  if (post % dp.mon.decimation != 0) return;
+  dft_phases(dp.mon, post, phase);
+  __syncthreads();
+  dft_cell(dp, phase, (long long)w.y * kDftItemCells + threadIdx.x);
 }
 
 }  // namespace
@@ -1148,6 +1275,7 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
   sim->desc = d;
   StepParams& p = sim->step;
   p.nx = d.nx; p.ny = d.ny; p.nz = d.nz;
+  p.pml = d.pml_active ? 1 : 0;
   for (int a = 0; a < 3; ++a) p.met[a] = d.metallic[a] ? 1 : 0;
   p.dtdx = d.dtdx;
   for (int l = 0; l < 2; ++l)
@@ -1322,5 +1450,333 @@ int mgb_select_kernels(mgb_sim* sim, int32_t family) {
 }
 
 void mgb_destroy(mgb_sim* sim) { delete sim; }
+
+}  // extern "C"
+
+// ======================================================================================
+// Batched stepping ABI
+struct mgb_batch {
+  int max_slots = 0, max_work = 0, max_dft_work = 0;
+  int block_z = 32, block_y = 4;
+  BatchTables dev = {};
+  std::vector<StepParams> params;
+  std::vector<SlotState> state;
+  std::vector<long long> n0;  // each slot's next step (host-tracked)
+  std::vector<DftParams> dft;
+  std::vector<unsigned char> dirty;
+  std::vector<int4> work, dwork;
+  int nwork = 0, ndwork = 0;
+  bool work_dirty = true;
+  cudaGraphExec_t graph = nullptr;
+  cudaGraph_t graph_src = nullptr;          // kept: its kernel nodes are updated in place
+  std::vector<cudaGraphNode_t> step_nodes;  // H and E launches of every captured step
+  std::vector<cudaGraphNode_t> dft_nodes;
+  int graph_steps = 0;
+  int graph_shape[3] = {0, 0, 0};
+  int graph_grid[2] = {0, 0};
+  cudaStream_t graph_stream = nullptr;
+};
+
+namespace {
+
+size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+void batch_layout(int max_slots, int max_work, int max_dft_work, size_t offsets[7], size_t* total) {
+  size_t o = 0;
+  offsets[0] = o; o = align256(o + sizeof(StepParams) * max_slots);
+  offsets[1] = o; o = align256(o + sizeof(SlotState) * max_slots);
+  offsets[2] = o; o = align256(o + sizeof(long long) * max_slots);
+  offsets[3] = o; o = align256(o + sizeof(DftParams) * max_slots * kSlotMonitors);
+  offsets[4] = o; o = align256(o + sizeof(int4) * max_work);
+  offsets[5] = o; o = align256(o + sizeof(int4) * max_dft_work);
+  offsets[6] = o; o = align256(o + sizeof(int) * 2);
+  *total = o;
+}
+
+long long monitor_cells(const mgb_monitor& mon) {
+  return (long long)(mon.region[1] - mon.region[0]) * (mon.region[3] - mon.region[2]) *
+         (mon.region[5] - mon.region[4]);
+}
+
+void rebuild_work(mgb_batch* b) {
+  b->work.clear();
+  b->dwork.clear();
+  const int bz = b->block_z, by = b->block_y, xc = b->dev.xchunk;
+  for (int sl = 0; sl < b->max_slots; ++sl) {
+    const SlotState& st = b->state[sl];
+    if (!st.active) continue;
+    const StepParams& p = b->params[sl];
+    const int tz = (p.nz + bz - 1) / bz, ty = (p.ny + by - 1) / by, tx = (p.nx + xc - 1) / xc;
+    for (int x = 0; x < tx; ++x)
+      for (int y = 0; y < ty; ++y)
+        for (int z = 0; z < tz; ++z) b->work.push_back(make_int4(sl, z, y, x));
+    for (int m = 0; m < st.nmon; ++m) {
+      const int blocks = (int)((monitor_cells(b->dft[sl * kSlotMonitors + m].mon) + kDftItemCells - 1) /
+                               kDftItemCells);
+      for (int q = 0; q < blocks; ++q) b->dwork.push_back(make_int4(sl * kSlotMonitors + m, q, 0, 0));
+    }
+  }
+}
+
+// One CTA per item (at least one, so an empty list still launches validly).
+int step_grid(const mgb_batch* b) { return std::max(1, b->nwork); }
+int dft_grid(const mgb_batch* b) { return std::max(1, b->ndwork); }
+
+void batch_launch_step(mgb_batch* b, int t, cudaStream_t s) {
+  const dim3 block(b->block_z, b->block_y, 1);
+  step_batched<0><<<step_grid(b), block, 0, s>>>(b->dev, t);
+  step_batched<1><<<step_grid(b), block, 0, s>>>(b->dev, t);
+  dft_batched<<<dft_grid(b), kDftItemCells, 0, s>>>(b->dev, t);
+}
+
+void drop_graph(mgb_batch* b) {
+  if (b->graph != nullptr) cudaGraphExecDestroy(b->graph);
+  if (b->graph_src != nullptr) cudaGraphDestroy(b->graph_src);
+  b->graph = nullptr;
+  b->graph_src = nullptr;
+  b->step_nodes.clear();
+  b->dft_nodes.clear();
+}
+
+// Point the captured launches at the current list lengths (grid sizes only).
+int update_graph_grids(mgb_batch* b) {
+  const int grids[2] = {step_grid(b), dft_grid(b)};
+  if (grids[0] == b->graph_grid[0] && grids[1] == b->graph_grid[1]) return MGB_OK;
+  for (int which = 0; which < 2; ++which) {
+    for (cudaGraphNode_t node : which == 0 ? b->step_nodes : b->dft_nodes) {
+      cudaKernelNodeParams kp;
+      if (cudaGraphKernelNodeGetParams(node, &kp) != cudaSuccess) return launch_error("graph node params");
+      kp.gridDim = dim3(grids[which], 1, 1);
+      if (cudaGraphExecKernelNodeSetParams(b->graph, node, &kp) != cudaSuccess)
+        return launch_error("graph node update");
+    }
+  }
+  b->graph_grid[0] = grids[0];
+  b->graph_grid[1] = grids[1];
+  return MGB_OK;
+}
+
+int capture_graph(mgb_batch* b, int nsteps, cudaStream_t s) {
+  drop_graph(b);
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    return launch_error("batch graph capture");
+  for (int t = 0; t < nsteps; ++t) batch_launch_step(b, t, s);
+  if (cudaStreamEndCapture(s, &b->graph_src) != cudaSuccess) {
+    b->graph_src = nullptr;
+    return launch_error("batch graph capture end");
+  }
+  const cudaError_t err = cudaGraphInstantiate(&b->graph, b->graph_src, 0);
+  if (err != cudaSuccess) {
+    b->graph = nullptr;
+    drop_graph(b);
+    return fail(MGB_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(err));
+  }
+  size_t count = 0;
+  cudaGraphGetNodes(b->graph_src, nullptr, &count);
+  std::vector<cudaGraphNode_t> nodes(count);
+  if (count > 0) cudaGraphGetNodes(b->graph_src, nodes.data(), &count);
+  const void* h_fn = reinterpret_cast<const void*>(step_batched<0>);
+  const void* e_fn = reinterpret_cast<const void*>(step_batched<1>);
+  const void* d_fn = reinterpret_cast<const void*>(dft_batched);
+  for (cudaGraphNode_t node : nodes) {
+    cudaGraphNodeType type;
+    if (cudaGraphNodeGetType(node, &type) != cudaSuccess || type != cudaGraphNodeTypeKernel) continue;
+    cudaKernelNodeParams kp;
+    if (cudaGraphKernelNodeGetParams(node, &kp) != cudaSuccess) continue;
+    if (kp.func == h_fn || kp.func == e_fn) b->step_nodes.push_back(node);
+    else if (kp.func == d_fn) b->dft_nodes.push_back(node);
+  }
+  if ((int)b->step_nodes.size() != 2 * nsteps || (int)b->dft_nodes.size() != nsteps) {
+    drop_graph(b);
+    return fail(MGB_ERR_CUDA, "captured batch graph does not hold the expected launches");
+  }
+  b->graph_steps = nsteps;
+  b->graph_stream = s;
+  b->graph_shape[0] = b->block_z;
+  b->graph_shape[1] = b->block_y;
+  b->graph_shape[2] = b->dev.xchunk;
+  b->graph_grid[0] = step_grid(b);
+  b->graph_grid[1] = dft_grid(b);
+  return MGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t mgb_batch_bytes(int32_t max_slots, int32_t max_work, int32_t max_dft_work) {
+  size_t offsets[7], total;
+  batch_layout(max_slots, max_work, max_dft_work, offsets, &total);
+  return total;
+}
+
+int mgb_batch_create(int32_t max_slots, int32_t max_work, int32_t max_dft_work, void* device_buffer,
+                     size_t bytes, mgb_batch** out) {
+  if (out == nullptr) return fail(MGB_ERR_ARGUMENT, "null output handle");
+  *out = nullptr;
+  if (device_buffer == nullptr || max_slots < 1 || max_work < 1 || max_dft_work < 1)
+    return fail(MGB_ERR_ARGUMENT, "a batch needs slots, work capacities and a device buffer");
+  size_t offsets[7], total;
+  batch_layout(max_slots, max_work, max_dft_work, offsets, &total);
+  if (bytes < total) return fail(MGB_ERR_ARGUMENT, "batch device buffer is smaller than mgb_batch_bytes()");
+  if ((reinterpret_cast<uintptr_t>(device_buffer) & 255u) != 0)
+    return fail(MGB_ERR_ARGUMENT, "batch device buffer must be 256-byte aligned");
+  mgb_batch* b = new (std::nothrow) mgb_batch();
+  if (b == nullptr) return fail(MGB_ERR_ARGUMENT, "host allocation of the batch failed");
+  unsigned char* base = static_cast<unsigned char*>(device_buffer);
+  b->max_slots = max_slots;
+  b->max_work = max_work;
+  b->max_dft_work = max_dft_work;
+  b->dev.params = reinterpret_cast<StepParams*>(base + offsets[0]);
+  b->dev.state = reinterpret_cast<SlotState*>(base + offsets[1]);
+  b->dev.n0 = reinterpret_cast<long long*>(base + offsets[2]);
+  b->dev.dft = reinterpret_cast<DftParams*>(base + offsets[3]);
+  b->dev.work = reinterpret_cast<int4*>(base + offsets[4]);
+  b->dev.dft_work = reinterpret_cast<int4*>(base + offsets[5]);
+  b->dev.counts = reinterpret_cast<int*>(base + offsets[6]);
+  b->dev.max_slots = max_slots;
+  b->dev.xchunk = 4;
+  b->params.assign(max_slots, StepParams{});
+  b->state.assign(max_slots, SlotState{});
+  b->n0.assign(max_slots, 0);
+  b->dft.assign((size_t)max_slots * kSlotMonitors, DftParams{});
+  b->dirty.assign(max_slots, 1);
+  *out = b;
+  return MGB_OK;
+}
+
+int mgb_batch_set_shape(mgb_batch* b, int32_t block_z, int32_t block_y, int32_t x_chunk) {
+  if (b == nullptr) return fail(MGB_ERR_ARGUMENT, "null batch");
+  if (block_z < 1 || block_y < 1 || x_chunk < 1 || block_z * block_y > 256 || block_z % 32 != 0)
+    return fail(MGB_ERR_ARGUMENT, "batch shape needs block_z a multiple of 32, block_z*block_y <= 256");
+  b->block_z = block_z;
+  b->block_y = block_y;
+  b->dev.xchunk = x_chunk;
+  b->work_dirty = true;
+  return MGB_OK;
+}
+
+int mgb_batch_set_slot(mgb_batch* b, int32_t slot, mgb_sim* sim, int64_t end_step, const double* words) {
+  if (b == nullptr || sim == nullptr) return fail(MGB_ERR_ARGUMENT, "null batch or plan");
+  if (slot < 0 || slot >= b->max_slots) return fail(MGB_ERR_ARGUMENT, "slot out of range");
+  if (end_step < 1) return fail(MGB_ERR_ARGUMENT, "a slot needs at least one step");
+  if (sim->step.nsrc > 0 && words == nullptr) return fail(MGB_ERR_ARGUMENT, "the slot's sources need deposit words");
+  if (sim->desc.nmonitors > kSlotMonitors)
+    return fail(MGB_ERR_UNSUPPORTED, "a batched slot holds at most " + std::to_string(kSlotMonitors) + " monitors");
+  for (int m = 0; m < sim->desc.nmonitors; ++m) {
+    if (sim->desc.monitors[m].decimation < 1) return fail(MGB_ERR_ARGUMENT, "monitor decimation must be >= 1");
+    if (sim->desc.monitors[m].nfreq > kBatchMaxFreq)
+      return fail(MGB_ERR_UNSUPPORTED, "a batched monitor holds at most " + std::to_string(kBatchMaxFreq) +
+                                           " frequencies");
+  }
+  b->params[slot] = sim->step;
+  b->params[slot].src_words = nullptr;
+  SlotState st = {};
+  st.end = end_step;
+  st.words = words;
+  st.active = 1;
+  st.nmon = sim->desc.nmonitors;
+  b->state[slot] = st;
+  b->n0[slot] = 0;
+  for (int m = 0; m < sim->desc.nmonitors; ++m) {
+    DftParams& q = b->dft[slot * kSlotMonitors + m];
+    q.nx = sim->step.nx; q.ny = sim->step.ny; q.nz = sim->step.nz;
+    for (int a = 0; a < 3; ++a) q.met[a] = sim->step.met[a];
+    for (int c = 0; c < 3; ++c) { q.E[c] = sim->step.E[c]; q.H[c] = sim->step.H[c]; }
+    q.mon = sim->desc.monitors[m];
+  }
+  b->dirty[slot] = 1;
+  b->work_dirty = true;
+  return MGB_OK;
+}
+
+int mgb_batch_clear_slot(mgb_batch* b, int32_t slot) {
+  if (b == nullptr) return fail(MGB_ERR_ARGUMENT, "null batch");
+  if (slot < 0 || slot >= b->max_slots) return fail(MGB_ERR_ARGUMENT, "slot out of range");
+  b->state[slot] = SlotState{};
+  b->n0[slot] = 0;
+  b->dirty[slot] = 1;
+  b->work_dirty = true;
+  return MGB_OK;
+}
+
+int mgb_batch_commit(mgb_batch* b, void* stream) {
+  if (b == nullptr) return fail(MGB_ERR_ARGUMENT, "null batch");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (b->work_dirty) {
+    rebuild_work(b);
+    if ((int)b->work.size() > b->max_work || (int)b->dwork.size() > b->max_dft_work)
+      return fail(MGB_ERR_RANGE, "the admitted slots need " + std::to_string(b->work.size()) + " step and " +
+                                     std::to_string(b->dwork.size()) + " monitor items; the batch holds " +
+                                     std::to_string(b->max_work) + " and " + std::to_string(b->max_dft_work));
+  }
+  // Pageable host sources: each copy is staged before the call returns, so the host
+  // vectors may change afterwards. Stream order puts them after the steps queued before.
+  for (int sl = 0; sl < b->max_slots; ++sl) {
+    if (!b->dirty[sl]) continue;
+    cudaMemcpyAsync(b->dev.params + sl, &b->params[sl], sizeof(StepParams), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(b->dev.state + sl, &b->state[sl], sizeof(SlotState), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(b->dev.dft + (size_t)sl * kSlotMonitors, &b->dft[(size_t)sl * kSlotMonitors],
+                    sizeof(DftParams) * kSlotMonitors, cudaMemcpyHostToDevice, s);
+    b->dirty[sl] = 0;
+  }
+  if (b->work_dirty) {
+    b->nwork = (int)b->work.size();
+    b->ndwork = (int)b->dwork.size();
+    if (b->nwork > 0)
+      cudaMemcpyAsync(b->dev.work, b->work.data(), sizeof(int4) * b->nwork, cudaMemcpyHostToDevice, s);
+    if (b->ndwork > 0)
+      cudaMemcpyAsync(b->dev.dft_work, b->dwork.data(), sizeof(int4) * b->ndwork, cudaMemcpyHostToDevice, s);
+    const int counts[2] = {b->nwork, b->ndwork};
+    cudaMemcpyAsync(b->dev.counts, counts, sizeof counts, cudaMemcpyHostToDevice, s);
+    b->work_dirty = false;
+  }
+  return launch_error("batch commit");
+}
+
+int mgb_batch_step(mgb_batch* b, int32_t nsteps, int32_t use_graph, void* stream) {
+  if (b == nullptr || nsteps < 0) return fail(MGB_ERR_ARGUMENT, "bad batch step");
+  if (b->work_dirty) return fail(MGB_ERR_ARGUMENT, "slots changed since the last mgb_batch_commit");
+  if (nsteps == 0) return MGB_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // Each slot's step at the first launch (staged copy: the host vector advances below).
+  cudaMemcpyAsync(b->dev.n0, b->n0.data(), sizeof(long long) * b->max_slots, cudaMemcpyHostToDevice, s);
+  if (!use_graph) {
+    for (int t = 0; t < nsteps; ++t) batch_launch_step(b, t, s);
+    const int rc = launch_error("batch step");
+    if (rc != MGB_OK) return rc;
+  } else {
+    const bool same = b->graph != nullptr && b->graph_steps == nsteps && b->graph_stream == s &&
+                      b->graph_shape[0] == b->block_z && b->graph_shape[1] == b->block_y &&
+                      b->graph_shape[2] == b->dev.xchunk;
+    if (!same) {
+      const int rc = capture_graph(b, nsteps, s);
+      if (rc != MGB_OK) return rc;
+    }
+    const int rc = update_graph_grids(b);
+    if (rc != MGB_OK) return rc;
+    if (cudaGraphLaunch(b->graph, s) != cudaSuccess) return launch_error("batch graph launch");
+  }
+  for (int sl = 0; sl < b->max_slots; ++sl)
+    if (b->state[sl].active) b->n0[sl] = std::min<long long>(b->state[sl].end, b->n0[sl] + nsteps);
+  return MGB_OK;
+}
+
+int mgb_batch_steps(mgb_batch* b, int64_t* steps) {
+  if (b == nullptr || steps == nullptr) return fail(MGB_ERR_ARGUMENT, "null argument");
+  for (int sl = 0; sl < b->max_slots; ++sl) steps[sl] = b->state[sl].active ? b->n0[sl] : -1;
+  return MGB_OK;
+}
+
+int64_t mgb_batch_items(mgb_batch* b, int32_t which) {
+  if (b == nullptr) return -1;
+  return which == 0 ? b->nwork : b->ndwork;
+}
+
+void mgb_batch_destroy(mgb_batch* b) {
+  if (b == nullptr) return;
+  drop_graph(b);
+  delete b;
+}
 
 }  // extern "C"

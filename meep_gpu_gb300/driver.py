@@ -248,6 +248,17 @@ class FdtdDriver:
             self.set_epsilon(1.0)
 
     def _freeze(self) -> None:
+        self.freeze()
+
+    def freeze(self, stream=None, autotune: bool = True):
+        """Fix the configuration and make the device state (once); returns the engine.
+
+        ``stream`` is the CUDA stream the engine steps and reads on (default: the current
+        stream at each call); ``autotune=False`` keeps the default kernel choice, for
+        simulations stepped by a batch rather than by this driver.
+        """
+        if self.engine is not None:
+            return self.engine
         import torch
 
         from .engine import Engine
@@ -255,7 +266,13 @@ class FdtdDriver:
         device = torch.device("cuda", self.gpu_id)
         self.engine = Engine(self.grid, self.pml, self._inv_eps, self._poles, self._sources,
                              list(self._flux_monitors) + list(self._dft_monitors), device=device,
-                             launch_shape=self.launch_shape, kernels=self.kernels)
+                             stream=stream, launch_shape=self.launch_shape, kernels=self.kernels,
+                             autotune=autotune)
+        return self.engine
+
+    @property
+    def sources(self):
+        return list(self._sources)
 
     # --- stepping -------------------------------------------------------------------
     @property

@@ -399,14 +399,27 @@ class Engine:
             return b
         raise ValueError(f"unknown component {name!r}")
 
-    def flux_spectrum(self, monitor: FluxMonitor) -> np.ndarray:
+    def queue_flux_spectrum(self, monitor: FluxMonitor):
+        """Queue one flux reduction and its read-back into pinned host memory on the
+        engine's stream; returns ``(host, event)``. Once ``event`` has completed, the
+        spectrum is ``host.numpy() * monitor.measure * monitor.weight``."""
         index = self.monitors.index(monitor)
         _, _, weights = self.monitor_tensors[index]
-        out = torch.zeros(monitor.num_frequencies, dtype=torch.float64, device=self.device)
-        _lib.check(self.lib, self.lib.mgb_flux_spectrum(self.handle, index, weights.data_ptr(),
-                                                        out.data_ptr(), self._stream_handle()))
-        sums = out.cpu().numpy()
-        return sums * monitor.measure * monitor.weight
+        stream = self.stream if self.stream is not None else torch.cuda.current_stream(self.device)
+        with torch.cuda.stream(stream):  # zero fill, reduction and read-back in stream order
+            out = torch.zeros(monitor.num_frequencies, dtype=torch.float64, device=self.device)
+            _lib.check(self.lib, self.lib.mgb_flux_spectrum(self.handle, index, weights.data_ptr(),
+                                                            out.data_ptr(), stream.cuda_stream))
+            host = torch.empty(monitor.num_frequencies, dtype=torch.float64, pin_memory=True)
+            host.copy_(out, non_blocking=True)
+            event = torch.cuda.Event()
+            event.record(stream)
+        return host, event
+
+    def flux_spectrum(self, monitor: FluxMonitor) -> np.ndarray:
+        host, event = self.queue_flux_spectrum(monitor)
+        event.synchronize()
+        return host.numpy() * monitor.measure * monitor.weight
 
     def close(self) -> None:
         if getattr(self, "handle", None) is not None and self.handle.value:

@@ -365,13 +365,70 @@ class Source:
         return current(self.waveform, t, self.grid.dt)
 
 
+# Current sequences from step 0, per waveform and time step: every simulation of a served
+# stream with the same source spectrum and resolution shares one.
+_CURRENT_CACHE: Dict[tuple, np.ndarray] = {}
+_CURRENT_CACHE_STEPS = 1 << 20
+
+
+def _waveform_key(waveform) -> Optional[tuple]:
+    if isinstance(waveform, GaussianWaveform):
+        return ("gaussian", waveform.frequency, waveform.fwidth, waveform.start_time, waveform.cutoff)
+    if isinstance(waveform, ContinuousWaveform):
+        return ("continuous", waveform.frequency, waveform.start_time, waveform.end_time,
+                waveform.width, waveform.slowness)
+    return None  # a caller's function may not be pure: never cached
+
+
+def _currents(waveform, dt: float, first: int, steps: int) -> np.ndarray:
+    out = np.empty((steps, 2), dtype=np.float64)
+    for row in range(steps):
+        n = first + row
+        out[row] = current(waveform, n * dt + 0.5 * dt, dt)
+    return out
+
+
+def current_sequence(waveform, dt: float, first: int, steps: int) -> np.ndarray:
+    """Currents ``(re, im)`` of steps ``first .. first+steps-1``, evaluated at ``n*dt + dt/2``
+    (MEEP's ``calc_sources(time() + dt/2)`` before the D half), shape ``(steps, 2)``."""
+    key = _waveform_key(waveform)
+    if key is None or first + steps > _CURRENT_CACHE_STEPS:
+        return _currents(waveform, dt, first, steps)
+    key = key + (dt,)
+    table = _CURRENT_CACHE.get(key)
+    have = 0 if table is None else len(table)
+    if have < first + steps:
+        grown = _currents(waveform, dt, have, first + steps - have)
+        table = grown if table is None else np.concatenate([table, grown])
+        _CURRENT_CACHE[key] = table
+    return table[first:first + steps]
+
+
 def deposit_words(sources: Sequence[Source], first_step: int, steps: int, dt: float) -> np.ndarray:
     """Float64 subtrahends ``A[step][point]`` for steps ``first_step .. first_step+steps-1``.
 
-    The electric current of step ``n`` is evaluated at ``n*dt + dt/2`` (MEEP's
-    ``calc_sources(time() + dt/2)`` before the D half). Points are laid out source by
-    source in table order, the order the device deposits them.
+    ``A = ((amp_re*c_re) - (amp_im*c_im))*dt`` with each product and the difference
+    rounded on its own (separate array operations), ``+0`` where the current is bitwise
+    ``(+0, +0)``. Points are laid out source by source in table order, the order the
+    device deposits them.
     """
+    count = sum(len(s.cells) for s in sources)
+    out = np.zeros((steps, count), dtype=np.float64)
+    column = 0
+    for source in sources:
+        seq = current_sequence(source.waveform, source.grid.dt, first_step, steps)
+        c_re, c_im = seq[:, 0], seq[:, 1]
+        plus_zero = ((c_re == 0.0) & ~np.signbit(c_re)) & ((c_im == 0.0) & ~np.signbit(c_im))
+        for amp in source.amps:
+            value = ((amp.real * c_re) - (amp.imag * c_im)) * dt
+            value[plus_zero] = 0.0
+            out[:, column] = value
+            column += 1
+    return out
+
+
+def deposit_words_scalar(sources: Sequence[Source], first_step: int, steps: int, dt: float) -> np.ndarray:
+    """The per-step, per-point form of :func:`deposit_words` (kept to check the array form)."""
     count = sum(len(s.cells) for s in sources)
     out = np.zeros((steps, count), dtype=np.float64)
     for row in range(steps):
@@ -383,11 +440,7 @@ def deposit_words(sources: Sequence[Source], first_step: int, steps: int, dt: fl
             plus_zero = (c[0] == 0.0 and math.copysign(1.0, c[0]) > 0
                          and c[1] == 0.0 and math.copysign(1.0, c[1]) > 0)
             for amp in source.amps:
-                if plus_zero:
-                    out[row, column] = 0.0
-                else:
-                    re = amp.real * c[0] - amp.imag * c[1]
-                    out[row, column] = re * dt
+                out[row, column] = 0.0 if plus_zero else (amp.real * c[0] - amp.imag * c[1]) * dt
                 column += 1
     return out
 

@@ -16,7 +16,7 @@ HEADER = ROOT / "include" / "meepgb.h"
 
 def declared_symbols():
     text = HEADER.read_text()
-    return sorted(set(re.findall(r"^\s*(?:int|void)\s+(mgb_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|void|size_t|int64_t)\s+(mgb_\w+)\s*\(", text, re.M)))
 
 
 def test_library_loads_and_exports_every_declared_symbol():
@@ -40,6 +40,25 @@ def test_create_refuses_bad_descriptors_without_a_gpu():
     desc.nx, desc.ny, desc.nz = 1, 8, 8
     assert lib.mgb_create(ctypes.byref(desc), ctypes.byref(handle)) == -3
     assert "at least 2 cells" in _lib.last_error(lib)
+
+
+def test_batch_entry_points_refuse_bad_arguments_without_a_gpu():
+    lib = _lib.load()
+    small = lib.mgb_batch_bytes(1, 1, 1)
+    big = lib.mgb_batch_bytes(64, 100000, 20000)
+    assert small % 256 == 0 and big > small
+    handle = ctypes.c_void_p()
+    assert lib.mgb_batch_create(4, 16, 16, None, big, ctypes.byref(handle)) == -1
+    assert "device buffer" in _lib.last_error(lib)
+    # size and alignment are checked before any device call
+    assert lib.mgb_batch_create(4, 16, 16, 256, 8, ctypes.byref(handle)) == -1
+    assert "smaller than" in _lib.last_error(lib)
+    assert lib.mgb_batch_create(4, 16, 16, 257, big, ctypes.byref(handle)) == -1
+    assert "aligned" in _lib.last_error(lib)
+    assert lib.mgb_batch_set_slot(None, 0, None, 10, None) == -1
+    assert lib.mgb_batch_set_shape(None, 32, 4, 4) == -1
+    assert lib.mgb_batch_items(None, 0) == -1
+    lib.mgb_batch_destroy(None)
 
 
 PROBE = r"""

@@ -57,3 +57,22 @@ def test_one_rank_membership_runs():
     rows = slab_index(record, np.arange(24))
     assert list(rows[:7]) == [-1, 0, 1, 2, 3, 4, -1]
     assert list(rows[19:]) == [-1, 5, 6, 7, 8]
+
+
+def test_array_deposit_words_equal_the_per_step_form():
+    from meep_gpu_gb300 import sources as S
+
+    grid = Grid((3.2, 3.2, 3.2), 10)
+    srcs = [
+        S.Source(grid, "Ez", (-0.8, 0.0, 0.0), (0, 0, 0), S.GaussianWaveform(0.15, 0.1)),
+        S.Source(grid, "Ex", (0.05, 0.1, 0.0), (0.3, 0, 0), S.ContinuousWaveform(0.4, width=2.0),
+                 amplitude=0.7 - 0.3j),
+        S.Source(grid, "Ey", (0.0, 0.0, 0.3), (0, 0, 0),
+                 S.CustomWaveform(lambda t: np.exp(-((t - 3.0) ** 2)) * (1 + 0.5j))),
+    ]
+    S._CURRENT_CACHE.clear()
+    for first, steps in ((0, 300), (250, 400), (0, 900), (1000, 17)):
+        fast = S.deposit_words(srcs, first, steps, grid.dt)
+        slow = S.deposit_words_scalar(srcs, first, steps, grid.dt)
+        assert fast.shape == slow.shape
+        assert np.array_equal(fast.view(np.uint64), slow.view(np.uint64)), (first, steps)

@@ -346,6 +346,8 @@ def bench_serving(device, args):
     request from host arrays and end with its flux spectrum on the host. Before timing,
     one short request per side runs through both arms (kernel choices, graph capture).
     """
+    import torch
+
     from meep_gpu_gb300 import serving
     requests = serving.make_stream(args.serving, rate=40.0, seed=0)
     warm = [serving.Request(-1 - i, s, 4.0, 0.3 * s, 70, 0.0) for i, s in enumerate(serving.SIDES)]

@@ -184,6 +184,45 @@ void mgb_destroy(mgb_sim* sim);
 /* Copy the last error message of the calling thread into buf (NUL-terminated). */
 int mgb_last_error(char* buf, size_t size);
 
+/* ---- Tensor-core DFT accumulation ---------------------------------------------------
+ * A monitor in buffered mode stores the cell-centred samples of up to MGB_DFT_DEPTH
+ * decimated steps and adds them to its accumulators in one contraction on the tcgen05
+ * tensor cores (TF32 with the 3xTF32 split, float32 accuracy; phases formed in float64
+ * as the step-by-step path forms them). Replaces DFTMonitor.update / FluxMonitor.update
+ * (meep_gpu/dft.py:2197, :3031) for K steps at once; the words differ from the
+ * step-by-step sums only by float32 rounding order. */
+#define MGB_DFT_DEPTH 32
+#define MGB_DFT_MAX_FREQ 512
+
+/* Bytes of the phase-table scratch a contraction of nfreq frequencies needs (0 when nfreq
+ * is outside 1..MGB_DFT_MAX_FREQ). */
+size_t mgb_dft_scratch_bytes(int32_t nfreq);
+
+/* Switch monitor `monitor` to buffered mode: samples is a device float32 buffer of
+ * MGB_DFT_DEPTH x (ncomp * cells) words, scratch at least mgb_dft_scratch_bytes(nfreq)
+ * bytes (both 16-byte aligned, owned by the caller, one scratch may serve every monitor
+ * of the plan). samples == NULL switches back to step-by-step accumulation. Refused
+ * while the monitor holds buffered samples. */
+int mgb_set_dft_buffer(mgb_sim* sim, int32_t monitor, float* samples, void* scratch,
+                       size_t scratch_bytes);
+
+/* Add every buffered sample to its monitor's accumulators (mgb_flux_spectrum does this
+ * for its monitor). Call before reading accumulators. Asynchronous on `stream`. */
+int mgb_dft_flush(mgb_sim* sim, void* stream);
+
+/* Samples a monitor holds buffered (-1 for a bad argument). */
+int32_t mgb_dft_pending(mgb_sim* sim, int32_t monitor);
+
+/* One contraction: acc[2f + 0][n] += sum_k cos(w_f t_k) * scale * samples[k * ld + n],
+ * acc[2f + 1][n] += the same with sin, for n < ncols, k < nsamples <= MGB_DFT_DEPTH,
+ * t_k = (first_step + k * step_stride) * dt (less dt/2 when half_step_back), w = omega
+ * (device float64 [nfreq]); acc is device float32 [2 nfreq][ncols]. scratch: device, at
+ * least mgb_dft_scratch_bytes(nfreq) bytes, rewritten by every call. Asynchronous. */
+int mgb_dft_contract(const float* samples, int64_t ld, int64_t ncols, int32_t nsamples,
+                     const double* omega, int32_t nfreq, int64_t first_step, int32_t step_stride,
+                     double dt, int32_t half_step_back, double scale, float* acc, void* scratch,
+                     size_t scratch_bytes, void* stream);
+
 /* ---- Batched stepping of independent simulations (serving) ---------------------------
  * No reference counterpart: the reference steps one simulation per process
  * (meep_gpu/driver.py:3419, one FdtdDriver per GPU, README.md:127). A batch is a slot

@@ -18,6 +18,8 @@ MGB_ABI_VERSION = 1
 MGB_MAX_POLES = 4
 MGB_MAX_MONITORS = 16
 MGB_MAX_MONITOR_COMPONENTS = 6
+MGB_DFT_DEPTH = 32
+MGB_DFT_MAX_FREQ = 512
 
 MGB_OK = 0
 ERROR_NAMES = {-1: "MGB_ERR_ARGUMENT", -2: "MGB_ERR_CUDA", -3: "MGB_ERR_UNSUPPORTED",
@@ -97,6 +99,15 @@ SIGNATURES = {
     "mgb_select_kernels": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "mgb_destroy": (None, [ctypes.c_void_p]),
     "mgb_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
+    "mgb_dft_scratch_bytes": (ctypes.c_size_t, [ctypes.c_int32]),
+    "mgb_set_dft_buffer": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_size_t]),
+    "mgb_dft_flush": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "mgb_dft_pending": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32]),
+    "mgb_dft_contract": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
+                                        ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,
+                                        ctypes.c_double, ctypes.c_int32, ctypes.c_double, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "mgb_batch_bytes": (ctypes.c_size_t, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     "mgb_batch_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                         ctypes.c_void_p, ctypes.c_size_t,

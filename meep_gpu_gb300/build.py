@@ -1,7 +1,7 @@
 """Build recipe of the CUDA library ``libmeepgb.so`` (sm_103a, in-tree).
 
-One translation unit compiled by nvcc straight into a shared object next to this
-file. ``-fmad=false`` is part of the numerics contract: no multiply-add may be
+Two translation units (the stepping library and the tensor-core DFT contraction)
+compiled by nvcc straight into a shared object next to this file. ``-fmad=false`` is part of the numerics contract: no multiply-add may be
 contracted, so every float32 word matches the reference's separately rounded
 operations.
 """
@@ -16,7 +16,8 @@ from pathlib import Path
 
 PACKAGE = Path(__file__).resolve().parent
 ROOT = PACKAGE.parent
-SOURCES = [PACKAGE / "csrc" / "meepgb.cu"]
+SOURCES = [PACKAGE / "csrc" / "meepgb.cu", PACKAGE / "csrc" / "dft_tc.cu"]
+HEADERS = [PACKAGE / "csrc" / "dft_tc.cuh"]
 LIBRARY = PACKAGE / "libmeepgb.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -35,7 +36,7 @@ def stale() -> bool:
     if not LIBRARY.exists():
         return True
     built = LIBRARY.stat().st_mtime
-    inputs = SOURCES + [ROOT / "include" / "meepgb.h", Path(__file__)]
+    inputs = SOURCES + HEADERS + [ROOT / "include" / "meepgb.h", Path(__file__)]
     return any(p.stat().st_mtime > built for p in inputs)
 
 

@@ -1,0 +1,285 @@
+// Tensor-core DFT contraction: acc[2 nfreq x N] += P[2 nfreq x K] . S[K x N] per
+// component, on the tcgen05 tensor cores (kind::tf32, accumulator in tensor memory),
+// with the 3xTF32 split for float32 accuracy. See dft_tc.cuh for the interface.
+//
+// Reference counterpart: the per-step accumulation of DFTMonitor.update /
+// FluxMonitor.update (meep_gpu/dft.py:2197, :3031), which adds phase * sample into every
+// accumulator word at each decimated step; here K such steps are buffered and added in
+// one pass, so the accumulators are read and written once per K samples.
+//
+// One CTA (four warps) owns a 256-column tile of one component: it stages the samples
+// (K = 32 rows) in shared memory as TF32 high and low parts, then for each 128-row tile
+// of phases stages the phase rows the same way, one thread issues the 12 MMAs
+// (4 K-slices x 3 products) into a 128 x 256 float32 accumulator in tensor memory, and
+// every warp reads its 32 lanes back (tcgen05.ld) and adds them to the accumulators in
+// global memory. Operands use the canonical K-major layout without swizzle.
+#include "dft_tc.cuh"
+
+#include <cstdint>
+
+namespace mgbdft {
+namespace {
+
+constexpr int kRows = 128;           // M per tile = tensor-memory lanes
+constexpr int kCols = 256;           // N per tile = tensor-memory columns
+constexpr int kThreads = 128;        // warp w reads lanes 32w .. 32w + 31
+constexpr int kSlices = kDepth / 8;  // kind::tf32 takes K = 8 per MMA
+// K-major without swizzle: core matrices of 8 rows x 16 bytes (4 elements). In one K
+// slice (8 elements, 32 bytes a row) the two core matrices of a row group are 128 bytes
+// apart (leading byte offset) and consecutive 8-row groups 256 bytes apart (stride
+// byte offset); slice j of a tile starts j * rows * 32 bytes in.
+constexpr unsigned kLBO = 128;
+constexpr unsigned kSBO = 256;
+constexpr int kSliceA = kRows * 32;
+constexpr int kSliceB = kCols * 32;
+constexpr int kTileA = kSliceA * kSlices;  // 16 KB
+constexpr int kTileB = kSliceB * kSlices;  // 32 KB
+constexpr int kSmemBytes = 2 * kTileB + 2 * kTileA + 64;
+// Instruction descriptor: D float32 (bits 4-5 = 1), A and B TF32 (bits 7-9, 10-12 = 2),
+// both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+constexpr unsigned kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((unsigned)(kCols >> 3) << 17) |
+                            ((unsigned)(kRows >> 4) << 24);
+static_assert(kDepth % 8 == 0, "K slices of 8");
+static_assert(kSmemBytes <= 227 * 1024, "shared memory");
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ int kmajor_offset(int r, int k, int slice_bytes) {
+  return (k >> 3) * slice_bytes + (r >> 3) * (int)kSBO + ((k >> 2) & 1) * (int)kLBO + (r & 7) * 16 +
+         (k & 3) * 4;
+}
+
+// Shared-memory matrix descriptor: start address, leading and stride byte offsets (each
+// >> 4), descriptor version 1 at bit 46, no swizzle.
+__device__ __forceinline__ unsigned long long smem_desc(unsigned addr) {
+  return (unsigned long long)((addr >> 4) & 0x3FFFu) |
+         ((unsigned long long)((kLBO >> 4) & 0x3FFFu) << 16) |
+         ((unsigned long long)((kSBO >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ float to_tf32(float x) {
+  unsigned r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void tmem_alloc(unsigned* slot, unsigned ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+               "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(unsigned taddr, unsigned ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void fence_before_sync() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_after_sync() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void mma_tf32(unsigned tmem_d, unsigned long long a, unsigned long long b,
+                                         unsigned accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(unsigned long long* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(unsigned taddr, unsigned (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+      "%12, %13, %14, %15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Wait for phase `parity` of the MMA barrier for at most ~1 s of wall time.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  unsigned long long start, now;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(start));
+  for (;;) {
+    for (int spin = 0; spin < 256; ++spin)
+      if (mbar_try_wait(bar, parity)) return true;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+    if (now - start > 1000000000ull) return false;
+  }
+}
+
+__device__ __forceinline__ int rows_of(int nfreq) { return ((2 * nfreq + kRows - 1) / kRows) * kRows; }
+
+__global__ void __launch_bounds__(256) table_kernel(const double* __restrict__ omega, int nfreq,
+                                                    long long first_post, int stride, double dt,
+                                                    int half_back, double scale, int nsamples,
+                                                    float* __restrict__ table) {
+  const int mpad = rows_of(nfreq);
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= mpad * kDepth) return;
+  const int m = idx / kDepth, k = idx % kDepth;
+  const int f = m >> 1;
+  float v = 0.f;
+  if (f < nfreq && k < nsamples) {
+    // the same float64 expressions as the step-by-step phases
+    const long long post = first_post + (long long)k * stride;
+    const double t_e = (double)post * dt;
+    const double t = half_back ? t_e - 0.5 * dt : t_e;
+    double s, co;
+    sincos(t * omega[f], &s, &co);
+    v = (m & 1) ? (float)(s * scale) : (float)(co * scale);
+  }
+  table[idx] = v;
+}
+
+__global__ void __launch_bounds__(kThreads, 1) contract_kernel(const __grid_constant__ Contraction c) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char* b_hi = smem;
+  unsigned char* b_lo = smem + kTileB;
+  unsigned char* a_hi = smem + 2 * kTileB;
+  unsigned char* a_lo = a_hi + kTileA;
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(a_lo + kTileA);
+  unsigned* tmem_slot = reinterpret_cast<unsigned*>(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int q = blockIdx.y;
+  const long long n0 = (long long)blockIdx.x * kCols;
+
+  if (warp == 0) tmem_alloc(tmem_slot, kCols);
+  if (tid == 0) mbar_init(bar);
+  // Samples: rows k < nsamples of this component's columns [n0, n0 + 256), zero beyond.
+  const float* src = c.samples + c.sample_off[q];
+  for (int idx = tid; idx < kDepth * kCols; idx += kThreads) {
+    const int k = idx / kCols, n = idx % kCols;
+    float v = 0.f;
+    if (k < c.nsamples && n0 + n < c.ncols) v = src[(long long)k * c.ld + n0 + n];
+    const float h = to_tf32(v);
+    const float l = to_tf32(v - h);
+    const int off = kmajor_offset(n, k, kSliceB);
+    *reinterpret_cast<float*>(b_hi + off) = h;
+    *reinterpret_cast<float*>(b_lo + off) = l;
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const unsigned tmem = *tmem_slot;
+  const int mpad = rows_of(c.nfreq);
+  const int mrows = 2 * c.nfreq;
+  float* acc = c.acc + c.acc_off[q];
+  unsigned parity = 0;
+  for (int mt = 0; mt < mpad / kRows; ++mt) {
+    for (int idx = tid; idx < kRows * kDepth; idx += kThreads) {
+      const int r = idx / kDepth, k = idx % kDepth;
+      const float v = c.table[(long long)(mt * kRows + r) * kDepth + k];
+      const float h = to_tf32(v);
+      const float l = to_tf32(v - h);
+      const int off = kmajor_offset(r, k, kSliceA);
+      *reinterpret_cast<float*>(a_hi + off) = h;
+      *reinterpret_cast<float*>(a_lo + off) = l;
+    }
+    // the generic-proxy stores must be visible to the tensor core's reads
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    fence_after_sync();
+    if (tid == 0) {
+#pragma unroll
+      for (int j = 0; j < kSlices; ++j) {
+        const unsigned long long ah = smem_desc(smem_u32(a_hi + j * kSliceA));
+        const unsigned long long al = smem_desc(smem_u32(a_lo + j * kSliceA));
+        const unsigned long long bh = smem_desc(smem_u32(b_hi + j * kSliceB));
+        const unsigned long long bl = smem_desc(smem_u32(b_lo + j * kSliceB));
+        mma_tf32(tmem, ah, bh, j > 0 ? 1u : 0u);
+        mma_tf32(tmem, ah, bl, 1u);
+        mma_tf32(tmem, al, bh, 1u);
+      }
+      mma_commit(bar);
+    }
+    bool ok = mbar_wait_bounded(bar, parity);
+    ok = __syncthreads_and(ok) != 0;
+    if (!ok) {
+      // The MMAs did not complete in time: report, give them one more bounded wait, and
+      // leave without touching the accumulators.
+      if (tid == 0 && c.status != nullptr) atomicOr(c.status, 4);
+      mbar_wait_bounded(bar, parity);
+      __syncthreads();
+      break;
+    }
+    parity ^= 1u;
+    fence_after_sync();
+    const int m = mt * kRows + warp * 32 + lane;
+    float* row = acc + (long long)m * c.acc_ld;
+#pragma unroll 1
+    for (int c0 = 0; c0 < kCols; c0 += 16) {
+      unsigned v[16];
+      tmem_ld16(tmem + ((unsigned)(warp * 32) << 16) + (unsigned)c0, v);
+      if (m < mrows) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const long long n = n0 + c0 + j;
+          if (n < c.ncols) row[n] = row[n] + __uint_as_float(v[j]);
+        }
+      }
+    }
+    fence_before_sync();
+    __syncthreads();  // tensor memory and the phase tile are free for the next tile
+  }
+  fence_after_sync();
+  if (warp == 0) tmem_dealloc(tmem, kCols);
+}
+
+}  // namespace
+
+int table_rows(int nfreq) { return ((2 * nfreq + kRows - 1) / kRows) * kRows; }
+
+size_t table_bytes(int nfreq) { return (size_t)table_rows(nfreq) * kDepth * sizeof(float); }
+
+cudaError_t launch_table(const double* omega, int nfreq, long long first_post, int stride, double dt,
+                         int half_back, double scale, int nsamples, float* table, cudaStream_t stream) {
+  const int total = table_rows(nfreq) * kDepth;
+  table_kernel<<<(total + 255) / 256, 256, 0, stream>>>(omega, nfreq, first_post, stride, dt, half_back,
+                                                        scale, nsamples, table);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_contract(const Contraction& c, cudaStream_t stream) {
+  if (c.ncols <= 0 || c.ncomp <= 0) return cudaSuccess;
+  // per device, so set at every launch (contractions are rare: one per kDepth samples)
+  const cudaError_t err =
+      cudaFuncSetAttribute(contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+  if (err != cudaSuccess) return err;
+  const dim3 grid((unsigned)((c.ncols + kCols - 1) / kCols), (unsigned)c.ncomp, 1);
+  contract_kernel<<<grid, kThreads, kSmemBytes, stream>>>(c);
+  return cudaGetLastError();
+}
+
+}  // namespace mgbdft

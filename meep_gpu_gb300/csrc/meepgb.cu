@@ -34,6 +34,7 @@
 //     16-byte row strides).
 
 #include "meepgb.h"
+#include "dft_tc.cuh"
 
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -939,6 +940,22 @@ __global__ void __launch_bounds__(256) dft_accumulate(const __grid_constant__ Df
   dft_cell(p, phase, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+// Buffered (tensor-core) accumulation: write one decimated step's cell-centred samples
+// of every component into row `row` of the monitor's sample buffer [depth][ncomp * cells].
+__global__ void __launch_bounds__(256) dft_sample(const __grid_constant__ DftParams p, float* row) {
+  const mgb_monitor& m = p.mon;
+  const int rx = m.region[1] - m.region[0], ry = m.region[3] - m.region[2],
+            rz = m.region[5] - m.region[4];
+  const long long cells = (long long)rx * ry * rz;
+  const long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= cells) return;
+  const int rk = (int)(cell % rz);
+  const int rj = (int)((cell / rz) % ry);
+  const int ri = (int)(cell / ((long long)ry * rz));
+  const int i = m.region[0] + ri, j = m.region[2] + rj, k = m.region[4] + rk;
+  for (int q = 0; q < m.ncomp; ++q) row[(long long)q * cells + cell] = centred(p, m.comp[q], i, j, k);
+}
+
 // Flux reduction, one block per frequency, float64 sums.
 __global__ void __launch_bounds__(256) flux_reduce(const __grid_constant__ mgb_monitor m,
                                                    const float* __restrict__ weights,
@@ -1084,6 +1101,14 @@ struct mgb_sim {
   int block_y = 4;
   int xchunk = 4;        // generic kernels
   int tile_xchunk = 8;   // tile kernels
+  // Monitors in buffered (tensor-core) mode: samples [kDepth][ncomp * cells], the phase
+  // table scratch, and the host-tracked fill of the buffer.
+  struct DftBuffer {
+    float* samples = nullptr;
+    float* table = nullptr;
+    int count = 0;              // samples buffered since the last contraction
+    long long first_post = 0;   // the step after which sample 0 was taken
+  } dbuf[MGB_MAX_MONITORS];
 };
 
 namespace {
@@ -1328,6 +1353,42 @@ int mgb_set_source_words(mgb_sim* sim, const double* words, int64_t first_step, 
 
 namespace {
 
+// Add a monitor's buffered samples to its accumulators: one phase table and one
+// contraction launch for its E components (sampled at post * dt), then the same for its
+// H components (at post * dt - dt / 2). The table scratch is reused in stream order.
+int flush_monitor(mgb_sim* sim, int m, cudaStream_t s) {
+  mgb_sim::DftBuffer& buf = sim->dbuf[m];
+  if (buf.samples == nullptr || buf.count == 0) return MGB_OK;
+  const mgb_monitor& mon = sim->desc.monitors[m];
+  const long long cells = (long long)(mon.region[1] - mon.region[0]) * (mon.region[3] - mon.region[2]) *
+                          (mon.region[5] - mon.region[4]);
+  for (int half_back = 0; half_back < 2; ++half_back) {
+    mgbdft::Contraction c = {};
+    c.samples = buf.samples;
+    c.ld = (long long)mon.ncomp * cells;
+    c.ncols = cells;
+    c.nsamples = buf.count;
+    c.acc = mon.acc;
+    c.acc_ld = cells;
+    c.nfreq = mon.nfreq;
+    c.table = buf.table;
+    c.status = sim->step.status;
+    for (int q = 0; q < mon.ncomp; ++q) {
+      if ((mon.comp[q] >= 3) != (half_back == 1)) continue;
+      c.sample_off[c.ncomp] = (long long)q * cells;
+      c.acc_off[c.ncomp] = (long long)q * 2 * mon.nfreq * cells;
+      ++c.ncomp;
+    }
+    if (c.ncomp == 0) continue;
+    if (mgbdft::launch_table(mon.omega, mon.nfreq, buf.first_post, mon.decimation, mon.dt, half_back,
+                             mon.scale, buf.count, buf.table, s) != cudaSuccess ||
+        mgbdft::launch_contract(c, s) != cudaSuccess)
+      return launch_error("tensor-core DFT contraction");
+  }
+  buf.count = 0;
+  return MGB_OK;
+}
+
 // Launches of one step, split by part so mgb_step and mgb_launch share them.
 int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s) {
   StepParams& p = sim->step;
@@ -1371,6 +1432,16 @@ int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s) {
     const long long cells = (long long)(mon.region[1] - mon.region[0]) *
                             (mon.region[3] - mon.region[2]) * (mon.region[5] - mon.region[4]);
     const unsigned blocks = (unsigned)((cells + 255) / 256);
+    mgb_sim::DftBuffer& buf = sim->dbuf[m];
+    if (buf.samples != nullptr) {
+      if (buf.count == 0) buf.first_post = post;
+      dft_sample<<<blocks, 256, 0, s>>>(q, buf.samples + (long long)buf.count * mon.ncomp * cells);
+      if (++buf.count == mgbdft::kDepth) {
+        const int rc = flush_monitor(sim, m, s);
+        if (rc != MGB_OK) return rc;
+      }
+      continue;
+    }
     const size_t smem = (size_t)mon.nfreq * 2 * sizeof(float2);
     dft_accumulate<<<blocks, 256, smem, s>>>(q, post);
   }
@@ -1429,8 +1500,47 @@ int mgb_flux_spectrum(mgb_sim* sim, int32_t monitor, const float* weights, doubl
   if (m.ncomp != 4 || m.comp[0] > 2 || m.comp[1] > 2 || m.comp[2] < 3 || m.comp[3] < 3) {
     return fail(MGB_ERR_ARGUMENT, "monitor is not a flux plane (Ea, Eb, Ha, Hb)");
   }
+  const int rc = flush_monitor(sim, monitor, static_cast<cudaStream_t>(stream));
+  if (rc != MGB_OK) return rc;
   flux_reduce<<<m.nfreq, 256, 0, static_cast<cudaStream_t>(stream)>>>(m, weights, out);
   return launch_error("flux reduction launch");
+}
+
+int mgb_set_dft_buffer(mgb_sim* sim, int32_t monitor, float* samples, void* scratch, size_t scratch_bytes) {
+  if (sim == nullptr) return fail(MGB_ERR_ARGUMENT, "null plan");
+  if (monitor < 0 || monitor >= sim->desc.nmonitors) return fail(MGB_ERR_ARGUMENT, "no such monitor");
+  mgb_sim::DftBuffer& buf = sim->dbuf[monitor];
+  if (buf.count != 0) return fail(MGB_ERR_ARGUMENT, "the monitor holds buffered samples: mgb_dft_flush first");
+  if (samples == nullptr) {
+    buf = mgb_sim::DftBuffer{};
+    return MGB_OK;
+  }
+  const mgb_monitor& m = sim->desc.monitors[monitor];
+  if (m.nfreq > mgbdft::kMaxFreq || m.ncomp > mgbdft::kMaxComps)
+    return fail(MGB_ERR_UNSUPPORTED, "tensor-core accumulation takes at most " + std::to_string(mgbdft::kMaxFreq) +
+                                         " frequencies");
+  if (scratch == nullptr || scratch_bytes < mgbdft::table_bytes(m.nfreq))
+    return fail(MGB_ERR_ARGUMENT, "scratch is smaller than mgb_dft_scratch_bytes(nfreq)");
+  if ((reinterpret_cast<uintptr_t>(samples) & 15u) != 0 || (reinterpret_cast<uintptr_t>(scratch) & 15u) != 0)
+    return fail(MGB_ERR_ARGUMENT, "sample buffer and scratch must be 16-byte aligned");
+  buf.samples = samples;
+  buf.table = static_cast<float*>(scratch);
+  buf.count = 0;
+  return MGB_OK;
+}
+
+int mgb_dft_flush(mgb_sim* sim, void* stream) {
+  if (sim == nullptr) return fail(MGB_ERR_ARGUMENT, "null plan");
+  for (int m = 0; m < sim->desc.nmonitors; ++m) {
+    const int rc = flush_monitor(sim, m, static_cast<cudaStream_t>(stream));
+    if (rc != MGB_OK) return rc;
+  }
+  return MGB_OK;
+}
+
+int32_t mgb_dft_pending(mgb_sim* sim, int32_t monitor) {
+  if (sim == nullptr || monitor < 0 || monitor >= sim->desc.nmonitors) return -1;
+  return sim->dbuf[monitor].count;
 }
 
 int mgb_uses_tiles(mgb_sim* sim) { return sim != nullptr && sim->tiles ? 1 : 0; }
@@ -1777,6 +1887,49 @@ void mgb_batch_destroy(mgb_batch* b) {
   if (b == nullptr) return;
   drop_graph(b);
   delete b;
+}
+
+}  // extern "C"
+
+// ======================================================================================
+// Tensor-core DFT contraction ABI
+extern "C" {
+
+size_t mgb_dft_scratch_bytes(int32_t nfreq) {
+  if (nfreq < 1 || nfreq > mgbdft::kMaxFreq) return 0;
+  return mgbdft::table_bytes(nfreq);
+}
+
+int mgb_dft_contract(const float* samples, int64_t ld, int64_t ncols, int32_t nsamples, const double* omega,
+                     int32_t nfreq, int64_t first_step, int32_t step_stride, double dt, int32_t half_step_back,
+                     double scale, float* acc, void* scratch, size_t scratch_bytes, void* stream) {
+  if (samples == nullptr || omega == nullptr || acc == nullptr || scratch == nullptr)
+    return fail(MGB_ERR_ARGUMENT, "null argument");
+  if (nfreq < 1 || nfreq > mgbdft::kMaxFreq)
+    return fail(MGB_ERR_ARGUMENT, "nfreq must be 1.." + std::to_string(mgbdft::kMaxFreq));
+  if (nsamples < 0 || nsamples > mgbdft::kDepth)
+    return fail(MGB_ERR_ARGUMENT, "nsamples must be 0.." + std::to_string(mgbdft::kDepth));
+  if (ncols < 0 || ld < ncols) return fail(MGB_ERR_ARGUMENT, "ld must be at least ncols");
+  if (scratch_bytes < mgbdft::table_bytes(nfreq))
+    return fail(MGB_ERR_ARGUMENT, "scratch is smaller than mgb_dft_scratch_bytes(nfreq)");
+  if (nsamples == 0 || ncols == 0) return MGB_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  float* table = static_cast<float*>(scratch);
+  mgbdft::Contraction c = {};
+  c.samples = samples;
+  c.ld = ld;
+  c.ncols = ncols;
+  c.nsamples = nsamples;
+  c.ncomp = 1;
+  c.acc = acc;
+  c.acc_ld = ncols;
+  c.nfreq = nfreq;
+  c.table = table;
+  if (mgbdft::launch_table(omega, nfreq, first_step, step_stride, dt, half_step_back ? 1 : 0, scale, nsamples,
+                           table, s) != cudaSuccess ||
+      mgbdft::launch_contract(c, s) != cudaSuccess)
+    return launch_error("tensor-core DFT contraction");
+  return MGB_OK;
 }
 
 }  // extern "C"

@@ -198,6 +198,8 @@ class _Monitor:
         if self.accumulator is None:
             return np.zeros((self.num_frequencies,) + self.region_shape, dtype=np.complex64)
         index = self.components.index(component)
+        if self._engine is not None:
+            self._engine.flush_dft()
         host = self.accumulator[index].detach().cpu().numpy()  # [nf][2][cells]
         values = host[:, 0, :] + 1j * host[:, 1, :]
         return values.astype(np.complex64).reshape((self.num_frequencies,) + self.region_shape)

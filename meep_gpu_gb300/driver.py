@@ -59,7 +59,8 @@ class FdtdDriver:
                  accurate_fields_near_cylorigin: bool = False, beta: float = 0.0,
                  bfast_scaled_k: Sequence[float] = (0.0, 0.0, 0.0), prefer_gpu: bool = True,
                  gpu_id: int = 0, launch_shape: Optional[Tuple[int, int, int]] = None,
-                 kernels: Optional[Tuple[int, int, int, int]] = None):
+                 kernels: Optional[Tuple[int, int, int, int]] = None,
+                 dft_accumulation: Optional[str] = None):
         if force_complex_fields:
             raise Unsupported("complex fields are not stepped by this engine; pass "
                               "force_complex_fields=False (real float32 fields)")
@@ -78,6 +79,9 @@ class FdtdDriver:
         # (family, block_z, block_y, x_chunk): 1 the TMA tile kernels, 0 the generic ones;
         # None lets the autotuner time both on this grid and keep the faster.
         self.kernels = kernels
+        # "tensor": buffered samples contracted on the tensor cores (default); "direct":
+        # every sample added into the accumulators as it is taken.
+        self.dft_accumulation = dft_accumulation
         self.pml: Optional[PML] = None
         self._eps: Optional[Tuple[np.ndarray, np.ndarray, np.ndarray]] = None
         self._inv_eps: Optional[Tuple[np.ndarray, np.ndarray, np.ndarray]] = None
@@ -250,7 +254,7 @@ class FdtdDriver:
     def _freeze(self) -> None:
         self.freeze()
 
-    def freeze(self, stream=None, autotune: bool = True):
+    def freeze(self, stream=None, autotune: bool = True, dft_accumulation: Optional[str] = None):
         """Fix the configuration and make the device state (once); returns the engine.
 
         ``stream`` is the CUDA stream the engine steps and reads on (default: the current
@@ -267,7 +271,8 @@ class FdtdDriver:
         self.engine = Engine(self.grid, self.pml, self._inv_eps, self._poles, self._sources,
                              list(self._flux_monitors) + list(self._dft_monitors), device=device,
                              stream=stream, launch_shape=self.launch_shape, kernels=self.kernels,
-                             autotune=autotune)
+                             autotune=autotune,
+                             dft_accumulation=dft_accumulation or self.dft_accumulation)
         return self.engine
 
     @property

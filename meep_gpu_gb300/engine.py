@@ -63,7 +63,8 @@ class Engine:
                  sources: Sequence[Source], monitors: Sequence[_Monitor],
                  device: Optional[torch.device] = None, stream: Optional[torch.cuda.Stream] = None,
                  launch_shape: Optional[Tuple[int, int, int]] = None, autotune: bool = True,
-                 kernels: Optional[Tuple[int, int, int, int]] = None):
+                 kernels: Optional[Tuple[int, int, int, int]] = None,
+                 dft_accumulation: Optional[str] = None):
         if not torch.cuda.is_available():
             raise RuntimeError("meep_gpu_gb300 steps on a CUDA GPU and none is visible")
         self.lib = _lib.load()
@@ -128,6 +129,7 @@ class Engine:
         handle = ctypes.c_void_p()
         _lib.check(self.lib, self.lib.mgb_create(ctypes.byref(d), ctypes.byref(handle)))
         self.handle = handle
+        self._setup_dft_buffers(dft_accumulation)
         self._pole_specs = list(poles)
         self.choice = None
         if kernels is not None:
@@ -249,6 +251,41 @@ class Engine:
             self.monitor_tensors.append((omega, acc, weights))
             monitor.accumulator = acc
             monitor._engine = self
+
+    def _setup_dft_buffers(self, mode: Optional[str]) -> None:
+        """Tensor-core accumulation (``"tensor"``, the default; ``MEEPGB_DFT`` overrides
+        it) buffers MGB_DFT_DEPTH samples per monitor and contracts them on the tensor
+        cores; ``"direct"`` adds every sample into the accumulators as it is taken."""
+        mode = mode or os.environ.get("MEEPGB_DFT", "tensor")
+        if mode not in ("tensor", "direct"):
+            raise ValueError(f"DFT accumulation is 'tensor' or 'direct', not {mode!r}")
+        self.dft_accumulation = mode
+        self.dft_samples: List[Optional[torch.Tensor]] = [None] * len(self.monitors)
+        self.dft_scratch = None
+        if mode != "tensor" or not self.monitors:
+            return
+        eligible = [m.num_frequencies <= _lib.MGB_DFT_MAX_FREQ for m in self.monitors]
+        if not any(eligible):
+            return
+        nbytes = max(self.lib.mgb_dft_scratch_bytes(m.num_frequencies)
+                     for m, ok in zip(self.monitors, eligible) if ok)
+        self.dft_scratch = torch.empty(nbytes // 4, dtype=torch.float32, device=self.device)
+        for index, (monitor, ok) in enumerate(zip(self.monitors, eligible)):
+            if not ok:
+                continue
+            samples = torch.empty((_lib.MGB_DFT_DEPTH, len(monitor.components) * monitor.cells),
+                                  dtype=torch.float32, device=self.device)
+            _lib.check(self.lib, self.lib.mgb_set_dft_buffer(self.handle, index, samples.data_ptr(),
+                                                             self.dft_scratch.data_ptr(), nbytes))
+            self.dft_samples[index] = samples
+
+    def flush_dft(self) -> None:
+        """Add buffered DFT samples to the accumulators; the current stream then sees them."""
+        stream = self.stream if self.stream is not None else torch.cuda.current_stream(self.device)
+        _lib.check(self.lib, self.lib.mgb_dft_flush(self.handle, stream.cuda_stream))
+        current = torch.cuda.current_stream(self.device)
+        if current != stream:
+            current.wait_stream(stream)
 
     # --- stepping -----------------------------------------------------------------------
     def set_launch_shape(self, block_z: int, block_y: int, x_chunk: int) -> None:

@@ -261,7 +261,8 @@ class BatchServer:
         """Make a job's device state (on the setup stream) and put it in a free slot."""
         slot = self.slots.index(None)
         with torch.cuda.stream(self.setup_stream):
-            job.engine = job.driver.freeze(stream=self.stream, autotune=False)
+            # the batch accumulates its monitors step by step (dft_batched)
+            job.engine = job.driver.freeze(stream=self.stream, autotune=False, dft_accumulation="direct")
             if job.driver.sources:
                 host = deposit_words(job.driver.sources, 0, job.request.steps, job.driver.grid.dt)
                 job.words = torch.from_numpy(host).to(self.device)

@@ -16,7 +16,7 @@ HEADER = ROOT / "include" / "meepgb.h"
 
 def declared_symbols():
     text = HEADER.read_text()
-    return sorted(set(re.findall(r"^\s*(?:int|void|size_t|int64_t)\s+(mgb_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|void|size_t|int64_t|int32_t)\s+(mgb_\w+)\s*\(", text, re.M)))
 
 
 def test_library_loads_and_exports_every_declared_symbol():

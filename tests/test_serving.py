@@ -143,8 +143,8 @@ SMALL = [Request(0, 24, 6.0, 6.0, 150, 0.0), Request(1, 32, 3.0, 9.0, 233, 0.0),
          Request(4, 32, 8.0, 10.0, 97, 0.0), Request(5, 48, 4.0, 15.0, 140, 0.0)]
 
 
-def plain(request, kernels):
-    driver, flux = serving.build_request(request, kernels=kernels)
+def plain(request, kernels, dft_accumulation="direct"):
+    driver, flux = serving.build_request(request, kernels=kernels, dft_accumulation=dft_accumulation)
     driver.step_many(request.steps)
     spectrum = flux.get_flux_spectrum()
     fields = {c: driver.get_field(c, cell_centered=False) for c in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")}
@@ -166,6 +166,11 @@ def test_served_spectra_equal_the_plain_solve(gpu, use_graph):
         for kernels in ((0, 32, 4, 4), (1, 64, 8, 8)):
             expected, _ = plain(request, kernels)
             assert np.array_equal(got[request.index], expected), (request.index, kernels)
+        # the plain drop-in's default (tensor-core) accumulation: the same spectrum to
+        # float32 rounding order
+        tensor, _ = plain(request, (0, 32, 4, 4), dft_accumulation="tensor")
+        rel = np.max(np.abs(tensor - got[request.index])) / np.max(np.abs(got[request.index]))
+        assert rel <= 1e-5, (request.index, rel)
 
 
 @pytest.mark.gpu

@@ -223,6 +223,15 @@ int mgb_dft_contract(const float* samples, int64_t ld, int64_t ncols, int32_t ns
                      double dt, int32_t half_step_back, double scale, float* acc, void* scratch,
                      size_t scratch_bytes, void* stream);
 
+/* mgb_dft_contract with no scratch argument and no allocation: the phase table lives in
+ * a device array of the library sized for MGB_DFT_MAX_FREQ frequencies (looked up once
+ * per device). Sizes beyond the maximum are refused before the device is touched. Calls
+ * that overlap on the device share that table and race: order them on one stream. */
+int mgb_dft_contract_noalloc(const float* samples, int64_t ld, int64_t ncols, int32_t nsamples,
+                             const double* omega, int32_t nfreq, int64_t first_step,
+                             int32_t step_stride, double dt, int32_t half_step_back, double scale,
+                             float* acc, void* stream);
+
 /* ---- Batched stepping of independent simulations (serving) ---------------------------
  * No reference counterpart: the reference steps one simulation per process
  * (meep_gpu/driver.py:3419, one FdtdDriver per GPU, README.md:127). A batch is a slot

@@ -108,6 +108,11 @@ SIGNATURES = {
                                         ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,
                                         ctypes.c_double, ctypes.c_int32, ctypes.c_double, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "mgb_dft_contract_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                                ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
+                                                ctypes.c_int64, ctypes.c_int32, ctypes.c_double,
+                                                ctypes.c_int32, ctypes.c_double, ctypes.c_void_p,
+                                                ctypes.c_void_p]),
     "mgb_batch_bytes": (ctypes.c_size_t, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     "mgb_batch_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                         ctypes.c_void_p, ctypes.c_size_t,

@@ -41,6 +41,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <mutex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -1930,6 +1931,60 @@ int mgb_dft_contract(const float* samples, int64_t ld, int64_t ncols, int32_t ns
       mgbdft::launch_contract(c, s) != cudaSuccess)
     return launch_error("tensor-core DFT contraction");
   return MGB_OK;
+}
+
+}  // extern "C"
+
+// ======================================================================================
+// Tensor-core DFT contraction without caller scratch
+//
+// The phase table lives in a file-scope device array sized for the largest contraction
+// (2 * MGB_DFT_MAX_FREQ rows of MGB_DFT_DEPTH words). Its address is looked up once per
+// device (cudaGetSymbolAddress with that device current) and cached. No word of it must
+// start at zero: the table kernel writes every word the contraction then reads. Calls
+// that overlap on the device (different streams, or threads without ordering) share the
+// one table and race.
+namespace {
+
+static __device__ __align__(256) float g_dft_table[2 * mgbdft::kMaxFreq * mgbdft::kDepth];
+
+std::mutex g_table_mutex;
+std::vector<void*> g_table_address;  // per device, null until looked up
+
+int static_table(void** out) {
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess) return launch_error("current device");
+  std::lock_guard<std::mutex> lock(g_table_mutex);
+  if ((int)g_table_address.size() <= device) g_table_address.resize(device + 1, nullptr);
+  if (g_table_address[device] == nullptr) {
+    void* address = nullptr;
+    if (cudaGetSymbolAddress(&address, g_dft_table) != cudaSuccess) return launch_error("static DFT table address");
+    g_table_address[device] = address;
+  }
+  *out = g_table_address[device];
+  return MGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mgb_dft_contract_noalloc(const float* samples, int64_t ld, int64_t ncols, int32_t nsamples,
+                             const double* omega, int32_t nfreq, int64_t first_step, int32_t step_stride,
+                             double dt, int32_t half_step_back, double scale, float* acc, void* stream) {
+  // the sizes are checked before the device is touched
+  if (nfreq < 1 || nfreq > mgbdft::kMaxFreq)
+    return fail(MGB_ERR_ARGUMENT, "nfreq must be 1.." + std::to_string(mgbdft::kMaxFreq));
+  if (nsamples < 0 || nsamples > mgbdft::kDepth)
+    return fail(MGB_ERR_ARGUMENT, "nsamples must be 0.." + std::to_string(mgbdft::kDepth));
+  static_assert(sizeof(g_dft_table) >= (size_t)2 * mgbdft::kMaxFreq * mgbdft::kDepth * sizeof(float),
+                "static table holds the largest contraction");
+  if (samples == nullptr || omega == nullptr || acc == nullptr) return fail(MGB_ERR_ARGUMENT, "null argument");
+  void* table = nullptr;
+  const int rc = static_table(&table);
+  if (rc != MGB_OK) return rc;
+  return mgb_dft_contract(samples, ld, ncols, nsamples, omega, nfreq, first_step, step_stride, dt,
+                          half_step_back, scale, acc, table, sizeof(g_dft_table), stream);
 }
 
 }  // extern "C"

@@ -232,6 +232,32 @@ int mgb_dft_contract_noalloc(const float* samples, int64_t ld, int64_t ncols, in
                              int32_t step_stride, double dt, int32_t half_step_back, double scale,
                              float* acc, void* stream);
 
+/* ---- Adjoint (reverse-time) stepping ------------------------------------------------
+ * No reference counterpart (the reference has no adjoint). The adjoint state is a second
+ * plan made by mgb_create over adjoint arrays laid out as the forward's (E, D, H and the
+ * PML auxiliaries), with the forward's coefficient tables, memberships and inverse
+ * permittivity, no sources or poles, and the objective's monitor whose acc points at the
+ * objective's derivative with respect to the monitor's accumulators. */
+typedef struct mgb_adjoint {
+  float* mu_b[3];       /* device volumes: adjoint of the H half's curl input */
+  float* mu_d[3];       /* device volumes: adjoint of the E half's curl input */
+  int32_t box[6];       /* gradient box (half-open cell ranges x, y, z) */
+  const float* d_after; /* device [3][box cells]: forward D after the step being reversed */
+  float* grad_inv;      /* device [box cells]: += dJ/d(inverse permittivity) */
+} mgb_adjoint;
+
+/* Reverse forward step `step`: the transposed E half (with the gather of mu_b left by
+ * the reversal of step + 1, and the gradient over the box), then the transposed H half.
+ * mu_b must be zero before the reversal of the last step. Asynchronous. */
+int mgb_adjoint_step(mgb_sim* adj, const mgb_adjoint* a, int64_t step, void* stream);
+
+/* Add the adjoint of the monitor's sample taken after step post - 1 (due when post is a
+ * multiple of its decimation) into the adjoint E and H. Asynchronous. */
+int mgb_adjoint_inject(mgb_sim* adj, int32_t monitor, int64_t post, void* stream);
+
+/* Copy [3][box cells] of a plan's E (family 0), D (1) or H (2) into dst. Asynchronous. */
+int mgb_copy_box(mgb_sim* sim, int32_t family, const int32_t* box, float* dst, void* stream);
+
 /* ---- Batched stepping of independent simulations (serving) ---------------------------
  * No reference counterpart: the reference steps one simulation per process
  * (meep_gpu/driver.py:3419, one FdtdDriver per GPU, README.md:127). A batch is a slot

@@ -84,6 +84,12 @@ class MgbSimDesc(ctypes.Structure):
     ]
 
 
+class MgbAdjoint(ctypes.Structure):
+    _fields_ = [("mu_b", ctypes.c_void_p * 3), ("mu_d", ctypes.c_void_p * 3),
+                ("box", ctypes.c_int32 * 6), ("d_after", ctypes.c_void_p),
+                ("grad_inv", ctypes.c_void_p)]
+
+
 # Every symbol include/meepgb.h declares, with its ctypes signature.
 SIGNATURES = {
     "mgb_abi_version": (ctypes.c_int, []),
@@ -113,6 +119,11 @@ SIGNATURES = {
                                                 ctypes.c_int64, ctypes.c_int32, ctypes.c_double,
                                                 ctypes.c_int32, ctypes.c_double, ctypes.c_void_p,
                                                 ctypes.c_void_p]),
+    "mgb_adjoint_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(MgbAdjoint), ctypes.c_int64,
+                                        ctypes.c_void_p]),
+    "mgb_adjoint_inject": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p]),
+    "mgb_copy_box": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_void_p]),
     "mgb_batch_bytes": (ctypes.c_size_t, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     "mgb_batch_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                         ctypes.c_void_p, ctypes.c_size_t,

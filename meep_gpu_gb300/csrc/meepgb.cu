@@ -104,6 +104,11 @@ struct TileMaps {
   int stages;
 };
 
+struct BoxArgs {
+  int box[6];
+  float* dst;
+};
+
 struct DftParams {
   int nx, ny, nz;
   int met[3];
@@ -1084,6 +1089,264 @@ __global__ void __launch_bounds__(kDftItemCells) dft_batched(const __grid_consta
   dft_cell(dp, phase, (long long)w.y * kDftItemCells + threadIdx.x);
 }
 
+// ------------------------------------------------------------------------------------
+// Adjoint (reverse-time) step: the transpose of one forward step, for gradients of a
+// flux objective with respect to the inverse permittivity. The adjoint state has the
+// forward state's layout (a second plan whose field and auxiliary pointers are the
+// adjoint arrays, with the forward's coefficient tables, memberships and inverse
+// permittivity). The forward step is linear in its state; each half is a local update
+// of every cell from its old words and a curl of the other family, so its transpose is
+// the transposed local update, which yields the adjoint of the curl input ("mu"), and
+// the transposed curl, a gather of mu from the neighbours:
+//   forward H half: curl = dtdx * C(E) (forward differences), then the B/H update;
+//   forward E half: curl = dtdx * C'(H) (backward differences), then the D/E update.
+// Reversing forward step n: kernel adj_e (E half) first adds dtdx * C^T(mu_B) of step
+// n + 1 into the adjoint of E, then runs the transposed E update, stores mu_D and adds
+// the gradient dJ/d(inv_eps) += (adjoint of w) * D' over the design box (w = inv * D'
+// is where the inverse permittivity enters); kernel adj_h then adds dtdx * C'^T(mu_D)
+// into the adjoint of H and runs the transposed B/H update, storing mu_B. Every
+// coefficient outside its membership is exactly 1, so the general forms serve every
+// cell. No poles (the caller refuses them). Derivations per operation are in comments.
+struct AdjParams {
+  float* mu_b[3];      // adjoint of the H half's curl input, per B component
+  float* mu_d[3];      // adjoint of the E half's curl input, per D component
+  int box[6];          // gradient box, half-open
+  const float* d_after;  // [3][box cells]: forward D after the step being reversed
+  float* grad_inv;       // [box cells]
+  int first_step;        // the step being reversed is step 0 (separate_h_from_b)
+};
+
+__device__ __forceinline__ float coef(const float* table, bool pml, int at) {
+  return pml ? __ldg(table + at) : 1.f;
+}
+
+// Reverse of the E half: gather mu_B, transposed D/E update, mu_D, gradient.
+template <bool PML>
+__global__ void __launch_bounds__(256) adj_e(const __grid_constant__ StepParams p,
+                                             const __grid_constant__ AdjParams a, int xchunk) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (k >= p.nz || j >= p.ny) return;
+  const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  const int sx = p.ny * p.nz, sy = p.nz;
+  const float dtdx = p.dtdx;
+  // "c - y": the cell whose forward (+y) neighbour is this one: none on a metallic
+  // axis at 0, the last row on a periodic one.
+  const int jm = j > 0 ? j - 1 : (p.met[1] ? -1 : p.ny - 1);
+  const int km = k > 0 ? k - 1 : (p.met[2] ? -1 : p.nz - 1);
+  const int box_ny = a.box[3] - a.box[2], box_nz = a.box[5] - a.box[4];
+  const bool jk_in_box = j >= a.box[2] && j < a.box[3] && k >= a.box[4] && k < a.box[5];
+  const long long box_cells = (long long)(a.box[1] - a.box[0]) * box_ny * box_nz;
+  for (int i = i0; i < i1; ++i) {
+    const int im = i > 0 ? i - 1 : (p.met[0] ? -1 : p.nx - 1);
+    const int c = i * sx + j * sy + k;
+    const int cym = jm >= 0 ? i * sx + jm * sy + k : -1;
+    const int czm = km >= 0 ? i * sx + j * sy + km : -1;
+    const int cxm = im >= 0 ? im * sx + j * sy + k : -1;
+    auto mb = [&](int q, int at) { return at >= 0 ? a.mu_b[q][at] : 0.f; };
+    // Transpose of the H half's curls (forward differences):
+    //   cx = dtdx*((Ez[+y] - Ez) + Ey - Ey[+z]), cy = dtdx*((Ex[+z] - Ex) + Ez - Ez[+x]),
+    //   cz = dtdx*((Ey[+x] - Ey) + Ex - Ex[+y]).
+    float le[3];
+    le[0] = p.E[0][c] + dtdx * ((mb(1, czm) - mb(1, c)) + (mb(2, c) - mb(2, cym)));
+    le[1] = p.E[1][c] + dtdx * ((mb(0, c) - mb(0, czm)) + (mb(2, cxm) - mb(2, c)));
+    le[2] = p.E[2][c] + dtdx * ((mb(0, cym) - mb(0, c)) + (mb(1, c) - mb(1, cxm)));
+    const bool wx = p.met[0] && i == 0, wy = p.met[1] && j == 0, wz = p.met[2] && k == 0;
+    const int coord[3] = {i, j, k};
+    float grad = 0.f;
+    const bool in_box = jk_in_box && i >= a.box[0] && i < a.box[1];
+    const long long bcell =
+        in_box ? ((long long)(i - a.box[0]) * box_ny + (j - a.box[2])) * box_nz + (k - a.box[4]) : 0;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const int a1 = (q + 1) % 3, a2 = (q + 2) % 3;
+      const bool masked = q == 0 ? (wy || wz) : q == 1 ? (wx || wz) : (wx || wy);
+      const bool own = PML && in_runs(p.fwE[q], coord[q]);
+      const bool f = PML && in_runs(p.fuD[q], coord[a2]);
+      const float k1 = coef(p.kms[kInteger][a1], PML, coord[a1]);
+      const float s1 = coef(p.sinv[kInteger][a1], PML, coord[a1]);
+      const float k2 = coef(p.kms[kInteger][a2], PML, coord[a2]);
+      const float s2 = coef(p.sinv[kInteger][a2], PML, coord[a2]);
+      // E' = E + (kps*w - kms*fw), fw' = w on the own membership; E' = w elsewhere.
+      float lw = le[q], le_in = 0.f;
+      if (own) {
+        const float kps = __ldg(p.kps[kHalf][q] + coord[q]);
+        const float kms = __ldg(p.kms[kHalf][q] + coord[q]);
+        lw = kps * le[q] + p.fwE[q].data[c];
+        le_in = le[q];
+        p.fwE[q].data[c] = -kms * le[q];
+      }
+      if (in_box) grad += lw * a.d_after[(long long)q * box_cells + bcell];
+      // w = inv * d'; D' = d'; d' is forced to 0 on the masked wall cells.
+      const float ld = masked ? 0.f : p.D[q][c] + p.inv_eps[q][c] * lw;
+      // d' from the curl: split-field recurrence on the dsigu membership, else
+      // d' = (k1*d - curl)*s1. fu' is stored even on masked cells (curl 0 there).
+      float ld_in, mu;
+      if (f) {
+        const float lu_out = p.fuD[q].data[c];
+        const float ln = s2 * ld + lu_out;
+        ld_in = k2 * s2 * ld;
+        p.fuD[q].data[c] = -s2 * ld + k1 * s1 * ln;
+        mu = -s1 * ln;
+      } else {
+        ld_in = k1 * s1 * ld;
+        mu = -s1 * ld;
+      }
+      p.D[q][c] = ld_in;
+      p.E[q][c] = le_in;
+      a.mu_d[q][c] = masked ? 0.f : mu;
+    }
+    if (in_box) a.grad_inv[bcell] += grad;
+  }
+}
+
+// Reverse of the H half: gather mu_D, transposed B/H update, mu_B.
+template <bool PML>
+__global__ void __launch_bounds__(256) adj_h(const __grid_constant__ StepParams p,
+                                             const __grid_constant__ AdjParams a, int xchunk) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (k >= p.nz || j >= p.ny) return;
+  const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  const int sx = p.ny * p.nz, sy = p.nz;
+  const float dtdx = p.dtdx;
+  // "c + y": the cell whose backward (-y) neighbour is this one: none on a metallic axis
+  // at the top, row 0 on a periodic one.
+  const int jp = j + 1 < p.ny ? j + 1 : (p.met[1] ? -1 : 0);
+  const int kp = k + 1 < p.nz ? k + 1 : (p.met[2] ? -1 : 0);
+  for (int i = i0; i < i1; ++i) {
+    const int ip = i + 1 < p.nx ? i + 1 : (p.met[0] ? -1 : 0);
+    const int c = i * sx + j * sy + k;
+    const int cyp = jp >= 0 ? i * sx + jp * sy + k : -1;
+    const int czp = kp >= 0 ? i * sx + j * sy + kp : -1;
+    const int cxp = ip >= 0 ? ip * sx + j * sy + k : -1;
+    auto md = [&](int q, int at) { return at >= 0 ? a.mu_d[q][at] : 0.f; };
+    // Transpose of the E half's curls (backward differences):
+    //   cx = dtdx*((Hz[-y] - Hz) + Hy - Hy[-z]), cy = dtdx*((Hx[-z] - Hx) + Hz - Hz[-x]),
+    //   cz = dtdx*((Hy[-x] - Hy) + Hx - Hx[-y]).
+    float lh[3];
+    lh[0] = p.H[0][c] + dtdx * ((md(1, czp) - md(1, c)) + (md(2, c) - md(2, cyp)));
+    lh[1] = p.H[1][c] + dtdx * ((md(0, c) - md(0, czp)) + (md(2, cxp) - md(2, c)));
+    lh[2] = p.H[2][c] + dtdx * ((md(0, cyp) - md(0, c)) + (md(1, c) - md(1, cxp)));
+    const int coord[3] = {i, j, k};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const int a1 = (q + 1) % 3, a2 = (q + 2) % 3;
+      // zero_metal_B: the curl and the new word of B_q are 0 at index 0 of a metallic
+      // own axis (never an own-axis membership cell).
+      const bool wall = p.met[q] && coord[q] == 0;
+      const bool own = PML && in_runs(p.B[q], coord[q]);
+      const bool f = PML && in_runs(p.fuB[q], coord[a2]);
+      const float k1 = coef(p.kms[kHalf][a1], PML, coord[a1]);
+      const float s1 = coef(p.sinv[kHalf][a1], PML, coord[a1]);
+      const float k2 = coef(p.kms[kHalf][a2], PML, coord[a2]);
+      const float s2 = coef(p.sinv[kHalf][a2], PML, coord[a2]);
+      // H' = H + (kps*b' - kms*fw) (step 0: b' + (kps*b' - kms*b')), fw' = b', B' = b' on
+      // the own membership; elsewhere H' = b' and H's storage is B's word.
+      float lb;
+      float lh_in = 0.f, lw_in = 0.f;
+      if (own) {
+        const float kps = __ldg(p.kps[kInteger][q] + coord[q]);
+        const float kms = __ldg(p.kms[kInteger][q] + coord[q]);
+        const float extra = p.fwH[q].data[c] + p.B[q].data[c];
+        if (a.first_step) {
+          lb = ((1.f + kps) - kms) * lh[q] + extra;
+        } else {
+          lb = kps * lh[q] + extra;
+          lh_in = lh[q];
+          lw_in = -kms * lh[q];
+        }
+      } else {
+        lb = wall ? 0.f : lh[q];
+      }
+      float lb_in, mu;
+      if (f) {
+        const float lu_out = p.fuB[q].data[c];
+        const float ln = s2 * lb + lu_out;
+        lb_in = k2 * s2 * lb;
+        p.fuB[q].data[c] = -s2 * lb + k1 * s1 * ln;
+        mu = -s1 * ln;
+      } else {
+        lb_in = k1 * s1 * lb;
+        mu = -s1 * lb;
+      }
+      if (own) {
+        p.B[q].data[c] = lb_in;
+        p.H[q][c] = lh_in;
+        p.fwH[q].data[c] = lw_in;
+      } else {
+        p.H[q][c] = lb_in;
+      }
+      a.mu_b[q][c] = wall ? 0.f : mu;
+    }
+  }
+}
+
+// Adjoint of one DFT sample taken after step post - 1: the sample's adjoint
+// g_q(c) = sum_f (cos(w_f t) scale * coef[q][f][0][c] + sin(w_f t) scale * coef[q][f][1][c])
+// (t at the component's time, coef in the accumulator layout) is spread back over the
+// Yee words the centred sample averaged, with the same weights (atomic adds: samples of
+// neighbouring cells share words).
+__device__ __forceinline__ void scatter_centred(const DftParams& p, int comp, int i, int j, int k, float g) {
+  const int q = comp % 3;
+  const bool electric = comp < 3;
+  const bool ax = electric ? (q != 0) : (q == 0);
+  const bool ay = electric ? (q != 1) : (q == 1);
+  const bool az = electric ? (q != 2) : (q == 2);
+  const float w = (ax ? 0.5f : 1.f) * (ay ? 0.5f : 1.f) * (az ? 0.5f : 1.f);
+  float* base = electric ? const_cast<float*>(p.E[q]) : const_cast<float*>(p.H[q]);
+  for (int b = 0; b <= (az ? 1 : 0); ++b)
+    for (int a = 0; a <= (ay ? 1 : 0); ++a)
+      for (int d = 0; d <= (ax ? 1 : 0); ++d) {
+        int ii = i + d, jj = j + a, kk = k + b;
+        if (ii >= p.nx) { if (p.met[0]) continue; ii -= p.nx; }
+        if (jj >= p.ny) { if (p.met[1]) continue; jj -= p.ny; }
+        if (kk >= p.nz) { if (p.met[2]) continue; kk -= p.nz; }
+        atomicAdd(base + ((long long)ii * p.ny + jj) * p.nz + kk, g * w);
+      }
+}
+
+__global__ void __launch_bounds__(256) adj_inject(const __grid_constant__ DftParams p, long long post) {
+  extern __shared__ float2 phase[];  // [0, nf): E phases, [nf, 2nf): H phases
+  dft_phases(p.mon, post, phase);
+  __syncthreads();
+  const mgb_monitor& m = p.mon;
+  const int nf = m.nfreq;
+  const int rx = m.region[1] - m.region[0], ry = m.region[3] - m.region[2],
+            rz = m.region[5] - m.region[4];
+  const long long cells = (long long)rx * ry * rz;
+  const long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= cells) return;
+  const int rk = (int)(cell % rz);
+  const int rj = (int)((cell / rz) % ry);
+  const int ri = (int)(cell / ((long long)ry * rz));
+  const int i = m.region[0] + ri, j = m.region[2] + rj, k = m.region[4] + rk;
+  for (int q = 0; q < m.ncomp; ++q) {
+    const int comp = m.comp[q];
+    const float2* ph = comp < 3 ? phase : phase + nf;
+    const float* cf = m.acc + (long long)q * nf * 2 * cells + cell;
+    float g = 0.f;
+    for (int f = 0; f < nf; ++f) g += ph[f].x * cf[(long long)(2 * f) * cells] + ph[f].y * cf[(long long)(2 * f + 1) * cells];
+    if (g != 0.f) scatter_centred(p, comp, i, j, k, g);
+  }
+}
+
+// Copy [3][box] of one field family (0 E, 1 D, 2 H) into dst.
+__global__ void __launch_bounds__(256) copy_box(const __grid_constant__ StepParams p, int family,
+                                                BoxArgs b) {
+  const long long cells = (long long)(b.box[1] - b.box[0]) * (b.box[3] - b.box[2]) * (b.box[5] - b.box[4]);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 3 * cells) return;
+  const int q = (int)(t / cells);
+  const long long cell = t % cells;
+  const int bz = b.box[5] - b.box[4], by = b.box[3] - b.box[2];
+  const int k = b.box[4] + (int)(cell % bz);
+  const int j = b.box[2] + (int)((cell / bz) % by);
+  const int i = b.box[0] + (int)(cell / ((long long)by * bz));
+  const float* src = family == 0 ? p.E[q] : family == 1 ? p.D[q] : p.H[q];
+  b.dst[t] = src[((long long)i * p.ny + j) * p.nz + k];
+}
+
 }  // namespace
 
 // ======================================================================================
@@ -1985,6 +2248,82 @@ int mgb_dft_contract_noalloc(const float* samples, int64_t ld, int64_t ncols, in
   if (rc != MGB_OK) return rc;
   return mgb_dft_contract(samples, ld, ncols, nsamples, omega, nfreq, first_step, step_stride, dt,
                           half_step_back, scale, acc, table, sizeof(g_dft_table), stream);
+}
+
+}  // extern "C"
+
+// ======================================================================================
+// Adjoint ABI
+extern "C" {
+
+int mgb_adjoint_step(mgb_sim* adj, const mgb_adjoint* a, int64_t step, void* stream) {
+  if (adj == nullptr || a == nullptr || a->grad_inv == nullptr || a->d_after == nullptr)
+    return fail(MGB_ERR_ARGUMENT, "null argument");
+  if (adj->step.npoles != 0) return fail(MGB_ERR_UNSUPPORTED, "the adjoint step does not carry susceptibility poles");
+  for (int q = 0; q < 3; ++q)
+    if (a->mu_b[q] == nullptr || a->mu_d[q] == nullptr) return fail(MGB_ERR_ARGUMENT, "missing mu volume");
+  const StepParams& p = adj->step;
+  const int n[3] = {p.nx, p.ny, p.nz};
+  for (int ax = 0; ax < 3; ++ax)
+    if (a->box[2 * ax] < 0 || a->box[2 * ax] >= a->box[2 * ax + 1] || a->box[2 * ax + 1] > n[ax])
+      return fail(MGB_ERR_ARGUMENT, "gradient box outside the grid");
+  AdjParams ap;
+  for (int q = 0; q < 3; ++q) {
+    ap.mu_b[q] = a->mu_b[q];
+    ap.mu_d[q] = a->mu_d[q];
+  }
+  for (int e = 0; e < 6; ++e) ap.box[e] = a->box[e];
+  ap.d_after = a->d_after;
+  ap.grad_inv = a->grad_inv;
+  ap.first_step = step == 0 ? 1 : 0;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int xc = 4;
+  const dim3 block(32, 4, 1);
+  const dim3 grid((p.nz + 31) / 32, (p.ny + 3) / 4, (p.nx + xc - 1) / xc);
+  const bool pml = adj->desc.pml_active != 0;
+  if (pml) {
+    adj_e<true><<<grid, block, 0, s>>>(p, ap, xc);
+    adj_h<true><<<grid, block, 0, s>>>(p, ap, xc);
+  } else {
+    adj_e<false><<<grid, block, 0, s>>>(p, ap, xc);
+    adj_h<false><<<grid, block, 0, s>>>(p, ap, xc);
+  }
+  return launch_error("adjoint step");
+}
+
+int mgb_adjoint_inject(mgb_sim* adj, int32_t monitor, int64_t post, void* stream) {
+  if (adj == nullptr) return fail(MGB_ERR_ARGUMENT, "null plan");
+  if (monitor < 0 || monitor >= adj->desc.nmonitors) return fail(MGB_ERR_ARGUMENT, "no such monitor");
+  const StepParams& p = adj->step;
+  const mgb_monitor& mon = adj->desc.monitors[monitor];
+  DftParams q;
+  q.nx = p.nx; q.ny = p.ny; q.nz = p.nz;
+  for (int ax = 0; ax < 3; ++ax) q.met[ax] = p.met[ax];
+  for (int c = 0; c < 3; ++c) { q.E[c] = p.E[c]; q.H[c] = p.H[c]; }
+  q.mon = mon;
+  const long long cells = (long long)(mon.region[1] - mon.region[0]) * (mon.region[3] - mon.region[2]) *
+                          (mon.region[5] - mon.region[4]);
+  const size_t smem = (size_t)mon.nfreq * 2 * sizeof(float2);
+  adj_inject<<<(unsigned)((cells + 255) / 256), 256, smem, static_cast<cudaStream_t>(stream)>>>(q, post);
+  return launch_error("adjoint injection");
+}
+
+int mgb_copy_box(mgb_sim* sim, int32_t family, const int32_t* box, float* dst, void* stream) {
+  if (sim == nullptr || box == nullptr || dst == nullptr) return fail(MGB_ERR_ARGUMENT, "null argument");
+  if (family < 0 || family > 2) return fail(MGB_ERR_ARGUMENT, "family is 0 (E), 1 (D) or 2 (H)");
+  const StepParams& p = sim->step;
+  const int n[3] = {p.nx, p.ny, p.nz};
+  BoxArgs b;
+  for (int ax = 0; ax < 3; ++ax) {
+    if (box[2 * ax] < 0 || box[2 * ax] >= box[2 * ax + 1] || box[2 * ax + 1] > n[ax])
+      return fail(MGB_ERR_ARGUMENT, "box outside the grid");
+    b.box[2 * ax] = box[2 * ax];
+    b.box[2 * ax + 1] = box[2 * ax + 1];
+  }
+  b.dst = dst;
+  const long long cells = 3LL * (box[1] - box[0]) * (box[3] - box[2]) * (box[5] - box[4]);
+  copy_box<<<(unsigned)((cells + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(p, family, b);
+  return launch_error("box copy");
 }
 
 }  // extern "C"

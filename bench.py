@@ -64,6 +64,12 @@ def parse_args():
     p.add_argument("--serving-replay", type=int, default=128, help="steps per captured replay")
     p.add_argument("--serving-budget-gb", type=float, default=16.0)
     p.add_argument("--no-plain", action="store_true", help="skip the one-at-a-time solve")
+    p.add_argument("--adjoint", action="store_true",
+                   help="instead of the step line: the 96^3 adjoint-gradient workload")
+    p.add_argument("--dft", action="store_true",
+                   help="instead of the step line: the tensor-core DFT contraction on a flux plane")
+    p.add_argument("--fd-voxels", type=int, default=4,
+                   help="voxels checked by float64 central differences in --adjoint mode")
     return p.parse_args()
 
 
@@ -182,6 +188,10 @@ def run_reference(args):
 
 
 def main():
+    if "--adjoint" in sys.argv:
+        return bench_adjoint(parse_args())
+    if "--dft" in sys.argv:
+        return bench_dft(parse_args())
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -389,6 +399,137 @@ def bench_serving(device, args):
                         "what": "FdtdDriver per request, autotuned kernels, step_many + flux read"}
         out["served_vs_plain_max_rel_diff"] = worst
     return out
+
+
+def bench_adjoint(args):
+    """96^3 adjoint gradient: forward with checkpoints, backward, float64 finite differences.
+
+    Prints one JSON line: the objective, the timing of forward and backward (CUDA events
+    around each), and the agreement with central differences (h = 1e-3) of the float64
+    oracle on ``--fd-voxels`` seeded voxels and along one seeded direction over the box.
+    """
+    import torch
+
+    from meep_gpu_gb300 import workloads
+    from meep_gpu_gb300.adjoint import FluxAdjoint
+    from oracle.oracle import Oracle, problem_from_driver
+
+    device = torch.device("cuda", 0)
+    driver, flux, box, eps_box = workloads.adjoint96()
+    steps = workloads.ADJOINT96_STEPS
+    problem = FluxAdjoint(driver, flux, box, steps, checkpoint_every=200)
+    eps = torch.tensor(eps_box, dtype=torch.float64, requires_grad=True)
+    problem.forward(torch.from_numpy(eps_box))  # warm-up (kernel choice, plan)
+    problem.backward()
+    torch.cuda.synchronize(device)
+    marks = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    marks[0].record()
+    value = problem.objective(eps)
+    marks[1].record()
+    value.backward()
+    marks[2].record()
+    torch.cuda.synchronize(device)
+    grad = eps.grad.numpy()
+    fwd_ms, bwd_ms = marks[0].elapsed_time(marks[1]), marks[1].elapsed_time(marks[2])
+    cells = driver.grid.total_cells
+
+    def oracle_j(values):
+        d, _, _, _ = workloads.adjoint96(eps_box=values)
+        prob = problem_from_driver(d)
+        full = np.ones(d.grid.shape)
+        (i0, i1), (j0, j1), (k0, k1) = box
+        full[i0:i1, j0:j1, k0:k1] = values
+        prob.inv_eps64 = [1.0 / full] * 3
+        o = Oracle(prob, "f64")
+        o.run(steps)
+        return float(np.sum(o.flux_spectrum(0)))
+
+    rng = np.random.default_rng(0)
+    h = 1e-3
+    j64 = oracle_j(eps_box)
+    picks = [tuple(int(rng.integers(0, n)) for n in eps_box.shape) for _ in range(args.fd_voxels)]
+    def bumped(v, sign):
+        values = eps_box.copy()
+        values[v] += sign * h
+        return values
+
+    fd = [(oracle_j(bumped(v, 1)) - oracle_j(bumped(v, -1))) / (2 * h) for v in picks]
+    ad = [float(grad[v]) for v in picks]
+    direction = rng.standard_normal(eps_box.shape)
+    direction /= np.linalg.norm(direction)
+    fd_dir = (oracle_j(eps_box + h * direction) - oracle_j(eps_box - h * direction)) / (2 * h)
+    ad_dir = float(np.sum(grad * direction))
+    line = {
+        "metric": "adjoint gradient (96^3, 4000 steps, checkpoints every 200)",
+        "objective": float(value.item()), "objective_f64": j64,
+        "objective_rel_err": abs(float(value.item()) - j64) / abs(j64),
+        "forward_ms": round(fwd_ms, 2), "backward_ms": round(bwd_ms, 2),
+        "gradient_ms": round(fwd_ms + bwd_ms, 2),
+        "mcell_steps_per_s_forward": round(cells * steps / (fwd_ms / 1e3) / 1e6, 1),
+        "fd_voxels": [{"voxel": list(v), "adjoint": a, "fd_f64": f} for v, a, f in zip(picks, ad, fd)],
+        "fd_rel_l2": float(np.linalg.norm(np.array(ad) - np.array(fd)) / np.linalg.norm(fd)) if fd else None,
+        "directional": {"adjoint": ad_dir, "fd_f64": fd_dir, "rel_err": abs(ad_dir - fd_dir) / abs(fd_dir)},
+        "h": h, "box": [list(b) for b in box], "data": "synthetic (seeded eps ~ U[1,12])",
+        "reference_adjoint": "unavailable: the reference has no adjoint gradient",
+    }
+    print(json.dumps(line), flush=True)
+    problem.close()
+
+
+def bench_dft(args):
+    """The tensor-core DFT contraction at the size of one 192^3 flux plane.
+
+    One launch adds K = 32 buffered samples of one component (2 x 170 x 170 region cells,
+    the plane one cell inside a 10-cell PML at 192^3) into 100 frequencies of
+    accumulators. Algorithmic work per launch: 3 TF32 products (3xTF32) of a
+    [2 nfreq x K] x [K x N] contraction, 6 * 2 * nfreq * K * N flops; algorithmic bytes:
+    the samples read once (K * N words) and the accumulators read and written once
+    (2 * 2 * nfreq * N words). Timed with CUDA events over 24 launches after 6 warm-up,
+    cycling six sets of buffers (more than L2 holds).
+    """
+    import torch
+
+    from meep_gpu_gb300 import _lib
+    lib = _lib.load()
+    nfreq, depth = 100, _lib.MGB_DFT_DEPTH
+    ncols = 2 * 170 * 170
+    rng = np.random.default_rng(0)
+    # six planes' worth of samples and accumulators (~320 MB), cycled, so every launch
+    # meets them in HBM rather than in the 129 MB L2
+    sets = 6
+    samples = [torch.from_numpy(rng.standard_normal((depth, ncols)).astype(np.float32)).cuda() for _ in range(sets)]
+    omega = torch.from_numpy(np.linspace(0.6, 1.3, nfreq)).cuda()
+    accs = [torch.zeros((2 * nfreq, ncols), dtype=torch.float32, device="cuda") for _ in range(sets)]
+    scratch = torch.empty(lib.mgb_dft_scratch_bytes(nfreq) // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    turn = [0]
+
+    def launch():
+        q = turn[0] % sets
+        turn[0] += 1
+        _lib.check(lib, lib.mgb_dft_contract(samples[q].data_ptr(), ncols, ncols, depth, omega.data_ptr(), nfreq,
+                                             120, 120, 0.5 / 24, 0, 0.1, accs[q].data_ptr(), scratch.data_ptr(),
+                                             scratch.numel() * 4, stream.cuda_stream))
+
+    for _ in range(sets):
+        launch()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 24
+    start.record(stream)
+    for _ in range(reps):
+        launch()
+    end.record(stream)
+    end.synchronize()
+    ms = start.elapsed_time(end) / reps
+    flops = 6.0 * 2 * nfreq * depth * ncols
+    nbytes = 4.0 * (depth * ncols + 2 * 2 * nfreq * ncols)
+    peak, kind = measured_peaks()
+    line = {"metric": "tensor-core DFT contraction (3xTF32)", "nfreq": nfreq, "depth": depth, "columns": ncols,
+            "ms_per_launch": round(ms, 4), "tflops": round(flops / (ms / 1e3) / 1e12, 2),
+            "gbs": round(nbytes / (ms / 1e3) / 1e9, 1), "hbm_frac": round(nbytes / (ms / 1e3) / 1e9 / peak, 3),
+            "hbm_peak": peak, "peak_source": kind,
+            "note": "phase table kernel included in each launch; six buffer sets cycled (larger than L2)"}
+    print(json.dumps(line), flush=True)
 
 
 def validate(device):

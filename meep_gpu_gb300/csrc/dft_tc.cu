@@ -7,12 +7,13 @@
 // accumulator word at each decimated step; here K such steps are buffered and added in
 // one pass, so the accumulators are read and written once per K samples.
 //
-// One CTA (four warps) owns a 256-column tile of one component: it stages the samples
+// One CTA (eight warps) owns a 256-column tile of one component: it stages the samples
 // (K = 32 rows) in shared memory as TF32 high and low parts, then for each 128-row tile
 // of phases stages the phase rows the same way, one thread issues the 12 MMAs
 // (4 K-slices x 3 products) into a 128 x 256 float32 accumulator in tensor memory, and
 // every warp reads its 32 lanes back (tcgen05.ld) and adds them to the accumulators in
-// global memory. Operands use the canonical K-major layout without swizzle.
+// global memory through a shared-memory transpose (coalesced rows). Operands use the
+// canonical K-major layout without swizzle.
 #include "dft_tc.cuh"
 
 #include <cstdint>
@@ -22,7 +23,7 @@ namespace {
 
 constexpr int kRows = 128;           // M per tile = tensor-memory lanes
 constexpr int kCols = 256;           // N per tile = tensor-memory columns
-constexpr int kThreads = 128;        // warp w reads lanes 32w .. 32w + 31
+constexpr int kThreads = 256;        // warp w reads lanes 32(w % 4) .. + 31, columns half w / 4
 constexpr int kSlices = kDepth / 8;  // kind::tf32 takes K = 8 per MMA
 // K-major without swizzle: core matrices of 8 rows x 16 bytes (4 elements). In one K
 // slice (8 elements, 32 bytes a row) the two core matrices of a row group are 128 bytes
@@ -41,6 +42,7 @@ constexpr unsigned kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((unsigned)(kCo
                             ((unsigned)(kRows >> 4) << 24);
 static_assert(kDepth % 8 == 0, "K slices of 8");
 static_assert(kSmemBytes <= 227 * 1024, "shared memory");
+static_assert((kThreads / 32) * 32 * 17 * 4 <= 2 * kTileA, "epilogue staging fits in the phase tiles");
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
   return static_cast<unsigned>(__cvta_generic_to_shared(p));
@@ -173,6 +175,7 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const __grid_cons
   unsigned* tmem_slot = reinterpret_cast<unsigned*>(bar + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int q = blockIdx.y;
+  static_assert(kThreads == 256, "two warps per 32 tensor-memory lanes");
   const long long n0 = (long long)blockIdx.x * kCols;
 
   if (warp == 0) tmem_alloc(tmem_slot, kCols);
@@ -236,19 +239,34 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const __grid_cons
     }
     parity ^= 1u;
     fence_after_sync();
-    const int m = mt * kRows + warp * 32 + lane;
-    float* row = acc + (long long)m * c.acc_ld;
+    // Epilogue: warp w reads its 32 lanes (rows) of one half of the columns 16 at a
+    // time, turns them round in shared memory (the phase tile's space, free once the
+    // MMAs are done; rows padded to 17 words, so neither side conflicts), and adds them
+    // to the accumulators with each half-warp on 16 consecutive columns of a row.
+    const int lane_base = (warp & 3) * 32;
+    const int c_begin = (warp >> 2) * (kCols / 2);
+    float* stage = reinterpret_cast<float*>(a_hi) + warp * (32 * 17);
+    const int col = lane & 15, rh = (lane >> 4) * 16;
 #pragma unroll 1
-    for (int c0 = 0; c0 < kCols; c0 += 16) {
+    for (int c0 = c_begin; c0 < c_begin + kCols / 2; c0 += 16) {
       unsigned v[16];
-      tmem_ld16(tmem + ((unsigned)(warp * 32) << 16) + (unsigned)c0, v);
-      if (m < mrows) {
+      tmem_ld16(tmem + ((unsigned)lane_base << 16) + (unsigned)c0, v);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const long long n = n0 + c0 + j;
-          if (n < c.ncols) row[n] = row[n] + __uint_as_float(v[j]);
-        }
+      for (int j = 0; j < 16; ++j) stage[lane * 17 + j] = __uint_as_float(v[j]);
+      __syncwarp();
+      const long long n = n0 + c0 + col;
+      if (n < c.ncols) {
+        // all 16 reads first (in flight together), then the adds and writes
+        float old[16];
+        const int m0 = mt * kRows + lane_base + rh;
+        float* a0 = acc + (long long)m0 * c.acc_ld + n;
+#pragma unroll
+        for (int r = 0; r < 16; ++r) old[r] = (m0 + r < mrows) ? a0[(long long)r * c.acc_ld] : 0.f;
+#pragma unroll
+        for (int r = 0; r < 16; ++r)
+          if (m0 + r < mrows) a0[(long long)r * c.acc_ld] = old[r] + stage[(rh + r) * 17 + col];
       }
+      __syncwarp();
     }
     fence_before_sync();
     __syncthreads();  // tensor memory and the phase tile are free for the next tile

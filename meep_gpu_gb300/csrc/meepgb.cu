@@ -71,6 +71,9 @@ constexpr int kBoxOwn = kTileZ * kTileY * 4;  // 2048 bytes
 struct StepParams {
   int nx, ny, nz;
   int pml;  // 1 when the run has an absorber (the PML memberships below are live)
+  // The box outside every membership of every auxiliary (x0, x1, y0, y1, z0, z1): a CTA
+  // whose cells all lie in it steps the plain update (no membership tests, no tables).
+  int inner[6];
   int met[3];
   float dtdx;
   const float* kms[2][3];
@@ -413,6 +416,13 @@ __device__ __forceinline__ void e_cell(const StepParams& p, const EColumn& col, 
   }
 }
 
+// Whether a CTA's cells [i0, i1) x [j0, j0 + by) x [k0, k0 + bz) all lie in the box that
+// no membership reaches (then the PML update is the plain one, word for word).
+__device__ __forceinline__ bool cta_inner(const StepParams& p, int i0, int i1, int j0, int by, int k0, int bz) {
+  return i0 >= p.inner[0] && i1 <= p.inner[1] && j0 >= p.inner[2] && j0 + by <= p.inner[3] &&
+         k0 >= p.inner[4] && k0 + bz <= p.inner[5];
+}
+
 // ------------------------------------------------------------------------------------
 // Generic kernels: plain loads, one thread per (y, z) column marching over x.
 // One thread's column (j, k) of the H half over planes [i0, i1).
@@ -542,6 +552,187 @@ __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i
   }
 }
 
+// Prefetching marches: the same cell updates, with every field load of plane i + 1
+// issued before plane i is computed and stored, so each thread keeps two planes of loads
+// in flight (the loads of a plane do not depend on the stores of the one before: other
+// cells, or the thread's own cell read before it is written).
+struct HLoads {
+  float ex, ey_xp, ez_xp, ez_yp, ex_yp, ey_zp, ex_zp, h[3];
+};
+
+__device__ __forceinline__ void h_loads(const StepParams& p, HLoads& L, int i, int c, int col, int sx,
+                                        int oy, int oz, bool ywall, bool zwall) {
+  L.ex = p.E[0][c];
+  if (i + 1 < p.nx) {
+    L.ey_xp = p.E[1][c + sx];
+    L.ez_xp = p.E[2][c + sx];
+  } else if (p.met[0]) {
+    L.ey_xp = 0.f;
+    L.ez_xp = 0.f;
+  } else {
+    L.ey_xp = p.E[1][col];
+    L.ez_xp = p.E[2][col];
+  }
+  L.ez_yp = ywall ? 0.f : p.E[2][c + oy];
+  L.ex_yp = ywall ? 0.f : p.E[0][c + oy];
+  L.ey_zp = zwall ? 0.f : p.E[1][c + oz];
+  L.ex_zp = zwall ? 0.f : p.E[0][c + oz];
+  L.h[0] = p.H[0][c];
+  L.h[1] = p.H[1][c];
+  L.h[2] = p.H[2][c];
+}
+
+template <bool PML>
+__device__ __forceinline__ void h_march_pf(const StepParams& p, int j, int k, int i0, int i1,
+                                           int first_step) {
+  const int sx = p.ny * p.nz;
+  const int sy = p.nz;
+  const float dtdx = p.dtdx;
+  const bool ytop = (j + 1 == p.ny), ztop = (k + 1 == p.nz);
+  const bool ywall = ytop && p.met[1], zwall = ztop && p.met[2];
+  const int oy = ytop ? -(p.ny - 1) * sy : sy;
+  const int oz = ztop ? -(p.nz - 1) : 1;
+  const int col = j * sy + k;
+  int c = i0 * sx + col;
+  HColumn hcol = {};
+  int col_axes = 0;
+  if (PML) {
+    hcol = h_column(p, j, k);
+    const unsigned lanes = __activemask();
+    col_axes = (__any_sync(lanes, hcol.f2 || hcol.b1) ? 2 : 0) |
+               (__any_sync(lanes, hcol.f0 || hcol.b2) ? 4 : 0);
+  }
+  float ey = p.E[1][c];
+  float ez = p.E[2][c];
+  HLoads cur;
+  h_loads(p, cur, i0, c, col, sx, oy, oz, ywall, zwall);
+  for (int i = i0; i < i1; ++i, c += sx) {
+    HLoads nxt;
+    if (i + 1 < i1) h_loads(p, nxt, i + 1, c + sx, col, sx, oy, oz, ywall, zwall);
+    const float cx = dtdx * (((cur.ez_yp - ez) + ey) - cur.ey_zp);
+    const float cy = dtdx * (((cur.ex_zp - cur.ex) + ez) - cur.ez_xp);
+    const float cz = dtdx * (((cur.ey_xp - ey) + cur.ex) - cur.ex_yp);
+    float h_new[3];
+    HPlane pl = {};
+    int axes = 0;
+    if (PML) {
+      pl = h_plane(p, i);
+      axes = col_axes | ((pl.f1 || pl.b0) ? 1 : 0);
+      if (h_needs_plane(axes)) h_plane_coefficients(p, i, pl);
+    }
+    h_cell<PML>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, cur.h, h_new);
+    p.H[0][c] = h_new[0];
+    p.H[1][c] = h_new[1];
+    p.H[2][c] = h_new[2];
+    ey = cur.ey_xp;
+    ez = cur.ez_xp;
+    cur = nxt;
+  }
+}
+
+struct ELoads {
+  float hx, hy, hz, hz_ym, hx_ym, hy_zm, hx_zm, d[3], inv[3];
+};
+
+__device__ __forceinline__ void e_loads(const StepParams& p, ELoads& L, int i, int c, int j, int k, int jm,
+                                        int km, int sx, int sy) {
+  L.hx = p.H[0][c];
+  L.hy = p.H[1][c];
+  L.hz = p.H[2][c];
+  L.hz_ym = L.hx_ym = L.hy_zm = L.hx_zm = 0.f;
+  if (jm >= 0) {
+    const int cm = i * sx + jm * sy + k;
+    L.hz_ym = p.H[2][cm];
+    L.hx_ym = p.H[0][cm];
+  }
+  if (km >= 0) {
+    const int cm = i * sx + j * sy + km;
+    L.hy_zm = p.H[1][cm];
+    L.hx_zm = p.H[0][cm];
+  }
+  L.d[0] = p.D[0][c];
+  L.d[1] = p.D[1][c];
+  L.d[2] = p.D[2][c];
+  L.inv[0] = __ldg(p.inv_eps[0] + c);
+  L.inv[1] = __ldg(p.inv_eps[1] + c);
+  L.inv[2] = __ldg(p.inv_eps[2] + c);
+}
+
+template <bool PML>
+__device__ __forceinline__ void e_march_pf(const StepParams& p, int j, int k, int i0, int i1,
+                                           int parity, const double* words) {
+  const int sx = p.ny * p.nz;
+  const int sy = p.nz;
+  const float dtdx = p.dtdx;
+  const int jm = j == 0 ? (p.met[1] ? -1 : p.ny - 1) : j - 1;
+  const int km = k == 0 ? (p.met[2] ? -1 : p.nz - 1) : k - 1;
+  const int col = j * sy + k;
+  int c = i0 * sx + col;
+  EColumn ecol = {};
+  int col_axes = 0;
+  if (PML) {
+    ecol = e_column(p, j, k);
+    const unsigned lanes = __activemask();
+    col_axes = (__any_sync(lanes, ecol.f2 || ecol.w1) ? 2 : 0) |
+               (__any_sync(lanes, ecol.f0 || ecol.w2) ? 4 : 0);
+  }
+  float hy_xm = 0.f, hz_xm = 0.f;
+  {
+    int im = i0 - 1;
+    if (im < 0) im = p.met[0] ? -1 : p.nx - 1;
+    if (im >= 0) {
+      hy_xm = p.H[1][im * sx + col];
+      hz_xm = p.H[2][im * sx + col];
+    }
+  }
+  ELoads cur;
+  e_loads(p, cur, i0, c, j, k, jm, km, sx, sy);
+  for (int i = i0; i < i1; ++i, c += sx) {
+    ELoads nxt;
+    if (i + 1 < i1) e_loads(p, nxt, i + 1, c + sx, j, k, jm, km, sx, sy);
+    const float cx = dtdx * (((cur.hz_ym - cur.hz) + cur.hy) - cur.hy_zm);
+    const float cy = dtdx * (((cur.hx_zm - cur.hx) + cur.hz) - hz_xm);
+    const float cz = dtdx * (((hy_xm - cur.hy) + cur.hx) - cur.hx_ym);
+    EPlane pl = {};
+    int axes = 0;
+    if (PML) {
+      pl = e_plane(p, i);
+      axes = col_axes | ((pl.f1 || pl.w0) ? 1 : 0);
+      if (axes & 1) e_plane_coefficients(p, i, pl);
+    }
+    e_cell<PML>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, cur.d, cur.inv, words);
+    hy_xm = cur.hy;
+    hz_xm = cur.hz;
+    cur = nxt;
+  }
+}
+
+template <bool PML>
+__global__ void __launch_bounds__(256, 4) h_generic_pf(const __grid_constant__ StepParams p,
+                                                       int first_step, int xchunk) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (k >= p.nz || j >= p.ny) return;
+  const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  if (PML && cta_inner(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x))
+    h_march_pf<false>(p, j, k, i0, i1, first_step);
+  else
+    h_march_pf<PML>(p, j, k, i0, i1, first_step);
+}
+
+template <bool PML>
+__global__ void __launch_bounds__(256, 4) e_generic_pf(const __grid_constant__ StepParams p, int parity,
+                                                       int xchunk) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (k >= p.nz || j >= p.ny) return;
+  const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  if (PML && cta_inner(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x))
+    e_march_pf<false>(p, j, k, i0, i1, parity, p.src_words);
+  else
+    e_march_pf<PML>(p, j, k, i0, i1, parity, p.src_words);
+}
+
 // Generic kernels: plain loads, one thread per (y, z) column marching over an x chunk.
 template <bool PML>
 __global__ void __launch_bounds__(256, 5) h_generic(const __grid_constant__ StepParams p,
@@ -549,8 +740,11 @@ __global__ void __launch_bounds__(256, 5) h_generic(const __grid_constant__ Step
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
-  const int i0 = blockIdx.z * xchunk;
-  h_march<PML>(p, j, k, i0, min(i0 + xchunk, p.nx), first_step);
+  const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  if (PML && cta_inner(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x))
+    h_march<false>(p, j, k, i0, i1, first_step);
+  else
+    h_march<PML>(p, j, k, i0, i1, first_step);
 }
 
 template <bool PML>
@@ -559,8 +753,11 @@ __global__ void __launch_bounds__(256, 5) e_generic(const __grid_constant__ Step
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
-  const int i0 = blockIdx.z * xchunk;
-  e_march<PML>(p, j, k, i0, min(i0 + xchunk, p.nx), parity, p.src_words);
+  const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  if (PML && cta_inner(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x))
+    e_march<false>(p, j, k, i0, i1, parity, p.src_words);
+  else
+    e_march<PML>(p, j, k, i0, i1, parity, p.src_words);
 }
 
 // ------------------------------------------------------------------------------------
@@ -1060,12 +1257,14 @@ __global__ void __launch_bounds__(256, 5) step_batched(const __grid_constant__ B
   if (k >= sp.nz || j >= sp.ny) return;
   const int i0 = w.w * tb.xchunk;
   const int i1 = min(i0 + tb.xchunk, sp.nx);
+  const bool pml = sp.pml && !cta_inner(sp, i0, i1, w.z * (int)blockDim.y, (int)blockDim.y,
+                                        w.y * (int)blockDim.x, (int)blockDim.x);
   if (PART == 0) {
-    if (sp.pml) h_march<true>(sp, j, k, i0, i1, n == 0);
+    if (pml) h_march<true>(sp, j, k, i0, i1, n == 0);
     else h_march<false>(sp, j, k, i0, i1, n == 0);
   } else {
     const double* words = st.words + n * sp.nsrc;
-    if (sp.pml) e_march<true>(sp, j, k, i0, i1, (int)(n & 1), words);
+    if (pml) e_march<true>(sp, j, k, i0, i1, (int)(n & 1), words);
     else e_march<false>(sp, j, k, i0, i1, (int)(n & 1), words);
   }
 }
@@ -1356,6 +1555,7 @@ struct mgb_sim {
   StepParams step;
   TileMaps maps;
   bool tiles = false;        // step with the tile kernels
+  bool prefetch = false;     // generic kernels: the prefetching marches
   bool tiles_ready = false;  // their tensor maps are built
   size_t h_smem = 0, e_smem = 0;
   const double* words = nullptr;
@@ -1565,6 +1765,22 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
   StepParams& p = sim->step;
   p.nx = d.nx; p.ny = d.ny; p.nz = d.nz;
   p.pml = d.pml_active ? 1 : 0;
+  {
+    const int n[3] = {d.nx, d.ny, d.nz};
+    for (int a = 0; a < 3; ++a) {
+      p.inner[2 * a] = 0;
+      p.inner[2 * a + 1] = n[a];
+    }
+    if (p.pml) {
+      const mgb_aux* families[5] = {d.B, d.fwH, d.fwE, d.fuB, d.fuD};
+      for (const mgb_aux* fam : families)
+        for (int q = 0; q < 3; ++q) {
+          const mgb_aux& a = fam[q];
+          if (a.a1 > a.a0) p.inner[2 * a.axis] = std::max(p.inner[2 * a.axis], a.a1);
+          if (a.b1 > a.b0) p.inner[2 * a.axis + 1] = std::min(p.inner[2 * a.axis + 1], a.b0);
+        }
+    }
+  }
   for (int a = 0; a < 3; ++a) p.met[a] = d.metallic[a] ? 1 : 0;
   p.dtdx = d.dtdx;
   for (int l = 0; l < 2; ++l)
@@ -1675,7 +1891,15 @@ int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s) {
     const dim3 block(sim->block_z, sim->block_y, 1);
     const dim3 grid((p.nz + block.x - 1) / block.x, (p.ny + block.y - 1) / block.y,
                     (p.nx + sim->xchunk - 1) / sim->xchunk);
-    if (part == 0) {
+    if (sim->prefetch) {
+      if (part == 0) {
+        if (pml) h_generic_pf<true><<<grid, block, 0, s>>>(p, n == 0, sim->xchunk);
+        else h_generic_pf<false><<<grid, block, 0, s>>>(p, n == 0, sim->xchunk);
+      } else {
+        if (pml) e_generic_pf<true><<<grid, block, 0, s>>>(p, (int)(n & 1), sim->xchunk);
+        else e_generic_pf<false><<<grid, block, 0, s>>>(p, (int)(n & 1), sim->xchunk);
+      }
+    } else if (part == 0) {
       if (pml) h_generic<true><<<grid, block, 0, s>>>(p, n == 0, sim->xchunk);
       else h_generic<false><<<grid, block, 0, s>>>(p, n == 0, sim->xchunk);
     } else {
@@ -1811,16 +2035,18 @@ int mgb_uses_tiles(mgb_sim* sim) { return sim != nullptr && sim->tiles ? 1 : 0; 
 
 int mgb_select_kernels(mgb_sim* sim, int32_t family) {
   if (sim == nullptr) return fail(MGB_ERR_ARGUMENT, "null plan");
-  if (family == 0) {
+  if (family == 0 || family == 2) {
     sim->tiles = false;
+    sim->prefetch = family == 2;
     return MGB_OK;
   }
   if (family == 1) {
     if (!sim->tiles_ready) return fail(MGB_ERR_UNSUPPORTED, "the tile kernels need a z extent that is a multiple of 4");
     sim->tiles = true;
+    sim->prefetch = false;
     return MGB_OK;
   }
-  return fail(MGB_ERR_ARGUMENT, "kernel family is 0 (generic) or 1 (tiles)");
+  return fail(MGB_ERR_ARGUMENT, "kernel family is 0 (generic), 1 (tiles) or 2 (generic, prefetching)");
 }
 
 void mgb_destroy(mgb_sim* sim) { delete sim; }

@@ -40,9 +40,11 @@ FIELD_NAMES = ("E", "D", "H")
 SOURCE_WINDOW = 4096
 
 # Kernel choices the autotuner times: (family, block_z, block_y, x_chunk); family 1 is
-# the tile kernels (block shape fixed at 64 x 8, x_chunk used), family 0 the generic ones.
+# the tile kernels (block shape fixed at 64 x 8, x_chunk used), family 0 the generic ones,
+# family 2 the generic ones with the next plane's loads issued ahead.
 AUTOTUNE_CANDIDATES = ((0, 32, 4, 4), (0, 32, 8, 4), (0, 32, 4, 8), (0, 64, 2, 8),
-                       (0, 16, 8, 4), (0, 16, 16, 4), (1, 64, 8, 4), (1, 64, 8, 8))
+                       (0, 16, 8, 4), (0, 16, 16, 4), (1, 64, 8, 4), (1, 64, 8, 8),
+                       (2, 32, 4, 4), (2, 32, 4, 8), (2, 32, 8, 4), (2, 64, 2, 4))
 _AUTOTUNE_CACHE: Dict[tuple, Tuple[int, int, int, int]] = {}
 
 
@@ -335,7 +337,7 @@ class Engine:
         """Apply a kernel choice (family, block_z, block_y, x_chunk)."""
         family, bz, by, xc = choice
         _lib.check(self.lib, self.lib.mgb_select_kernels(self.handle, family))
-        if family == 0:
+        if family in (0, 2):
             self.set_launch_shape(bz, by, xc)
         else:
             self.set_launch_shape(32, 8, xc)

@@ -18,6 +18,10 @@ grid's cell centres, as the configurations specify; there is no dataset.
 * ``sphere128``: a 128^3 sphere case with one flux plane.
 * ``sphere192``: the 192^3 sphere case with one 50-frequency flux plane (working set
   ~0.4 GB, above the L2 size): the case detailed kernel profiles are taken on.
+* ``adjoint96`` (:func:`adjoint96`): 96^3 at resolution 10, 10-cell PML, a 16 x 64 x 64
+  design box centred in the cell with eps ~ U[1, 12] (seed 0), Ez Gaussian (fcen 0.15,
+  df 0.05) at x = -L/4, a 10-frequency x-normal flux plane 4 cells past the box;
+  4000 steps, checkpoints every 200.
 """
 
 from __future__ import annotations
@@ -82,3 +86,30 @@ def build(name: str, driver_cls=None, susceptibility_cls=None, **driver_kwargs):
                                    size=(0, 7.6, 7.6), decimation_factor=0) for sign in (1.0, -1.0)]
         return d, flux, []
     raise ValueError(f"unknown workload {name!r}; choose from {WORKLOADS}")
+
+
+ADJOINT96_BOX = ((40, 56), (16, 80), (16, 80))
+ADJOINT96_STEPS = 4000
+
+
+def adjoint96(eps_box=None, driver_cls=None, seed: int = 0, **driver_kwargs):
+    """The adjoint workload; returns ``(driver, flux, box, eps_box)``."""
+    if driver_cls is None:
+        from .driver import FdtdDriver as driver_cls  # noqa: N813
+    box = ADJOINT96_BOX
+    shape = tuple(b - a for a, b in box)
+    if eps_box is None:
+        eps_box = np.random.default_rng(seed).uniform(1.0, 12.0, shape)
+    d = driver_cls(cell_size=(9.6, 9.6, 9.6), resolution=10, courant=0.5, force_complex_fields=False,
+                   boundaries="metallic", **driver_kwargs)
+    d.setup_pml(10)
+    eps = np.ones(d.grid.shape)
+    (i0, i1), (j0, j1), (k0, k1) = box
+    eps[i0:i1, j0:j1, k0:k1] = eps_box
+    d.set_epsilon(eps)
+    d.add_source({"source_type": "gaussian", "component": "Ez", "center": (-2.4, 0.0, 0.0),
+                  "size": (0, 0, 0), "frequency": 0.15, "fwidth": 0.05})
+    plane_x = (i1 + 4 - 48) / 10.0
+    flux = d.add_flux_monitor(fcen=0.15, df=0.05, nfreq=10, center=(plane_x, 0.0, 0.0), size=(0, 6.4, 6.4),
+                              decimation_factor=0)
+    return d, flux, box, eps_box

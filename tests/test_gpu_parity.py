@@ -27,6 +27,8 @@ FIELDS = ("Ex", "Ey", "Ez", "Dx", "Dy", "Dz", "Bx", "By", "Bz", "Hx", "Hy", "Hz"
 
 TILES = (1, 64, 8, 8)
 GENERIC = (0, 32, 8, 4)
+PREFETCH = (2, 32, 4, 4)
+MODES = {"tiles": TILES, "generic": GENERIC, "prefetch": PREFETCH}
 
 
 def gpu_case(case, steps=None, kernels=None, chunks=None):
@@ -44,15 +46,15 @@ def gpu_case(case, steps=None, kernels=None, chunks=None):
     return driver, flux, dft
 
 
-@pytest.mark.parametrize("mode", ["tiles", "generic"])
+@pytest.mark.parametrize("mode", sorted(MODES))
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_fields_are_the_reference_words(gpu, name, mode):
-    """Both kernel families: the TMA tile kernels (z extent a multiple of 4) and the
-    generic plain-load kernels."""
+    """Every kernel family: the TMA tile kernels (z extent a multiple of 4), the generic
+    plain-load kernels and their prefetching form."""
     case = CASES[name]
     gold = golden_io.fields(name)
     tiles = mode == "tiles" and case["n"][2] % 4 == 0
-    driver, flux, dft = gpu_case(case, kernels=TILES if tiles else GENERIC)
+    driver, flux, dft = gpu_case(case, kernels=TILES if tiles else MODES["generic" if mode == "tiles" else mode])
     assert driver.engine.uses_tiles == tiles
     for c in FIELDS:
         got = driver.get_field(c, cell_centered=False)
@@ -79,7 +81,8 @@ def test_fields_are_the_reference_words(gpu, name, mode):
 
 @pytest.mark.parametrize("name", ["mixed", "tile_mixed", "tile_periodic_pml"])
 @pytest.mark.parametrize("choice", [(0, 32, 8, 16), (0, 64, 4, 7), (0, 16, 16, 200), (0, 128, 2, 1),
-                                    (0, 32, 4, 3), (1, 64, 8, 1), (1, 64, 8, 5), (1, 64, 8, 200)])
+                                    (0, 32, 4, 3), (1, 64, 8, 1), (1, 64, 8, 5), (1, 64, 8, 200),
+                                    (2, 32, 8, 16), (2, 64, 4, 7), (2, 32, 4, 1), (2, 128, 2, 3)])
 def test_launch_shape_does_not_change_a_word(gpu, choice, name):
     """The x chunk (both families) and block shape (generic family) change no word."""
     case = CASES[name]
@@ -88,7 +91,7 @@ def test_launch_shape_does_not_change_a_word(gpu, choice, name):
     gold = golden_io.fields(name)
     driver, _, _ = gpu_case(case, kernels=choice)
     for c in FIELDS:
-        assert np.array_equal(driver.get_field(c, cell_centered=False), gold[c]), (shape, c)
+        assert np.array_equal(driver.get_field(c, cell_centered=False), gold[c]), (choice, c)
     driver.close()
 
 
@@ -114,11 +117,10 @@ def test_chunked_runs_equal_one_run(gpu):
     driver.close()
 
 
-@pytest.mark.parametrize("mode", ["tiles", "generic"])
+@pytest.mark.parametrize("mode", sorted(MODES))
 def test_sphere80_words_after_200_steps(gpu, mode):
     gold = golden_io.digest()
-    driver, flux, _ = gpu_case(SPHERE80, steps=gold["steps"],
-                               kernels=TILES if mode == "tiles" else GENERIC)
+    driver, flux, _ = gpu_case(SPHERE80, steps=gold["steps"], kernels=MODES[mode])
     assert driver.engine.uses_tiles == (mode == "tiles")
     for c, expected in gold["sha256"].items():
         words = np.ascontiguousarray(driver.get_field(c, cell_centered=False), dtype=np.float32)

@@ -197,23 +197,37 @@ __device__ __forceinline__ float curl_form(float f, float curl, bool member, flo
 // Each axis switches on one feature per component (x: Bx own, By dsigu, Bz dsig;
 // y: Bx dsig, By own, Bz dsigu; z: Bx dsigu, By dsig, Bz own). `h_old` is the stored H
 // word (the old B outside the own-axis membership).
+// Every auxiliary word an H cell reads, loaded from the membership flags alone, so the
+// caller issues these loads together with the field loads (one round trip per plane).
+struct HAux {
+  float b[3], w[3], u[3];
+};
+
+__device__ __forceinline__ void h_aux_load(const StepParams& p, const HColumn& col, const HPlane& pl, int c,
+                                           HAux& a) {
+  const bool sb[3] = {pl.b0, col.b1, col.b2};
+  const bool sf[3] = {col.f0, pl.f1, col.f2};
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    a.b[q] = sb[q] ? p.B[q].data[c] : 0.f;
+    a.w[q] = sb[q] ? p.fwH[q].data[c] : 0.f;
+    a.u[q] = sf[q] ? p.fuB[q].data[c] : 0.f;
+  }
+}
+
 template <bool SX, bool SY, bool SZ>
 __device__ __forceinline__ void h_cell_v(const StepParams& p, const HColumn& col,
                                          const HPlane& pl, int first_step, int c, float cx,
-                                         float cy, float cz, const float h_old[3],
+                                         float cy, float cz, const float h_old[3], const HAux& a,
                                          float h_new[3]) {
   const bool sb0 = SX && pl.b0, sb1 = SY && col.b1, sb2 = SZ && col.b2;
   const bool sf0 = SZ && col.f0, sf1 = SX && pl.f1, sf2 = SY && col.f2;
-  // Loads: every auxiliary word of the cell, before any store.
-  float b0 = sb0 ? p.B[0].data[c] : h_old[0];
-  float b1 = sb1 ? p.B[1].data[c] : h_old[1];
-  float b2 = sb2 ? p.B[2].data[c] : h_old[2];
-  const float w0 = sb0 ? p.fwH[0].data[c] : 0.f;
-  const float w1 = sb1 ? p.fwH[1].data[c] : 0.f;
-  const float w2 = sb2 ? p.fwH[2].data[c] : 0.f;
-  const float u0 = sf0 ? p.fuB[0].data[c] : 0.f;
-  const float u1 = sf1 ? p.fuB[1].data[c] : 0.f;
-  const float u2 = sf2 ? p.fuB[2].data[c] : 0.f;
+  // The cell's auxiliary words (loaded by the caller, before any store).
+  float b0 = sb0 ? a.b[0] : h_old[0];
+  float b1 = sb1 ? a.b[1] : h_old[1];
+  float b2 = sb2 ? a.b[2] : h_old[2];
+  const float w0 = a.w[0], w1 = a.w[1], w2 = a.w[2];
+  const float u0 = a.u[0], u1 = a.u[1], u2 = a.u[2];
   // Bx: dsig y, dsigu z; By: dsig z, dsigu x; Bz: dsig x, dsigu y.
   float n0 = 0.f, n1 = 0.f, n2 = 0.f;
   b0 = curl_form<SY, SZ>(b0, cx, sf0, u0, col.kms_yh, col.sinv_yh, col.kms_zh, col.sinv_zh, n0);
@@ -243,7 +257,7 @@ template <bool PML>
 __device__ __forceinline__ void h_cell(const StepParams& p, const HColumn& col, const HPlane& pl,
                                        int axes, int first_step, int i, int j, int k, int c,
                                        float cx, float cy, float cz, const float h_old[3],
-                                       float h_new[3]) {
+                                       const HAux& a, float h_new[3]) {
   if (p.met[0] && i == 0) cx = 0.f;
   if (p.met[1] && j == 0) cy = 0.f;
   if (p.met[2] && k == 0) cz = 0.f;
@@ -251,12 +265,12 @@ __device__ __forceinline__ void h_cell(const StepParams& p, const HColumn& col, 
   // in its component's own-axis membership, so there H is B and clearing H_new after
   // the accumulation is the same word.
   if (!PML || axes == 0) {
-    h_cell_v<false, false, false>(p, col, pl, first_step, c, cx, cy, cz, h_old, h_new);
+    h_cell_v<false, false, false>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new);
   } else {
     // The z-only edge (the two z-edge warps of every interior row) is the commonest slow
     // case; every other mix takes the general variant.
-    if (axes == 4) h_cell_v<false, false, true>(p, col, pl, first_step, c, cx, cy, cz, h_old, h_new);
-    else h_cell_v<true, true, true>(p, col, pl, first_step, c, cx, cy, cz, h_old, h_new);
+    if (axes == 4) h_cell_v<false, false, true>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new);
+    else h_cell_v<true, true, true>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new);
   }
   if (p.met[0] && i == 0) h_new[0] = 0.f;
   if (p.met[1] && j == 0) h_new[1] = 0.f;
@@ -302,27 +316,39 @@ __device__ __forceinline__ void e_plane_coefficients(const StepParams& p, int i,
 // for one cell at offset c, for a warp that may touch the x (SX), y (SY) and z (SZ)
 // memberships (x: Dx own, Dy dsigu, Dz dsig; y: Dx dsig, Dy own, Dz dsigu; z: Dx dsigu,
 // Dy dsig, Dz own). <false, false, false> is the plain update.
+// Every auxiliary word an E cell reads (split-field fu of D, f_w of E, and the old E on
+// the own-axis membership), loaded from the flags alone with the field loads.
+struct EAux {
+  float u[3], fw[3], e[3];
+};
+
+__device__ __forceinline__ void e_aux_load(const StepParams& p, const EColumn& col, const EPlane& pl, int c,
+                                           EAux& a) {
+  const bool sf[3] = {col.f0, pl.f1, col.f2};
+  const bool sw[3] = {pl.w0, col.w1, col.w2};
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    a.u[q] = sf[q] ? p.fuD[q].data[c] : 0.f;
+    a.fw[q] = sw[q] ? p.fwE[q].data[c] : 0.f;
+    a.e[q] = sw[q] ? p.E[q][c] : 0.f;
+  }
+}
+
 template <bool SX, bool SY, bool SZ>
 __device__ __forceinline__ void e_cell_v(const StepParams& p, const EColumn& col, const EPlane& pl,
                                          int parity, int i, int j, int k, int c, float cx,
                                          float cy, float cz, float d[3], const float inv[3],
-                                         const double* words) {
+                                         const double* words, const EAux& a) {
   const bool wx = p.met[0] && i == 0, wy = p.met[1] && j == 0, wz = p.met[2] && k == 0;
   if (wy || wz) cx = 0.f;
   if (wx || wz) cy = 0.f;
   if (wx || wy) cz = 0.f;
   const bool sf0 = SZ && col.f0, sf1 = SX && pl.f1, sf2 = SY && col.f2;
   const bool sw0 = SX && pl.w0, sw1 = SY && col.w1, sw2 = SZ && col.w2;
-  // Loads: every auxiliary word of the cell, before any store.
-  const float u0 = sf0 ? p.fuD[0].data[c] : 0.f;
-  const float u1 = sf1 ? p.fuD[1].data[c] : 0.f;
-  const float u2 = sf2 ? p.fuD[2].data[c] : 0.f;
-  const float fw0 = sw0 ? p.fwE[0].data[c] : 0.f;
-  const float fw1 = sw1 ? p.fwE[1].data[c] : 0.f;
-  const float fw2 = sw2 ? p.fwE[2].data[c] : 0.f;
-  const float e0 = sw0 ? p.E[0][c] : 0.f;
-  const float e1 = sw1 ? p.E[1][c] : 0.f;
-  const float e2 = sw2 ? p.E[2][c] : 0.f;
+  // The cell's auxiliary words (loaded by the caller, before any store).
+  const float u0 = a.u[0], u1 = a.u[1], u2 = a.u[2];
+  const float fw0 = a.fw[0], fw1 = a.fw[1], fw2 = a.fw[2];
+  const float e0 = a.e[0], e1 = a.e[1], e2 = a.e[2];
   // Dx: dsig y, dsigu z; Dy: dsig z, dsigu x; Dz: dsig x, dsigu y.
   float n0 = 0.f, n1 = 0.f, n2 = 0.f;
   d[0] = curl_form<SY, SZ>(d[0], cx, sf0, u0, col.kms_y, col.sinv_y, col.kms_z, col.sinv_z, n0);
@@ -402,17 +428,17 @@ template <bool PML>
 __device__ __forceinline__ void e_cell(const StepParams& p, const EColumn& col, const EPlane& pl,
                                        int axes, int parity, int i, int j, int k, int c, float cx,
                                        float cy, float cz, float d[3], const float inv[3],
-                                       const double* words) {
+                                       const double* words, const EAux& a) {
   if (!PML) axes = 0;
   switch (axes) {
-    case 0: e_cell_v<false, false, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words); break;
-    case 1: e_cell_v<true, false, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words); break;
-    case 2: e_cell_v<false, true, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words); break;
-    case 3: e_cell_v<true, true, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words); break;
-    case 4: e_cell_v<false, false, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words); break;
-    case 5: e_cell_v<true, false, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words); break;
-    case 6: e_cell_v<false, true, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words); break;
-    default: e_cell_v<true, true, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words); break;
+    case 0: e_cell_v<false, false, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words, a); break;
+    case 1: e_cell_v<true, false, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words, a); break;
+    case 2: e_cell_v<false, true, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words, a); break;
+    case 3: e_cell_v<true, true, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words, a); break;
+    case 4: e_cell_v<false, false, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words, a); break;
+    case 5: e_cell_v<true, false, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words, a); break;
+    case 6: e_cell_v<false, true, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words, a); break;
+    default: e_cell_v<true, true, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words, a); break;
   }
 }
 
@@ -452,6 +478,13 @@ __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i
   float ey = Ey[c];
   float ez = Ez[c];
   for (int i = i0; i < i1; ++i, c += sx) {
+    HPlane pl = {};
+    int axes = 0;
+    if (PML) {
+      pl = h_plane(p, i);
+      axes = col_axes | ((pl.f1 || pl.b0) ? 1 : 0);
+      if (h_needs_plane(axes)) h_plane_coefficients(p, i, pl);
+    }
     const float ex = Ex[c];
     float ey_xp, ez_xp;
     if (i + 1 < p.nx) {
@@ -468,20 +501,15 @@ __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i
     const float ex_yp = ywall ? 0.f : Ex[c + oy];
     const float ey_zp = zwall ? 0.f : Ey[c + oz];
     const float ex_zp = zwall ? 0.f : Ex[c + oz];
+    const float h_old[3] = {p.H[0][c], p.H[1][c], p.H[2][c]};
+    HAux ax = {};
+    if (PML && axes != 0) h_aux_load(p, hcol, pl, c, ax);
     // MEEP's association ((g1s - g1) + g2) - g2s, then the dtdx scale.
     const float cx = dtdx * (((ez_yp - ez) + ey) - ey_zp);
     const float cy = dtdx * (((ex_zp - ex) + ez) - ez_xp);
     const float cz = dtdx * (((ey_xp - ey) + ex) - ex_yp);
-    const float h_old[3] = {p.H[0][c], p.H[1][c], p.H[2][c]};
     float h_new[3];
-    HPlane pl = {};
-    int axes = 0;
-    if (PML) {
-      pl = h_plane(p, i);
-      axes = col_axes | ((pl.f1 || pl.b0) ? 1 : 0);
-      if (h_needs_plane(axes)) h_plane_coefficients(p, i, pl);
-    }
-    h_cell<PML>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, h_old, h_new);
+    h_cell<PML>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, h_old, ax, h_new);
     p.H[0][c] = h_new[0];
     p.H[1][c] = h_new[1];
     p.H[2][c] = h_new[2];
@@ -522,6 +550,13 @@ __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i
     }
   }
   for (int i = i0; i < i1; ++i, c += sx) {
+    EPlane pl = {};
+    int axes = 0;
+    if (PML) {
+      pl = e_plane(p, i);
+      axes = col_axes | ((pl.f1 || pl.w0) ? 1 : 0);
+      if (axes & 1) e_plane_coefficients(p, i, pl);
+    }
     const float hx = Hx[c], hy = Hy[c], hz = Hz[c];
     float hz_ym = 0.f, hx_ym = 0.f, hy_zm = 0.f, hx_zm = 0.f;
     if (jm >= 0) {
@@ -534,19 +569,14 @@ __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i
       hy_zm = Hy[cm];
       hx_zm = Hx[cm];
     }
+    float d[3] = {p.D[0][c], p.D[1][c], p.D[2][c]};
+    const float inv[3] = {__ldg(p.inv_eps[0] + c), __ldg(p.inv_eps[1] + c), __ldg(p.inv_eps[2] + c)};
+    EAux ax = {};
+    if (PML && axes != 0) e_aux_load(p, ecol, pl, c, ax);
     const float cx = dtdx * (((hz_ym - hz) + hy) - hy_zm);
     const float cy = dtdx * (((hx_zm - hx) + hz) - hz_xm);
     const float cz = dtdx * (((hy_xm - hy) + hx) - hx_ym);
-    float d[3] = {p.D[0][c], p.D[1][c], p.D[2][c]};
-    const float inv[3] = {__ldg(p.inv_eps[0] + c), __ldg(p.inv_eps[1] + c), __ldg(p.inv_eps[2] + c)};
-    EPlane pl = {};
-    int axes = 0;
-    if (PML) {
-      pl = e_plane(p, i);
-      axes = col_axes | ((pl.f1 || pl.w0) ? 1 : 0);
-      if (axes & 1) e_plane_coefficients(p, i, pl);
-    }
-    e_cell<PML>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, d, inv, words);
+    e_cell<PML>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, d, inv, words, ax);
     hy_xm = hy;
     hz_xm = hz;
   }
@@ -609,10 +639,6 @@ __device__ __forceinline__ void h_march_pf(const StepParams& p, int j, int k, in
   for (int i = i0; i < i1; ++i, c += sx) {
     HLoads nxt;
     if (i + 1 < i1) h_loads(p, nxt, i + 1, c + sx, col, sx, oy, oz, ywall, zwall);
-    const float cx = dtdx * (((cur.ez_yp - ez) + ey) - cur.ey_zp);
-    const float cy = dtdx * (((cur.ex_zp - cur.ex) + ez) - cur.ez_xp);
-    const float cz = dtdx * (((cur.ey_xp - ey) + cur.ex) - cur.ex_yp);
-    float h_new[3];
     HPlane pl = {};
     int axes = 0;
     if (PML) {
@@ -620,7 +646,13 @@ __device__ __forceinline__ void h_march_pf(const StepParams& p, int j, int k, in
       axes = col_axes | ((pl.f1 || pl.b0) ? 1 : 0);
       if (h_needs_plane(axes)) h_plane_coefficients(p, i, pl);
     }
-    h_cell<PML>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, cur.h, h_new);
+    HAux ax = {};
+    if (PML && axes != 0) h_aux_load(p, hcol, pl, c, ax);
+    const float cx = dtdx * (((cur.ez_yp - ez) + ey) - cur.ey_zp);
+    const float cy = dtdx * (((cur.ex_zp - cur.ex) + ez) - cur.ez_xp);
+    const float cz = dtdx * (((cur.ey_xp - ey) + cur.ex) - cur.ex_yp);
+    float h_new[3];
+    h_cell<PML>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, cur.h, ax, h_new);
     p.H[0][c] = h_new[0];
     p.H[1][c] = h_new[1];
     p.H[2][c] = h_new[2];
@@ -690,9 +722,6 @@ __device__ __forceinline__ void e_march_pf(const StepParams& p, int j, int k, in
   for (int i = i0; i < i1; ++i, c += sx) {
     ELoads nxt;
     if (i + 1 < i1) e_loads(p, nxt, i + 1, c + sx, j, k, jm, km, sx, sy);
-    const float cx = dtdx * (((cur.hz_ym - cur.hz) + cur.hy) - cur.hy_zm);
-    const float cy = dtdx * (((cur.hx_zm - cur.hx) + cur.hz) - hz_xm);
-    const float cz = dtdx * (((hy_xm - cur.hy) + cur.hx) - cur.hx_ym);
     EPlane pl = {};
     int axes = 0;
     if (PML) {
@@ -700,7 +729,12 @@ __device__ __forceinline__ void e_march_pf(const StepParams& p, int j, int k, in
       axes = col_axes | ((pl.f1 || pl.w0) ? 1 : 0);
       if (axes & 1) e_plane_coefficients(p, i, pl);
     }
-    e_cell<PML>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, cur.d, cur.inv, words);
+    EAux ax = {};
+    if (PML && axes != 0) e_aux_load(p, ecol, pl, c, ax);
+    const float cx = dtdx * (((cur.hz_ym - cur.hz) + cur.hy) - cur.hy_zm);
+    const float cy = dtdx * (((cur.hx_zm - cur.hx) + cur.hz) - hz_xm);
+    const float cz = dtdx * (((hy_xm - cur.hy) + cur.hx) - cur.hx_ym);
+    e_cell<PML>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, cur.d, cur.inv, words, ax);
     hy_xm = cur.hy;
     hz_xm = cur.hz;
     cur = nxt;
@@ -926,7 +960,9 @@ __global__ void __launch_bounds__(kThreads, 2) h_tile(const __grid_constant__ St
         axes = col_axes | ((pl.f1 || pl.b0) ? 1 : 0);
         if (h_needs_plane(axes)) h_plane_coefficients(p, i, pl);
       }
-      h_cell<PML>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, h_old, h_new);
+      HAux ax = {};
+      if (PML && axes != 0) h_aux_load(p, hcol, pl, c, ax);
+      h_cell<PML>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, h_old, ax, h_new);
       p.H[0][c] = h_new[0];
       p.H[1][c] = h_new[1];
       p.H[2][c] = h_new[2];
@@ -1041,7 +1077,9 @@ __global__ void __launch_bounds__(kThreads, 2) e_tile(const __grid_constant__ St
         axes = col_axes | ((pl.f1 || pl.w0) ? 1 : 0);
         if (axes & 1) e_plane_coefficients(p, i, pl);
       }
-      e_cell<PML>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, d, inv, p.src_words);
+      EAux ax = {};
+      if (PML && axes != 0) e_aux_load(p, ecol, pl, c, ax);
+      e_cell<PML>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, d, inv, p.src_words, ax);
     }
     __syncthreads();  // the stage of plane i - 1 is read by everyone
     if (abort_flag) {

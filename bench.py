@@ -147,14 +147,21 @@ def cpu_threads() -> int:
     return os.cpu_count() or 1
 
 
-def time_oracle(workload: str, steps: int, budget_s: float = 20.0):
-    """Float32 oracle Mcell-steps/s on ``steps`` steps (capped to a ~``budget_s`` sample)."""
+def time_oracle(workload: str, steps: int, budget_s: float = 20.0, warmup: int = 1):
+    """Float32 oracle Mcell-steps/s on ``steps`` steps (capped to a ~``budget_s`` sample),
+    after ``warmup`` untimed steps (also capped to the budget)."""
     from meep_gpu_gb300 import FdtdDriver, workloads
     from oracle.oracle import Oracle, problem_from_driver
     os.environ.setdefault("OMP_NUM_THREADS", str(cpu_threads()))
     driver, _, _ = workloads.build(workload, FdtdDriver)
     oracle = Oracle(problem_from_driver(driver), "f32")
     oracle.run(1)  # warm-up (page-in, thread pool)
+    t0 = time.perf_counter()
+    oracle.run(1)
+    first = max(time.perf_counter() - t0, 1e-6)
+    extra = max(0, min(warmup - 2, int(0.25 * budget_s / first)))
+    if extra:
+        oracle.run(extra)
     t0 = time.perf_counter()
     oracle.run(1)
     per_step = max(time.perf_counter() - t0, 1e-6)
@@ -170,17 +177,17 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    value, sample, cells = time_oracle(args.workload, max(args.steps, 1), budget_s=60.0)
+    value, sample, cells = time_oracle(args.workload, max(args.steps, 1), budget_s=60.0, warmup=args.warmup)
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mcell-steps/s",
-        "n_gpus": args.gpus, "steps": sample, "warmup": 1,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(cells / (value * 1e6) * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": args.workload, "cells": cells},
         "cpu_baseline": {"value": round(value, 3), "unit": "Mcell-steps/s", "cores": cpu_threads(),
                          "kind": "port",
                          "sample": f"{sample} full-grid steps of {args.workload} on the float32 C oracle "
-                                   f"(OpenMP, {cpu_threads()} threads)"},
+                                   f"(OpenMP, {cpu_threads()} threads), timed after the warm-up"},
         "e2e": {"value": round(value, 3), "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -444,20 +451,36 @@ def bench_adjoint(args):
         o.run(steps)
         return float(np.sum(o.flux_spectrum(0)))
 
-    rng = np.random.default_rng(0)
     h = 1e-3
-    j64 = oracle_j(eps_box)
-    picks = [tuple(int(rng.integers(0, n)) for n in eps_box.shape) for _ in range(args.fd_voxels)]
-    def bumped(v, sign):
-        values = eps_box.copy()
-        values[v] += sign * h
-        return values
-
-    fd = [(oracle_j(bumped(v, 1)) - oracle_j(bumped(v, -1))) / (2 * h) for v in picks]
-    ad = [float(grad[v]) for v in picks]
+    fixture = ROOT / "tests" / "golden" / "adjoint96_fd.json"
+    if fixture.exists():
+        # float64 central differences recorded by tests/golden/make_adjoint_fd.py, whose
+        # voxels and direction come from the same seeded generator as below
+        record = json.loads(fixture.read_text())
+        count = len(record["voxels"])
+    else:
+        record, count = None, args.fd_voxels
+    rng = np.random.default_rng(0)
+    picks = [tuple(int(rng.integers(0, n)) for n in eps_box.shape) for _ in range(count)]
     direction = rng.standard_normal(eps_box.shape)
     direction /= np.linalg.norm(direction)
-    fd_dir = (oracle_j(eps_box + h * direction) - oracle_j(eps_box - h * direction)) / (2 * h)
+    if record is not None:
+        assert [tuple(v["voxel"]) for v in record["voxels"]] == picks, "fixture voxels differ from the seeds"
+        j64 = record["objective"]
+        fd = [v["fd"] for v in record["voxels"]]
+        fd_dir = record["directional_fd"]
+        fd_source = "tests/golden/adjoint96_fd.json (float64 oracle)"
+    else:
+        def bumped(v, sign):
+            values = eps_box.copy()
+            values[v] += sign * h
+            return values
+
+        j64 = oracle_j(eps_box)
+        fd = [(oracle_j(bumped(v, 1)) - oracle_j(bumped(v, -1))) / (2 * h) for v in picks]
+        fd_dir = (oracle_j(eps_box + h * direction) - oracle_j(eps_box - h * direction)) / (2 * h)
+        fd_source = "float64 oracle, this run"
+    ad = [float(grad[v]) for v in picks]
     ad_dir = float(np.sum(grad * direction))
     line = {
         "metric": "adjoint gradient (96^3, 4000 steps, checkpoints every 200)",
@@ -469,7 +492,8 @@ def bench_adjoint(args):
         "fd_voxels": [{"voxel": list(v), "adjoint": a, "fd_f64": f} for v, a, f in zip(picks, ad, fd)],
         "fd_rel_l2": float(np.linalg.norm(np.array(ad) - np.array(fd)) / np.linalg.norm(fd)) if fd else None,
         "directional": {"adjoint": ad_dir, "fd_f64": fd_dir, "rel_err": abs(ad_dir - fd_dir) / abs(fd_dir)},
-        "h": h, "box": [list(b) for b in box], "data": "synthetic (seeded eps ~ U[1,12])",
+        "h": h, "fd_source": fd_source, "box": [list(b) for b in box],
+        "data": "synthetic (seeded eps ~ U[1,12])",
         "reference_adjoint": "unavailable: the reference has no adjoint gradient",
     }
     print(json.dumps(line), flush=True)

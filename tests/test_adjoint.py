@@ -109,3 +109,36 @@ def test_autograd_and_checkpoint_interval(gpu):
         problem.close()
         d.close()
     assert np.max(np.abs(grads[0] - grads[1])) <= 1e-5 * np.max(np.abs(grads[0]))
+
+
+@pytest.mark.gpu
+def test_adjoint96_against_float64_fixture(gpu):
+    """The 96^3 workload (4000 steps, checkpoints every 200): the GPU gradient against
+    float64 central differences (h = 1e-3) at 32 seeded voxels and along one seeded
+    direction over the whole 16 x 64 x 64 box (tests/golden/adjoint96_fd.json, made by
+    tests/golden/make_adjoint_fd.py)."""
+    import json
+    from pathlib import Path
+
+    import torch
+
+    from meep_gpu_gb300 import workloads
+
+    record = json.loads((Path(__file__).parent / "golden" / "adjoint96_fd.json").read_text())
+    driver, flux, box, eps_box = workloads.adjoint96()
+    problem = FluxAdjoint(driver, flux, box, workloads.ADJOINT96_STEPS, checkpoint_every=200)
+    value = problem.forward(torch.from_numpy(eps_box))
+    grad = problem.backward().cpu().numpy()
+    assert abs(value - record["objective"]) <= 1e-5 * abs(record["objective"])
+    rng = np.random.default_rng(0)
+    picks = [tuple(int(rng.integers(0, n)) for n in eps_box.shape) for _ in record["voxels"]]
+    assert picks == [tuple(v["voxel"]) for v in record["voxels"]]
+    direction = rng.standard_normal(eps_box.shape)
+    direction /= np.linalg.norm(direction)
+    fd = np.array([v["fd"] for v in record["voxels"]])
+    ad = np.array([grad[v] for v in picks])
+    assert np.linalg.norm(ad - fd) <= 2e-3 * np.linalg.norm(fd), (ad, fd)
+    along = float(np.sum(grad * direction))
+    assert abs(along - record["directional_fd"]) <= 1e-4 * abs(record["directional_fd"])
+    problem.close()
+    driver.close()

@@ -73,6 +73,14 @@ def parse_args():
     return p.parse_args()
 
 
+def family_name(choice) -> str:
+    """(family, block_z, block_y, x_chunk) as words."""
+    family, bz, by, xc = choice
+    if family == 1:
+        return f"tiles 64x8, x chunk {xc}"
+    return f"{'prefetching ' if family == 2 else ''}generic {bz}x{by}, x chunk {xc}"
+
+
 def measured_peaks():
     path = ROOT / "MEASURED_PEAKS.json"
     if path.exists():
@@ -346,7 +354,8 @@ def main():
         "data": "synthetic",
         "config": {"workload": args.workload, "cells": cells, "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 (no flush needed)",
-                   "kernels": {"family": ("tiles" if choice and choice[0] == 1 else "generic"),
+                   "kernels": {"h_half": family_name(choice[0]) if choice else None,
+                               "e_half": family_name(choice[1]) if choice else None,
                                "choice": choice, "chosen_by": "argument" if kernels else "autotuner"},
                    "monitors": {"flux_planes": len(flux), "dft_volumes": len(dft),
                                 "decimation": [m.decimation_factor for m in list(flux) + list(dft)][:1]}},

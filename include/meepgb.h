@@ -171,12 +171,21 @@ int mgb_flux_spectrum(mgb_sim* sim, int32_t monitor, const float* weights, doubl
  * extent that is not a multiple of 4, or MEEPGB_TILES=0 in the environment). */
 int mgb_uses_tiles(mgb_sim* sim);
 
-/* Choose the kernel family: 0 the generic kernels (plain loads), 1 the tile kernels
- * (TMA-staged shared-memory planes; needs a z extent that is a multiple of 4). Both
+/* Choose the kernel family of both halves: 0 the generic kernels (plain loads), 1 the
+ * tile kernels (TMA-staged shared-memory planes; needs a z extent that is a multiple of
+ * 4), 2 the generic kernels with the next plane's loads issued ahead. All
  * compute the same words; the autotuner picks the faster for a grid. No reference
  * counterpart (the reference's dispatch arbiter picks among its own kernel tables,
  * meep_gpu/dispatch_preference.py). */
 int mgb_select_kernels(mgb_sim* sim, int32_t family);
+
+/* Choose the family and launch shape of one half alone (part 0 the H half, 1 the E
+ * half): family 0 generic, 1 tiles, 2 generic with the next plane's loads issued ahead;
+ * block_z x block_y cells per CTA (a multiple of 32, at most 256; the tile kernels'
+ * block is fixed) and x_chunk planes per CTA. The halves are separate launches, so any
+ * pair computes the same words. No reference counterpart. */
+int mgb_select_half(mgb_sim* sim, int32_t part, int32_t family, int32_t block_z, int32_t block_y,
+                    int32_t x_chunk);
 
 /* Release the plan (never the caller's arrays). */
 void mgb_destroy(mgb_sim* sim);

@@ -1592,17 +1592,19 @@ struct mgb_sim {
   mgb_sim_desc desc;
   StepParams step;
   TileMaps maps;
-  bool tiles = false;        // step with the tile kernels
-  bool prefetch = false;     // generic kernels: the prefetching marches
+  // Kernel choice of each half (0 the H half, 1 the E half): the autotuner may pick a
+  // different family and launch shape for each.
+  struct HalfChoice {
+    bool tiles = false;     // the tile kernels
+    bool prefetch = false;  // generic kernels: the prefetching marches
+    int block_z = 32, block_y = 4, xchunk = 4;  // generic kernels
+    int tile_xchunk = 8;                        // tile kernels
+  } half[2];
   bool tiles_ready = false;  // their tensor maps are built
   size_t h_smem = 0, e_smem = 0;
   const double* words = nullptr;
   long long words_first = 0;
   long long words_steps = 0;
-  int block_z = 32;
-  int block_y = 4;
-  int xchunk = 4;        // generic kernels
-  int tile_xchunk = 8;   // tile kernels
   // Monitors in buffered (tensor-core) mode: samples [kDepth][ncomp * cells], the phase
   // table scratch, and the host-tracked fill of the buffer.
   struct DftBuffer {
@@ -1706,9 +1708,11 @@ void setup_tiles(mgb_sim* sim) {
     }
   }
   const char* xc = getenv("MEEPGB_TILE_XCHUNK");
-  if (xc != nullptr && atoi(xc) >= 1) sim->tile_xchunk = atoi(xc);
+  for (auto& h : sim->half) {
+    if (xc != nullptr && atoi(xc) >= 1) h.tile_xchunk = atoi(xc);
+    h.tiles = true;
+  }
   sim->tiles_ready = true;
-  sim->tiles = true;
 }
 
 }  // namespace
@@ -1851,10 +1855,12 @@ int mgb_set_launch_shape(mgb_sim* sim, int block_z, int block_y, int xchunk) {
     return fail(MGB_ERR_ARGUMENT,
                 "launch shape needs block_z*block_y a multiple of 32 up to 256 and x_chunk >= 1");
   }
-  sim->block_z = block_z;
-  sim->block_y = block_y;
-  sim->xchunk = xchunk;
-  sim->tile_xchunk = xchunk;
+  for (auto& h : sim->half) {
+    h.block_z = block_z;
+    h.block_y = block_y;
+    h.xchunk = xchunk;
+    h.tile_xchunk = xchunk;
+  }
   return MGB_OK;
 }
 
@@ -1913,8 +1919,9 @@ int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s) {
   const bool pml = sim->desc.pml_active != 0;
   if (part == 0 || part == 1) {
     if (p.nsrc > 0) p.src_words = sim->words + (n - sim->words_first) * p.nsrc;
-    if (sim->tiles) {
-      const int xc = sim->tile_xchunk;
+    const mgb_sim::HalfChoice& hc = sim->half[part];
+    if (hc.tiles) {
+      const int xc = hc.tile_xchunk;
       const dim3 grid((p.nz + kTileZ - 1) / kTileZ, (p.ny + kTileY - 1) / kTileY,
                       (p.nx + xc - 1) / xc);
       if (part == 0) {
@@ -1926,23 +1933,23 @@ int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s) {
       }
       return MGB_OK;
     }
-    const dim3 block(sim->block_z, sim->block_y, 1);
-    const dim3 grid((p.nz + block.x - 1) / block.x, (p.ny + block.y - 1) / block.y,
-                    (p.nx + sim->xchunk - 1) / sim->xchunk);
-    if (sim->prefetch) {
+    const dim3 block(hc.block_z, hc.block_y, 1);
+    const int xc = hc.xchunk;
+    const dim3 grid((p.nz + block.x - 1) / block.x, (p.ny + block.y - 1) / block.y, (p.nx + xc - 1) / xc);
+    if (hc.prefetch) {
       if (part == 0) {
-        if (pml) h_generic_pf<true><<<grid, block, 0, s>>>(p, n == 0, sim->xchunk);
-        else h_generic_pf<false><<<grid, block, 0, s>>>(p, n == 0, sim->xchunk);
+        if (pml) h_generic_pf<true><<<grid, block, 0, s>>>(p, n == 0, xc);
+        else h_generic_pf<false><<<grid, block, 0, s>>>(p, n == 0, xc);
       } else {
-        if (pml) e_generic_pf<true><<<grid, block, 0, s>>>(p, (int)(n & 1), sim->xchunk);
-        else e_generic_pf<false><<<grid, block, 0, s>>>(p, (int)(n & 1), sim->xchunk);
+        if (pml) e_generic_pf<true><<<grid, block, 0, s>>>(p, (int)(n & 1), xc);
+        else e_generic_pf<false><<<grid, block, 0, s>>>(p, (int)(n & 1), xc);
       }
     } else if (part == 0) {
-      if (pml) h_generic<true><<<grid, block, 0, s>>>(p, n == 0, sim->xchunk);
-      else h_generic<false><<<grid, block, 0, s>>>(p, n == 0, sim->xchunk);
+      if (pml) h_generic<true><<<grid, block, 0, s>>>(p, n == 0, xc);
+      else h_generic<false><<<grid, block, 0, s>>>(p, n == 0, xc);
     } else {
-      if (pml) e_generic<true><<<grid, block, 0, s>>>(p, (int)(n & 1), sim->xchunk);
-      else e_generic<false><<<grid, block, 0, s>>>(p, (int)(n & 1), sim->xchunk);
+      if (pml) e_generic<true><<<grid, block, 0, s>>>(p, (int)(n & 1), xc);
+      else e_generic<false><<<grid, block, 0, s>>>(p, (int)(n & 1), xc);
     }
     return MGB_OK;
   }
@@ -2069,22 +2076,51 @@ int32_t mgb_dft_pending(mgb_sim* sim, int32_t monitor) {
   return sim->dbuf[monitor].count;
 }
 
-int mgb_uses_tiles(mgb_sim* sim) { return sim != nullptr && sim->tiles ? 1 : 0; }
+int mgb_uses_tiles(mgb_sim* sim) {
+  return sim != nullptr && (sim->half[0].tiles || sim->half[1].tiles) ? 1 : 0;
+}
 
-int mgb_select_kernels(mgb_sim* sim, int32_t family) {
-  if (sim == nullptr) return fail(MGB_ERR_ARGUMENT, "null plan");
+namespace {
+int choose_family(mgb_sim* sim, mgb_sim::HalfChoice& h, int family) {
   if (family == 0 || family == 2) {
-    sim->tiles = false;
-    sim->prefetch = family == 2;
+    h.tiles = false;
+    h.prefetch = family == 2;
     return MGB_OK;
   }
   if (family == 1) {
     if (!sim->tiles_ready) return fail(MGB_ERR_UNSUPPORTED, "the tile kernels need a z extent that is a multiple of 4");
-    sim->tiles = true;
-    sim->prefetch = false;
+    h.tiles = true;
+    h.prefetch = false;
     return MGB_OK;
   }
   return fail(MGB_ERR_ARGUMENT, "kernel family is 0 (generic), 1 (tiles) or 2 (generic, prefetching)");
+}
+}  // namespace
+
+int mgb_select_kernels(mgb_sim* sim, int32_t family) {
+  if (sim == nullptr) return fail(MGB_ERR_ARGUMENT, "null plan");
+  for (auto& h : sim->half) {
+    const int rc = choose_family(sim, h, family);
+    if (rc != MGB_OK) return rc;
+  }
+  return MGB_OK;
+}
+
+int mgb_select_half(mgb_sim* sim, int32_t part, int32_t family, int32_t block_z, int32_t block_y,
+                    int32_t x_chunk) {
+  if (sim == nullptr) return fail(MGB_ERR_ARGUMENT, "null plan");
+  if (part != 0 && part != 1) return fail(MGB_ERR_ARGUMENT, "part is 0 (H half) or 1 (E half)");
+  if (block_z < 1 || block_y < 1 || block_z * block_y > 256 || (block_z * block_y) % 32 != 0 || x_chunk < 1)
+    return fail(MGB_ERR_ARGUMENT, "launch shape needs block_z*block_y a multiple of 32 up to 256 and x_chunk >= 1");
+  mgb_sim::HalfChoice h = sim->half[part];
+  const int rc = choose_family(sim, h, family);
+  if (rc != MGB_OK) return rc;
+  h.block_z = block_z;
+  h.block_y = block_y;
+  h.xchunk = x_chunk;
+  h.tile_xchunk = x_chunk;
+  sim->half[part] = h;
+  return MGB_OK;
 }
 
 void mgb_destroy(mgb_sim* sim) { delete sim; }

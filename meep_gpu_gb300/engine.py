@@ -333,23 +333,27 @@ class Engine:
         """Whether the plan steps with the TMA tile kernels (else the generic ones)."""
         return bool(self.lib.mgb_uses_tiles(self.handle))
 
-    def select(self, choice: Tuple[int, int, int, int]) -> None:
-        """Apply a kernel choice (family, block_z, block_y, x_chunk)."""
-        family, bz, by, xc = choice
-        _lib.check(self.lib, self.lib.mgb_select_kernels(self.handle, family))
-        if family in (0, 2):
-            self.set_launch_shape(bz, by, xc)
+    def select(self, choice) -> None:
+        """Apply a kernel choice: one (family, block_z, block_y, x_chunk) for both halves,
+        or a pair of them (H half, E half)."""
+        if len(choice) == 2 and isinstance(choice[0], (tuple, list)):
+            h, e = (tuple(int(v) for v in c) for c in choice)
         else:
-            self.set_launch_shape(32, 8, xc)
-        self.choice = choice
+            h = e = tuple(int(v) for v in choice)
+        for part, (family, bz, by, xc) in enumerate((h, e)):
+            if family == 1:
+                bz, by = 32, 8  # the tile kernels' block is fixed; the shape check still applies
+            _lib.check(self.lib, self.lib.mgb_select_half(self.handle, part, family, bz, by, xc))
+        self.choice = (h, e)
 
-    def autotune(self, steps: int = 4) -> Tuple[int, int, int, int]:
-        """Pick the fastest kernel choice for this grid and apply it.
+    def autotune(self, steps: int = 4):
+        """Pick the fastest kernel choice of each half for this grid and apply them.
 
-        Candidates are timed (CUDA events, H and E halves) on a scratch engine with the
+        Candidates are timed (CUDA events around each half) on a scratch engine with the
         same grid, absorber, materials and poles but zero fields and no sources or
-        monitors, so this simulation's state is untouched; the result is cached per
-        configuration for the life of the process.
+        monitors, so this simulation's state is untouched; the H and E halves are
+        separate launches, so each keeps its own fastest candidate. The result is cached
+        per configuration for the life of the process.
         """
         key = autotune_key(self.grid, self.pml, len(getattr(self, "pole_tensors", [])),
                            len({t.data_ptr() for t in self.inv_eps}))
@@ -359,7 +363,8 @@ class Engine:
         scratch = Engine(self.grid, self.pml, [t.cpu().numpy() for t in self.inv_eps],
                          self._pole_specs, [], [], device=self.device, autotune=False)
         stream = torch.cuda.current_stream(self.device)
-        best, best_ms = None, float("inf")
+        best = [None, None]
+        best_ms = [float("inf"), float("inf")]
         for choice in AUTOTUNE_CANDIDATES:
             try:
                 scratch.select(choice)
@@ -368,23 +373,24 @@ class Engine:
             for n in range(2):
                 scratch.launch(n, 0, stream)
                 scratch.launch(n, 1, stream)
-            start = torch.cuda.Event(enable_timing=True)
-            end = torch.cuda.Event(enable_timing=True)
-            start.record(stream)
-            for n in range(2, 2 + steps):
-                scratch.launch(n, 0, stream)
-                scratch.launch(n, 1, stream)
-            end.record(stream)
-            end.synchronize()
-            ms = start.elapsed_time(end) / steps
-            if ms < best_ms:
-                best, best_ms = choice, ms
+            marks = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+            for t, ev in enumerate(marks):
+                ev[0].record(stream)
+                scratch.launch(2 + t, 0, stream)
+                ev[1].record(stream)
+                scratch.launch(2 + t, 1, stream)
+                ev[2].record(stream)
+            marks[-1][2].synchronize()
+            for part in (0, 1):
+                ms = float(np.median([ev[part].elapsed_time(ev[part + 1]) for ev in marks]))
+                if ms < best_ms[part]:
+                    best[part], best_ms[part] = choice, ms
         scratch.close()
         del scratch
-        _AUTOTUNE_CACHE[key] = best
-        self.select(best)
-        self.autotune_ms = best_ms
-        return best
+        _AUTOTUNE_CACHE[key] = (best[0], best[1])
+        self.select((best[0], best[1]))
+        self.autotune_ms = best_ms[0] + best_ms[1]
+        return self.choice
 
     def launch(self, step: int, part: int, stream=None) -> None:
         """Launch one kernel of one step: 0 the H half, 1 the E half, 2 the monitors."""

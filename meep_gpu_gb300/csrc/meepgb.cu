@@ -442,6 +442,15 @@ __device__ __forceinline__ void e_cell(const StepParams& p, const EColumn& col, 
   }
 }
 
+// Whether the next (previous) lane of the warp holds this thread's +z (-z) neighbour in
+// the same block row: the block's rows are blockDim.x consecutive z cells, a warp holds
+// one or more whole rows or 32 cells of one row.
+__device__ __forceinline__ int lane_id() { return (int)((threadIdx.x + blockDim.x * threadIdx.y) & 31); }
+__device__ __forceinline__ bool next_lane_has_z(int k, int nz) {
+  return lane_id() != 31 && threadIdx.x + 1 < blockDim.x && k + 1 < nz;
+}
+__device__ __forceinline__ bool prev_lane_has_z() { return lane_id() != 0 && threadIdx.x > 0; }
+
 // Whether a CTA's cells [i0, i1) x [j0, j0 + by) x [k0, k0 + bz) all lie in the box that
 // no membership reaches (then the PML update is the plain one, word for word).
 __device__ __forceinline__ bool cta_inner(const StepParams& p, int i0, int i1, int j0, int by, int k0, int bz) {
@@ -585,13 +594,15 @@ __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i
 // Prefetching marches: the same cell updates, with every field load of plane i + 1
 // issued before plane i is computed and stored, so each thread keeps two planes of loads
 // in flight (the loads of a plane do not depend on the stores of the one before: other
-// cells, or the thread's own cell read before it is written).
+// cells, or the thread's own cell read before it is written). The z neighbours held by
+// the adjacent lane of the same row come by shuffle instead of a load (with their 64
+// registers these marches can afford it; at the generic marches' 48 it spilled).
 struct HLoads {
   float ex, ey_xp, ez_xp, ez_yp, ex_yp, ey_zp, ex_zp, h[3];
 };
 
 __device__ __forceinline__ void h_loads(const StepParams& p, HLoads& L, int i, int c, int col, int sx,
-                                        int oy, int oz, bool ywall, bool zwall) {
+                                        int oy, int oz, bool ywall, bool zwall, bool z_from_lane) {
   L.ex = p.E[0][c];
   if (i + 1 < p.nx) {
     L.ey_xp = p.E[1][c + sx];
@@ -605,8 +616,9 @@ __device__ __forceinline__ void h_loads(const StepParams& p, HLoads& L, int i, i
   }
   L.ez_yp = ywall ? 0.f : p.E[2][c + oy];
   L.ex_yp = ywall ? 0.f : p.E[0][c + oy];
-  L.ey_zp = zwall ? 0.f : p.E[1][c + oz];
-  L.ex_zp = zwall ? 0.f : p.E[0][c + oz];
+  // +z neighbours: loaded only by lanes whose next lane does not hold them
+  L.ey_zp = (zwall || z_from_lane) ? 0.f : p.E[1][c + oz];
+  L.ex_zp = (zwall || z_from_lane) ? 0.f : p.E[0][c + oz];
   L.h[0] = p.H[0][c];
   L.h[1] = p.H[1][c];
   L.h[2] = p.H[2][c];
@@ -634,11 +646,21 @@ __device__ __forceinline__ void h_march_pf(const StepParams& p, int j, int k, in
   }
   float ey = p.E[1][c];
   float ez = p.E[2][c];
+  const unsigned zlanes = __activemask();
+  const bool z_from_lane = next_lane_has_z(k, p.nz);
   HLoads cur;
-  h_loads(p, cur, i0, c, col, sx, oy, oz, ywall, zwall);
+  h_loads(p, cur, i0, c, col, sx, oy, oz, ywall, zwall, z_from_lane);
   for (int i = i0; i < i1; ++i, c += sx) {
     HLoads nxt;
-    if (i + 1 < i1) h_loads(p, nxt, i + 1, c + sx, col, sx, oy, oz, ywall, zwall);
+    if (i + 1 < i1) h_loads(p, nxt, i + 1, c + sx, col, sx, oy, oz, ywall, zwall, z_from_lane);
+    {
+      const float ey_up = __shfl_down_sync(zlanes, ey, 1);
+      const float ex_up = __shfl_down_sync(zlanes, cur.ex, 1);
+      if (z_from_lane && !zwall) {
+        cur.ey_zp = ey_up;
+        cur.ex_zp = ex_up;
+      }
+    }
     HPlane pl = {};
     int axes = 0;
     if (PML) {
@@ -677,7 +699,8 @@ __device__ __forceinline__ void e_loads(const StepParams& p, ELoads& L, int i, i
     L.hz_ym = p.H[2][cm];
     L.hx_ym = p.H[0][cm];
   }
-  if (km >= 0) {
+  // -z neighbours: loaded only where the previous lane does not hold them
+  if (km >= 0 && !prev_lane_has_z()) {
     const int cm = i * sx + j * sy + km;
     L.hy_zm = p.H[1][cm];
     L.hx_zm = p.H[0][cm];
@@ -717,11 +740,20 @@ __device__ __forceinline__ void e_march_pf(const StepParams& p, int j, int k, in
       hz_xm = p.H[2][im * sx + col];
     }
   }
+  const unsigned zlanes = __activemask();
   ELoads cur;
   e_loads(p, cur, i0, c, j, k, jm, km, sx, sy);
   for (int i = i0; i < i1; ++i, c += sx) {
     ELoads nxt;
     if (i + 1 < i1) e_loads(p, nxt, i + 1, c + sx, j, k, jm, km, sx, sy);
+    {
+      const float hy_dn = __shfl_up_sync(zlanes, cur.hy, 1);
+      const float hx_dn = __shfl_up_sync(zlanes, cur.hx, 1);
+      if (prev_lane_has_z()) {
+        cur.hy_zm = hy_dn;
+        cur.hx_zm = hx_dn;
+      }
+    }
     EPlane pl = {};
     int axes = 0;
     if (PML) {
@@ -1280,7 +1312,7 @@ __device__ __forceinline__ void copy_to_shared(T* dst, const T* src) {
 // Register budget as the generic kernels' (48 per thread): more costs occupancy the
 // column march needs. `t` is the launch's step within the batch step call.
 template <int PART>
-__global__ void __launch_bounds__(256, 5) step_batched(const __grid_constant__ BatchTables tb, int t) {
+__global__ void __launch_bounds__(256, 4) step_batched(const __grid_constant__ BatchTables tb, int t) {
   __shared__ StepParams sp;
   if ((int)blockIdx.x >= tb.counts[0]) return;
   const int4 w = tb.work[blockIdx.x];
@@ -1298,12 +1330,12 @@ __global__ void __launch_bounds__(256, 5) step_batched(const __grid_constant__ B
   const bool pml = sp.pml && !cta_inner(sp, i0, i1, w.z * (int)blockDim.y, (int)blockDim.y,
                                         w.y * (int)blockDim.x, (int)blockDim.x);
   if (PART == 0) {
-    if (pml) h_march<true>(sp, j, k, i0, i1, n == 0);
-    else h_march<false>(sp, j, k, i0, i1, n == 0);
+    if (pml) h_march_pf<true>(sp, j, k, i0, i1, n == 0);
+    else h_march_pf<false>(sp, j, k, i0, i1, n == 0);
   } else {
     const double* words = st.words + n * sp.nsrc;
-    if (pml) e_march<true>(sp, j, k, i0, i1, (int)(n & 1), words);
-    else e_march<false>(sp, j, k, i0, i1, (int)(n & 1), words);
+    if (pml) e_march_pf<true>(sp, j, k, i0, i1, (int)(n & 1), words);
+    else e_march_pf<false>(sp, j, k, i0, i1, (int)(n & 1), words);
   }
 }
 

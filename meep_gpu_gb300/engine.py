@@ -43,8 +43,10 @@ SOURCE_WINDOW = 4096
 # the tile kernels (block shape fixed at 64 x 8, x_chunk used), family 0 the generic ones,
 # family 2 the generic ones with the next plane's loads issued ahead.
 AUTOTUNE_CANDIDATES = ((0, 32, 4, 4), (0, 32, 8, 4), (0, 32, 4, 8), (0, 64, 2, 8),
-                       (0, 16, 8, 4), (0, 16, 16, 4), (1, 64, 8, 4), (1, 64, 8, 8),
-                       (2, 32, 4, 4), (2, 32, 4, 8), (2, 32, 8, 4), (2, 64, 2, 4))
+                       (0, 16, 8, 4), (0, 16, 16, 4), (0, 16, 8, 2), (0, 16, 8, 8), (0, 32, 2, 4),
+                       (1, 64, 8, 4), (1, 64, 8, 8),
+                       (2, 32, 4, 4), (2, 32, 4, 8), (2, 32, 8, 4), (2, 64, 2, 4), (2, 16, 8, 4),
+                       (2, 32, 4, 2), (2, 32, 2, 4))
 _AUTOTUNE_CACHE: Dict[tuple, Tuple[int, int, int, int]] = {}
 
 

@@ -41,6 +41,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <utility>
 #include <mutex>
 #include <cstdio>
 #include <cstdlib>
@@ -74,6 +75,7 @@ struct StepParams {
   // The box outside every membership of every auxiliary (x0, x1, y0, y1, z0, z1): a CTA
   // whose cells all lie in it steps the plain update (no membership tests, no tables).
   int inner[6];
+  int inv_iso;  // 1 when the three inverse-permittivity volumes are one (isotropic)
   int met[3];
   float dtdx;
   const float* kms[2][3];
@@ -579,7 +581,14 @@ __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i
       hx_zm = Hx[cm];
     }
     float d[3] = {p.D[0][c], p.D[1][c], p.D[2][c]};
-    const float inv[3] = {__ldg(p.inv_eps[0] + c), __ldg(p.inv_eps[1] + c), __ldg(p.inv_eps[2] + c)};
+    float inv[3];
+    if (p.inv_iso) {
+      inv[0] = inv[1] = inv[2] = __ldg(p.inv_eps[0] + c);
+    } else {
+      inv[0] = __ldg(p.inv_eps[0] + c);
+      inv[1] = __ldg(p.inv_eps[1] + c);
+      inv[2] = __ldg(p.inv_eps[2] + c);
+    }
     EAux ax = {};
     if (PML && axes != 0) e_aux_load(p, ecol, pl, c, ax);
     const float cx = dtdx * (((hz_ym - hz) + hy) - hy_zm);
@@ -708,9 +717,13 @@ __device__ __forceinline__ void e_loads(const StepParams& p, ELoads& L, int i, i
   L.d[0] = p.D[0][c];
   L.d[1] = p.D[1][c];
   L.d[2] = p.D[2][c];
-  L.inv[0] = __ldg(p.inv_eps[0] + c);
-  L.inv[1] = __ldg(p.inv_eps[1] + c);
-  L.inv[2] = __ldg(p.inv_eps[2] + c);
+  if (p.inv_iso) {
+    L.inv[0] = L.inv[1] = L.inv[2] = __ldg(p.inv_eps[0] + c);
+  } else {
+    L.inv[0] = __ldg(p.inv_eps[0] + c);
+    L.inv[1] = __ldg(p.inv_eps[1] + c);
+    L.inv[2] = __ldg(p.inv_eps[2] + c);
+  }
 }
 
 template <bool PML>
@@ -1839,6 +1852,7 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
   StepParams& p = sim->step;
   p.nx = d.nx; p.ny = d.ny; p.nz = d.nz;
   p.pml = d.pml_active ? 1 : 0;
+  p.inv_iso = (d.inv_eps[0] == d.inv_eps[1] && d.inv_eps[1] == d.inv_eps[2]) ? 1 : 0;
   {
     const int n[3] = {d.nx, d.ny, d.nz};
     for (int a = 0; a < 3; ++a) {
@@ -1909,6 +1923,13 @@ int mgb_set_source_words(mgb_sim* sim, const double* words, int64_t first_step, 
 
 namespace {
 
+// Launch a step kernel.
+template <typename... KArgs, typename... Args>
+void launch_step(const mgb_sim*, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                 Args&&... args) {
+  kernel<<<grid, block, smem, s>>>(std::forward<Args>(args)...);
+}
+
 // Add a monitor's buffered samples to its accumulators: one phase table and one
 // contraction launch for its E components (sampled at post * dt), then the same for its
 // H components (at post * dt - dt / 2). The table scratch is reused in stream order.
@@ -1957,11 +1978,11 @@ int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s) {
       const dim3 grid((p.nz + kTileZ - 1) / kTileZ, (p.ny + kTileY - 1) / kTileY,
                       (p.nx + xc - 1) / xc);
       if (part == 0) {
-        if (pml) h_tile<true><<<grid, kThreads, sim->h_smem, s>>>(p, sim->maps, n == 0, xc);
-        else h_tile<false><<<grid, kThreads, sim->h_smem, s>>>(p, sim->maps, n == 0, xc);
+        if (pml) launch_step(sim, h_tile<true>, grid, dim3(kThreads), sim->h_smem, s, p, sim->maps, (int)(n == 0), xc);
+        else launch_step(sim, h_tile<false>, grid, dim3(kThreads), sim->h_smem, s, p, sim->maps, (int)(n == 0), xc);
       } else {
-        if (pml) e_tile<true><<<grid, kThreads, sim->e_smem, s>>>(p, sim->maps, (int)(n & 1), xc);
-        else e_tile<false><<<grid, kThreads, sim->e_smem, s>>>(p, sim->maps, (int)(n & 1), xc);
+        if (pml) launch_step(sim, e_tile<true>, grid, dim3(kThreads), sim->e_smem, s, p, sim->maps, (int)(n & 1), xc);
+        else launch_step(sim, e_tile<false>, grid, dim3(kThreads), sim->e_smem, s, p, sim->maps, (int)(n & 1), xc);
       }
       return MGB_OK;
     }
@@ -1970,18 +1991,18 @@ int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s) {
     const dim3 grid((p.nz + block.x - 1) / block.x, (p.ny + block.y - 1) / block.y, (p.nx + xc - 1) / xc);
     if (hc.prefetch) {
       if (part == 0) {
-        if (pml) h_generic_pf<true><<<grid, block, 0, s>>>(p, n == 0, xc);
-        else h_generic_pf<false><<<grid, block, 0, s>>>(p, n == 0, xc);
+        if (pml) launch_step(sim, h_generic_pf<true>, grid, block, 0, s, p, (int)(n == 0), xc);
+        else launch_step(sim, h_generic_pf<false>, grid, block, 0, s, p, (int)(n == 0), xc);
       } else {
-        if (pml) e_generic_pf<true><<<grid, block, 0, s>>>(p, (int)(n & 1), xc);
-        else e_generic_pf<false><<<grid, block, 0, s>>>(p, (int)(n & 1), xc);
+        if (pml) launch_step(sim, e_generic_pf<true>, grid, block, 0, s, p, (int)(n & 1), xc);
+        else launch_step(sim, e_generic_pf<false>, grid, block, 0, s, p, (int)(n & 1), xc);
       }
     } else if (part == 0) {
-      if (pml) h_generic<true><<<grid, block, 0, s>>>(p, n == 0, xc);
-      else h_generic<false><<<grid, block, 0, s>>>(p, n == 0, xc);
+      if (pml) launch_step(sim, h_generic<true>, grid, block, 0, s, p, (int)(n == 0), xc);
+      else launch_step(sim, h_generic<false>, grid, block, 0, s, p, (int)(n == 0), xc);
     } else {
-      if (pml) e_generic<true><<<grid, block, 0, s>>>(p, (int)(n & 1), xc);
-      else e_generic<false><<<grid, block, 0, s>>>(p, (int)(n & 1), xc);
+      if (pml) launch_step(sim, e_generic<true>, grid, block, 0, s, p, (int)(n & 1), xc);
+      else launch_step(sim, e_generic<false>, grid, block, 0, s, p, (int)(n & 1), xc);
     }
     return MGB_OK;
   }
@@ -2659,3 +2680,4 @@ int mgb_copy_box(mgb_sim* sim, int32_t family, const int32_t* box, float* dst, v
 }
 
 }  // extern "C"
+

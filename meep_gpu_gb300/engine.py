@@ -82,9 +82,13 @@ class Engine:
         dev = self.device
         zeros = lambda s: torch.zeros(s, dtype=torch.float32, device=dev)  # noqa: E731
         self.fields: Dict[str, torch.Tensor] = {}
+        # each family's three components in one allocation (one contiguous range)
+        self.families: Dict[str, torch.Tensor] = {}
         for family in FIELD_NAMES:
+            block = zeros((3,) + tuple(shape))
+            self.families[family] = block
             for q, axis in enumerate("xyz"):
-                self.fields[family + axis] = zeros(shape)
+                self.fields[family + axis] = block[q]
         # inverse epsilon: one device volume per distinct host array
         self.inv_eps: List[torch.Tensor] = []
         seen: Dict[int, torch.Tensor] = {}
@@ -348,7 +352,7 @@ class Engine:
             _lib.check(self.lib, self.lib.mgb_select_half(self.handle, part, family, bz, by, xc))
         self.choice = (h, e)
 
-    def autotune(self, steps: int = 4):
+    def autotune(self, steps: int = 8):
         """Pick the fastest kernel choice of each half for this grid and apply them.
 
         Candidates are timed (CUDA events around each half) on a scratch engine with the

@@ -73,6 +73,34 @@ def parse_args():
     return p.parse_args()
 
 
+def max_over_ranks(value: float, device, world: int) -> float:
+    """The largest of every rank's value (the job's time is its slowest replica's)."""
+    if world <= 1:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def step_launches(engine, first: int, steps: int) -> int:
+    """Kernels of ours that steps first .. first+steps-1 launch: the two halves, and per
+    monitor due after a step either its accumulation (step by step) or its sample plus,
+    every MGB_DFT_DEPTH samples, a phase table and a contraction per time group (E, H)."""
+    from meep_gpu_gb300 import _lib
+    count = 2 * steps
+    for index, m in enumerate(engine.monitors):
+        due = sum(1 for n in range(first, first + steps) if (n + 1) % m.decimation_factor == 0)
+        if engine.dft_samples[index] is None:
+            count += due
+            continue
+        pending = engine.lib.mgb_dft_pending(engine.handle, index)
+        groups = len({c[0] for c in m.components})  # "E" and/or "H"
+        flushes = (pending + due) // _lib.MGB_DFT_DEPTH
+        count += due + flushes * 2 * groups
+    return count
+
+
 def family_name(choice) -> str:
     """(family, block_z, block_y, x_chunk) as words."""
     family, bz, by, xc = choice
@@ -239,9 +267,7 @@ def main():
     engine.ensure_source_words(first, args.steps)
     stream = torch.cuda.current_stream(device)
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    launches = 2 * args.steps + sum(
-        1 for n in range(first, first + args.steps) for m in engine.monitors
-        if (n + 1) % m.decimation_factor == 0)
+    launches = step_launches(engine, first, args.steps)
     torch.cuda.synchronize(device)
     barrier()
     with ClockSampler(local) as clocks:
@@ -250,11 +276,7 @@ def main():
         end.record(stream)
         torch.cuda.synchronize(device)
     driver.step_count += args.steps
-    ms = start.elapsed_time(end)
-    if world > 1:
-        t = torch.tensor([ms], device=device)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(start.elapsed_time(end), device, world)
     value = cells * args.steps * world / (ms / 1e3) / 1e6
     if engine.nonfinite():
         raise RuntimeError("the benchmark run wrote a non-finite field")

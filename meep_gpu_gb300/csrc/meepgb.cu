@@ -75,7 +75,6 @@ struct StepParams {
   // The box outside every membership of every auxiliary (x0, x1, y0, y1, z0, z1): a CTA
   // whose cells all lie in it steps the plain update (no membership tests, no tables).
   int inner[6];
-  int inv_iso;  // 1 when the three inverse-permittivity volumes are one (isotropic)
   int met[3];
   float dtdx;
   const float* kms[2][3];
@@ -581,14 +580,7 @@ __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i
       hx_zm = Hx[cm];
     }
     float d[3] = {p.D[0][c], p.D[1][c], p.D[2][c]};
-    float inv[3];
-    if (p.inv_iso) {
-      inv[0] = inv[1] = inv[2] = __ldg(p.inv_eps[0] + c);
-    } else {
-      inv[0] = __ldg(p.inv_eps[0] + c);
-      inv[1] = __ldg(p.inv_eps[1] + c);
-      inv[2] = __ldg(p.inv_eps[2] + c);
-    }
+    const float inv[3] = {__ldg(p.inv_eps[0] + c), __ldg(p.inv_eps[1] + c), __ldg(p.inv_eps[2] + c)};
     EAux ax = {};
     if (PML && axes != 0) e_aux_load(p, ecol, pl, c, ax);
     const float cx = dtdx * (((hz_ym - hz) + hy) - hy_zm);
@@ -717,13 +709,9 @@ __device__ __forceinline__ void e_loads(const StepParams& p, ELoads& L, int i, i
   L.d[0] = p.D[0][c];
   L.d[1] = p.D[1][c];
   L.d[2] = p.D[2][c];
-  if (p.inv_iso) {
-    L.inv[0] = L.inv[1] = L.inv[2] = __ldg(p.inv_eps[0] + c);
-  } else {
-    L.inv[0] = __ldg(p.inv_eps[0] + c);
-    L.inv[1] = __ldg(p.inv_eps[1] + c);
-    L.inv[2] = __ldg(p.inv_eps[2] + c);
-  }
+  L.inv[0] = __ldg(p.inv_eps[0] + c);
+  L.inv[1] = __ldg(p.inv_eps[1] + c);
+  L.inv[2] = __ldg(p.inv_eps[2] + c);
 }
 
 template <bool PML>
@@ -1137,6 +1125,142 @@ __global__ void __launch_bounds__(kThreads, 2) e_tile(const __grid_constant__ St
       issue(chain - 1 + S);
       issued = chain - 1 + S + 1;
     }
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Warp-specialized tile kernel (E half): the tile kernels' staging, with one producer
+// warp that keeps the ring of plane stages full (it waits on each stage's "empty"
+// barrier, then issues the plane's TMA loads against its "full" barrier) and 16
+// consumer warps that each wait only for the stage they need and release the stage of
+// the plane before once they are done with it. No CTA-wide barrier in the plane loop:
+// each consumer warp runs ahead as far as the data allows. Waits are bounded (2 s); a
+// timeout raises the shared abort flag and status bit 2, consumers leave, and the
+// producer waits (bounded) for its copies still in flight before it leaves.
+constexpr int kWsThreads = kThreads + 32;
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+template <bool PML>
+__global__ void __launch_bounds__(kWsThreads, 2) e_ws(const __grid_constant__ StepParams p,
+                                                     const __grid_constant__ TileMaps maps,
+                                                     int parity, int xchunk) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int S = maps.stages;
+  const int stage_bytes = 3 * kBoxHalo + (3 + maps.ninv) * kBoxOwn;
+  unsigned long long* full = reinterpret_cast<unsigned long long*>(smem + S * stage_bytes);
+  unsigned long long* empty = full + S;
+  __shared__ int abort_flag;
+  const int tid = threadIdx.x;
+  const int k0 = blockIdx.x * kTileZ, j0 = blockIdx.y * kTileY;
+  const int i0 = blockIdx.z * xchunk;
+  const int i1 = min(i0 + xchunk, p.nx);
+  const int nchain = i1 - i0 + 1;  // planes i0-1 .. i1-1
+  if (tid == 0) {
+    abort_flag = 0;
+    for (int st = 0; st < S; ++st) {
+      mbar_init(&full[st], 1);
+      mbar_init(&empty[st], kThreads / 32);
+    }
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (tid >= kThreads) {
+    // producer warp: one lane issues
+    if (tid == kThreads) {
+      int issued = 0;
+      for (int c = 0; c < nchain; ++c) {
+        const int st = c % S;
+        if (c >= S && !mbar_wait(&empty[st], (unsigned)(((c / S) - 1) & 1))) {
+          atomicExch(&abort_flag, 1);
+          break;
+        }
+        if (*reinterpret_cast<volatile int*>(&abort_flag)) break;
+        fence_proxy_async_smem();
+        unsigned char* base = smem + st * stage_bytes;
+        const int plane = i0 - 1 + c;
+        const bool own = plane >= i0;
+        const int xplane = (plane < 0 && !p.met[0]) ? plane + p.nx : plane;
+        mbar_expect_tx(&full[st], 3 * (kHaloZ * kHaloY * 4) + (own ? (3 + maps.ninv) * kBoxOwn : 0));
+        for (int q = 0; q < 3; ++q)
+          tma_load(base + q * kBoxHalo, &maps.Hhalo[q], &full[st], k0 - 4, j0 - 1, xplane);
+        if (own) {
+          for (int q = 0; q < 3; ++q)
+            tma_load(base + 3 * kBoxHalo + q * kBoxOwn, &maps.D[q], &full[st], k0, j0, plane);
+          for (int q = 0; q < maps.ninv; ++q)
+            tma_load(base + 3 * kBoxHalo + (3 + q) * kBoxOwn, &maps.inv[q], &full[st], k0, j0, plane);
+        }
+        issued = c + 1;
+      }
+      // no copy may land after the CTA has left: wait (bounded) for the last ones
+      for (int c = issued > S ? issued - S : 0; c < issued; ++c)
+        mbar_wait(&full[c % S], (unsigned)((c / S) & 1));
+    }
+    return;
+  }
+  const int tz = tid & (kTileZ - 1), ty = tid / kTileZ;
+  const int j = j0 + ty, k = k0 + tz;
+  const bool live = j < p.ny && k < p.nz;
+  EColumn ecol = {};
+  int col_axes = 0;  // bit 1: the warp touches the y memberships, bit 2: the z ones
+  if (PML) {
+    if (live) ecol = e_column(p, j, k);
+    col_axes = (__any_sync(0xffffffffu, live && (ecol.f2 || ecol.w1)) ? 2 : 0) |
+               (__any_sync(0xffffffffu, live && (ecol.f0 || ecol.w2)) ? 4 : 0);
+  }
+  const bool wrap_y = live && !p.met[1] && j == 0;
+  const bool wrap_z = live && !p.met[2] && k == 0;
+  const int sx = p.ny * p.nz;
+  const int col = j * p.nz + k;
+  const int h = (ty + 1) * kHaloZ + tz + 4;  // this cell in an H box
+  const int o = ty * kTileZ + tz;            // this cell in an own box
+  const int inv0 = 3 + maps.inv_of[0], inv1 = 3 + maps.inv_of[1], inv2 = 3 + maps.inv_of[2];
+  const float dtdx = p.dtdx;
+  bool ok = __all_sync(0xffffffffu, mbar_wait(&full[0], 0));
+  for (int i = i0; i < i1 && ok; ++i) {
+    const int chain = i - i0 + 1;
+    ok = __all_sync(0xffffffffu, mbar_wait(&full[chain % S], (unsigned)((chain / S) & 1)));
+    if (!ok) break;
+    if (live) {
+      const float* st1 = reinterpret_cast<const float*>(smem + (chain % S) * stage_bytes);
+      const float* st0 = reinterpret_cast<const float*>(smem + ((chain - 1) % S) * stage_bytes);
+      const float* Hx = st1;
+      const float* Hy = st1 + kBoxHalo / 4;
+      const float* Hz = st1 + 2 * kBoxHalo / 4;
+      const float* own = st1 + 3 * kBoxHalo / 4;
+      const int c = i * sx + col;
+      EPlane pl = {};
+      int axes = 0;
+      if (PML) {
+        pl = e_plane(p, i);
+        axes = col_axes | ((pl.f1 || pl.w0) ? 1 : 0);
+        if (axes & 1) e_plane_coefficients(p, i, pl);
+      }
+      EAux ax = {};
+      if (PML && axes != 0) e_aux_load(p, ecol, pl, c, ax);
+      const float hx = Hx[h], hy = Hy[h], hz = Hz[h];
+      float hz_ym = Hz[h - kHaloZ], hx_ym = Hx[h - kHaloZ];
+      float hy_zm = Hy[h - 1], hx_zm = Hx[h - 1];
+      if (wrap_y) { hz_ym = p.H[2][c + (p.ny - 1) * p.nz]; hx_ym = p.H[0][c + (p.ny - 1) * p.nz]; }
+      if (wrap_z) { hy_zm = p.H[1][c + (p.nz - 1)]; hx_zm = p.H[0][c + (p.nz - 1)]; }
+      const float cx = dtdx * (((hz_ym - hz) + hy) - hy_zm);
+      const float cy = dtdx * (((hx_zm - hx) + hz) - (st0 + 2 * kBoxHalo / 4)[h]);
+      const float cz = dtdx * ((((st0 + kBoxHalo / 4)[h] - hy) + hx) - hx_ym);
+      float d[3] = {own[o], own[kBoxOwn / 4 + o], own[2 * kBoxOwn / 4 + o]};
+      const float inv[3] = {own[inv0 * (kBoxOwn / 4) + o], own[inv1 * (kBoxOwn / 4) + o],
+                            own[inv2 * (kBoxOwn / 4) + o]};
+      e_cell<PML>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, d, inv, p.src_words, ax);
+    }
+    // the stage of plane i - 1 is no longer read by this warp
+    __syncwarp();
+    if ((tid & 31) == 0) mbar_arrive(&empty[(chain - 1) % S]);
+    if (*reinterpret_cast<volatile int*>(&abort_flag)) ok = false;
+  }
+  if (!ok) {
+    atomicExch(&abort_flag, 1);
+    if (p.status != nullptr && (tid & 31) == 0) atomicOr(p.status, 2);
   }
 }
 
@@ -1641,12 +1765,13 @@ struct mgb_sim {
   // different family and launch shape for each.
   struct HalfChoice {
     bool tiles = false;     // the tile kernels
+    bool ws = false;        // the tile kernels' warp-specialized form (E half)
     bool prefetch = false;  // generic kernels: the prefetching marches
     int block_z = 32, block_y = 4, xchunk = 4;  // generic kernels
     int tile_xchunk = 8;                        // tile kernels
   } half[2];
   bool tiles_ready = false;  // their tensor maps are built
-  size_t h_smem = 0, e_smem = 0;
+  size_t h_smem = 0, e_smem = 0, e_ws_smem = 0;
   const double* words = nullptr;
   long long words_first = 0;
   long long words_steps = 0;
@@ -1742,10 +1867,12 @@ void setup_tiles(mgb_sim* sim) {
   if (st != nullptr && atoi(st) >= 2 && atoi(st) <= 8) m.stages = atoi(st);
   sim->h_smem = (size_t)m.stages * (3 * kBoxHalo + 3 * kBoxOwn) + 8 * m.stages;
   sim->e_smem = (size_t)m.stages * (3 * kBoxHalo + (3 + m.ninv) * kBoxOwn) + 8 * m.stages;
-  const void* kernels[4] = {(const void*)h_tile<true>, (const void*)h_tile<false>,
-                            (const void*)e_tile<true>, (const void*)e_tile<false>};
-  for (int t = 0; t < 4; ++t) {
-    const size_t bytes = t < 2 ? sim->h_smem : sim->e_smem;
+  sim->e_ws_smem = (size_t)m.stages * (3 * kBoxHalo + (3 + m.ninv) * kBoxOwn) + 16 * m.stages;
+  const void* kernels[6] = {(const void*)h_tile<true>, (const void*)h_tile<false>,
+                            (const void*)e_tile<true>, (const void*)e_tile<false>,
+                            (const void*)e_ws<true>, (const void*)e_ws<false>};
+  for (int t = 0; t < 6; ++t) {
+    const size_t bytes = t < 2 ? sim->h_smem : t < 4 ? sim->e_smem : sim->e_ws_smem;
     if (cudaFuncSetAttribute(kernels[t], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
         cudaSuccess) {
       cudaGetLastError();
@@ -1852,7 +1979,6 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
   StepParams& p = sim->step;
   p.nx = d.nx; p.ny = d.ny; p.nz = d.nz;
   p.pml = d.pml_active ? 1 : 0;
-  p.inv_iso = (d.inv_eps[0] == d.inv_eps[1] && d.inv_eps[1] == d.inv_eps[2]) ? 1 : 0;
   {
     const int n[3] = {d.nx, d.ny, d.nz};
     for (int a = 0; a < 3; ++a) {
@@ -1981,8 +2107,14 @@ int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s) {
         if (pml) launch_step(sim, h_tile<true>, grid, dim3(kThreads), sim->h_smem, s, p, sim->maps, (int)(n == 0), xc);
         else launch_step(sim, h_tile<false>, grid, dim3(kThreads), sim->h_smem, s, p, sim->maps, (int)(n == 0), xc);
       } else {
-        if (pml) launch_step(sim, e_tile<true>, grid, dim3(kThreads), sim->e_smem, s, p, sim->maps, (int)(n & 1), xc);
-        else launch_step(sim, e_tile<false>, grid, dim3(kThreads), sim->e_smem, s, p, sim->maps, (int)(n & 1), xc);
+        if (hc.ws) {
+          if (pml) launch_step(sim, e_ws<true>, grid, dim3(kWsThreads), sim->e_ws_smem, s, p, sim->maps, (int)(n & 1), xc);
+          else launch_step(sim, e_ws<false>, grid, dim3(kWsThreads), sim->e_ws_smem, s, p, sim->maps, (int)(n & 1), xc);
+        } else if (pml) {
+          launch_step(sim, e_tile<true>, grid, dim3(kThreads), sim->e_smem, s, p, sim->maps, (int)(n & 1), xc);
+        } else {
+          launch_step(sim, e_tile<false>, grid, dim3(kThreads), sim->e_smem, s, p, sim->maps, (int)(n & 1), xc);
+        }
       }
       return MGB_OK;
     }
@@ -2134,26 +2266,31 @@ int mgb_uses_tiles(mgb_sim* sim) {
 }
 
 namespace {
-int choose_family(mgb_sim* sim, mgb_sim::HalfChoice& h, int family) {
+int choose_family(mgb_sim* sim, mgb_sim::HalfChoice& h, int family, int part) {
   if (family == 0 || family == 2) {
     h.tiles = false;
+    h.ws = false;
     h.prefetch = family == 2;
     return MGB_OK;
   }
-  if (family == 1) {
+  if (family == 1 || family == 3) {
     if (!sim->tiles_ready) return fail(MGB_ERR_UNSUPPORTED, "the tile kernels need a z extent that is a multiple of 4");
+    if (family == 3 && part != 1) return fail(MGB_ERR_UNSUPPORTED, "the warp-specialized tile kernel steps the E half");
     h.tiles = true;
+    h.ws = family == 3;
     h.prefetch = false;
     return MGB_OK;
   }
-  return fail(MGB_ERR_ARGUMENT, "kernel family is 0 (generic), 1 (tiles) or 2 (generic, prefetching)");
+  return fail(MGB_ERR_ARGUMENT,
+              "kernel family is 0 (generic), 1 (tiles), 2 (generic, prefetching) or 3 (tiles, warp-specialized)");
 }
 }  // namespace
 
 int mgb_select_kernels(mgb_sim* sim, int32_t family) {
   if (sim == nullptr) return fail(MGB_ERR_ARGUMENT, "null plan");
-  for (auto& h : sim->half) {
-    const int rc = choose_family(sim, h, family);
+  if (family == 3) return fail(MGB_ERR_UNSUPPORTED, "the warp-specialized tile kernel steps the E half only");
+  for (int part = 0; part < 2; ++part) {
+    const int rc = choose_family(sim, sim->half[part], family, part);
     if (rc != MGB_OK) return rc;
   }
   return MGB_OK;
@@ -2166,7 +2303,7 @@ int mgb_select_half(mgb_sim* sim, int32_t part, int32_t family, int32_t block_z,
   if (block_z < 1 || block_y < 1 || block_z * block_y > 256 || (block_z * block_y) % 32 != 0 || x_chunk < 1)
     return fail(MGB_ERR_ARGUMENT, "launch shape needs block_z*block_y a multiple of 32 up to 256 and x_chunk >= 1");
   mgb_sim::HalfChoice h = sim->half[part];
-  const int rc = choose_family(sim, h, family);
+  const int rc = choose_family(sim, h, family, part);
   if (rc != MGB_OK) return rc;
   h.block_z = block_z;
   h.block_y = block_y;

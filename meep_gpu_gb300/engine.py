@@ -41,12 +41,13 @@ SOURCE_WINDOW = 4096
 
 # Kernel choices the autotuner times: (family, block_z, block_y, x_chunk); family 1 is
 # the tile kernels (block shape fixed at 64 x 8, x_chunk used), family 0 the generic ones,
-# family 2 the generic ones with the next plane's loads issued ahead.
+# family 2 the generic ones with the next plane's loads issued ahead, family 3 the tile
+# kernels' warp-specialized form (E half only; the H half refuses it).
 AUTOTUNE_CANDIDATES = ((0, 32, 4, 4), (0, 32, 8, 4), (0, 32, 4, 8), (0, 64, 2, 8),
                        (0, 16, 8, 4), (0, 16, 16, 4), (0, 16, 8, 2), (0, 16, 8, 8), (0, 32, 2, 4),
                        (1, 64, 8, 4), (1, 64, 8, 8),
                        (2, 32, 4, 4), (2, 32, 4, 8), (2, 32, 8, 4), (2, 64, 2, 4), (2, 16, 8, 4),
-                       (2, 32, 4, 2), (2, 32, 2, 4))
+                       (2, 32, 4, 2), (2, 32, 2, 4), (3, 64, 8, 4), (3, 64, 8, 8), (3, 64, 8, 16))
 _AUTOTUNE_CACHE: Dict[tuple, Tuple[int, int, int, int]] = {}
 
 
@@ -82,13 +83,9 @@ class Engine:
         dev = self.device
         zeros = lambda s: torch.zeros(s, dtype=torch.float32, device=dev)  # noqa: E731
         self.fields: Dict[str, torch.Tensor] = {}
-        # each family's three components in one allocation (one contiguous range)
-        self.families: Dict[str, torch.Tensor] = {}
         for family in FIELD_NAMES:
-            block = zeros((3,) + tuple(shape))
-            self.families[family] = block
             for q, axis in enumerate("xyz"):
-                self.fields[family + axis] = block[q]
+                self.fields[family + axis] = zeros(shape)
         # inverse epsilon: one device volume per distinct host array
         self.inv_eps: List[torch.Tensor] = []
         seen: Dict[int, torch.Tensor] = {}
@@ -347,7 +344,7 @@ class Engine:
         else:
             h = e = tuple(int(v) for v in choice)
         for part, (family, bz, by, xc) in enumerate((h, e)):
-            if family == 1:
+            if family in (1, 3):
                 bz, by = 32, 8  # the tile kernels' block is fixed; the shape check still applies
             _lib.check(self.lib, self.lib.mgb_select_half(self.handle, part, family, bz, by, xc))
         self.choice = (h, e)
@@ -372,9 +369,18 @@ class Engine:
         best = [None, None]
         best_ms = [float("inf"), float("inf")]
         for choice in AUTOTUNE_CANDIDATES:
-            try:
-                scratch.select(choice)
-            except _lib.MeepGBError:
+            # a candidate one half refuses is timed on the other half only
+            applies = []
+            for part in (0, 1):
+                try:
+                    family, bz, by, xc = choice
+                    if family in (1, 3):
+                        bz, by = 32, 8
+                    _lib.check(self.lib, self.lib.mgb_select_half(scratch.handle, part, family, bz, by, xc))
+                    applies.append(part)
+                except _lib.MeepGBError:
+                    _lib.check(self.lib, self.lib.mgb_select_half(scratch.handle, part, 0, 32, 4, 4))
+            if not applies:
                 continue
             for n in range(2):
                 scratch.launch(n, 0, stream)
@@ -387,7 +393,7 @@ class Engine:
                 scratch.launch(2 + t, 1, stream)
                 ev[2].record(stream)
             marks[-1][2].synchronize()
-            for part in (0, 1):
+            for part in applies:
                 # the fastest of the timed launches: the least disturbed by anything else
                 ms = float(np.min([ev[part].elapsed_time(ev[part + 1]) for ev in marks]))
                 if ms < best_ms[part]:

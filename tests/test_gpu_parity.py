@@ -28,7 +28,8 @@ FIELDS = ("Ex", "Ey", "Ez", "Dx", "Dy", "Dz", "Bx", "By", "Bz", "Hx", "Hy", "Hz"
 TILES = (1, 64, 8, 8)
 GENERIC = (0, 32, 8, 4)
 PREFETCH = (2, 32, 4, 4)
-MODES = {"tiles": TILES, "generic": GENERIC, "prefetch": PREFETCH}
+WARP_SPECIALIZED = ((2, 16, 8, 4), (3, 64, 8, 8))  # H prefetching, E warp-specialized tiles
+MODES = {"tiles": TILES, "generic": GENERIC, "prefetch": PREFETCH, "ws": WARP_SPECIALIZED}
 
 
 def gpu_case(case, steps=None, kernels=None, chunks=None):
@@ -53,9 +54,11 @@ def test_fields_are_the_reference_words(gpu, name, mode):
     plain-load kernels and their prefetching form."""
     case = CASES[name]
     gold = golden_io.fields(name)
-    tiles = mode == "tiles" and case["n"][2] % 4 == 0
-    driver, flux, dft = gpu_case(case, kernels=TILES if tiles else MODES["generic" if mode == "tiles" else mode])
-    assert driver.engine.uses_tiles == tiles
+    tileable = case["n"][2] % 4 == 0
+    if mode in ("tiles", "ws") and not tileable:
+        mode = "generic"
+    driver, flux, dft = gpu_case(case, kernels=MODES[mode])
+    assert driver.engine.uses_tiles == (mode in ("tiles", "ws"))
     for c in FIELDS:
         got = driver.get_field(c, cell_centered=False)
         mismatched = int(np.sum(got != gold[c]))
@@ -82,11 +85,14 @@ def test_fields_are_the_reference_words(gpu, name, mode):
 @pytest.mark.parametrize("name", ["mixed", "tile_mixed", "tile_periodic_pml"])
 @pytest.mark.parametrize("choice", [(0, 32, 8, 16), (0, 64, 4, 7), (0, 16, 16, 200), (0, 128, 2, 1),
                                     (0, 32, 4, 3), (1, 64, 8, 1), (1, 64, 8, 5), (1, 64, 8, 200),
-                                    (2, 32, 8, 16), (2, 64, 4, 7), (2, 32, 4, 1), (2, 128, 2, 3)])
+                                    (2, 32, 8, 16), (2, 64, 4, 7), (2, 32, 4, 1), (2, 128, 2, 3),
+                                    (3, 64, 8, 1), (3, 64, 8, 5), (3, 64, 8, 200)])
 def test_launch_shape_does_not_change_a_word(gpu, choice, name):
-    """The x chunk (both families) and block shape (generic family) change no word."""
+    """The x chunk (every family) and block shape (generic families) change no word."""
     case = CASES[name]
-    if choice[0] == 1 and case["n"][2] % 4:
+    if choice[0] == 3:
+        choice = ((0, 32, 4, 4), choice)  # the warp-specialized kernel steps the E half
+    if (choice[0] == 1 or (isinstance(choice[0], tuple) and choice[1][0] == 3)) and case["n"][2] % 4:
         pytest.skip("the tile kernels need a z extent that is a multiple of 4")
     gold = golden_io.fields(name)
     driver, _, _ = gpu_case(case, kernels=choice)
@@ -95,12 +101,13 @@ def test_launch_shape_does_not_change_a_word(gpu, choice, name):
     driver.close()
 
 
+@pytest.mark.parametrize("kernels", [TILES, WARP_SPECIALIZED])
 @pytest.mark.parametrize("stages", ["2", "3", "6"])
-def test_ring_depth_does_not_change_a_word(gpu, stages, monkeypatch):
+def test_ring_depth_does_not_change_a_word(gpu, stages, kernels, monkeypatch):
     monkeypatch.setenv("MEEPGB_STAGES", stages)
     case = CASES["tile_lorentz"]
     gold = golden_io.fields("tile_lorentz")
-    driver, _, _ = gpu_case(case, kernels=TILES)
+    driver, _, _ = gpu_case(case, kernels=kernels)
     assert driver.engine.uses_tiles
     for c in FIELDS:
         assert np.array_equal(driver.get_field(c, cell_centered=False), gold[c]), (stages, c)
@@ -121,7 +128,7 @@ def test_chunked_runs_equal_one_run(gpu):
 def test_sphere80_words_after_200_steps(gpu, mode):
     gold = golden_io.digest()
     driver, flux, _ = gpu_case(SPHERE80, steps=gold["steps"], kernels=MODES[mode])
-    assert driver.engine.uses_tiles == (mode == "tiles")
+    assert driver.engine.uses_tiles == (mode in ("tiles", "ws"))
     for c, expected in gold["sha256"].items():
         words = np.ascontiguousarray(driver.get_field(c, cell_centered=False), dtype=np.float32)
         assert hashlib.sha256(words.tobytes()).hexdigest() == expected, c

@@ -228,3 +228,37 @@ def test_batch_autotuner_picks_a_candidate(gpu):
     for result in report.results:
         expected, _ = plain(SMALL[result.index], (0, 32, 4, 4))
         assert np.array_equal(result.spectrum, expected)
+
+
+@pytest.mark.gpu
+def test_batch_steps_every_golden_configuration_to_the_reference_words(gpu):
+    """Slots of different kinds in one batch -- absorbers on some faces, periodic axes,
+    Lorentz and Drude poles, extended and continuous sources -- each reach the reference's
+    own words (the golden fixtures) after its step count, bit for bit."""
+    from meep_gpu_gb300 import FdtdDriver, Susceptibility
+    from tests import golden_io
+    from tests.golden.cases import CASES, build_case
+
+    names = [n for n in sorted(CASES) if n not in ("mixed", "tile_mixed")]  # <= 2 monitors a slot
+    server = serving.BatchServer(gpu, max_slots=len(names), steps_per_replay=16, max_side=72)
+    jobs = []
+    for name in names:
+        driver, flux, dft = build_case(FdtdDriver, Susceptibility, CASES[name])
+        request = Request(len(jobs), 0, 1.0, 0.0, CASES[name]["steps"], 0.0)
+        job = serving._Job(request, driver, flux[0] if flux else None, serving.footprint_bytes(driver))
+        server.admit(job, 0.0)
+        jobs.append((name, job, flux, dft))
+    server.commit()
+    for _ in range(max(CASES[n]["steps"] for n in names) // 16 + 1):
+        server.launch()
+    server.stream.synchronize()
+    for name, job, flux, dft in jobs:
+        gold = golden_io.fields(name)
+        for c in ("Ex", "Ey", "Ez", "Dx", "Dy", "Dz", "Bx", "By", "Bz", "Hx", "Hy", "Hz"):
+            got = job.driver.get_field(c, cell_centered=False)
+            assert np.array_equal(got, gold[c]), (name, c)
+        for index, monitor in enumerate(flux):
+            expected = gold[f"flux{index}"]
+            assert np.max(np.abs(monitor.get_flux_spectrum() - expected)) <= 1e-5 * np.max(np.abs(expected)), name
+    server.close()
+

@@ -434,8 +434,26 @@ class Engine:
                 e += 4 * int(p0.numel())
         return {"h_half": word * h, "e_half": word * e}
 
+    # status bits the kernels set: 1 a non-finite E was written; 2 a tile kernel's wait
+    # for its shared-memory copies timed out; 4 a tensor-core contraction's wait timed out
+    STATUS_NONFINITE, STATUS_TILE_TIMEOUT, STATUS_MMA_TIMEOUT = 1, 2, 4
+
+    def device_status(self) -> int:
+        """The status word (one small device-to-host read); raises if a kernel timed out."""
+        word = int(self.status.item())
+        if word & (self.STATUS_TILE_TIMEOUT | self.STATUS_MMA_TIMEOUT):
+            what = []
+            if word & self.STATUS_TILE_TIMEOUT:
+                what.append("a tile kernel's wait for its staged planes")
+            if word & self.STATUS_MMA_TIMEOUT:
+                what.append("a tensor-core contraction's wait for its MMAs")
+            raise RuntimeError(f"{' and '.join(what)} timed out on the device; the results of "
+                               "the steps since the last check are not valid")
+        return word
+
     def nonfinite(self) -> bool:
-        return bool(self.status.item() != 0)
+        """Whether a non-finite E has been written (raises on a device timeout)."""
+        return bool(self.device_status() & self.STATUS_NONFINITE)
 
     # --- read-out -----------------------------------------------------------------------
     def field(self, name: str) -> torch.Tensor:

@@ -76,3 +76,27 @@ def test_array_deposit_words_equal_the_per_step_form():
         slow = S.deposit_words_scalar(srcs, first, steps, grid.dt)
         assert fast.shape == slow.shape
         assert np.array_equal(fast.view(np.uint64), slow.view(np.uint64)), (first, steps)
+
+
+def test_device_status_word_is_decoded():
+    """Bit 1 is a divergence (reported to the caller as such); the wait time-out bits raise."""
+    import types
+
+    import torch
+
+    from meep_gpu_gb300.engine import Engine
+
+    def fake(word):
+        return types.SimpleNamespace(status=torch.tensor([word], dtype=torch.int32),
+                                     STATUS_NONFINITE=1, STATUS_TILE_TIMEOUT=2, STATUS_MMA_TIMEOUT=4,
+                                     device_status=lambda: Engine.device_status(fake_obj[0]))
+
+    fake_obj = [None]
+    for word, diverged in ((0, False), (1, True)):
+        fake_obj[0] = fake(word)
+        assert Engine.device_status(fake_obj[0]) == word
+        assert Engine.nonfinite(fake_obj[0]) is diverged
+    for word in (2, 4, 6, 3):
+        fake_obj[0] = fake(word)
+        with pytest.raises(RuntimeError, match="timed out"):
+            Engine.device_status(fake_obj[0])

@@ -264,6 +264,15 @@ int mgb_adjoint_step(mgb_sim* adj, const mgb_adjoint* a, int64_t step, void* str
  * multiple of its decimation) into the adjoint E and H. Asynchronous. */
 int mgb_adjoint_inject(mgb_sim* adj, int32_t monitor, int64_t post, void* stream);
 
+/* One checkpoint interval in one call: the forward plan (restored to the state before
+ * first_step by the caller) steps first_step .. first_step+nsteps-1 again (H and E halves,
+ * no monitors), saving D over the box after each step into d_history [nsteps][3][box
+ * cells]; then the adjoint steps back through the same steps, with the adjoint of every
+ * sample of monitor `monitor` added where the forward took one. The forward plan's
+ * source words must cover the interval. Asynchronous. */
+int mgb_adjoint_segment(mgb_sim* fwd, mgb_sim* adj, const mgb_adjoint* a, int64_t first_step,
+                        int32_t nsteps, int32_t monitor, float* d_history, void* stream);
+
 /* Copy [3][box cells] of a plan's E (family 0), D (1) or H (2) into dst. Asynchronous. */
 int mgb_copy_box(mgb_sim* sim, int32_t family, const int32_t* box, float* dst, void* stream);
 

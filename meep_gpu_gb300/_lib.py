@@ -124,6 +124,9 @@ SIGNATURES = {
     "mgb_adjoint_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(MgbAdjoint), ctypes.c_int64,
                                         ctypes.c_void_p]),
     "mgb_adjoint_inject": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p]),
+    "mgb_adjoint_segment": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(MgbAdjoint),
+                                           ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+                                           ctypes.c_void_p]),
     "mgb_copy_box": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_void_p]),
     "mgb_batch_bytes": (ctypes.c_size_t, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),

@@ -177,23 +177,16 @@ class FluxAdjoint:
         self.grad_inv.zero_()
         self.adj.grad_inv = self.grad_inv.data_ptr()
         self.adj.box[:] = list(self._box_arg)
-        decimation = self.monitor.decimation_factor
+        self.adj.d_after = self.d_history.data_ptr()
         for seg in range(len(self.checkpoints) - 1, -1, -1):
             n0 = seg * self.every
             n1 = min(self.steps, n0 + self.every)
             for t, saved in zip(self.state, self.checkpoints[seg]):
                 t.copy_(saved)
-            for n in range(n0, n1):
-                engine.launch(n, 0, stream)
-                engine.launch(n, 1, stream)
-                _lib.check(lib, lib.mgb_copy_box(engine.handle, 1, self._box_arg,
-                                                 self.d_history[n - n0].data_ptr(), handle))
-            for n in range(n1 - 1, n0 - 1, -1):
-                post = n + 1
-                if post % decimation == 0:
-                    _lib.check(lib, lib.mgb_adjoint_inject(self.adj_handle, 0, post, handle))
-                self.adj.d_after = self.d_history[n - n0].data_ptr()
-                _lib.check(lib, lib.mgb_adjoint_step(self.adj_handle, ctypes.byref(self.adj), n, handle))
+            engine.ensure_source_words(n0, n1 - n0)
+            # recompute the segment and step the adjoint back through it (one library call)
+            _lib.check(lib, lib.mgb_adjoint_segment(engine.handle, self.adj_handle, ctypes.byref(self.adj),
+                                                    n0, n1 - n0, 0, self.d_history.data_ptr(), handle))
         grad_inv = self.grad_inv.to(torch.float64).reshape(self.box_shape)
         return -grad_inv / (self.eps_box * self.eps_box)
 

@@ -2818,3 +2818,45 @@ int mgb_copy_box(mgb_sim* sim, int32_t family, const int32_t* box, float* dst, v
 
 }  // extern "C"
 
+
+// ======================================================================================
+// Adjoint segment: one checkpoint interval recomputed and reversed in one call
+extern "C" {
+
+int mgb_adjoint_segment(mgb_sim* fwd, mgb_sim* adj, const mgb_adjoint* a, int64_t first_step, int32_t nsteps,
+                        int32_t monitor, float* d_history, void* stream) {
+  if (fwd == nullptr || adj == nullptr || a == nullptr || d_history == nullptr)
+    return fail(MGB_ERR_ARGUMENT, "null argument");
+  if (nsteps < 1) return fail(MGB_ERR_ARGUMENT, "a segment has at least one step");
+  if (monitor < 0 || monitor >= adj->desc.nmonitors) return fail(MGB_ERR_ARGUMENT, "no such monitor");
+  int rc = check_words(fwd, first_step, nsteps);
+  if (rc != MGB_OK) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const long long box_cells =
+      (long long)(a->box[1] - a->box[0]) * (a->box[3] - a->box[2]) * (a->box[5] - a->box[4]);
+  // forward again from the restored checkpoint (the halves only: monitors are not
+  // needed), keeping D over the box after every step
+  for (int t = 0; t < nsteps; ++t) {
+    const long long n = first_step + t;
+    rc = launch_part(fwd, n, 0, s);
+    if (rc == MGB_OK) rc = launch_part(fwd, n, 1, s);
+    if (rc == MGB_OK) rc = mgb_copy_box(fwd, 1, a->box, d_history + (long long)t * 3 * box_cells, stream);
+    if (rc != MGB_OK) return rc;
+  }
+  // then the adjoint back through the segment
+  const int decimation = adj->desc.monitors[monitor].decimation;
+  mgb_adjoint step_args = *a;
+  for (int t = nsteps - 1; t >= 0; --t) {
+    const long long n = first_step + t;
+    if ((n + 1) % decimation == 0) {
+      rc = mgb_adjoint_inject(adj, monitor, n + 1, stream);
+      if (rc != MGB_OK) return rc;
+    }
+    step_args.d_after = d_history + (long long)t * 3 * box_cells;
+    rc = mgb_adjoint_step(adj, &step_args, n, stream);
+    if (rc != MGB_OK) return rc;
+  }
+  return launch_error("adjoint segment");
+}
+
+}  // extern "C"

@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define MGB_ABI_VERSION 1
+#define MGB_ABI_VERSION 2
 #define MGB_MAX_POLES 4
 #define MGB_MAX_MONITORS 16
 #define MGB_MAX_MONITOR_COMPONENTS 6
@@ -84,6 +84,28 @@ typedef struct mgb_monitor {
   float* acc;           /* device */
 } mgb_monitor;
 
+/* MEEP's D and B conductivity (mp.Medium D_conductivity / B_conductivity and the graded
+ * mp.Absorber), which replaces the curl update f -= curl of a lossy component by
+ * f = ((condfac f) - curl) condinv (step_generic.cpp step_curl). Index [side][q]: side 0
+ * is B (stepped in the H half), side 1 is D (the E half). Replaces the conductivity
+ * volumes Fields.set_d_conductivity / set_b_conductivity install
+ * (meep_gpu/fields.py:775, :822) and the conductive curl forms of
+ * meep_gpu/stepping.py:2828 (_apply_conductive_update) and :2844
+ * (_apply_conductive_pml_update). */
+typedef struct mgb_conductivity {
+  const float* condfac[2][3]; /* device volumes, 1 - sigma dt/2 in float32; NULL: lossless */
+  const float* condinv[2][3]; /* device volumes, 1 / (1 + sigma dt/2) rounded once from double */
+  /* With a PML (pml_active), per lossy component: */
+  float* fcond[2][3]; /* the conductive-stage history, a full volume read and written on
+                       * the dsig membership of the chunks that keep the conductivity */
+  /* [lattice: 0 integer, 1 half-integer][axis]: the one-rank chunk of every stored row
+   * (0 the low PML chunk, 1 the interior, 2 the high one), device, length of the axis */
+  const int8_t* chunk_of[2][3];
+  /* per lossy component, bit (x * 9 + y * 3 + z) set when the chunk with those pieces
+   * keeps a conductivity array for it (some sample of its loop volume is nonzero) */
+  uint32_t keeps[2][3];
+} mgb_conductivity;
+
 typedef struct mgb_sim_desc {
   int32_t abi_version; /* MGB_ABI_VERSION */
   int32_t nx, ny, nz;
@@ -126,6 +148,10 @@ typedef struct mgb_sim_desc {
    * 2 when a wait for its own shared-memory copies exceeds its time limit (the kernel
    * then stops stepping instead of spinning). */
   int32_t* status; /* device, may be NULL */
+  /* D and B conductivity, NULL for a lossless run; the library keeps a copy. A run with
+   * a conductivity steps with the generic kernels (family 0) and is refused by the
+   * batch and the adjoint entry points. */
+  const mgb_conductivity* conductivity;
 } mgb_sim_desc;
 
 typedef struct mgb_sim mgb_sim;

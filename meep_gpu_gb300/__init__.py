@@ -5,6 +5,7 @@
 step in ``libmeepgb.so`` (C ABI: ``include/meepgb.h``). There is no CPU stepping path.
 """
 
+from .conductivity import AbsorberLayer
 from .dft import DFTMonitor, FluxMonitor
 from .dispersion import DRUDE, LORENTZ, Susceptibility
 from .driver import FdtdCancelled, FdtdDivergence, FdtdDriver
@@ -12,5 +13,5 @@ from .grid import Grid, Unsupported
 from .pml import PML
 
 __all__ = ["FdtdDriver", "FdtdCancelled", "FdtdDivergence", "Susceptibility", "LORENTZ",
-           "DRUDE", "Grid", "PML", "FluxMonitor", "DFTMonitor", "Unsupported"]
+           "DRUDE", "Grid", "PML", "FluxMonitor", "DFTMonitor", "Unsupported", "AbsorberLayer"]
 __version__ = "0.1.0"

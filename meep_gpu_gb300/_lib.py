@@ -14,7 +14,7 @@ from typing import Optional
 
 PACKAGE = Path(__file__).resolve().parent
 
-MGB_ABI_VERSION = 1
+MGB_ABI_VERSION = 2
 MGB_MAX_POLES = 4
 MGB_MAX_MONITORS = 16
 MGB_MAX_MONITOR_COMPONENTS = 6
@@ -52,6 +52,16 @@ class MgbMonitor(ctypes.Structure):
                 ("omega", ctypes.c_void_p), ("acc", ctypes.c_void_p)]
 
 
+class MgbConductivity(ctypes.Structure):
+    _fields_ = [
+        ("condfac", (ctypes.c_void_p * 3) * 2),
+        ("condinv", (ctypes.c_void_p * 3) * 2),
+        ("fcond", (ctypes.c_void_p * 3) * 2),
+        ("chunk_of", (ctypes.c_void_p * 3) * 2),
+        ("keeps", (ctypes.c_uint32 * 3) * 2),
+    ]
+
+
 class MgbSimDesc(ctypes.Structure):
     _fields_ = [
         ("abi_version", ctypes.c_int32),
@@ -81,6 +91,7 @@ class MgbSimDesc(ctypes.Structure):
         ("nmonitors", ctypes.c_int32),
         ("monitors", MgbMonitor * MGB_MAX_MONITORS),
         ("status", ctypes.c_void_p),
+        ("conductivity", ctypes.POINTER(MgbConductivity)),
     ]
 
 

@@ -40,6 +40,8 @@ class FluxAdjoint:
             raise ValueError("the objective's monitor must be a flux monitor of the driver")
         if driver._poles:
             raise Unsupported("the adjoint step does not carry susceptibility poles")
+        if driver.has_conductivity:
+            raise Unsupported("the adjoint step does not carry a conductivity")
         if driver.engine is not None:
             raise RuntimeError("the adjoint problem needs a driver that has not been stepped")
         if steps < 1 or checkpoint_every < 1:

@@ -193,6 +193,57 @@ __device__ __forceinline__ float curl_form(float f, float curl, bool member, flo
   return DSIG ? (kms * f - curl) * sinv : f - curl;
 }
 
+// One curl component of a lossy side (MEEP's step_curl with a conductivity, restated
+// from meep_gpu/stepping.py:2828 and :2844). `side` 0 is B, 1 is D; `sg` / `su` whether
+// the cell's chunk carries the component's dsig / dsigu layer. With cf = condfac and
+// ci = condinv, in float32 in this order:
+//   no PML:                 f' = ((cf*f) - curl)*ci
+//   a chunk that keeps the component's conductivity, dsig and dsigu:
+//     g' = ((cf*g) - curl)*ci (the conductive-stage history g), u' = ((kms*u) + (g' - g))*sinv,
+//     f' = (((kms_u*f) + u') - u)*sinv_u
+//   dsig only: g' as above, f' = ((kms*f) + (g' - g))*sinv
+//   dsigu only: u' = ((cf*u) - curl)*ci, f' = (((kms_u*f) + u') - u)*sinv_u
+//   neither: f' = ((cf*f) - curl)*ci
+//   a chunk that keeps none: the lossless forms of curl_form.
+// A component without a conductivity takes curl_form. The increment (g' - g) is formed
+// before it is added, as MEEP groups it.
+template <bool PML>
+__device__ __forceinline__ float cond_curl(const mgb_conductivity& cp, int side, int q, int i, int j, int k,
+                                           int c, float f, float curl, bool sg, bool su, float u, float kms,
+                                           float sinv, float kms_u, float sinv_u, float& n) {
+  const float* fac = cp.condfac[side][q];
+  if (fac == nullptr) return curl_form<PML, PML>(f, curl, su, u, kms, sinv, kms_u, sinv_u, n);
+  const float cf = __ldg(fac + c);
+  const float ci = __ldg(cp.condinv[side][q] + c);
+  if (!PML) return ((cf * f) - curl) * ci;
+  // the chunk of this cell: per axis, the piece on the component's lattice there (B sits
+  // on the integer lattice of its own axis and the half lattice of the others, D the
+  // other way round)
+  const int own = side == 0 ? kInteger : kHalf, other = side == 0 ? kHalf : kInteger;
+  const int px = __ldg(cp.chunk_of[q == 0 ? own : other][0] + i);
+  const int py = __ldg(cp.chunk_of[q == 1 ? own : other][1] + j);
+  const int pz = __ldg(cp.chunk_of[q == 2 ? own : other][2] + k);
+  if (((cp.keeps[side][q] >> (px * 9 + py * 3 + pz)) & 1u) == 0)
+    return curl_form<true, true>(f, curl, su, u, kms, sinv, kms_u, sinv_u, n);
+  if (sg) {
+    float* hist = cp.fcond[side][q] + c;
+    const float g = *hist;
+    const float g_new = ((cf * g) - curl) * ci;
+    *hist = g_new;
+    const float inc = g_new - g;
+    if (su) {
+      n = ((kms * u) + inc) * sinv;
+      return (((kms_u * f) + n) - u) * sinv_u;
+    }
+    return ((kms * f) + inc) * sinv;
+  }
+  if (su) {
+    n = ((cf * u) - curl) * ci;
+    return (((kms_u * f) + n) - u) * sinv_u;
+  }
+  return ((cf * f) - curl) * ci;
+}
+
 // B from its curls, zero_metal_B, H from B (update_H) for one cell at offset c, and the
 // auxiliary stores, for a warp that may touch the x (SX), y (SY) and z (SZ) memberships.
 // Each axis switches on one feature per component (x: Bx own, By dsigu, Bz dsig;
@@ -216,11 +267,12 @@ __device__ __forceinline__ void h_aux_load(const StepParams& p, const HColumn& c
   }
 }
 
-template <bool SX, bool SY, bool SZ>
+template <bool SX, bool SY, bool SZ, bool COND = false>
 __device__ __forceinline__ void h_cell_v(const StepParams& p, const HColumn& col,
                                          const HPlane& pl, int first_step, int c, float cx,
                                          float cy, float cz, const float h_old[3], const HAux& a,
-                                         float h_new[3]) {
+                                         float h_new[3], const mgb_conductivity* cp = nullptr,
+                                         int i = 0, int j = 0, int k = 0) {
   const bool sb0 = SX && pl.b0, sb1 = SY && col.b1, sb2 = SZ && col.b2;
   const bool sf0 = SZ && col.f0, sf1 = SX && pl.f1, sf2 = SY && col.f2;
   // The cell's auxiliary words (loaded by the caller, before any store).
@@ -231,9 +283,18 @@ __device__ __forceinline__ void h_cell_v(const StepParams& p, const HColumn& col
   const float u0 = a.u[0], u1 = a.u[1], u2 = a.u[2];
   // Bx: dsig y, dsigu z; By: dsig z, dsigu x; Bz: dsig x, dsigu y.
   float n0 = 0.f, n1 = 0.f, n2 = 0.f;
-  b0 = curl_form<SY, SZ>(b0, cx, sf0, u0, col.kms_yh, col.sinv_yh, col.kms_zh, col.sinv_zh, n0);
-  b1 = curl_form<SZ, SX>(b1, cy, sf1, u1, col.kms_zh, col.sinv_zh, pl.kms_xh, pl.sinv_xh, n1);
-  b2 = curl_form<SX, SY>(b2, cz, sf2, u2, pl.kms_xh, pl.sinv_xh, col.kms_yh, col.sinv_yh, n2);
+  if (COND) {
+    // the dsig membership of each component is the dsigu membership of the component
+    // two after it (same axis, same lattice)
+    constexpr bool P = SX || SY || SZ;
+    b0 = cond_curl<P>(*cp, 0, 0, i, j, k, c, b0, cx, col.f2, sf0, u0, col.kms_yh, col.sinv_yh, col.kms_zh, col.sinv_zh, n0);
+    b1 = cond_curl<P>(*cp, 0, 1, i, j, k, c, b1, cy, col.f0, sf1, u1, col.kms_zh, col.sinv_zh, pl.kms_xh, pl.sinv_xh, n1);
+    b2 = cond_curl<P>(*cp, 0, 2, i, j, k, c, b2, cz, pl.f1, sf2, u2, pl.kms_xh, pl.sinv_xh, col.kms_yh, col.sinv_yh, n2);
+  } else {
+    b0 = curl_form<SY, SZ>(b0, cx, sf0, u0, col.kms_yh, col.sinv_yh, col.kms_zh, col.sinv_zh, n0);
+    b1 = curl_form<SZ, SX>(b1, cy, sf1, u1, col.kms_zh, col.sinv_zh, pl.kms_xh, pl.sinv_xh, n1);
+    b2 = curl_form<SX, SY>(b2, cz, sf2, u2, pl.kms_xh, pl.sinv_xh, col.kms_yh, col.sinv_yh, n2);
+  }
   // zero_metal_B happens in the caller before this returns its words (masks above).
   h_new[0] = b0; h_new[1] = b1; h_new[2] = b2;
   // update_H on the own-axis integer membership (MEEP starts H and f_w from B once).
@@ -254,18 +315,23 @@ __device__ __forceinline__ bool h_needs_plane(int axes) { return axes != 0 && ax
 
 // One cell of the H half: masks, the variant for the warp's memberships, zero_metal_B.
 // `axes` bit 0/1/2: the warp touches the x/y/z memberships (0 on the fast path).
-template <bool PML>
+template <bool PML, bool COND = false>
 __device__ __forceinline__ void h_cell(const StepParams& p, const HColumn& col, const HPlane& pl,
                                        int axes, int first_step, int i, int j, int k, int c,
                                        float cx, float cy, float cz, const float h_old[3],
-                                       const HAux& a, float h_new[3]) {
+                                       const HAux& a, float h_new[3], const mgb_conductivity* cp = nullptr) {
   if (p.met[0] && i == 0) cx = 0.f;
   if (p.met[1] && j == 0) cy = 0.f;
   if (p.met[2] && k == 0) cz = 0.f;
   // zero_metal_B clears the wall samples after the curl update; a wall cell is never
   // in its component's own-axis membership, so there H is B and clearing H_new after
   // the accumulation is the same word.
-  if (!PML || axes == 0) {
+  if (COND) {
+    // a lossy run: every cell of a PML run takes the general variant (the conductive
+    // forms test each membership per cell)
+    if (PML) h_cell_v<true, true, true, true>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new, cp, i, j, k);
+    else h_cell_v<false, false, false, true>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new, cp, i, j, k);
+  } else if (!PML || axes == 0) {
     h_cell_v<false, false, false>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new);
   } else {
     // The z-only edge (the two z-edge warps of every interior row) is the commonest slow
@@ -335,11 +401,12 @@ __device__ __forceinline__ void e_aux_load(const StepParams& p, const EColumn& c
   }
 }
 
-template <bool SX, bool SY, bool SZ>
+template <bool SX, bool SY, bool SZ, bool COND = false>
 __device__ __forceinline__ void e_cell_v(const StepParams& p, const EColumn& col, const EPlane& pl,
                                          int parity, int i, int j, int k, int c, float cx,
                                          float cy, float cz, float d[3], const float inv[3],
-                                         const double* words, const EAux& a) {
+                                         const double* words, const EAux& a,
+                                         const mgb_conductivity* cp = nullptr) {
   const bool wx = p.met[0] && i == 0, wy = p.met[1] && j == 0, wz = p.met[2] && k == 0;
   if (wy || wz) cx = 0.f;
   if (wx || wz) cy = 0.f;
@@ -352,9 +419,17 @@ __device__ __forceinline__ void e_cell_v(const StepParams& p, const EColumn& col
   const float e0 = a.e[0], e1 = a.e[1], e2 = a.e[2];
   // Dx: dsig y, dsigu z; Dy: dsig z, dsigu x; Dz: dsig x, dsigu y.
   float n0 = 0.f, n1 = 0.f, n2 = 0.f;
-  d[0] = curl_form<SY, SZ>(d[0], cx, sf0, u0, col.kms_y, col.sinv_y, col.kms_z, col.sinv_z, n0);
-  d[1] = curl_form<SZ, SX>(d[1], cy, sf1, u1, col.kms_z, col.sinv_z, pl.kms_x, pl.sinv_x, n1);
-  d[2] = curl_form<SX, SY>(d[2], cz, sf2, u2, pl.kms_x, pl.sinv_x, col.kms_y, col.sinv_y, n2);
+  if (COND) {
+    // dsig of each component = the dsigu membership of the component two after it
+    constexpr bool P = SX || SY || SZ;
+    d[0] = cond_curl<P>(*cp, 1, 0, i, j, k, c, d[0], cx, col.f2, sf0, u0, col.kms_y, col.sinv_y, col.kms_z, col.sinv_z, n0);
+    d[1] = cond_curl<P>(*cp, 1, 1, i, j, k, c, d[1], cy, col.f0, sf1, u1, col.kms_z, col.sinv_z, pl.kms_x, pl.sinv_x, n1);
+    d[2] = cond_curl<P>(*cp, 1, 2, i, j, k, c, d[2], cz, pl.f1, sf2, u2, pl.kms_x, pl.sinv_x, col.kms_y, col.sinv_y, n2);
+  } else {
+    d[0] = curl_form<SY, SZ>(d[0], cx, sf0, u0, col.kms_y, col.sinv_y, col.kms_z, col.sinv_z, n0);
+    d[1] = curl_form<SZ, SX>(d[1], cy, sf1, u1, col.kms_z, col.sinv_z, pl.kms_x, pl.sinv_x, n1);
+    d[2] = curl_form<SX, SY>(d[2], cz, sf2, u2, pl.kms_x, pl.sinv_x, col.kms_y, col.sinv_y, n2);
+  }
   // Electric sources at t + dt/2: f = float(double(f) - A), point by point in order.
   if (p.nsrc > 0 && i >= p.src_box[0] && i < p.src_box[1] && j >= p.src_box[2] &&
       j < p.src_box[3] && k >= p.src_box[4] && k < p.src_box[5]) {
@@ -425,11 +500,18 @@ __device__ __forceinline__ void e_cell_v(const StepParams& p, const EColumn& col
   if (bad && p.status != nullptr) atomicOr(p.status, 1);
 }
 
-template <bool PML>
+template <bool PML, bool COND = false>
 __device__ __forceinline__ void e_cell(const StepParams& p, const EColumn& col, const EPlane& pl,
                                        int axes, int parity, int i, int j, int k, int c, float cx,
                                        float cy, float cz, float d[3], const float inv[3],
-                                       const double* words, const EAux& a) {
+                                       const double* words, const EAux& a,
+                                       const mgb_conductivity* cp = nullptr) {
+  if (COND) {
+    // a lossy run: every cell of a PML run takes the general variant
+    if (PML) e_cell_v<true, true, true, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words, a, cp);
+    else e_cell_v<false, false, false, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words, a, cp);
+    return;
+  }
   if (!PML) axes = 0;
   switch (axes) {
     case 0: e_cell_v<false, false, false>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words, a); break;
@@ -462,9 +544,9 @@ __device__ __forceinline__ bool cta_inner(const StepParams& p, int i0, int i1, i
 // ------------------------------------------------------------------------------------
 // Generic kernels: plain loads, one thread per (y, z) column marching over x.
 // One thread's column (j, k) of the H half over planes [i0, i1).
-template <bool PML>
+template <bool PML, bool COND = false>
 __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i0, int i1,
-                                        int first_step) {
+                                        int first_step, const mgb_conductivity* cp = nullptr) {
   const int sx = p.ny * p.nz;
   const int sy = p.nz;
   const float* Ex = p.E[0];
@@ -492,7 +574,7 @@ __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i
     int axes = 0;
     if (PML) {
       pl = h_plane(p, i);
-      axes = col_axes | ((pl.f1 || pl.b0) ? 1 : 0);
+      axes = COND ? 7 : col_axes | ((pl.f1 || pl.b0) ? 1 : 0);
       if (h_needs_plane(axes)) h_plane_coefficients(p, i, pl);
     }
     const float ex = Ex[c];
@@ -519,7 +601,7 @@ __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i
     const float cy = dtdx * (((ex_zp - ex) + ez) - ez_xp);
     const float cz = dtdx * (((ey_xp - ey) + ex) - ex_yp);
     float h_new[3];
-    h_cell<PML>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, h_old, ax, h_new);
+    h_cell<PML, COND>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, h_old, ax, h_new, cp);
     p.H[0][c] = h_new[0];
     p.H[1][c] = h_new[1];
     p.H[2][c] = h_new[2];
@@ -529,9 +611,10 @@ __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i
 }
 
 // One thread's column (j, k) of the E half over planes [i0, i1).
-template <bool PML>
+template <bool PML, bool COND = false>
 __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i0, int i1,
-                                        int parity, const double* words) {
+                                        int parity, const double* words,
+                                        const mgb_conductivity* cp = nullptr) {
   const int sx = p.ny * p.nz;
   const int sy = p.nz;
   const float dtdx = p.dtdx;
@@ -564,7 +647,7 @@ __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i
     int axes = 0;
     if (PML) {
       pl = e_plane(p, i);
-      axes = col_axes | ((pl.f1 || pl.w0) ? 1 : 0);
+      axes = COND ? 7 : col_axes | ((pl.f1 || pl.w0) ? 1 : 0);
       if (axes & 1) e_plane_coefficients(p, i, pl);
     }
     const float hx = Hx[c], hy = Hy[c], hz = Hz[c];
@@ -586,7 +669,7 @@ __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i
     const float cx = dtdx * (((hz_ym - hz) + hy) - hy_zm);
     const float cy = dtdx * (((hx_zm - hx) + hz) - hz_xm);
     const float cz = dtdx * (((hy_xm - hy) + hx) - hx_ym);
-    e_cell<PML>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, d, inv, words, ax);
+    e_cell<PML, COND>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, d, inv, words, ax, cp);
     hy_xm = hy;
     hz_xm = hz;
   }
@@ -825,6 +908,37 @@ __global__ void __launch_bounds__(256, 5) e_generic(const __grid_constant__ Step
     e_march<false>(p, j, k, i0, i1, parity, p.src_words);
   else
     e_march<PML>(p, j, k, i0, i1, parity, p.src_words);
+}
+
+// Generic kernels of a lossy run (a D or B conductivity): the same column march with
+// the conductive curl forms; the conductivity volumes and tables come as a second
+// parameter block so the lossless kernels' parameters stay as they are.
+template <bool PML>
+__global__ void __launch_bounds__(256) h_generic_cond(const __grid_constant__ StepParams p,
+                                                      const __grid_constant__ mgb_conductivity cp,
+                                                      int first_step, int xchunk) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (k >= p.nz || j >= p.ny) return;
+  const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  if (PML && cta_inner(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x))
+    h_march<false, true>(p, j, k, i0, i1, first_step, &cp);
+  else
+    h_march<PML, true>(p, j, k, i0, i1, first_step, &cp);
+}
+
+template <bool PML>
+__global__ void __launch_bounds__(256) e_generic_cond(const __grid_constant__ StepParams p,
+                                                      const __grid_constant__ mgb_conductivity cp,
+                                                      int parity, int xchunk) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (k >= p.nz || j >= p.ny) return;
+  const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  if (PML && cta_inner(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x))
+    e_march<false, true>(p, j, k, i0, i1, parity, p.src_words, &cp);
+  else
+    e_march<PML, true>(p, j, k, i0, i1, parity, p.src_words, &cp);
 }
 
 // ------------------------------------------------------------------------------------
@@ -1771,6 +1885,10 @@ struct mgb_sim {
     int tile_xchunk = 8;                        // tile kernels
   } half[2];
   bool tiles_ready = false;  // their tensor maps are built
+  // A D or B conductivity: the lossy generic kernels step the run (no tiles, no
+  // prefetching marches, no batch slot, no adjoint).
+  bool has_cond = false;
+  mgb_conductivity cond = {};
   size_t h_smem = 0, e_smem = 0, e_ws_smem = 0;
   const double* words = nullptr;
   long long words_first = 0;
@@ -1843,6 +1961,7 @@ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) ==
 void setup_tiles(mgb_sim* sim) {
   const char* env = getenv("MEEPGB_TILES");
   if (env != nullptr && env[0] == '0') return;
+  if (sim->has_cond) return;
   const StepParams& p = sim->step;
   if (p.nz % 4 != 0) return;
   for (int q = 0; q < 3; ++q)
@@ -1973,9 +2092,34 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
       return fail(MGB_ERR_UNSUPPORTED, "a monitor holds at most 3072 frequencies");
     }
   }
+  bool lossy = false;
+  if (d.conductivity != nullptr) {
+    const mgb_conductivity& cd = *d.conductivity;
+    static const char* names[2][3] = {{"Bx", "By", "Bz"}, {"Dx", "Dy", "Dz"}};
+    for (int side = 0; side < 2; ++side)
+      for (int q = 0; q < 3; ++q) {
+        if (cd.condfac[side][q] == nullptr) continue;
+        lossy = true;
+        if (cd.condinv[side][q] == nullptr)
+          return fail(MGB_ERR_ARGUMENT, std::string("the conductivity of ") + names[side][q] + " has no condinv volume");
+        if (d.pml_active && cd.fcond[side][q] == nullptr)
+          return fail(MGB_ERR_ARGUMENT, std::string("the conductivity of ") + names[side][q] +
+                                            " under a PML needs its conductive-stage history (fcond)");
+      }
+    if (lossy && d.pml_active)
+      for (int l = 0; l < 2; ++l)
+        for (int a = 0; a < 3; ++a)
+          if (cd.chunk_of[l][a] == nullptr)
+            return fail(MGB_ERR_ARGUMENT, "a conductivity under a PML needs the chunk of every row (chunk_of)");
+  }
   mgb_sim* sim = new (std::nothrow) mgb_sim();
   if (sim == nullptr) return fail(MGB_ERR_ARGUMENT, "host allocation of the plan failed");
   sim->desc = d;
+  sim->desc.conductivity = nullptr;  // the caller's struct need not outlive this call
+  if (lossy) {
+    sim->has_cond = true;
+    sim->cond = *d.conductivity;
+  }
   StepParams& p = sim->step;
   p.nx = d.nx; p.ny = d.ny; p.nz = d.nz;
   p.pml = d.pml_active ? 1 : 0;
@@ -2121,6 +2265,16 @@ int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s) {
     const dim3 block(hc.block_z, hc.block_y, 1);
     const int xc = hc.xchunk;
     const dim3 grid((p.nz + block.x - 1) / block.x, (p.ny + block.y - 1) / block.y, (p.nx + xc - 1) / xc);
+    if (sim->has_cond) {
+      if (part == 0) {
+        if (pml) launch_step(sim, h_generic_cond<true>, grid, block, 0, s, p, sim->cond, (int)(n == 0), xc);
+        else launch_step(sim, h_generic_cond<false>, grid, block, 0, s, p, sim->cond, (int)(n == 0), xc);
+      } else {
+        if (pml) launch_step(sim, e_generic_cond<true>, grid, block, 0, s, p, sim->cond, (int)(n & 1), xc);
+        else launch_step(sim, e_generic_cond<false>, grid, block, 0, s, p, sim->cond, (int)(n & 1), xc);
+      }
+      return MGB_OK;
+    }
     if (hc.prefetch) {
       if (part == 0) {
         if (pml) launch_step(sim, h_generic_pf<true>, grid, block, 0, s, p, (int)(n == 0), xc);
@@ -2267,6 +2421,8 @@ int mgb_uses_tiles(mgb_sim* sim) {
 
 namespace {
 int choose_family(mgb_sim* sim, mgb_sim::HalfChoice& h, int family, int part) {
+  if (sim->has_cond && family != 0)
+    return fail(MGB_ERR_UNSUPPORTED, "a run with a conductivity steps with the generic kernels (family 0)");
   if (family == 0 || family == 2) {
     h.tiles = false;
     h.ws = false;
@@ -2525,6 +2681,7 @@ int mgb_batch_set_slot(mgb_batch* b, int32_t slot, mgb_sim* sim, int64_t end_ste
   if (slot < 0 || slot >= b->max_slots) return fail(MGB_ERR_ARGUMENT, "slot out of range");
   if (end_step < 1) return fail(MGB_ERR_ARGUMENT, "a slot needs at least one step");
   if (sim->step.nsrc > 0 && words == nullptr) return fail(MGB_ERR_ARGUMENT, "the slot's sources need deposit words");
+  if (sim->has_cond) return fail(MGB_ERR_UNSUPPORTED, "a batched slot does not carry a conductivity");
   if (sim->desc.nmonitors > kSlotMonitors)
     return fail(MGB_ERR_UNSUPPORTED, "a batched slot holds at most " + std::to_string(kSlotMonitors) + " monitors");
   for (int m = 0; m < sim->desc.nmonitors; ++m) {
@@ -2750,6 +2907,7 @@ int mgb_adjoint_step(mgb_sim* adj, const mgb_adjoint* a, int64_t step, void* str
   if (adj == nullptr || a == nullptr || a->grad_inv == nullptr || a->d_after == nullptr)
     return fail(MGB_ERR_ARGUMENT, "null argument");
   if (adj->step.npoles != 0) return fail(MGB_ERR_UNSUPPORTED, "the adjoint step does not carry susceptibility poles");
+  if (adj->has_cond) return fail(MGB_ERR_UNSUPPORTED, "the adjoint step does not carry a conductivity");
   for (int q = 0; q < 3; ++q)
     if (a->mu_b[q] == nullptr || a->mu_d[q] == nullptr) return fail(MGB_ERR_ARGUMENT, "missing mu volume");
   const StepParams& p = adj->step;
@@ -2829,6 +2987,7 @@ int mgb_adjoint_segment(mgb_sim* fwd, mgb_sim* adj, const mgb_adjoint* a, int64_
     return fail(MGB_ERR_ARGUMENT, "null argument");
   if (nsteps < 1) return fail(MGB_ERR_ARGUMENT, "a segment has at least one step");
   if (monitor < 0 || monitor >= adj->desc.nmonitors) return fail(MGB_ERR_ARGUMENT, "no such monitor");
+  if (fwd->has_cond || adj->has_cond) return fail(MGB_ERR_UNSUPPORTED, "the adjoint step does not carry a conductivity");
   int rc = check_words(fwd, first_step, nsteps);
   if (rc != MGB_OK) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -3,9 +3,11 @@
 Mirrors ``meep_gpu/driver.py``'s ``FdtdDriver`` (constructor :810, ``set_epsilon``
 :1170, ``add_susceptibility`` :1531, ``setup_pml`` :2155, ``add_source`` :2567,
 ``add_dft_monitor`` :2783, ``add_flux_monitor`` :3001, ``step`` :3419, ``run`` :3667,
-``get_field`` :4056) for the configurations this engine steps: 3-D, real float32
+``get_field`` :4056, ``set_conductivity`` :1649, ``set_b_conductivity`` :1752,
+``set_absorber`` :1863) for the configurations this engine steps: 3-D, real float32
 fields, metallic or periodic (k = 0) boundaries, no mirror symmetry, isotropic or
-diagonal chi1inv, Lorentz/Drude poles, electric sources and DFT/flux monitors.
+diagonal chi1inv, Lorentz/Drude poles, D and B conductivity (material and
+``mp.Absorber``), electric sources and DFT/flux monitors.
 Anything else is refused by name when it is asked for, never approximated.
 
 The configuration freezes at the first step (as the reference's fast-path plan
@@ -23,6 +25,8 @@ from typing import Any, Callable, Dict, List, Mapping, Optional, Sequence, Tuple
 
 import numpy as np
 
+from . import conductivity as cond
+from .conductivity import AbsorberLayer
 from .dft import (DFTMonitor, FluxMonitor, absorbing_cells, automatic_decimation,
                   normalize_frequencies)
 from .dispersion import Susceptibility
@@ -87,6 +91,14 @@ class FdtdDriver:
         self._inv_eps: Optional[Tuple[np.ndarray, np.ndarray, np.ndarray]] = None
         self._poles: List[Tuple[Susceptibility, List[Optional[np.ndarray]]]] = []
         self._sources: List[Source] = []
+        # conductivity: the material's own sigma per side (component -> float32 volume or
+        # None), the absorber faces and their float64 ramp, and the installed sum
+        self._material_d_conductivity: Optional[Dict[str, Optional[np.ndarray]]] = None
+        self._material_b_conductivity: Optional[Dict[str, Optional[np.ndarray]]] = None
+        self._material_includes_absorber = False
+        self._absorber_layers: Tuple[AbsorberLayer, ...] = ()
+        self._absorber_sigma: Dict[str, np.ndarray] = {}
+        self._conductivity: Dict[str, Optional[np.ndarray]] = {}
         self._flux_monitors: List[FluxMonitor] = []
         self._dft_monitors: List[DFTMonitor] = []
         self._automatic: List[Any] = []
@@ -138,8 +150,93 @@ class FdtdDriver:
 
     def setup_pml(self, thickness_cells: Any, order: int = 2) -> PML:
         self._require_unfrozen("setup_pml")
-        self.pml = PML(self.grid, thickness_cells, order=order)
+        pml = PML(self.grid, thickness_cells, order=order)
+        if self.has_conductivity:
+            for source in self._sources:
+                self._require_source_clear_of_conductive_pml(source.center, source.size, pml.faces)
+        self.pml = pml
         return self.pml
+
+    # --- conductivity -----------------------------------------------------------------
+    @property
+    def has_conductivity(self) -> bool:
+        return any(v is not None for v in self._conductivity.values())
+
+    def set_conductivity(self, d_conductivity: Any, absorber_included: bool = False) -> None:
+        """MEEP's ``D_conductivity`` (driver.py:1649): a scalar, a grid-shaped or
+        (n+1)-padded volume, or a ``{'Dx': .., 'Dy': .., 'Dz': ..}`` mapping of those;
+        zero or None removes it. ``absorber_included`` says the volumes already carry the
+        absorber ramp, which is then not added a second time on the D side."""
+        self._require_unfrozen("set_conductivity")
+        per_component = self._conductivity_components(d_conductivity, cond.D_COMPONENTS, "D")
+        if any(v is not None for v in per_component.values()):
+            self._require_existing_sources_clear()
+        self._material_d_conductivity = (per_component if any(v is not None for v in per_component.values())
+                                         else None)
+        self._material_includes_absorber = bool(absorber_included)
+        self._install_conductivity()
+
+    def set_b_conductivity(self, b_conductivity: Any) -> None:
+        """MEEP's ``B_conductivity`` (driver.py:1752), the magnetic twin of
+        :meth:`set_conductivity`, with the B keys."""
+        self._require_unfrozen("set_b_conductivity")
+        per_component = self._conductivity_components(b_conductivity, cond.B_COMPONENTS, "B")
+        self._material_b_conductivity = (per_component if any(v is not None for v in per_component.values())
+                                         else None)
+        self._install_conductivity()
+
+    def set_absorber(self, layers: Any) -> None:
+        """``mp.Absorber`` faces (driver.py:1863): a sequence of :class:`AbsorberLayer`,
+        installed as a graded D and B conductivity added to the material's own; an empty
+        sequence removes it. The faces keep their boundary condition."""
+        self._require_unfrozen("set_absorber")
+        resolved = tuple(layers or ())
+        for layer in resolved:
+            if not isinstance(layer, AbsorberLayer):
+                raise TypeError(f"set_absorber takes AbsorberLayer instances, got {type(layer).__name__}")
+        self._absorber_layers = resolved
+        self._absorber_sigma = cond.absorber_conductivity(self.grid, resolved)
+        self._install_conductivity()
+
+    @property
+    def absorber_layers(self) -> Tuple[AbsorberLayer, ...]:
+        return self._absorber_layers
+
+    def conductivity_volumes(self) -> Dict[str, Optional[np.ndarray]]:
+        """The installed float32 sigma volume of each D and B component (None: lossless)."""
+        return {name: self._conductivity.get(name) for name in cond.CONDUCTIVITY_COMPONENTS}
+
+    def _conductivity_components(self, value: Any, components: Tuple[str, ...], side: str):
+        if isinstance(value, Mapping):
+            unknown = sorted(set(value) - set(components))
+            if unknown:
+                raise ValueError(f"{side} conductivity mapping carries {unknown}; the keys are the {side} "
+                                 f"components {list(components)}")
+            return {c: cond.coerce(value.get(c), self.grid.shape, side) for c in components}
+        shared = cond.coerce(value, self.grid.shape, side)
+        return {c: shared for c in components}
+
+    def _install_conductivity(self) -> None:
+        """Material sigma plus the absorber ramp per side (driver.py:1915)."""
+        ramp = self._absorber_sigma
+        electric_ramp = {} if (self._material_includes_absorber and self._material_d_conductivity) else ramp
+        installed = {}
+        installed.update(cond.compose(cond.D_COMPONENTS, self._material_d_conductivity, electric_ramp))
+        installed.update(cond.compose(cond.B_COMPONENTS, self._material_b_conductivity, ramp))
+        self._conductivity = installed
+
+    def _require_existing_sources_clear(self) -> None:
+        if self.pml is None:
+            return
+        for source in self._sources:
+            self._require_source_clear_of_conductive_pml(source.center, source.size, self.pml.faces)
+
+    def _require_source_clear_of_conductive_pml(self, center, size, faces) -> None:
+        """A source stays two cells inside every absorbing face when the installed
+        conductivity reaches into a PML (driver.py:2520)."""
+        if not cond.reaches_a_pml(self.grid, faces, self._conductivity):
+            return
+        cond.require_source_clear(self.grid, faces, center, size)
 
     def add_susceptibility(self, susceptibility: Susceptibility, sigma: Any) -> None:
         """One Lorentz/Drude term of ``eps_inf + sum_n sigma_n chi_n`` (scalar, volume or per component)."""
@@ -185,6 +282,8 @@ class FdtdDriver:
                         waveform, complex(spec.get("amplitude", 1.0)), spec.get("amp_func"))
         if complex(spec.get("amplitude", 1.0)).imag != 0.0:
             raise Unsupported("a complex source amplitude needs complex fields")
+        if self.pml is not None and self.has_conductivity:
+            self._require_source_clear_of_conductive_pml(source.center, source.size, self.pml.faces)
         self._sources.append(source)
         return source
 
@@ -272,7 +371,8 @@ class FdtdDriver:
                              list(self._flux_monitors) + list(self._dft_monitors), device=device,
                              stream=stream, launch_shape=self.launch_shape, kernels=self.kernels,
                              autotune=autotune,
-                             dft_accumulation=dft_accumulation or self.dft_accumulation)
+                             dft_accumulation=dft_accumulation or self.dft_accumulation,
+                             conductivity=self._conductivity)
         return self.engine
 
     @property

@@ -29,11 +29,12 @@ import numpy as np
 import torch
 
 from . import _lib
+from .conductivity import coefficients, keeps_mask, piece_line
 from .dft import COMPONENTS, FluxMonitor, _Monitor
 from .grid import Grid
 from .pml import (HALF, INTEGER, PML, aux_shape, constitutive_aux_key, curl_aux_key,
                   identity_tables, no_pml_records, slab_index)
-from .sources import Source, deposit_words
+from .sources import Source, deposit_scales, deposit_words
 
 FIELD_NAMES = ("E", "D", "H")
 # Source words are uploaded in windows of this many steps.
@@ -51,9 +52,9 @@ AUTOTUNE_CANDIDATES = ((0, 32, 4, 4), (0, 32, 8, 4), (0, 32, 4, 8), (0, 64, 2, 8
 _AUTOTUNE_CACHE: Dict[tuple, Tuple[int, int, int, int]] = {}
 
 
-def autotune_key(grid: Grid, pml: Optional[PML], npoles: int, ninv: int) -> tuple:
+def autotune_key(grid: Grid, pml: Optional[PML], npoles: int, ninv: int, lossy: bool = False) -> tuple:
     faces = pml.faces if (pml is not None and pml.is_active) else None
-    return (grid.shape, grid.boundaries, faces, npoles, ninv)
+    return (grid.shape, grid.boundaries, faces, npoles, ninv, lossy)
 
 
 def _ptr(t: Optional[torch.Tensor]) -> Optional[int]:
@@ -69,7 +70,8 @@ class Engine:
                  device: Optional[torch.device] = None, stream: Optional[torch.cuda.Stream] = None,
                  launch_shape: Optional[Tuple[int, int, int]] = None, autotune: bool = True,
                  kernels: Optional[Tuple[int, int, int, int]] = None,
-                 dft_accumulation: Optional[str] = None):
+                 dft_accumulation: Optional[str] = None,
+                 conductivity: Optional[Dict[str, Optional[np.ndarray]]] = None):
         if not torch.cuda.is_available():
             raise RuntimeError("meep_gpu_gb300 steps on a CUDA GPU and none is visible")
         self.lib = _lib.load()
@@ -127,6 +129,7 @@ class Engine:
             d.pml_active = 0
             self.records = no_pml_records(grid)
         self._setup_poles(poles)
+        self._setup_conductivity(conductivity)
         self._setup_sources()
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         d.status = self.status.data_ptr()
@@ -209,8 +212,50 @@ class Engine:
                 pole.p[q][1] = p1.data_ptr()
             self.pole_tensors.append(kept)
 
+    def _setup_conductivity(self, conductivity) -> None:
+        """D and B conductivity: condfac / condinv volumes per lossy component and,
+        under a PML, its conductive-stage history, the chunk of every stored row and the
+        mask of the chunks that keep the component's conductivity."""
+        self.conductivity = {k: v for k, v in (conductivity or {}).items() if v is not None}
+        self.cond_tensors: Dict[str, torch.Tensor] = {}
+        self.cond_history: Dict[str, torch.Tensor] = {}
+        self.cond_desc = None
+        if not self.conductivity:
+            return
+        grid, dev = self.grid, self.device
+        cd = _lib.MgbConductivity()
+        for name, sigma in self.conductivity.items():
+            side = 0 if name[0] == "B" else 1
+            q = "xyz".index(name[1])
+            fac, inv = coefficients(sigma, grid.dt)
+            self.cond_tensors[name + ".condfac"] = torch.from_numpy(fac).to(dev)
+            self.cond_tensors[name + ".condinv"] = torch.from_numpy(inv).to(dev)
+            cd.condfac[side][q] = self.cond_tensors[name + ".condfac"].data_ptr()
+            cd.condinv[side][q] = self.cond_tensors[name + ".condinv"].data_ptr()
+            if self.pml is not None:
+                history = torch.zeros(grid.shape, dtype=torch.float32, device=dev)
+                self.cond_history[name] = history
+                cd.fcond[side][q] = history.data_ptr()
+                cd.keeps[side][q] = keeps_mask(grid, self.pml.faces, sigma)
+        if self.pml is not None:
+            for lattice in (INTEGER, HALF):
+                for axis in range(3):
+                    line = piece_line(grid.shape[axis], self.pml.faces[axis], lattice, grid.axis_wraps(axis))
+                    t = torch.from_numpy(line).to(dev)
+                    self.cond_tensors[f"chunk_of.{lattice}.{axis}"] = t
+                    cd.chunk_of[lattice][axis] = t.data_ptr()
+        self.cond_desc = cd
+        self.desc.conductivity = ctypes.pointer(cd)
+
     def _setup_sources(self) -> None:
         d = self.desc
+        # a source on a lossy D component deposits current * dt * condinv at its cell
+        condinv = {}
+        for q, axis in enumerate("xyz"):
+            sigma = self.conductivity.get("D" + axis)
+            if sigma is not None:
+                condinv[q] = coefficients(sigma, self.grid.dt)[1]
+        self.src_scales = deposit_scales(self.sources, condinv)
         cells: List[int] = []
         comps: List[int] = []
         ny, nz = self.grid.ny, self.grid.nz
@@ -308,7 +353,7 @@ class Engine:
                 and first_step + steps <= self._words_first + self._words_steps):
             return
         count = max(steps, SOURCE_WINDOW)
-        host = deposit_words(self.sources, first_step, count, self.grid.dt)
+        host = deposit_words(self.sources, first_step, count, self.grid.dt, self.src_scales)
         # The previous table may still be read by queued kernels: keep it alive until
         # the stream has passed them.
         stream = self.stream if self.stream is not None else torch.cuda.current_stream(self.device)
@@ -359,12 +404,13 @@ class Engine:
         per configuration for the life of the process.
         """
         key = autotune_key(self.grid, self.pml, len(getattr(self, "pole_tensors", [])),
-                           len({t.data_ptr() for t in self.inv_eps}))
+                           len({t.data_ptr() for t in self.inv_eps}), bool(self.conductivity))
         if key in _AUTOTUNE_CACHE:
             self.select(_AUTOTUNE_CACHE[key])
             return self.choice
         scratch = Engine(self.grid, self.pml, [t.cpu().numpy() for t in self.inv_eps],
-                         self._pole_specs, [], [], device=self.device, autotune=False)
+                         self._pole_specs, [], [], device=self.device, autotune=False,
+                         conductivity=self.conductivity)
         stream = torch.cuda.current_stream(self.device)
         best = [None, None]
         best_ms = [float("inf"), float("inf")]
@@ -432,6 +478,13 @@ class Engine:
         for kept in getattr(self, "pole_tensors", []):
             for _, (s, p0, _p1) in kept.items():
                 e += 4 * int(p0.numel())
+        # a lossy component reads its condfac and condinv volumes (its conductive-stage
+        # history, touched on part of the dsig membership only, is left out: a lower bound)
+        for name in self.conductivity:
+            if name[0] == "B":
+                h += 2 * cells
+            else:
+                e += 2 * cells
         return {"h_half": word * h, "e_half": word * e}
 
     # status bits the kernels set: 1 a non-finite E was written; 2 a tile kernel's wait

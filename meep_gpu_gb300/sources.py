@@ -404,13 +404,16 @@ def current_sequence(waveform, dt: float, first: int, steps: int) -> np.ndarray:
     return table[first:first + steps]
 
 
-def deposit_words(sources: Sequence[Source], first_step: int, steps: int, dt: float) -> np.ndarray:
+def deposit_words(sources: Sequence[Source], first_step: int, steps: int, dt: float,
+                  scales: Optional[np.ndarray] = None) -> np.ndarray:
     """Float64 subtrahends ``A[step][point]`` for steps ``first_step .. first_step+steps-1``.
 
     ``A = ((amp_re*c_re) - (amp_im*c_im))*dt`` with each product and the difference
     rounded on its own (separate array operations), ``+0`` where the current is bitwise
     ``(+0, +0)``. Points are laid out source by source in table order, the order the
-    device deposits them.
+    device deposits them. ``scales`` (one float64 per point) multiplies each word last:
+    a lossy target component's ``condinv`` at the point (reference ``sources.py:1357``
+    ``_deposit``, MEEP's ``A = current * dt * cndinv[i]``).
     """
     count = sum(len(s.cells) for s in sources)
     out = np.zeros((steps, count), dtype=np.float64)
@@ -424,7 +427,23 @@ def deposit_words(sources: Sequence[Source], first_step: int, steps: int, dt: fl
             value[plus_zero] = 0.0
             out[:, column] = value
             column += 1
+    if scales is not None:
+        out *= np.asarray(scales, dtype=np.float64)[None, :]
     return out
+
+
+def deposit_scales(sources: Sequence[Source], condinv: Dict[int, np.ndarray]) -> Optional[np.ndarray]:
+    """Per deposit point, the float64 ``condinv`` word of its target component at its
+    cell (``condinv``: component index 0..2 -> float32 volume of the lossy D components),
+    or None when no point lands on a lossy component."""
+    if not any(source.comp_index in condinv for source in sources):
+        return None
+    scales = []
+    for source in sources:
+        volume = condinv.get(source.comp_index)
+        for (i, j, k) in source.cells:
+            scales.append(1.0 if volume is None else float(volume[i, j, k]))
+    return np.asarray(scales, dtype=np.float64)
 
 
 def deposit_words_scalar(sources: Sequence[Source], first_step: int, steps: int, dt: float) -> np.ndarray:

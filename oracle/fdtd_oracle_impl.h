@@ -20,6 +20,10 @@
  *                        and MEEP's start of H (separate_h_from_b :2789)
  *   source deposit       sources.py _deposit :1357 (double subtract, one rounding)
  *   update_P             dispersion.py PolarizationState.update :689
+ *   conductivity         stepping.py _apply_conductive_update :2828 (no PML) and
+ *                        _apply_conductive_pml_update :2844 (the four conductive forms
+ *                        on the dsig / dsigu memberships of the chunks that keep the
+ *                        component's conductivity, the lossless forms elsewhere)
  *   DFT accumulation     dft.py _phase_factors :316, _apply_yee_interpolation :352,
  *                        FluxMonitor.update :3031
  */
@@ -57,6 +61,13 @@ typedef struct SUF(oracle_state) {
   const long long* src_cell;
   const int* src_comp;
   int h_separated;
+  /* D and B conductivity, [side: 0 B, 1 D][component]; NULL for a lossless component.
+   * keeps: full volume, 1 where the cell's chunk keeps the component's conductivity;
+   * fcond: the conductive-stage history (PML runs). */
+  const REAL* condfac[2][3];
+  const REAL* condinv[2][3];
+  const unsigned char* keeps[2][3];
+  REAL* fcond[2][3];
 } SUF(oracle_state);
 
 static inline long long SUF(lin)(const SUF(oracle_state)* s, int i, int j, int k) {
@@ -93,6 +104,7 @@ static inline REAL SUF(down)(const SUF(oracle_state)* s, const REAL* f, int axis
 static void SUF(curl_family)(SUF(oracle_state)* s, REAL* const target[3], REAL* const src[3],
                              REAL* const fu[3], int backward) {
   const int lattice = backward ? 0 : 1;
+  const int side = backward ? 1 : 0; /* conductivity side: D steps backward, B forward */
   const int n[3] = {s->nx, s->ny, s->nz};
   for (int q = 0; q < 3; ++q) {
     const int a1 = (q + 1) % 3, a2 = (q + 2) % 3;
@@ -127,7 +139,56 @@ static void SUF(curl_family)(SUF(oracle_state)* s, REAL* const target[3], REAL* 
           const int at[3] = {i, j, k};
           const REAL curl = s->scratch[c];
           REAL f = target[q][c];
-          if (!s->pml) {
+          const REAL* cf = s->condfac[side][q];
+          const int lossy = cf != NULL && (!s->pml || s->keeps[side][q][c]);
+          if (lossy && !s->pml) {
+            REAL g = cf[c] * f;
+            g = g - curl;
+            f = g * s->condinv[side][q][c];
+          } else if (lossy) {
+            const REAL fac = cf[c], inv = s->condinv[side][q][c];
+            const int sg = s->member[lattice][a1][at[a1]];
+            const int su = s->member[lattice][a2][at[a2]];
+            const REAL kms = s->kms[lattice][a1][at[a1]], sinv = s->sinv[lattice][a1][at[a1]];
+            const REAL kms_u = s->kms[lattice][a2][at[a2]], sinv_u = s->sinv[lattice][a2][at[a2]];
+            if (sg) {
+              const REAL prev_g = s->fcond[side][q][c];
+              REAL g = fac * prev_g;
+              g = g - curl;
+              g = g * inv;
+              s->fcond[side][q][c] = g;
+              const REAL inc = g - prev_g;
+              if (su) {
+                const REAL prev = fu[q][c];
+                REAL next = kms * prev;
+                next = next + inc;
+                next = next * sinv;
+                fu[q][c] = next;
+                REAL h = kms_u * f;
+                h = h + next;
+                h = h - prev;
+                f = h * sinv_u;
+              } else {
+                REAL h = kms * f;
+                h = h + inc;
+                f = h * sinv;
+              }
+            } else if (su) {
+              const REAL prev = fu[q][c];
+              REAL next = fac * prev;
+              next = next - curl;
+              next = next * inv;
+              fu[q][c] = next;
+              REAL h = kms_u * f;
+              h = h + next;
+              h = h - prev;
+              f = h * sinv_u;
+            } else {
+              REAL h = fac * f;
+              h = h - curl;
+              f = h * inv;
+            }
+          } else if (!s->pml) {
             f = f - curl;
           } else {
             const REAL kms = s->kms[lattice][a1][at[a1]];

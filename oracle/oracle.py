@@ -66,7 +66,9 @@ def _state_type(real) -> type:
                     ("inv_eps", P * 3), ("scratch", P), ("drive", P * 3),
                     ("npoles", ctypes.c_int), ("poles", Pole * 4),
                     ("nsrc", ctypes.c_int), ("src_cell", P), ("src_comp", P),
-                    ("h_separated", ctypes.c_int)]
+                    ("h_separated", ctypes.c_int),
+                    ("condfac", (P * 3) * 2), ("condinv", (P * 3) * 2), ("keeps", (P * 3) * 2),
+                    ("fcond", (P * 3) * 2)]
     return State
 
 
@@ -104,13 +106,64 @@ class Problem:
     src_comps: np.ndarray          # int32
     words: Callable[[int, int], np.ndarray]
     monitors: List[MonitorSpec] = field(default_factory=list)
+    # float32 sigma volume per lossy D / B component ("Dx" .. "Bz"), and the PML faces in
+    # cells ((low, high) per axis) the one-rank chunks are cut by
+    conductivity: Dict[str, np.ndarray] = field(default_factory=dict)
+    faces: Tuple[Tuple[float, float], ...] = ((0.0, 0.0),) * 3
+
+
+YEE = {"Dx": (1, 0, 0), "Dy": (0, 1, 0), "Dz": (0, 0, 1),
+       "Bx": (0, 1, 1), "By": (1, 0, 1), "Bz": (1, 1, 0)}
+
+
+def keeps_volume(shape, metallic, faces, iyee, sigma: np.ndarray) -> np.ndarray:
+    """Per cell of one component lattice: does the one-rank chunk owning it keep a
+    conductivity array? (meep_gpu/chunk_map.py ``ChunkLayout.one_rank`` :384,
+    ``owner_volume`` :649, ``loop_rows`` :675, ``conductive_chunks`` :720.)
+
+    Per axis the chunk boxes are [0, 2s_lo], [2s_lo, 2n - 2s_hi], [2n - 2s_hi, 2n] in
+    doubled offsets (s = int(cells + 1.5) for a face with a layer). A chunk keeps the
+    array when any sample of its loop volume (doubled lo + shift .. hi + shift) is
+    nonzero; a cell belongs to the chunk whose box holds its doubled coordinate
+    (lo < p <= hi), a wall row that no chunk owns taking its nearest owned row's.
+    """
+    boxes, coords = [], []
+    for axis in range(3):
+        n = shape[axis]
+        low, high = faces[axis]
+        cut_lo = 2 * min(n, int(low + 1.5)) if low > 0 else 0
+        cut_hi = 2 * n - 2 * min(n, int(high + 1.5)) if high > 0 else 2 * n
+        edges = [(0, cut_lo), (cut_lo, cut_hi), (cut_hi, 2 * n)]
+        boxes.append([e for e in edges if e[0] < e[1]])
+        p = 2 * np.arange(n) + iyee[axis]
+        if not metallic[axis]:
+            p = np.where(p <= 0, p + 2 * n, p)
+        owned = (p > 0) & (p <= 2 * n)
+        owned_at = np.flatnonzero(owned)
+        for row in np.flatnonzero(~owned):
+            p[row] = p[owned_at[np.argmin(np.abs(owned_at - row))]]
+        coords.append(p)
+    out = np.zeros(shape, dtype=bool)
+    for bx in boxes[0]:
+        for by in boxes[1]:
+            for bz in boxes[2]:
+                rows = []
+                for axis, (lo, hi) in enumerate((bx, by, bz)):
+                    n = shape[axis]
+                    r = np.arange(lo // 2, hi // 2 + 1)
+                    rows.append(r % n if not metallic[axis] else np.clip(r, 0, n - 1))
+                if not np.any(sigma[np.ix_(*rows)] != 0):
+                    continue
+                sel = [(c > lo) & (c <= hi) for c, (lo, hi) in zip(coords, (bx, by, bz))]
+                out |= sel[0][:, None, None] & sel[1][None, :, None] & sel[2][None, None, :]
+    return out
 
 
 def problem_from_driver(driver) -> Problem:
     """The oracle's description of a configured ``meep_gpu_gb300.FdtdDriver`` (host data only)."""
     from meep_gpu_gb300.dft import FluxMonitor
     from meep_gpu_gb300.pml import identity_tables
-    from meep_gpu_gb300.sources import deposit_words
+    from meep_gpu_gb300.sources import deposit_scales, deposit_words
 
     driver.prepare()
     grid = driver.grid
@@ -145,13 +198,22 @@ def problem_from_driver(driver) -> Problem:
             omegas=m.omegas, scale=m.scale, decimation=m.decimation_factor,
             weights=m.weights.reshape(-1) if flux else None,
             measure=m.measure if flux else 1.0, weight=m.weight if flux else 1.0))
+    conductivity = {name: v for name, v in driver.conductivity_volumes().items() if v is not None}
+    # a deposit on a lossy D component is scaled by its condinv word (sources.py:1357)
+    condinv = {}
+    for q, axis in enumerate("xyz"):
+        sigma = conductivity.get("D" + axis)
+        if sigma is not None:
+            condinv[q] = (1.0 / (1.0 + (sigma.astype(np.float64) * grid.dt) * 0.5)).astype(np.float32)
+    scales = deposit_scales(sources, condinv)
     return Problem(shape=grid.shape, metallic=tuple(int(grid.is_metallic(a)) for a in range(3)),
                    dt=grid.dt, dx=grid.dx, pml=pml is not None, tables32=tables32,
                    tables64=tables64, member=member, inv_eps32=inv32, inv_eps64=inv64,
                    poles=poles, src_cells=np.array(cells, dtype=np.int64),
                    src_comps=np.array(comps, dtype=np.int32),
-                   words=lambda first, steps: deposit_words(sources, first, steps, grid.dt),
-                   monitors=monitors)
+                   words=lambda first, steps: deposit_words(sources, first, steps, grid.dt, scales),
+                   monitors=monitors, conductivity=conductivity,
+                   faces=tuple(pml.faces) if pml is not None else ((0.0, 0.0),) * 3)
 
 
 class Oracle:
@@ -215,6 +277,26 @@ class Oracle:
         s.src_cell = self._ptr(np.ascontiguousarray(problem.src_cells, dtype=np.int64))
         s.src_comp = self._ptr(np.ascontiguousarray(problem.src_comps, dtype=np.int32))
         s.h_separated = 0
+        self.fcond: Dict[str, np.ndarray] = {}
+        for name, sigma in problem.conductivity.items():
+            side = 0 if name[0] == "B" else 1
+            q = "xyz".index(name[1])
+            if precision == "f32":
+                values = np.ascontiguousarray(sigma, dtype=np.float32)
+                dt2 = np.float32(np.float32(problem.dt) * np.float32(0.5))
+                fac = (np.float32(1.0) - values * dt2).astype(np.float32)
+                inv = (1.0 / (1.0 + (values.astype(np.float64) * problem.dt) * 0.5)).astype(np.float32)
+            else:
+                wide = np.asarray(sigma, dtype=np.float64)
+                fac = 1.0 - wide * (problem.dt / 2.0)
+                inv = 1.0 / (1.0 + wide * (problem.dt / 2.0))
+            s.condfac[side][q] = self._ptr(np.ascontiguousarray(fac, dtype=dtype))
+            s.condinv[side][q] = self._ptr(np.ascontiguousarray(inv, dtype=dtype))
+            if problem.pml:
+                keeps = keeps_volume(shape, problem.metallic, problem.faces, YEE[name], sigma)
+                s.keeps[side][q] = self._ptr(np.ascontiguousarray(keeps, dtype=np.uint8))
+                self.fcond[name] = z()
+                s.fcond[side][q] = self.fcond[name].ctypes.data
         self.state = s
         self.step_count = 0
         self.accumulators: List[np.ndarray] = []

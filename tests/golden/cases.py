@@ -24,6 +24,18 @@ CASES = {
     "tile_periodic": dict(n=(10, 12, 16), pml=0, steps=40, boundaries="periodic"),
     "tile_mixed": dict(n=(11, 18, 68), pml={"x": 2, "y": {"low": 3, "high": 2}, "z": 4}, steps=40,
                        mixed=True),
+    # D and B conductivity under a PML: a D-lossy band |x| < 0.25 that runs through the y
+    # and z layers (the x-layer chunks keep no D conductivity; the others take all four
+    # conductive forms), a B-lossy block reaching one corner, the source two cells inside
+    # the layers.
+    "cond_pml": dict(n=(14, 12, 16), pml=3, steps=60, conductivity="band"),
+    # A lossy run without PML: a graded absorber on all six faces plus a uniform D
+    # conductivity (the two add).
+    "absorber": dict(n=(13, 12, 14), pml=0, steps=60, conductivity="absorber"),
+    # Periodic axes, PML on x only, a one-sided absorber on each z face (different
+    # thicknesses), per-component D conductivity and a Lorentz pole.
+    "absorber_pml_periodic": dict(n=(14, 12, 16), pml={"x": 3}, steps=50, boundaries="periodic",
+                                  conductivity="mixed", lorentz=True),
 }
 
 # The 80^3 sphere-under-PML workload (resolution 10, 10-cell PML, eps 4 sphere of radius
@@ -59,8 +71,12 @@ def build_case(driver_cls, susceptibility_cls, case: dict, reference: bool = Fal
     else:
         d.set_epsilon(np.where(x ** 2 + y ** 2 + z ** 2 < 0.35 ** 2, 4.0, 1.0).astype(np.float32))
         fcen, fwidth = 0.15, 0.1
+    lossy = case.get("conductivity")
+    if lossy:
+        _set_conductivity(d, case, x, y, z, lengths, reference)
+    source_x = -0.15 if lossy else -lengths[0] / 4
     d.add_source({"source_type": "gaussian", "component": "Ez",
-                  "center": (-lengths[0] / 4, 0.03, 0.0), "size": (0, 0, 0),
+                  "center": (source_x, 0.03, 0.0), "size": (0, 0, 0),
                   "frequency": fcen, "fwidth": fwidth})
     if case.get("mixed"):
         block = (np.abs(x - 0.2) < 0.15) & (np.abs(y) < 0.3)
@@ -82,3 +98,25 @@ def build_case(driver_cls, susceptibility_cls, case: dict, reference: bool = Fal
     flux.append(d.add_flux_monitor(fcen=fcen, df=fwidth / 2, nfreq=4, center=(lengths[0] / 4, 0, 0),
                                    size=(0, lengths[1] - 0.5, lengths[2] - 0.5), decimation_factor=0))
     return d, flux, dft
+
+
+def _set_conductivity(d, case: dict, x, y, z, lengths, reference: bool) -> None:
+    """The lossy cases' conductivity (through the same calls on either driver)."""
+    if reference:
+        from meep_gpu.absorber import AbsorberLayer
+    else:
+        from meep_gpu_gb300 import AbsorberLayer
+    kind = case["conductivity"]
+    if kind == "band":
+        d.set_conductivity(np.where(np.abs(x) < 0.25, 0.4, 0.0).astype(np.float32))
+        d.set_b_conductivity({"Bx": np.where((x > 0.2) & (y > 0.0), 0.3, 0.0).astype(np.float32),
+                              "Bz": np.where((x > 0.2) & (y > 0.0), 0.2, 0.0).astype(np.float32)})
+    elif kind == "absorber":
+        d.set_conductivity(0.05)
+        d.set_absorber([AbsorberLayer(0.3, axis, side) for axis in range(3) for side in ("low", "high")])
+    elif kind == "mixed":
+        d.set_conductivity({"Dx": np.where(np.abs(z) < 0.3, 0.25, 0.0).astype(np.float32),
+                            "Dz": np.where(y > 0.1, 0.15, 0.0).astype(np.float32)})
+        d.set_absorber([AbsorberLayer(0.25, 2, "low"), AbsorberLayer(0.35, 2, "high")])
+    else:
+        raise ValueError(f"unknown conductivity case {kind!r}")

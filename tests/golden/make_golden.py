@@ -10,7 +10,10 @@ beside the repository) and writes small fixtures into this directory:
 * ``digest_sphere80.json``: SHA-256 of every field component after 200 steps of the
   80^3 sphere-under-PML workload (the full-size configuration), plus its flux spectrum;
 * ``tables.npz``: PML coefficient vectors, source deposition tables, flux-plane
-  regions and weights and automatic decimation factors for a sweep of requests.
+  regions and weights and automatic decimation factors for a sweep of requests;
+* ``conductivity_tables.npz``: ``mp.Absorber`` sigma volumes, conductivity
+  coefficients (condfac / condinv) and, under a one-rank PML, the cells whose chunk
+  keeps a conductivity, for seeded configurations (``python make_golden.py conductivity``).
 
 The fixtures are committed; this script is how they were made. It is not run by the
 tests (the reference is not available where the GPU tests run).
@@ -129,6 +132,63 @@ def record_tables() -> None:
     print("tables written")
 
 
+# Conductivity host tables: absorber ramps, condfac / condinv, and the chunks that keep a
+# conductivity under a one-rank PML, each for a few seeded configurations.
+ABSORBER_GRIDS = [
+    {"cell": [1.4, 1.2, 1.6], "resolution": 10, "boundaries": "metallic",
+     "layers": [[0.3, axis, side] for axis in range(3) for side in ("low", "high")]},
+    {"cell": [1.3, 1.1, 1.5], "resolution": 13, "boundaries": "periodic",
+     "layers": [[0.35, 0, "low"], [0.25, 2, "high"]]},
+    {"cell": [2.0, 1.0, 1.0], "resolution": 10, "boundaries": "metallic", "layers": [[0.5, 0, "high"]]},
+]
+CHUNK_GRIDS = [
+    {"cell": [1.4, 1.2, 1.6], "boundaries": "metallic", "pml": 3},
+    {"cell": [1.4, 1.3, 1.2], "boundaries": "periodic", "pml": {"x": 3, "y": {"low": 2, "high": 4}, "z": 2.5}},
+    {"cell": [1.3, 1.5, 1.2], "boundaries": "metallic", "pml": {"x": 3, "z": 2}},
+]
+YEE_DB = {"Dx": (1, 0, 0), "Dy": (0, 1, 0), "Dz": (0, 0, 1), "Bx": (0, 1, 1), "By": (1, 0, 1), "Bz": (1, 1, 0)}
+
+
+def record_conductivity_tables() -> None:
+    from meep_gpu.absorber import AbsorberLayer, absorber_conductivity
+    from meep_gpu.chunk_map import ChunkLayout
+    from meep_gpu.grid import Grid
+    from meep_gpu.pml import PML
+
+    out = {}
+    for g, spec in enumerate(ABSORBER_GRIDS):
+        grid = Grid(cell_size=tuple(spec["cell"]), resolution=spec["resolution"], boundaries=spec["boundaries"])
+        volumes = absorber_conductivity(grid, [AbsorberLayer(t, a, side) for t, a, side in spec["layers"]])
+        for name, volume in volumes.items():
+            out[f"absorber{g}_{name}"] = np.asarray(volume, dtype=np.float64)
+    # condfac / condinv of sigma words that round differently in float32 and double
+    driver = FdtdDriver(cell_size=(1.0, 1.0, 1.0), resolution=10, force_complex_fields=False,
+                        boundaries="metallic", prefer_gpu=False)
+    rng = np.random.default_rng(11)
+    sigma = rng.choice(np.array([0.5, 0.3, 0.25, 0.1, 1.7, 3.0, 0.0], dtype=np.float32), driver.grid.shape)
+    sigma[0, 0, 0] = 0.5
+    driver.set_conductivity(sigma)
+    out["coef_sigma"] = sigma
+    out["coef_condfac"] = np.asarray(driver.fields.condfac_for("Dx"))
+    out["coef_condinv"] = np.asarray(driver.fields.condinv_for("Dx"))
+    for g, spec in enumerate(CHUNK_GRIDS):
+        grid = Grid(cell_size=tuple(spec["cell"]), resolution=10, boundaries=spec["boundaries"])
+        layout = ChunkLayout.one_rank(grid, PML(grid, spec["pml"]))
+        for t in range(12):
+            sig = np.zeros(grid.shape, np.float32)
+            lo = [int(rng.integers(0, n)) for n in grid.shape]
+            hi = [min(n, a + int(rng.integers(1, 4))) for a, n in zip(lo, grid.shape)]
+            sig[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]] = 0.3
+            out[f"chunks{g}_{t}_sigma"] = sig
+            for name, iyee in YEE_DB.items():
+                out[f"chunks{g}_{t}_{name}"] = np.packbits(layout.conductive_mask(sig, iyee).ravel())
+    np.savez_compressed(HERE / "conductivity_tables.npz", **out)
+    (HERE / "conductivity_tables.json").write_text(json.dumps(
+        {"absorber_grids": ABSORBER_GRIDS, "chunk_grids": CHUNK_GRIDS, "chunk_trials": 12,
+         "coef_dt": driver.grid.dt}, indent=1) + "\n")
+    print("conductivity tables written")
+
+
 if __name__ == "__main__":
     which = sys.argv[1:] or ["fields", "digest", "tables"]
     if "fields" in which or any(w in CASES for w in which):
@@ -139,3 +199,5 @@ if __name__ == "__main__":
         record_tables()
     if "digest" in which:
         record_digest()
+    if "conductivity" in which:
+        record_conductivity_tables()

@@ -71,11 +71,14 @@ int main(void) {
   printf("sizeof.mgb_monitor %zu\n", sizeof(mgb_monitor));
   printf("sizeof.mgb_pole %zu\n", sizeof(mgb_pole));
   printf("sizeof.mgb_aux %zu\n", sizeof(mgb_aux));
+  printf("sizeof.mgb_conductivity %zu\n", sizeof(mgb_conductivity));
   F(mgb_sim_desc, dtdx) F(mgb_sim_desc, kms) F(mgb_sim_desc, E) F(mgb_sim_desc, H) F(mgb_sim_desc, B)
   F(mgb_sim_desc, fuD) F(mgb_sim_desc, npoles) F(mgb_sim_desc, poles) F(mgb_sim_desc, nsrc)
   F(mgb_sim_desc, src_box) F(mgb_sim_desc, nmonitors) F(mgb_sim_desc, monitors)
   F(mgb_sim_desc, status) F(mgb_monitor, scale) F(mgb_monitor, omega) F(mgb_monitor, acc)
-  F(mgb_pole, sigma) F(mgb_pole, p)
+  F(mgb_pole, sigma) F(mgb_pole, p) F(mgb_sim_desc, conductivity)
+  F(mgb_conductivity, condinv) F(mgb_conductivity, fcond) F(mgb_conductivity, chunk_of)
+  F(mgb_conductivity, keeps)
   return 0;
 }
 """
@@ -90,7 +93,8 @@ def test_ctypes_layout_matches_the_header(tmp_path):
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
     layout = dict(line.split() for line in out.strip().splitlines())
     types = {"mgb_sim_desc": _lib.MgbSimDesc, "mgb_monitor": _lib.MgbMonitor,
-             "mgb_pole": _lib.MgbPole, "mgb_aux": _lib.MgbAux}
+             "mgb_pole": _lib.MgbPole, "mgb_aux": _lib.MgbAux,
+             "mgb_conductivity": _lib.MgbConductivity}
     for key, value in layout.items():
         kind, member = key.split(".")
         if kind == "sizeof":

@@ -55,6 +55,8 @@ def test_fields_are_the_reference_words(gpu, name, mode):
     case = CASES[name]
     gold = golden_io.fields(name)
     tileable = case["n"][2] % 4 == 0
+    if case.get("conductivity") and mode != "generic":
+        pytest.skip("a lossy run steps with the generic kernels only (the others are refused)")
     if mode in ("tiles", "ws") and not tileable:
         mode = "generic"
     driver, flux, dft = gpu_case(case, kernels=MODES[mode])

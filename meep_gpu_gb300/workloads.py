@@ -18,6 +18,17 @@ grid's cell centres, as the configurations specify; there is no dataset.
 * ``sphere128``: a 128^3 sphere case with one flux plane.
 * ``sphere192``: the 192^3 sphere case with one 50-frequency flux plane (working set
   ~0.4 GB, above the L2 size): the case detailed kernel profiles are taken on.
+* ``absorber192``: the ``sphere192`` case with ``mp.Absorber(1.0)`` on all six faces (a
+  graded D and B conductivity, 24 cells deep) in place of the PML, and a D conductivity
+  0.05 inside the sphere; 5000 steps.
+* ``lossy_pml192``: the ``sphere192`` case (10-cell PML) with a D conductivity 0.05 in
+  the sphere and a B conductivity 0.02 in the |x| < 3 slab, which runs through the y and
+  z layers (every conductive PML form is live); 5000 steps.
+* ``lossy40``: 40^3 at resolution 10: PML (6 cells) on x and y, an absorber on each z
+  face (0.6 and 0.5), an eps-3 sphere of radius 0.8, a D conductivity 0.35 in |y| < 0.7
+  (through the x layers), a B conductivity (0.2 on Bx for x > 0.5, 0.05 on Bz), a
+  Lorentz slab, an extended Ez source on a lossy component and a 20-frequency flux
+  plane; the case the lossy path's float64 error is quoted on (300 steps).
 * ``adjoint96`` (:func:`adjoint96`): 96^3 at resolution 10, 10-cell PML, a 16 x 64 x 64
   design box centred in the cell with eps ~ U[1, 12] (seed 0), Ez Gaussian (fcen 0.15,
   df 0.05) at x = -L/4, a 10-frequency x-normal flux plane 4 cells past the box;
@@ -28,9 +39,10 @@ from __future__ import annotations
 
 import numpy as np
 
-WORKLOADS = ("sphere80", "sphere192_8dft", "lorentz192", "sphere128", "sphere192")
+WORKLOADS = ("sphere80", "sphere192_8dft", "lorentz192", "sphere128", "sphere192", "absorber192",
+             "lossy_pml192", "lossy40")
 STEPS = {"sphere80": 2000, "sphere192_8dft": 5000, "lorentz192": 10000, "sphere128": 1000,
-         "sphere192": 5000}
+         "sphere192": 5000, "absorber192": 5000, "lossy_pml192": 5000, "lossy40": 300}
 
 
 def build(name: str, driver_cls=None, susceptibility_cls=None, **driver_kwargs):
@@ -69,6 +81,41 @@ def build(name: str, driver_cls=None, susceptibility_cls=None, **driver_kwargs):
                                          center=(sign * 1.6, 0.0, 0.0), size=(side, side, side),
                                          decimation_factor=0))
         return d, flux, dft
+    if name in ("absorber192", "lossy_pml192"):
+        from .conductivity import AbsorberLayer
+        d = driver_cls(cell_size=(8.0, 8.0, 8.0), resolution=24, courant=0.5,
+                       force_complex_fields=False, boundaries="metallic", **driver_kwargs)
+        x, y, z = d.grid.meshgrid()
+        sphere = x ** 2 + y ** 2 + z ** 2 < 2.0 ** 2
+        d.set_epsilon(np.where(sphere, 4.0, 1.0).astype(np.float32))
+        d.set_conductivity(np.where(sphere, 0.05, 0.0).astype(np.float32))
+        if name == "absorber192":
+            d.set_absorber([AbsorberLayer(1.0, axis, side) for axis in range(3) for side in ("low", "high")])
+        else:
+            d.setup_pml(10)
+            d.set_b_conductivity(np.where(np.abs(x) < 3.0, 0.02, 0.0).astype(np.float32))
+        d.add_source({"source_type": "gaussian", "component": "Ez", "center": (-2.0, 0.0, 0.0),
+                      "size": (0, 0, 0), "frequency": 0.15, "fwidth": 0.1})
+        flux = [d.add_flux_monitor(fcen=0.15, df=0.1, nfreq=50, center=(2.5, 0, 0), size=(0, 5, 5),
+                                   decimation_factor=0)]
+        return d, flux, []
+    if name == "lossy40":
+        from .conductivity import AbsorberLayer
+        d = driver_cls(cell_size=(4.0, 4.0, 4.0), resolution=10, courant=0.5,
+                       force_complex_fields=False, boundaries="metallic", **driver_kwargs)
+        d.setup_pml({"x": 6, "y": 6})
+        d.set_absorber([AbsorberLayer(0.6, 2, "low"), AbsorberLayer(0.5, 2, "high")])
+        x, y, z = d.grid.meshgrid()
+        d.set_epsilon(np.where(x * x + y * y + z * z < 0.8 ** 2, 3.0, 1.0))
+        d.set_conductivity(np.where(np.abs(y) < 0.7, 0.35, 0.0))
+        d.set_b_conductivity({"Bx": np.where(x > 0.5, 0.2, 0.0), "Bz": 0.05})
+        d.add_susceptibility(susceptibility_cls(frequency=1.1, gamma=0.05),
+                             np.where(np.abs(x + 0.8) < 0.2, 0.5, 0.0))
+        d.add_source({"source_type": "gaussian", "component": "Ez", "center": (-0.6, 0.1, 0.0),
+                      "size": (0, 0.6, 0.4), "frequency": 0.4, "fwidth": 0.3})
+        flux = [d.add_flux_monitor(fcen=0.4, df=0.3, nfreq=20, center=(0.9, 0, 0), size=(0, 2.0, 2.0),
+                                   decimation_factor=2)]
+        return d, flux, []
     if name == "lorentz192":
         res = 20
         length = 9.6

@@ -198,22 +198,12 @@ def test_a_conductivity_changes_the_fields():
 
 # --- GPU --------------------------------------------------------------------------------
 def lossy_big(kernels=None):
-    """A 40^3 lossy run: PML 6, an absorber on both z faces, a material D sigma band,
-    a B sigma block, a Lorentz slab, a lossy extended source and a flux plane."""
-    d = FdtdDriver((4.0, 4.0, 4.0), 10, force_complex_fields=False, boundaries="metallic", kernels=kernels)
-    d.setup_pml({"x": 6, "y": 6})
-    d.set_absorber([AbsorberLayer(0.6, 2, "low"), AbsorberLayer(0.5, 2, "high")])
-    x, y, z = d.grid.meshgrid()
-    d.set_epsilon(np.where(x * x + y * y + z * z < 0.8 ** 2, 3.0, 1.0))
-    d.set_conductivity(np.where(np.abs(y) < 0.7, 0.35, 0.0))
-    d.set_b_conductivity({"Bx": np.where(x > 0.5, 0.2, 0.0), "Bz": 0.05})
-    d.add_susceptibility(Susceptibility(frequency=1.1, gamma=0.05),
-                         np.where(np.abs(x + 0.8) < 0.2, 0.5, 0.0))
-    d.add_source({"source_type": "gaussian", "component": "Ez", "center": (-0.6, 0.1, 0.0),
-                  "size": (0, 0.6, 0.4), "frequency": 0.4, "fwidth": 0.3})
-    flux = d.add_flux_monitor(fcen=0.4, df=0.3, nfreq=20, center=(0.9, 0, 0), size=(0, 2.0, 2.0),
-                              decimation_factor=2)
-    return d, flux
+    """The 40^3 lossy workload (PML on x and y, absorber on z, D and B sigma, a pole, a
+    lossy extended source, a flux plane)."""
+    from meep_gpu_gb300 import workloads
+
+    d, flux, _ = workloads.build("lossy40", FdtdDriver, kernels=kernels)
+    return d, flux[0]
 
 
 @pytest.mark.gpu

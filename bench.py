@@ -111,7 +111,10 @@ def family_name(choice) -> str:
     family, bz, by, xc = choice
     if family == 1:
         return f"tiles 64x8, x chunk {xc}"
-    return f"{'prefetching ' if family == 2 else ''}generic {bz}x{by}, x chunk {xc}"
+    if family == 3:
+        return f"warp-specialized tiles 64x8, x chunk {xc}"
+    words = f"{'prefetching ' if family in (2, 5) else ''}generic {bz}x{by}, x chunk {xc}"
+    return words + (" prefetched into L2" if family in (4, 5) else "")
 
 
 def measured_peaks():

@@ -149,7 +149,7 @@ typedef struct mgb_sim_desc {
    * then stops stepping instead of spinning). */
   int32_t* status; /* device, may be NULL */
   /* D and B conductivity, NULL for a lossless run; the library keeps a copy. A run with
-   * a conductivity steps with the generic kernels (family 0) and is refused by the
+   * a conductivity steps with the generic kernels (family 0 or 4) and is refused by the
    * batch and the adjoint entry points. */
   const mgb_conductivity* conductivity;
 } mgb_sim_desc;
@@ -199,14 +199,18 @@ int mgb_uses_tiles(mgb_sim* sim);
 
 /* Choose the kernel family of both halves: 0 the generic kernels (plain loads), 1 the
  * tile kernels (TMA-staged shared-memory planes; needs a z extent that is a multiple of
- * 4), 2 the generic kernels with the next plane's loads issued ahead. All
- * compute the same words; the autotuner picks the faster for a grid. No reference
- * counterpart (the reference's dispatch arbiter picks among its own kernel tables,
- * meep_gpu/dispatch_preference.py). */
+ * 4), 2 the generic kernels with the next plane's loads issued ahead, 4 and 5 families 0
+ * and 2 with each thread's x chunk prefetched into L2 before it marches (3, the
+ * warp-specialized tile kernel, steps the E half only: see mgb_select_half). All
+ * compute the same words; the autotuner picks the faster for a grid. A run with a
+ * conductivity takes families 0 and 4 only. No reference counterpart (the reference's
+ * dispatch arbiter picks among its own kernel tables, meep_gpu/dispatch_preference.py). */
 int mgb_select_kernels(mgb_sim* sim, int32_t family);
 
 /* Choose the family and launch shape of one half alone (part 0 the H half, 1 the E
- * half): family 0 generic, 1 tiles, 2 generic with the next plane's loads issued ahead;
+ * half): family 0 generic, 1 tiles, 2 generic with the next plane's loads issued ahead,
+ * 3 warp-specialized tiles (E half), 4 / 5 families 0 / 2 with the x chunk prefetched
+ * into L2;
  * block_z x block_y cells per CTA (a multiple of 32, at most 256; the tile kernels'
  * block is fixed) and x_chunk planes per CTA. The halves are separate launches, so any
  * pair computes the same words. No reference counterpart. */

@@ -94,6 +94,7 @@ struct StepParams {
   int src_box[6];
   const double* src_words;  // row for the current step, [nsrc]
   int32_t* status;
+  int l2pf;  // 1: each thread prefetches its x chunk's field planes into L2 before marching
 };
 
 // Tensor maps of the tile kernels (each 64-byte aligned, passed as __grid_constant__).
@@ -126,6 +127,22 @@ __device__ __forceinline__ bool in_runs(const mgb_aux& a, int x) {
 }
 
 __device__ __forceinline__ float ldgf(const float* base, int at) { return __ldg(base + at); }
+
+__device__ __forceinline__ void l2_prefetch(const float* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// Prefetch into L2 the words of `count` planes (stride sx) from offset c of the first
+// `nvol` of NV volumes: the march's later loads then find them in L2. Lane-wise, so a
+// warp's 32 z cells make one line per volume and plane.
+template <int NV>
+__device__ __forceinline__ void prefetch_planes(const float* const (&vols)[NV], int nvol, int c, int sx, int count) {
+  for (int t = 0; t < count; ++t) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      if (v < nvol) l2_prefetch(vols[v] + c + t * sx);
+  }
+}
 
 // ---- per-cell updates ----------------------------------------------------------------
 //
@@ -559,6 +576,10 @@ __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i
   const int oz = ztop ? -(p.nz - 1) : 1;
   const int col = j * sy + k;
   int c = i0 * sx + col;
+  if (p.l2pf) {
+    const float* vols[6] = {Ex, Ey, Ez, p.H[0], p.H[1], p.H[2]};
+    prefetch_planes(vols, 6, c, sx, i1 - i0);
+  }
   HColumn hcol = {};
   int col_axes = 0;  // bit 1: the warp touches the y memberships, bit 2: the z ones
   if (PML) {
@@ -625,6 +646,10 @@ __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i
   const int km = k == 0 ? (p.met[2] ? -1 : p.nz - 1) : k - 1;
   const int col = j * sy + k;
   int c = i0 * sx + col;
+  if (p.l2pf) {
+    const float* vols[7] = {Hx, Hy, Hz, p.D[0], p.D[1], p.D[2], p.inv_eps[0]};
+    prefetch_planes(vols, p.inv_eps[1] == p.inv_eps[0] ? 7 : 6, c, sx, i1 - i0);
+  }
   EColumn ecol = {};
   int col_axes = 0;  // bit 1: the warp touches the y memberships, bit 2: the z ones
   if (PML) {
@@ -720,6 +745,10 @@ __device__ __forceinline__ void h_march_pf(const StepParams& p, int j, int k, in
   const int oz = ztop ? -(p.nz - 1) : 1;
   const int col = j * sy + k;
   int c = i0 * sx + col;
+  if (p.l2pf) {
+    const float* vols[6] = {p.E[0], p.E[1], p.E[2], p.H[0], p.H[1], p.H[2]};
+    prefetch_planes(vols, 6, c, sx, i1 - i0);
+  }
   HColumn hcol = {};
   int col_axes = 0;
   if (PML) {
@@ -807,6 +836,10 @@ __device__ __forceinline__ void e_march_pf(const StepParams& p, int j, int k, in
   const int km = k == 0 ? (p.met[2] ? -1 : p.nz - 1) : k - 1;
   const int col = j * sy + k;
   int c = i0 * sx + col;
+  if (p.l2pf) {
+    const float* vols[7] = {p.H[0], p.H[1], p.H[2], p.D[0], p.D[1], p.D[2], p.inv_eps[0]};
+    prefetch_planes(vols, p.inv_eps[1] == p.inv_eps[0] ? 7 : 6, c, sx, i1 - i0);
+  }
   EColumn ecol = {};
   int col_axes = 0;
   if (PML) {
@@ -1881,6 +1914,7 @@ struct mgb_sim {
     bool tiles = false;     // the tile kernels
     bool ws = false;        // the tile kernels' warp-specialized form (E half)
     bool prefetch = false;  // generic kernels: the prefetching marches
+    bool l2pf = false;      // generic kernels: each thread's x chunk prefetched into L2 first
     int block_z = 32, block_y = 4, xchunk = 4;  // generic kernels
     int tile_xchunk = 8;                        // tile kernels
   } half[2];
@@ -2159,6 +2193,7 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
   p.src_comp = d.src_comp;
   p.src_words = nullptr;
   p.status = d.status;
+  p.l2pf = 0;
   setup_tiles(sim);
   *out = sim;
   return MGB_OK;
@@ -2265,6 +2300,7 @@ int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s) {
     const dim3 block(hc.block_z, hc.block_y, 1);
     const int xc = hc.xchunk;
     const dim3 grid((p.nz + block.x - 1) / block.x, (p.ny + block.y - 1) / block.y, (p.nx + xc - 1) / xc);
+    p.l2pf = hc.l2pf ? 1 : 0;  // per half; the launch takes the parameters by value
     if (sim->has_cond) {
       if (part == 0) {
         if (pml) launch_step(sim, h_generic_cond<true>, grid, block, 0, s, p, sim->cond, (int)(n == 0), xc);
@@ -2421,12 +2457,13 @@ int mgb_uses_tiles(mgb_sim* sim) {
 
 namespace {
 int choose_family(mgb_sim* sim, mgb_sim::HalfChoice& h, int family, int part) {
-  if (sim->has_cond && family != 0)
-    return fail(MGB_ERR_UNSUPPORTED, "a run with a conductivity steps with the generic kernels (family 0)");
-  if (family == 0 || family == 2) {
+  if (sim->has_cond && family != 0 && family != 4)
+    return fail(MGB_ERR_UNSUPPORTED, "a run with a conductivity steps with the generic kernels (family 0 or 4)");
+  if (family == 0 || family == 2 || family == 4 || family == 5) {
     h.tiles = false;
     h.ws = false;
-    h.prefetch = family == 2;
+    h.prefetch = family == 2 || family == 5;
+    h.l2pf = family == 4 || family == 5;
     return MGB_OK;
   }
   if (family == 1 || family == 3) {
@@ -2435,10 +2472,12 @@ int choose_family(mgb_sim* sim, mgb_sim::HalfChoice& h, int family, int part) {
     h.tiles = true;
     h.ws = family == 3;
     h.prefetch = false;
+    h.l2pf = false;
     return MGB_OK;
   }
   return fail(MGB_ERR_ARGUMENT,
-              "kernel family is 0 (generic), 1 (tiles), 2 (generic, prefetching) or 3 (tiles, warp-specialized)");
+              "kernel family is 0 (generic), 1 (tiles), 2 (generic, prefetching), 3 (tiles, warp-specialized), "
+              "4 (generic, x chunk prefetched into L2) or 5 (prefetching, x chunk prefetched into L2)");
 }
 }  // namespace
 
@@ -2692,6 +2731,7 @@ int mgb_batch_set_slot(mgb_batch* b, int32_t slot, mgb_sim* sim, int64_t end_ste
   }
   b->params[slot] = sim->step;
   b->params[slot].src_words = nullptr;
+  b->params[slot].l2pf = 0;  // measured: no gain for the batch's mix of small grids
   SlotState st = {};
   st.end = end_step;
   st.words = words;

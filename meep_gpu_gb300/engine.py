@@ -43,12 +43,15 @@ SOURCE_WINDOW = 4096
 # Kernel choices the autotuner times: (family, block_z, block_y, x_chunk); family 1 is
 # the tile kernels (block shape fixed at 64 x 8, x_chunk used), family 0 the generic ones,
 # family 2 the generic ones with the next plane's loads issued ahead, family 3 the tile
-# kernels' warp-specialized form (E half only; the H half refuses it).
+# kernels' warp-specialized form (E half only; the H half refuses it), families 4 and 5
+# families 0 and 2 with each thread's x chunk prefetched into L2 before it marches.
 AUTOTUNE_CANDIDATES = ((0, 32, 4, 4), (0, 32, 8, 4), (0, 32, 4, 8), (0, 64, 2, 8),
                        (0, 16, 8, 4), (0, 16, 16, 4), (0, 16, 8, 2), (0, 16, 8, 8), (0, 32, 2, 4),
                        (1, 64, 8, 4), (1, 64, 8, 8),
                        (2, 32, 4, 4), (2, 32, 4, 8), (2, 32, 8, 4), (2, 64, 2, 4), (2, 16, 8, 4),
-                       (2, 32, 4, 2), (2, 32, 2, 4), (3, 64, 8, 4), (3, 64, 8, 8), (3, 64, 8, 16))
+                       (2, 32, 4, 2), (2, 32, 2, 4), (3, 64, 8, 4), (3, 64, 8, 8), (3, 64, 8, 16),
+                       (4, 32, 4, 4), (4, 16, 8, 4), (4, 32, 4, 8), (4, 32, 8, 4), (4, 32, 4, 2),
+                       (5, 32, 4, 4), (5, 16, 8, 4), (5, 32, 4, 8), (5, 32, 2, 8), (5, 32, 4, 2))
 _AUTOTUNE_CACHE: Dict[tuple, Tuple[int, int, int, int]] = {}
 
 

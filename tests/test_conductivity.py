@@ -207,7 +207,7 @@ def lossy_big(kernels=None):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kernels", [(0, 32, 4, 4), (0, 16, 8, 3), (0, 64, 2, 40)])
+@pytest.mark.parametrize("kernels", [(0, 32, 4, 4), (0, 16, 8, 3), (0, 64, 2, 40), (4, 32, 4, 4)])
 def test_lossy_run_is_the_float32_oracle(gpu, kernels):
     steps = 150
     d, flux = lossy_big(kernels)
@@ -263,11 +263,12 @@ def test_lossy_run_refuses_the_other_kernel_families(gpu):
     d, _ = lossy_big()
     engine = d.freeze(autotune=False)
     lib = engine.lib
-    for family, bz, by in ((1, 32, 8), (2, 32, 4), (3, 32, 8)):
+    for family, bz, by in ((1, 32, 8), (2, 32, 4), (3, 32, 8), (5, 32, 4)):
         for part in (0, 1):
             assert lib.mgb_select_half(engine.handle, part, family, bz, by, 4) == UNSUPPORTED
             assert "generic kernels" in _lib.last_error(lib)
     assert lib.mgb_select_half(engine.handle, 0, 0, 32, 4, 4) == 0
+    assert lib.mgb_select_half(engine.handle, 1, 4, 32, 4, 4) == 0
     d.close()
 
 
@@ -276,7 +277,7 @@ def test_lossy_autotune_picks_a_generic_shape(gpu):
     d, _ = lossy_big()
     engine = d.freeze()
     (h, e) = engine.choice
-    assert h[0] == 0 and e[0] == 0
+    assert h[0] in (0, 4) and e[0] in (0, 4)
     d.close()
 
 

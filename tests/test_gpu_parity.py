@@ -29,7 +29,9 @@ TILES = (1, 64, 8, 8)
 GENERIC = (0, 32, 8, 4)
 PREFETCH = (2, 32, 4, 4)
 WARP_SPECIALIZED = ((2, 16, 8, 4), (3, 64, 8, 8))  # H prefetching, E warp-specialized tiles
-MODES = {"tiles": TILES, "generic": GENERIC, "prefetch": PREFETCH, "ws": WARP_SPECIALIZED}
+L2_PREFETCH = ((4, 32, 4, 4), (5, 16, 8, 4))  # families 0 / 2 with the x chunk prefetched into L2
+MODES = {"tiles": TILES, "generic": GENERIC, "prefetch": PREFETCH, "ws": WARP_SPECIALIZED,
+         "l2": L2_PREFETCH}
 
 
 def gpu_case(case, steps=None, kernels=None, chunks=None):
@@ -51,15 +53,19 @@ def gpu_case(case, steps=None, kernels=None, chunks=None):
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_fields_are_the_reference_words(gpu, name, mode):
     """Every kernel family: the TMA tile kernels (z extent a multiple of 4), the generic
-    plain-load kernels and their prefetching form."""
+    plain-load kernels, their prefetching form, and both with the x chunk prefetched
+    into L2."""
     case = CASES[name]
     gold = golden_io.fields(name)
     tileable = case["n"][2] % 4 == 0
-    if case.get("conductivity") and mode != "generic":
+    if case.get("conductivity") and mode not in ("generic", "l2"):
         pytest.skip("a lossy run steps with the generic kernels only (the others are refused)")
     if mode in ("tiles", "ws") and not tileable:
         mode = "generic"
-    driver, flux, dft = gpu_case(case, kernels=MODES[mode])
+    kernels = MODES[mode]
+    if case.get("conductivity") and mode == "l2":
+        kernels = (4, 32, 4, 4)  # a lossy run takes families 0 and 4
+    driver, flux, dft = gpu_case(case, kernels=kernels)
     assert driver.engine.uses_tiles == (mode in ("tiles", "ws"))
     for c in FIELDS:
         got = driver.get_field(c, cell_centered=False)
@@ -88,7 +94,8 @@ def test_fields_are_the_reference_words(gpu, name, mode):
 @pytest.mark.parametrize("choice", [(0, 32, 8, 16), (0, 64, 4, 7), (0, 16, 16, 200), (0, 128, 2, 1),
                                     (0, 32, 4, 3), (1, 64, 8, 1), (1, 64, 8, 5), (1, 64, 8, 200),
                                     (2, 32, 8, 16), (2, 64, 4, 7), (2, 32, 4, 1), (2, 128, 2, 3),
-                                    (3, 64, 8, 1), (3, 64, 8, 5), (3, 64, 8, 200)])
+                                    (3, 64, 8, 1), (3, 64, 8, 5), (3, 64, 8, 200),
+                                    (4, 32, 8, 16), (4, 64, 4, 7), (5, 32, 4, 1), (5, 128, 2, 3)])
 def test_launch_shape_does_not_change_a_word(gpu, choice, name):
     """The x chunk (every family) and block shape (generic families) change no word."""
     case = CASES[name]

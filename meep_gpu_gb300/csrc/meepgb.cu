@@ -332,7 +332,7 @@ __device__ __forceinline__ bool h_needs_plane(int axes) { return axes != 0 && ax
 
 // One cell of the H half: masks, the variant for the warp's memberships, zero_metal_B.
 // `axes` bit 0/1/2: the warp touches the x/y/z memberships (0 on the fast path).
-template <bool PML, bool COND = false>
+template <bool PML, bool COND = false, int AX = -1>
 __device__ __forceinline__ void h_cell(const StepParams& p, const HColumn& col, const HPlane& pl,
                                        int axes, int first_step, int i, int j, int k, int c,
                                        float cx, float cy, float cz, const float h_old[3],
@@ -348,6 +348,9 @@ __device__ __forceinline__ void h_cell(const StepParams& p, const HColumn& col, 
     // forms test each membership per cell)
     if (PML) h_cell_v<true, true, true, true>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new, cp, i, j, k);
     else h_cell_v<false, false, false, true>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new, cp, i, j, k);
+  } else if (PML && AX >= 0) {
+    // the CTA's memberships are known: exactly the variant of its axes
+    h_cell_v<(AX & 1) != 0, (AX & 2) != 0, (AX & 4) != 0>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new);
   } else if (!PML || axes == 0) {
     h_cell_v<false, false, false>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new);
   } else {
@@ -415,6 +418,40 @@ __device__ __forceinline__ void e_aux_load(const StepParams& p, const EColumn& c
     a.u[q] = sf[q] ? p.fuD[q].data[c] : 0.f;
     a.fw[q] = sw[q] ? p.fwE[q].data[c] : 0.f;
     a.e[q] = sw[q] ? p.E[q][c] : 0.f;
+  }
+}
+
+// Prefetch into L2 the auxiliary words a thread's cells of planes [i0, i1) will read
+// (the PML counterpart of prefetch_planes), from the membership flags alone.
+__device__ __forceinline__ void h_aux_prefetch(const StepParams& p, const HColumn& col, int c, int i0, int i1,
+                                               int sx) {
+  for (int i = i0; i < i1; ++i, c += sx) {
+    const bool b[3] = {in_runs(p.B[0], i), col.b1, col.b2};
+    const bool f[3] = {col.f0, in_runs(p.fuB[1], i), col.f2};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      if (b[q]) {
+        l2_prefetch(p.B[q].data + c);
+        l2_prefetch(p.fwH[q].data + c);
+      }
+      if (f[q]) l2_prefetch(p.fuB[q].data + c);
+    }
+  }
+}
+
+__device__ __forceinline__ void e_aux_prefetch(const StepParams& p, const EColumn& col, int c, int i0, int i1,
+                                               int sx) {
+  for (int i = i0; i < i1; ++i, c += sx) {
+    const bool f[3] = {col.f0, in_runs(p.fuD[1], i), col.f2};
+    const bool w[3] = {in_runs(p.fwE[0], i), col.w1, col.w2};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      if (f[q]) l2_prefetch(p.fuD[q].data + c);
+      if (w[q]) {
+        l2_prefetch(p.fwE[q].data + c);
+        l2_prefetch(p.E[q] + c);
+      }
+    }
   }
 }
 
@@ -558,10 +595,19 @@ __device__ __forceinline__ bool cta_inner(const StepParams& p, int i0, int i1, i
          k0 >= p.inner[4] && k0 + bz <= p.inner[5];
 }
 
+// The axes (bit 0 x, 1 y, 2 z) along which a CTA's cells reach some membership: outside
+// the inner box's range on an axis some auxiliary's run may hold a cell; inside it none
+// does, so every coefficient of that axis is exactly 1 for the whole CTA.
+__device__ __forceinline__ int cta_axes(const StepParams& p, int i0, int i1, int j0, int by, int k0, int bz) {
+  return ((i0 >= p.inner[0] && i1 <= p.inner[1]) ? 0 : 1) |
+         ((j0 >= p.inner[2] && j0 + by <= p.inner[3]) ? 0 : 2) |
+         ((k0 >= p.inner[4] && k0 + bz <= p.inner[5]) ? 0 : 4);
+}
+
 // ------------------------------------------------------------------------------------
 // Generic kernels: plain loads, one thread per (y, z) column marching over x.
 // One thread's column (j, k) of the H half over planes [i0, i1).
-template <bool PML, bool COND = false>
+template <bool PML, bool COND = false, int AX = -1>
 __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i0, int i1,
                                         int first_step, const mgb_conductivity* cp = nullptr) {
   const int sx = p.ny * p.nz;
@@ -584,9 +630,12 @@ __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i
   int col_axes = 0;  // bit 1: the warp touches the y memberships, bit 2: the z ones
   if (PML) {
     hcol = h_column(p, j, k);
-    const unsigned lanes = __activemask();
-    col_axes = (__any_sync(lanes, hcol.f2 || hcol.b1) ? 2 : 0) |
-               (__any_sync(lanes, hcol.f0 || hcol.b2) ? 4 : 0);
+    if (AX < 0) {
+      const unsigned lanes = __activemask();
+      col_axes = (__any_sync(lanes, hcol.f2 || hcol.b1) ? 2 : 0) |
+                 (__any_sync(lanes, hcol.f0 || hcol.b2) ? 4 : 0);
+    }
+    if (p.l2pf) h_aux_prefetch(p, hcol, c, i0, i1, sx);
   }
   float ey = Ey[c];
   float ez = Ez[c];
@@ -595,7 +644,7 @@ __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i
     int axes = 0;
     if (PML) {
       pl = h_plane(p, i);
-      axes = COND ? 7 : col_axes | ((pl.f1 || pl.b0) ? 1 : 0);
+      axes = COND ? 7 : AX >= 0 ? AX : col_axes | ((pl.f1 || pl.b0) ? 1 : 0);
       if (h_needs_plane(axes)) h_plane_coefficients(p, i, pl);
     }
     const float ex = Ex[c];
@@ -622,7 +671,7 @@ __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i
     const float cy = dtdx * (((ex_zp - ex) + ez) - ez_xp);
     const float cz = dtdx * (((ey_xp - ey) + ex) - ex_yp);
     float h_new[3];
-    h_cell<PML, COND>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, h_old, ax, h_new, cp);
+    h_cell<PML, COND, AX>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, h_old, ax, h_new, cp);
     p.H[0][c] = h_new[0];
     p.H[1][c] = h_new[1];
     p.H[2][c] = h_new[2];
@@ -632,7 +681,7 @@ __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i
 }
 
 // One thread's column (j, k) of the E half over planes [i0, i1).
-template <bool PML, bool COND = false>
+template <bool PML, bool COND = false, int AX = -1>
 __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i0, int i1,
                                         int parity, const double* words,
                                         const mgb_conductivity* cp = nullptr) {
@@ -654,9 +703,12 @@ __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i
   int col_axes = 0;  // bit 1: the warp touches the y memberships, bit 2: the z ones
   if (PML) {
     ecol = e_column(p, j, k);
-    const unsigned lanes = __activemask();
-    col_axes = (__any_sync(lanes, ecol.f2 || ecol.w1) ? 2 : 0) |
-               (__any_sync(lanes, ecol.f0 || ecol.w2) ? 4 : 0);
+    if (AX < 0) {
+      const unsigned lanes = __activemask();
+      col_axes = (__any_sync(lanes, ecol.f2 || ecol.w1) ? 2 : 0) |
+                 (__any_sync(lanes, ecol.f0 || ecol.w2) ? 4 : 0);
+    }
+    if (p.l2pf) e_aux_prefetch(p, ecol, c, i0, i1, sx);
   }
   float hy_xm = 0.f, hz_xm = 0.f;
   {
@@ -672,7 +724,7 @@ __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i
     int axes = 0;
     if (PML) {
       pl = e_plane(p, i);
-      axes = COND ? 7 : col_axes | ((pl.f1 || pl.w0) ? 1 : 0);
+      axes = COND ? 7 : AX >= 0 ? AX : col_axes | ((pl.f1 || pl.w0) ? 1 : 0);
       if (axes & 1) e_plane_coefficients(p, i, pl);
     }
     const float hx = Hx[c], hy = Hy[c], hz = Hz[c];
@@ -756,6 +808,7 @@ __device__ __forceinline__ void h_march_pf(const StepParams& p, int j, int k, in
     const unsigned lanes = __activemask();
     col_axes = (__any_sync(lanes, hcol.f2 || hcol.b1) ? 2 : 0) |
                (__any_sync(lanes, hcol.f0 || hcol.b2) ? 4 : 0);
+    if (p.l2pf) h_aux_prefetch(p, hcol, c, i0, i1, sx);
   }
   float ey = p.E[1][c];
   float ez = p.E[2][c];
@@ -847,6 +900,7 @@ __device__ __forceinline__ void e_march_pf(const StepParams& p, int j, int k, in
     const unsigned lanes = __activemask();
     col_axes = (__any_sync(lanes, ecol.f2 || ecol.w1) ? 2 : 0) |
                (__any_sync(lanes, ecol.f0 || ecol.w2) ? 4 : 0);
+    if (p.l2pf) e_aux_prefetch(p, ecol, c, i0, i1, sx);
   }
   float hy_xm = 0.f, hz_xm = 0.f;
   {
@@ -924,10 +978,21 @@ __global__ void __launch_bounds__(256, 5) h_generic(const __grid_constant__ Step
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
   const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
-  if (PML && cta_inner(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x))
+  if (!PML) {
     h_march<false>(p, j, k, i0, i1, first_step);
-  else
-    h_march<PML>(p, j, k, i0, i1, first_step);
+    return;
+  }
+  // one march compiled for exactly the axes whose memberships the CTA reaches
+  switch (cta_axes(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x)) {
+    case 0: h_march<false>(p, j, k, i0, i1, first_step); break;
+    case 1: h_march<true, false, 1>(p, j, k, i0, i1, first_step); break;
+    case 2: h_march<true, false, 2>(p, j, k, i0, i1, first_step); break;
+    case 3: h_march<true, false, 3>(p, j, k, i0, i1, first_step); break;
+    case 4: h_march<true, false, 4>(p, j, k, i0, i1, first_step); break;
+    case 5: h_march<true, false, 5>(p, j, k, i0, i1, first_step); break;
+    case 6: h_march<true, false, 6>(p, j, k, i0, i1, first_step); break;
+    default: h_march<true, false, 7>(p, j, k, i0, i1, first_step); break;
+  }
 }
 
 template <bool PML>
@@ -937,10 +1002,22 @@ __global__ void __launch_bounds__(256, 5) e_generic(const __grid_constant__ Step
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
   const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
-  if (PML && cta_inner(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x))
+  if (!PML) {
     e_march<false>(p, j, k, i0, i1, parity, p.src_words);
-  else
-    e_march<PML>(p, j, k, i0, i1, parity, p.src_words);
+    return;
+  }
+  // one march compiled for exactly the axes whose memberships the CTA reaches
+  const double* w = p.src_words;
+  switch (cta_axes(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x)) {
+    case 0: e_march<false>(p, j, k, i0, i1, parity, w); break;
+    case 1: e_march<true, false, 1>(p, j, k, i0, i1, parity, w); break;
+    case 2: e_march<true, false, 2>(p, j, k, i0, i1, parity, w); break;
+    case 3: e_march<true, false, 3>(p, j, k, i0, i1, parity, w); break;
+    case 4: e_march<true, false, 4>(p, j, k, i0, i1, parity, w); break;
+    case 5: e_march<true, false, 5>(p, j, k, i0, i1, parity, w); break;
+    case 6: e_march<true, false, 6>(p, j, k, i0, i1, parity, w); break;
+    default: e_march<true, false, 7>(p, j, k, i0, i1, parity, w); break;
+  }
 }
 
 // Generic kernels of a lossy run (a D or B conductivity): the same column march with

@@ -344,9 +344,10 @@ __device__ __forceinline__ void h_cell(const StepParams& p, const HColumn& col, 
   // in its component's own-axis membership, so there H is B and clearing H_new after
   // the accumulation is the same word.
   if (COND) {
-    // a lossy run: every cell of a PML run takes the general variant (the conductive
+    // a lossy run: the variant of the CTA's axes, or the general one (the conductive
     // forms test each membership per cell)
-    if (PML) h_cell_v<true, true, true, true>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new, cp, i, j, k);
+    constexpr bool X = AX < 0 || (AX & 1), Y = AX < 0 || (AX & 2), Z = AX < 0 || (AX & 4);
+    if (PML) h_cell_v<X, Y, Z, true>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new, cp, i, j, k);
     else h_cell_v<false, false, false, true>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new, cp, i, j, k);
   } else if (PML && AX >= 0) {
     // the CTA's memberships are known: exactly the variant of its axes
@@ -554,15 +555,16 @@ __device__ __forceinline__ void e_cell_v(const StepParams& p, const EColumn& col
   if (bad && p.status != nullptr) atomicOr(p.status, 1);
 }
 
-template <bool PML, bool COND = false>
+template <bool PML, bool COND = false, int AX = -1>
 __device__ __forceinline__ void e_cell(const StepParams& p, const EColumn& col, const EPlane& pl,
                                        int axes, int parity, int i, int j, int k, int c, float cx,
                                        float cy, float cz, float d[3], const float inv[3],
                                        const double* words, const EAux& a,
                                        const mgb_conductivity* cp = nullptr) {
   if (COND) {
-    // a lossy run: every cell of a PML run takes the general variant
-    if (PML) e_cell_v<true, true, true, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words, a, cp);
+    // a lossy run: the variant of the CTA's axes, or the general one
+    constexpr bool X = AX < 0 || (AX & 1), Y = AX < 0 || (AX & 2), Z = AX < 0 || (AX & 4);
+    if (PML) e_cell_v<X, Y, Z, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words, a, cp);
     else e_cell_v<false, false, false, true>(p, col, pl, parity, i, j, k, c, cx, cy, cz, d, inv, words, a, cp);
     return;
   }
@@ -604,6 +606,19 @@ __device__ __forceinline__ int cta_axes(const StepParams& p, int i0, int i1, int
          ((k0 >= p.inner[4] && k0 + bz <= p.inner[5]) ? 0 : 4);
 }
 
+// Dispatch a march on the CTA's axes: MARCH(AXV, PMLV) expands to one call.
+#define MGB_AXES_SWITCH(AXES, MARCH)           \
+  switch (AXES) {                              \
+    case 0: MARCH(-1, false); break;           \
+    case 1: MARCH(1, true); break;             \
+    case 2: MARCH(2, true); break;             \
+    case 3: MARCH(3, true); break;             \
+    case 4: MARCH(4, true); break;             \
+    case 5: MARCH(5, true); break;             \
+    case 6: MARCH(6, true); break;             \
+    default: MARCH(7, true); break;            \
+  }
+
 // ------------------------------------------------------------------------------------
 // Generic kernels: plain loads, one thread per (y, z) column marching over x.
 // One thread's column (j, k) of the H half over planes [i0, i1).
@@ -644,7 +659,7 @@ __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i
     int axes = 0;
     if (PML) {
       pl = h_plane(p, i);
-      axes = COND ? 7 : AX >= 0 ? AX : col_axes | ((pl.f1 || pl.b0) ? 1 : 0);
+      axes = AX >= 0 ? AX : COND ? 7 : col_axes | ((pl.f1 || pl.b0) ? 1 : 0);
       if (h_needs_plane(axes)) h_plane_coefficients(p, i, pl);
     }
     const float ex = Ex[c];
@@ -724,7 +739,7 @@ __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i
     int axes = 0;
     if (PML) {
       pl = e_plane(p, i);
-      axes = COND ? 7 : AX >= 0 ? AX : col_axes | ((pl.f1 || pl.w0) ? 1 : 0);
+      axes = AX >= 0 ? AX : COND ? 7 : col_axes | ((pl.f1 || pl.w0) ? 1 : 0);
       if (axes & 1) e_plane_coefficients(p, i, pl);
     }
     const float hx = Hx[c], hy = Hy[c], hz = Hz[c];
@@ -746,7 +761,7 @@ __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i
     const float cx = dtdx * (((hz_ym - hz) + hy) - hy_zm);
     const float cy = dtdx * (((hx_zm - hx) + hz) - hz_xm);
     const float cz = dtdx * (((hy_xm - hy) + hx) - hx_ym);
-    e_cell<PML, COND>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, d, inv, words, ax, cp);
+    e_cell<PML, COND, AX>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, d, inv, words, ax, cp);
     hy_xm = hy;
     hz_xm = hz;
   }
@@ -785,7 +800,7 @@ __device__ __forceinline__ void h_loads(const StepParams& p, HLoads& L, int i, i
   L.h[2] = p.H[2][c];
 }
 
-template <bool PML>
+template <bool PML, int AX = -1>
 __device__ __forceinline__ void h_march_pf(const StepParams& p, int j, int k, int i0, int i1,
                                            int first_step) {
   const int sx = p.ny * p.nz;
@@ -805,9 +820,11 @@ __device__ __forceinline__ void h_march_pf(const StepParams& p, int j, int k, in
   int col_axes = 0;
   if (PML) {
     hcol = h_column(p, j, k);
-    const unsigned lanes = __activemask();
-    col_axes = (__any_sync(lanes, hcol.f2 || hcol.b1) ? 2 : 0) |
-               (__any_sync(lanes, hcol.f0 || hcol.b2) ? 4 : 0);
+    if (AX < 0) {
+      const unsigned lanes = __activemask();
+      col_axes = (__any_sync(lanes, hcol.f2 || hcol.b1) ? 2 : 0) |
+                 (__any_sync(lanes, hcol.f0 || hcol.b2) ? 4 : 0);
+    }
     if (p.l2pf) h_aux_prefetch(p, hcol, c, i0, i1, sx);
   }
   float ey = p.E[1][c];
@@ -831,7 +848,7 @@ __device__ __forceinline__ void h_march_pf(const StepParams& p, int j, int k, in
     int axes = 0;
     if (PML) {
       pl = h_plane(p, i);
-      axes = col_axes | ((pl.f1 || pl.b0) ? 1 : 0);
+      axes = AX >= 0 ? AX : col_axes | ((pl.f1 || pl.b0) ? 1 : 0);
       if (h_needs_plane(axes)) h_plane_coefficients(p, i, pl);
     }
     HAux ax = {};
@@ -840,7 +857,7 @@ __device__ __forceinline__ void h_march_pf(const StepParams& p, int j, int k, in
     const float cy = dtdx * (((cur.ex_zp - cur.ex) + ez) - cur.ez_xp);
     const float cz = dtdx * (((cur.ey_xp - ey) + cur.ex) - cur.ex_yp);
     float h_new[3];
-    h_cell<PML>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, cur.h, ax, h_new);
+    h_cell<PML, false, AX>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, cur.h, ax, h_new);
     p.H[0][c] = h_new[0];
     p.H[1][c] = h_new[1];
     p.H[2][c] = h_new[2];
@@ -879,7 +896,7 @@ __device__ __forceinline__ void e_loads(const StepParams& p, ELoads& L, int i, i
   L.inv[2] = __ldg(p.inv_eps[2] + c);
 }
 
-template <bool PML>
+template <bool PML, int AX = -1>
 __device__ __forceinline__ void e_march_pf(const StepParams& p, int j, int k, int i0, int i1,
                                            int parity, const double* words) {
   const int sx = p.ny * p.nz;
@@ -897,9 +914,11 @@ __device__ __forceinline__ void e_march_pf(const StepParams& p, int j, int k, in
   int col_axes = 0;
   if (PML) {
     ecol = e_column(p, j, k);
-    const unsigned lanes = __activemask();
-    col_axes = (__any_sync(lanes, ecol.f2 || ecol.w1) ? 2 : 0) |
-               (__any_sync(lanes, ecol.f0 || ecol.w2) ? 4 : 0);
+    if (AX < 0) {
+      const unsigned lanes = __activemask();
+      col_axes = (__any_sync(lanes, ecol.f2 || ecol.w1) ? 2 : 0) |
+                 (__any_sync(lanes, ecol.f0 || ecol.w2) ? 4 : 0);
+    }
     if (p.l2pf) e_aux_prefetch(p, ecol, c, i0, i1, sx);
   }
   float hy_xm = 0.f, hz_xm = 0.f;
@@ -929,7 +948,7 @@ __device__ __forceinline__ void e_march_pf(const StepParams& p, int j, int k, in
     int axes = 0;
     if (PML) {
       pl = e_plane(p, i);
-      axes = col_axes | ((pl.f1 || pl.w0) ? 1 : 0);
+      axes = AX >= 0 ? AX : col_axes | ((pl.f1 || pl.w0) ? 1 : 0);
       if (axes & 1) e_plane_coefficients(p, i, pl);
     }
     EAux ax = {};
@@ -937,7 +956,7 @@ __device__ __forceinline__ void e_march_pf(const StepParams& p, int j, int k, in
     const float cx = dtdx * (((cur.hz_ym - cur.hz) + cur.hy) - cur.hy_zm);
     const float cy = dtdx * (((cur.hx_zm - cur.hx) + cur.hz) - hz_xm);
     const float cz = dtdx * (((hy_xm - cur.hy) + cur.hx) - cur.hx_ym);
-    e_cell<PML>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, cur.d, cur.inv, words, ax);
+    e_cell<PML, false, AX>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, cur.d, cur.inv, words, ax);
     hy_xm = cur.hy;
     hz_xm = cur.hz;
     cur = nxt;
@@ -951,10 +970,14 @@ __global__ void __launch_bounds__(256, 4) h_generic_pf(const __grid_constant__ S
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
   const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
-  if (PML && cta_inner(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x))
+  if (!PML) {
     h_march_pf<false>(p, j, k, i0, i1, first_step);
-  else
-    h_march_pf<PML>(p, j, k, i0, i1, first_step);
+    return;
+  }
+#define MGB_MARCH(AXV, PMLV) h_march_pf<PMLV, AXV>(p, j, k, i0, i1, first_step)
+  MGB_AXES_SWITCH(cta_axes(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x),
+                  MGB_MARCH)
+#undef MGB_MARCH
 }
 
 template <bool PML>
@@ -964,10 +987,14 @@ __global__ void __launch_bounds__(256, 4) e_generic_pf(const __grid_constant__ S
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
   const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
-  if (PML && cta_inner(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x))
+  if (!PML) {
     e_march_pf<false>(p, j, k, i0, i1, parity, p.src_words);
-  else
-    e_march_pf<PML>(p, j, k, i0, i1, parity, p.src_words);
+    return;
+  }
+#define MGB_MARCH(AXV, PMLV) e_march_pf<PMLV, AXV>(p, j, k, i0, i1, parity, p.src_words)
+  MGB_AXES_SWITCH(cta_axes(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x),
+                  MGB_MARCH)
+#undef MGB_MARCH
 }
 
 // Generic kernels: plain loads, one thread per (y, z) column marching over an x chunk.
@@ -983,16 +1010,10 @@ __global__ void __launch_bounds__(256, 5) h_generic(const __grid_constant__ Step
     return;
   }
   // one march compiled for exactly the axes whose memberships the CTA reaches
-  switch (cta_axes(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x)) {
-    case 0: h_march<false>(p, j, k, i0, i1, first_step); break;
-    case 1: h_march<true, false, 1>(p, j, k, i0, i1, first_step); break;
-    case 2: h_march<true, false, 2>(p, j, k, i0, i1, first_step); break;
-    case 3: h_march<true, false, 3>(p, j, k, i0, i1, first_step); break;
-    case 4: h_march<true, false, 4>(p, j, k, i0, i1, first_step); break;
-    case 5: h_march<true, false, 5>(p, j, k, i0, i1, first_step); break;
-    case 6: h_march<true, false, 6>(p, j, k, i0, i1, first_step); break;
-    default: h_march<true, false, 7>(p, j, k, i0, i1, first_step); break;
-  }
+#define MGB_MARCH(AXV, PMLV) h_march<PMLV, false, AXV>(p, j, k, i0, i1, first_step)
+  MGB_AXES_SWITCH(cta_axes(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x),
+                  MGB_MARCH)
+#undef MGB_MARCH
 }
 
 template <bool PML>
@@ -1007,17 +1028,10 @@ __global__ void __launch_bounds__(256, 5) e_generic(const __grid_constant__ Step
     return;
   }
   // one march compiled for exactly the axes whose memberships the CTA reaches
-  const double* w = p.src_words;
-  switch (cta_axes(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x)) {
-    case 0: e_march<false>(p, j, k, i0, i1, parity, w); break;
-    case 1: e_march<true, false, 1>(p, j, k, i0, i1, parity, w); break;
-    case 2: e_march<true, false, 2>(p, j, k, i0, i1, parity, w); break;
-    case 3: e_march<true, false, 3>(p, j, k, i0, i1, parity, w); break;
-    case 4: e_march<true, false, 4>(p, j, k, i0, i1, parity, w); break;
-    case 5: e_march<true, false, 5>(p, j, k, i0, i1, parity, w); break;
-    case 6: e_march<true, false, 6>(p, j, k, i0, i1, parity, w); break;
-    default: e_march<true, false, 7>(p, j, k, i0, i1, parity, w); break;
-  }
+#define MGB_MARCH(AXV, PMLV) e_march<PMLV, false, AXV>(p, j, k, i0, i1, parity, p.src_words)
+  MGB_AXES_SWITCH(cta_axes(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x),
+                  MGB_MARCH)
+#undef MGB_MARCH
 }
 
 // Generic kernels of a lossy run (a D or B conductivity): the same column march with
@@ -1031,10 +1045,14 @@ __global__ void __launch_bounds__(256) h_generic_cond(const __grid_constant__ St
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
   const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
-  if (PML && cta_inner(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x))
+  if (!PML) {
     h_march<false, true>(p, j, k, i0, i1, first_step, &cp);
-  else
-    h_march<PML, true>(p, j, k, i0, i1, first_step, &cp);
+    return;
+  }
+#define MGB_MARCH(AXV, PMLV) h_march<PMLV, true, AXV>(p, j, k, i0, i1, first_step, &cp)
+  MGB_AXES_SWITCH(cta_axes(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x),
+                  MGB_MARCH)
+#undef MGB_MARCH
 }
 
 template <bool PML>
@@ -1045,10 +1063,14 @@ __global__ void __launch_bounds__(256) e_generic_cond(const __grid_constant__ St
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
   const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
-  if (PML && cta_inner(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x))
+  if (!PML) {
     e_march<false, true>(p, j, k, i0, i1, parity, p.src_words, &cp);
-  else
-    e_march<PML, true>(p, j, k, i0, i1, parity, p.src_words, &cp);
+    return;
+  }
+#define MGB_MARCH(AXV, PMLV) e_march<PMLV, true, AXV>(p, j, k, i0, i1, parity, p.src_words, &cp)
+  MGB_AXES_SWITCH(cta_axes(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x),
+                  MGB_MARCH)
+#undef MGB_MARCH
 }
 
 // ------------------------------------------------------------------------------------
@@ -1688,15 +1710,19 @@ __global__ void __launch_bounds__(256, 4) step_batched(const __grid_constant__ B
   if (k >= sp.nz || j >= sp.ny) return;
   const int i0 = w.w * tb.xchunk;
   const int i1 = min(i0 + tb.xchunk, sp.nx);
-  const bool pml = sp.pml && !cta_inner(sp, i0, i1, w.z * (int)blockDim.y, (int)blockDim.y,
-                                        w.y * (int)blockDim.x, (int)blockDim.x);
+  const int axes = sp.pml ? cta_axes(sp, i0, i1, w.z * (int)blockDim.y, (int)blockDim.y,
+                                      w.y * (int)blockDim.x, (int)blockDim.x) : 0;
   if (PART == 0) {
-    if (pml) h_march_pf<true>(sp, j, k, i0, i1, n == 0);
-    else h_march_pf<false>(sp, j, k, i0, i1, n == 0);
+    const int first = n == 0;
+#define MGB_MARCH(AXV, PMLV) h_march_pf<PMLV, AXV>(sp, j, k, i0, i1, first)
+    MGB_AXES_SWITCH(axes, MGB_MARCH)
+#undef MGB_MARCH
   } else {
     const double* words = st.words + n * sp.nsrc;
-    if (pml) e_march_pf<true>(sp, j, k, i0, i1, (int)(n & 1), words);
-    else e_march_pf<false>(sp, j, k, i0, i1, (int)(n & 1), words);
+    const int parity = (int)(n & 1);
+#define MGB_MARCH(AXV, PMLV) e_march_pf<PMLV, AXV>(sp, j, k, i0, i1, parity, words)
+    MGB_AXES_SWITCH(axes, MGB_MARCH)
+#undef MGB_MARCH
   }
 }
 

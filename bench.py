@@ -55,8 +55,9 @@ def parse_args():
     p.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     p.add_argument("--workload", default="sphere192_8dft")
     p.add_argument("--kernels", default=None,
-                   help="family,block_z,block_y,x_chunk (family 1: TMA tiles, 0: generic); "
-                        "default: the autotuner's choice")
+                   help="family,block_z,block_y,x_chunk for both halves, or eight numbers (H half, "
+                        "then E half); families 0/2/4/5 generic, 1/3 TMA tiles; default: the "
+                        "autotuner's choice")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-validate", action="store_true")
@@ -259,7 +260,11 @@ def main():
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     device = torch.device("cuda", local)
-    kernels = tuple(int(v) for v in args.kernels.split(",")) if args.kernels else None
+    kernels = None
+    if args.kernels:
+        values = tuple(int(v) for v in args.kernels.split(","))
+        # four numbers: one choice for both halves; eight: the H half's, then the E half's
+        kernels = values if len(values) == 4 else (values[:4], values[4:])
 
     def barrier():
         if world > 1:

@@ -136,11 +136,13 @@ typedef struct mgb_sim_desc {
   int32_t npoles;
   int32_t pbox[6];
   mgb_pole poles[MGB_MAX_POLES];
-  /* electric sources: nsrc points in deposit order */
+  /* sources: nsrc points in deposit order, the electric ones (components 0..2, into D
+   * in the E half) first and then the last nsrc_magnetic magnetic ones (components
+   * 3..5, into B in the H half, MEEP's step_source(B) after step_B) */
   int32_t nsrc;
   const int64_t* src_cell; /* device, linear index into the component volume */
-  const int32_t* src_comp; /* device, 0..2 */
-  int32_t src_box[6];      /* bounding box of the points, half-open */
+  const int32_t* src_comp; /* device, 0..2 (Dx..Dz) or 3..5 (Bx..Bz) */
+  int32_t src_box[6];      /* bounding box of the electric points, half-open */
   /* monitors */
   int32_t nmonitors;
   mgb_monitor monitors[MGB_MAX_MONITORS];
@@ -152,6 +154,10 @@ typedef struct mgb_sim_desc {
    * a conductivity steps with the generic kernels (family 0 or 4) and is refused by the
    * batch and the adjoint entry points. */
   const mgb_conductivity* conductivity;
+  /* magnetic source points: the last nsrc_magnetic of the nsrc, and their bounding box
+   * (half-open). A run with magnetic sources is refused by the batch. */
+  int32_t nsrc_magnetic;
+  int32_t src_box_magnetic[6];
 } mgb_sim_desc;
 
 typedef struct mgb_sim mgb_sim;
@@ -172,7 +178,9 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out);
 int mgb_set_launch_shape(mgb_sim* sim, int block_z, int block_y, int x_chunk);
 
 /* Install the float64 source-deposit words for steps [first_step, first_step+steps):
- * words is a device array [steps][nsrc]; borrowed until replaced. */
+ * words is a device array [steps][nsrc]; borrowed until replaced. Row n holds each
+ * electric point's A = real(amp * J(n dt + dt/2)) * dt and each magnetic point's
+ * real(amp * J(n dt)) * dt (times its lossy component's condinv). */
 int mgb_set_source_words(mgb_sim* sim, const double* words, int64_t first_step, int64_t steps);
 
 /* Advance steps first_step .. first_step+nsteps-1 on `stream` (a cudaStream_t; NULL is

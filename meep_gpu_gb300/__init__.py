@@ -6,12 +6,13 @@ step in ``libmeepgb.so`` (C ABI: ``include/meepgb.h``). There is no CPU stepping
 """
 
 from .conductivity import AbsorberLayer
-from .dft import DFTMonitor, FluxMonitor
+from .dft import DFTMonitor, FluxDftData, FluxMonitor, FluxPlaneDft
 from .dispersion import DRUDE, LORENTZ, Susceptibility
 from .driver import FdtdCancelled, FdtdDivergence, FdtdDriver
 from .grid import Grid, Unsupported
 from .pml import PML
 
 __all__ = ["FdtdDriver", "FdtdCancelled", "FdtdDivergence", "Susceptibility", "LORENTZ",
-           "DRUDE", "Grid", "PML", "FluxMonitor", "DFTMonitor", "Unsupported", "AbsorberLayer"]
+           "DRUDE", "Grid", "PML", "FluxMonitor", "DFTMonitor", "Unsupported", "AbsorberLayer",
+           "FluxDftData", "FluxPlaneDft"]
 __version__ = "0.1.0"

@@ -92,6 +92,8 @@ class MgbSimDesc(ctypes.Structure):
         ("monitors", MgbMonitor * MGB_MAX_MONITORS),
         ("status", ctypes.c_void_p),
         ("conductivity", ctypes.POINTER(MgbConductivity)),
+        ("nsrc_magnetic", ctypes.c_int32),
+        ("src_box_magnetic", ctypes.c_int32 * 6),
     ]
 
 

@@ -105,6 +105,7 @@ class FluxAdjoint:
                     slots[q].data = self.lam_aux[name].data_ptr()
         d.npoles = 0
         d.nsrc = 0
+        d.nsrc_magnetic = 0
         d.src_cell = None
         d.src_comp = None
         d.monitors[0] = engine.desc.monitors[self.index]

@@ -88,11 +88,13 @@ struct StepParams {
   int npoles;
   int pbox[6];
   mgb_pole poles[MGB_MAX_POLES];
-  int nsrc;
+  int nsrc;                 // every point; the last nsrc_h are magnetic (into B)
   const int64_t* src_cell;
   const int32_t* src_comp;
-  int src_box[6];
+  int src_box[6];           // box of the electric points
   const double* src_words;  // row for the current step, [nsrc]
+  int nsrc_h;
+  int src_box_h[6];         // box of the magnetic points
   int32_t* status;
   int l2pf;  // 1: each thread prefetches its x chunk's field planes into L2 before marching
 };
@@ -284,7 +286,7 @@ __device__ __forceinline__ void h_aux_load(const StepParams& p, const HColumn& c
   }
 }
 
-template <bool SX, bool SY, bool SZ, bool COND = false>
+template <bool SX, bool SY, bool SZ, bool COND = false, bool MSRC = false>
 __device__ __forceinline__ void h_cell_v(const StepParams& p, const HColumn& col,
                                          const HPlane& pl, int first_step, int c, float cx,
                                          float cy, float cz, const float h_old[3], const HAux& a,
@@ -312,6 +314,19 @@ __device__ __forceinline__ void h_cell_v(const StepParams& p, const HColumn& col
     b1 = curl_form<SZ, SX>(b1, cy, sf1, u1, col.kms_zh, col.sinv_zh, pl.kms_xh, pl.sinv_xh, n1);
     b2 = curl_form<SX, SY>(b2, cz, sf2, u2, pl.kms_xh, pl.sinv_xh, col.kms_yh, col.sinv_yh, n2);
   }
+  // Magnetic sources at t (MEEP's step_source(B) right after step_B): the same double
+  // subtract into B, before zero_metal_B and update_H.
+  if (MSRC && i >= p.src_box_h[0] && i < p.src_box_h[1] && j >= p.src_box_h[2] &&
+      j < p.src_box_h[3] && k >= p.src_box_h[4] && k < p.src_box_h[5]) {
+    for (int s = p.nsrc - p.nsrc_h; s < p.nsrc; ++s) {
+      if (p.src_cell[s] != c) continue;
+      const int q = p.src_comp[s];
+      const double w = p.src_words[s];
+      if (q == 3) b0 = __double2float_rn(__dsub_rn((double)b0, w));
+      else if (q == 4) b1 = __double2float_rn(__dsub_rn((double)b1, w));
+      else b2 = __double2float_rn(__dsub_rn((double)b2, w));
+    }
+  }
   // zero_metal_B happens in the caller before this returns its words (masks above).
   h_new[0] = b0; h_new[1] = b1; h_new[2] = b2;
   // update_H on the own-axis integer membership (MEEP starts H and f_w from B once).
@@ -332,7 +347,7 @@ __device__ __forceinline__ bool h_needs_plane(int axes) { return axes != 0 && ax
 
 // One cell of the H half: masks, the variant for the warp's memberships, zero_metal_B.
 // `axes` bit 0/1/2: the warp touches the x/y/z memberships (0 on the fast path).
-template <bool PML, bool COND = false, int AX = -1>
+template <bool PML, bool COND = false, int AX = -1, bool MSRC = false>
 __device__ __forceinline__ void h_cell(const StepParams& p, const HColumn& col, const HPlane& pl,
                                        int axes, int first_step, int i, int j, int k, int c,
                                        float cx, float cy, float cz, const float h_old[3],
@@ -347,18 +362,21 @@ __device__ __forceinline__ void h_cell(const StepParams& p, const HColumn& col, 
     // a lossy run: the variant of the CTA's axes, or the general one (the conductive
     // forms test each membership per cell)
     constexpr bool X = AX < 0 || (AX & 1), Y = AX < 0 || (AX & 2), Z = AX < 0 || (AX & 4);
-    if (PML) h_cell_v<X, Y, Z, true>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new, cp, i, j, k);
-    else h_cell_v<false, false, false, true>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new, cp, i, j, k);
+    if (PML) h_cell_v<X, Y, Z, true, MSRC>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new, cp, i, j, k);
+    else h_cell_v<false, false, false, true, MSRC>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new, cp, i, j, k);
   } else if (PML && AX >= 0) {
     // the CTA's memberships are known: exactly the variant of its axes
-    h_cell_v<(AX & 1) != 0, (AX & 2) != 0, (AX & 4) != 0>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new);
+    h_cell_v<(AX & 1) != 0, (AX & 2) != 0, (AX & 4) != 0, false, MSRC>(p, col, pl, first_step, c, cx, cy, cz, h_old,
+                                                                        a, h_new, nullptr, i, j, k);
   } else if (!PML || axes == 0) {
-    h_cell_v<false, false, false>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new);
+    h_cell_v<false, false, false, false, MSRC>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new, nullptr, i, j, k);
   } else {
     // The z-only edge (the two z-edge warps of every interior row) is the commonest slow
     // case; every other mix takes the general variant.
-    if (axes == 4) h_cell_v<false, false, true>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new);
-    else h_cell_v<true, true, true>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new);
+    if (axes == 4)
+      h_cell_v<false, false, true, false, MSRC>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new, nullptr, i, j, k);
+    else
+      h_cell_v<true, true, true, false, MSRC>(p, col, pl, first_step, c, cx, cy, cz, h_old, a, h_new, nullptr, i, j, k);
   }
   if (p.met[0] && i == 0) h_new[0] = 0.f;
   if (p.met[1] && j == 0) h_new[1] = 0.f;
@@ -486,9 +504,9 @@ __device__ __forceinline__ void e_cell_v(const StepParams& p, const EColumn& col
     d[2] = curl_form<SX, SY>(d[2], cz, sf2, u2, pl.kms_x, pl.sinv_x, col.kms_y, col.sinv_y, n2);
   }
   // Electric sources at t + dt/2: f = float(double(f) - A), point by point in order.
-  if (p.nsrc > 0 && i >= p.src_box[0] && i < p.src_box[1] && j >= p.src_box[2] &&
+  if (p.nsrc > p.nsrc_h && i >= p.src_box[0] && i < p.src_box[1] && j >= p.src_box[2] &&
       j < p.src_box[3] && k >= p.src_box[4] && k < p.src_box[5]) {
-    for (int s = 0; s < p.nsrc; ++s) {
+    for (int s = 0; s < p.nsrc - p.nsrc_h; ++s) {
       if (p.src_cell[s] != c) continue;
       const int q = p.src_comp[s];
       const double w = words[s];
@@ -590,16 +608,17 @@ __device__ __forceinline__ bool next_lane_has_z(int k, int nz) {
 }
 __device__ __forceinline__ bool prev_lane_has_z() { return lane_id() != 0 && threadIdx.x > 0; }
 
-// Whether a CTA's cells [i0, i1) x [j0, j0 + by) x [k0, k0 + bz) all lie in the box that
-// no membership reaches (then the PML update is the plain one, word for word).
-__device__ __forceinline__ bool cta_inner(const StepParams& p, int i0, int i1, int j0, int by, int k0, int bz) {
-  return i0 >= p.inner[0] && i1 <= p.inner[1] && j0 >= p.inner[2] && j0 + by <= p.inner[3] &&
-         k0 >= p.inner[4] && k0 + bz <= p.inner[5];
+// The axes (bit 0 x, 1 y, 2 z) along which a CTA's cells [i0, i1) x [j0, j0 + by) x
+// [k0, k0 + bz) reach some membership: outside the range of the box no membership
+// reaches (StepParams.inner) some auxiliary's run may hold a cell; inside it none does,
+// so every coefficient of that axis is exactly 1 for the whole CTA. 0: the CTA steps the
+// plain update, word for word.
+// Whether a CTA's cells reach the bounding box of the magnetic source points.
+__device__ __forceinline__ bool cta_msrc(const StepParams& p, int i0, int i1, int j0, int by, int k0, int bz) {
+  return p.nsrc_h > 0 && i0 < p.src_box_h[1] && i1 > p.src_box_h[0] && j0 < p.src_box_h[3] &&
+         j0 + by > p.src_box_h[2] && k0 < p.src_box_h[5] && k0 + bz > p.src_box_h[4];
 }
 
-// The axes (bit 0 x, 1 y, 2 z) along which a CTA's cells reach some membership: outside
-// the inner box's range on an axis some auxiliary's run may hold a cell; inside it none
-// does, so every coefficient of that axis is exactly 1 for the whole CTA.
 __device__ __forceinline__ int cta_axes(const StepParams& p, int i0, int i1, int j0, int by, int k0, int bz) {
   return ((i0 >= p.inner[0] && i1 <= p.inner[1]) ? 0 : 1) |
          ((j0 >= p.inner[2] && j0 + by <= p.inner[3]) ? 0 : 2) |
@@ -622,7 +641,7 @@ __device__ __forceinline__ int cta_axes(const StepParams& p, int i0, int i1, int
 // ------------------------------------------------------------------------------------
 // Generic kernels: plain loads, one thread per (y, z) column marching over x.
 // One thread's column (j, k) of the H half over planes [i0, i1).
-template <bool PML, bool COND = false, int AX = -1>
+template <bool PML, bool COND = false, int AX = -1, bool MSRC = false>
 __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i0, int i1,
                                         int first_step, const mgb_conductivity* cp = nullptr) {
   const int sx = p.ny * p.nz;
@@ -686,7 +705,7 @@ __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i
     const float cy = dtdx * (((ex_zp - ex) + ez) - ez_xp);
     const float cz = dtdx * (((ey_xp - ey) + ex) - ex_yp);
     float h_new[3];
-    h_cell<PML, COND, AX>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, h_old, ax, h_new, cp);
+    h_cell<PML, COND, AX, MSRC>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, h_old, ax, h_new, cp);
     p.H[0][c] = h_new[0];
     p.H[1][c] = h_new[1];
     p.H[2][c] = h_new[2];
@@ -800,7 +819,7 @@ __device__ __forceinline__ void h_loads(const StepParams& p, HLoads& L, int i, i
   L.h[2] = p.H[2][c];
 }
 
-template <bool PML, int AX = -1>
+template <bool PML, int AX = -1, bool MSRC = false>
 __device__ __forceinline__ void h_march_pf(const StepParams& p, int j, int k, int i0, int i1,
                                            int first_step) {
   const int sx = p.ny * p.nz;
@@ -857,7 +876,7 @@ __device__ __forceinline__ void h_march_pf(const StepParams& p, int j, int k, in
     const float cy = dtdx * (((cur.ex_zp - cur.ex) + ez) - cur.ez_xp);
     const float cz = dtdx * (((cur.ey_xp - ey) + cur.ex) - cur.ex_yp);
     float h_new[3];
-    h_cell<PML, false, AX>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, cur.h, ax, h_new);
+    h_cell<PML, false, AX, MSRC>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, cur.h, ax, h_new);
     p.H[0][c] = h_new[0];
     p.H[1][c] = h_new[1];
     p.H[2][c] = h_new[2];
@@ -970,6 +989,11 @@ __global__ void __launch_bounds__(256, 4) h_generic_pf(const __grid_constant__ S
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
   const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  // the CTAs that hold magnetic source points deposit them (the others skip the test)
+  if (cta_msrc(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x)) {
+    h_march_pf<PML, -1, true>(p, j, k, i0, i1, first_step);
+    return;
+  }
   if (!PML) {
     h_march_pf<false>(p, j, k, i0, i1, first_step);
     return;
@@ -1005,6 +1029,11 @@ __global__ void __launch_bounds__(256, 5) h_generic(const __grid_constant__ Step
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
   const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  // the CTAs that hold magnetic source points deposit them (the others skip the test)
+  if (cta_msrc(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x)) {
+    h_march<PML, false, -1, true>(p, j, k, i0, i1, first_step);
+    return;
+  }
   if (!PML) {
     h_march<false>(p, j, k, i0, i1, first_step);
     return;
@@ -1045,6 +1074,11 @@ __global__ void __launch_bounds__(256) h_generic_cond(const __grid_constant__ St
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
   const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  // the CTAs that hold magnetic source points deposit them (the others skip the test)
+  if (cta_msrc(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x)) {
+    h_march<PML, true, -1, true>(p, j, k, i0, i1, first_step, &cp);
+    return;
+  }
   if (!PML) {
     h_march<false, true>(p, j, k, i0, i1, first_step, &cp);
     return;
@@ -1241,7 +1275,7 @@ __global__ void __launch_bounds__(kThreads, 2) h_tile(const __grid_constant__ St
       }
       HAux ax = {};
       if (PML && axes != 0) h_aux_load(p, hcol, pl, c, ax);
-      h_cell<PML>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, h_old, ax, h_new);
+      h_cell<PML, false, -1, true>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, h_old, ax, h_new);
       p.H[0][c] = h_new[0];
       p.H[1][c] = h_new[1];
       p.H[2][c] = h_new[2];
@@ -2205,6 +2239,9 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
         if (d.poles[m].sigma[q] != nullptr && (d.poles[m].p[q][0] == nullptr || d.poles[m].p[q][1] == nullptr))
           return fail(MGB_ERR_ARGUMENT, "a driven polarization component has no P buffers");
   }
+  if (d.nsrc_magnetic < 0 || d.nsrc_magnetic > d.nsrc) {
+    return fail(MGB_ERR_ARGUMENT, "nsrc_magnetic must lie in 0..nsrc");
+  }
   if (d.nsrc < 0 || (d.nsrc > 0 && (d.src_cell == nullptr || d.src_comp == nullptr))) {
     return fail(MGB_ERR_ARGUMENT, "source point tables are missing");
   }
@@ -2292,6 +2329,8 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
   for (int a = 0; a < 6; ++a) { p.pbox[a] = d.pbox[a]; p.src_box[a] = d.src_box[a]; }
   for (int m = 0; m < d.npoles; ++m) p.poles[m] = d.poles[m];
   p.nsrc = d.nsrc;
+  p.nsrc_h = d.nsrc_magnetic;
+  for (int a = 0; a < 6; ++a) p.src_box_h[a] = d.src_box_magnetic[a];
   p.src_cell = d.src_cell;
   p.src_comp = d.src_comp;
   p.src_words = nullptr;
@@ -2824,6 +2863,7 @@ int mgb_batch_set_slot(mgb_batch* b, int32_t slot, mgb_sim* sim, int64_t end_ste
   if (end_step < 1) return fail(MGB_ERR_ARGUMENT, "a slot needs at least one step");
   if (sim->step.nsrc > 0 && words == nullptr) return fail(MGB_ERR_ARGUMENT, "the slot's sources need deposit words");
   if (sim->has_cond) return fail(MGB_ERR_UNSUPPORTED, "a batched slot does not carry a conductivity");
+  if (sim->step.nsrc_h > 0) return fail(MGB_ERR_UNSUPPORTED, "a batched slot does not carry magnetic sources");
   if (sim->desc.nmonitors > kSlotMonitors)
     return fail(MGB_ERR_UNSUPPORTED, "a batched slot holds at most " + std::to_string(kSlotMonitors) + " monitors");
   for (int m = 0; m < sim->desc.nmonitors; ++m) {

@@ -25,6 +25,7 @@ summed in float64 by the device.
 from __future__ import annotations
 
 import math
+from dataclasses import dataclass
 from typing import Any, List, Optional, Sequence, Tuple
 
 import numpy as np
@@ -233,11 +234,32 @@ class DFTMonitor(_Monitor):
         return self.raw(component)[freq_index]
 
 
+@dataclass(frozen=True)
+class FluxPlaneDft:
+    """One flux plane's accumulated E and H transforms, host copies detached from the run
+    (reference ``dft.py:2618``): ``{"Ex"/"Ey"/"Ez": (nf,) + region complex64}`` and the
+    same for H."""
+
+    E: dict
+    H: dict
+    frequencies: tuple
+
+
+@dataclass(frozen=True)
+class FluxDftData:
+    """What a flux monitor's ``get_dft_data()`` returns (reference ``dft.py:2638``,
+    MEEP's ``sim.get_flux_data``): one :class:`FluxPlaneDft` per plane, to be handed to
+    ``load_dft_data`` / ``load_minus_dft_data`` of a monitor built the same way."""
+
+    planes: tuple
+
+
 class FluxMonitor(_Monitor):
     """Poynting flux through an axis-aligned plane (reference dft.py:2814).
 
     Only the tangential pair of E and of H is accumulated: the normal components
-    never enter the flux.
+    never enter the flux. In the saved transforms (:meth:`get_dft_data`) they are
+    zero, and loading ignores them.
     """
 
     kind = "flux"
@@ -278,6 +300,100 @@ class FluxMonitor(_Monitor):
 
     def get_flux(self, freq_index: int = 0) -> float:
         return float(self.get_flux_spectrum()[freq_index])
+
+    # --- saved transforms: the two-run normalisation idiom ----------------------------
+    def _shape(self) -> Tuple[int, ...]:
+        return (self.num_frequencies,) + self.region_shape
+
+    def _tangential(self) -> dict:
+        """The accumulated tangential transforms (complex64, ``(nf,) + region``)."""
+        if self.accumulator is not None:
+            return {name: self.raw(name) for name in self.components}
+        pending = getattr(self, "_pending", None)
+        if pending is not None:
+            return {name: pending[name].copy() for name in self.components}
+        return {name: np.zeros(self._shape(), dtype=np.complex64) for name in self.components}
+
+    def get_dft_data(self) -> FluxDftData:
+        """This plane's accumulated transforms (reference ``FluxMonitor.get_dft_data``
+        :3261, MEEP's ``sim.get_flux_data``), as host copies."""
+        blocks = self._tangential()
+        full = {name: blocks.get(name, np.zeros(self._shape(), dtype=np.complex64)) for name in COMPONENTS}
+        return FluxDftData(planes=(FluxPlaneDft(E={n: full[n] for n in ELECTRIC},
+                                                H={n: full[n] for n in MAGNETIC},
+                                                frequencies=tuple(self.frequencies)),))
+
+    def load_dft_data(self, data: FluxDftData) -> None:
+        """Replace this plane's transforms with ``data`` (MEEP's ``load_flux_data``: the
+        stored words are replaced, not added to). Checked as the reference checks it
+        (``dft.py:2660`` ``_load_flux_planes``): one plane, the same frequencies, all six
+        components, each block of this plane's shape; a refusal changes nothing."""
+        where = "FluxMonitor.load_dft_data"
+        if not isinstance(data, FluxDftData):
+            raise TypeError(f"{where} takes the object a flux monitor's get_dft_data() returned "
+                            f"(FluxDftData), got {type(data).__name__}")
+        if len(data.planes) != 1:
+            raise ValueError(f"{where} was given data for {len(data.planes)} flux plane(s) but this "
+                             f"monitor has 1")
+        record = data.planes[0]
+        if len(record.frequencies) != self.num_frequencies:
+            raise ValueError(f"{where}: the data holds {len(record.frequencies)} frequencies and this "
+                             f"monitor accumulates {self.num_frequencies}")
+        for saved, mine in zip(record.frequencies, self.frequencies):
+            if not math.isclose(float(saved), float(mine), rel_tol=1e-12, abs_tol=0.0):
+                raise ValueError(f"{where}: the data was accumulated at frequencies {record.frequencies} "
+                                 f"and this monitor accumulates {self.frequencies}")
+        for side, names, block in (("E", ELECTRIC, record.E), ("H", MAGNETIC, record.H)):
+            if set(block) != set(names):
+                raise ValueError(f"{where}: the data's {side} components are {sorted(block)}, "
+                                 f"expected {sorted(names)}")
+            for name in names:
+                if np.asarray(block[name]).shape != self._shape():
+                    raise ValueError(f"{where}: {name} in the data has shape {np.asarray(block[name]).shape} "
+                                     f"and this monitor's plane is {self._shape()}")
+        incoming = {}
+        for name in self.components:
+            block = record.E[name] if name in record.E else record.H[name]
+            incoming[name] = np.ascontiguousarray(np.asarray(block), dtype=np.complex64)
+        if self.accumulator is None:
+            self._pending = incoming  # written into the accumulators when the run freezes
+            return
+        self._engine.flush_dft()
+        self._write(incoming)
+
+    def _write(self, blocks: dict) -> None:
+        import torch
+
+        cells = self.cells
+        for q, name in enumerate(self.components):
+            values = blocks[name].reshape(self.num_frequencies, cells)
+            pair = np.stack([values.real, values.imag], axis=1).astype(np.float32)  # [nf][2][cells]
+            self.accumulator[q].copy_(torch.from_numpy(pair))
+
+    def scale_dfts(self, scale: complex) -> None:
+        """Multiply every accumulated transform by ``scale`` (``dft_flux::scale_dfts``:
+        both the E and the H side)."""
+        factor = complex(scale)
+        blocks = self._tangential()
+        scaled = {name: (block * factor).astype(np.complex64) for name, block in blocks.items()}
+        if self.accumulator is None:
+            self._pending = scaled
+            return
+        self._write(scaled)
+
+    def load_minus_dft_data(self, data: FluxDftData) -> None:
+        """``load_dft_data`` then negate (MEEP's ``load_minus_flux_data``): the second
+        run's accumulators start at -E1, -H1, so its flux is that of the field
+        difference, ``Re[(E2 - E1) x conj(H2 - H1)]``."""
+        self.load_dft_data(data)
+        self.scale_dfts(-1.0)
+
+    def reset(self) -> None:
+        """Zero every accumulator (buffered samples included)."""
+        self._pending = None
+        if self.accumulator is not None:
+            self._engine.flush_dft()
+            self.accumulator.zero_()
 
 
 def automatic_decimation(dt: float, monitor_frequencies: Sequence[float], sources) -> int:

@@ -83,7 +83,9 @@ class Engine:
         self.pml = pml if (pml is not None and pml.is_active) else None
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.stream = stream
-        self.sources = list(sources)
+        # electric points first, then magnetic ones: the library's table layout (each
+        # kind keeps its own order, the order the reference deposits in)
+        self.sources = [s for s in sources if not s.magnetic] + [s for s in sources if s.magnetic]
         self.monitors = list(monitors)
         shape = grid.shape
         dev = self.device
@@ -253,12 +255,12 @@ class Engine:
 
     def _setup_sources(self) -> None:
         d = self.desc
-        # a source on a lossy D component deposits current * dt * condinv at its cell
+        # a source on a lossy D or B component deposits current * dt * condinv at its cell
         condinv = {}
-        for q, axis in enumerate("xyz"):
-            sigma = self.conductivity.get("D" + axis)
+        for index, name in enumerate(("Dx", "Dy", "Dz", "Bx", "By", "Bz")):
+            sigma = self.conductivity.get(name)
             if sigma is not None:
-                condinv[q] = coefficients(sigma, self.grid.dt)[1]
+                condinv[index] = coefficients(sigma, self.grid.dt)[1]
         self.src_scales = deposit_scales(self.sources, condinv)
         cells: List[int] = []
         comps: List[int] = []
@@ -274,9 +276,14 @@ class Engine:
         self.src_comp = torch.tensor(comps, dtype=torch.int32, device=self.device)
         d.src_cell = self.src_cell.data_ptr()
         d.src_comp = self.src_comp.data_ptr()
-        ijk = np.array([c for s in self.sources for c in s.cells])
-        lo, hi = ijk.min(axis=0), ijk.max(axis=0) + 1
-        d.src_box[:] = [int(lo[0]), int(hi[0]), int(lo[1]), int(hi[1]), int(lo[2]), int(hi[2])]
+        d.nsrc_magnetic = sum(len(s.cells) for s in self.sources if s.magnetic)
+        for magnetic, box in ((False, d.src_box), (True, d.src_box_magnetic)):
+            ijk = np.array([c for s in self.sources if s.magnetic == magnetic for c in s.cells]).reshape(-1, 3)
+            if ijk.size == 0:
+                box[:] = [0, 0, 0, 0, 0, 0]
+                continue
+            lo, hi = ijk.min(axis=0), ijk.max(axis=0) + 1
+            box[:] = [int(lo[0]), int(hi[0]), int(lo[1]), int(hi[1]), int(lo[2]), int(hi[2])]
 
     def _setup_monitors(self) -> None:
         d = self.desc
@@ -305,6 +312,10 @@ class Engine:
             self.monitor_tensors.append((omega, acc, weights))
             monitor.accumulator = acc
             monitor._engine = self
+            pending = getattr(monitor, "_pending", None)
+            if pending is not None:  # transforms loaded before the run froze
+                monitor._write(pending)
+                monitor._pending = None
 
     def _setup_dft_buffers(self, mode: Optional[str]) -> None:
         """Tensor-core accumulation (``"tensor"``, the default; ``MEEPGB_DFT`` overrides

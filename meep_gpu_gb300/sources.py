@@ -29,7 +29,9 @@ import numpy as np
 from .grid import IYEE, Grid, Unsupported
 
 ELECTRIC = ("Ex", "Ey", "Ez")
-_COMPONENT_ALIASES = {"Ex": "Ex", "Ey": "Ey", "Ez": "Ez", "Dx": "Ex", "Dy": "Ey", "Dz": "Ez"}
+MAGNETIC = ("Hx", "Hy", "Hz")
+_COMPONENT_ALIASES = {"Ex": "Ex", "Ey": "Ey", "Ez": "Ez", "Dx": "Ex", "Dy": "Ey", "Dz": "Ez",
+                      "Hx": "Hx", "Hy": "Hy", "Hz": "Hz", "Bx": "Hx", "By": "Hy", "Bz": "Hz"}
 
 
 def amp_factor(frequency: float) -> Tuple[float, float]:
@@ -194,7 +196,8 @@ def deposition_table(grid: Grid, component: str, center: Sequence[float], size: 
                      amplitude: complex = 1.0,
                      amp_func: Optional[Callable[[float, float, float], complex]] = None,
                      ) -> Tuple[List[Tuple[int, int, int]], List[complex]]:
-    """Cells an electric source deposits into and each cell's complex amplitude.
+    """Cells a source deposits into (D for an electric one, B for a magnetic one) and
+    each cell's complex amplitude.
 
     MEEP's ``add_volume_source`` over one chunk: the request's doubled-coordinate
     bounds on the component's lattice, the Simpson tapers of the request, the owned
@@ -205,7 +208,7 @@ def deposition_table(grid: Grid, component: str, center: Sequence[float], size: 
     """
     comp = _COMPONENT_ALIASES.get(component)
     if comp is None:
-        raise Unsupported(f"only electric sources are stepped by this engine, got {component!r}")
+        raise Unsupported(f"source component {component!r} is not one of Ex..Ez, Hx..Hz")
     a = grid.resolution
     inva = grid.dx
     where_min = [float(center[d]) - float(size[d]) / 2 for d in range(3)]
@@ -336,7 +339,9 @@ def deposition_table(grid: Grid, component: str, center: Sequence[float], size: 
 
 @dataclass
 class Source:
-    """One electric current source: a waveform, a component and a deposition table."""
+    """One current source: a waveform, a component and a deposition table. An electric
+    source deposits into D in the E half at t + dt/2; a magnetic one (Hx, Hy, Hz) into B
+    right after step_B, at t (reference ``driver.py:3527-3535``)."""
 
     grid: Grid
     component: str
@@ -350,16 +355,24 @@ class Source:
 
     def __post_init__(self):
         self.component = _COMPONENT_ALIASES.get(self.component, self.component)
-        if self.component not in ELECTRIC:
-            raise Unsupported(
-                f"source component {self.component!r} is not stepped by this engine "
-                "(magnetic and integrated sources are refused)")
+        if self.component not in ELECTRIC + MAGNETIC:
+            raise Unsupported(f"source component {self.component!r} is not stepped by this engine")
         self.cells, self.amps = deposition_table(self.grid, self.component, self.center,
                                                  self.size, self.amplitude, self.amp_func)
 
     @property
+    def magnetic(self) -> bool:
+        return self.component in MAGNETIC
+
+    @property
     def comp_index(self) -> int:
-        return ELECTRIC.index(self.component)
+        """0..2 for Dx..Dz, 3..5 for Bx..Bz: the component the deposit writes."""
+        return (ELECTRIC + MAGNETIC).index(self.component)
+
+    @property
+    def time_offset(self) -> float:
+        """The current's time within step n, in steps: n + 1/2 (electric), n (magnetic)."""
+        return 0.0 if self.magnetic else 0.5
 
     def current(self, t: float) -> Tuple[float, float]:
         return current(self.waveform, t, self.grid.dt)
@@ -380,25 +393,29 @@ def _waveform_key(waveform) -> Optional[tuple]:
     return None  # a caller's function may not be pure: never cached
 
 
-def _currents(waveform, dt: float, first: int, steps: int) -> np.ndarray:
+def _currents(waveform, dt: float, first: int, steps: int, offset: float = 0.5) -> np.ndarray:
     out = np.empty((steps, 2), dtype=np.float64)
     for row in range(steps):
         n = first + row
-        out[row] = current(waveform, n * dt + 0.5 * dt, dt)
+        t = n * dt + 0.5 * dt if offset == 0.5 else n * dt
+        out[row] = current(waveform, t, dt)
     return out
 
 
-def current_sequence(waveform, dt: float, first: int, steps: int) -> np.ndarray:
+def current_sequence(waveform, dt: float, first: int, steps: int, offset: float = 0.5) -> np.ndarray:
     """Currents ``(re, im)`` of steps ``first .. first+steps-1``, evaluated at ``n*dt + dt/2``
-    (MEEP's ``calc_sources(time() + dt/2)`` before the D half), shape ``(steps, 2)``."""
+    (``offset`` 0.5: MEEP's ``calc_sources(time() + dt/2)`` before the D half) or at
+    ``n*dt`` (``offset`` 0: a magnetic source after step_B), shape ``(steps, 2)``."""
+    if offset not in (0.0, 0.5):
+        raise ValueError("a current is evaluated at n*dt or n*dt + dt/2")
     key = _waveform_key(waveform)
     if key is None or first + steps > _CURRENT_CACHE_STEPS:
-        return _currents(waveform, dt, first, steps)
-    key = key + (dt,)
+        return _currents(waveform, dt, first, steps, offset)
+    key = key + (dt, offset)
     table = _CURRENT_CACHE.get(key)
     have = 0 if table is None else len(table)
     if have < first + steps:
-        grown = _currents(waveform, dt, have, first + steps - have)
+        grown = _currents(waveform, dt, have, first + steps - have, offset)
         table = grown if table is None else np.concatenate([table, grown])
         _CURRENT_CACHE[key] = table
     return table[first:first + steps]
@@ -419,7 +436,7 @@ def deposit_words(sources: Sequence[Source], first_step: int, steps: int, dt: fl
     out = np.zeros((steps, count), dtype=np.float64)
     column = 0
     for source in sources:
-        seq = current_sequence(source.waveform, source.grid.dt, first_step, steps)
+        seq = current_sequence(source.waveform, source.grid.dt, first_step, steps, source.time_offset)
         c_re, c_im = seq[:, 0], seq[:, 1]
         plus_zero = ((c_re == 0.0) & ~np.signbit(c_re)) & ((c_im == 0.0) & ~np.signbit(c_im))
         for amp in source.amps:
@@ -434,8 +451,8 @@ def deposit_words(sources: Sequence[Source], first_step: int, steps: int, dt: fl
 
 def deposit_scales(sources: Sequence[Source], condinv: Dict[int, np.ndarray]) -> Optional[np.ndarray]:
     """Per deposit point, the float64 ``condinv`` word of its target component at its
-    cell (``condinv``: component index 0..2 -> float32 volume of the lossy D components),
-    or None when no point lands on a lossy component."""
+    cell (``condinv``: component index 0..2 (D) or 3..5 (B) -> float32 volume of the
+    lossy components), or None when no point lands on a lossy component."""
     if not any(source.comp_index in condinv for source in sources):
         return None
     scales = []
@@ -452,9 +469,9 @@ def deposit_words_scalar(sources: Sequence[Source], first_step: int, steps: int,
     out = np.zeros((steps, count), dtype=np.float64)
     for row in range(steps):
         n = first_step + row
-        t = n * dt + 0.5 * dt
         column = 0
         for source in sources:
+            t = n * dt + 0.5 * dt if not source.magnetic else n * dt
             c = source.current(t)
             plus_zero = (c[0] == 0.0 and math.copysign(1.0, c[0]) > 0
                          and c[1] == 0.0 and math.copysign(1.0, c[1]) > 0)

@@ -18,7 +18,8 @@
  *   zero_metal_B/D       stepping.py:3120 / :3093
  *   update_H / update_E  stepping.py:1216 / :1243 with _apply_constitutive_pml :2991
  *                        and MEEP's start of H (separate_h_from_b :2789)
- *   source deposit       sources.py _deposit :1357 (double subtract, one rounding)
+ *   source deposit       sources.py _deposit :1357 (double subtract, one rounding);
+ *                        magnetic sources into B right after step_B (driver.py:3534)
  *   update_P             dispersion.py PolarizationState.update :689
  *   conductivity         stepping.py _apply_conductive_update :2828 (no PML) and
  *                        _apply_conductive_pml_update :2844 (the four conductive forms
@@ -233,8 +234,15 @@ static void SUF(zero_metal)(SUF(oracle_state)* s, REAL* const f[3], int electric
 void SUF(oracle_step)(SUF(oracle_state)* s, const double* words) {
   const int n[3] = {s->nx, s->ny, s->nz};
   const long long cells = (long long)n[0] * n[1] * n[2];
-  /* 1. step_B, 2b. zero_metal_B */
+  /* 1. step_B, 2. magnetic sources (components 3..5, B = NARROW(double(B) - A)),
+   * 2b. zero_metal_B */
   SUF(curl_family)(s, s->B, s->E, s->fuB, 0);
+  for (int p = 0; p < s->nsrc; ++p) {
+    if (s->src_comp[p] < 3) continue;
+    REAL* b = s->B[s->src_comp[p] - 3];
+    const long long c = s->src_cell[p];
+    b[c] = NARROW((double)b[c] - words[p]);
+  }
   SUF(zero_metal)(s, s->B, 0);
   /* 3. update_H (stored H only under a PML) */
   if (s->pml) {
@@ -274,6 +282,7 @@ void SUF(oracle_step)(SUF(oracle_state)* s, const double* words) {
   SUF(curl_family)(s, s->D, s->H, s->fuD, 1);
   /* 5. electric sources: D = NARROW(double(D) - A) point by point */
   for (int p = 0; p < s->nsrc; ++p) {
+    if (s->src_comp[p] >= 3) continue;
     REAL* d = s->D[s->src_comp[p]];
     const long long c = s->src_cell[p];
     d[c] = NARROW((double)d[c] - words[p]);

@@ -199,12 +199,12 @@ def problem_from_driver(driver) -> Problem:
             weights=m.weights.reshape(-1) if flux else None,
             measure=m.measure if flux else 1.0, weight=m.weight if flux else 1.0))
     conductivity = {name: v for name, v in driver.conductivity_volumes().items() if v is not None}
-    # a deposit on a lossy D component is scaled by its condinv word (sources.py:1357)
+    # a deposit on a lossy D or B component is scaled by its condinv word (sources.py:1357)
     condinv = {}
-    for q, axis in enumerate("xyz"):
-        sigma = conductivity.get("D" + axis)
+    for index, name in enumerate(("Dx", "Dy", "Dz", "Bx", "By", "Bz")):
+        sigma = conductivity.get(name)
         if sigma is not None:
-            condinv[q] = (1.0 / (1.0 + (sigma.astype(np.float64) * grid.dt) * 0.5)).astype(np.float32)
+            condinv[index] = (1.0 / (1.0 + (sigma.astype(np.float64) * grid.dt) * 0.5)).astype(np.float32)
     scales = deposit_scales(sources, condinv)
     return Problem(shape=grid.shape, metallic=tuple(int(grid.is_metallic(a)) for a in range(3)),
                    dt=grid.dt, dx=grid.dx, pml=pml is not None, tables32=tables32,

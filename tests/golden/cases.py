@@ -36,6 +36,11 @@ CASES = {
     # thicknesses), per-component D conductivity and a Lorentz pole.
     "absorber_pml_periodic": dict(n=(14, 12, 16), pml={"x": 3}, steps=50, boundaries="periodic",
                                   conductivity="mixed", lorentz=True),
+    # Magnetic sources (a Gaussian Hx point and a CW Hz sheet) beside the Ez one, under a
+    # PML; and again in a lossy run without PML (absorber, D and B conductivity), where
+    # the magnetic deposit carries B's condinv.
+    "magnetic": dict(n=(14, 12, 16), pml=3, steps=60, magnetic=True),
+    "magnetic_lossy": dict(n=(13, 14, 12), pml=0, steps=60, magnetic=True, conductivity="absorber_b"),
 }
 
 # The 80^3 sphere-under-PML workload (resolution 10, 10-cell PML, eps 4 sphere of radius
@@ -78,6 +83,11 @@ def build_case(driver_cls, susceptibility_cls, case: dict, reference: bool = Fal
     d.add_source({"source_type": "gaussian", "component": "Ez",
                   "center": (source_x, 0.03, 0.0), "size": (0, 0, 0),
                   "frequency": fcen, "fwidth": fwidth})
+    if case.get("magnetic"):
+        d.add_source({"source_type": "gaussian", "component": "Hx", "center": (0.1, -0.05, 0.07),
+                      "size": (0, 0, 0), "frequency": fcen, "fwidth": fwidth})
+        d.add_source({"source_type": "continuous", "component": "Hz", "center": (-0.05, 0.1, -0.1),
+                      "size": (0.3, 0, 0.2), "frequency": 0.3, "amplitude": 0.5})
     if case.get("mixed"):
         block = (np.abs(x - 0.2) < 0.15) & (np.abs(y) < 0.3)
         d.add_susceptibility(susceptibility_cls(frequency=0.9, gamma=0.1),
@@ -114,9 +124,35 @@ def _set_conductivity(d, case: dict, x, y, z, lengths, reference: bool) -> None:
     elif kind == "absorber":
         d.set_conductivity(0.05)
         d.set_absorber([AbsorberLayer(0.3, axis, side) for axis in range(3) for side in ("low", "high")])
+    elif kind == "absorber_b":
+        d.set_conductivity(0.05)
+        d.set_b_conductivity(0.1)
+        d.set_absorber([AbsorberLayer(0.3, axis, side) for axis in range(3) for side in ("low", "high")])
     elif kind == "mixed":
         d.set_conductivity({"Dx": np.where(np.abs(z) < 0.3, 0.25, 0.0).astype(np.float32),
                             "Dz": np.where(y > 0.1, 0.15, 0.0).astype(np.float32)})
         d.set_absorber([AbsorberLayer(0.25, 2, "low"), AbsorberLayer(0.35, 2, "high")])
     else:
         raise ValueError(f"unknown conductivity case {kind!r}")
+
+
+# The two-run flux normalisation: run 1 in vacuum saves its flux-plane transforms, run 2
+# (a dielectric sphere between the source and the plane) starts from minus them.
+FLUX_NORM = dict(n=(14, 12, 16), pml=3, steps=120)
+
+
+def build_flux_norm(driver_cls, structure: bool, reference: bool = False):
+    """One run of the normalisation pair; returns (driver, flux monitor)."""
+    res = 10
+    lengths = tuple(v / res for v in FLUX_NORM["n"])
+    d = driver_cls(cell_size=lengths, resolution=res, courant=0.5, force_complex_fields=False,
+                   boundaries="metallic", **({"prefer_gpu": False} if reference else {}))
+    d.setup_pml(FLUX_NORM["pml"])
+    x, y, z = d.grid.meshgrid()
+    if structure:
+        d.set_epsilon(np.where((x - 0.1) ** 2 + y ** 2 + z ** 2 < 0.2 ** 2, 4.0, 1.0).astype(np.float32))
+    d.add_source({"source_type": "gaussian", "component": "Ez", "center": (-0.2, 0.03, 0.0),
+                  "size": (0, 0, 0), "frequency": 0.5, "fwidth": 0.4})
+    flux = d.add_flux_monitor(fcen=0.5, df=0.3, nfreq=4, center=(0.35, 0, 0), size=(0, 0.7, 1.1),
+                              decimation_factor=0)
+    return d, flux

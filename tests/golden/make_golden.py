@@ -13,7 +13,10 @@ beside the repository) and writes small fixtures into this directory:
   regions and weights and automatic decimation factors for a sweep of requests;
 * ``conductivity_tables.npz``: ``mp.Absorber`` sigma volumes, conductivity
   coefficients (condfac / condinv) and, under a one-rank PML, the cells whose chunk
-  keeps a conductivity, for seeded configurations (``python make_golden.py conductivity``).
+  keeps a conductivity, for seeded configurations (``python make_golden.py conductivity``);
+* ``flux_normalization.npz``: the two-run normalisation idiom (``python make_golden.py
+  flux_norm``): the vacuum run's saved flux-plane transforms and spectrum, and the
+  structure run's spectrum started from minus them and alone.
 
 The fixtures are committed; this script is how they were made. It is not run by the
 tests (the reference is not available where the GPU tests run).
@@ -189,6 +192,29 @@ def record_conductivity_tables() -> None:
     print("conductivity tables written")
 
 
+def record_flux_normalization() -> None:
+    from tests.golden.cases import FLUX_NORM, build_flux_norm
+
+    steps = FLUX_NORM["steps"]
+    d1, f1 = build_flux_norm(FdtdDriver, structure=False, reference=True)
+    d1.run(num_steps=steps)
+    data = f1.get_dft_data()
+    out = {"flux1": np.asarray(f1.get_flux_spectrum(), dtype=np.float64),
+           "frequencies": np.asarray(data.planes[0].frequencies, dtype=np.float64)}
+    for side in (data.planes[0].E, data.planes[0].H):
+        for name, block in side.items():
+            out[f"data_{name}"] = np.asarray(block, dtype=np.complex64)
+    d2, f2 = build_flux_norm(FdtdDriver, structure=True, reference=True)
+    f2.load_minus_dft_data(data)
+    d2.run(num_steps=steps)
+    out["flux2_minus"] = np.asarray(f2.get_flux_spectrum(), dtype=np.float64)
+    d3, f3 = build_flux_norm(FdtdDriver, structure=True, reference=True)
+    d3.run(num_steps=steps)
+    out["flux2_plain"] = np.asarray(f3.get_flux_spectrum(), dtype=np.float64)
+    np.savez_compressed(HERE / "flux_normalization.npz", **out)
+    print("flux normalization written")
+
+
 if __name__ == "__main__":
     which = sys.argv[1:] or ["fields", "digest", "tables"]
     if "fields" in which or any(w in CASES for w in which):
@@ -201,3 +227,5 @@ if __name__ == "__main__":
         record_digest()
     if "conductivity" in which:
         record_conductivity_tables()
+    if "flux_norm" in which:
+        record_flux_normalization()

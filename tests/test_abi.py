@@ -78,7 +78,7 @@ int main(void) {
   F(mgb_sim_desc, status) F(mgb_monitor, scale) F(mgb_monitor, omega) F(mgb_monitor, acc)
   F(mgb_pole, sigma) F(mgb_pole, p) F(mgb_sim_desc, conductivity)
   F(mgb_conductivity, condinv) F(mgb_conductivity, fcond) F(mgb_conductivity, chunk_of)
-  F(mgb_conductivity, keeps)
+  F(mgb_conductivity, keeps) F(mgb_sim_desc, nsrc_magnetic) F(mgb_sim_desc, src_box_magnetic)
   return 0;
 }
 """

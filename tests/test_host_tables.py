@@ -69,6 +69,9 @@ def test_array_deposit_words_equal_the_per_step_form():
                  amplitude=0.7 - 0.3j),
         S.Source(grid, "Ey", (0.0, 0.0, 0.3), (0, 0, 0),
                  S.CustomWaveform(lambda t: np.exp(-((t - 3.0) ** 2)) * (1 + 0.5j))),
+        # magnetic: its current is taken at n*dt, not n*dt + dt/2
+        S.Source(grid, "Hx", (0.1, 0.0, 0.0), (0, 0, 0), S.GaussianWaveform(0.15, 0.1)),
+        S.Source(grid, "Hz", (0.0, 0.1, 0.0), (0.2, 0, 0), S.ContinuousWaveform(0.4)),
     ]
     S._CURRENT_CACHE.clear()
     for first, steps in ((0, 300), (250, 400), (0, 900), (1000, 17)):
@@ -100,3 +103,20 @@ def test_device_status_word_is_decoded():
         fake_obj[0] = fake(word)
         with pytest.raises(RuntimeError, match="timed out"):
             Engine.device_status(fake_obj[0])
+
+
+def test_magnetic_sources_take_their_current_at_the_whole_step():
+    from meep_gpu_gb300 import sources as S
+
+    grid = Grid((3.2, 3.2, 3.2), 10)
+    wave = S.GaussianWaveform(0.15, 0.1)
+    electric = S.Source(grid, "Ez", (0.0, 0.0, 0.0), (0, 0, 0), wave)
+    magnetic = S.Source(grid, "Bz", (0.0, 0.0, 0.0), (0, 0, 0), wave)
+    assert magnetic.component == "Hz" and magnetic.magnetic and magnetic.comp_index == 5
+    assert electric.comp_index == 2 and not electric.magnetic
+    n = 123
+    e = S.deposit_words([electric], n, 1, grid.dt)[0, 0] / (electric.amps[0].real * grid.dt)
+    m = S.deposit_words([magnetic], n, 1, grid.dt)
+    assert e == S.current(wave, n * grid.dt + 0.5 * grid.dt, grid.dt)[0]
+    assert m[0, 0] == (magnetic.amps[0].real * S.current(wave, n * grid.dt, grid.dt)[0]
+                       - magnetic.amps[0].imag * S.current(wave, n * grid.dt, grid.dt)[1]) * grid.dt

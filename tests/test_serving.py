@@ -239,8 +239,9 @@ def test_batch_steps_every_golden_configuration_to_the_reference_words(gpu):
     from tests import golden_io
     from tests.golden.cases import CASES, build_case
 
-    # <= 2 monitors a slot; a lossy run is not batched (refused by name)
-    names = [n for n in sorted(CASES) if n not in ("mixed", "tile_mixed") and not CASES[n].get("conductivity")]
+    # <= 2 monitors a slot; lossy runs and magnetic sources are not batched (refused by name)
+    names = [n for n in sorted(CASES) if n not in ("mixed", "tile_mixed")
+             and not CASES[n].get("conductivity") and not CASES[n].get("magnetic")]
     server = serving.BatchServer(gpu, max_slots=len(names), steps_per_replay=16, max_side=72)
     jobs = []
     for name in names:

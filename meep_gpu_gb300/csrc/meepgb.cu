@@ -982,15 +982,15 @@ __device__ __forceinline__ void e_march_pf(const StepParams& p, int j, int k, in
   }
 }
 
-template <bool PML>
+template <bool PML, bool MSRC>
 __global__ void __launch_bounds__(256, 4) h_generic_pf(const __grid_constant__ StepParams p,
                                                        int first_step, int xchunk) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
   const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
-  // the CTAs that hold magnetic source points deposit them (the others skip the test)
-  if (cta_msrc(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x)) {
+  // a run with magnetic sources: the CTAs that hold source points deposit them
+  if (MSRC && cta_msrc(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x)) {
     h_march_pf<PML, -1, true>(p, j, k, i0, i1, first_step);
     return;
   }
@@ -1022,15 +1022,15 @@ __global__ void __launch_bounds__(256, 4) e_generic_pf(const __grid_constant__ S
 }
 
 // Generic kernels: plain loads, one thread per (y, z) column marching over an x chunk.
-template <bool PML>
+template <bool PML, bool MSRC>
 __global__ void __launch_bounds__(256, 5) h_generic(const __grid_constant__ StepParams p,
                                                     int first_step, int xchunk) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
   const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
-  // the CTAs that hold magnetic source points deposit them (the others skip the test)
-  if (cta_msrc(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x)) {
+  // a run with magnetic sources: the CTAs that hold source points deposit them
+  if (MSRC && cta_msrc(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x)) {
     h_march<PML, false, -1, true>(p, j, k, i0, i1, first_step);
     return;
   }
@@ -1066,16 +1066,16 @@ __global__ void __launch_bounds__(256, 5) e_generic(const __grid_constant__ Step
 // Generic kernels of a lossy run (a D or B conductivity): the same column march with
 // the conductive curl forms; the conductivity volumes and tables come as a second
 // parameter block so the lossless kernels' parameters stay as they are.
-template <bool PML>
-__global__ void __launch_bounds__(256) h_generic_cond(const __grid_constant__ StepParams p,
+template <bool PML, bool MSRC>
+__global__ void __launch_bounds__(256, 4) h_generic_cond(const __grid_constant__ StepParams p,
                                                       const __grid_constant__ mgb_conductivity cp,
                                                       int first_step, int xchunk) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
   const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
-  // the CTAs that hold magnetic source points deposit them (the others skip the test)
-  if (cta_msrc(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x)) {
+  // a run with magnetic sources: the CTAs that hold source points deposit them
+  if (MSRC && cta_msrc(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x)) {
     h_march<PML, true, -1, true>(p, j, k, i0, i1, first_step, &cp);
     return;
   }
@@ -1090,7 +1090,7 @@ __global__ void __launch_bounds__(256) h_generic_cond(const __grid_constant__ St
 }
 
 template <bool PML>
-__global__ void __launch_bounds__(256) e_generic_cond(const __grid_constant__ StepParams p,
+__global__ void __launch_bounds__(256, 4) e_generic_cond(const __grid_constant__ StepParams p,
                                                       const __grid_constant__ mgb_conductivity cp,
                                                       int parity, int xchunk) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2443,10 +2443,13 @@ int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s) {
     const int xc = hc.xchunk;
     const dim3 grid((p.nz + block.x - 1) / block.x, (p.ny + block.y - 1) / block.y, (p.nx + xc - 1) / xc);
     p.l2pf = hc.l2pf ? 1 : 0;  // per half; the launch takes the parameters by value
+    const bool msrc = p.nsrc_h > 0;  // the H kernels with the magnetic deposit compiled in
     if (sim->has_cond) {
       if (part == 0) {
-        if (pml) launch_step(sim, h_generic_cond<true>, grid, block, 0, s, p, sim->cond, (int)(n == 0), xc);
-        else launch_step(sim, h_generic_cond<false>, grid, block, 0, s, p, sim->cond, (int)(n == 0), xc);
+        if (pml && msrc) launch_step(sim, h_generic_cond<true, true>, grid, block, 0, s, p, sim->cond, (int)(n == 0), xc);
+        else if (pml) launch_step(sim, h_generic_cond<true, false>, grid, block, 0, s, p, sim->cond, (int)(n == 0), xc);
+        else if (msrc) launch_step(sim, h_generic_cond<false, true>, grid, block, 0, s, p, sim->cond, (int)(n == 0), xc);
+        else launch_step(sim, h_generic_cond<false, false>, grid, block, 0, s, p, sim->cond, (int)(n == 0), xc);
       } else {
         if (pml) launch_step(sim, e_generic_cond<true>, grid, block, 0, s, p, sim->cond, (int)(n & 1), xc);
         else launch_step(sim, e_generic_cond<false>, grid, block, 0, s, p, sim->cond, (int)(n & 1), xc);
@@ -2455,15 +2458,19 @@ int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s) {
     }
     if (hc.prefetch) {
       if (part == 0) {
-        if (pml) launch_step(sim, h_generic_pf<true>, grid, block, 0, s, p, (int)(n == 0), xc);
-        else launch_step(sim, h_generic_pf<false>, grid, block, 0, s, p, (int)(n == 0), xc);
+        if (pml && msrc) launch_step(sim, h_generic_pf<true, true>, grid, block, 0, s, p, (int)(n == 0), xc);
+        else if (pml) launch_step(sim, h_generic_pf<true, false>, grid, block, 0, s, p, (int)(n == 0), xc);
+        else if (msrc) launch_step(sim, h_generic_pf<false, true>, grid, block, 0, s, p, (int)(n == 0), xc);
+        else launch_step(sim, h_generic_pf<false, false>, grid, block, 0, s, p, (int)(n == 0), xc);
       } else {
         if (pml) launch_step(sim, e_generic_pf<true>, grid, block, 0, s, p, (int)(n & 1), xc);
         else launch_step(sim, e_generic_pf<false>, grid, block, 0, s, p, (int)(n & 1), xc);
       }
     } else if (part == 0) {
-      if (pml) launch_step(sim, h_generic<true>, grid, block, 0, s, p, (int)(n == 0), xc);
-      else launch_step(sim, h_generic<false>, grid, block, 0, s, p, (int)(n == 0), xc);
+      if (pml && msrc) launch_step(sim, h_generic<true, true>, grid, block, 0, s, p, (int)(n == 0), xc);
+      else if (pml) launch_step(sim, h_generic<true, false>, grid, block, 0, s, p, (int)(n == 0), xc);
+      else if (msrc) launch_step(sim, h_generic<false, true>, grid, block, 0, s, p, (int)(n == 0), xc);
+      else launch_step(sim, h_generic<false, false>, grid, block, 0, s, p, (int)(n == 0), xc);
     } else {
       if (pml) launch_step(sim, e_generic<true>, grid, block, 0, s, p, (int)(n & 1), xc);
       else launch_step(sim, e_generic<false>, grid, block, 0, s, p, (int)(n & 1), xc);

@@ -42,6 +42,8 @@ class FluxAdjoint:
             raise Unsupported("the adjoint step does not carry susceptibility poles")
         if driver.has_conductivity:
             raise Unsupported("the adjoint step does not carry a conductivity")
+        if driver.complex_fields:
+            raise Unsupported("the adjoint gradient takes real fields (force_complex_fields=False)")
         if driver.engine is not None:
             raise RuntimeError("the adjoint problem needs a driver that has not been stepped")
         if steps < 1 or checkpoint_every < 1:

@@ -193,17 +193,13 @@ class _Monitor:
             raise ValueError(f"monitor accumulators need {size} bytes, above the 4 GiB budget")
 
     def raw(self, component: str) -> np.ndarray:
-        """Complex128 host copy of one component's accumulator, shape ``(nf,) + region``."""
+        """Complex64 host copy of one component's accumulator, shape ``(nf,) + region``."""
         if component not in self.components:
             raise ValueError(f"component {component!r} is not monitored ({self.components})")
-        if self.accumulator is None:
+        if self._engine is None:
             return np.zeros((self.num_frequencies,) + self.region_shape, dtype=np.complex64)
-        index = self.components.index(component)
-        if self._engine is not None:
-            self._engine.flush_dft()
-        host = self.accumulator[index].detach().cpu().numpy()  # [nf][2][cells]
-        values = host[:, 0, :] + 1j * host[:, 1, :]
-        return values.astype(np.complex64).reshape((self.num_frequencies,) + self.region_shape)
+        values = self._engine.read_accumulator(self, self.components.index(component))
+        return values.reshape((self.num_frequencies,) + self.region_shape)
 
 
 class DFTMonitor(_Monitor):
@@ -307,7 +303,7 @@ class FluxMonitor(_Monitor):
 
     def _tangential(self) -> dict:
         """The accumulated tangential transforms (complex64, ``(nf,) + region``)."""
-        if self.accumulator is not None:
+        if self._engine is not None:
             return {name: self.raw(name) for name in self.components}
         pending = getattr(self, "_pending", None)
         if pending is not None:
@@ -355,20 +351,14 @@ class FluxMonitor(_Monitor):
         for name in self.components:
             block = record.E[name] if name in record.E else record.H[name]
             incoming[name] = np.ascontiguousarray(np.asarray(block), dtype=np.complex64)
-        if self.accumulator is None:
+        if self._engine is None:
             self._pending = incoming  # written into the accumulators when the run freezes
             return
-        self._engine.flush_dft()
         self._write(incoming)
 
     def _write(self, blocks: dict) -> None:
-        import torch
-
-        cells = self.cells
         for q, name in enumerate(self.components):
-            values = blocks[name].reshape(self.num_frequencies, cells)
-            pair = np.stack([values.real, values.imag], axis=1).astype(np.float32)  # [nf][2][cells]
-            self.accumulator[q].copy_(torch.from_numpy(pair))
+            self._engine.write_accumulator(self, q, blocks[name].reshape(self.num_frequencies, self.cells))
 
     def scale_dfts(self, scale: complex) -> None:
         """Multiply every accumulated transform by ``scale`` (``dft_flux::scale_dfts``:
@@ -376,7 +366,7 @@ class FluxMonitor(_Monitor):
         factor = complex(scale)
         blocks = self._tangential()
         scaled = {name: (block * factor).astype(np.complex64) for name, block in blocks.items()}
-        if self.accumulator is None:
+        if self._engine is None:
             self._pending = scaled
             return
         self._write(scaled)
@@ -391,9 +381,9 @@ class FluxMonitor(_Monitor):
     def reset(self) -> None:
         """Zero every accumulator (buffered samples included)."""
         self._pending = None
-        if self.accumulator is not None:
-            self._engine.flush_dft()
-            self.accumulator.zero_()
+        if self._engine is not None:
+            for q in range(len(self.components)):
+                self._engine.write_accumulator(self, q, None)
 
 
 def automatic_decimation(dt: float, monitor_frequencies: Sequence[float], sources) -> int:

@@ -4,8 +4,8 @@ Mirrors ``meep_gpu/driver.py``'s ``FdtdDriver`` (constructor :810, ``set_epsilon
 :1170, ``add_susceptibility`` :1531, ``setup_pml`` :2155, ``add_source`` :2567,
 ``add_dft_monitor`` :2783, ``add_flux_monitor`` :3001, ``step`` :3419, ``run`` :3667,
 ``get_field`` :4056, ``set_conductivity`` :1649, ``set_b_conductivity`` :1752,
-``set_absorber`` :1863) for the configurations this engine steps: 3-D, real float32
-fields, metallic or periodic (k = 0) boundaries, no mirror symmetry, isotropic or
+``set_absorber`` :1863) for the configurations this engine steps: 3-D, real float32 or
+complex64 fields, metallic or periodic (k = 0) boundaries, no mirror symmetry, isotropic or
 diagonal chi1inv, Lorentz/Drude poles, D and B conductivity (material and
 ``mp.Absorber``), electric sources and DFT/flux monitors.
 Anything else is refused by name when it is asked for, never approximated.
@@ -65,9 +65,6 @@ class FdtdDriver:
                  gpu_id: int = 0, launch_shape: Optional[Tuple[int, int, int]] = None,
                  kernels: Optional[Tuple[int, int, int, int]] = None,
                  dft_accumulation: Optional[str] = None):
-        if force_complex_fields:
-            raise Unsupported("complex fields are not stepped by this engine; pass "
-                              "force_complex_fields=False (real float32 fields)")
         if tuple(symmetry):
             raise Unsupported("mirror symmetry is not stepped by this engine")
         if any(float(k) != 0.0 for k in k_point):
@@ -78,6 +75,9 @@ class FdtdDriver:
             raise Unsupported("out-of-plane beta and BFAST are not stepped by this engine")
         del m, accurate_fields_near_cylorigin, prefer_gpu
         self.grid = Grid(cell_size, resolution, courant, boundaries)
+        # complex64 fields (the reference's default): at k = 0 the real and imaginary
+        # parts step as two real runs (engine.ComplexEngine)
+        self.complex_fields = bool(force_complex_fields)
         self.gpu_id = int(gpu_id)
         self.launch_shape = launch_shape
         # (family, block_z, block_y, x_chunk): 1 the TMA tile kernels, 0 the generic ones;
@@ -280,7 +280,7 @@ class FdtdDriver:
                         _as_xyz("center", spec.get("center", (0.0, 0.0, 0.0))),
                         _as_xyz("size", spec.get("size", (0.0, 0.0, 0.0))),
                         waveform, complex(spec.get("amplitude", 1.0)), spec.get("amp_func"))
-        if complex(spec.get("amplitude", 1.0)).imag != 0.0:
+        if complex(spec.get("amplitude", 1.0)).imag != 0.0 and not self.complex_fields:
             raise Unsupported("a complex source amplitude needs complex fields")
         if self.pml is not None and self.has_conductivity:
             self._require_source_clear_of_conductive_pml(source.center, source.size, self.pml.faces)
@@ -364,10 +364,11 @@ class FdtdDriver:
             return self.engine
         import torch
 
-        from .engine import Engine
+        from .engine import ComplexEngine, Engine
         self.prepare()
         device = torch.device("cuda", self.gpu_id)
-        self.engine = Engine(self.grid, self.pml, self._inv_eps, self._poles, self._sources,
+        engine_cls = ComplexEngine if self.complex_fields else Engine
+        self.engine = engine_cls(self.grid, self.pml, self._inv_eps, self._poles, self._sources,
                              list(self._flux_monitors) + list(self._dft_monitors), device=device,
                              stream=stream, launch_shape=self.launch_shape, kernels=self.kernels,
                              autotune=autotune,
@@ -473,7 +474,7 @@ class FdtdDriver:
         if component not in FIELD_COMPONENTS:
             raise ValueError(f"unknown component {component!r}; supported {FIELD_COMPONENTS}")
         if self.engine is None:
-            return np.zeros(self.grid.shape, dtype=np.float32)
+            return np.zeros(self.grid.shape, dtype=np.complex64 if self.complex_fields else np.float32)
         name = {"D": "D", "E": "E", "B": "B", "H": "H"}[component[0]] + component[1]
         raw = self.engine.field(name).detach().cpu().numpy().copy()
         if not cell_centered:
@@ -496,13 +497,13 @@ class FdtdDriver:
         if len(axes) == 1:
             o = [0, 0, 0]
             o[axes[0]] = 1
-            return (np.float32(0.5) * (view((0, 0, 0)) + view(o))).astype(np.float32)
+            return (np.float32(0.5) * (view((0, 0, 0)) + view(o))).astype(raw.dtype)
         a0, a1 = axes
         o1 = [0, 0, 0]; o1[a0] = 1
         o2 = [0, 0, 0]; o2[a1] = 1
         o3 = [0, 0, 0]; o3[a0] = 1; o3[a1] = 1
         total = ((view((0, 0, 0)) + view(o1)) + view(o2)) + view(o3)
-        return (np.float32(0.25) * total).astype(np.float32)
+        return (np.float32(0.25) * total).astype(raw.dtype)
 
     def get_flux_spectrum(self, monitor: FluxMonitor) -> np.ndarray:
         return monitor.get_flux_spectrum()

@@ -65,6 +65,15 @@ def _ptr(t: Optional[torch.Tensor]) -> Optional[int]:
     return None if t is None else t.data_ptr()
 
 
+def _fill_accumulator(acc: torch.Tensor, q: int, values: Optional[np.ndarray]) -> None:
+    """Write complex ``values [nf][cells]`` (None: zeros) into ``acc[q]`` ([nf][re, im][cells])."""
+    if values is None:
+        acc[q].zero_()
+        return
+    pair = np.stack([values.real, values.imag], axis=1).astype(np.float32)
+    acc[q].copy_(torch.from_numpy(np.ascontiguousarray(pair)))
+
+
 class Engine:
     """One simulation resident on one GPU."""
 
@@ -75,10 +84,15 @@ class Engine:
                  launch_shape: Optional[Tuple[int, int, int]] = None, autotune: bool = True,
                  kernels: Optional[Tuple[int, int, int, int]] = None,
                  dft_accumulation: Optional[str] = None,
-                 conductivity: Optional[Dict[str, Optional[np.ndarray]]] = None):
+                 conductivity: Optional[Dict[str, Optional[np.ndarray]]] = None,
+                 part: str = "real", own_monitors: bool = True):
         if not torch.cuda.is_available():
             raise RuntimeError("meep_gpu_gb300 steps on a CUDA GPU and none is visible")
         self.lib = _lib.load()
+        # "real": the fields a real run steps (or a complex run's real parts), driven by
+        # real(A); "imag": a complex run's imaginary parts, driven by imag(A)
+        self.part = part
+        self.own_monitors = own_monitors
         self.grid = grid
         self.pml = pml if (pml is not None and pml.is_active) else None
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
@@ -310,11 +324,14 @@ class Engine:
             if isinstance(monitor, FluxMonitor):
                 weights = torch.from_numpy(monitor.weights.reshape(-1).copy()).to(self.device)
             self.monitor_tensors.append((omega, acc, weights))
+            if not self.own_monitors:
+                continue
             monitor.accumulator = acc
             monitor._engine = self
             pending = getattr(monitor, "_pending", None)
             if pending is not None:  # transforms loaded before the run froze
-                monitor._write(pending)
+                for q, name in enumerate(monitor.components):
+                    _fill_accumulator(acc, q, pending[name].reshape(monitor.num_frequencies, -1))
                 monitor._pending = None
 
     def _setup_dft_buffers(self, mode: Optional[str]) -> None:
@@ -344,6 +361,20 @@ class Engine:
                                                              self.dft_scratch.data_ptr(), nbytes))
             self.dft_samples[index] = samples
 
+    def read_accumulator(self, monitor, q: int) -> np.ndarray:
+        """Complex64 host copy ``[nf][cells]`` of component ``q`` of a monitor (buffered
+        samples contracted first)."""
+        self.flush_dft()
+        acc = self.monitor_tensors[self.monitors.index(monitor)][1]
+        host = acc[q].detach().cpu().numpy()  # [nf][2][cells]
+        return (host[:, 0, :] + 1j * host[:, 1, :]).astype(np.complex64)
+
+    def write_accumulator(self, monitor, q: int, values: Optional[np.ndarray]) -> None:
+        """Replace component ``q`` of a monitor by ``values`` (``[nf][cells]``; None: zero)."""
+        self.flush_dft()
+        acc = self.monitor_tensors[self.monitors.index(monitor)][1]
+        _fill_accumulator(acc, q, values)
+
     def flush_dft(self) -> None:
         """Add buffered DFT samples to the accumulators; the current stream then sees them."""
         stream = self.stream if self.stream is not None else torch.cuda.current_stream(self.device)
@@ -368,7 +399,7 @@ class Engine:
                 and first_step + steps <= self._words_first + self._words_steps):
             return
         count = max(steps, SOURCE_WINDOW)
-        host = deposit_words(self.sources, first_step, count, self.grid.dt, self.src_scales)
+        host = deposit_words(self.sources, first_step, count, self.grid.dt, self.src_scales, self.part)
         # The previous table may still be read by queued kernels: keep it alive until
         # the stream has passed them.
         stream = self.stream if self.stream is not None else torch.cuda.current_stream(self.device)
@@ -575,3 +606,104 @@ class Engine:
             self.close()
         except Exception:
             pass
+
+
+class ComplexEngine:
+    """Complex fields at k = 0 (the reference's default ``force_complex_fields=True``).
+
+    With every coefficient real and no Bloch phase, the real and imaginary parts step
+    independently (the reference's complex run's real part is, word for word, the real
+    run's): two real engines over the same coefficient tables, the real one driven by
+    real(A) and the imaginary one by imag(A) (``sources.py:1357``: ``f[c][0] -= real(A);
+    f[c][1] -= imag(A)``). A monitor's complex transform is the sum of the two parts'
+    transforms, ``acc = acc_re + i * acc_im``, formed when it is read.
+    """
+
+    def __init__(self, grid: Grid, pml: Optional[PML], inv_eps, poles, sources, monitors, device=None,
+                 stream=None, launch_shape=None, autotune: bool = True, kernels=None,
+                 dft_accumulation: Optional[str] = None, conductivity=None):
+        self.re = Engine(grid, pml, inv_eps, poles, sources, monitors, device=device, stream=stream,
+                         launch_shape=launch_shape, autotune=autotune, kernels=kernels,
+                         dft_accumulation=dft_accumulation, conductivity=conductivity, part="real")
+        self.im = Engine(grid, pml, inv_eps, poles, sources, monitors, device=device, stream=stream,
+                         launch_shape=launch_shape, autotune=False,
+                         kernels=self.re.choice if self.re.choice is not None else kernels,
+                         dft_accumulation=dft_accumulation, conductivity=conductivity, part="imag",
+                         own_monitors=False)
+        self.grid = grid
+        self.device = self.re.device
+        self.monitors = self.re.monitors
+        self.lib = self.re.lib
+        self.dft_accumulation = self.re.dft_accumulation
+        for monitor in self.monitors:
+            monitor._engine = self
+
+    # --- the Engine calls the driver and the monitors make ---------------------------------
+    @property
+    def choice(self):
+        return self.re.choice
+
+    @property
+    def uses_tiles(self) -> bool:
+        return self.re.uses_tiles
+
+    def select(self, choice) -> None:
+        self.re.select(choice)
+        self.im.select(choice)
+
+    def ensure_source_words(self, first_step: int, steps: int) -> None:
+        self.re.ensure_source_words(first_step, steps)
+        self.im.ensure_source_words(first_step, steps)
+
+    def step(self, first_step: int, nsteps: int) -> None:
+        self.re.step(first_step, nsteps)
+        self.im.step(first_step, nsteps)
+
+    def launch(self, step: int, part: int, stream=None) -> None:
+        self.re.launch(step, part, stream)
+        self.im.launch(step, part, stream)
+
+    def flush_dft(self) -> None:
+        self.re.flush_dft()
+        self.im.flush_dft()
+
+    def read_accumulator(self, monitor, q: int) -> np.ndarray:
+        real = self.re.read_accumulator(monitor, q)
+        imag = self.im.read_accumulator(monitor, q)
+        return (real + np.complex64(1j) * imag).astype(np.complex64)
+
+    def write_accumulator(self, monitor, q: int, values: Optional[np.ndarray]) -> None:
+        self.re.write_accumulator(monitor, q, values)
+        self.im.write_accumulator(monitor, q, None)
+
+    def flux_spectrum(self, monitor: FluxMonitor) -> np.ndarray:
+        """``sum w * Re(Ea conj(Hb) - Eb conj(Ha)) * dA * weight`` of the complex transforms,
+        summed in float64 on the device."""
+        self.flush_dft()
+        index = self.monitors.index(monitor)
+        parts = []
+        for engine in (self.re, self.im):
+            acc = engine.monitor_tensors[index][1].to(torch.float64)  # [4][nf][2][cells]
+            parts.append(torch.complex(acc[:, :, 0, :], acc[:, :, 1, :]))
+        total = parts[0] + 1j * parts[1]
+        ea, eb, ha, hb = total[0], total[1], total[2], total[3]
+        weights = self.re.monitor_tensors[index][2].to(torch.float64)
+        flux = torch.real(ea * torch.conj(hb) - eb * torch.conj(ha)) @ weights
+        return flux.cpu().numpy() * monitor.measure * monitor.weight
+
+    def field(self, name: str) -> torch.Tensor:
+        return torch.complex(self.re.field(name), self.im.field(name))
+
+    def device_status(self) -> int:
+        return self.re.device_status() | self.im.device_status()
+
+    def nonfinite(self) -> bool:
+        return self.re.nonfinite() or self.im.nonfinite()
+
+    def algorithmic_bytes(self) -> Dict[str, int]:
+        a, b = self.re.algorithmic_bytes(), self.im.algorithmic_bytes()
+        return {k: a[k] + b[k] for k in a}
+
+    def close(self) -> None:
+        self.re.close()
+        self.im.close()

@@ -32,6 +32,7 @@ import numpy as np
 import torch
 
 from . import _lib
+from .grid import Unsupported
 from .sources import deposit_words
 
 SIDES = (32, 48, 64, 96, 128)
@@ -260,6 +261,8 @@ class BatchServer:
     def admit(self, job: _Job, now: float) -> None:
         """Make a job's device state (on the setup stream) and put it in a free slot."""
         slot = self.slots.index(None)
+        if job.driver.complex_fields:
+            raise Unsupported("a batched slot steps real fields (force_complex_fields=False)")
         with torch.cuda.stream(self.setup_stream):
             # the batch accumulates its monitors step by step (dft_batched)
             job.engine = job.driver.freeze(stream=self.stream, autotune=False, dft_accumulation="direct")

@@ -422,7 +422,7 @@ def current_sequence(waveform, dt: float, first: int, steps: int, offset: float 
 
 
 def deposit_words(sources: Sequence[Source], first_step: int, steps: int, dt: float,
-                  scales: Optional[np.ndarray] = None) -> np.ndarray:
+                  scales: Optional[np.ndarray] = None, part: str = "real") -> np.ndarray:
     """Float64 subtrahends ``A[step][point]`` for steps ``first_step .. first_step+steps-1``.
 
     ``A = ((amp_re*c_re) - (amp_im*c_im))*dt`` with each product and the difference
@@ -430,8 +430,12 @@ def deposit_words(sources: Sequence[Source], first_step: int, steps: int, dt: fl
     ``(+0, +0)``. Points are laid out source by source in table order, the order the
     device deposits them. ``scales`` (one float64 per point) multiplies each word last:
     a lossy target component's ``condinv`` at the point (reference ``sources.py:1357``
-    ``_deposit``, MEEP's ``A = current * dt * cndinv[i]``).
+    ``_deposit``, MEEP's ``A = current * dt * cndinv[i]``). ``part="imag"`` gives the
+    words a complex run subtracts from its imaginary fields,
+    ``((amp_re*c_im) + (amp_im*c_re))*dt``.
     """
+    if part not in ("real", "imag"):
+        raise ValueError("part is 'real' or 'imag'")
     count = sum(len(s.cells) for s in sources)
     out = np.zeros((steps, count), dtype=np.float64)
     column = 0
@@ -440,7 +444,10 @@ def deposit_words(sources: Sequence[Source], first_step: int, steps: int, dt: fl
         c_re, c_im = seq[:, 0], seq[:, 1]
         plus_zero = ((c_re == 0.0) & ~np.signbit(c_re)) & ((c_im == 0.0) & ~np.signbit(c_im))
         for amp in source.amps:
-            value = ((amp.real * c_re) - (amp.imag * c_im)) * dt
+            if part == "real":
+                value = ((amp.real * c_re) - (amp.imag * c_im)) * dt
+            else:
+                value = ((amp.real * c_im) + (amp.imag * c_re)) * dt
             value[plus_zero] = 0.0
             out[:, column] = value
             column += 1

@@ -211,19 +211,25 @@ def problem_from_driver(driver) -> Problem:
                    tables64=tables64, member=member, inv_eps32=inv32, inv_eps64=inv64,
                    poles=poles, src_cells=np.array(cells, dtype=np.int64),
                    src_comps=np.array(comps, dtype=np.int32),
-                   words=lambda first, steps: deposit_words(sources, first, steps, grid.dt, scales),
+                   words=lambda first, steps, part="real": deposit_words(sources, first, steps, grid.dt,
+                                                                           scales, part),
                    monitors=monitors, conductivity=conductivity,
                    faces=tuple(pml.faces) if pml is not None else ((0.0, 0.0),) * 3)
 
 
 class Oracle:
-    """One run of the CPU oracle over a :class:`Problem`, in ``precision`` f32 or f64."""
+    """One run of the CPU oracle over a :class:`Problem`, in ``precision`` f32 or f64.
 
-    def __init__(self, problem: Problem, precision: str = "f32"):
+    ``part="imag"`` runs a complex run's imaginary fields (driven by imag(A)): at k = 0
+    the two parts of a complex run step independently, so a complex run is two real runs.
+    """
+
+    def __init__(self, problem: Problem, precision: str = "f32", part: str = "real"):
         if precision not in _DTYPE:
             raise ValueError("precision is 'f32' or 'f64'")
         self.problem = problem
         self.precision = precision
+        self.part = part
         self.lib = load()
         dtype = _DTYPE[precision]
         self.dtype = dtype
@@ -315,7 +321,7 @@ class Oracle:
 
     def run(self, nsteps: int) -> None:
         nsrc = int(self.problem.src_cells.size)
-        words = self.problem.words(self.step_count, nsteps) if nsrc else None
+        words = self.problem.words(self.step_count, nsteps, self.part) if nsrc else None
         empty = np.zeros(1)
         for t in range(nsteps):
             row = np.ascontiguousarray(words[t]) if nsrc else empty
@@ -353,3 +359,22 @@ class Oracle:
         mon = self.problem.monitors[index]
         acc = self.accumulators[index][mon.components.index(component)]
         return acc[:, 0] + 1j * acc[:, 1]
+
+
+def complex_accumulator(real: "Oracle", imag: "Oracle", index: int) -> np.ndarray:
+    """A complex run's transform ``acc_re + i * acc_im`` from its two parts' oracles:
+    complex ``[ncomp][nf][cells]``."""
+    parts = []
+    for oracle in (real, imag):
+        acc = oracle.accumulators[index].astype(np.float64)
+        parts.append(acc[:, :, 0] + 1j * acc[:, :, 1])
+    return parts[0] + 1j * parts[1]
+
+
+def complex_flux_spectrum(real: "Oracle", imag: "Oracle", index: int) -> np.ndarray:
+    """``sum w * Re(Ea conj(Hb) - Eb conj(Ha)) * dA * weight`` of a complex run."""
+    mon = real.problem.monitors[index]
+    total = complex_accumulator(real, imag, index)
+    ea, eb, ha, hb = total[0], total[1], total[2], total[3]
+    w = mon.weights.astype(np.float64)
+    return (np.real(ea * np.conj(hb) - eb * np.conj(ha)) @ w) * mon.measure * mon.weight

@@ -41,6 +41,13 @@ CASES = {
     # the magnetic deposit carries B's condinv.
     "magnetic": dict(n=(14, 12, 16), pml=3, steps=60, magnetic=True),
     "magnetic_lossy": dict(n=(13, 14, 12), pml=0, steps=60, magnetic=True, conductivity="absorber_b"),
+    # Complex fields (the reference's default) at k = 0: the mixed case's sources (a
+    # complex-amplitude one added), poles and monitors, periodic y; and with a lossy
+    # PML run and magnetic sources.
+    "complex_mixed": dict(n=(13, 15, 12), pml={"x": 3, "z": 2}, steps=45, mixed=True, complex=True,
+                          boundaries=("metallic", "periodic", "metallic")),
+    "complex_cond": dict(n=(14, 12, 16), pml=3, steps=50, conductivity="band", magnetic=True,
+                         complex=True),
 }
 
 # The 80^3 sphere-under-PML workload (resolution 10, 10-cell PML, eps 4 sphere of radius
@@ -54,7 +61,8 @@ def build_case(driver_cls, susceptibility_cls, case: dict, reference: bool = Fal
     n = case["n"]
     lengths = tuple(v / res for v in n)
     boundaries = case.get("boundaries", "metallic")
-    d = driver_cls(cell_size=lengths, resolution=res, courant=0.5, force_complex_fields=False,
+    d = driver_cls(cell_size=lengths, resolution=res, courant=0.5,
+                   force_complex_fields=bool(case.get("complex", False)),
                    boundaries=boundaries, **({"prefer_gpu": False} if reference else {}))
     if case["pml"]:
         d.setup_pml(case["pml"])
@@ -98,6 +106,9 @@ def build_case(driver_cls, susceptibility_cls, case: dict, reference: bool = Fal
                       "size": (0, 0.4, 0), "frequency": 0.5, "fwidth": 0.4})
         d.add_source({"source_type": "continuous", "component": "Ey", "center": (-0.2, 0.21, -0.1),
                       "size": (0, 0, 0), "frequency": 0.3, "amplitude": 0.5})
+        if case.get("complex"):
+            d.add_source({"source_type": "gaussian", "component": "Ez", "center": (0.15, -0.1, 0.0),
+                          "size": (0, 0, 0.3), "frequency": 0.4, "fwidth": 0.3, "amplitude": 0.6 - 0.8j})
         flux.append(d.add_flux_monitor(fcen=0.3, df=0.2, nfreq=3, center=(0, 0.4, 0),
                                        size=(0.8, 0, 0.7), decimation_factor=0))
         flux.append(d.add_flux_monitor(frequencies=[0.2, 0.35], center=(0.05, -0.05, 0.25),

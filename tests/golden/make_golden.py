@@ -54,7 +54,8 @@ def record_fields(name: str, case: dict) -> None:
     driver.run(num_steps=case["steps"])
     out = {}
     for c in COMPONENTS:
-        out[c] = np.asarray(driver.get_field(c, cell_centered=False), dtype=np.float32)
+        words = np.asarray(driver.get_field(c, cell_centered=False))
+        out[c] = words.astype(np.complex64 if np.iscomplexobj(words) else np.float32)
     for index, monitor in enumerate(flux):
         out[f"flux{index}"] = np.asarray(monitor.get_flux_spectrum(), dtype=np.float64)
     for index, monitor in enumerate(dft):
@@ -62,7 +63,7 @@ def record_fields(name: str, case: dict) -> None:
             out[f"dft{index}_{c}"] = np.asarray(monitor._dft[c], dtype=np.complex64)
     for m, state in enumerate(driver.fields.polarizations):
         for c, array in state.P.items():
-            out[f"P{m}_{c}"] = np.asarray(array, dtype=np.float32)
+            out[f"P{m}_{c}"] = np.asarray(array, dtype=np.complex64 if np.iscomplexobj(array) else np.float32)
     np.savez_compressed(HERE / f"fields_{name}.npz", **out)
     print(name, "written")
 

@@ -168,7 +168,7 @@ def test_overlapping_pml_chunks_are_refused():
 
 
 # --- oracle ---------------------------------------------------------------------------
-@pytest.mark.parametrize("name", LOSSY)
+@pytest.mark.parametrize("name", [n for n in LOSSY if not CASES[n].get("complex")])
 def test_float64_oracle_agrees_to_single_precision(name):
     case = CASES[name]
     gold = golden_io.fields(name)

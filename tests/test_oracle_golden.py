@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from meep_gpu_gb300 import FdtdDriver, Susceptibility
-from oracle.oracle import Oracle, problem_from_driver
+from oracle.oracle import Oracle, complex_accumulator, complex_flux_spectrum, problem_from_driver
 from tests.golden.cases import CASES, SPHERE80, build_case
 from tests import golden_io
 
@@ -27,11 +27,50 @@ def run_case(case, precision="f32", steps=None):
     return driver, oracle
 
 
+def run_complex_case(case, precision="f32"):
+    """A complex case at k = 0 as two real oracle runs (real parts, imaginary parts)."""
+    driver, flux, dft = build_case(FdtdDriver, Susceptibility, case)
+    problem = problem_from_driver(driver)
+    parts = []
+    for part in ("real", "imag"):
+        oracle = Oracle(problem, precision, part)
+        oracle.run(case["steps"])
+        parts.append(oracle)
+    return driver, parts[0], parts[1]
+
+
+@pytest.mark.parametrize("name", sorted(n for n, c in CASES.items() if c.get("complex")))
+def test_complex_case_is_two_real_oracle_runs(name):
+    """The reference's complex run at k = 0: its real words are one float32 oracle run
+    driven by real(A), its imaginary words another driven by imag(A); its transforms are
+    the two runs' sums, acc_re + i acc_im."""
+    case = CASES[name]
+    gold = golden_io.fields(name)
+    driver, re, im = run_complex_case(case)
+    for c in FIELDS:
+        assert np.array_equal(re.field(c), gold[c].real), f"{name} {c} real"
+        assert np.array_equal(im.field(c), gold[c].imag), f"{name} {c} imag"
+    nflux = len(driver._flux_monitors)
+    for index in range(nflux):
+        expected = gold[f"flux{index}"]
+        got = complex_flux_spectrum(re, im, index)
+        assert np.max(np.abs(got - expected)) <= 1e-5 * np.max(np.abs(expected)), f"{name} flux {index}"
+    for index, monitor in enumerate(driver._dft_monitors):
+        total = complex_accumulator(re, im, nflux + index)
+        for q, c in enumerate(monitor.components):
+            expected = gold[f"dft{index}_{c}"].reshape(len(monitor.frequencies), -1)
+            assert np.max(np.abs(total[q] - expected)) <= 1e-5 * np.max(np.abs(expected)), f"{name} dft {c}"
+    for m, (pr, pi) in enumerate(zip(re.polarization, im.polarization)):
+        for q in pr:
+            expected = gold[f"P{m}_{'Ex Ey Ez'.split()[q]}"]
+            assert np.array_equal(pr[q][0], expected.real) and np.array_equal(pi[q][0], expected.imag)
+
+
 def oracle_field(oracle, name):
     return oracle.field(name)
 
 
-@pytest.mark.parametrize("name", sorted(CASES))
+@pytest.mark.parametrize("name", sorted(n for n, c in CASES.items() if not c.get("complex")))
 def test_float32_oracle_matches_reference_words(name):
     case = CASES[name]
     gold = golden_io.fields(name)

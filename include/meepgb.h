@@ -338,6 +338,11 @@ int mgb_batch_create(int32_t max_slots, int32_t max_work, int32_t max_dft_work,
  * mgb_batch_commit. The default is 32 x 4 x 4. */
 int mgb_batch_set_shape(mgb_batch* batch, int32_t block_z, int32_t block_y, int32_t x_chunk);
 
+/* Set the marches the step items run: family 2 (the prefetching marches, the default)
+ * or 4 (the generic marches with each item's x chunk prefetched into L2). Takes effect
+ * at the next mgb_batch_step (a captured graph is rebuilt). */
+int mgb_batch_set_family(mgb_batch* batch, int32_t family);
+
 /* Put a plan in a slot, to run steps 0 .. end_step-1 from its arrays' current words
  * (normally zero). words: device float64 [end_step][points] deposit words of its electric
  * sources from step 0 (NULL if it has none); the plan's own mgb_set_source_words table is

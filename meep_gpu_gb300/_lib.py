@@ -148,6 +148,7 @@ SIGNATURES = {
                                         ctypes.POINTER(ctypes.c_void_p)]),
     "mgb_batch_set_shape": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                            ctypes.c_int32]),
+    "mgb_batch_set_family": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "mgb_batch_set_slot": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
                                           ctypes.c_int64, ctypes.c_void_p]),
     "mgb_batch_clear_slot": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),

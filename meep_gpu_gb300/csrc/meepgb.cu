@@ -1726,10 +1726,11 @@ __device__ __forceinline__ void copy_to_shared(T* dst, const T* src) {
   for (int i = tid; i < n; i += blockDim.x * blockDim.y) to[i] = from[i];
 }
 
-// Register budget as the generic kernels' (48 per thread): more costs occupancy the
-// column march needs. `t` is the launch's step within the batch step call.
-template <int PART>
-__global__ void __launch_bounds__(256, 4) step_batched(const __grid_constant__ BatchTables tb, int t) {
+// GEN false: the prefetching marches (family 2, 64 registers); true: the generic marches
+// with each item's x chunk prefetched into L2 (family 4, 48 registers). `t` is the
+// launch's step within the batch step call.
+template <int PART, bool GEN>
+__global__ void __launch_bounds__(256, GEN ? 5 : 4) step_batched(const __grid_constant__ BatchTables tb, int t) {
   __shared__ StepParams sp;
   if ((int)blockIdx.x >= tb.counts[0]) return;
   const int4 w = tb.work[blockIdx.x];
@@ -1738,6 +1739,8 @@ __global__ void __launch_bounds__(256, 4) step_batched(const __grid_constant__ B
   const SlotState st = tb.state[w.x];
   const long long n = tb.n0[w.x] + t;
   if (!st.active || n >= st.end) return;  // uniform over the CTA
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) sp.l2pf = GEN ? 1 : 0;
   __syncthreads();
   const int k = w.y * (int)blockDim.x + (int)threadIdx.x;
   const int j = w.z * (int)blockDim.y + (int)threadIdx.y;
@@ -1748,15 +1751,27 @@ __global__ void __launch_bounds__(256, 4) step_batched(const __grid_constant__ B
                                       w.y * (int)blockDim.x, (int)blockDim.x) : 0;
   if (PART == 0) {
     const int first = n == 0;
-#define MGB_MARCH(AXV, PMLV) h_march_pf<PMLV, AXV>(sp, j, k, i0, i1, first)
-    MGB_AXES_SWITCH(axes, MGB_MARCH)
+    if (GEN) {
+#define MGB_MARCH(AXV, PMLV) h_march<PMLV, false, AXV>(sp, j, k, i0, i1, first)
+      MGB_AXES_SWITCH(axes, MGB_MARCH)
 #undef MGB_MARCH
+    } else {
+#define MGB_MARCH(AXV, PMLV) h_march_pf<PMLV, AXV>(sp, j, k, i0, i1, first)
+      MGB_AXES_SWITCH(axes, MGB_MARCH)
+#undef MGB_MARCH
+    }
   } else {
     const double* words = st.words + n * sp.nsrc;
     const int parity = (int)(n & 1);
-#define MGB_MARCH(AXV, PMLV) e_march_pf<PMLV, AXV>(sp, j, k, i0, i1, parity, words)
-    MGB_AXES_SWITCH(axes, MGB_MARCH)
+    if (GEN) {
+#define MGB_MARCH(AXV, PMLV) e_march<PMLV, false, AXV>(sp, j, k, i0, i1, parity, words)
+      MGB_AXES_SWITCH(axes, MGB_MARCH)
 #undef MGB_MARCH
+    } else {
+#define MGB_MARCH(AXV, PMLV) e_march_pf<PMLV, AXV>(sp, j, k, i0, i1, parity, words)
+      MGB_AXES_SWITCH(axes, MGB_MARCH)
+#undef MGB_MARCH
+    }
   }
 }
 
@@ -2666,6 +2681,7 @@ void mgb_destroy(mgb_sim* sim) { delete sim; }
 struct mgb_batch {
   int max_slots = 0, max_work = 0, max_dft_work = 0;
   int block_z = 32, block_y = 4;
+  int family = 2;  // the marches the step items run: 2 prefetching, 4 generic with L2 prefetch
   BatchTables dev = {};
   std::vector<StepParams> params;
   std::vector<SlotState> state;
@@ -2732,8 +2748,13 @@ int dft_grid(const mgb_batch* b) { return std::max(1, b->ndwork); }
 
 void batch_launch_step(mgb_batch* b, int t, cudaStream_t s) {
   const dim3 block(b->block_z, b->block_y, 1);
-  step_batched<0><<<step_grid(b), block, 0, s>>>(b->dev, t);
-  step_batched<1><<<step_grid(b), block, 0, s>>>(b->dev, t);
+  if (b->family == 4) {
+    step_batched<0, true><<<step_grid(b), block, 0, s>>>(b->dev, t);
+    step_batched<1, true><<<step_grid(b), block, 0, s>>>(b->dev, t);
+  } else {
+    step_batched<0, false><<<step_grid(b), block, 0, s>>>(b->dev, t);
+    step_batched<1, false><<<step_grid(b), block, 0, s>>>(b->dev, t);
+  }
   dft_batched<<<dft_grid(b), kDftItemCells, 0, s>>>(b->dev, t);
 }
 
@@ -2783,8 +2804,11 @@ int capture_graph(mgb_batch* b, int nsteps, cudaStream_t s) {
   cudaGraphGetNodes(b->graph_src, nullptr, &count);
   std::vector<cudaGraphNode_t> nodes(count);
   if (count > 0) cudaGraphGetNodes(b->graph_src, nodes.data(), &count);
-  const void* h_fn = reinterpret_cast<const void*>(step_batched<0>);
-  const void* e_fn = reinterpret_cast<const void*>(step_batched<1>);
+  const bool gen = b->family == 4;
+  const void* h_fn = gen ? reinterpret_cast<const void*>(step_batched<0, true>)
+                         : reinterpret_cast<const void*>(step_batched<0, false>);
+  const void* e_fn = gen ? reinterpret_cast<const void*>(step_batched<1, true>)
+                         : reinterpret_cast<const void*>(step_batched<1, false>);
   const void* d_fn = reinterpret_cast<const void*>(dft_batched);
   for (cudaGraphNode_t node : nodes) {
     cudaGraphNodeType type;
@@ -2864,6 +2888,19 @@ int mgb_batch_set_shape(mgb_batch* b, int32_t block_z, int32_t block_y, int32_t 
   return MGB_OK;
 }
 
+int mgb_batch_set_family(mgb_batch* b, int32_t family) {
+  if (b == nullptr) return fail(MGB_ERR_ARGUMENT, "null batch");
+  if (family != 2 && family != 4)
+    return fail(MGB_ERR_ARGUMENT,
+                "a batch steps with family 2 (prefetching marches) or 4 (generic marches, x chunk prefetched "
+                "into L2)");
+  if (family != b->family) {
+    b->family = family;
+    drop_graph(b);  // the captured launches name the other kernels
+  }
+  return MGB_OK;
+}
+
 int mgb_batch_set_slot(mgb_batch* b, int32_t slot, mgb_sim* sim, int64_t end_step, const double* words) {
   if (b == nullptr || sim == nullptr) return fail(MGB_ERR_ARGUMENT, "null batch or plan");
   if (slot < 0 || slot >= b->max_slots) return fail(MGB_ERR_ARGUMENT, "slot out of range");
@@ -2881,7 +2918,7 @@ int mgb_batch_set_slot(mgb_batch* b, int32_t slot, mgb_sim* sim, int64_t end_ste
   }
   b->params[slot] = sim->step;
   b->params[slot].src_words = nullptr;
-  b->params[slot].l2pf = 0;  // measured: no gain for the batch's mix of small grids
+  b->params[slot].l2pf = 0;  // the batch kernel sets it from the batch's family
   SlotState st = {};
   st.end = end_step;
   st.words = words;

@@ -39,10 +39,13 @@ SIDES = (32, 48, 64, 96, 128)
 RESOLUTION = 10
 PML_CELLS = 8
 NFREQ = 64
-# Launch shapes (block_z, block_y, x_chunk) the batch autotuner times.
-SHAPE_CANDIDATES = ((32, 4, 4), (32, 8, 4), (32, 4, 8), (32, 2, 8), (64, 2, 4), (64, 4, 4),
-                    (32, 8, 2), (32, 4, 2))
-_SHAPE_CACHE: Dict[tuple, Tuple[int, int, int]] = {}
+# Launch shapes (block_z, block_y, x_chunk, family) the batch autotuner times: family 2
+# the prefetching marches, 4 the generic marches with the x chunk prefetched into L2.
+SHAPE_CANDIDATES = ((32, 4, 4, 2), (32, 8, 4, 2), (32, 4, 8, 2), (32, 2, 8, 2), (64, 2, 4, 2),
+                    (64, 4, 4, 2), (32, 8, 2, 2), (32, 4, 2, 2),
+                    (32, 4, 4, 4), (32, 8, 4, 4), (32, 4, 8, 4), (32, 2, 8, 4), (64, 4, 4, 4),
+                    (32, 4, 2, 4))
+_SHAPE_CACHE: Dict[tuple, Tuple[int, ...]] = {}
 
 
 @dataclass
@@ -181,16 +184,20 @@ class BatchServer:
         self.handle = handle
         self.slots: List[Optional[_Job]] = [None] * self.max_slots
         self.draining: List[_Job] = []
-        self.shape = (32, 4, 4)
+        self.shape = (32, 4, 4, 2)
         if shape is not None:
             self.set_shape(shape)
         self.replays = 0
 
     # --- configuration ------------------------------------------------------------------
     def set_shape(self, shape: Sequence[int]) -> None:
-        """(block_z, block_y, x_chunk): the CTA's (z, y) cells and x planes per item."""
+        """(block_z, block_y, x_chunk[, family]): the CTA's (z, y) cells and x planes per
+        item, and the marches it runs (family 2 by default, or 4)."""
         shape = tuple(int(v) for v in shape)
-        _lib.check(self.lib, self.lib.mgb_batch_set_shape(self.handle, *shape))
+        if len(shape) == 3:
+            shape = shape + (2,)
+        _lib.check(self.lib, self.lib.mgb_batch_set_shape(self.handle, *shape[:3]))
+        _lib.check(self.lib, self.lib.mgb_batch_set_family(self.handle, shape[3]))
         self.shape = shape
 
     def autotune(self, sides: Sequence[int] = SIDES, steps: int = 8) -> Tuple[int, int, int]:

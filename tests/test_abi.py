@@ -57,6 +57,7 @@ def test_batch_entry_points_refuse_bad_arguments_without_a_gpu():
     assert "aligned" in _lib.last_error(lib)
     assert lib.mgb_batch_set_slot(None, 0, None, 10, None) == -1
     assert lib.mgb_batch_set_shape(None, 32, 4, 4) == -1
+    assert lib.mgb_batch_set_family(None, 2) == -1
     assert lib.mgb_batch_items(None, 0) == -1
     lib.mgb_batch_destroy(None)
 

@@ -158,9 +158,25 @@ typedef struct mgb_sim_desc {
    * (half-open). A run with magnetic sources is refused by the batch. */
   int32_t nsrc_magnetic;
   int32_t src_box_magnetic[6];
+  /* Bloch-periodic complex runs (k_point != 0): a complex run is two plans, one over the
+   * real parts (part 0) and one over the imaginary parts (part 1), stepped together by
+   * mgb_step_pair. bloch_axes bit a: axis a (periodic) carries the phase
+   * eikna[a] = bloch_phase[a][0] + i bloch_phase[a][1] (f(x + L) = eikna f(x)); the
+   * partner arrays are the other part's E and H. Zero bloch_axes: no phase. */
+  int32_t bloch_axes;
+  int32_t part;
+  double bloch_phase[3][2];
+  const float* partner_E[3];
+  const float* partner_H[3];
 } mgb_sim_desc;
 
 typedef struct mgb_sim mgb_sim;
+
+/* Step the two parts of a Bloch-periodic complex run together, steps [first_step,
+ * first_step + nsteps): per step the H half of `real` then of `imag`, the E half of each,
+ * then each one's monitors (a half of one part reads the other part's fields across the
+ * phased faces). Both plans need their source words installed. */
+int mgb_step_pair(mgb_sim* real, mgb_sim* imag, int64_t first_step, int32_t nsteps, void* stream);
 
 /* Version of this ABI (MGB_ABI_VERSION). */
 int mgb_abi_version(void);

@@ -94,6 +94,11 @@ class MgbSimDesc(ctypes.Structure):
         ("conductivity", ctypes.POINTER(MgbConductivity)),
         ("nsrc_magnetic", ctypes.c_int32),
         ("src_box_magnetic", ctypes.c_int32 * 6),
+        ("bloch_axes", ctypes.c_int32),
+        ("part", ctypes.c_int32),
+        ("bloch_phase", (ctypes.c_double * 2) * 3),
+        ("partner_E", ctypes.c_void_p * 3),
+        ("partner_H", ctypes.c_void_p * 3),
     ]
 
 
@@ -111,6 +116,8 @@ SIGNATURES = {
     "mgb_set_source_words": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                             ctypes.c_int64]),
     "mgb_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p]),
+    "mgb_step_pair": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
+                                     ctypes.c_void_p]),
     "mgb_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p]),
     "mgb_flux_spectrum": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.c_void_p]),

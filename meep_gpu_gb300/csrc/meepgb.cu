@@ -97,6 +97,15 @@ struct StepParams {
   int src_box_h[6];         // box of the magnetic points
   int32_t* status;
   int l2pf;  // 1: each thread prefetches its x chunk's field planes into L2 before marching
+  // Bloch phases (complex runs with k != 0): per axis 0 none, 1 copy, 2 negate, 3 the
+  // phase (re, im) rounded to float32; `part` 0 steps real parts, 1 imaginary parts;
+  // pE / pH the other part's E and H
+  int bloch;
+  int bmode[3];
+  float bre[3], bim[3];
+  int part;
+  const float* pE[3];
+  const float* pH[3];
 };
 
 // Tensor maps of the tile kernels (each 64-byte aligned, passed as __grid_constant__).
@@ -122,6 +131,14 @@ struct DftParams {
   const float* E[3];
   const float* H[3];
   mgb_monitor mon;
+  // Bloch phases as in StepParams (a sample at ladder index 0 of a phased axis is the
+  // stored word times conj(eikna) there)
+  int bloch;
+  int bmode[3];
+  float bre[3], bim[3];
+  int part;
+  const float* pE[3];
+  const float* pH[3];
 };
 
 __device__ __forceinline__ bool in_runs(const mgb_aux& a, int x) {
@@ -129,6 +146,23 @@ __device__ __forceinline__ bool in_runs(const mgb_aux& a, int x) {
 }
 
 __device__ __forceinline__ float ldgf(const float* base, int at) { return __ldg(base + at); }
+
+// A curl operand read across a Bloch-phased face at the same stored index (MEEP's
+// not-owned word): the stored word of this part (`own`) and of the other part
+// (`partner[c]`) times the axis's phase, conjugated for the word below the window
+// (`conj`), each product and sum rounded on its own: copy within 1e-13 of +1, negation
+// within 1e-13 of -1, else re = (a*re) - (b*im), im = (a*im) + (b*re).
+template <typename P>
+__device__ __forceinline__ float bloch_word(const P& p, int axis, bool conj, float own, const float* partner,
+                                            long long c) {
+  const int mode = p.bmode[axis];
+  if (mode == 2) return -own;
+  if (mode != 3) return own;
+  const float a = p.bre[axis];
+  const float b = conj ? -p.bim[axis] : p.bim[axis];
+  const float other = partner[c];
+  return p.part ? (a * own) + (b * other) : (a * own) - (b * other);
+}
 
 __device__ __forceinline__ void l2_prefetch(const float* p) {
   asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
@@ -613,6 +647,11 @@ __device__ __forceinline__ bool prev_lane_has_z() { return lane_id() != 0 && thr
 // reaches (StepParams.inner) some auxiliary's run may hold a cell; inside it none does,
 // so every coefficient of that axis is exactly 1 for the whole CTA. 0: the CTA steps the
 // plain update, word for word.
+// Whether a CTA holds index 0 of a Bloch-phased axis (its cells read across the face).
+__device__ __forceinline__ bool cta_bloch(const StepParams& p, int i0, int j0, int k0) {
+  return p.bloch && (((p.bloch & 1) && i0 == 0) || ((p.bloch & 2) && j0 == 0) || ((p.bloch & 4) && k0 == 0));
+}
+
 // Whether a CTA's cells reach the bounding box of the magnetic source points.
 __device__ __forceinline__ bool cta_msrc(const StepParams& p, int i0, int i1, int j0, int by, int k0, int bz) {
   return p.nsrc_h > 0 && i0 < p.src_box_h[1] && i1 > p.src_box_h[0] && j0 < p.src_box_h[3] &&
@@ -641,7 +680,7 @@ __device__ __forceinline__ int cta_axes(const StepParams& p, int i0, int i1, int
 // ------------------------------------------------------------------------------------
 // Generic kernels: plain loads, one thread per (y, z) column marching over x.
 // One thread's column (j, k) of the H half over planes [i0, i1).
-template <bool PML, bool COND = false, int AX = -1, bool MSRC = false>
+template <bool PML, bool COND = false, int AX = -1, bool MSRC = false, bool BLOCH = false>
 __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i0, int i1,
                                         int first_step, const mgb_conductivity* cp = nullptr) {
   const int sx = p.ny * p.nz;
@@ -701,9 +740,18 @@ __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i
     HAux ax = {};
     if (PML && axes != 0) h_aux_load(p, hcol, pl, c, ax);
     // MEEP's association ((g1s - g1) + g2) - g2s, then the dtdx scale.
-    const float cx = dtdx * (((ez_yp - ez) + ey) - ey_zp);
-    const float cy = dtdx * (((ex_zp - ex) + ez) - ez_xp);
-    const float cz = dtdx * (((ey_xp - ey) + ex) - ex_yp);
+    // the same-index curl operands: on a Bloch-phased axis the word below the window
+    // at index 0 (B's forward curl reads E at the low wall: conj(eikna) times the stored
+    // top word, both parts)
+    float gx1 = ez, gx2 = ey, gy1 = ex, gy2 = ez, gz1 = ey, gz2 = ex;
+    if (BLOCH) {
+      if (j == 0) { gx1 = bloch_word(p, 1, true, ez, p.pE[2], c); gz2 = bloch_word(p, 1, true, ex, p.pE[0], c); }
+      if (k == 0) { gx2 = bloch_word(p, 2, true, ey, p.pE[1], c); gy1 = bloch_word(p, 2, true, ex, p.pE[0], c); }
+      if (i == 0) { gy2 = bloch_word(p, 0, true, ez, p.pE[2], c); gz1 = bloch_word(p, 0, true, ey, p.pE[1], c); }
+    }
+    const float cx = dtdx * (((ez_yp - gx1) + gx2) - ey_zp);
+    const float cy = dtdx * (((ex_zp - gy1) + gy2) - ez_xp);
+    const float cz = dtdx * (((ey_xp - gz1) + gz2) - ex_yp);
     float h_new[3];
     h_cell<PML, COND, AX, MSRC>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, h_old, ax, h_new, cp);
     p.H[0][c] = h_new[0];
@@ -715,7 +763,7 @@ __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i
 }
 
 // One thread's column (j, k) of the E half over planes [i0, i1).
-template <bool PML, bool COND = false, int AX = -1>
+template <bool PML, bool COND = false, int AX = -1, bool BLOCH = false>
 __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i0, int i1,
                                         int parity, const double* words,
                                         const mgb_conductivity* cp = nullptr) {
@@ -777,9 +825,17 @@ __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i
     const float inv[3] = {__ldg(p.inv_eps[0] + c), __ldg(p.inv_eps[1] + c), __ldg(p.inv_eps[2] + c)};
     EAux ax = {};
     if (PML && axes != 0) e_aux_load(p, ecol, pl, c, ax);
-    const float cx = dtdx * (((hz_ym - hz) + hy) - hy_zm);
-    const float cy = dtdx * (((hx_zm - hx) + hz) - hz_xm);
-    const float cz = dtdx * (((hy_xm - hy) + hx) - hx_ym);
+    // on a Bloch-phased axis D's backward curl at index 0 reads H above the window:
+    // eikna times the stored word, both parts
+    float gx1 = hz, gx2 = hy, gy1 = hx, gy2 = hz, gz1 = hy, gz2 = hx;
+    if (BLOCH) {
+      if (j == 0) { gx1 = bloch_word(p, 1, false, hz, p.pH[2], c); gz2 = bloch_word(p, 1, false, hx, p.pH[0], c); }
+      if (k == 0) { gx2 = bloch_word(p, 2, false, hy, p.pH[1], c); gy1 = bloch_word(p, 2, false, hx, p.pH[0], c); }
+      if (i == 0) { gy2 = bloch_word(p, 0, false, hz, p.pH[2], c); gz1 = bloch_word(p, 0, false, hy, p.pH[1], c); }
+    }
+    const float cx = dtdx * (((hz_ym - gx1) + gx2) - hy_zm);
+    const float cy = dtdx * (((hx_zm - gy1) + gy2) - hz_xm);
+    const float cz = dtdx * (((hy_xm - gz1) + gz2) - hx_ym);
     e_cell<PML, COND, AX>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, d, inv, words, ax, cp);
     hy_xm = hy;
     hz_xm = hz;
@@ -1029,6 +1085,11 @@ __global__ void __launch_bounds__(256, 5) h_generic(const __grid_constant__ Step
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
   const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  // a Bloch-phased run: the CTAs at index 0 of a phased axis read the other part there
+  if (cta_bloch(p, i0, blockIdx.y * blockDim.y, blockIdx.x * blockDim.x)) {
+    h_march<PML, false, -1, true, true>(p, j, k, i0, i1, first_step);
+    return;
+  }
   // a run with magnetic sources: the CTAs that hold source points deposit them
   if (MSRC && cta_msrc(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x)) {
     h_march<PML, false, -1, true>(p, j, k, i0, i1, first_step);
@@ -1052,6 +1113,11 @@ __global__ void __launch_bounds__(256, 5) e_generic(const __grid_constant__ Step
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
   const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  // a Bloch-phased run: the CTAs at index 0 of a phased axis read the other part there
+  if (cta_bloch(p, i0, blockIdx.y * blockDim.y, blockIdx.x * blockDim.x)) {
+    e_march<PML, false, -1, true>(p, j, k, i0, i1, parity, p.src_words);
+    return;
+  }
   if (!PML) {
     e_march<false>(p, j, k, i0, i1, parity, p.src_words);
     return;
@@ -1074,6 +1140,11 @@ __global__ void __launch_bounds__(256, 4) h_generic_cond(const __grid_constant__
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
   const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  // a Bloch-phased run: the CTAs at index 0 of a phased axis read the other part there
+  if (cta_bloch(p, i0, blockIdx.y * blockDim.y, blockIdx.x * blockDim.x)) {
+    h_march<PML, true, -1, true, true>(p, j, k, i0, i1, first_step, &cp);
+    return;
+  }
   // a run with magnetic sources: the CTAs that hold source points deposit them
   if (MSRC && cta_msrc(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x)) {
     h_march<PML, true, -1, true>(p, j, k, i0, i1, first_step, &cp);
@@ -1097,6 +1168,11 @@ __global__ void __launch_bounds__(256, 4) e_generic_cond(const __grid_constant__
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
   const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  // a Bloch-phased run: the CTAs at index 0 of a phased axis read the other part there
+  if (cta_bloch(p, i0, blockIdx.y * blockDim.y, blockIdx.x * blockDim.x)) {
+    e_march<PML, true, -1, true>(p, j, k, i0, i1, parity, p.src_words, &cp);
+    return;
+  }
   if (!PML) {
     e_march<false, true>(p, j, k, i0, i1, parity, p.src_words, &cp);
     return;
@@ -1547,12 +1623,48 @@ __global__ void __launch_bounds__(kWsThreads, 2) e_ws(const __grid_constant__ St
 // ------------------------------------------------------------------------------------
 // DFT accumulation on one monitor: cell-centred samples times float64-formed phases.
 __device__ __forceinline__ float field_at(const DftParams& p, int comp, int i, int j, int k) {
-  // Past a face: metallic walls hold zero, periodic axes wrap.
-  if (i >= p.nx) { if (p.met[0]) return 0.f; i -= p.nx; }
-  if (j >= p.ny) { if (p.met[1]) return 0.f; j -= p.ny; }
-  if (k >= p.nz) { if (p.met[2]) return 0.f; k -= p.nz; }
-  const long long c = ((long long)i * p.ny + j) * p.nz + k;
-  return comp < 3 ? p.E[comp][c] : p.H[comp - 3][c];
+  // A monitor's ladder may reach past a periodic face (MEEP's lattice-image gather): the
+  // ladder point r samples stored cell r mod n, one lattice vector (or more) away from
+  // it; past a metallic face the wall holds zero.
+  const int raw[3] = {i, j, k};
+  const int n[3] = {p.nx, p.ny, p.nz};
+  int at[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    int r = raw[a];
+    if (r < 0 || r >= n[a]) {
+      if (p.met[a]) return 0.f;
+      r %= n[a];
+      if (r < 0) r += n[a];
+    }
+    at[a] = r;
+  }
+  const long long c = ((long long)at[0] * p.ny + at[1]) * p.nz + at[2];
+  const float own = comp < 3 ? p.E[comp][c] : p.H[comp - 3][c];
+  if (!p.bloch) return own;
+  // On a Bloch-phased axis the ladder point is eikna^count times the stored word, count
+  // the lattice vectors between them: floor((r - low) / n), low = 1 for a component with
+  // Yee shift 0 there (its cell 0 stores MEEP's owned top point) and 0 otherwise.
+  const int q = comp % 3;
+  float fr = 1.f, fi = 0.f;
+  bool any = false;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (!((p.bloch >> a) & 1)) continue;
+    const int low = (comp < 3 ? (a != q) : (a == q)) ? 1 : 0;
+    const int shifted = raw[a] - low;
+    int count = shifted >= 0 ? shifted / n[a] : -((-shifted + n[a] - 1) / n[a]);
+    const float br = p.bre[a], bi = count < 0 ? -p.bim[a] : p.bim[a];
+    for (count = count < 0 ? -count : count; count > 0; --count) {
+      const float nr = fr * br - fi * bi, ni = fr * bi + fi * br;
+      fr = nr;
+      fi = ni;
+      any = true;
+    }
+  }
+  if (!any) return own;
+  const float other = comp < 3 ? p.pE[comp][c] : p.pH[comp - 3][c];
+  return p.part ? (fr * own) + (fi * other) : (fr * own) - (fi * other);
 }
 
 // Yee-to-centre average along every axis where the component's shift is 0, x then y
@@ -2147,7 +2259,7 @@ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) ==
 void setup_tiles(mgb_sim* sim) {
   const char* env = getenv("MEEPGB_TILES");
   if (env != nullptr && env[0] == '0') return;
-  if (sim->has_cond) return;
+  if (sim->has_cond || sim->step.bloch) return;
   const StepParams& p = sim->step;
   if (p.nz % 4 != 0) return;
   for (int q = 0; q < 3; ++q)
@@ -2266,7 +2378,9 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
   for (int m = 0; m < d.nmonitors; ++m) {
     const mgb_monitor& mon = d.monitors[m];
     for (int a = 0; a < 3; ++a) {
-      if (mon.region[2 * a] < 0 || mon.region[2 * a] >= mon.region[2 * a + 1] || mon.region[2 * a + 1] > n[a]) {
+      // on a periodic axis the ladder may reach one period past either face (lattice images)
+      const int lo = d.metallic[a] ? 0 : -n[a], hi = d.metallic[a] ? n[a] : 2 * n[a];
+      if (mon.region[2 * a] < lo || mon.region[2 * a] >= mon.region[2 * a + 1] || mon.region[2 * a + 1] > hi) {
         return fail(MGB_ERR_ARGUMENT, "monitor " + std::to_string(m) + " region is not inside the grid");
       }
     }
@@ -2280,6 +2394,19 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
     if ((size_t)mon.nfreq * 2 * sizeof(float2) > 48 * 1024) {
       return fail(MGB_ERR_UNSUPPORTED, "a monitor holds at most 3072 frequencies");
     }
+  }
+  if (d.bloch_axes & ~7) return fail(MGB_ERR_ARGUMENT, "bloch_axes holds bits 0..2 only");
+  for (int a = 0; a < 3; ++a) {
+    if (!((d.bloch_axes >> a) & 1)) continue;
+    if (d.metallic[a]) return fail(MGB_ERR_ARGUMENT, "a Bloch phase needs a periodic axis");
+    const double re = d.bloch_phase[a][0], im = d.bloch_phase[a][1];
+    if (!std::isfinite(re) || !std::isfinite(im) || std::fabs(std::hypot(re, im) - 1.0) > 1e-9)
+      return fail(MGB_ERR_ARGUMENT, "a Bloch phase must be a finite unit-modulus number");
+  }
+  if (d.bloch_axes) {
+    for (int q = 0; q < 3; ++q)
+      if (d.partner_E[q] == nullptr || d.partner_H[q] == nullptr)
+        return fail(MGB_ERR_ARGUMENT, "a Bloch-phased plan needs the other part's E and H (partner_E, partner_H)");
   }
   bool lossy = false;
   if (d.conductivity != nullptr) {
@@ -2351,6 +2478,21 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
   p.src_words = nullptr;
   p.status = d.status;
   p.l2pf = 0;
+  p.bloch = d.bloch_axes & 7;
+  p.part = d.part ? 1 : 0;
+  for (int a = 0; a < 3; ++a) {
+    p.bmode[a] = 0;
+    p.bre[a] = 1.f;
+    p.bim[a] = 0.f;
+    p.pE[a] = d.partner_E[a];
+    p.pH[a] = d.partner_H[a];
+    if (!((p.bloch >> a) & 1)) continue;
+    const double re = d.bloch_phase[a][0], im = d.bloch_phase[a][1];
+    // MEEP's connection rule: a copy within 1e-13 of +1, a negation within 1e-13 of -1
+    if (std::fabs(im) < 1e-13 && std::fabs(re - 1.0) < 1e-13) p.bmode[a] = 1;
+    else if (std::fabs(im) < 1e-13 && std::fabs(re + 1.0) < 1e-13) { p.bmode[a] = 2; p.bre[a] = -1.f; }
+    else { p.bmode[a] = 3; p.bre[a] = (float)re; p.bim[a] = (float)im; }
+  }
   setup_tiles(sim);
   *out = sim;
   return MGB_OK;
@@ -2496,11 +2638,17 @@ int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s) {
   for (int m = 0; m < sim->desc.nmonitors; ++m) {
     const mgb_monitor& mon = sim->desc.monitors[m];
     if (post % mon.decimation != 0) continue;
-    DftParams q;
+    DftParams q = {};
     q.nx = p.nx; q.ny = p.ny; q.nz = p.nz;
     for (int a = 0; a < 3; ++a) q.met[a] = p.met[a];
     for (int c = 0; c < 3; ++c) { q.E[c] = p.E[c]; q.H[c] = p.H[c]; }
     q.mon = mon;
+    q.bloch = p.bloch;
+    q.part = p.part;
+    for (int a = 0; a < 3; ++a) {
+      q.bmode[a] = p.bmode[a]; q.bre[a] = p.bre[a]; q.bim[a] = p.bim[a];
+      q.pE[a] = p.pE[a]; q.pH[a] = p.pH[a];
+    }
     const long long cells = (long long)(mon.region[1] - mon.region[0]) *
                             (mon.region[3] - mon.region[2]) * (mon.region[5] - mon.region[4]);
     const unsigned blocks = (unsigned)((cells + 255) / 256);
@@ -2545,6 +2693,30 @@ int mgb_step(mgb_sim* sim, int64_t first_step, int32_t nsteps, void* stream) {
   for (int32_t t = 0; t < nsteps; ++t) {
     const long long n = first_step + t;
     for (int part = 0; part < 3; ++part) launch_part(sim, n, part, s);
+    if (t == 0) {
+      const int err = launch_error("step launch");
+      if (err != MGB_OK) return err;
+    }
+  }
+  return launch_error("step launch");
+}
+
+int mgb_step_pair(mgb_sim* real, mgb_sim* imag, int64_t first_step, int32_t nsteps, void* stream) {
+  if (real == nullptr || imag == nullptr) return fail(MGB_ERR_ARGUMENT, "null plan");
+  if (real->step.part != 0 || imag->step.part != 1)
+    return fail(MGB_ERR_ARGUMENT, "mgb_step_pair takes the real-part plan, then the imaginary-part plan");
+  if (nsteps < 0 || first_step < 0) return fail(MGB_ERR_ARGUMENT, "negative step range");
+  if (nsteps == 0) return MGB_OK;
+  int rc = check_words(real, first_step, nsteps);
+  if (rc == MGB_OK) rc = check_words(imag, first_step, nsteps);
+  if (rc != MGB_OK) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  for (int32_t t = 0; t < nsteps; ++t) {
+    const long long n = first_step + t;
+    for (int part = 0; part < 3; ++part) {
+      launch_part(real, n, part, s);
+      launch_part(imag, n, part, s);
+    }
     if (t == 0) {
       const int err = launch_error("step launch");
       if (err != MGB_OK) return err;
@@ -2623,6 +2795,8 @@ namespace {
 int choose_family(mgb_sim* sim, mgb_sim::HalfChoice& h, int family, int part) {
   if (sim->has_cond && family != 0 && family != 4)
     return fail(MGB_ERR_UNSUPPORTED, "a run with a conductivity steps with the generic kernels (family 0 or 4)");
+  if (sim->step.bloch && family != 0 && family != 4)
+    return fail(MGB_ERR_UNSUPPORTED, "a Bloch-phased run steps with the generic kernels (family 0 or 4)");
   if (family == 0 || family == 2 || family == 4 || family == 5) {
     h.tiles = false;
     h.ws = false;
@@ -2908,6 +3082,7 @@ int mgb_batch_set_slot(mgb_batch* b, int32_t slot, mgb_sim* sim, int64_t end_ste
   if (sim->step.nsrc > 0 && words == nullptr) return fail(MGB_ERR_ARGUMENT, "the slot's sources need deposit words");
   if (sim->has_cond) return fail(MGB_ERR_UNSUPPORTED, "a batched slot does not carry a conductivity");
   if (sim->step.nsrc_h > 0) return fail(MGB_ERR_UNSUPPORTED, "a batched slot does not carry magnetic sources");
+  if (sim->step.bloch) return fail(MGB_ERR_UNSUPPORTED, "a batched slot does not carry Bloch phases");
   if (sim->desc.nmonitors > kSlotMonitors)
     return fail(MGB_ERR_UNSUPPORTED, "a batched slot holds at most " + std::to_string(kSlotMonitors) + " monitors");
   for (int m = 0; m < sim->desc.nmonitors; ++m) {
@@ -3171,7 +3346,7 @@ int mgb_adjoint_inject(mgb_sim* adj, int32_t monitor, int64_t post, void* stream
   if (monitor < 0 || monitor >= adj->desc.nmonitors) return fail(MGB_ERR_ARGUMENT, "no such monitor");
   const StepParams& p = adj->step;
   const mgb_monitor& mon = adj->desc.monitors[monitor];
-  DftParams q;
+  DftParams q = {};
   q.nx = p.nx; q.ny = p.ny; q.nz = p.nz;
   for (int ax = 0; ax < 3; ++ax) q.met[ax] = p.met[ax];
   for (int c = 0; c < 3; ++c) { q.E[c] = p.E[c]; q.H[c] = p.H[c]; }

@@ -115,19 +115,22 @@ def volume_bounds(center: Sequence[float], size: Sequence[float], what: str):
 def register_volume(grid: Grid, center: Sequence[float], size: Sequence[float], what: str):
     """Half-open stored-index region ``(x0, x1, y0, y1, z0, z1)`` a monitor volume covers.
 
-    Non-wrapping axes clamp the ladder to the stored grid. A ladder that reaches
-    past a wrapping face (including the one extra plane the cell-centre average
-    consumes) would need MEEP's lattice-shift gather, which this engine refuses.
+    Non-wrapping axes clamp the ladder to the stored grid. On a wrapping axis the
+    ladder is kept whole even where it reaches past a face: its cells past the face
+    sample the lattice images of stored cells (MEEP's lattice-shift gather,
+    ``loop_in_chunks``; reference ``dft.py:927`` ``_lattice_gather``), which the device
+    sampling folds back, with the Bloch factor on a phased axis.
     """
     bounds = volume_bounds(center, size, what)
     region: List[int] = []
     for axis in range(3):
         first, count, _ = axis_ladder(grid, axis, *bounds[axis])
         n = grid.shape[axis]
-        if grid.axis_wraps(axis) and (first < 0 or first + count + 1 > n):
-            raise Unsupported(
-                f"{what} reaches past the periodic {AXIS_NAMES[axis]} face; lattice-image "
-                "gathers are not supported by this engine")
+        if grid.axis_wraps(axis):
+            if first < -n or first + count > 2 * n:
+                raise Unsupported(f"{what} reaches more than one period past the {AXIS_NAMES[axis]} face")
+            region += [first, first + count]
+            continue
         lo, hi = max(first, 0), min(first + count, n)
         if hi <= lo:
             raise ValueError(f"{what} lies outside the cell on the {AXIS_NAMES[axis]} axis")

@@ -5,7 +5,7 @@ Mirrors ``meep_gpu/driver.py``'s ``FdtdDriver`` (constructor :810, ``set_epsilon
 ``add_dft_monitor`` :2783, ``add_flux_monitor`` :3001, ``step`` :3419, ``run`` :3667,
 ``get_field`` :4056, ``set_conductivity`` :1649, ``set_b_conductivity`` :1752,
 ``set_absorber`` :1863) for the configurations this engine steps: 3-D, real float32 or
-complex64 fields, metallic or periodic (k = 0) boundaries, no mirror symmetry, isotropic or
+complex64 fields, metallic, periodic or Bloch-periodic boundaries, no mirror symmetry, isotropic or
 diagonal chi1inv, Lorentz/Drude poles, D and B conductivity (material and
 ``mp.Absorber``), electric sources and DFT/flux monitors.
 Anything else is refused by name when it is asked for, never approximated.
@@ -32,7 +32,7 @@ from .dft import (DFTMonitor, FluxMonitor, absorbing_cells, automatic_decimation
 from .dispersion import Susceptibility
 from .grid import AXIS_NAMES, IYEE, Grid, Unsupported
 from .pml import PML
-from .sources import Source, make_waveform
+from .sources import Source, bind_src_vols, make_waveform
 
 FIELD_COMPONENTS = ("Ex", "Ey", "Ez", "Dx", "Dy", "Dz", "Hx", "Hy", "Hz", "Bx", "By", "Bz")
 STEP_TOLERANCE = 1e-9
@@ -67,17 +67,18 @@ class FdtdDriver:
                  dft_accumulation: Optional[str] = None):
         if tuple(symmetry):
             raise Unsupported("mirror symmetry is not stepped by this engine")
-        if any(float(k) != 0.0 for k in k_point):
-            raise Unsupported("a nonzero Bloch k_point needs complex fields; not stepped")
         if dimensions != 3 or cylindrical:
             raise Unsupported("only 3-D Cartesian runs are stepped by this engine")
         if beta != 0.0 or any(float(k) != 0.0 for k in bfast_scaled_k):
             raise Unsupported("out-of-plane beta and BFAST are not stepped by this engine")
         del m, accurate_fields_near_cylorigin, prefer_gpu
-        self.grid = Grid(cell_size, resolution, courant, boundaries)
+        self.grid = Grid(cell_size, resolution, courant, boundaries, k_point)
         # complex64 fields (the reference's default): at k = 0 the real and imaginary
         # parts step as two real runs (engine.ComplexEngine)
         self.complex_fields = bool(force_complex_fields)
+        if self.grid.has_bloch and not self.complex_fields:
+            raise ValueError("Bloch boundaries need complex fields: build the driver with "
+                             "force_complex_fields=True or use k_point = (0, 0, 0)")
         self.gpu_id = int(gpu_id)
         self.launch_shape = launch_shape
         # (family, block_z, block_y, x_chunk): 1 the TMA tile kernels, 0 the generic ones;
@@ -349,6 +350,9 @@ class FdtdDriver:
         self._resolve_regions()
         if self._inv_eps is None:
             self.set_epsilon(1.0)
+        # the sources' deposit entries in MEEP's src_vol lists on this run's chunks
+        faces = self.pml.faces if (self.pml is not None and self.pml.is_active) else None
+        bind_src_vols(self._sources, self.grid, faces)
 
     def _freeze(self) -> None:
         self.freeze()
@@ -490,8 +494,24 @@ class FdtdDriver:
             else:
                 padded = np.pad(padded, pad, mode="wrap")
         n = self.grid.shape
+        # On a Bloch-phased axis cell 0 of a shift-0 component stores the owned top point:
+        # the word at ladder index 0 (the low face) is conj(eikna) times it.
+        low_factor = {}
+        for axis in axes:
+            phase = self.grid.bloch_phase(axis)
+            if phase is not None:
+                line = np.ones(n[axis], dtype=np.complex64)
+                line[0] = np.complex64(np.conj(phase))
+                shape = [1, 1, 1]
+                shape[axis] = n[axis]
+                low_factor[axis] = line.reshape(shape)
+
         def view(offsets):
-            return padded[tuple(slice(o, o + n[a]) for a, o in enumerate(offsets))]
+            term = padded[tuple(slice(o, o + n[a]) for a, o in enumerate(offsets))]
+            for axis, factor in low_factor.items():
+                if offsets[axis] == 0:
+                    term = term * factor
+            return term
         if not axes:
             return raw
         if len(axes) == 1:

@@ -85,7 +85,7 @@ class Engine:
                  kernels: Optional[Tuple[int, int, int, int]] = None,
                  dft_accumulation: Optional[str] = None,
                  conductivity: Optional[Dict[str, Optional[np.ndarray]]] = None,
-                 part: str = "real", own_monitors: bool = True):
+                 part: str = "real", own_monitors: bool = True, create: bool = True):
         if not torch.cuda.is_available():
             raise RuntimeError("meep_gpu_gb300 steps on a CUDA GPU and none is visible")
         self.lib = _lib.load()
@@ -154,21 +154,33 @@ class Engine:
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         d.status = self.status.data_ptr()
         self._setup_monitors()
-        handle = ctypes.c_void_p()
-        _lib.check(self.lib, self.lib.mgb_create(ctypes.byref(d), ctypes.byref(handle)))
-        self.handle = handle
-        self._setup_dft_buffers(dft_accumulation)
         self._pole_specs = list(poles)
         self.choice = None
+        self.handle = None
+        self._words: Optional[torch.Tensor] = None
+        self._words_first = 0
+        self._words_steps = 0
+        # kernel families the plan may take: the generic ones only when a conductivity or
+        # a Bloch phase is stepped (the library refuses the others for such a plan)
+        self.allowed_families = (0, 4) if (self.conductivity or grid.has_bloch) else (0, 1, 2, 3, 4, 5)
+        self._finish_args = (dft_accumulation, kernels, launch_shape, autotune)
+        if create:
+            self.finish()
+
+    def finish(self) -> None:
+        """Make the library's plan from the descriptor (deferred while a complex run's
+        two parts are wired to each other), then its DFT buffers and kernel choice."""
+        dft_accumulation, kernels, launch_shape, autotune = self._finish_args
+        handle = ctypes.c_void_p()
+        _lib.check(self.lib, self.lib.mgb_create(ctypes.byref(self.desc), ctypes.byref(handle)))
+        self.handle = handle
+        self._setup_dft_buffers(dft_accumulation)
         if kernels is not None:
-            self.select(tuple(kernels))
+            self.select(tuple(kernels) if not isinstance(kernels[0], (tuple, list)) else kernels)
         elif launch_shape is not None:
             self.set_launch_shape(*launch_shape)
         elif autotune and os.environ.get("MEEPGB_AUTOTUNE", "1") != "0":
             self.autotune()
-        self._words: Optional[torch.Tensor] = None
-        self._words_first = 0
-        self._words_steps = 0
 
     # --- setup --------------------------------------------------------------------------
     def _aux(self, slot, name: str, q: int, key: Tuple[int, int]) -> None:
@@ -451,6 +463,7 @@ class Engine:
         """
         key = autotune_key(self.grid, self.pml, len(getattr(self, "pole_tensors", [])),
                            len({t.data_ptr() for t in self.inv_eps}), bool(self.conductivity))
+        key = key + (self.allowed_families,)
         if key in _AUTOTUNE_CACHE:
             self.select(_AUTOTUNE_CACHE[key])
             return self.choice
@@ -461,6 +474,8 @@ class Engine:
         best = [None, None]
         best_ms = [float("inf"), float("inf")]
         for choice in AUTOTUNE_CANDIDATES:
+            if choice[0] not in self.allowed_families:
+                continue
             # a candidate one half refuses is timed on the other half only
             applies = []
             for part in (0, 1):
@@ -622,14 +637,37 @@ class ComplexEngine:
     def __init__(self, grid: Grid, pml: Optional[PML], inv_eps, poles, sources, monitors, device=None,
                  stream=None, launch_shape=None, autotune: bool = True, kernels=None,
                  dft_accumulation: Optional[str] = None, conductivity=None):
+        self.bloch = grid.has_bloch
         self.re = Engine(grid, pml, inv_eps, poles, sources, monitors, device=device, stream=stream,
                          launch_shape=launch_shape, autotune=autotune, kernels=kernels,
-                         dft_accumulation=dft_accumulation, conductivity=conductivity, part="real")
+                         dft_accumulation=dft_accumulation, conductivity=conductivity, part="real",
+                         create=False)
         self.im = Engine(grid, pml, inv_eps, poles, sources, monitors, device=device, stream=stream,
-                         launch_shape=launch_shape, autotune=False,
-                         kernels=self.re.choice if self.re.choice is not None else kernels,
+                         launch_shape=launch_shape, autotune=False, kernels=kernels,
                          dft_accumulation=dft_accumulation, conductivity=conductivity, part="imag",
-                         own_monitors=False)
+                         own_monitors=False, create=False)
+        if self.bloch:
+            # the two parts meet across the phased faces: each plan reads the other's E, H
+            axes = 0
+            for a in range(3):
+                phase = grid.bloch_phase(a)
+                if phase is None:
+                    continue
+                axes |= 1 << a
+                for engine in (self.re, self.im):
+                    engine.desc.bloch_phase[a][0] = phase.real
+                    engine.desc.bloch_phase[a][1] = phase.imag
+            for engine, partner, part in ((self.re, self.im, 0), (self.im, self.re, 1)):
+                engine.desc.bloch_axes = axes
+                engine.desc.part = part
+                for q, axis in enumerate("xyz"):
+                    engine.desc.partner_E[q] = partner.fields["E" + axis].data_ptr()
+                    engine.desc.partner_H[q] = partner.fields["H" + axis].data_ptr()
+        self.re.finish()
+        self.im._finish_args = (self.im._finish_args[0],
+                                self.re.choice if self.re.choice is not None else kernels,
+                                launch_shape, False)
+        self.im.finish()
         self.grid = grid
         self.device = self.re.device
         self.monitors = self.re.monitors
@@ -656,8 +694,18 @@ class ComplexEngine:
         self.im.ensure_source_words(first_step, steps)
 
     def step(self, first_step: int, nsteps: int) -> None:
-        self.re.step(first_step, nsteps)
-        self.im.step(first_step, nsteps)
+        if not self.bloch:
+            self.re.step(first_step, nsteps)
+            self.im.step(first_step, nsteps)
+            return
+        # the parts read each other across the phased faces: step them half by half
+        done = 0
+        while done < nsteps:
+            chunk = min(nsteps - done, SOURCE_WINDOW)
+            self.ensure_source_words(first_step + done, chunk)
+            _lib.check(self.lib, self.lib.mgb_step_pair(self.re.handle, self.im.handle, first_step + done,
+                                                        chunk, self.re._stream_handle()))
+            done += chunk
 
     def launch(self, step: int, part: int, stream=None) -> None:
         self.re.launch(step, part, stream)

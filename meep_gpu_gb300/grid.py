@@ -2,9 +2,9 @@
 
 Follows the reference's ``meep_gpu/grid.py`` (``Grid``, :288 ``meep_cell_count``,
 :426-438 dx/dt/counts, :1095 ``origin_doubled``, :1292 ``_create_coordinates``) for
-the subset this engine steps: three resolved dimensions, real fields, no mirror
-symmetry, and per-axis boundaries that are either MEEP metallic walls or plain
-periodic wrap (Bloch vector zero).
+the subset this engine steps: three resolved dimensions, no mirror symmetry, and
+per-axis boundaries that are either MEEP metallic walls or periodic wraps, Bloch-phased
+where the axis has a nonzero ``k_point`` component.
 
 Registration: cell ``i`` of a component with Yee shift ``s`` on an axis sits at the
 doubled coordinate ``origin_doubled + 2*i + s``; ``origin_doubled`` is ``-(n - n % 2)``,
@@ -13,8 +13,10 @@ MEEP's centred origin (odd counts start half a cell higher).
 
 from __future__ import annotations
 
+import ctypes
+import ctypes.util
 import math
-from typing import Any, Sequence, Tuple
+from typing import Any, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -34,6 +36,56 @@ IYEE = {
 
 class Unsupported(ValueError):
     """A configuration outside what this engine steps, refused by name before any launch."""
+
+
+_LIBM = None
+
+
+def sincos(x: float) -> Tuple[float, float]:
+    """``(sin x, cos x)`` from one libm ``sincos`` call, as a compiled ``exp`` of an
+    imaginary argument takes them (reference ``readback.py:170``)."""
+    global _LIBM
+    if _LIBM is None:
+        _LIBM = ctypes.CDLL(ctypes.util.find_library("m") or "libm.so.6")
+    if hasattr(_LIBM, "sincos"):
+        s, c = ctypes.c_double(), ctypes.c_double()
+        _LIBM.sincos(ctypes.c_double(float(x)), ctypes.byref(s), ctypes.byref(c))
+        return float(s.value), float(c.value)
+    return math.sin(x), math.cos(x)
+
+
+def cmul(a: Tuple[float, float], b: Tuple[float, float]) -> Tuple[float, float]:
+    """Complex product, each operation rounded on its own: ``(ac - bd, ad + bc)``."""
+    return (a[0] * b[0] - a[1] * b[1], a[0] * b[1] + a[1] * b[0])
+
+
+def creciprocal(c: float, d: float) -> Tuple[float, float]:
+    """``1 / (c + i d)`` by Smith's algorithm (the complex division a C runtime without
+    fast-math performs; no rescaling is needed for the unit-modulus phases it serves)."""
+    if not (1e-150 < math.hypot(c, d) < 1e150):
+        raise ValueError("a Bloch phase power must be of moderate modulus")
+    if abs(c) < abs(d):
+        ratio = c / d
+        denom = (c * ratio) + d
+        return ((1.0 * ratio + 0.0) / denom, (0.0 * ratio - 1.0) / denom)
+    ratio = d / c
+    denom = (d * ratio) + c
+    return ((0.0 * ratio + 1.0) / denom, (0.0 - 1.0 * ratio) / denom)
+
+
+def cpow_int(x: Tuple[float, float], n: int) -> Tuple[float, float]:
+    """``pow(complex, int)`` by repeated squaring, and the reciprocal of the power for a
+    negative exponent (the integer power a GCC-built C++ runtime takes)."""
+    if n < 0:
+        return creciprocal(*cpow_int(x, -n))
+    y = x if n % 2 else (1.0, 0.0)
+    n >>= 1
+    while n:
+        x = cmul(x, x)
+        if n % 2:
+            y = cmul(y, x)
+        n >>= 1
+    return y
 
 
 def cell_count(length: float, resolution: float) -> int:
@@ -71,7 +123,7 @@ class Grid:
     """Cell counts, spacing, dt and registration of one 3-D simulation."""
 
     def __init__(self, cell_size: Sequence[float], resolution: float, courant: float = 0.5,
-                 boundaries: Any = None):
+                 boundaries: Any = None, k_point: Sequence[float] = (0.0, 0.0, 0.0)):
         if len(tuple(cell_size)) != 3:
             raise ValueError(f"cell_size needs three lengths, got {cell_size!r}")
         self.cell_size = tuple(float(v) for v in cell_size)
@@ -88,6 +140,18 @@ class Grid:
                 "are not stepped by this engine")
         self.nx, self.ny, self.nz = counts
         self.boundaries = normalize_boundaries(boundaries)
+        self.k_point = tuple(float(k) for k in k_point)
+        if len(self.k_point) != 3 or not all(math.isfinite(k) for k in self.k_point):
+            raise ValueError(f"k_point needs three finite components, got {k_point!r}")
+        for axis, k in enumerate(self.k_point):
+            if k != 0.0 and not self.axis_wraps(axis):
+                raise ValueError(
+                    f"k_point component {AXIS_NAMES[axis]} = {k!r} on an axis declared "
+                    f"{self.boundaries[axis]!r}: a Bloch phase says what the field is one lattice "
+                    f"vector away, and a perfect-electric-conductor wall terminates the axis "
+                    f"instead of repeating it. Make the axis periodic or set its k component to 0.")
+        self.bloch_phases = tuple(self._bloch_phase(self.k_point[a], counts[a]) for a in range(3))
+        self.has_bloch = any(p is not None for p in self.bloch_phases)
 
     # --- registration -------------------------------------------------------------
     @property
@@ -136,6 +200,25 @@ class Grid:
     def meshgrid(self):
         """Cell-centre coordinates in (x, y, z) index order, as the reference's ``Grid.meshgrid``."""
         return np.meshgrid(self.x, self.y, self.z, indexing="ij")
+
+    def _bloch_phase(self, k: float, n: int) -> Optional[complex]:
+        """MEEP's ``eikna`` of one axis, ``exp(i k (2 pi / a) n)`` with the argument
+        associated as MEEP forms it (reference ``grid.py:1009``): None at k = 0, exactly -1
+        at the zone edge."""
+        if k == 0.0:
+            return None
+        if k * n == 0.5 * self.resolution:
+            return complex(-1.0, 0.0)
+        sin_a, cos_a = sincos(k * ((2 * math.pi / self.resolution) * n))
+        return complex(cos_a, sin_a)
+
+    def bloch_phase(self, axis: int) -> Optional[complex]:
+        """``f(x + L) = bloch_phase * f(x)`` on a phased axis; None where k is 0."""
+        return self.bloch_phases[axis]
+
+    def eikna(self, axis: int) -> Tuple[float, float]:
+        phase = self.bloch_phases[axis]
+        return (1.0, 0.0) if phase is None else (phase.real, phase.imag)
 
     def __repr__(self) -> str:
         return (f"Grid({self.nx}x{self.ny}x{self.nz}, res={self.resolution:g}, "

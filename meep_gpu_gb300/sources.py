@@ -26,7 +26,7 @@ from typing import Callable, Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
 
-from .grid import IYEE, Grid, Unsupported
+from .grid import IYEE, Grid, Unsupported, cmul, cpow_int
 
 ELECTRIC = ("Ex", "Ey", "Ez")
 MAGNETIC = ("Hx", "Hy", "Hz")
@@ -192,19 +192,64 @@ def loop_weight(i: int, n: int, s0: float, s1: float, e0: float, e1: float) -> f
     return 1.0
 
 
-def deposition_table(grid: Grid, component: str, center: Sequence[float], size: Sequence[float],
-                     amplitude: complex = 1.0,
-                     amp_func: Optional[Callable[[float, float, float], complex]] = None,
-                     ) -> Tuple[List[Tuple[int, int, int]], List[complex]]:
-    """Cells a source deposits into (D for an electric one, B for a magnetic one) and
-    each cell's complex amplitude.
+def _chunk_weights(start: int, end: int, is_d: int, ie_d: int, taper) -> Tuple[float, float, float, float]:
+    """The end weights of a clipped run ``[start, end]`` (source-frame doubled ends): the
+    request's tapers where the run meets the request's ends, 1 elsewhere, and the
+    narrow-range minima (MEEP's ``loop_in_chunks``)."""
+    s0, s1, e0, e1 = taper
+    ws0 = ws1 = we0 = we1 = 1.0
+    if start == is_d:
+        ws0, ws1 = s0, s1
+    elif start == is_d + 2:
+        ws0 = s1
+    if end == ie_d:
+        we0, we1 = e0, e1
+    elif end == ie_d - 2:
+        we0 = e1
+    if end == start:
+        w = min(ws0, we0)
+        ws0 = we0 = ws1 = we1 = w
+    elif end == start + 2:
+        w = min(ws0, we1)
+        ws0 = we1 = w
+        w = min(ws1, we0)
+        ws1 = we0 = w
+    elif end == start + 4:
+        w = min(ws1, we1)
+        ws1 = we1 = w
+    return ws0, ws1, we0, we1
 
-    MEEP's ``add_volume_source`` over one chunk: the request's doubled-coordinate
-    bounds on the component's lattice, the Simpson tapers of the request, the owned
-    window ``[origin + 2 - iyee, origin + 2n - iyee]`` (the plane on a metallic high
-    wall takes no deposit), one pass per lattice shift on a periodic axis, and the
-    amplitude ``amplitude * a`` per zero-extent axis times the product of the three
-    position weights. Cells listed by several passes are summed in pass order.
+
+def chunk_boxes(grid: Grid, faces) -> List[Tuple[Tuple[int, int, int], Tuple[int, int, int]]]:
+    """The one-rank chunk boxes (doubled corners): per axis the low PML piece, the interior
+    and the high PML piece, x outermost (reference ``chunk_map.py:384``); one box
+    spanning the window without a PML."""
+    from .conductivity import axis_pieces
+    per_axis = []
+    for d in range(3):
+        io = grid.origin_doubled(d)
+        pieces = axis_pieces(grid.shape[d], faces[d] if faces is not None else (0.0, 0.0))
+        per_axis.append([(io + lo, io + hi) for _piece, lo, hi in pieces])
+    return [((bx[0], by[0], bz[0]), (bx[1], by[1], bz[1]))
+            for bx in per_axis[0] for by in per_axis[1] for bz in per_axis[2]]
+
+
+def deposition_pieces(grid: Grid, component: str, center: Sequence[float], size: Sequence[float],
+                      amplitude: complex = 1.0,
+                      amp_func: Optional[Callable[[float, float, float], complex]] = None,
+                      boxes=None) -> List[Tuple[int, List[Tuple[int, int, int]], List[complex]]]:
+    """MEEP's ``src_vol`` pieces of one source, in ``add_volume_source`` order:
+    ``(chunk, cells, amplitudes)`` per (lattice shift, chunk) (reference ``sources.py:1061``
+    ``_src_vol_pieces``, :787 ``_source_geometry``).
+
+    The request's doubled-coordinate bounds on the component's lattice, the Simpson
+    tapers of the request, the owned window ``[origin + 2 - iyee, origin + 2n - iyee]``
+    (the plane on a metallic high wall takes no deposit), one pass per lattice shift on
+    a periodic axis (with ``amp * conj(ph)``, ``ph`` the product of ``eikna^shift`` on a
+    Bloch-phased run), the amplitude ``amplitude * a`` per zero-extent axis, and per
+    chunk the pass clipped to the chunk's owned corners with its own end weights.
+    ``boxes``: the chunk boxes (:func:`chunk_boxes`), or None for one box spanning the
+    window.
     """
     comp = _COMPONENT_ALIASES.get(component)
     if comp is None:
@@ -213,7 +258,7 @@ def deposition_table(grid: Grid, component: str, center: Sequence[float], size: 
     inva = grid.dx
     where_min = [float(center[d]) - float(size[d]) / 2 for d in range(3)]
     where_max = [float(center[d]) + float(size[d]) / 2 for d in range(3)]
-    lengths = grid.cell_size
+    lengths = tuple(n * grid.dx for n in grid.shape)  # the snapped cell (reference Grid.Lx/Ly/Lz)
     for d in range(3):
         span = where_max[d] - where_min[d]
         if span > lengths[d] + inva:
@@ -241,6 +286,8 @@ def deposition_table(grid: Grid, component: str, center: Sequence[float], size: 
     big = [io[d] + 2 * counts[d] for d in range(3)]
     window_low = [io[d] + 2 - iyee[d] for d in range(3)]
     window_high = [big[d] - iyee[d] for d in range(3)]
+    if boxes is None:
+        boxes = [((io[0], io[1], io[2]), (big[0], big[1], big[2]))]
     wraps = [grid.axis_wraps(d) for d in range(3)]
     half_inva = 0.5 * inva
     min_shift = [0, 0, 0]
@@ -255,76 +302,82 @@ def deposition_table(grid: Grid, component: str, center: Sequence[float], size: 
         max_shift[d] = int(math.ceil((where_max[d] - io[d] * half_inva) / lattice))
     centre = [(where_min[d] + where_max[d]) * 0.5 for d in range(3)]
 
-    accumulated: Dict[Tuple[int, int, int], Tuple[float, float]] = {}
+    pieces: List[Tuple[int, List[Tuple[int, int, int]], List[complex]]] = []
     shift = list(min_shift)
     while True:
         shifted = [period[d] * shift[d] for d in range(3)]
+        # a pass one lattice vector away on a Bloch-phased axis carries amp * conj(ph),
+        # ph the product of eikna^shift over the axes (MEEP's loop_in_chunks)
+        pass_amp = amp
+        if grid.has_bloch:
+            ph = (1.0, 0.0)
+            for d in range(3):
+                ph = cmul(ph, cpow_int(grid.eikna(d), shift[d]))
+            pass_amp = cmul(amp, (ph[0], -ph[1]))
         ranges = []
-        weights = []
         for d in range(3):
             low = max(is_[d] - shifted[d], window_low[d])
             high = min(ie[d] - shifted[d], window_high[d])
-            points = list(range(low, high + 1, 2)) if low <= high else []
-            ranges.append(points)
-            s0, s1, e0, e1 = tapers[d]
-            start, end = low + shifted[d], high + shifted[d]
-            ws0 = ws1 = we0 = we1 = 1.0
-            if start == is_[d]:
-                ws0, ws1 = s0, s1
-            elif start == is_[d] + 2:
-                ws0 = s1
-            if end == ie[d]:
-                we0, we1 = e0, e1
-            elif end == ie[d] - 2:
-                we0 = e1
-            if end == start:
-                w = min(ws0, we0)
-                ws0 = we0 = ws1 = we1 = w
-            elif end == start + 2:
-                w = min(ws0, we1)
-                ws0 = we1 = w
-                w = min(ws1, we0)
-                ws1 = we0 = w
-            elif end == start + 4:
-                w = min(ws1, we1)
-                ws1 = we1 = w
-            weights.append((ws0, ws1, we0, we1, (high - low) // 2 + 1, low))
-        for px in ranges[0]:
-            for py in ranges[1]:
-                for pz in ranges[2]:
-                    coords = (px, py, pz)
-                    cell = []
-                    inert = False
-                    rel = []
-                    for d in range(3):
-                        loc = (0.5 * coords[d]) * inva + shifted[d] * half_inva
-                        rel.append(loc - centre[d])
-                        ladder = (coords[d] - io[d]) // 2
-                        if wraps[d]:
-                            cell.append(ladder % counts[d])
-                        elif ladder >= counts[d]:
-                            inert = True
-                            cell.append(-1)
+            ranges.append(list(range(low, high + 1, 2)) if low <= high else [])
+        points = []
+        if all(ranges):
+            for px in ranges[0]:
+                for py in ranges[1]:
+                    for pz in ranges[2]:
+                        coords = (px, py, pz)
+                        cell = []
+                        inert = False
+                        rel = []
+                        for d in range(3):
+                            loc = (0.5 * coords[d]) * inva + shifted[d] * half_inva
+                            rel.append(loc - centre[d])
+                            ladder = (coords[d] - io[d]) // 2
+                            if wraps[d]:
+                                cell.append(ladder % counts[d])
+                            elif ladder >= counts[d]:
+                                inert = True
+                                cell.append(-1)
+                            else:
+                                cell.append(ladder)
+                        if amp_func is None:
+                            value = (1.0, 0.0)
                         else:
-                            cell.append(ladder)
-                    factors = []
-                    for d in range(3):
-                        ws0, ws1, we0, we1, n, low = weights[d]
-                        factors.append(loop_weight((coords[d] - low) // 2, n, ws0, ws1, we0, we1))
-                    if inert:
-                        continue
-                    weight = factors[2] * (factors[1] * (1.0 * factors[0]))
-                    scaled = (weight * amp[0], weight * amp[1])
-                    if amp_func is None:
-                        value = (1.0, 0.0)
-                    else:
-                        result = complex(amp_func(rel[0], rel[1], rel[2]))
-                        value = (result.real, result.imag)
-                    product = _cmul(scaled, value)
-                    key = (cell[0], cell[1], cell[2])
-                    previous = accumulated.get(key)
-                    accumulated[key] = product if previous is None else (
-                        previous[0] + product[0], previous[1] + product[1])
+                            result = complex(amp_func(rel[0], rel[1], rel[2]))
+                            value = (result.real, result.imag)
+                        points.append((coords, None if inert else tuple(cell), value))
+        for chunk, (lo, hi) in enumerate(boxes if points else ()):
+            isc = [0, 0, 0]
+            iec = [0, 0, 0]
+            weights = []
+            empty = False
+            for d in range(3):
+                isc[d] = max(is_[d] - shifted[d], window_low[d], lo[d] + 2 - iyee[d])
+                iec[d] = min(ie[d] - shifted[d], hi[d] - iyee[d])
+                if isc[d] > iec[d]:
+                    empty = True
+                    break
+                ends = _chunk_weights(isc[d] + shifted[d], iec[d] + shifted[d], is_[d], ie[d], tapers[d])
+                weights.append(ends + ((iec[d] - isc[d]) // 2 + 1,))
+            if empty:
+                continue
+            cells: List[Tuple[int, int, int]] = []
+            amps: List[complex] = []
+            for coords, cell, value in points:
+                if any(not isc[d] <= coords[d] <= iec[d] for d in range(3)):
+                    continue
+                factors = []
+                for d in range(3):
+                    ws0, ws1, we0, we1, n = weights[d]
+                    factors.append(loop_weight((coords[d] - isc[d]) // 2, n, ws0, ws1, we0, we1))
+                weight = factors[2] * (factors[1] * (1.0 * factors[0]))
+                if cell is None:
+                    continue
+                scaled = (weight * pass_amp[0], weight * pass_amp[1])
+                product = _cmul(scaled, value)
+                cells.append(cell)
+                amps.append(complex(product[0], product[1]))
+            if cells:
+                pieces.append((chunk, cells, amps))
         for d in range(3):
             if shift[d] + 1 <= max_shift[d]:
                 shift[d] += 1
@@ -332,9 +385,54 @@ def deposition_table(grid: Grid, component: str, center: Sequence[float], size: 
             shift[d] = min_shift[d]
         else:
             break
+    return pieces
+
+
+def deposition_table(grid: Grid, component: str, center: Sequence[float], size: Sequence[float],
+                     amplitude: complex = 1.0,
+                     amp_func: Optional[Callable[[float, float, float], complex]] = None,
+                     ) -> Tuple[List[Tuple[int, int, int]], List[complex]]:
+    """Every cell a source deposits into (D for an electric one, B for a magnetic one),
+    once, with its pieces' amplitudes summed in placement order (one chunk spanning the
+    window; reference ``sources.py:1144`` ``_summed_table``)."""
+    accumulated: Dict[Tuple[int, int, int], complex] = {}
+    for _chunk, cells, amps in deposition_pieces(grid, component, center, size, amplitude, amp_func):
+        for cell, value in zip(cells, amps):
+            previous = accumulated.get(cell)
+            accumulated[cell] = value if previous is None else complex(previous.real + value.real,
+                                                                       previous.imag + value.imag)
     cells = list(accumulated)
-    amps = [complex(*accumulated[c]) for c in cells]
-    return cells, amps
+    return cells, [accumulated[c] for c in cells]
+
+
+def bind_src_vols(sources: Sequence["Source"], grid: Grid, faces) -> None:
+    """Give every source the entries it deposits in MEEP's ``src_vol`` lists (reference
+    ``sources.py:1585`` ``bind_src_vols``): one piece per (lattice shift, chunk); a piece
+    whose chunk, component, waveform and cells equal an earlier entry's is summed into it
+    and deposits once; pieces that share a cell without sharing their cells -- the two
+    ends of a request across a periodic seam -- stay two entries, and the cell is
+    deposited twice. Each source's ``cells`` / ``amps`` become its entries, in creation
+    order.
+    """
+    boxes = chunk_boxes(grid, faces)
+    entries = {}
+    owned: Dict[int, List[list]] = {}
+    for index, source in enumerate(sources):
+        key_time = _waveform_key(source.waveform) or ("object", id(source.waveform))
+        for chunk, cells, amps in deposition_pieces(grid, source.component, source.center, source.size,
+                                                    source.amplitude, source.amp_func, boxes):
+            key = (chunk, source.component, key_time, tuple(cells))
+            entry = entries.get(key)
+            if entry is None:
+                entry = [cells, list(amps)]
+                entries[key] = entry
+                owned.setdefault(index, []).append(entry)
+                continue
+            entry[1] = [complex(x.real + y.real, x.imag + y.imag) for x, y in zip(entry[1], amps)]
+    for index, source in enumerate(sources):
+        mine = owned.get(index, [])
+        source.cells = [cell for cells, _ in mine for cell in cells]
+        source.amps = [amp for _, amps in mine for amp in amps]
 
 
 @dataclass

@@ -341,9 +341,10 @@ static REAL SUF(sample_at)(const SUF(oracle_state)* s, const REAL* f, int i, int
   const int n[3] = {s->nx, s->ny, s->nz};
   int at[3] = {i, j, k};
   for (int a = 0; a < 3; ++a) {
-    if (at[a] >= n[a]) {
+    if (at[a] >= n[a] || at[a] < 0) {
       if (s->metallic[a]) return (REAL)0;
-      at[a] -= n[a];
+      at[a] %= n[a];
+      if (at[a] < 0) at[a] += n[a];
     }
   }
   return f[SUF(lin)(s, at[0], at[1], at[2])];

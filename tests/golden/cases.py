@@ -48,6 +48,14 @@ CASES = {
                           boundaries=("metallic", "periodic", "metallic")),
     "complex_cond": dict(n=(14, 12, 16), pml=3, steps=50, conductivity="band", magnetic=True,
                          complex=True),
+    # Bloch-periodic fields (complex, k != 0): phased x and y with an interior point
+    # source, a DFT volume and a flux plane spanning the whole y-z cross-section; and
+    # a phased x axis under a z PML with a line source wrapping the phased axis, odd
+    # and even counts.
+    "bloch": dict(n=(12, 13, 14), pml=0, steps=50, complex=True, boundaries="periodic",
+                  k_point=(0.3, -0.2, 0.0), bloch_monitors=True),
+    "bloch_pml": dict(n=(15, 12, 16), pml={"z": 3}, steps=50, complex=True, boundaries="periodic",
+                      k_point=(0.45, 0.0, 0.0), bloch_line=True, bloch_monitors=True),
 }
 
 # The 80^3 sphere-under-PML workload (resolution 10, 10-cell PML, eps 4 sphere of radius
@@ -63,6 +71,7 @@ def build_case(driver_cls, susceptibility_cls, case: dict, reference: bool = Fal
     boundaries = case.get("boundaries", "metallic")
     d = driver_cls(cell_size=lengths, resolution=res, courant=0.5,
                    force_complex_fields=bool(case.get("complex", False)),
+                   k_point=case.get("k_point", (0.0, 0.0, 0.0)),
                    boundaries=boundaries, **({"prefer_gpu": False} if reference else {}))
     if case["pml"]:
         d.setup_pml(case["pml"])
@@ -91,6 +100,16 @@ def build_case(driver_cls, susceptibility_cls, case: dict, reference: bool = Fal
     d.add_source({"source_type": "gaussian", "component": "Ez",
                   "center": (source_x, 0.03, 0.0), "size": (0, 0, 0),
                   "frequency": fcen, "fwidth": fwidth})
+    if case.get("bloch_line"):
+        d.add_source({"source_type": "gaussian", "component": "Ey", "center": (0.0, -0.1, 0.1),
+                      "size": (lengths[0], 0, 0), "frequency": fcen, "fwidth": fwidth,
+                      "amplitude": 0.7})
+    if case.get("bloch_monitors"):
+        flux.append(d.add_flux_monitor(fcen=fcen, df=fwidth / 2, nfreq=3, center=(0, 0, 0.25),
+                                       size=(lengths[0], lengths[1], 0), decimation_factor=1))
+        dft.append(d.add_dft_monitor(frequencies=[fcen, 1.5 * fcen], components=("Ex", "Ez", "Hy"),
+                                     center=(0.0, 0.0, 0.0), size=(lengths[0], lengths[1], 0.4),
+                                     decimation_factor=2))
     if case.get("magnetic"):
         d.add_source({"source_type": "gaussian", "component": "Hx", "center": (0.1, -0.05, 0.07),
                       "size": (0, 0, 0), "frequency": fcen, "fwidth": fwidth})

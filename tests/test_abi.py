@@ -80,6 +80,8 @@ int main(void) {
   F(mgb_pole, sigma) F(mgb_pole, p) F(mgb_sim_desc, conductivity)
   F(mgb_conductivity, condinv) F(mgb_conductivity, fcond) F(mgb_conductivity, chunk_of)
   F(mgb_conductivity, keeps) F(mgb_sim_desc, nsrc_magnetic) F(mgb_sim_desc, src_box_magnetic)
+  F(mgb_sim_desc, bloch_axes) F(mgb_sim_desc, bloch_phase) F(mgb_sim_desc, partner_E)
+  F(mgb_sim_desc, partner_H)
   return 0;
 }
 """

@@ -58,13 +58,13 @@ def test_fields_are_the_reference_words(gpu, name, mode):
     case = CASES[name]
     gold = golden_io.fields(name)
     tileable = case["n"][2] % 4 == 0
-    if case.get("conductivity") and mode not in ("generic", "l2"):
-        pytest.skip("a lossy run steps with the generic kernels only (the others are refused)")
+    if (case.get("conductivity") or case.get("k_point")) and mode not in ("generic", "l2"):
+        pytest.skip("lossy and Bloch-phased runs step with the generic kernels only (the others are refused)")
     if mode in ("tiles", "ws") and not tileable:
         mode = "generic"
     kernels = MODES[mode]
-    if case.get("conductivity") and mode == "l2":
-        kernels = (4, 32, 4, 4)  # a lossy run takes families 0 and 4
+    if (case.get("conductivity") or case.get("k_point")) and mode == "l2":
+        kernels = (4, 32, 4, 4)  # lossy and Bloch-phased runs take families 0 and 4
     driver, flux, dft = gpu_case(case, kernels=kernels)
     assert driver.engine.uses_tiles == (mode in ("tiles", "ws"))
     for c in FIELDS:

@@ -39,7 +39,7 @@ def run_complex_case(case, precision="f32"):
     return driver, parts[0], parts[1]
 
 
-@pytest.mark.parametrize("name", sorted(n for n, c in CASES.items() if c.get("complex")))
+@pytest.mark.parametrize("name", sorted(n for n, c in CASES.items() if c.get("complex") and not c.get("k_point")))
 def test_complex_case_is_two_real_oracle_runs(name):
     """The reference's complex run at k = 0: its real words are one float32 oracle run
     driven by real(A), its imaginary words another driven by imag(A); its transforms are

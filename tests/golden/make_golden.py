@@ -16,7 +16,10 @@ beside the repository) and writes small fixtures into this directory:
   keeps a conductivity, for seeded configurations (``python make_golden.py conductivity``);
 * ``flux_normalization.npz``: the two-run normalisation idiom (``python make_golden.py
   flux_norm``): the vacuum run's saved flux-plane transforms and spectrum, and the
-  structure run's spectrum started from minus them and alone.
+  structure run's spectrum started from minus them and alone;
+* ``src_vol_tables.npz``: each source's deposit entries in MEEP's ``src_vol`` lists
+  (``python make_golden.py src_vols``) for seeded multi-source cells, with the Bloch
+  factors ``eikna`` of each.
 
 The fixtures are committed; this script is how they were made. It is not run by the
 tests (the reference is not available where the GPU tests run).
@@ -216,6 +219,36 @@ def record_flux_normalization() -> None:
     print("flux normalization written")
 
 
+from tests.golden.make_golden_configs import SRC_VOL_CONFIGS, src_vol_config  # noqa: E402
+
+
+def record_src_vols() -> None:
+    from meep_gpu.chunk_map import ChunkLayout
+    from meep_gpu.sources import bind_src_vols
+
+    out = {}
+    for t in range(SRC_VOL_CONFIGS):
+        dims, k, pml, specs = src_vol_config(t)
+        d = FdtdDriver(cell_size=dims, resolution=10, k_point=k, boundaries="periodic", prefer_gpu=False,
+                       force_complex_fields=True)
+        if pml is not None:
+            d.setup_pml(pml)
+        for spec in specs:
+            d.add_source(spec)
+        bind_src_vols(d._sources, ChunkLayout.one_rank(d.grid, d.pml), d.grid)
+        for m, source in enumerate(d._sources):
+            cells, amps = [], []
+            for table in source._src_vol:
+                ix, iy, iz = (np.asarray(a).reshape(-1) for a in (table.ix, table.iy, table.iz))
+                cells += [(int(a), int(b), int(c)) for a, b, c in zip(ix, iy, iz)]
+                amps += list(np.asarray(table.amps).reshape(-1))
+            out[f"c{t}_s{m}_cells"] = np.asarray(cells, dtype=np.int64).reshape(-1, 3)
+            out[f"c{t}_s{m}_amps"] = np.asarray(amps, dtype=np.complex128)
+        out[f"c{t}_eikna"] = np.asarray([complex(p) if p is not None else 0j for p in d.grid.bloch_phases])
+    np.savez_compressed(HERE / "src_vol_tables.npz", **out)
+    print("src_vol tables written")
+
+
 if __name__ == "__main__":
     which = sys.argv[1:] or ["fields", "digest", "tables"]
     if "fields" in which or any(w in CASES for w in which):
@@ -230,3 +263,5 @@ if __name__ == "__main__":
         record_conductivity_tables()
     if "flux_norm" in which:
         record_flux_normalization()
+    if "src_vols" in which:
+        record_src_vols()

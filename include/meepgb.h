@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define MGB_ABI_VERSION 2
+#define MGB_ABI_VERSION 3
 #define MGB_MAX_POLES 4
 #define MGB_MAX_MONITORS 16
 #define MGB_MAX_MONITOR_COMPONENTS 6
@@ -106,6 +106,21 @@ typedef struct mgb_conductivity {
   uint32_t keeps[2][3];
 } mgb_conductivity;
 
+/* The ghost words of mirror-folded axes, built by the caller (see mgb_sim_desc.mirror).
+ * [0]: the B ghosts (H half), [1]: the D ghosts (E half). Entry t of a list: the ghost's
+ * cell offset, the offset of the stored word it images, and a code (bits 0-1 the
+ * component 0..2, bit 2 negate, bit 3 zero: the ghost sits on a metallic wall of
+ * another axis). saved[h]: device scratch of MGB_FOLD_WORDS * count[h] floats, zeroed
+ * by the caller, where the library keeps each ghost's state from before its half. */
+#define MGB_FOLD_WORDS (2 + MGB_MAX_POLES)
+typedef struct mgb_fold {
+  int32_t count[2];
+  const int32_t* ghost[2];
+  const int32_t* image[2];
+  const uint8_t* code[2];
+  float* saved[2];
+} mgb_fold;
+
 typedef struct mgb_sim_desc {
   int32_t abi_version; /* MGB_ABI_VERSION */
   int32_t nx, ny, nz;
@@ -168,6 +183,17 @@ typedef struct mgb_sim_desc {
   double bloch_phase[3][2];
   const float* partner_E[3];
   const float* partner_H[3];
+  /* mirror symmetry (MEEP's mp.Mirror): mirror[a] = +1 (even) or -1 (odd) folds the
+   * metallic axis a about the plane at its stored cell 1 (MEEP's halve(): n = full -
+   * full/2 + 1 stored cells from one cell below the plane, the far wall metallic[a]);
+   * 0: no plane. full[a]: the unfolded cell count. Cell 0 of every component with Yee
+   * shift 0 on a folded axis is the plane's ghost: after each half's sources the library
+   * writes it from stored row 2 with the component's parity (the `fold` lists) and steps
+   * its E (H) from that word. Monitors read a ladder site below the plane from its
+   * image. Folded runs are refused by the batch and the adjoint. */
+  int32_t mirror[3];
+  int32_t full[3];
+  mgb_fold fold;
 } mgb_sim_desc;
 
 typedef struct mgb_sim mgb_sim;

@@ -9,10 +9,10 @@ from .conductivity import AbsorberLayer
 from .dft import DFTMonitor, FluxDftData, FluxMonitor, FluxPlaneDft
 from .dispersion import DRUDE, LORENTZ, Susceptibility
 from .driver import FdtdCancelled, FdtdDivergence, FdtdDriver
-from .grid import Grid, Unsupported
+from .grid import Grid, Mirror, Unsupported
 from .pml import PML
 
 __all__ = ["FdtdDriver", "FdtdCancelled", "FdtdDivergence", "Susceptibility", "LORENTZ",
            "DRUDE", "Grid", "PML", "FluxMonitor", "DFTMonitor", "Unsupported", "AbsorberLayer",
-           "FluxDftData", "FluxPlaneDft"]
+           "FluxDftData", "FluxPlaneDft", "Mirror"]
 __version__ = "0.1.0"

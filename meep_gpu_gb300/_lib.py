@@ -14,7 +14,7 @@ from typing import Optional
 
 PACKAGE = Path(__file__).resolve().parent
 
-MGB_ABI_VERSION = 2
+MGB_ABI_VERSION = 3
 MGB_MAX_POLES = 4
 MGB_MAX_MONITORS = 16
 MGB_MAX_MONITOR_COMPONENTS = 6
@@ -62,6 +62,20 @@ class MgbConductivity(ctypes.Structure):
     ]
 
 
+MGB_FOLD_WORDS = 2 + MGB_MAX_POLES
+
+
+class MgbFold(ctypes.Structure):
+    """``mgb_fold``: the B (0) and D (1) ghost lists of mirror-folded axes."""
+    _fields_ = [
+        ("count", ctypes.c_int32 * 2),
+        ("ghost", ctypes.c_void_p * 2),
+        ("image", ctypes.c_void_p * 2),
+        ("code", ctypes.c_void_p * 2),
+        ("saved", ctypes.c_void_p * 2),
+    ]
+
+
 class MgbSimDesc(ctypes.Structure):
     _fields_ = [
         ("abi_version", ctypes.c_int32),
@@ -99,6 +113,9 @@ class MgbSimDesc(ctypes.Structure):
         ("bloch_phase", (ctypes.c_double * 2) * 3),
         ("partner_E", ctypes.c_void_p * 3),
         ("partner_H", ctypes.c_void_p * 3),
+        ("mirror", ctypes.c_int32 * 3),
+        ("full", ctypes.c_int32 * 3),
+        ("fold", MgbFold),
     ]
 
 

@@ -44,6 +44,8 @@ class FluxAdjoint:
             raise Unsupported("the adjoint step does not carry a conductivity")
         if driver.complex_fields:
             raise Unsupported("the adjoint gradient takes real fields (force_complex_fields=False)")
+        if driver.grid.has_symmetry:
+            raise Unsupported("the adjoint step does not carry mirror symmetry")
         if driver.engine is not None:
             raise RuntimeError("the adjoint problem needs a driver that has not been stepped")
         if steps < 1 or checkpoint_every < 1:

@@ -108,8 +108,10 @@ def _layer_sigma(coordinates: np.ndarray, layer: AbsorberLayer, half_length: flo
 
 
 def snapped_lengths(grid: Grid) -> Tuple[float, float, float]:
-    """The cell lengths snapped to the grid, n * dx (the reference's Grid.Lx/Ly/Lz)."""
-    return tuple(n * grid.dx for n in grid.shape)  # type: ignore[return-value]
+    """The unfolded cell lengths snapped to the grid, n * dx (the reference's
+    Grid.Lx/Ly/Lz); on a folded axis the full cell's, so a low-face absorber there never
+    reaches a stored cell (reference ``absorber.py:174``)."""
+    return tuple(n * grid.dx for n in grid.shape_full)  # type: ignore[return-value]
 
 
 def _axis_coordinates(grid: Grid, axis: int, shift: int) -> np.ndarray:

@@ -108,6 +108,15 @@ struct StepParams {
   const float* pH[3];
 };
 
+// The ghost lists of mirror-folded axes (mgb_fold), passed to the fold kernels.
+struct FoldArgs {
+  int count[2];
+  const int32_t* ghost[2];
+  const int32_t* image[2];
+  const uint8_t* code[2];
+  float* saved[2];
+};
+
 // Tensor maps of the tile kernels (each 64-byte aligned, passed as __grid_constant__).
 struct TileMaps {
   CUtensorMap E[3];     // box 68 x 9 x 1 (halo above in z and y)
@@ -139,6 +148,11 @@ struct DftParams {
   int part;
   const float* pE[3];
   const float* pH[3];
+  // mirror folds: bit a of `fold` folds axis a (full[a] unfolded cells); bit a of
+  // neg[comp] says the component is odd about that plane
+  int fold;
+  int full[3];
+  int neg[6];
 };
 
 __device__ __forceinline__ bool in_runs(const mgb_aux& a, int x) {
@@ -1626,8 +1640,41 @@ __device__ __forceinline__ float field_at(const DftParams& p, int comp, int i, i
   // A monitor's ladder may reach past a periodic face (MEEP's lattice-image gather): the
   // ladder point r samples stored cell r mod n, one lattice vector (or more) away from
   // it; past a metallic face the wall holds zero.
-  const int raw[3] = {i, j, k};
   const int n[3] = {p.nx, p.ny, p.nz};
+  if (p.fold) {
+    // A folded axis (MEEP's sn loop, reference dft.py:1004): site r of a component with
+    // Yee shift s sits at doubled -2 + 2r + s; outside the unfolded cell's owned window
+    // (its walls) it reads zero, below the plane it is the image at -d with the
+    // component's parity, and at the far wall (stored index n) zero.
+    int at[3] = {i, j, k};
+    bool flip = false;
+    const int q = comp % 3;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      if (!((p.fold >> a) & 1)) {
+        if (at[a] < 0 || at[a] >= n[a]) {
+          if (p.met[a]) return 0.f;
+          at[a] %= n[a];
+          if (at[a] < 0) at[a] += n[a];
+        }
+        continue;
+      }
+      const int s = (comp < 3) == (a == q) ? 1 : 0;
+      const int low = -(p.full[a] - p.full[a] % 2);
+      int d = -2 + 2 * at[a] + s;
+      if (d < low + 2 - s || d > low + 2 * p.full[a] - s) return 0.f;
+      if (d < -s) {
+        d = -d;
+        if ((p.neg[comp] >> a) & 1) flip = !flip;
+      }
+      at[a] = (d + 2 - s) >> 1;
+      if (at[a] >= n[a]) return 0.f;
+    }
+    const long long c = ((long long)at[0] * p.ny + at[1]) * p.nz + at[2];
+    const float own = comp < 3 ? p.E[comp][c] : p.H[comp - 3][c];
+    return flip ? -own : own;
+  }
+  const int raw[3] = {i, j, k};
   int at[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
@@ -2164,6 +2211,146 @@ __global__ void __launch_bounds__(256) copy_box(const __grid_constant__ StepPara
   b.dst[t] = src[((long long)i * p.ny + j) * p.nz + k];
 }
 
+// ------------------------------------------------------------------------------------
+// Mirror folds (reference stepping.py:2004-2045 fill_symmetry_bc_B/D). Cell 0 of a
+// component with Yee shift 0 on a folded axis is the plane's ghost: the step kernels
+// treat it as a metallic wall sample (curl masked, as MEEP's owned-cell loop skips it),
+// and after the half's sources it becomes the parity-signed word of stored row 2 (the
+// product of the parities at a corner), then zero_metal of the other axes' walls, and
+// its E (H) is stepped from that word with the ghost's own coefficients. The step
+// kernels have by then overwritten the ghost's E, f_w and P (H, f_w) from the wall word,
+// so each ghost's state from before the half is kept in `saved` (words [w * count + t]):
+// the H fold kernel keeps the D ghosts' state for the E half that follows, the E fold
+// kernel the B ghosts' state for the next step's H half.
+
+__device__ __forceinline__ void cell_of(const StepParams& p, int c, int& i, int& j, int& k) {
+  const int sx = p.ny * p.nz;
+  i = c / sx;
+  const int r = c - i * sx;
+  j = r / p.nz;
+  k = r - j * p.nz;
+}
+
+__device__ __forceinline__ int coord_along(int q, int i, int j, int k) { return q == 0 ? i : q == 1 ? j : k; }
+
+__device__ __forceinline__ long long pole_index(const StepParams& p, int i, int j, int k, bool& in_box) {
+  in_box = p.npoles > 0 && i >= p.pbox[0] && i < p.pbox[1] && j >= p.pbox[2] && j < p.pbox[3] &&
+           k >= p.pbox[4] && k < p.pbox[5];
+  if (!in_box) return 0;
+  const int bny = p.pbox[3] - p.pbox[2], bnz = p.pbox[5] - p.pbox[4];
+  return ((long long)(i - p.pbox[0]) * bny + (j - p.pbox[2])) * bnz + (k - p.pbox[4]);
+}
+
+// The B ghosts' H and f_w before the H half.
+__device__ __forceinline__ void fold_keep_h(const StepParams& p, const FoldArgs& f, int t) {
+  const int n = f.count[0], g = f.ghost[0][t], q = f.code[0][t] & 3;
+  int i, j, k;
+  cell_of(p, g, i, j, k);
+  const bool sb = p.pml && in_runs(p.B[q], coord_along(q, i, j, k));
+  f.saved[0][t] = p.H[q][g];
+  f.saved[0][n + t] = sb ? p.fwH[q].data[g] : 0.f;
+}
+
+// The D ghosts' E, f_w and the polarization the E half overwrites, before the E half.
+__device__ __forceinline__ void fold_keep_e(const StepParams& p, const FoldArgs& f, int t, int parity) {
+  const int n = f.count[1], g = f.ghost[1][t], q = f.code[1][t] & 3;
+  int i, j, k;
+  cell_of(p, g, i, j, k);
+  const bool sw = p.pml && in_runs(p.fwE[q], coord_along(q, i, j, k));
+  f.saved[1][t] = p.E[q][g];
+  f.saved[1][n + t] = sw ? p.fwE[q].data[g] : 0.f;
+  bool in_box;
+  const long long pb = pole_index(p, i, j, k, in_box);
+  for (int m = 0; m < p.npoles; ++m) {
+    const mgb_pole& pole = p.poles[m];
+    const float* prv = parity ? pole.p[q][0] : pole.p[q][1];
+    f.saved[1][(2 + m) * n + t] = (in_box && pole.sigma[q] != nullptr) ? prv[pb] : 0.f;
+  }
+}
+
+// One B ghost: B from its image, zero_metal_B, then update_H on its own-axis membership.
+__device__ __forceinline__ void fold_h_ghost(const StepParams& p, const FoldArgs& f, int t, int first_step) {
+  const int n = f.count[0], g = f.ghost[0][t], r = f.image[0][t], code = f.code[0][t], q = code & 3;
+  int i, j, k;
+  cell_of(p, r, i, j, k);
+  const bool sb_image = p.pml && in_runs(p.B[q], coord_along(q, i, j, k));
+  float b = sb_image ? p.B[q].data[r] : p.H[q][r];
+  if (code & 4) b = -b;
+  if (code & 8) b = 0.f;
+  cell_of(p, g, i, j, k);
+  const int cq = coord_along(q, i, j, k);
+  float h = b;
+  if (p.pml && in_runs(p.B[q], cq)) {
+    const float h_old = f.saved[0][t], w_old = f.saved[0][n + t];
+    const float kps = ldgf(p.kps[kInteger][q], cq), kms = ldgf(p.kms[kInteger][q], cq);
+    h = (first_step ? b : h_old) + (kps * b - kms * (first_step ? b : w_old));
+    p.B[q].data[g] = b;
+    p.fwH[q].data[g] = b;
+  }
+  p.H[q][g] = h;
+}
+
+// One D ghost: D from its image, zero_metal_D, then update_E and update_P.
+__device__ __forceinline__ void fold_e_ghost(const StepParams& p, const FoldArgs& f, int t, int parity) {
+  const int n = f.count[1], g = f.ghost[1][t], r = f.image[1][t], code = f.code[1][t], q = code & 3;
+  float d = p.D[q][r];
+  if (code & 4) d = -d;
+  if (code & 8) d = 0.f;
+  p.D[q][g] = d;
+  int i, j, k;
+  cell_of(p, g, i, j, k);
+  const int cq = coord_along(q, i, j, k);
+  bool in_box;
+  const long long pb = pole_index(p, i, j, k, in_box);
+  float w = d;
+  if (in_box)
+    for (int m = 0; m < p.npoles; ++m) {
+      const mgb_pole& pole = p.poles[m];
+      if (pole.sigma[q] != nullptr) w = w - (parity ? pole.p[q][1] : pole.p[q][0])[pb];
+    }
+  w = __ldg(p.inv_eps[q] + g) * w;
+  float e = w;
+  if (p.pml && in_runs(p.fwE[q], cq)) {
+    const float e_old = f.saved[1][t], fw_old = f.saved[1][n + t];
+    e = e_old + (ldgf(p.kps[kHalf][q], cq) * w - ldgf(p.kms[kHalf][q], cq) * fw_old);
+    p.fwE[q].data[g] = w;
+  }
+  p.E[q][g] = e;
+  if (in_box)
+    for (int m = 0; m < p.npoles; ++m) {
+      const mgb_pole& pole = p.poles[m];
+      if (pole.sigma[q] == nullptr) continue;
+      const float* cur = parity ? pole.p[q][1] : pole.p[q][0];
+      float* prv = parity ? pole.p[q][0] : pole.p[q][1];
+      const float pp = f.saved[1][(2 + m) * n + t];
+      const float drive = pole.omega0dtsqr * (__ldg(pole.sigma[q] + pb) * w);
+      prv[pb] = pole.gamma1inv * ((cur[pb] * pole.two_minus_od - pole.gamma1 * pp) + drive);
+    }
+  if (!isfinite(e) && p.status != nullptr) atomicOr(p.status, 1);
+}
+
+// After the H half: the B ghosts, and the D ghosts' state for the E half of this step.
+__global__ void __launch_bounds__(256) fold_h(const __grid_constant__ StepParams p, const __grid_constant__ FoldArgs f,
+                                              int first_step, int parity) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < f.count[0]) fold_h_ghost(p, f, t, first_step);
+  if (t < f.count[1]) fold_keep_e(p, f, t, parity);
+}
+
+// After the E half: the D ghosts, and the B ghosts' state for the next step's H half.
+__global__ void __launch_bounds__(256) fold_e(const __grid_constant__ StepParams p, const __grid_constant__ FoldArgs f,
+                                              int parity) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < f.count[1]) fold_e_ghost(p, f, t, parity);
+  if (t < f.count[0]) fold_keep_h(p, f, t);
+}
+
+// The B ghosts' state, when a step is launched without the E fold of the step before.
+__global__ void __launch_bounds__(256) fold_keep(const __grid_constant__ StepParams p, const __grid_constant__ FoldArgs f) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < f.count[0]) fold_keep_h(p, f, t);
+}
+
 }  // namespace
 
 // ======================================================================================
@@ -2187,6 +2374,11 @@ struct mgb_sim {
   // prefetching marches, no batch slot, no adjoint).
   bool has_cond = false;
   mgb_conductivity cond = {};
+  // Mirror folds: the ghost lists, and the step whose H half the B ghosts' kept state is
+  // for (-1: none kept yet).
+  bool folded = false;
+  FoldArgs fold = {};
+  long long fold_kept = -1;
   size_t h_smem = 0, e_smem = 0, e_ws_smem = 0;
   const double* words = nullptr;
   long long words_first = 0;
@@ -2428,6 +2620,43 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
           if (cd.chunk_of[l][a] == nullptr)
             return fail(MGB_ERR_ARGUMENT, "a conductivity under a PML needs the chunk of every row (chunk_of)");
   }
+  int fold_mask = 0;
+  for (int a = 0; a < 3; ++a) {
+    if (d.mirror[a] == 0) continue;
+    if (d.mirror[a] != 1 && d.mirror[a] != -1)
+      return fail(MGB_ERR_ARGUMENT, "a mirror phase must be +1 (even) or -1 (odd)");
+    if (!d.metallic[a])
+      return fail(MGB_ERR_UNSUPPORTED, "a mirror plane on a periodic axis is not stepped by this engine");
+    if (d.full[a] < 2 || n[a] != d.full[a] - d.full[a] / 2 + 1 || n[a] < 4)
+      return fail(MGB_ERR_ARGUMENT, "a folded axis stores full - full/2 + 1 cells (at least 4)");
+    fold_mask |= 1 << a;
+  }
+  if (fold_mask != 0) {
+    if (d.bloch_axes != 0) return fail(MGB_ERR_UNSUPPORTED, "a folded run carries no Bloch phase");
+    const long long cells = (long long)n[0] * n[1] * n[2];
+    for (int h = 0; h < 2; ++h) {
+      const int count = d.fold.count[h];
+      if (count < 0 || (count > 0 && (d.fold.ghost[h] == nullptr || d.fold.image[h] == nullptr ||
+                                      d.fold.code[h] == nullptr || d.fold.saved[h] == nullptr)))
+        return fail(MGB_ERR_ARGUMENT, "a mirror-fold ghost list is missing");
+      if (count == 0) continue;
+      // every offset inside the volume and every component 0..2, checked on the host once
+      std::vector<int32_t> ghost(count), image(count);
+      std::vector<uint8_t> code(count);
+      if (cudaMemcpy(ghost.data(), d.fold.ghost[h], count * sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess ||
+          cudaMemcpy(image.data(), d.fold.image[h], count * sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess ||
+          cudaMemcpy(code.data(), d.fold.code[h], count * sizeof(uint8_t), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(MGB_ERR_ARGUMENT, "the mirror-fold ghost lists are not readable device memory");
+      }
+      for (int t = 0; t < count; ++t)
+        if (ghost[t] < 0 || ghost[t] >= cells || image[t] < 0 || image[t] >= cells || (code[t] & 3) == 3 ||
+            (code[t] & ~15) != 0)
+          return fail(MGB_ERR_ARGUMENT, "a mirror-fold ghost entry lies outside the volume");
+    }
+  } else if (d.fold.count[0] != 0 || d.fold.count[1] != 0) {
+    return fail(MGB_ERR_ARGUMENT, "mirror-fold ghost lists without a mirror plane");
+  }
   mgb_sim* sim = new (std::nothrow) mgb_sim();
   if (sim == nullptr) return fail(MGB_ERR_ARGUMENT, "host allocation of the plan failed");
   sim->desc = d;
@@ -2492,6 +2721,16 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
     if (std::fabs(im) < 1e-13 && std::fabs(re - 1.0) < 1e-13) p.bmode[a] = 1;
     else if (std::fabs(im) < 1e-13 && std::fabs(re + 1.0) < 1e-13) { p.bmode[a] = 2; p.bre[a] = -1.f; }
     else { p.bmode[a] = 3; p.bre[a] = (float)re; p.bim[a] = (float)im; }
+  }
+  if (fold_mask != 0) {
+    sim->folded = true;
+    for (int h = 0; h < 2; ++h) {
+      sim->fold.count[h] = d.fold.count[h];
+      sim->fold.ghost[h] = d.fold.ghost[h];
+      sim->fold.image[h] = d.fold.image[h];
+      sim->fold.code[h] = d.fold.code[h];
+      sim->fold.saved[h] = d.fold.saved[h];
+    }
   }
   setup_tiles(sim);
   *out = sim;
@@ -2571,7 +2810,7 @@ int flush_monitor(mgb_sim* sim, int m, cudaStream_t s) {
 }
 
 // Launches of one step, split by part so mgb_step and mgb_launch share them.
-int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s) {
+int launch_part_kernels(mgb_sim* sim, long long n, int part, cudaStream_t s) {
   StepParams& p = sim->step;
   const bool pml = sim->desc.pml_active != 0;
   if (part == 0 || part == 1) {
@@ -2643,6 +2882,19 @@ int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s) {
     for (int a = 0; a < 3; ++a) q.met[a] = p.met[a];
     for (int c = 0; c < 3; ++c) { q.E[c] = p.E[c]; q.H[c] = p.H[c]; }
     q.mon = mon;
+    if (sim->folded) {
+      for (int a = 0; a < 3; ++a) {
+        if (sim->desc.mirror[a] == 0) continue;
+        q.fold |= 1 << a;
+        q.full[a] = sim->desc.full[a];
+        // E/D odd about the plane normal to its own direction, H/B about the others
+        for (int comp = 0; comp < 6; ++comp) {
+          const bool own = comp % 3 == a;
+          const int parity = (comp < 3) == own ? -sim->desc.mirror[a] : sim->desc.mirror[a];
+          if (parity < 0) q.neg[comp] |= 1 << a;
+        }
+      }
+    }
     q.bloch = p.bloch;
     q.part = p.part;
     for (int a = 0; a < 3; ++a) {
@@ -2664,6 +2916,26 @@ int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s) {
     }
     const size_t smem = (size_t)mon.nfreq * 2 * sizeof(float2);
     dft_accumulate<<<blocks, 256, smem, s>>>(q, post);
+  }
+  return MGB_OK;
+}
+
+// One part of step n, with the mirror folds after each half of a folded run.
+int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s) {
+  if (!sim->folded || part == 2) return launch_part_kernels(sim, n, part, s);
+  const StepParams& p = sim->step;
+  const int count = std::max(sim->fold.count[0], sim->fold.count[1]);
+  const unsigned blocks = (unsigned)((count + 255) / 256);
+  if (part == 0 && sim->fold_kept != n && sim->fold.count[0] > 0)
+    fold_keep<<<(unsigned)((sim->fold.count[0] + 255) / 256), 256, 0, s>>>(p, sim->fold);
+  const int rc = launch_part_kernels(sim, n, part, s);
+  if (rc != MGB_OK) return rc;
+  if (blocks == 0) return MGB_OK;
+  if (part == 0) {
+    fold_h<<<blocks, 256, 0, s>>>(sim->step, sim->fold, (int)(n == 0), (int)(n & 1));
+  } else {
+    fold_e<<<blocks, 256, 0, s>>>(sim->step, sim->fold, (int)(n & 1));
+    sim->fold_kept = n + 1;
   }
   return MGB_OK;
 }
@@ -3083,6 +3355,7 @@ int mgb_batch_set_slot(mgb_batch* b, int32_t slot, mgb_sim* sim, int64_t end_ste
   if (sim->has_cond) return fail(MGB_ERR_UNSUPPORTED, "a batched slot does not carry a conductivity");
   if (sim->step.nsrc_h > 0) return fail(MGB_ERR_UNSUPPORTED, "a batched slot does not carry magnetic sources");
   if (sim->step.bloch) return fail(MGB_ERR_UNSUPPORTED, "a batched slot does not carry Bloch phases");
+  if (sim->folded) return fail(MGB_ERR_UNSUPPORTED, "a batched slot does not carry mirror folds");
   if (sim->desc.nmonitors > kSlotMonitors)
     return fail(MGB_ERR_UNSUPPORTED, "a batched slot holds at most " + std::to_string(kSlotMonitors) + " monitors");
   for (int m = 0; m < sim->desc.nmonitors; ++m) {
@@ -3310,6 +3583,7 @@ int mgb_adjoint_step(mgb_sim* adj, const mgb_adjoint* a, int64_t step, void* str
     return fail(MGB_ERR_ARGUMENT, "null argument");
   if (adj->step.npoles != 0) return fail(MGB_ERR_UNSUPPORTED, "the adjoint step does not carry susceptibility poles");
   if (adj->has_cond) return fail(MGB_ERR_UNSUPPORTED, "the adjoint step does not carry a conductivity");
+  if (adj->folded) return fail(MGB_ERR_UNSUPPORTED, "the adjoint step does not carry mirror folds");
   for (int q = 0; q < 3; ++q)
     if (a->mu_b[q] == nullptr || a->mu_d[q] == nullptr) return fail(MGB_ERR_ARGUMENT, "missing mu volume");
   const StepParams& p = adj->step;
@@ -3390,6 +3664,7 @@ int mgb_adjoint_segment(mgb_sim* fwd, mgb_sim* adj, const mgb_adjoint* a, int64_
   if (nsteps < 1) return fail(MGB_ERR_ARGUMENT, "a segment has at least one step");
   if (monitor < 0 || monitor >= adj->desc.nmonitors) return fail(MGB_ERR_ARGUMENT, "no such monitor");
   if (fwd->has_cond || adj->has_cond) return fail(MGB_ERR_UNSUPPORTED, "the adjoint step does not carry a conductivity");
+  if (fwd->folded || adj->folded) return fail(MGB_ERR_UNSUPPORTED, "the adjoint step does not carry mirror folds");
   int rc = check_words(fwd, first_step, nsteps);
   if (rc != MGB_OK) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -115,7 +115,9 @@ def volume_bounds(center: Sequence[float], size: Sequence[float], what: str):
 def register_volume(grid: Grid, center: Sequence[float], size: Sequence[float], what: str):
     """Half-open stored-index region ``(x0, x1, y0, y1, z0, z1)`` a monitor volume covers.
 
-    Non-wrapping axes clamp the ladder to the stored grid. On a wrapping axis the
+    Non-wrapping axes clamp the ladder to the stored grid, a folded one to the unfolded
+    cell (its sites below the plane are read from their mirror images, with the
+    component's parity, by the device sampling). On a wrapping axis the
     ladder is kept whole even where it reaches past a face: its cells past the face
     sample the lattice images of stored cells (MEEP's lattice-shift gather,
     ``loop_in_chunks``; reference ``dft.py:927`` ``_lattice_gather``), which the device
@@ -131,7 +133,14 @@ def register_volume(grid: Grid, center: Sequence[float], size: Sequence[float], 
                 raise Unsupported(f"{what} reaches more than one period past the {AXIS_NAMES[axis]} face")
             region += [first, first + count]
             continue
-        lo, hi = max(first, 0), min(first + count, n)
+        low = 0
+        if grid.is_mirrored(axis):
+            # a folded axis serves the sites below the plane from their images (reference
+            # dft.py:1004 folded_axis_sites): the region may start below the stored cells,
+            # down to the unfolded cell's low wall
+            full = grid.shape_full[axis]
+            low = 1 - (full - full % 2) // 2
+        lo, hi = max(first, low), min(first + count, n)
         if hi <= lo:
             raise ValueError(f"{what} lies outside the cell on the {AXIS_NAMES[axis]} axis")
         region += [lo, hi]

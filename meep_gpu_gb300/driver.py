@@ -5,7 +5,8 @@ Mirrors ``meep_gpu/driver.py``'s ``FdtdDriver`` (constructor :810, ``set_epsilon
 ``add_dft_monitor`` :2783, ``add_flux_monitor`` :3001, ``step`` :3419, ``run`` :3667,
 ``get_field`` :4056, ``set_conductivity`` :1649, ``set_b_conductivity`` :1752,
 ``set_absorber`` :1863) for the configurations this engine steps: 3-D, real float32 or
-complex64 fields, metallic, periodic or Bloch-periodic boundaries, no mirror symmetry, isotropic or
+complex64 fields, metallic, periodic or Bloch-periodic boundaries, mirror planes (``Mirror``)
+folding metallic axes, isotropic or
 diagonal chi1inv, Lorentz/Drude poles, D and B conductivity (material and
 ``mp.Absorber``), electric sources and DFT/flux monitors.
 Anything else is refused by name when it is asked for, never approximated.
@@ -65,14 +66,12 @@ class FdtdDriver:
                  gpu_id: int = 0, launch_shape: Optional[Tuple[int, int, int]] = None,
                  kernels: Optional[Tuple[int, int, int, int]] = None,
                  dft_accumulation: Optional[str] = None):
-        if tuple(symmetry):
-            raise Unsupported("mirror symmetry is not stepped by this engine")
         if dimensions != 3 or cylindrical:
             raise Unsupported("only 3-D Cartesian runs are stepped by this engine")
         if beta != 0.0 or any(float(k) != 0.0 for k in bfast_scaled_k):
             raise Unsupported("out-of-plane beta and BFAST are not stepped by this engine")
         del m, accurate_fields_near_cylorigin, prefer_gpu
-        self.grid = Grid(cell_size, resolution, courant, boundaries, k_point)
+        self.grid = Grid(cell_size, resolution, courant, boundaries, k_point, symmetry)
         # complex64 fields (the reference's default): at k = 0 the real and imaginary
         # parts step as two real runs (engine.ComplexEngine)
         self.complex_fields = bool(force_complex_fields)

@@ -31,7 +31,7 @@ import torch
 from . import _lib
 from .conductivity import coefficients, keeps_mask, piece_line
 from .dft import COMPONENTS, FluxMonitor, _Monitor
-from .grid import Grid
+from .grid import IYEE, Grid
 from .pml import (HALF, INTEGER, PML, aux_shape, constitutive_aux_key, curl_aux_key,
                   identity_tables, no_pml_records, slab_index)
 from .sources import Source, deposit_scales, deposit_words
@@ -72,6 +72,51 @@ def _fill_accumulator(acc: torch.Tensor, q: int, values: Optional[np.ndarray]) -
         return
     pair = np.stack([values.real, values.imag], axis=1).astype(np.float32)
     acc[q].copy_(torch.from_numpy(np.ascontiguousarray(pair)))
+
+
+def fold_ghosts(grid: Grid, family: str) -> Dict[str, np.ndarray]:
+    """The mirror-plane ghosts of one family ("B" or "D") as the library's lists
+    (reference ``stepping.py:2004-2045`` ``fill_symmetry_bc_B/D``, ``MIRROR_SOURCE_INDEX``
+    2): every cell with index 0 on a folded axis where the component has Yee shift 0,
+    imaged from index 2 on each such axis with the product of the component's parities
+    there (the x, y, z passes of the fill compose to that at a corner), zero where it
+    sits on a metallic wall of an unfolded axis (``zero_metal`` follows the fill).
+    ``ghost`` / ``image``: int32 cell offsets; ``code``: component | 4 negate | 8 zero."""
+    nx, ny, nz = grid.shape
+    strides = (ny * nz, nz, 1)
+    ghosts, images, codes = [], [], []
+    for q in range(3):
+        comp = family + "xyz"[q]
+        shifts = IYEE[comp]
+        folded = [a for a in range(3) if grid.is_mirrored(a) and shifts[a] == 0]
+        if not folded:
+            continue
+        planes = []
+        for a in folded:
+            ranges = [np.arange(n, dtype=np.int64) for n in grid.shape]
+            ranges[a] = np.zeros(1, dtype=np.int64)
+            ii, jj, kk = np.meshgrid(*ranges, indexing="ij")
+            planes.append(ii.ravel() * strides[0] + jj.ravel() * strides[1] + kk.ravel())
+        offsets = np.unique(np.concatenate(planes))
+        coords = [offsets // strides[0], (offsets // strides[1]) % ny, offsets % nz]
+        sign = np.ones(offsets.size, dtype=np.int64)
+        image = list(coords)
+        for a in folded:
+            at = coords[a] == 0
+            image[a] = np.where(at, 2, image[a])
+            sign = np.where(at, sign * grid.parity(comp, a), sign)
+        zero = np.zeros(offsets.size, dtype=bool)
+        for b in range(3):
+            if grid.is_metallic(b) and not grid.is_mirrored(b) and shifts[b] == 0:
+                zero |= coords[b] == 0
+        ghosts.append(offsets)
+        images.append(image[0] * strides[0] + image[1] * strides[1] + image[2])
+        codes.append(q | np.where(sign < 0, 4, 0) | np.where(zero, 8, 0))
+    if not ghosts:
+        return {"ghost": np.zeros(0, np.int32), "image": np.zeros(0, np.int32), "code": np.zeros(0, np.uint8)}
+    return {"ghost": np.concatenate(ghosts).astype(np.int32),
+            "image": np.concatenate(images).astype(np.int32),
+            "code": np.concatenate(codes).astype(np.uint8)}
 
 
 class Engine:
@@ -151,6 +196,7 @@ class Engine:
         self._setup_poles(poles)
         self._setup_conductivity(conductivity)
         self._setup_sources()
+        self._setup_folds()
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         d.status = self.status.data_ptr()
         self._setup_monitors()
@@ -278,6 +324,31 @@ class Engine:
                     cd.chunk_of[lattice][axis] = t.data_ptr()
         self.cond_desc = cd
         self.desc.conductivity = ctypes.pointer(cd)
+
+    def _setup_folds(self) -> None:
+        """The ghost lists of the mirror-folded axes (:func:`fold_ghosts`) on the device,
+        with the zeroed scratch the library keeps each ghost's state in."""
+        grid = self.grid
+        d = self.desc
+        self.fold_tables: Dict[str, torch.Tensor] = {}
+        if not grid.has_symmetry:
+            return
+        for axis in range(3):
+            d.mirror[axis] = grid.mirror_phase(axis) or 0
+            d.full[axis] = grid.shape_full[axis]
+        for h, family in ((0, "B"), (1, "D")):
+            tables = fold_ghosts(grid, family)
+            count = int(tables["ghost"].size)
+            d.fold.count[h] = count
+            if count == 0:
+                continue
+            for name, array in tables.items():
+                tensor = torch.from_numpy(array).to(self.device)
+                self.fold_tables[f"{name}{h}"] = tensor
+                getattr(d.fold, name)[h] = tensor.data_ptr()
+            saved = torch.zeros(_lib.MGB_FOLD_WORDS * count, dtype=torch.float32, device=self.device)
+            self.fold_tables[f"saved{h}"] = saved
+            d.fold.saved[h] = saved.data_ptr()
 
     def _setup_sources(self) -> None:
         d = self.desc

@@ -2,13 +2,14 @@
 
 Follows the reference's ``meep_gpu/grid.py`` (``Grid``, :288 ``meep_cell_count``,
 :426-438 dx/dt/counts, :1095 ``origin_doubled``, :1292 ``_create_coordinates``) for
-the subset this engine steps: three resolved dimensions, no mirror symmetry, and
-per-axis boundaries that are either MEEP metallic walls or periodic wraps, Bloch-phased
-where the axis has a nonzero ``k_point`` component.
+the subset this engine steps: three resolved dimensions, per-axis boundaries that are
+either MEEP metallic walls or periodic wraps (Bloch-phased where the axis has a nonzero
+``k_point`` component), and mirror planes (``Mirror``) folding metallic axes.
 
 Registration: cell ``i`` of a component with Yee shift ``s`` on an axis sits at the
 doubled coordinate ``origin_doubled + 2*i + s``; ``origin_doubled`` is ``-(n - n % 2)``,
-MEEP's centred origin (odd counts start half a cell higher).
+MEEP's centred origin (odd counts start half a cell higher), and ``-2`` on a folded
+axis (MEEP's ``grid_volume::halve``: cell 0 one cell below the plane at doubled 0).
 """
 
 from __future__ import annotations
@@ -36,6 +37,63 @@ IYEE = {
 
 class Unsupported(ValueError):
     """A configuration outside what this engine steps, refused by name before any launch."""
+
+
+MIRROR_AXES = ("X", "Y", "Z")
+
+
+class Mirror:
+    """One mirror plane through the cell centre: the axis it is normal to and its phase
+    (reference ``grid.py:100``; MEEP's ``mp.Mirror(direction, phase)``). ``phase`` +1 is
+    an even mirror, -1 an odd one; a mirror is an involution, so nothing else is taken."""
+
+    __slots__ = ("axis", "phase")
+
+    def __init__(self, axis: str, phase: int = 1):
+        name = str(axis).upper()
+        if name not in MIRROR_AXES:
+            raise ValueError(f"mirror axis must be one of {list(MIRROR_AXES)}, got {axis!r}")
+        if phase not in (1, -1) or isinstance(phase, bool):
+            raise ValueError(f"mirror phase must be +1 (even) or -1 (odd), got {phase!r}")
+        self.axis = name
+        self.phase = int(phase)
+
+    @property
+    def axis_index(self) -> int:
+        return MIRROR_AXES.index(self.axis)
+
+    def __eq__(self, other) -> bool:
+        return isinstance(other, Mirror) and (self.axis, self.phase) == (other.axis, other.phase)
+
+    def __hash__(self) -> int:
+        return hash((self.axis, self.phase))
+
+    def __repr__(self) -> str:
+        return f"Mirror({self.axis!r}, phase={self.phase:+d})"
+
+
+def normalize_mirrors(symmetry: Any) -> Tuple[Optional[Mirror], Optional[Mirror], Optional[Mirror]]:
+    """The plane on each axis, or None (reference ``grid.py:155``): a bare axis name is an
+    even mirror; two planes on one axis are refused."""
+    planes: list = [None, None, None]
+    for entry in tuple(symmetry or ()):
+        plane = entry if isinstance(entry, Mirror) else Mirror(entry)
+        clash = planes[plane.axis_index]
+        if clash is not None:
+            raise ValueError(f"two mirror planes normal to {plane.axis}: {clash!r} and {plane!r}")
+        planes[plane.axis_index] = plane
+    return tuple(planes)  # type: ignore[return-value]
+
+
+def mirror_parity(component: str, axis: int, phase: int = 1) -> int:
+    """The sign a component takes under the mirror normal to ``axis`` (MEEP's
+    ``symmetry::phase_shift``; reference ``fields.py:121``): a vector (E, D) is odd about
+    the plane it is normal to and even otherwise, a pseudovector (H, B) the opposite, and
+    the plane's phase multiplies both."""
+    direction = "xyz".index(component[1])
+    if component[0] in "ED":
+        return -phase if direction == axis else phase
+    return phase if direction == axis else -phase
 
 
 _LIBM = None
@@ -123,7 +181,8 @@ class Grid:
     """Cell counts, spacing, dt and registration of one 3-D simulation."""
 
     def __init__(self, cell_size: Sequence[float], resolution: float, courant: float = 0.5,
-                 boundaries: Any = None, k_point: Sequence[float] = (0.0, 0.0, 0.0)):
+                 boundaries: Any = None, k_point: Sequence[float] = (0.0, 0.0, 0.0),
+                 symmetry: Any = ()):
         if len(tuple(cell_size)) != 3:
             raise ValueError(f"cell_size needs three lengths, got {cell_size!r}")
         self.cell_size = tuple(float(v) for v in cell_size)
@@ -138,8 +197,24 @@ class Grid:
             raise Unsupported(
                 f"every axis needs at least 2 cells (got {counts}); reduced-dimension runs "
                 "are not stepped by this engine")
-        self.nx, self.ny, self.nz = counts
+        self.shape_full = counts
+        self.nx_full, self.ny_full, self.nz_full = counts
         self.boundaries = normalize_boundaries(boundaries)
+        self.mirrors = normalize_mirrors(symmetry)
+        for axis, plane in enumerate(self.mirrors):
+            if plane is not None and not self.is_metallic(axis):
+                raise Unsupported(
+                    f"a mirror plane on the periodic {AXIS_NAMES[axis]} axis (its second mirror at "
+                    f"+L/2 and the far ghost slot it stores) is not stepped by this engine; fold a "
+                    f"metallic axis")
+        # MEEP's halve(): n - n//2 + 1 cells on a folded axis, from one cell below the plane
+        # (reference grid.py:604, vec.cpp halve)
+        self.nx, self.ny, self.nz = (
+            counts[a] - counts[a] // 2 + 1 if self.mirrors[a] is not None else counts[a] for a in range(3))
+        for axis in range(3):
+            if self.mirrors[axis] is not None and self.shape[axis] < 4:
+                raise Unsupported(f"a folded axis needs at least 4 stored cells, {AXIS_NAMES[axis]} has "
+                                  f"{self.shape[axis]}")
         self.k_point = tuple(float(k) for k in k_point)
         if len(self.k_point) != 3 or not all(math.isfinite(k) for k in self.k_point):
             raise ValueError(f"k_point needs three finite components, got {k_point!r}")
@@ -150,6 +225,9 @@ class Grid:
                     f"{self.boundaries[axis]!r}: a Bloch phase says what the field is one lattice "
                     f"vector away, and a perfect-electric-conductor wall terminates the axis "
                     f"instead of repeating it. Make the axis periodic or set its k component to 0.")
+        if self.has_symmetry and any(k != 0.0 for k in self.k_point):
+            raise Unsupported("a nonzero k_point together with mirror symmetry is not stepped by this "
+                              "engine (a folded axis carries no Bloch phase)")
         self.bloch_phases = tuple(self._bloch_phase(self.k_point[a], counts[a]) for a in range(3))
         self.has_bloch = any(p is not None for p in self.bloch_phases)
 
@@ -169,11 +247,35 @@ class Grid:
         return self.boundaries[axis] == METALLIC
 
     def axis_wraps(self, axis: int) -> bool:
-        return self.boundaries[axis] == PERIODIC
+        return self.boundaries[axis] == PERIODIC and self.mirrors[axis] is None
+
+    @property
+    def has_symmetry(self) -> bool:
+        return any(plane is not None for plane in self.mirrors)
+
+    def is_mirrored(self, axis: int) -> bool:
+        return self.mirrors[axis] is not None
+
+    def mirror_phase(self, axis: int) -> Optional[int]:
+        """The declared phase of the axis's plane, None on an unfolded axis."""
+        plane = self.mirrors[axis]
+        return None if plane is None else plane.phase
+
+    def parity(self, component: str, axis: int) -> int:
+        """``mirror_parity`` of a component about the axis's plane (the axis must be folded)."""
+        return mirror_parity(component, axis, self.mirrors[axis].phase)
 
     def origin_doubled(self, axis: int) -> int:
-        """MEEP's little corner on one axis in doubled units (reference grid.py:1095)."""
-        n = self.shape[axis]
+        """MEEP's little corner on one axis in doubled units (reference grid.py:1095):
+        ``-(n - n % 2)`` of the full count, ``-2`` on a folded axis."""
+        if self.mirrors[axis] is not None:
+            return -2
+        n = self.shape_full[axis]
+        return -(n - n % 2)
+
+    def full_origin_doubled(self, axis: int) -> int:
+        """The unfolded cell's little corner (the user volume)."""
+        n = self.shape_full[axis]
         return -(n - n % 2)
 
     def axis_origin(self, axis: int) -> float:
@@ -221,5 +323,6 @@ class Grid:
         return (1.0, 0.0) if phase is None else (phase.real, phase.imag)
 
     def __repr__(self) -> str:
+        folds = "" if not self.has_symmetry else f", symmetry={[m for m in self.mirrors if m]}"
         return (f"Grid({self.nx}x{self.ny}x{self.nz}, res={self.resolution:g}, "
-                f"dt={self.dt:g}, boundaries={self.boundaries})")
+                f"dt={self.dt:g}, boundaries={self.boundaries}{folds})")

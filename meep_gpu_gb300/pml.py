@@ -167,7 +167,7 @@ class PML:
         self.grid = grid
         self.order = int(order)
         self.R_asymptotic = float(R_asymptotic)
-        self.faces: Faces = normalize_thickness(thickness)
+        self.faces: Faces = self._resolve_mirror_faces(normalize_thickness(thickness), thickness)
         for axis, n in enumerate(grid.shape):
             low, high = self.faces[axis]
             if low + high > n:
@@ -183,6 +183,26 @@ class PML:
                                      grid.axis_wraps(axis))
                 self.records[(lattice, axis)] = runs_of(line)
                 self._check_unit_outside(axis, lattice, line)
+
+    def _resolve_mirror_faces(self, faces: Faces, request: Any) -> Faces:
+        """No layer on the low face of a folded axis: its cell 0 straddles the mirror plane,
+        a boundary condition, not a wall. A scalar request means every face that can carry
+        a layer and skips it; a request naming that face is refused (reference
+        ``pml.py:387`` ``_resolve_mirror_faces``)."""
+        uniform = not isinstance(request, (dict, tuple, list))
+        resolved = list(faces)
+        for axis in range(3):
+            low, high = faces[axis]
+            if not self.grid.is_mirrored(axis) or low == 0:
+                continue
+            if not uniform:
+                raise ValueError(
+                    f"PML requested at the {AXIS_NAMES[axis]} low face ({low} cells), but the "
+                    f"{AXIS_NAMES[axis].upper()} axis is mirror-symmetric: cell 0 lies on the mirror "
+                    f"plane, which is a boundary condition, not an absorber. Ask for the high face "
+                    f"only, e.g. {{'{AXIS_NAMES[axis]}': {{'high': {low}}}}}.")
+            resolved[axis] = (0.0, high)
+        return tuple(resolved)  # type: ignore[return-value]
 
     @property
     def is_active(self) -> bool:

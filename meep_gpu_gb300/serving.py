@@ -270,6 +270,8 @@ class BatchServer:
         slot = self.slots.index(None)
         if job.driver.complex_fields:
             raise Unsupported("a batched slot steps real fields (force_complex_fields=False)")
+        if job.driver.grid.has_symmetry:
+            raise Unsupported("a batched slot does not carry mirror symmetry")
         with torch.cuda.stream(self.setup_stream):
             # the batch accumulates its monitors step by step (dft_batched)
             job.engine = job.driver.freeze(stream=self.stream, autotune=False, dft_accumulation="direct")

@@ -26,7 +26,7 @@ from typing import Callable, Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
 
-from .grid import IYEE, Grid, Unsupported, cmul, cpow_int
+from .grid import AXIS_NAMES, IYEE, Grid, Unsupported, cmul, cpow_int
 
 ELECTRIC = ("Ex", "Ey", "Ez")
 MAGNETIC = ("Hx", "Hy", "Hz")
@@ -258,7 +258,7 @@ def deposition_pieces(grid: Grid, component: str, center: Sequence[float], size:
     inva = grid.dx
     where_min = [float(center[d]) - float(size[d]) / 2 for d in range(3)]
     where_max = [float(center[d]) + float(size[d]) / 2 for d in range(3)]
-    lengths = tuple(n * grid.dx for n in grid.shape)  # the snapped cell (reference Grid.Lx/Ly/Lz)
+    lengths = tuple(n * grid.dx for n in grid.shape_full)  # the snapped cell (reference Grid.Lx/Ly/Lz)
     for d in range(3):
         span = where_max[d] - where_min[d]
         if span > lengths[d] + inva:
@@ -435,6 +435,61 @@ def bind_src_vols(sources: Sequence["Source"], grid: Grid, faces) -> None:
         source.amps = [amp for _, amps in mine for amp in amps]
 
 
+def require_stored_half(grid: Grid, center: Sequence[float]) -> None:
+    """A source centre must lie in the half a folded axis stores (reference
+    ``sources.py:333``): MEEP deposits with ``use_symmetry=false``, so a source in the
+    discarded half reaches no stored cell and the run is silently empty."""
+    tol = grid.dx / 10
+    for axis in range(3):
+        if not grid.is_mirrored(axis) or center[axis] >= -tol:
+            continue
+        name = AXIS_NAMES[axis]
+        raise ValueError(
+            f"With {name.upper()} symmetry the stored half is {name} >= 0, and this source is at "
+            f"{name}={center[axis]:g}, in the half the fold discards; nothing would be deposited. "
+            f"Declare it at {name}={-center[axis]:g} instead: under this plane that is the same "
+            f"physical configuration, and its image is supplied by the fold.")
+
+
+def mirror_parity_offenders(grid: Grid, component: str, center: Sequence[float],
+                            size: Sequence[float], has_amp_func: bool) -> list:
+    """The planes a source centred on them cannot carry the parity of (reference
+    ``sources.py:500``): a component odd about a plane, on it, with no extent across it
+    or a uniform profile over it, would deposit a current the fold images with the
+    opposite sign. One ``(axis, phase, why)`` per offending plane."""
+    from .grid import mirror_parity
+    tol = grid.dx / 10
+    offenders = []
+    for axis in range(3):
+        phase = grid.mirror_phase(axis)
+        if phase is None or mirror_parity(component, axis, phase) > 0 or abs(center[axis]) > tol:
+            continue
+        name = AXIS_NAMES[axis]
+        if size[axis] <= tol:
+            why = (f"it has no extent along {name} (size[{name}]={size[axis]:g}), so the parity "
+                   f"condition admits only zero current")
+        elif not has_amp_func:
+            why = (f"its profile over |{name}| <= {size[axis] / 2:g} is uniform (no amp_func), and a "
+                   f"constant is even about every plane")
+        else:
+            continue
+        offenders.append((axis, phase, why))
+    return offenders
+
+
+def mirror_parity_message(component: str, offenders: list) -> str:
+    from .grid import mirror_parity
+    parts = []
+    for axis, phase, why in offenders:
+        odd = [n for n in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz") if mirror_parity(n, axis, phase) < 0]
+        parts.append(f"the {'even' if phase > 0 else 'odd'} {'XYZ'[axis]} plane (phase {phase:+d}) gives "
+                     f"it parity -1 (odd there: {', '.join(odd)}), and {why}")
+    return (f"A {component} source centred on the mirror plane cannot carry the parity the fold "
+            f"demands: " + "; also ".join(parts) + ". Give it an extent across the plane with an "
+            f"amp_func odd about it, drive a component the plane leaves even, declare the opposite "
+            f"phase, or run the full domain.")
+
+
 @dataclass
 class Source:
     """One current source: a waveform, a component and a deposition table. An electric
@@ -455,6 +510,12 @@ class Source:
         self.component = _COMPONENT_ALIASES.get(self.component, self.component)
         if self.component not in ELECTRIC + MAGNETIC:
             raise Unsupported(f"source component {self.component!r} is not stepped by this engine")
+        if self.grid.has_symmetry:
+            require_stored_half(self.grid, self.center)
+            offenders = mirror_parity_offenders(self.grid, self.component, self.center, self.size,
+                                                self.amp_func is not None)
+            if offenders:
+                raise ValueError(mirror_parity_message(self.component, offenders))
         self.cells, self.amps = deposition_table(self.grid, self.component, self.center,
                                                  self.size, self.amplitude, self.amp_func)
 

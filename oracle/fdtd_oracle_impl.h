@@ -69,6 +69,11 @@ typedef struct SUF(oracle_state) {
   const REAL* condinv[2][3];
   const unsigned char* keeps[2][3];
   REAL* fcond[2][3];
+  /* mirror planes: fold[a] = +1 / -1 (even / odd) folds the metallic axis a, whose
+   * unfolded count is full[a]; 0: no plane. metallic[a] stays 1 on a folded axis (its
+   * far wall). */
+  int fold[3];
+  int full[3];
 } SUF(oracle_state);
 
 static inline long long SUF(lin)(const SUF(oracle_state)* s, int i, int j, int k) {
@@ -122,7 +127,8 @@ static void SUF(curl_family)(SUF(oracle_state)* s, REAL* const target[3], REAL* 
           bracket = bracket + g2[c];
           bracket = bracket - g2s;
           REAL curl = s->dtdx * bracket;
-          /* mask: cell 0 of every metallic axis where the target's Yee shift is 0.
+          /* mask: cell 0 of every metallic axis where the target's Yee shift is 0 (the
+           * wall, or on a folded axis the plane's ghost: reference stepping.py:2589).
            * B (shift 1 on the two transverse axes) has shift 0 only on its own axis q;
            * D has shift 0 on the two transverse axes. */
           const int at[3] = {i, j, k};
@@ -215,7 +221,8 @@ static void SUF(curl_family)(SUF(oracle_state)* s, REAL* const target[3], REAL* 
   }
 }
 
-/* Hold every component's wall samples at zero: shift-0 axes that are metallic. */
+/* Hold every component's wall samples at zero: shift-0 axes that are metallic (a
+ * folded axis's cell 0 is the plane's ghost, not a wall). */
 static void SUF(zero_metal)(SUF(oracle_state)* s, REAL* const f[3], int electric) {
   const int n[3] = {s->nx, s->ny, s->nz};
   for (int q = 0; q < 3; ++q)
@@ -226,9 +233,36 @@ static void SUF(zero_metal)(SUF(oracle_state)* s, REAL* const f[3], int electric
           const int at[3] = {i, j, k};
           for (int a = 0; a < 3; ++a) {
             const int shift0 = electric ? (a != q) : (a == q);
-            if (shift0 && s->metallic[a] && at[a] == 0) f[q][SUF(lin)(s, i, j, k)] = (REAL)0;
+            if (shift0 && s->metallic[a] && !s->fold[a] && at[a] == 0) f[q][SUF(lin)(s, i, j, k)] = (REAL)0;
           }
         }
+}
+
+/* The sign of component q of a family about the plane normal to axis a (MEEP's
+ * phase_shift, reference fields.py:121): E and D odd about their own axis, H and B
+ * about the other two, times the plane's phase. */
+static int SUF(parity)(const SUF(oracle_state)* s, int q, int a, int electric) {
+  const int own = q == a;
+  return (electric ? own : !own) ? -s->fold[a] : s->fold[a];
+}
+
+/* fill_symmetry_bc (reference stepping.py:2038): cell 0 = parity * cell 2 on every
+ * folded axis where the component's Yee shift is 0, axes in x, y, z order. */
+static void SUF(fill_symmetry)(SUF(oracle_state)* s, REAL* const f[3], int electric) {
+  const int n[3] = {s->nx, s->ny, s->nz};
+  for (int q = 0; q < 3; ++q)
+    for (int a = 0; a < 3; ++a) {
+      const int shift0 = electric ? (a != q) : (a == q);
+      if (!s->fold[a] || !shift0) continue;
+      const REAL sign = (REAL)SUF(parity)(s, q, a, electric);
+      for (int i = 0; i < (a == 0 ? 1 : n[0]); ++i)
+        for (int j = 0; j < (a == 1 ? 1 : n[1]); ++j)
+          for (int k = 0; k < (a == 2 ? 1 : n[2]); ++k) {
+            int src[3] = {i, j, k};
+            src[a] = 2;
+            f[q][SUF(lin)(s, i, j, k)] = sign * f[q][SUF(lin)(s, src[0], src[1], src[2])];
+          }
+    }
 }
 
 void SUF(oracle_step)(SUF(oracle_state)* s, const double* words) {
@@ -243,6 +277,7 @@ void SUF(oracle_step)(SUF(oracle_state)* s, const double* words) {
     const long long c = s->src_cell[p];
     b[c] = NARROW((double)b[c] - words[p]);
   }
+  SUF(fill_symmetry)(s, s->B, 0);
   SUF(zero_metal)(s, s->B, 0);
   /* 3. update_H (stored H only under a PML) */
   if (s->pml) {
@@ -287,7 +322,8 @@ void SUF(oracle_step)(SUF(oracle_state)* s, const double* words) {
     const long long c = s->src_cell[p];
     d[c] = NARROW((double)d[c] - words[p]);
   }
-  /* 6b. zero_metal_D */
+  /* 6. fill_symmetry_bc_D, 6b. zero_metal_D */
+  SUF(fill_symmetry)(s, s->D, 1);
   SUF(zero_metal)(s, s->D, 1);
   /* 7. update_E: W = chi1inv * (D - sum P); E = W, or the own-axis accumulation. */
   for (int q = 0; q < 3; ++q)
@@ -337,17 +373,36 @@ void SUF(oracle_step)(SUF(oracle_state)* s, const double* words) {
  * z averages on shift-0 axes) times exp(i w t) * scale, E at t = step*dt, H at t - dt/2.
  * comp: 0..2 E, 3..5 H. acc: [ncomp][nfreq][2][cells]. In the float32 oracle the
  * phase is rounded to float32 and the products and sums are float32, as complex64. */
-static REAL SUF(sample_at)(const SUF(oracle_state)* s, const REAL* f, int i, int j, int k) {
+static REAL SUF(sample_at)(const SUF(oracle_state)* s, const REAL* f, int cp, int i, int j, int k) {
   const int n[3] = {s->nx, s->ny, s->nz};
   int at[3] = {i, j, k};
+  REAL sign = (REAL)1;
   for (int a = 0; a < 3; ++a) {
+    if (s->fold[a]) {
+      /* a folded axis (reference dft.py:1004 folded_axis_sites): site r of a component
+       * with Yee shift p sits at doubled -2 + 2r + p; outside the unfolded cell's owned
+       * window it is zero, below the plane the image at -d with the component's parity,
+       * and at the far wall zero */
+      const int q = cp % 3, electric = cp < 3;
+      const int p = electric ? (a == q) : (a != q);
+      const int low = -(s->full[a] - s->full[a] % 2);
+      int d = -2 + 2 * at[a] + p;
+      if (d < low + 2 - p || d > low + 2 * s->full[a] - p) return (REAL)0;
+      if (d < -p) {
+        d = -d;
+        sign = sign * (REAL)SUF(parity)(s, q, a, electric);
+      }
+      at[a] = (d + 2 - p) / 2;
+      if (at[a] >= n[a]) return (REAL)0;
+      continue;
+    }
     if (at[a] >= n[a] || at[a] < 0) {
       if (s->metallic[a]) return (REAL)0;
       at[a] %= n[a];
       if (at[a] < 0) at[a] += n[a];
     }
   }
-  return f[SUF(lin)(s, at[0], at[1], at[2])];
+  return sign * f[SUF(lin)(s, at[0], at[1], at[2])];
 }
 
 void SUF(oracle_dft)(const SUF(oracle_state)* s, const int region[6], int ncomp, const int* comp,
@@ -372,9 +427,9 @@ void SUF(oracle_dft)(const SUF(oracle_state)* s, const int region[6], int ncomp,
       for (int b = 0; b < 2; ++b)
         for (int a = 0; a < 2; ++a) {
           if ((a && !avg[1]) || (b && !avg[2])) { v[b][a] = 0; continue; }
-          const REAL f0 = SUF(sample_at)(s, f, i, j + a, k + b);
+          const REAL f0 = SUF(sample_at)(s, f, cp, i, j + a, k + b);
           if (avg[0]) {
-            const REAL f1 = SUF(sample_at)(s, f, i + 1, j + a, k + b);
+            const REAL f1 = SUF(sample_at)(s, f, cp, i + 1, j + a, k + b);
             v[b][a] = (REAL)0.5 * (f0 + f1);
           } else {
             v[b][a] = f0;

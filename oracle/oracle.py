@@ -68,7 +68,8 @@ def _state_type(real) -> type:
                     ("nsrc", ctypes.c_int), ("src_cell", P), ("src_comp", P),
                     ("h_separated", ctypes.c_int),
                     ("condfac", (P * 3) * 2), ("condinv", (P * 3) * 2), ("keeps", (P * 3) * 2),
-                    ("fcond", (P * 3) * 2)]
+                    ("fcond", (P * 3) * 2), ("fold", ctypes.c_int * 3),
+                    ("full", ctypes.c_int * 3)]
     return State
 
 
@@ -110,6 +111,10 @@ class Problem:
     # cells ((low, high) per axis) the one-rank chunks are cut by
     conductivity: Dict[str, np.ndarray] = field(default_factory=dict)
     faces: Tuple[Tuple[float, float], ...] = ((0.0, 0.0),) * 3
+    # mirror planes: the phase (+1 / -1) of each folded axis, 0 elsewhere, and the
+    # unfolded counts
+    mirror: Tuple[int, int, int] = (0, 0, 0)
+    full: Tuple[int, int, int] = (0, 0, 0)
 
 
 YEE = {"Dx": (1, 0, 0), "Dy": (0, 1, 0), "Dz": (0, 0, 1),
@@ -214,7 +219,9 @@ def problem_from_driver(driver) -> Problem:
                    words=lambda first, steps, part="real": deposit_words(sources, first, steps, grid.dt,
                                                                            scales, part),
                    monitors=monitors, conductivity=conductivity,
-                   faces=tuple(pml.faces) if pml is not None else ((0.0, 0.0),) * 3)
+                   faces=tuple(pml.faces) if pml is not None else ((0.0, 0.0),) * 3,
+                   mirror=tuple(grid.mirror_phase(a) or 0 for a in range(3)),
+                   full=tuple(grid.shape_full))
 
 
 class Oracle:
@@ -247,6 +254,8 @@ class Oracle:
         s = _STATE[precision]()
         s.nx, s.ny, s.nz = shape
         s.metallic[:] = list(problem.metallic)
+        s.fold[:] = list(problem.mirror)
+        s.full[:] = list(problem.full) if any(problem.mirror) else list(shape)
         s.dtdx = float(np.float32(problem.dt / problem.dx)) if precision == "f32" else problem.dt / problem.dx
         s.pml = 1 if problem.pml else 0
         tables = problem.tables32 if precision == "f32" else problem.tables64

@@ -56,6 +56,19 @@ CASES = {
                   k_point=(0.3, -0.2, 0.0), bloch_monitors=True),
     "bloch_pml": dict(n=(15, 12, 16), pml={"z": 3}, steps=50, complex=True, boundaries="periodic",
                       k_point=(0.45, 0.0, 0.0), bloch_line=True, bloch_monitors=True),
+    # Mirror symmetry (folded metallic axes): an even X and an odd Y plane under a PML
+    # (the scalar thickness skips the planes' faces) with a Lorentz slab across the x
+    # plane; an odd Z plane on an odd count with an absorber (its low face lands on no
+    # stored cell), D and B conductivity; complex fields with an even Z plane beside a
+    # periodic y axis. Sources in the stored half (one on the x plane, one sheet across
+    # it), a flux plane and a DFT volume spanning both halves of every plane.
+    "mirror_pml": dict(n=(14, 12, 16), pml=3, steps=60, symmetry=(("X", 1), ("Y", -1)),
+                       mirror_sources=True, lorentz=True),
+    "mirror_odd_lossy": dict(n=(13, 12, 15), pml=0, steps=60, symmetry=(("Z", -1),),
+                             conductivity="absorber_b", mirror_sources=True),
+    "mirror_complex": dict(n=(12, 14, 14), pml={"x": 3, "z": {"high": 2}}, steps=50,
+                           symmetry=(("Z", 1),), complex=True, mirror_sources=True,
+                           boundaries=("metallic", "periodic", "metallic")),
 }
 
 # The 80^3 sphere-under-PML workload (resolution 10, 10-cell PML, eps 4 sphere of radius
@@ -69,9 +82,16 @@ def build_case(driver_cls, susceptibility_cls, case: dict, reference: bool = Fal
     n = case["n"]
     lengths = tuple(v / res for v in n)
     boundaries = case.get("boundaries", "metallic")
+    symmetry = ()
+    if case.get("symmetry"):
+        if reference:
+            from meep_gpu.grid import Mirror
+        else:
+            from meep_gpu_gb300 import Mirror
+        symmetry = tuple(Mirror(axis, phase) for axis, phase in case["symmetry"])
     d = driver_cls(cell_size=lengths, resolution=res, courant=0.5,
                    force_complex_fields=bool(case.get("complex", False)),
-                   k_point=case.get("k_point", (0.0, 0.0, 0.0)),
+                   k_point=case.get("k_point", (0.0, 0.0, 0.0)), symmetry=symmetry,
                    boundaries=boundaries, **({"prefer_gpu": False} if reference else {}))
     if case["pml"]:
         d.setup_pml(case["pml"])
@@ -97,9 +117,23 @@ def build_case(driver_cls, susceptibility_cls, case: dict, reference: bool = Fal
     if lossy:
         _set_conductivity(d, case, x, y, z, lengths, reference)
     source_x = -0.15 if lossy else -lengths[0] / 4
-    d.add_source({"source_type": "gaussian", "component": "Ez",
-                  "center": (source_x, 0.03, 0.0), "size": (0, 0, 0),
-                  "frequency": fcen, "fwidth": fwidth})
+    if case.get("mirror_sources"):
+        d.add_source({"source_type": "gaussian", "component": "Ez", "center": (0.25, 0.13, 0.17),
+                      "size": (0, 0, 0), "frequency": fcen, "fwidth": fwidth})
+        d.add_source({"source_type": "gaussian", "component": "Ey", "center": (0.0, 0.21, 0.1),
+                      "size": (0, 0, 0), "frequency": 0.5, "fwidth": 0.4,
+                      "amplitude": (0.5 + 0.3j) if case.get("complex") else 0.5})
+        d.add_source({"source_type": "continuous", "component": "Hx", "center": (0.1, 0.2, 0.3),
+                      "size": (0.3, 0, 0.2), "frequency": 0.3, "amplitude": 0.5})
+        flux.append(d.add_flux_monitor(fcen=fcen, df=fwidth / 2, nfreq=3, center=(0, 0, 0.25),
+                                       size=(1.0, 0.9, 0), decimation_factor=1))
+        dft.append(d.add_dft_monitor(frequencies=[fcen, 0.4], components=("Ex", "Ez", "Hy", "Hx"),
+                                     center=(0.0, 0.0, 0.0), size=(0.6, 0.5, 0.4),
+                                     decimation_factor=2))
+    else:
+        d.add_source({"source_type": "gaussian", "component": "Ez",
+                      "center": (source_x, 0.03, 0.0), "size": (0, 0, 0),
+                      "frequency": fcen, "fwidth": fwidth})
     if case.get("bloch_line"):
         d.add_source({"source_type": "gaussian", "component": "Ey", "center": (0.0, -0.1, 0.1),
                       "size": (lengths[0], 0, 0), "frequency": fcen, "fwidth": fwidth,

@@ -81,7 +81,9 @@ int main(void) {
   F(mgb_conductivity, condinv) F(mgb_conductivity, fcond) F(mgb_conductivity, chunk_of)
   F(mgb_conductivity, keeps) F(mgb_sim_desc, nsrc_magnetic) F(mgb_sim_desc, src_box_magnetic)
   F(mgb_sim_desc, bloch_axes) F(mgb_sim_desc, bloch_phase) F(mgb_sim_desc, partner_E)
-  F(mgb_sim_desc, partner_H)
+  F(mgb_sim_desc, partner_H) F(mgb_sim_desc, mirror) F(mgb_sim_desc, full) F(mgb_sim_desc, fold)
+  F(mgb_fold, ghost) F(mgb_fold, image) F(mgb_fold, code) F(mgb_fold, saved)
+  printf("sizeof.mgb_fold %zu\n", sizeof(mgb_fold));
   return 0;
 }
 """
@@ -97,7 +99,7 @@ def test_ctypes_layout_matches_the_header(tmp_path):
     layout = dict(line.split() for line in out.strip().splitlines())
     types = {"mgb_sim_desc": _lib.MgbSimDesc, "mgb_monitor": _lib.MgbMonitor,
              "mgb_pole": _lib.MgbPole, "mgb_aux": _lib.MgbAux,
-             "mgb_conductivity": _lib.MgbConductivity}
+             "mgb_conductivity": _lib.MgbConductivity, "mgb_fold": _lib.MgbFold}
     for key, value in layout.items():
         kind, member = key.split(".")
         if kind == "sizeof":

@@ -242,7 +242,7 @@ def test_batch_steps_every_golden_configuration_to_the_reference_words(gpu):
     # <= 2 monitors a slot; lossy runs and magnetic sources are not batched (refused by name)
     names = [n for n in sorted(CASES) if n not in ("mixed", "tile_mixed")
              and not CASES[n].get("conductivity") and not CASES[n].get("magnetic")
-             and not CASES[n].get("complex")]
+             and not CASES[n].get("complex") and not CASES[n].get("symmetry")]
     server = serving.BatchServer(gpu, max_slots=len(names), steps_per_replay=16, max_side=72)
     jobs = []
     for name in names:

@@ -2570,8 +2570,12 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
   for (int m = 0; m < d.nmonitors; ++m) {
     const mgb_monitor& mon = d.monitors[m];
     for (int a = 0; a < 3; ++a) {
-      // on a periodic axis the ladder may reach one period past either face (lattice images)
-      const int lo = d.metallic[a] ? 0 : -n[a], hi = d.metallic[a] ? n[a] : 2 * n[a];
+      // on a periodic axis the ladder may reach one period past either face (lattice
+      // images); on a folded one it may start below the plane, down to the unfolded
+      // cell's low wall (mirror images)
+      int lo = d.metallic[a] ? 0 : -n[a];
+      const int hi = d.metallic[a] ? n[a] : 2 * n[a];
+      if (d.mirror[a] != 0) lo = 1 - (d.full[a] - d.full[a] % 2) / 2;
       if (mon.region[2 * a] < lo || mon.region[2 * a] >= mon.region[2 * a + 1] || mon.region[2 * a + 1] > hi) {
         return fail(MGB_ERR_ARGUMENT, "monitor " + std::to_string(m) + " region is not inside the grid");
       }

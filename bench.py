@@ -22,6 +22,10 @@ decimated steps).
 * ``lossy``: the lossy kernels (D and B conductivity) on two 192^3 workloads, an
   absorber in place of the PML and a conductivity under the PML, each with its per-half
   roofline, and their float64 error on a 40^3 lossy case.
+* ``mirror``: the folded path on the headline case under an even Y and an odd Z mirror
+  (192 x 97 x 97 stored cells), its throughput on the stored cells and as the unfolded
+  run it stands for, its per-half roofline with the fold kernels, and the float64 error
+  of the folded 80^3 case.
 
 ``--impl reference`` times the reference path's CPU implementation (the oracle port:
 the reference itself is Python and does not travel) on the same workload instead.
@@ -62,6 +66,8 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-validate", action="store_true")
     p.add_argument("--kernel-steps", type=int, default=40, help="steps timed kernel by kernel")
+    p.add_argument("--mirror-steps", type=int, default=200,
+                   help="steps timed on the folded mirror192 workload (0: skip the mirror section)")
     p.add_argument("--lossy-steps", type=int, default=100,
                    help="steps timed on each lossy 192^3 workload (0: skip the lossy section)")
     p.add_argument("--serving", type=int, default=512,
@@ -383,8 +389,11 @@ def main():
     if args.serving > 0:
         served = bench_serving(device, args)
     lossy = None
+    mirror = None
     if args.lossy_steps > 0:
         lossy = bench_lossy(device, args)
+    if args.mirror_steps > 0:
+        mirror = bench_mirror(device, args)
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "Mcell-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 5),
@@ -398,7 +407,7 @@ def main():
                    "monitors": {"flux_planes": len(flux), "dft_volumes": len(dft),
                                 "decimation": [m.decimation_factor for m in list(flux) + list(dft)][:1]}},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-        "clocks": clocks.summary(), "error": error, "serving": served, "lossy": lossy,
+        "clocks": clocks.summary(), "error": error, "serving": served, "lossy": lossy, "mirror": mirror,
     }
     print(json.dumps(line), flush=True)
 
@@ -672,6 +681,83 @@ def bench_lossy(device, args):
     got = flux[0].get_flux_spectrum()
     expected = o64.flux_spectrum(0)
     out["error"] = {"lossy40_300_steps": {
+        "fields_rel_l2_vs_f64": float(math.sqrt(num / den)),
+        "flux_rel_vs_f64": float(np.max(np.abs(got - expected)) / np.max(np.abs(expected)))}}
+    gpu.close()
+    return out
+
+
+def bench_mirror(device, args):
+    """The folded path on mirror192 (the headline case under an even Y and an odd Z
+    mirror): device-resident throughput over K steps on the stored cells and as the
+    unfolded run it stands for, each half's roofline (the fold kernels included in their
+    half), and the float64 error of the folded 80^3 case."""
+    import torch
+
+    from meep_gpu_gb300 import FdtdDriver, workloads
+    from oracle.oracle import Oracle, problem_from_driver
+
+    peak, _ = measured_peaks()
+    stream = torch.cuda.current_stream(device)
+    driver, _, _ = workloads.build("mirror192", FdtdDriver)
+    driver.step_many(3)
+    engine = driver.engine
+    first, steps = driver.step_count, args.mirror_steps
+    engine.ensure_source_words(first, steps + 20)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(device)
+    with ClockSampler(device.index or 0) as clocks:
+        start.record(stream)
+        engine.step(first, steps)
+        end.record(stream)
+        torch.cuda.synchronize(device)
+    ms = start.elapsed_time(end) / steps
+    n0 = first + steps
+    events = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(20)]
+    for t, ev in enumerate(events):
+        ev[0].record(stream)
+        engine.launch(n0 + t, 0, stream)
+        ev[1].record(stream)
+        engine.launch(n0 + t, 1, stream)
+        ev[2].record(stream)
+    torch.cuda.synchronize(device)
+    nbytes = engine.algorithmic_bytes()
+    halves = {}
+    for part, key in enumerate(("h_half", "e_half")):
+        half_ms = float(np.mean([ev[part].elapsed_time(ev[part + 1]) for ev in events]))
+        gbs = nbytes[key] / (half_ms / 1e3) / 1e9
+        halves[key] = {"ms": round(half_ms, 4), "GB/s": round(gbs, 1), "frac": round(gbs / peak, 4)}
+    cells = driver.grid.total_cells
+    full = int(np.prod(driver.grid.shape_full))
+    step_bytes = nbytes["h_half"] + nbytes["e_half"]
+    out = {"mirror192": {
+        "value": round(cells / (ms / 1e3) / 1e6, 3), "unit": "Mcell-steps/s (stored cells)",
+        "unfolded_equivalent": round(full / (ms / 1e3) / 1e6, 3),
+        "stored_cells": cells, "unfolded_cells": full, "ms_per_step": round(ms, 5), "steps": steps,
+        "step_frac": round(step_bytes / (ms / 1e3) / 1e9 / peak, 4), "per_kernel": halves,
+        "ghosts": [int(engine.desc.fold.count[0]), int(engine.desc.fold.count[1])],
+        "kernels": [list(c) for c in engine.choice], "clocks": clocks.summary(),
+        "note": "each half's time includes its fold kernel (ghost words and their E/H)"}}
+    if engine.nonfinite():
+        raise RuntimeError("the mirror192 run wrote a non-finite field")
+    driver.close()
+    del driver, engine
+    torch.cuda.empty_cache()
+    steps = workloads.STEPS["mirror80"]
+    gpu, flux, _ = workloads.build("mirror80", FdtdDriver)
+    gpu.run(num_steps=steps, progress_interval=steps)
+    ref, _, _ = workloads.build("mirror80", FdtdDriver)
+    o64 = Oracle(problem_from_driver(ref), "f64")
+    o64.run(steps)
+    num = den = 0.0
+    for c in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz"):
+        a = gpu.get_field(c, cell_centered=False).astype(np.float64)
+        b = o64.field(c)
+        num += float(np.sum((a - b) ** 2))
+        den += float(np.sum(b ** 2))
+    got = flux[0].get_flux_spectrum()
+    expected = o64.flux_spectrum(0)
+    out["error"] = {"mirror80_600_steps": {
         "fields_rel_l2_vs_f64": float(math.sqrt(num / den)),
         "flux_rel_vs_f64": float(np.max(np.abs(got - expected)) / np.max(np.abs(expected)))}}
     gpu.close()

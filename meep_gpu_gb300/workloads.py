@@ -29,6 +29,12 @@ grid's cell centres, as the configurations specify; there is no dataset.
   (through the x layers), a B conductivity (0.2 on Bx for x > 0.5, 0.05 on Bz), a
   Lorentz slab, an extended Ez source on a lossy component and a 20-frequency flux
   plane; the case the lossy path's float64 error is quoted on (300 steps).
+* ``mirror192``: the ``sphere192_8dft`` case (its eight DFT objects included) folded by
+  an even Y and an odd Z mirror (``mp.Mirror``): 192 x 97 x 97 stored cells, the
+  discarded halves' flux planes and volume parts read from their mirror images; 5000
+  steps.
+* ``mirror80``: the ``sphere80`` case folded the same way (80 x 41 x 41); the case the
+  folded path's float64 error is quoted on (600 steps).
 * ``adjoint96`` (:func:`adjoint96`): 96^3 at resolution 10, 10-cell PML, a 16 x 64 x 64
   design box centred in the cell with eps ~ U[1, 12] (seed 0), Ez Gaussian (fcen 0.15,
   df 0.05) at x = -L/4, a 10-frequency x-normal flux plane 4 cells past the box;
@@ -40,9 +46,10 @@ from __future__ import annotations
 import numpy as np
 
 WORKLOADS = ("sphere80", "sphere192_8dft", "lorentz192", "sphere128", "sphere192", "absorber192",
-             "lossy_pml192", "lossy40")
+             "lossy_pml192", "lossy40", "mirror192", "mirror80")
 STEPS = {"sphere80": 2000, "sphere192_8dft": 5000, "lorentz192": 10000, "sphere128": 1000,
-         "sphere192": 5000, "absorber192": 5000, "lossy_pml192": 5000, "lossy40": 300}
+         "sphere192": 5000, "absorber192": 5000, "lossy_pml192": 5000, "lossy40": 300,
+         "mirror192": 5000, "mirror80": 600}
 
 
 def build(name: str, driver_cls=None, susceptibility_cls=None, **driver_kwargs):
@@ -50,9 +57,16 @@ def build(name: str, driver_cls=None, susceptibility_cls=None, **driver_kwargs):
         from .driver import FdtdDriver as driver_cls  # noqa: N813
     if susceptibility_cls is None:
         from .dispersion import Susceptibility as susceptibility_cls  # noqa: N813
-    if name in ("sphere80", "sphere192_8dft", "sphere128", "sphere192"):
-        res = {"sphere80": 10, "sphere192_8dft": 24, "sphere128": 16, "sphere192": 24}[name]
+    if name in ("sphere80", "sphere192_8dft", "sphere128", "sphere192", "mirror192", "mirror80"):
+        res = {"sphere80": 10, "sphere192_8dft": 24, "sphere128": 16, "sphere192": 24,
+               "mirror192": 24, "mirror80": 10}[name]
         length = 8.0
+        if name.startswith("mirror"):
+            from .grid import Mirror
+            # the Ez source on both planes is even about them: Ez is even under an even Y
+            # mirror and, lying along z, under an odd Z one
+            driver_kwargs = dict(driver_kwargs, symmetry=(Mirror("Y", 1), Mirror("Z", -1)))
+            name = "sphere192_8dft" if name == "mirror192" else "sphere80"
         d = driver_cls(cell_size=(length, length, length), resolution=res, courant=0.5,
                        force_complex_fields=False, boundaries="metallic", **driver_kwargs)
         d.setup_pml(10)

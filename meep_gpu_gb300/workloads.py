@@ -174,3 +174,33 @@ def adjoint96(eps_box=None, driver_cls=None, seed: int = 0, **driver_kwargs):
     flux = d.add_flux_monitor(fcen=0.15, df=0.05, nfreq=10, center=(plane_x, 0.0, 0.0), size=(0, 6.4, 6.4),
                               decimation_factor=0)
     return d, flux, box, eps_box
+
+
+def main(argv=None) -> None:
+    """Build one workload on the GPU and step it: ``python -m meep_gpu_gb300.workloads NAME
+    [--steps K]`` (three steps to make the plan and choose its kernels, then K timed)."""
+    import argparse
+    import time
+
+    import torch
+
+    from .driver import FdtdDriver
+
+    parser = argparse.ArgumentParser(description=main.__doc__)
+    parser.add_argument("name", choices=WORKLOADS)
+    parser.add_argument("--steps", type=int, default=10)
+    args = parser.parse_args(argv)
+    driver, _, _ = build(args.name, FdtdDriver)
+    driver.step_many(3)
+    torch.cuda.synchronize()
+    start = time.perf_counter()
+    driver.engine.step(driver.step_count, args.steps)
+    torch.cuda.synchronize()
+    elapsed = time.perf_counter() - start
+    print(f"{args.name}: {driver.grid}, kernels {driver.engine.choice}, "
+          f"{1e3 * elapsed / max(args.steps, 1):.4f} ms/step over {args.steps} steps")
+    driver.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -183,13 +183,16 @@ typedef struct mgb_sim_desc {
   double bloch_phase[3][2];
   const float* partner_E[3];
   const float* partner_H[3];
-  /* mirror symmetry (MEEP's mp.Mirror): mirror[a] = +1 (even) or -1 (odd) folds the
-   * metallic axis a about the plane at its stored cell 1 (MEEP's halve(): n = full -
-   * full/2 + 1 stored cells from one cell below the plane, the far wall metallic[a]);
-   * 0: no plane. full[a]: the unfolded cell count. Cell 0 of every component with Yee
-   * shift 0 on a folded axis is the plane's ghost: after each half's sources the library
-   * writes it from stored row 2 with the component's parity (the `fold` lists) and steps
-   * its E (H) from that word. Monitors read a ladder site below the plane from its
+  /* mirror symmetry (MEEP's mp.Mirror): mirror[a] = +1 (even) or -1 (odd) folds axis a
+   * about the plane at its stored cell 1 (MEEP's halve(): full - full/2 + 1 cells from
+   * one cell below the plane); 0: no plane. full[a]: the unfolded cell count.
+   * metallic[a] is the far face: 1 a metallic wall; 0 periodic, when the axis stores
+   * one cell more (MEEP's big_corner plane, then the far ghost slot past the second
+   * mirror at doubled full[a]). Cell 0 of every component with Yee shift 0 on a folded
+   * axis is the plane's ghost, and on a periodic one the last slot of every component
+   * with shift 1 the second mirror's: after each half's sources the library writes them
+   * from their images with the component's parity (the `fold` lists) and steps their E
+   * (H) from those words. Monitors read a ladder site the fold does not store from its
    * image. Folded runs are refused by the batch and the adjoint. */
   int32_t mirror[3];
   int32_t full[3];

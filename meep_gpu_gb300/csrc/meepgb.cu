@@ -148,9 +148,11 @@ struct DftParams {
   int part;
   const float* pE[3];
   const float* pH[3];
-  // mirror folds: bit a of `fold` folds axis a (full[a] unfolded cells); bit a of
-  // neg[comp] says the component is odd about that plane
+  // mirror folds: bit a of `fold` folds axis a (full[a] unfolded cells), of `far` when
+  // its outer face is periodic (a second mirror at doubled full[a]); bit a of neg[comp]
+  // says the component is odd about that plane
   int fold;
+  int far;
   int full[3];
   int neg[6];
 };
@@ -1643,9 +1645,11 @@ __device__ __forceinline__ float field_at(const DftParams& p, int comp, int i, i
   const int n[3] = {p.nx, p.ny, p.nz};
   if (p.fold) {
     // A folded axis (MEEP's sn loop, reference dft.py:1004): site r of a component with
-    // Yee shift s sits at doubled -2 + 2r + s; outside the unfolded cell's owned window
-    // (its walls) it reads zero, below the plane it is the image at -d with the
-    // component's parity, and at the far wall (stored index n) zero.
+    // Yee shift s sits at doubled -2 + 2r + s. Outside the unfolded cell's owned window
+    // it reads zero past a metallic face, or its image one lattice vector over past a
+    // periodic one; below the plane it is the image at -d with the component's parity;
+    // past the stored rows it is zero (a metallic far wall) or the image about the second
+    // mirror at doubled full (a periodic face), with the parity again.
     int at[3] = {i, j, k};
     bool flip = false;
     const int q = comp % 3;
@@ -1660,15 +1664,28 @@ __device__ __forceinline__ float field_at(const DftParams& p, int comp, int i, i
         continue;
       }
       const int s = (comp < 3) == (a == q) ? 1 : 0;
-      const int low = -(p.full[a] - p.full[a] % 2);
+      const bool periodic = (p.far >> a) & 1;
+      const bool odd = (p.neg[comp] >> a) & 1;
+      const int low = -(p.full[a] - p.full[a] % 2), lattice = 2 * p.full[a];
       int d = -2 + 2 * at[a] + s;
-      if (d < low + 2 - s || d > low + 2 * p.full[a] - s) return 0.f;
+      if (d < low + 2 - s || d > low + lattice - s) {
+        if (!periodic) return 0.f;
+        d += d < low + 2 - s ? lattice : -lattice;
+        if (d < low + 2 - s || d > low + lattice - s) return 0.f;
+      }
       if (d < -s) {
         d = -d;
-        if ((p.neg[comp] >> a) & 1) flip = !flip;
+        if (odd) flip = !flip;
       }
-      at[a] = (d + 2 - s) >> 1;
-      if (at[a] >= n[a]) return 0.f;
+      int row = (d + 2 - s) >> 1;
+      if (row >= n[a]) {
+        if (!periodic) return 0.f;
+        d = lattice - d;
+        if (odd) flip = !flip;
+        row = (d + 2 - s) >> 1;
+        if (d + 2 - s < 0 || row >= n[a]) return 0.f;
+      }
+      at[a] = row;
     }
     const long long c = ((long long)at[0] * p.ny + at[1]) * p.nz + at[2];
     const float own = comp < 3 ? p.E[comp][c] : p.H[comp - 3][c];
@@ -2574,8 +2591,11 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
       // images); on a folded one it may start below the plane, down to the unfolded
       // cell's low wall (mirror images)
       int lo = d.metallic[a] ? 0 : -n[a];
-      const int hi = d.metallic[a] ? n[a] : 2 * n[a];
-      if (d.mirror[a] != 0) lo = 1 - (d.full[a] - d.full[a] % 2) / 2;
+      int hi = d.metallic[a] ? n[a] : 2 * n[a];
+      if (d.mirror[a] != 0) {
+        lo = 1 - (d.full[a] - d.full[a] % 2) / 2 - (d.metallic[a] ? 0 : d.full[a]);
+        hi = d.metallic[a] ? n[a] : n[a] + d.full[a];
+      }
       if (mon.region[2 * a] < lo || mon.region[2 * a] >= mon.region[2 * a + 1] || mon.region[2 * a + 1] > hi) {
         return fail(MGB_ERR_ARGUMENT, "monitor " + std::to_string(m) + " region is not inside the grid");
       }
@@ -2629,10 +2649,12 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
     if (d.mirror[a] == 0) continue;
     if (d.mirror[a] != 1 && d.mirror[a] != -1)
       return fail(MGB_ERR_ARGUMENT, "a mirror phase must be +1 (even) or -1 (odd)");
-    if (!d.metallic[a])
-      return fail(MGB_ERR_UNSUPPORTED, "a mirror plane on a periodic axis is not stepped by this engine");
-    if (d.full[a] < 2 || n[a] != d.full[a] - d.full[a] / 2 + 1 || n[a] < 4)
-      return fail(MGB_ERR_ARGUMENT, "a folded axis stores full - full/2 + 1 cells (at least 4)");
+    // a folded periodic axis stores one cell past MEEP's window (big_corner's plane and
+    // the far ghost slot)
+    const int owned = d.full[a] - d.full[a] / 2 + 1;
+    if (d.full[a] < 2 || n[a] != owned + (d.metallic[a] ? 0 : 1) || n[a] < 4)
+      return fail(MGB_ERR_ARGUMENT, "a folded axis stores full - full/2 + 1 cells, one more when periodic "
+                                    "(at least 4)");
     fold_mask |= 1 << a;
   }
   if (fold_mask != 0) {
@@ -2688,7 +2710,11 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
         }
     }
   }
-  for (int a = 0; a < 3; ++a) p.met[a] = d.metallic[a] ? 1 : 0;
+  // a folded axis steps as a metallic one (zero words past either face, its cell 0 of
+  // the shift-0 components masked and held like a wall sample until the fold writes it),
+  // whatever its outer face: past a periodic one the readers are the far ghost slot,
+  // which the fold writes too
+  for (int a = 0; a < 3; ++a) p.met[a] = (d.metallic[a] || d.mirror[a] != 0) ? 1 : 0;
   p.dtdx = d.dtdx;
   for (int l = 0; l < 2; ++l)
     for (int a = 0; a < 3; ++a) {
@@ -2890,6 +2916,7 @@ int launch_part_kernels(mgb_sim* sim, long long n, int part, cudaStream_t s) {
       for (int a = 0; a < 3; ++a) {
         if (sim->desc.mirror[a] == 0) continue;
         q.fold |= 1 << a;
+        if (!sim->desc.metallic[a]) q.far |= 1 << a;
         q.full[a] = sim->desc.full[a];
         // E/D odd about the plane normal to its own direction, H/B about the others
         for (int comp = 0; comp < 6; ++comp) {

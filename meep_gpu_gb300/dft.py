@@ -102,6 +102,41 @@ def axis_ladder(grid: Grid, axis: int, where_min: float, where_max: float):
     return first, count, taper
 
 
+def folded_site(grid: Grid, axis: int, parity: int, site: int):
+    """Where a monitor reads site ``site`` (stored-index convention, doubled coordinate
+    ``-2 + 2*site + parity``) of a component with Yee shift ``parity`` on a folded axis
+    (reference ``dft.py:1004`` ``folded_axis_sites``, MEEP's sn loop): ``(row, flipped)``
+    -- a stored row, read with the component's parity when flipped -- or ``"zero"`` (a
+    metallic wall) or None (no chunk serves it). The device sampling maps sites the same
+    way."""
+    full = grid.shape_full[axis]
+    stored = grid.shape[axis]
+    metallic = grid.is_metallic(axis)
+    low = -(full - full % 2)
+    lattice = 2 * full
+    doubled = -2 + 2 * site + parity
+    flipped = False
+    if doubled < low + 2 - parity or doubled > low + lattice - parity:
+        if metallic:
+            return "zero" if parity == 0 and doubled == low else None
+        doubled += lattice if doubled < low + 2 - parity else -lattice
+        if doubled < low + 2 - parity or doubled > low + lattice - parity:
+            return None
+    if doubled < -parity:
+        doubled = -doubled
+        flipped = True
+    row = (doubled + 2 - parity) // 2
+    if row >= stored:
+        if metallic:
+            return "zero" if parity == 0 and row == stored else None
+        doubled = lattice - doubled  # the second mirror at doubled n_full
+        flipped = not flipped
+        row = (doubled + 2 - parity) // 2
+        if not 0 <= row < stored:
+            return None
+    return row, flipped
+
+
 def volume_bounds(center: Sequence[float], size: Sequence[float], what: str):
     center = tuple(float(v) for v in center)
     size = tuple(float(v) for v in size)
@@ -133,14 +168,19 @@ def register_volume(grid: Grid, center: Sequence[float], size: Sequence[float], 
                 raise Unsupported(f"{what} reaches more than one period past the {AXIS_NAMES[axis]} face")
             region += [first, first + count]
             continue
-        low = 0
         if grid.is_mirrored(axis):
             # a folded axis serves the sites below the plane from their images (reference
-            # dft.py:1004 folded_axis_sites): the region may start below the stored cells,
-            # down to the unfolded cell's low wall
-            full = grid.shape_full[axis]
-            low = 1 - (full - full % 2) // 2
-        lo, hi = max(first, low), min(first + count, n)
+            # dft.py:1004 folded_axis_sites): the region keeps the ladder's cell-centre
+            # sites some chunk serves, which may start below the stored cells
+            served = [r for r in range(first, first + count) if folded_site(grid, axis, 1, r) is not None]
+            if not served:
+                raise ValueError(f"{what} lies outside the cell on the {AXIS_NAMES[axis]} axis")
+            if served[-1] - served[0] + 1 != len(served):
+                raise RuntimeError(f"{what}: the served sites of the folded {AXIS_NAMES[axis]} axis "
+                                   "are not one interval")
+            region += [served[0], served[-1] + 1]
+            continue
+        lo, hi = max(first, 0), min(first + count, n)
         if hi <= lo:
             raise ValueError(f"{what} lies outside the cell on the {AXIS_NAMES[axis]} axis")
         region += [lo, hi]

@@ -77,33 +77,38 @@ def _fill_accumulator(acc: torch.Tensor, q: int, values: Optional[np.ndarray]) -
 def fold_ghosts(grid: Grid, family: str) -> Dict[str, np.ndarray]:
     """The mirror-plane ghosts of one family ("B" or "D") as the library's lists
     (reference ``stepping.py:2004-2045`` ``fill_symmetry_bc_B/D``, ``MIRROR_SOURCE_INDEX``
-    2): every cell with index 0 on a folded axis where the component has Yee shift 0,
-    imaged from index 2 on each such axis with the product of the component's parities
-    there (the x, y, z passes of the fill compose to that at a corner), zero where it
-    sits on a metallic wall of an unfolded axis (``zero_metal`` follows the fill).
-    ``ghost`` / ``image``: int32 cell offsets; ``code``: component | 4 negate | 8 zero."""
+    2, and ``:2092`` ``fill_folded_far_ghosts_B/D``): every cell with index 0 on a folded
+    axis where the component has Yee shift 0, imaged from index 2, and on a folded
+    periodic axis every cell in the last slot where it has shift 1, imaged from the far
+    reflect row; each with the product of the component's parities over those axes (the
+    near passes, ``zero_metal`` and the far passes compose to that), zero where it sits
+    on a metallic wall of an unfolded axis. ``ghost`` / ``image``: int32 cell offsets;
+    ``code``: component | 4 negate | 8 zero."""
     nx, ny, nz = grid.shape
     strides = (ny * nz, nz, 1)
     ghosts, images, codes = [], [], []
     for q in range(3):
         comp = family + "xyz"[q]
         shifts = IYEE[comp]
-        folded = [a for a in range(3) if grid.is_mirrored(a) and shifts[a] == 0]
-        if not folded:
+        # (axis, ghost row, image row) of every plane of this component's ghosts
+        planes_of = [(a, 0, 2) for a in range(3) if grid.is_mirrored(a) and shifts[a] == 0]
+        planes_of += [(a, grid.shape[a] - 1, grid.far_reflect_row(a)) for a in range(3)
+                      if grid.far_reflect_row(a) is not None and shifts[a] == 1]
+        if not planes_of:
             continue
         planes = []
-        for a in folded:
+        for a, row, _ in planes_of:
             ranges = [np.arange(n, dtype=np.int64) for n in grid.shape]
-            ranges[a] = np.zeros(1, dtype=np.int64)
+            ranges[a] = np.full(1, row, dtype=np.int64)
             ii, jj, kk = np.meshgrid(*ranges, indexing="ij")
             planes.append(ii.ravel() * strides[0] + jj.ravel() * strides[1] + kk.ravel())
         offsets = np.unique(np.concatenate(planes))
         coords = [offsets // strides[0], (offsets // strides[1]) % ny, offsets % nz]
         sign = np.ones(offsets.size, dtype=np.int64)
         image = list(coords)
-        for a in folded:
-            at = coords[a] == 0
-            image[a] = np.where(at, 2, image[a])
+        for a, row, source in planes_of:
+            at = coords[a] == row
+            image[a] = np.where(at, source, image[a])
             sign = np.where(at, sign * grid.parity(comp, a), sign)
         zero = np.zeros(offsets.size, dtype=bool)
         for b in range(3):

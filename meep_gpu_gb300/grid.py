@@ -201,16 +201,12 @@ class Grid:
         self.nx_full, self.ny_full, self.nz_full = counts
         self.boundaries = normalize_boundaries(boundaries)
         self.mirrors = normalize_mirrors(symmetry)
-        for axis, plane in enumerate(self.mirrors):
-            if plane is not None and not self.is_metallic(axis):
-                raise Unsupported(
-                    f"a mirror plane on the periodic {AXIS_NAMES[axis]} axis (its second mirror at "
-                    f"+L/2 and the far ghost slot it stores) is not stepped by this engine; fold a "
-                    f"metallic axis")
-        # MEEP's halve(): n - n//2 + 1 cells on a folded axis, from one cell below the plane
-        # (reference grid.py:604, vec.cpp halve)
+        # MEEP's halve(): n - n//2 + 1 owned cells on a folded axis, from one cell below the
+        # plane (reference grid.py:604, vec.cpp halve); a folded periodic axis stores one
+        # more, MEEP's big_corner plane and the far ghost slot past it
         self.nx, self.ny, self.nz = (
-            counts[a] - counts[a] // 2 + 1 if self.mirrors[a] is not None else counts[a] for a in range(3))
+            self.owned_cells(a) + (0 if self.mirrors[a] is None or self.is_metallic(a) else 1)
+            for a in range(3))
         for axis in range(3):
             if self.mirrors[axis] is not None and self.shape[axis] < 4:
                 raise Unsupported(f"a folded axis needs at least 4 stored cells, {AXIS_NAMES[axis]} has "
@@ -255,6 +251,21 @@ class Grid:
 
     def is_mirrored(self, axis: int) -> bool:
         return self.mirrors[axis] is not None
+
+    def owned_cells(self, axis: int) -> int:
+        """MEEP's cell count of the axis (reference ``grid.py:1343``): the halved count
+        ``n - n//2 + 1`` on a folded axis, the full count elsewhere. It differs from the
+        stored count only on a folded periodic axis, which stores one cell more."""
+        n = self.shape_full[axis]
+        return n - n // 2 + 1 if self.mirrors[axis] is not None else n
+
+    def far_reflect_row(self, axis: int) -> Optional[int]:
+        """On a folded periodic axis, the stored row the far ghost slot (the last shift-1
+        slot) and the sample past the top image about the second mirror at doubled
+        ``n_full`` (reference ``stepping.py:2361``): ``n_full - stored + 2``; else None."""
+        if self.mirrors[axis] is None or self.is_metallic(axis):
+            return None
+        return self.shape_full[axis] - self.shape[axis] + 2
 
     def mirror_phase(self, axis: int) -> Optional[int]:
         """The declared phase of the axis's plane, None on an unfolded axis."""

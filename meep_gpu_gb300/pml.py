@@ -227,7 +227,10 @@ class PML:
         half_index = 2 * np.arange(n) + lattice
         if self.grid.axis_wraps(axis):
             half_index = (half_index - 1) % (2 * n) + 1
-        for wall, n_pml in ((0, self.faces[axis][0]), (2 * n, self.faces[axis][1])):
+        # the upper wall is MEEP's window top, 2 * owned cells: on a folded periodic axis
+        # the stored rows run one cell past it (reference pml.py:600 _wall_high)
+        wall_high = 2 * self.grid.owned_cells(axis)
+        for wall, n_pml in ((0, self.faces[axis][0]), (wall_high, self.faces[axis][1])):
             if n_pml <= 0:
                 continue
             scale = scale_factor * self.prefac(n_pml)

@@ -228,7 +228,8 @@ def chunk_boxes(grid: Grid, faces) -> List[Tuple[Tuple[int, int, int], Tuple[int
     per_axis = []
     for d in range(3):
         io = grid.origin_doubled(d)
-        pieces = axis_pieces(grid.shape[d], faces[d] if faces is not None else (0.0, 0.0))
+        # MEEP's window is owned cells long (a folded periodic axis stores one more)
+        pieces = axis_pieces(grid.owned_cells(d), faces[d] if faces is not None else (0.0, 0.0))
         per_axis.append([(io + lo, io + hi) for _piece, lo, hi in pieces])
     return [((bx[0], by[0], bz[0]), (bx[1], by[1], bz[1]))
             for bx in per_axis[0] for by in per_axis[1] for bz in per_axis[2]]
@@ -283,20 +284,26 @@ def deposition_pieces(grid: Grid, component: str, center: Sequence[float], size:
         tapers.append(boundary_weights(where_min[d], where_max[d], is_[d], ie[d], a))
     io = [grid.origin_doubled(d) for d in range(3)]
     counts = grid.shape
-    big = [io[d] + 2 * counts[d] for d in range(3)]
+    # the window top is MEEP's big corner, owned cells up: a folded periodic axis's far
+    # ghost slot is never deposited into
+    big = [io[d] + 2 * grid.owned_cells(d) for d in range(3)]
     window_low = [io[d] + 2 - iyee[d] for d in range(3)]
     window_high = [big[d] - iyee[d] for d in range(3)]
     if boxes is None:
         boxes = [((io[0], io[1], io[2]), (big[0], big[1], big[2]))]
     wraps = [grid.axis_wraps(d) for d in range(3)]
+    # MEEP loops lattice shifts on every axis with a periodic outer face, a folded one
+    # included (its second mirror is a lattice image; reference sources.py:925), by the
+    # full cell's lattice vector
+    periodic = [wraps[d] or (grid.is_mirrored(d) and not grid.is_metallic(d)) for d in range(3)]
     half_inva = 0.5 * inva
     min_shift = [0, 0, 0]
     max_shift = [0, 0, 0]
     period = [0, 0, 0]
     for d in range(3):
-        if not wraps[d]:
+        if not periodic[d]:
             continue
-        period[d] = 2 * counts[d]
+        period[d] = 2 * grid.shape_full[d]
         lattice = abs(period[d] * half_inva)
         min_shift[d] = int(math.floor((where_min[d] - big[d] * half_inva) / lattice))
         max_shift[d] = int(math.ceil((where_max[d] - io[d] * half_inva) / lattice))

@@ -69,9 +69,9 @@ typedef struct SUF(oracle_state) {
   const REAL* condinv[2][3];
   const unsigned char* keeps[2][3];
   REAL* fcond[2][3];
-  /* mirror planes: fold[a] = +1 / -1 (even / odd) folds the metallic axis a, whose
-   * unfolded count is full[a]; 0: no plane. metallic[a] stays 1 on a folded axis (its
-   * far wall). */
+  /* mirror planes: fold[a] = +1 / -1 (even / odd) folds axis a, whose unfolded count is
+   * full[a]; 0: no plane. metallic[a] is the folded axis's far face: on a periodic one
+   * (metallic 0) the last slot of the shift-1 components is the second mirror's ghost. */
   int fold[3];
   int full[3];
 } SUF(oracle_state);
@@ -87,7 +87,7 @@ static inline REAL SUF(up)(const SUF(oracle_state)* s, const REAL* f, int axis, 
   const int n[3] = {s->nx, s->ny, s->nz};
   idx[axis] += 1;
   if (idx[axis] == n[axis]) {
-    if (s->metallic[axis]) return (REAL)0;
+    if (s->metallic[axis] || s->fold[axis]) return (REAL)0;
     idx[axis] = 0;
   }
   return f[SUF(lin)(s, idx[0], idx[1], idx[2])];
@@ -98,7 +98,7 @@ static inline REAL SUF(down)(const SUF(oracle_state)* s, const REAL* f, int axis
   const int n[3] = {s->nx, s->ny, s->nz};
   idx[axis] -= 1;
   if (idx[axis] < 0) {
-    if (s->metallic[axis]) return (REAL)0;
+    if (s->metallic[axis] || s->fold[axis]) return (REAL)0;
     idx[axis] = n[axis] - 1;
   }
   return f[SUF(lin)(s, idx[0], idx[1], idx[2])];
@@ -134,7 +134,9 @@ static void SUF(curl_family)(SUF(oracle_state)* s, REAL* const target[3], REAL* 
           const int at[3] = {i, j, k};
           for (int a = 0; a < 3; ++a) {
             const int shift0 = backward ? (a != q) : (a == q);
-            if (shift0 && s->metallic[a] && at[a] == 0) curl = (REAL)0;
+            if (shift0 && (s->metallic[a] || s->fold[a]) && at[a] == 0) curl = (REAL)0;
+            /* the far ghost slot of a folded periodic axis (reference stepping.py:2618) */
+            if (!shift0 && s->fold[a] && !s->metallic[a] && at[a] == n[a] - 1) curl = (REAL)0;
           }
           s->scratch[c] = curl;
         }
@@ -246,6 +248,27 @@ static int SUF(parity)(const SUF(oracle_state)* s, int q, int a, int electric) {
   return (electric ? own : !own) ? -s->fold[a] : s->fold[a];
 }
 
+/* fill_folded_far_ghosts (reference stepping.py:2092): on a folded periodic axis the
+ * last slot of every shift-1 component = parity * the row it images about the second
+ * mirror at doubled full, full - n + 2. */
+static void SUF(fill_far)(SUF(oracle_state)* s, REAL* const f[3], int electric) {
+  const int n[3] = {s->nx, s->ny, s->nz};
+  for (int q = 0; q < 3; ++q)
+    for (int a = 0; a < 3; ++a) {
+      const int shift1 = electric ? (a == q) : (a != q);
+      if (!s->fold[a] || s->metallic[a] || !shift1) continue;
+      const REAL sign = (REAL)SUF(parity)(s, q, a, electric);
+      const int row = s->full[a] - n[a] + 2;
+      for (int i = (a == 0 ? n[0] - 1 : 0); i < n[0]; ++i)
+        for (int j = (a == 1 ? n[1] - 1 : 0); j < n[1]; ++j)
+          for (int k = (a == 2 ? n[2] - 1 : 0); k < n[2]; ++k) {
+            int src[3] = {i, j, k};
+            src[a] = row;
+            f[q][SUF(lin)(s, i, j, k)] = sign * f[q][SUF(lin)(s, src[0], src[1], src[2])];
+          }
+    }
+}
+
 /* fill_symmetry_bc (reference stepping.py:2038): cell 0 = parity * cell 2 on every
  * folded axis where the component's Yee shift is 0, axes in x, y, z order. */
 static void SUF(fill_symmetry)(SUF(oracle_state)* s, REAL* const f[3], int electric) {
@@ -279,6 +302,7 @@ void SUF(oracle_step)(SUF(oracle_state)* s, const double* words) {
   }
   SUF(fill_symmetry)(s, s->B, 0);
   SUF(zero_metal)(s, s->B, 0);
+  SUF(fill_far)(s, s->B, 0);
   /* 3. update_H (stored H only under a PML) */
   if (s->pml) {
     if (!s->h_separated) {
@@ -325,6 +349,7 @@ void SUF(oracle_step)(SUF(oracle_state)* s, const double* words) {
   /* 6. fill_symmetry_bc_D, 6b. zero_metal_D */
   SUF(fill_symmetry)(s, s->D, 1);
   SUF(zero_metal)(s, s->D, 1);
+  SUF(fill_far)(s, s->D, 1);
   /* 7. update_E: W = chi1inv * (D - sum P); E = W, or the own-axis accumulation. */
   for (int q = 0; q < 3; ++q)
 #pragma omp parallel for schedule(static)
@@ -385,15 +410,26 @@ static REAL SUF(sample_at)(const SUF(oracle_state)* s, const REAL* f, int cp, in
        * and at the far wall zero */
       const int q = cp % 3, electric = cp < 3;
       const int p = electric ? (a == q) : (a != q);
-      const int low = -(s->full[a] - s->full[a] % 2);
+      const int periodic = !s->metallic[a];
+      const int low = -(s->full[a] - s->full[a] % 2), lattice = 2 * s->full[a];
       int d = -2 + 2 * at[a] + p;
-      if (d < low + 2 - p || d > low + 2 * s->full[a] - p) return (REAL)0;
+      if (d < low + 2 - p || d > low + lattice - p) {
+        if (!periodic) return (REAL)0;
+        d += d < low + 2 - p ? lattice : -lattice;
+        if (d < low + 2 - p || d > low + lattice - p) return (REAL)0;
+      }
       if (d < -p) {
         d = -d;
         sign = sign * (REAL)SUF(parity)(s, q, a, electric);
       }
       at[a] = (d + 2 - p) / 2;
-      if (at[a] >= n[a]) return (REAL)0;
+      if (at[a] >= n[a]) {
+        if (!periodic) return (REAL)0;
+        d = lattice - d; /* the second mirror at doubled full */
+        sign = sign * (REAL)SUF(parity)(s, q, a, electric);
+        if (d + 2 - p < 0 || (d + 2 - p) / 2 >= n[a]) return (REAL)0;
+        at[a] = (d + 2 - p) / 2;
+      }
       continue;
     }
     if (at[a] >= n[a] || at[a] < 0) {

@@ -69,6 +69,14 @@ CASES = {
     "mirror_complex": dict(n=(12, 14, 14), pml={"x": 3, "z": {"high": 2}}, steps=50,
                            symmetry=(("Z", 1),), complex=True, mirror_sources=True,
                            boundaries=("metallic", "periodic", "metallic")),
+    # Folds of periodic axes (one more stored cell: MEEP's big_corner plane and the far
+    # ghost slot past the second mirror): an even count and an odd one, without an
+    # absorber, with a Lorentz slab; and a PML on a folded periodic axis's high face.
+    "mirror_periodic": dict(n=(14, 13, 12), pml={"z": 3}, steps=60, symmetry=(("X", 1), ("Y", -1)),
+                            boundaries="periodic", mirror_sources=True, lorentz=True),
+    "mirror_periodic_pml": dict(n=(16, 12, 13), pml={"z": {"high": 3}, "x": 2}, steps=50,
+                                symmetry=(("Z", -1),), boundaries=("metallic", "periodic", "periodic"),
+                                mirror_sources=True),
 }
 
 # The 80^3 sphere-under-PML workload (resolution 10, 10-cell PML, eps 4 sphere of radius

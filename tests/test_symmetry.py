@@ -20,6 +20,15 @@ from oracle.oracle import Oracle, problem_from_driver
 from tests.golden.cases import CASES, build_case
 
 
+def test_periodic_folds_store_the_far_slot():
+    grid = Grid((1.4, 1.3, 1.2), 10, boundaries="periodic", symmetry=("X", "Y"))
+    assert grid.shape == (9, 9, 12)  # owned + 1: big_corner's plane, then the far ghost slot
+    assert (grid.owned_cells(0), grid.owned_cells(1)) == (8, 8)
+    # the second mirror at doubled n_full: two rows below the top at an even count, three
+    # at an odd one (reference stepping.py:2361)
+    assert (grid.far_reflect_row(0), grid.far_reflect_row(1), grid.far_reflect_row(2)) == (7, 6, None)
+
+
 def test_folded_counts_origin_and_coordinates():
     grid = Grid((2.0, 1.5, 1.8), 10, boundaries="metallic", symmetry=(Mirror("X", -1), "y"))
     assert grid.shape_full == (20, 15, 18)
@@ -35,8 +44,10 @@ def test_folded_counts_origin_and_coordinates():
 
 
 def test_folds_that_are_not_stepped_are_refused():
+    d = FdtdDriver((1.4, 1.4, 1.4), 10, force_complex_fields=False, boundaries="periodic",
+                   symmetry=("X",))
     with pytest.raises(Unsupported, match="periodic"):
-        Grid((2.0, 2.0, 2.0), 10, boundaries="periodic", symmetry=("X",))
+        d.set_conductivity(0.1)
     with pytest.raises(Unsupported, match="k_point"):
         Grid((2.0, 2.0, 2.0), 10, boundaries=("metallic", "periodic", "periodic"),
              k_point=(0, 0.2, 0), symmetry=("X",))
@@ -97,7 +108,8 @@ def _zero_metal(grid, family, volumes):
 
 
 def _fill_like_the_reference(grid, family, volumes):
-    """cell 0 = parity * cell 2 per folded axis in x, y, z order, then zero_metal."""
+    """cell 0 = parity * cell 2 per folded axis in x, y, z order, zero_metal, then the far
+    slot of a folded periodic axis = parity * its reflect row."""
     out = [v.copy() for v in volumes]
     for q in range(3):
         comp = family + "xyz"[q]
@@ -107,14 +119,23 @@ def _fill_like_the_reference(grid, family, volumes):
                 src = [slice(None)] * 3
                 dst[a], src[a] = 0, 2
                 out[q][tuple(dst)] = grid.parity(comp, a) * out[q][tuple(src)]
-    return _zero_metal(grid, family, out)
+    out = _zero_metal(grid, family, out)
+    for q in range(3):
+        comp = family + "xyz"[q]
+        for a in range(3):
+            if grid.far_reflect_row(a) is not None and IYEE[comp][a] == 1:
+                dst = [slice(None)] * 3
+                src = [slice(None)] * 3
+                dst[a], src[a] = -1, grid.far_reflect_row(a)
+                out[q][tuple(dst)] = grid.parity(comp, a) * out[q][tuple(src)]
+    return out
 
 
+@pytest.mark.parametrize("boundaries", ["metallic", ("periodic", "metallic", "periodic"), "periodic"])
 @pytest.mark.parametrize("symmetry", [("X",), (Mirror("Y", -1),), ("X", Mirror("Z", -1)),
                                       (Mirror("X", -1), "Y", "Z")])
-def test_ghost_lists_are_the_fill(symmetry):
-    grid = Grid((1.2, 1.1, 1.4), 10, boundaries=("metallic", "metallic", "metallic"),
-                symmetry=symmetry)
+def test_ghost_lists_are_the_fill(symmetry, boundaries):
+    grid = Grid((1.2, 1.1, 1.4), 10, boundaries=boundaries, symmetry=symmetry)
     rng = np.random.default_rng(7)
     for family in ("B", "D"):
         # the step kernels have zeroed the walls (zero_metal) before the ghosts are written
@@ -139,15 +160,15 @@ def test_ghost_lists_are_the_fill(symmetry):
         assert not np.intersect1d(keyed(tables["ghost"]), keyed(tables["image"])).size
 
 
-def _mirror_pair(folded: bool):
+def _mirror_pair(folded: bool, boundaries: str = "metallic"):
     """An even X and an odd Y plane under a PML, a dielectric slab and a Lorentz slab
     normal to z (a medium the planes leave invariant: a cell-centred medium that varies
     along a folded axis is not symmetric about the plane on the shift-0 lattice), an Ez
     point source; unfolded, the same run with the source's parity-signed images."""
     symmetry = (Mirror("X", 1), Mirror("Y", -1)) if folded else ()
-    d = FdtdDriver((1.2, 1.0, 1.2), 10, force_complex_fields=False, boundaries="metallic",
+    d = FdtdDriver((1.2, 1.0, 1.2), 10, force_complex_fields=False, boundaries=boundaries,
                    symmetry=symmetry)
-    d.setup_pml(2)
+    d.setup_pml(2 if boundaries == "metallic" else {"z": 2})
     x, y, z = d.grid.meshgrid()
     d.set_epsilon(np.where(np.abs(z - 0.1) < 0.2, 3.0, 1.0).astype(np.float32))
     d.add_susceptibility(Susceptibility(frequency=1.1, gamma=0.05),
@@ -162,23 +183,32 @@ def _mirror_pair(folded: bool):
     return d, flux
 
 
-def test_a_folded_run_is_the_unfolded_run_with_image_sources():
-    """The float64 oracle: the folded run's stored words (ghosts included) equal the
-    unfolded run's at the same positions, and its flux through a plane spanning both
-    halves equals the unfolded flux (the device sampling's images and signs)."""
+@pytest.mark.parametrize("boundaries", ["metallic", "periodic"])
+def test_a_folded_run_is_the_unfolded_run_with_image_sources(boundaries):
+    """The float64 oracle: the folded run's stored words (ghosts included, and on a
+    periodic fold the far ghost slot past the second mirror) equal the unfolded run's at
+    the same positions, and its flux through a plane spanning both halves equals the
+    unfolded flux (the device sampling's images and signs)."""
     steps = 70
     runs = {}
     for folded in (True, False):
-        driver, _ = _mirror_pair(folded)
+        driver, _ = _mirror_pair(folded, boundaries)
         oracle = Oracle(problem_from_driver(driver), "f64")
         oracle.run(steps)
         runs[folded] = (driver, oracle)
     (fd, fo), (ud, uo) = runs[True], runs[False]
     offset = [(ud.grid.shape[a] - 2) // 2 if fd.grid.is_mirrored(a) else 0 for a in range(3)]
+    # a periodic fold's last stored row lies one cell past the unfolded window: its
+    # image is the unfolded row 0 (one lattice vector over)
+    unfolded = {c: uo.field(c) for c in ("Ex", "Ey", "Ez", "Dx", "Dy", "Dz", "Bx", "By", "Bz", "Hx",
+                                          "Hy", "Hz")}
+    if boundaries == "periodic":
+        unfolded = {c: np.concatenate([v, v[:1]], axis=0) for c, v in unfolded.items()}
+        unfolded = {c: np.concatenate([v, v[:, :1]], axis=1) for c, v in unfolded.items()}
     view = tuple(slice(offset[a], offset[a] + fd.grid.shape[a]) for a in range(3))
-    scale = max(np.max(np.abs(uo.field(c))) for c in ("Ez", "Hx", "Hy"))
+    scale = max(np.max(np.abs(unfolded[c])) for c in ("Ez", "Hx", "Hy"))
     for c in ("Ex", "Ey", "Ez", "Dx", "Dy", "Dz", "Bx", "By", "Bz", "Hx", "Hy", "Hz"):
-        assert np.max(np.abs(fo.field(c) - uo.field(c)[view])) <= 1e-12 * scale, c
+        assert np.max(np.abs(fo.field(c) - unfolded[c][view])) <= 1e-12 * scale, c
     unfolded = uo.flux_spectrum(0)
     assert np.max(np.abs(fo.flux_spectrum(0) - unfolded)) <= 1e-10 * np.max(np.abs(unfolded))
 

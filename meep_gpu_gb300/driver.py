@@ -123,14 +123,28 @@ class FdtdDriver:
             raise ValueError(f"{label} shape {array.shape} does not match the grid {shape}")
         return array
 
+    def _epsilon_and_inverse(self, value: Any, label: str) -> Tuple[np.ndarray, np.ndarray]:
+        """Float32 epsilon and float32(1 / float64(epsilon)) (MEEP's chi1inv, formed in
+        double), checked finite and positive; slab by slab, so the float64 temporaries
+        stay in cache. Both are private copies."""
+        array = self._volume(value, label)
+        flat = np.ascontiguousarray(array).reshape(-1)
+        epsilon = np.empty(flat.size, dtype=np.float32)
+        inverse = np.empty(flat.size, dtype=np.float32)
+        step = 1 << 18
+        for start in range(0, flat.size, step):
+            wide = flat[start:start + step].astype(np.float64)
+            if not np.isfinite(wide).all() or (wide <= 0).any():
+                raise ValueError(f"{label} must be finite and positive everywhere")
+            epsilon[start:start + step] = wide
+            np.divide(1.0, wide, out=wide)
+            inverse[start:start + step] = wide
+        return epsilon.reshape(self.grid.shape), inverse.reshape(self.grid.shape)
+
     def set_epsilon(self, eps: Any) -> None:
         """Isotropic permittivity: a scalar or a volume at the integer Yee positions."""
         self._require_unfrozen("set_epsilon")
-        wide = self._volume(eps, "epsilon").astype(np.float64)
-        if not np.all(np.isfinite(wide)) or np.any(wide <= 0):
-            raise ValueError("epsilon must be finite and positive everywhere")
-        inverse = np.ascontiguousarray((1.0 / wide).astype(np.float32))
-        epsilon = np.ascontiguousarray(wide.astype(np.float32))
+        epsilon, inverse = self._epsilon_and_inverse(eps, "epsilon")
         self._eps = (epsilon, epsilon, epsilon)
         self._inv_eps = (inverse, inverse, inverse)
 
@@ -140,11 +154,9 @@ class FdtdDriver:
         eps = []
         inv = []
         for label, value in (("eps_x", eps_x), ("eps_y", eps_y), ("eps_z", eps_z)):
-            wide = self._volume(value, label).astype(np.float64)
-            if not np.all(np.isfinite(wide)) or np.any(wide <= 0):
-                raise ValueError(f"{label} must be finite and positive everywhere")
-            eps.append(np.ascontiguousarray(wide.astype(np.float32)))
-            inv.append(np.ascontiguousarray((1.0 / wide).astype(np.float32)))
+            epsilon, inverse = self._epsilon_and_inverse(value, label)
+            eps.append(epsilon)
+            inv.append(inverse)
         self._eps = tuple(eps)  # type: ignore[assignment]
         self._inv_eps = tuple(inv)  # type: ignore[assignment]
 

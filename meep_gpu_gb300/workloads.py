@@ -52,6 +52,12 @@ STEPS = {"sphere80": 2000, "sphere192_8dft": 5000, "lorentz192": 10000, "sphere1
          "mirror192": 5000, "mirror80": 600}
 
 
+def _axes(grid):
+    """The cell-centre coordinates as broadcastable (n, 1, 1), (1, n, 1), (1, 1, n)
+    float32 arrays: the same words as the dense meshgrid, without its three volumes."""
+    return grid.x[:, None, None], grid.y[None, :, None], grid.z[None, None, :]
+
+
 def build(name: str, driver_cls=None, susceptibility_cls=None, **driver_kwargs):
     if driver_cls is None:
         from .driver import FdtdDriver as driver_cls  # noqa: N813
@@ -70,8 +76,8 @@ def build(name: str, driver_cls=None, susceptibility_cls=None, **driver_kwargs):
         d = driver_cls(cell_size=(length, length, length), resolution=res, courant=0.5,
                        force_complex_fields=False, boundaries="metallic", **driver_kwargs)
         d.setup_pml(10)
-        x, y, z = d.grid.meshgrid()
-        d.set_epsilon(np.where(x ** 2 + y ** 2 + z ** 2 < 2.0 ** 2, 4.0, 1.0).astype(np.float32))
+        x, y, z = _axes(d.grid)
+        d.set_epsilon(np.where(x ** 2 + y ** 2 + z ** 2 < 2.0 ** 2, np.float32(4.0), np.float32(1.0)))
         d.add_source({"source_type": "gaussian", "component": "Ez", "center": (-2.0, 0.0, 0.0),
                       "size": (0, 0, 0), "frequency": 0.15, "fwidth": 0.1})
         flux, dft = [], []

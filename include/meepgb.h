@@ -302,6 +302,14 @@ int mgb_set_dft_buffer(mgb_sim* sim, int32_t monitor, float* samples, void* scra
  * for its monitor). Call before reading accumulators. Asynchronous on `stream`. */
 int mgb_dft_flush(mgb_sim* sim, void* stream);
 
+/* Component `comp` (its index in the monitor's comp list) of monitor `monitor` as
+ * interleaved complex64 words (re, im) [nfreq][cells] into `dst` (device, 2 * nfreq *
+ * cells floats), buffered samples added first; for a complex run, `imag` is the
+ * imaginary-part plan and the words are acc_re + i acc_im as complex64 sums round them,
+ * (re.re - im.im, re.im + im.re). imag NULL: a real run. Asynchronous on `stream`. */
+int mgb_read_accumulator(mgb_sim* real, mgb_sim* imag, int32_t monitor, int32_t comp, float* dst,
+                         void* stream);
+
 /* Samples a monitor holds buffered (-1 for a bad argument). */
 int32_t mgb_dft_pending(mgb_sim* sim, int32_t monitor);
 

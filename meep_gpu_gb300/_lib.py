@@ -148,6 +148,8 @@ SIGNATURES = {
     "mgb_set_dft_buffer": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
                                           ctypes.c_void_p, ctypes.c_size_t]),
     "mgb_dft_flush": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "mgb_read_accumulator": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                            ctypes.c_void_p, ctypes.c_void_p]),
     "mgb_dft_pending": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32]),
     "mgb_dft_contract": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
                                         ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,

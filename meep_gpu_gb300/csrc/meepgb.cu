@@ -2212,6 +2212,24 @@ __global__ void __launch_bounds__(256) adj_inject(const __grid_constant__ DftPar
   }
 }
 
+// One accumulator component as interleaved complex64: planar rows [nf][2][cells] (re,
+// im) of the real-part plan, and of the imaginary-part plan when `b` is not null.
+__global__ void __launch_bounds__(256) interleave_accumulator(const float* __restrict__ a,
+                                                              const float* __restrict__ b, long long nf,
+                                                              long long cells, float2* __restrict__ dst) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nf * cells) return;
+  const long long f = t / cells, c = t - f * cells;
+  const float* ra = a + f * 2 * cells;
+  float re = ra[c], im = ra[cells + c];
+  if (b != nullptr) {
+    const float* rb = b + f * 2 * cells;
+    re = re - rb[cells + c];
+    im = im + rb[c];
+  }
+  dst[t] = make_float2(re, im);
+}
+
 // Copy [3][box] of one field family (0 E, 1 D, 2 H) into dst.
 __global__ void __launch_bounds__(256) copy_box(const __grid_constant__ StepParams p, int family,
                                                 BoxArgs b) {
@@ -3083,6 +3101,35 @@ int mgb_dft_flush(mgb_sim* sim, void* stream) {
     if (rc != MGB_OK) return rc;
   }
   return MGB_OK;
+}
+
+int mgb_read_accumulator(mgb_sim* real, mgb_sim* imag, int32_t monitor, int32_t comp, float* dst,
+                         void* stream) {
+  if (real == nullptr || dst == nullptr) return fail(MGB_ERR_ARGUMENT, "null plan or destination");
+  if (monitor < 0 || monitor >= real->desc.nmonitors) return fail(MGB_ERR_ARGUMENT, "no such monitor");
+  const mgb_monitor& m = real->desc.monitors[monitor];
+  if (comp < 0 || comp >= m.ncomp) return fail(MGB_ERR_ARGUMENT, "no such monitor component");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const long long cells = (long long)(m.region[1] - m.region[0]) * (m.region[3] - m.region[2]) *
+                          (m.region[5] - m.region[4]);
+  const long long nf = m.nfreq;
+  const float* b = nullptr;
+  int rc = flush_monitor(real, monitor, s);
+  if (rc != MGB_OK) return rc;
+  if (imag != nullptr) {
+    if (monitor >= imag->desc.nmonitors) return fail(MGB_ERR_ARGUMENT, "the imaginary plan lacks the monitor");
+    const mgb_monitor& mi = imag->desc.monitors[monitor];
+    if (mi.nfreq != m.nfreq || mi.ncomp != m.ncomp || memcmp(mi.region, m.region, sizeof m.region) != 0)
+      return fail(MGB_ERR_ARGUMENT, "the two plans' monitors differ");
+    rc = flush_monitor(imag, monitor, s);
+    if (rc != MGB_OK) return rc;
+    b = mi.acc + (long long)comp * nf * 2 * cells;
+  }
+  const long long n = nf * cells;
+  if (n == 0) return MGB_OK;
+  interleave_accumulator<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(m.acc + (long long)comp * nf * 2 * cells, b,
+                                                                    nf, cells, reinterpret_cast<float2*>(dst));
+  return launch_error("accumulator read");
 }
 
 int32_t mgb_dft_pending(mgb_sim* sim, int32_t monitor) {

@@ -452,10 +452,23 @@ class Engine:
     def read_accumulator(self, monitor, q: int) -> np.ndarray:
         """Complex64 host copy ``[nf][cells]`` of component ``q`` of a monitor (buffered
         samples contracted first)."""
-        self.flush_dft()
-        acc = self.monitor_tensors[self.monitors.index(monitor)][1]
-        host = acc[q].detach().cpu().numpy()  # [nf][2][cells]
-        return (host[:, 0, :] + 1j * host[:, 1, :]).astype(np.complex64)
+        return self.device_accumulator(monitor, q).cpu().numpy()
+
+    def device_accumulator(self, monitor, q: int, imag: Optional["Engine"] = None) -> torch.Tensor:
+        """Component ``q`` of a monitor as a complex64 device tensor ``[nf][cells]``,
+        interleaved by the library (``mgb_read_accumulator``) so the host copy is one
+        transfer; with ``imag`` (the imaginary-part plan of a complex run), the complex
+        sum of the two parts' transforms."""
+        index = self.monitors.index(monitor)
+        nf, cells = self.monitor_tensors[index][1].shape[1], self.monitor_tensors[index][1].shape[3]
+        out = torch.empty((nf, cells), dtype=torch.complex64, device=self.device)
+        stream = self.stream if self.stream is not None else torch.cuda.current_stream(self.device)
+        _lib.check(self.lib, self.lib.mgb_read_accumulator(
+            self.handle, None if imag is None else imag.handle, index, q, out.data_ptr(), stream.cuda_stream))
+        current = torch.cuda.current_stream(self.device)
+        if current != stream:
+            current.wait_stream(stream)
+        return out
 
     def write_accumulator(self, monitor, q: int, values: Optional[np.ndarray]) -> None:
         """Replace component ``q`` of a monitor by ``values`` (``[nf][cells]``; None: zero)."""
@@ -792,9 +805,8 @@ class ComplexEngine:
         self.im.flush_dft()
 
     def read_accumulator(self, monitor, q: int) -> np.ndarray:
-        real = self.re.read_accumulator(monitor, q)
-        imag = self.im.read_accumulator(monitor, q)
-        return (real + np.complex64(1j) * imag).astype(np.complex64)
+        # acc_re + i acc_im as the complex64 sum rounds it: (re.re - im.im) + i (re.im + im.re)
+        return self.re.device_accumulator(monitor, q, imag=self.im).cpu().numpy()
 
     def write_accumulator(self, monitor, q: int, values: Optional[np.ndarray]) -> None:
         self.re.write_accumulator(monitor, q, values)

@@ -18,6 +18,8 @@ grid's cell centres, as the configurations specify; there is no dataset.
 * ``sphere128``: a 128^3 sphere case with one flux plane.
 * ``sphere192``: the 192^3 sphere case with one 50-frequency flux plane (working set
   ~0.4 GB, above the L2 size): the case detailed kernel profiles are taken on.
+* ``sphere192_nopml``: the same without the PML (a bare metallic box): every CTA steps
+  the plain update, the case the PML's own cost is measured against.
 * ``absorber192``: the ``sphere192`` case with ``mp.Absorber(1.0)`` on all six faces (a
   graded D and B conductivity, 24 cells deep) in place of the PML, and a D conductivity
   0.05 inside the sphere; 5000 steps.
@@ -46,10 +48,10 @@ from __future__ import annotations
 import numpy as np
 
 WORKLOADS = ("sphere80", "sphere192_8dft", "lorentz192", "sphere128", "sphere192", "absorber192",
-             "lossy_pml192", "lossy40", "mirror192", "mirror80")
+             "lossy_pml192", "lossy40", "mirror192", "mirror80", "sphere192_nopml")
 STEPS = {"sphere80": 2000, "sphere192_8dft": 5000, "lorentz192": 10000, "sphere128": 1000,
          "sphere192": 5000, "absorber192": 5000, "lossy_pml192": 5000, "lossy40": 300,
-         "mirror192": 5000, "mirror80": 600}
+         "mirror192": 5000, "mirror80": 600, "sphere192_nopml": 5000}
 
 
 def _axes(grid):
@@ -63,9 +65,10 @@ def build(name: str, driver_cls=None, susceptibility_cls=None, **driver_kwargs):
         from .driver import FdtdDriver as driver_cls  # noqa: N813
     if susceptibility_cls is None:
         from .dispersion import Susceptibility as susceptibility_cls  # noqa: N813
-    if name in ("sphere80", "sphere192_8dft", "sphere128", "sphere192", "mirror192", "mirror80"):
+    if name in ("sphere80", "sphere192_8dft", "sphere128", "sphere192", "mirror192", "mirror80",
+                "sphere192_nopml"):
         res = {"sphere80": 10, "sphere192_8dft": 24, "sphere128": 16, "sphere192": 24,
-               "mirror192": 24, "mirror80": 10}[name]
+               "mirror192": 24, "mirror80": 10, "sphere192_nopml": 24}[name]
         length = 8.0
         if name.startswith("mirror"):
             from .grid import Mirror
@@ -73,9 +76,13 @@ def build(name: str, driver_cls=None, susceptibility_cls=None, **driver_kwargs):
             # mirror and, lying along z, under an odd Z one
             driver_kwargs = dict(driver_kwargs, symmetry=(Mirror("Y", 1), Mirror("Z", -1)))
             name = "sphere192_8dft" if name == "mirror192" else "sphere80"
+        open_box = name == "sphere192_nopml"
+        if open_box:
+            name = "sphere192"
         d = driver_cls(cell_size=(length, length, length), resolution=res, courant=0.5,
                        force_complex_fields=False, boundaries="metallic", **driver_kwargs)
-        d.setup_pml(10)
+        if not open_box:
+            d.setup_pml(10)
         x, y, z = _axes(d.grid)
         d.set_epsilon(np.where(x ** 2 + y ** 2 + z ** 2 < 2.0 ** 2, np.float32(4.0), np.float32(1.0)))
         d.add_source({"source_type": "gaussian", "component": "Ez", "center": (-2.0, 0.0, 0.0),
@@ -195,8 +202,15 @@ def main(argv=None) -> None:
     parser = argparse.ArgumentParser(description=main.__doc__)
     parser.add_argument("name", choices=WORKLOADS)
     parser.add_argument("--steps", type=int, default=10)
+    parser.add_argument("--kernels", default=None,
+                        help="fixed kernel choice: 4 numbers (family, block_z, block_y, x_chunk) "
+                             "or 8 (the H half's, then the E half's); default: autotuned")
     args = parser.parse_args(argv)
-    driver, _, _ = build(args.name, FdtdDriver)
+    kernels = None
+    if args.kernels:
+        values = tuple(int(v) for v in args.kernels.split(","))
+        kernels = values if len(values) == 4 else (values[:4], values[4:])
+    driver, _, _ = build(args.name, FdtdDriver, kernels=kernels)
     driver.step_many(3)
     torch.cuda.synchronize()
     start = time.perf_counter()

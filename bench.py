@@ -22,6 +22,8 @@ decimated steps).
 * ``lossy``: the lossy kernels (D and B conductivity) on two 192^3 workloads, an
   absorber in place of the PML and a conductivity under the PML, each with its per-half
   roofline, and their float64 error on a 40^3 lossy case.
+* ``complex``: complex fields on the Bloch-periodic 192^3 case (both parts stepped
+  together), its per-half roofline, and the float64 error of a complex 80^3 case.
 * ``mirror``: the folded path on the headline case under an even Y and an odd Z mirror
   (192 x 97 x 97 stored cells), its throughput on the stored cells and as the unfolded
   run it stands for, its per-half roofline with the fold kernels, and the float64 error
@@ -66,6 +68,8 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-validate", action="store_true")
     p.add_argument("--kernel-steps", type=int, default=40, help="steps timed kernel by kernel")
+    p.add_argument("--complex-steps", type=int, default=100,
+                   help="steps timed on the Bloch-periodic complex bloch192 workload (0: skip)")
     p.add_argument("--mirror-steps", type=int, default=200,
                    help="steps timed on the folded mirror192 workload (0: skip the mirror section)")
     p.add_argument("--lossy-steps", type=int, default=100,
@@ -390,10 +394,13 @@ def main():
         served = bench_serving(device, args)
     lossy = None
     mirror = None
+    complex_ = None
     if args.lossy_steps > 0:
         lossy = bench_lossy(device, args)
     if args.mirror_steps > 0:
         mirror = bench_mirror(device, args)
+    if args.complex_steps > 0:
+        complex_ = bench_complex(device, args)
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "Mcell-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 5),
@@ -407,7 +414,7 @@ def main():
                    "monitors": {"flux_planes": len(flux), "dft_volumes": len(dft),
                                 "decimation": [m.decimation_factor for m in list(flux) + list(dft)][:1]}},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-        "clocks": clocks.summary(), "error": error, "serving": served, "lossy": lossy, "mirror": mirror,
+        "clocks": clocks.summary(), "error": error, "serving": served, "lossy": lossy, "mirror": mirror, "complex": complex_,
     }
     print(json.dumps(line), flush=True)
 
@@ -681,6 +688,84 @@ def bench_lossy(device, args):
     got = flux[0].get_flux_spectrum()
     expected = o64.flux_spectrum(0)
     out["error"] = {"lossy40_300_steps": {
+        "fields_rel_l2_vs_f64": float(math.sqrt(num / den)),
+        "flux_rel_vs_f64": float(np.max(np.abs(got - expected)) / np.max(np.abs(expected)))}}
+    gpu.close()
+    return out
+
+
+def bench_complex(device, args):
+    """Complex fields: bloch192 (the 192^3 sphere on a lattice periodic in x and y with a
+    Bloch vector, the two parts stepped together) device-resident over K steps, each half
+    of both parts timed with events; the float64 error of the complex (k = 0) 80^3 case
+    (its two parts against two float64 oracle runs)."""
+    import torch
+
+    from meep_gpu_gb300 import FdtdDriver, workloads
+    from oracle.oracle import Oracle, complex_flux_spectrum, problem_from_driver
+
+    peak, _ = measured_peaks()
+    stream = torch.cuda.current_stream(device)
+    driver, _, _ = workloads.build("bloch192", FdtdDriver)
+    driver.step_many(3)
+    engine = driver.engine
+    first, steps = driver.step_count, args.complex_steps
+    engine.ensure_source_words(first, steps + 20)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(device)
+    with ClockSampler(device.index or 0) as clocks:
+        start.record(stream)
+        engine.step(first, steps)
+        end.record(stream)
+        torch.cuda.synchronize(device)
+    ms = start.elapsed_time(end) / steps
+    n0 = first + steps
+    events = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(20)]
+    for t, ev in enumerate(events):
+        ev[0].record(stream)
+        engine.launch(n0 + t, 0, stream)
+        ev[1].record(stream)
+        engine.launch(n0 + t, 1, stream)
+        ev[2].record(stream)
+    torch.cuda.synchronize(device)
+    # both parts move the real plan's bytes (the phased reads of the other part touch one
+    # plane per phased axis)
+    nbytes = {k: 2 * v for k, v in engine.re.algorithmic_bytes().items()}
+    halves = {}
+    for part, key in enumerate(("h_half", "e_half")):
+        half_ms = float(np.mean([ev[part].elapsed_time(ev[part + 1]) for ev in events]))
+        gbs = nbytes[key] / (half_ms / 1e3) / 1e9
+        halves[key] = {"ms": round(half_ms, 4), "GB/s": round(gbs, 1), "frac": round(gbs / peak, 4)}
+    cells = driver.grid.total_cells
+    step_bytes = nbytes["h_half"] + nbytes["e_half"]
+    out = {"bloch192": {
+        "value": round(cells / (ms / 1e3) / 1e6, 3), "unit": "Mcell-steps/s (complex cells)",
+        "ms_per_step": round(ms, 5), "steps": steps, "k_point": list(driver.grid.k_point),
+        "step_frac": round(step_bytes / (ms / 1e3) / 1e9 / peak, 4), "per_kernel": halves,
+        "kernels": [list(c) for c in engine.choice], "clocks": clocks.summary(),
+        "note": "two float32 parts per complex word, stepped together (mgb_step_pair)"}}
+    if engine.re.nonfinite() or engine.im.nonfinite():
+        raise RuntimeError("the bloch192 run wrote a non-finite field")
+    driver.close()
+    del driver, engine
+    torch.cuda.empty_cache()
+    steps = workloads.STEPS["complex80"]
+    gpu, flux, _ = workloads.build("complex80", FdtdDriver)
+    gpu.run(num_steps=steps, progress_interval=steps)
+    ref, _, _ = workloads.build("complex80", FdtdDriver)
+    problem = problem_from_driver(ref)
+    parts = [Oracle(problem, "f64", part) for part in ("real", "imag")]
+    for oracle in parts:
+        oracle.run(steps)
+    num = den = 0.0
+    for c in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz"):
+        a = gpu.get_field(c, cell_centered=False).astype(np.complex128)
+        b = parts[0].field(c) + 1j * parts[1].field(c)
+        num += float(np.sum(np.abs(a - b) ** 2))
+        den += float(np.sum(np.abs(b) ** 2))
+    got = flux[0].get_flux_spectrum()
+    expected = complex_flux_spectrum(parts[0], parts[1], 0)
+    out["error"] = {"complex80_600_steps": {
         "fields_rel_l2_vs_f64": float(math.sqrt(num / den)),
         "flux_rel_vs_f64": float(np.max(np.abs(got - expected)) / np.max(np.abs(expected)))}}
     gpu.close()

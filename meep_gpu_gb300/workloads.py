@@ -18,6 +18,12 @@ grid's cell centres, as the configurations specify; there is no dataset.
 * ``sphere128``: a 128^3 sphere case with one flux plane.
 * ``sphere192``: the 192^3 sphere case with one 50-frequency flux plane (working set
   ~0.4 GB, above the L2 size): the case detailed kernel profiles are taken on.
+* ``bloch192``: the 192^3 sphere case (resolution 24) with complex fields on a lattice
+  periodic in x and y with Bloch vector k = (0.25, 0.1, 0), the 10-cell PML on z only,
+  a z-normal 50-frequency flux plane at z = 2.5 across the whole period; 5000 steps.
+* ``complex80``: the ``sphere80`` case with complex fields (k = 0) and a complex source
+  amplitude (0.6 - 0.8i); the case the complex path's float64 error is quoted on (600
+  steps).
 * ``sphere192_nopml``: the same without the PML (a bare metallic box): every CTA steps
   the plain update, the case the PML's own cost is measured against.
 * ``absorber192``: the ``sphere192`` case with ``mp.Absorber(1.0)`` on all six faces (a
@@ -48,10 +54,12 @@ from __future__ import annotations
 import numpy as np
 
 WORKLOADS = ("sphere80", "sphere192_8dft", "lorentz192", "sphere128", "sphere192", "absorber192",
-             "lossy_pml192", "lossy40", "mirror192", "mirror80", "sphere192_nopml")
+             "lossy_pml192", "lossy40", "mirror192", "mirror80", "sphere192_nopml", "bloch192",
+             "complex80")
 STEPS = {"sphere80": 2000, "sphere192_8dft": 5000, "lorentz192": 10000, "sphere128": 1000,
          "sphere192": 5000, "absorber192": 5000, "lossy_pml192": 5000, "lossy40": 300,
-         "mirror192": 5000, "mirror80": 600, "sphere192_nopml": 5000}
+         "mirror192": 5000, "mirror80": 600, "sphere192_nopml": 5000, "bloch192": 5000,
+         "complex80": 600}
 
 
 def _axes(grid):
@@ -108,6 +116,25 @@ def build(name: str, driver_cls=None, susceptibility_cls=None, **driver_kwargs):
                                          center=(sign * 1.6, 0.0, 0.0), size=(side, side, side),
                                          decimation_factor=0))
         return d, flux, dft
+    if name in ("bloch192", "complex80"):
+        bloch = name == "bloch192"
+        res = 24 if bloch else 10
+        d = driver_cls(cell_size=(8.0, 8.0, 8.0), resolution=res, courant=0.5, force_complex_fields=True,
+                       boundaries=("periodic", "periodic", "metallic") if bloch else "metallic",
+                       k_point=(0.25, 0.1, 0.0) if bloch else (0.0, 0.0, 0.0), **driver_kwargs)
+        d.setup_pml({"z": 10} if bloch else 10)
+        x, y, z = _axes(d.grid)
+        d.set_epsilon(np.where(x ** 2 + y ** 2 + z ** 2 < 2.0 ** 2, np.float32(4.0), np.float32(1.0)))
+        d.add_source({"source_type": "gaussian", "component": "Ez", "center": (-2.0, 0.0, 0.0),
+                      "size": (0, 0, 0), "frequency": 0.15, "fwidth": 0.1,
+                      "amplitude": 1.0 if bloch else 0.6 - 0.8j})
+        if bloch:
+            flux = [d.add_flux_monitor(fcen=0.15, df=0.1, nfreq=50, center=(0, 0, 2.5), size=(8.0, 8.0, 0),
+                                       decimation_factor=0)]
+        else:
+            flux = [d.add_flux_monitor(fcen=0.15, df=0.1, nfreq=50, center=(2.5, 0, 0), size=(0, 6, 6),
+                                       decimation_factor=0)]
+        return d, flux, []
     if name in ("absorber192", "lossy_pml192"):
         from .conductivity import AbsorberLayer
         d = driver_cls(cell_size=(8.0, 8.0, 8.0), resolution=24, courant=0.5,

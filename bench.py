@@ -698,11 +698,12 @@ def bench_complex(device, args):
     """Complex fields: bloch192 (the 192^3 sphere on a lattice periodic in x and y with a
     Bloch vector, the two parts stepped together) device-resident over K steps, each half
     of both parts timed with events; the float64 error of the complex (k = 0) 80^3 case
-    (its two parts against two float64 oracle runs)."""
+    (its two parts against two float64 oracle runs) and of the Bloch 48^3 case (against
+    the float64 oracle's two parts stepped together)."""
     import torch
 
     from meep_gpu_gb300 import FdtdDriver, workloads
-    from oracle.oracle import Oracle, complex_flux_spectrum, problem_from_driver
+    from oracle.oracle import BlochPair, Oracle, complex_flux_spectrum, problem_from_driver
 
     peak, _ = measured_peaks()
     stream = torch.cuda.current_stream(device)
@@ -768,6 +769,25 @@ def bench_complex(device, args):
     out["error"] = {"complex80_600_steps": {
         "fields_rel_l2_vs_f64": float(math.sqrt(num / den)),
         "flux_rel_vs_f64": float(np.max(np.abs(got - expected)) / np.max(np.abs(expected)))}}
+    gpu.close()
+    # a Bloch run against the float64 oracle's two parts stepped together
+    steps = workloads.STEPS["bloch48"]
+    gpu, flux, _ = workloads.build("bloch48", FdtdDriver)
+    gpu.run(num_steps=steps, progress_interval=steps)
+    ref, _, _ = workloads.build("bloch48", FdtdDriver)
+    pair = BlochPair(problem_from_driver(ref), "f64")
+    pair.run(steps)
+    num = den = 0.0
+    for c in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz"):
+        a = gpu.get_field(c, cell_centered=False).astype(np.complex128)
+        b = pair.field(c)
+        num += float(np.sum(np.abs(a - b) ** 2))
+        den += float(np.sum(np.abs(b) ** 2))
+    got = flux[0].get_flux_spectrum()
+    expected = complex_flux_spectrum(pair.re, pair.im, 0)
+    out["error"]["bloch48_600_steps"] = {
+        "fields_rel_l2_vs_f64": float(math.sqrt(num / den)),
+        "flux_rel_vs_f64": float(np.max(np.abs(got - expected)) / np.max(np.abs(expected)))}
     gpu.close()
     return out
 

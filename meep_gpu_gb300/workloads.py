@@ -21,6 +21,8 @@ grid's cell centres, as the configurations specify; there is no dataset.
 * ``bloch192``: the 192^3 sphere case (resolution 24) with complex fields on a lattice
   periodic in x and y with Bloch vector k = (0.25, 0.1, 0), the 10-cell PML on z only,
   a z-normal 50-frequency flux plane at z = 2.5 across the whole period; 5000 steps.
+* ``bloch48``: the ``bloch192`` case at resolution 6 (48^3, 5-cell PML on z); the case
+  the Bloch path's float64 error is quoted on (600 steps).
 * ``complex80``: the ``sphere80`` case with complex fields (k = 0) and a complex source
   amplitude (0.6 - 0.8i); the case the complex path's float64 error is quoted on (600
   steps).
@@ -55,11 +57,11 @@ import numpy as np
 
 WORKLOADS = ("sphere80", "sphere192_8dft", "lorentz192", "sphere128", "sphere192", "absorber192",
              "lossy_pml192", "lossy40", "mirror192", "mirror80", "sphere192_nopml", "bloch192",
-             "complex80")
+             "complex80", "bloch48")
 STEPS = {"sphere80": 2000, "sphere192_8dft": 5000, "lorentz192": 10000, "sphere128": 1000,
          "sphere192": 5000, "absorber192": 5000, "lossy_pml192": 5000, "lossy40": 300,
          "mirror192": 5000, "mirror80": 600, "sphere192_nopml": 5000, "bloch192": 5000,
-         "complex80": 600}
+         "complex80": 600, "bloch48": 600}
 
 
 def _axes(grid):
@@ -116,13 +118,13 @@ def build(name: str, driver_cls=None, susceptibility_cls=None, **driver_kwargs):
                                          center=(sign * 1.6, 0.0, 0.0), size=(side, side, side),
                                          decimation_factor=0))
         return d, flux, dft
-    if name in ("bloch192", "complex80"):
-        bloch = name == "bloch192"
-        res = 24 if bloch else 10
+    if name in ("bloch192", "complex80", "bloch48"):
+        bloch = name != "complex80"
+        res = {"bloch192": 24, "bloch48": 6, "complex80": 10}[name]
         d = driver_cls(cell_size=(8.0, 8.0, 8.0), resolution=res, courant=0.5, force_complex_fields=True,
                        boundaries=("periodic", "periodic", "metallic") if bloch else "metallic",
                        k_point=(0.25, 0.1, 0.0) if bloch else (0.0, 0.0, 0.0), **driver_kwargs)
-        d.setup_pml({"z": 10} if bloch else 10)
+        d.setup_pml({"z": 5 if name == "bloch48" else 10} if bloch else 10)
         x, y, z = _axes(d.grid)
         d.set_epsilon(np.where(x ** 2 + y ** 2 + z ** 2 < 2.0 ** 2, np.float32(4.0), np.float32(1.0)))
         d.add_source({"source_type": "gaussian", "component": "Ez", "center": (-2.0, 0.0, 0.0),

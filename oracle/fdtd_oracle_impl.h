@@ -74,7 +74,29 @@ typedef struct SUF(oracle_state) {
    * (metallic 0) the last slot of the shift-1 components is the second mirror's ghost. */
   int fold[3];
   int full[3];
+  /* Bloch phases (a complex run with k != 0, its two parts stepped together): per axis
+   * bmode 0 none, 1 copy, 2 negate, 3 the phase (bre, bim); `part` 0 steps the real
+   * parts, 1 the imaginary ones; pE / pH the other part's E and H. */
+  int bloch;
+  int bmode[3];
+  REAL bre[3], bim[3];
+  int part;
+  REAL* pE[3];
+  REAL* pH[3];
 } SUF(oracle_state);
+
+/* A curl operand read across a Bloch-phased face at the same stored index (reference
+ * stepping.py:2544 _bloch_ghost_operand): this part's word and the other part's times
+ * the axis's phase, conjugated for the word below the window (B's forward curl), each
+ * product and sum rounded on its own. */
+static inline REAL SUF(bloch_word)(const SUF(oracle_state)* s, int axis, int conj, REAL own, REAL other) {
+  const int mode = s->bmode[axis];
+  if (mode == 2) return -own;
+  if (mode != 3) return own;
+  const REAL a = s->bre[axis];
+  const REAL b = conj ? -s->bim[axis] : s->bim[axis];
+  return s->part ? (a * own) + (b * other) : (a * own) - (b * other);
+}
 
 static inline long long SUF(lin)(const SUF(oracle_state)* s, int i, int j, int k) {
   return ((long long)i * s->ny + j) * s->nz + k;
@@ -108,7 +130,7 @@ static inline REAL SUF(down)(const SUF(oracle_state)* s, const REAL* f, int axis
  * (backward, integer lattice). Component q: first = (q+2)%3 along axis (q+1)%3,
  * second = (q+1)%3 along axis (q+2)%3; dsig = (q+1)%3, dsigu = (q+2)%3. */
 static void SUF(curl_family)(SUF(oracle_state)* s, REAL* const target[3], REAL* const src[3],
-                             REAL* const fu[3], int backward) {
+                             REAL* const fu[3], int backward, REAL* const partner[3]) {
   const int lattice = backward ? 0 : 1;
   const int side = backward ? 1 : 0; /* conductivity side: D steps backward, B forward */
   const int n[3] = {s->nx, s->ny, s->nz};
@@ -123,8 +145,16 @@ static void SUF(curl_family)(SUF(oracle_state)* s, REAL* const target[3], REAL* 
           const long long c = SUF(lin)(s, i, j, k);
           const REAL g1s = backward ? SUF(down)(s, g1, a1, i, j, k) : SUF(up)(s, g1, a1, i, j, k);
           const REAL g2s = backward ? SUF(down)(s, g2, a2, i, j, k) : SUF(up)(s, g2, a2, i, j, k);
-          REAL bracket = g1s - g1[c];
-          bracket = bracket + g2[c];
+          REAL g1c = g1[c], g2c = g2[c];
+          if (s->bloch) {
+            /* the same-index operands at index 0 of a phased axis: conj(eikna) below the
+             * window for B, eikna above it for D */
+            const int at0[3] = {i, j, k};
+            if (at0[a1] == 0 && s->bmode[a1]) g1c = SUF(bloch_word)(s, a1, !backward, g1c, partner[a2][c]);
+            if (at0[a2] == 0 && s->bmode[a2]) g2c = SUF(bloch_word)(s, a2, !backward, g2c, partner[a1][c]);
+          }
+          REAL bracket = g1s - g1c;
+          bracket = bracket + g2c;
           bracket = bracket - g2s;
           REAL curl = s->dtdx * bracket;
           /* mask: cell 0 of every metallic axis where the target's Yee shift is 0 (the
@@ -288,12 +318,16 @@ static void SUF(fill_symmetry)(SUF(oracle_state)* s, REAL* const f[3], int elect
     }
 }
 
-void SUF(oracle_step)(SUF(oracle_state)* s, const double* words) {
+/* One half of a step: 0 the H half (step_B, magnetic sources, fills, update_H), 1 the E
+ * half (step_D, electric sources, fills, update_E, update_P). A Bloch run steps the H
+ * halves of both parts, then the E halves. */
+void SUF(oracle_half)(SUF(oracle_state)* s, const double* words, int half) {
   const int n[3] = {s->nx, s->ny, s->nz};
   const long long cells = (long long)n[0] * n[1] * n[2];
+  if (half == 1) goto e_half;
   /* 1. step_B, 2. magnetic sources (components 3..5, B = NARROW(double(B) - A)),
    * 2b. zero_metal_B */
-  SUF(curl_family)(s, s->B, s->E, s->fuB, 0);
+  SUF(curl_family)(s, s->B, s->E, s->fuB, 0, s->pE);
   for (int p = 0; p < s->nsrc; ++p) {
     if (s->src_comp[p] < 3) continue;
     REAL* b = s->B[s->src_comp[p] - 3];
@@ -337,8 +371,10 @@ void SUF(oracle_step)(SUF(oracle_state)* s, const double* words) {
           }
   }
   s->h_separated = 1;
+  return;
+e_half:
   /* 4. step_D */
-  SUF(curl_family)(s, s->D, s->H, s->fuD, 1);
+  SUF(curl_family)(s, s->D, s->H, s->fuD, 1, s->pH);
   /* 5. electric sources: D = NARROW(double(D) - A) point by point */
   for (int p = 0; p < s->nsrc; ++p) {
     if (s->src_comp[p] >= 3) continue;
@@ -394,11 +430,17 @@ void SUF(oracle_step)(SUF(oracle_state)* s, const double* words) {
   }
 }
 
+void SUF(oracle_step)(SUF(oracle_state)* s, const double* words) {
+  SUF(oracle_half)(s, words, 0);
+  SUF(oracle_half)(s, words, 1);
+}
+
 /* Monitor accumulation on a post-increment step: cell-centred samples (x, then y, then
  * z averages on shift-0 axes) times exp(i w t) * scale, E at t = step*dt, H at t - dt/2.
  * comp: 0..2 E, 3..5 H. acc: [ncomp][nfreq][2][cells]. In the float32 oracle the
  * phase is rounded to float32 and the products and sums are float32, as complex64. */
-static REAL SUF(sample_at)(const SUF(oracle_state)* s, const REAL* f, int cp, int i, int j, int k) {
+static REAL SUF(sample_at)(const SUF(oracle_state)* s, const REAL* f, const REAL* other, int cp, int i, int j,
+                           int k) {
   const int n[3] = {s->nx, s->ny, s->nz};
   int at[3] = {i, j, k};
   REAL sign = (REAL)1;
@@ -438,7 +480,33 @@ static REAL SUF(sample_at)(const SUF(oracle_state)* s, const REAL* f, int cp, in
       if (at[a] < 0) at[a] += n[a];
     }
   }
-  return sign * f[SUF(lin)(s, at[0], at[1], at[2])];
+  const REAL own = sign * f[SUF(lin)(s, at[0], at[1], at[2])];
+  if (!s->bloch) return own;
+  /* On a Bloch-phased axis the ladder point r is eikna^count times the stored word, count
+   * = floor((r - low) / n), low 1 for a component with Yee shift 0 there (its cell 0
+   * stores the owned top point), the powers by repeated products (reference dft.py:927) */
+  const int raw[3] = {i, j, k};
+  const int q = cp % 3, electric = cp < 3;
+  REAL fr = (REAL)1, fi = (REAL)0;
+  int any = 0;
+  for (int a = 0; a < 3; ++a) {
+    if (!s->bmode[a]) continue;
+    const int low = (electric ? (a != q) : (a == q)) ? 1 : 0;
+    const int shifted = raw[a] - low;
+    int count = shifted >= 0 ? shifted / n[a] : -((-shifted + n[a] - 1) / n[a]);
+    const REAL br = s->bmode[a] == 2 ? (REAL)-1 : s->bmode[a] == 1 ? (REAL)1 : s->bre[a];
+    const REAL bi0 = s->bmode[a] == 3 ? s->bim[a] : (REAL)0;
+    const REAL bi = count < 0 ? -bi0 : bi0;
+    for (count = count < 0 ? -count : count; count > 0; --count) {
+      const REAL nr = fr * br - fi * bi, ni = fr * bi + fi * br;
+      fr = nr;
+      fi = ni;
+      any = 1;
+    }
+  }
+  if (!any) return own;
+  const REAL o = other[SUF(lin)(s, at[0], at[1], at[2])];
+  return s->part ? (fr * own) + (fi * o) : (fr * own) - (fi * o);
 }
 
 void SUF(oracle_dft)(const SUF(oracle_state)* s, const int region[6], int ncomp, const int* comp,
@@ -453,6 +521,7 @@ void SUF(oracle_dft)(const SUF(oracle_state)* s, const int region[6], int ncomp,
     const int axis = cp % 3;
     const int electric = cp < 3;
     const REAL* f = electric ? s->E[axis] : s->H[axis];
+    const REAL* other = electric ? s->pE[axis] : s->pH[axis];
     int avg[3];
     for (int a = 0; a < 3; ++a) avg[a] = electric ? (a != axis) : (a == axis);
 #pragma omp parallel for schedule(static)
@@ -463,9 +532,9 @@ void SUF(oracle_dft)(const SUF(oracle_state)* s, const int region[6], int ncomp,
       for (int b = 0; b < 2; ++b)
         for (int a = 0; a < 2; ++a) {
           if ((a && !avg[1]) || (b && !avg[2])) { v[b][a] = 0; continue; }
-          const REAL f0 = SUF(sample_at)(s, f, cp, i, j + a, k + b);
+          const REAL f0 = SUF(sample_at)(s, f, other, cp, i, j + a, k + b);
           if (avg[0]) {
-            const REAL f1 = SUF(sample_at)(s, f, cp, i + 1, j + a, k + b);
+            const REAL f1 = SUF(sample_at)(s, f, other, cp, i + 1, j + a, k + b);
             v[b][a] = (REAL)0.5 * (f0 + f1);
           } else {
             v[b][a] = f0;

@@ -69,7 +69,9 @@ def _state_type(real) -> type:
                     ("h_separated", ctypes.c_int),
                     ("condfac", (P * 3) * 2), ("condinv", (P * 3) * 2), ("keeps", (P * 3) * 2),
                     ("fcond", (P * 3) * 2), ("fold", ctypes.c_int * 3),
-                    ("full", ctypes.c_int * 3)]
+                    ("full", ctypes.c_int * 3), ("bloch", ctypes.c_int), ("bmode", ctypes.c_int * 3),
+                    ("bre", real * 3), ("bim", real * 3), ("part", ctypes.c_int),
+                    ("pE", P * 3), ("pH", P * 3)]
     return State
 
 
@@ -115,6 +117,8 @@ class Problem:
     # unfolded counts
     mirror: Tuple[int, int, int] = (0, 0, 0)
     full: Tuple[int, int, int] = (0, 0, 0)
+    # Bloch phases per axis: None, or eikna as (re, im) in float64
+    bloch: Tuple[Optional[Tuple[float, float]], ...] = (None, None, None)
 
 
 YEE = {"Dx": (1, 0, 0), "Dy": (0, 1, 0), "Dz": (0, 0, 1),
@@ -221,7 +225,8 @@ def problem_from_driver(driver) -> Problem:
                    monitors=monitors, conductivity=conductivity,
                    faces=tuple(pml.faces) if pml is not None else ((0.0, 0.0),) * 3,
                    mirror=tuple(grid.mirror_phase(a) or 0 for a in range(3)),
-                   full=tuple(grid.shape_full))
+                   full=tuple(grid.shape_full),
+                   bloch=tuple(None if grid.bloch_phase(a) is None else grid.eikna(a) for a in range(3)))
 
 
 class Oracle:
@@ -256,6 +261,21 @@ class Oracle:
         s.metallic[:] = list(problem.metallic)
         s.fold[:] = list(problem.mirror)
         s.full[:] = list(problem.full) if any(problem.mirror) else list(shape)
+        s.part = 1 if part == "imag" else 0
+        s.bloch = 1 if any(b is not None for b in problem.bloch) else 0
+        for a, phase in enumerate(problem.bloch):
+            if phase is None:
+                continue
+            re_, im_ = phase
+            # the library's connection rule: a copy within 1e-13 of +1, a negation of -1
+            if abs(im_) < 1e-13 and abs(re_ - 1.0) < 1e-13:
+                s.bmode[a] = 1
+            elif abs(im_) < 1e-13 and abs(re_ + 1.0) < 1e-13:
+                s.bmode[a] = 2
+            else:
+                s.bmode[a] = 3
+                s.bre[a] = float(np.float32(re_)) if precision == "f32" else re_
+                s.bim[a] = float(np.float32(im_)) if precision == "f32" else im_
         s.dtdx = float(np.float32(problem.dt / problem.dx)) if precision == "f32" else problem.dt / problem.dx
         s.pml = 1 if problem.pml else 0
         tables = problem.tables32 if precision == "f32" else problem.tables64
@@ -320,6 +340,8 @@ class Oracle:
             self.accumulators.append(np.zeros((len(mon.components), mon.omegas.size, 2, cells), dtype=dtype))
         self._step_fn = getattr(self.lib, f"oracle_step_{precision}")
         self._step_fn.argtypes = [P, P]
+        self._half_fn = getattr(self.lib, f"oracle_half_{precision}")
+        self._half_fn.argtypes = [P, P, ctypes.c_int]
         self._dft_fn = getattr(self.lib, f"oracle_dft_{precision}")
         self._dft_fn.argtypes = [P, P, ctypes.c_int, P, ctypes.c_int, P, ctypes.c_double,
                                  ctypes.c_double, ctypes.c_longlong, P]
@@ -329,6 +351,8 @@ class Oracle:
         return array.ctypes.data
 
     def run(self, nsteps: int) -> None:
+        if self.state.bloch:
+            raise RuntimeError("a Bloch-phased run steps its two parts together: use BlochPair")
         nsrc = int(self.problem.src_cells.size)
         words = self.problem.words(self.step_count, nsteps, self.part) if nsrc else None
         empty = np.zeros(1)
@@ -345,6 +369,18 @@ class Oracle:
                 self._dft_fn(ctypes.addressof(self.state), ctypes.addressof(region), len(comps),
                              comps.ctypes.data, omegas.size, omegas.ctypes.data, mon.scale,
                              self.problem.dt, self.step_count, acc.ctypes.data)
+
+    def accumulate(self) -> None:
+        """The monitors' accumulation after a completed step (step_count already advanced)."""
+        for mon, acc in zip(self.problem.monitors, self.accumulators):
+            if self.step_count % mon.decimation:
+                continue
+            region = (ctypes.c_int * 6)(*mon.region)
+            comps = np.array([COMPONENTS.index(c) for c in mon.components], dtype=np.int32)
+            omegas = np.ascontiguousarray(mon.omegas, dtype=np.float64)
+            self._dft_fn(ctypes.addressof(self.state), ctypes.addressof(region), len(comps),
+                         comps.ctypes.data, omegas.size, omegas.ctypes.data, mon.scale,
+                         self.problem.dt, self.step_count, acc.ctypes.data)
 
     def field(self, name: str) -> np.ndarray:
         return self.fields[name]
@@ -387,3 +423,38 @@ def complex_flux_spectrum(real: "Oracle", imag: "Oracle", index: int) -> np.ndar
     ea, eb, ha, hb = total[0], total[1], total[2], total[3]
     w = mon.weights.astype(np.float64)
     return (np.real(ea * np.conj(hb) - eb * np.conj(ha)) @ w) * mon.measure * mon.weight
+
+
+class BlochPair:
+    """A Bloch-phased complex run on the oracle: the real and imaginary parts, each
+    reading the other's E and H across the phased faces, stepped half by half (H of both,
+    then E of both) as the reference's complex run steps (reference ``stepping.py:2544``,
+    ``part_products.py:186``)."""
+
+    def __init__(self, problem: Problem, precision: str = "f32"):
+        self.re = Oracle(problem, precision, "real")
+        self.im = Oracle(problem, precision, "imag")
+        for own, other in ((self.re, self.im), (self.im, self.re)):
+            for q, axis in enumerate("xyz"):
+                own.state.pE[q] = other.fields["E" + axis].ctypes.data
+                own.state.pH[q] = other.fields["H" + axis].ctypes.data
+        self.problem = problem
+        self.step_count = 0
+
+    def run(self, nsteps: int) -> None:
+        nsrc = int(self.problem.src_cells.size)
+        words = {part: (self.problem.words(self.step_count, nsteps, part) if nsrc else None)
+                 for part in ("real", "imag")}
+        empty = np.zeros(1)
+        for t in range(nsteps):
+            rows = {part: (np.ascontiguousarray(words[part][t]) if nsrc else empty) for part in words}
+            for half in (0, 1):
+                for oracle, part in ((self.re, "real"), (self.im, "imag")):
+                    oracle._half_fn(ctypes.addressof(oracle.state), rows[part].ctypes.data, half)
+            self.step_count += 1
+            for oracle in (self.re, self.im):
+                oracle.step_count += 1
+                oracle.accumulate()
+
+    def field(self, name: str) -> np.ndarray:
+        return self.re.field(name) + 1j * self.im.field(name)

@@ -180,19 +180,25 @@ def axis_pieces(n: int, faces: Tuple[float, float]) -> Tuple[Tuple[int, int, int
     return tuple(p for p in pieces if p[1] < p[2])
 
 
-def piece_line(n: int, faces: Tuple[float, float], lattice: int, wraps: bool) -> np.ndarray:
+def piece_line(n: int, faces: Tuple[float, float], lattice: int, wraps: bool,
+               owned: Optional[int] = None) -> np.ndarray:
     """The piece owning each stored row of one sub-lattice (0 integer, 1 half).
 
     A row at doubled offset p belongs to the piece with lo < p <= hi (MEEP's ``owns``).
     The integer row 0 is the wall: on a wrapping axis it is the image of the top wall
-    (p = 2n), on a metallic one it is not owned and takes its neighbour row 1's chunk.
+    (p = 2n), on a metallic or folded one it is not owned and takes its neighbour row 1's
+    chunk. The pieces span MEEP's window, ``owned`` cells (the stored count unless a
+    folded periodic axis stores one row past it, the far ghost slot, which takes the top
+    piece).
     """
-    pieces = axis_pieces(n, faces)
+    owned = n if owned is None else owned
+    pieces = axis_pieces(owned, faces)
     line = np.empty(n, dtype=np.int8)
     for r in range(n):
         p = 2 * r + lattice
         if p == 0:
             p = 2 * n if wraps else 2
+        p = min(p, 2 * owned)
         line[r] = next(piece for piece, lo, hi in pieces if lo < p <= hi)
     return line
 
@@ -206,7 +212,7 @@ def piece_rows(n: int, lo: int, hi: int, wraps: bool) -> np.ndarray:
 
 def keeps_mask(grid: Grid, faces, sigma: np.ndarray) -> int:
     """Bit (x * 9 + y * 3 + z) set for each chunk whose loop volume holds a nonzero sigma."""
-    per_axis = [axis_pieces(grid.shape[a], faces[a]) for a in range(3)]
+    per_axis = [axis_pieces(grid.owned_cells(a), faces[a]) for a in range(3)]
     mask = 0
     nonzero = sigma != 0
     for px, xlo, xhi in per_axis[0]:
@@ -230,11 +236,12 @@ def reaches_a_pml(grid: Grid, faces, volumes: Mapping[str, Optional[np.ndarray]]
         for axis in range(3):
             low, high = faces[axis]
             n = grid.shape[axis]
+            top = grid.owned_cells(axis)  # the high face sits at MEEP's window top
             line = np.zeros(n, dtype=bool)
             if low:
                 line[:min(int(math.ceil(low)) + 1, n)] = True
             if high:
-                line[max(n - int(math.ceil(high)) - 1, 0):] = True
+                line[max(top - int(math.ceil(high)) - 1, 0):] = True
             view = [1, 1, 1]
             view[axis] = n
             inside |= line.reshape(view)

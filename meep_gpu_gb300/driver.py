@@ -235,10 +235,6 @@ class FdtdDriver:
         installed = {}
         installed.update(cond.compose(cond.D_COMPONENTS, self._material_d_conductivity, electric_ramp))
         installed.update(cond.compose(cond.B_COMPONENTS, self._material_b_conductivity, ramp))
-        if any(v is not None for v in installed.values()) and any(
-                self.grid.far_reflect_row(a) is not None for a in range(3)):
-            raise Unsupported("a conductivity in a run that folds a periodic axis is not stepped by "
-                              "this engine (its chunks past the window top)")
         self._conductivity = installed
 
     def _require_existing_sources_clear(self) -> None:

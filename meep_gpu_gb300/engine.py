@@ -323,7 +323,8 @@ class Engine:
         if self.pml is not None:
             for lattice in (INTEGER, HALF):
                 for axis in range(3):
-                    line = piece_line(grid.shape[axis], self.pml.faces[axis], lattice, grid.axis_wraps(axis))
+                    line = piece_line(grid.shape[axis], self.pml.faces[axis], lattice, grid.axis_wraps(axis),
+                                      grid.owned_cells(axis))
                     t = torch.from_numpy(line).to(dev)
                     self.cond_tensors[f"chunk_of.{lattice}.{axis}"] = t
                     cd.chunk_of[lattice][axis] = t.data_ptr()

@@ -119,13 +119,17 @@ class Problem:
     full: Tuple[int, int, int] = (0, 0, 0)
     # Bloch phases per axis: None, or eikna as (re, im) in float64
     bloch: Tuple[Optional[Tuple[float, float]], ...] = (None, None, None)
+    # MEEP's window per axis in cells, and whether each axis wraps (None: the stored
+    # counts, and every non-metallic axis)
+    owned: Optional[Tuple[int, int, int]] = None
+    wraps: Optional[Tuple[bool, bool, bool]] = None
 
 
 YEE = {"Dx": (1, 0, 0), "Dy": (0, 1, 0), "Dz": (0, 0, 1),
        "Bx": (0, 1, 1), "By": (1, 0, 1), "Bz": (1, 1, 0)}
 
 
-def keeps_volume(shape, metallic, faces, iyee, sigma: np.ndarray) -> np.ndarray:
+def keeps_volume(shape, metallic, faces, iyee, sigma: np.ndarray, owned=None, wraps=None) -> np.ndarray:
     """Per cell of one component lattice: does the one-rank chunk owning it keep a
     conductivity array? (meep_gpu/chunk_map.py ``ChunkLayout.one_rank`` :384,
     ``owner_volume`` :649, ``loop_rows`` :675, ``conductive_chunks`` :720.)
@@ -135,21 +139,27 @@ def keeps_volume(shape, metallic, faces, iyee, sigma: np.ndarray) -> np.ndarray:
     array when any sample of its loop volume (doubled lo + shift .. hi + shift) is
     nonzero; a cell belongs to the chunk whose box holds its doubled coordinate
     (lo < p <= hi), a wall row that no chunk owns taking its nearest owned row's.
+    ``owned``: MEEP's window per axis in cells (the stored count but on a folded periodic
+    axis, which stores one row past it); ``wraps``: whether the axis wraps (default: not
+    metallic).
     """
+    owned = tuple(shape) if owned is None else tuple(owned)
+    wraps = tuple(not m for m in metallic) if wraps is None else tuple(wraps)
     boxes, coords = [], []
     for axis in range(3):
         n = shape[axis]
+        w = owned[axis]
         low, high = faces[axis]
-        cut_lo = 2 * min(n, int(low + 1.5)) if low > 0 else 0
-        cut_hi = 2 * n - 2 * min(n, int(high + 1.5)) if high > 0 else 2 * n
-        edges = [(0, cut_lo), (cut_lo, cut_hi), (cut_hi, 2 * n)]
+        cut_lo = 2 * min(w, int(low + 1.5)) if low > 0 else 0
+        cut_hi = 2 * w - 2 * min(w, int(high + 1.5)) if high > 0 else 2 * w
+        edges = [(0, cut_lo), (cut_lo, cut_hi), (cut_hi, 2 * w)]
         boxes.append([e for e in edges if e[0] < e[1]])
         p = 2 * np.arange(n) + iyee[axis]
-        if not metallic[axis]:
+        if wraps[axis]:
             p = np.where(p <= 0, p + 2 * n, p)
-        owned = (p > 0) & (p <= 2 * n)
-        owned_at = np.flatnonzero(owned)
-        for row in np.flatnonzero(~owned):
+        inside = (p > 0) & (p <= 2 * w)
+        owned_at = np.flatnonzero(inside)
+        for row in np.flatnonzero(~inside):
             p[row] = p[owned_at[np.argmin(np.abs(owned_at - row))]]
         coords.append(p)
     out = np.zeros(shape, dtype=bool)
@@ -160,7 +170,7 @@ def keeps_volume(shape, metallic, faces, iyee, sigma: np.ndarray) -> np.ndarray:
                 for axis, (lo, hi) in enumerate((bx, by, bz)):
                     n = shape[axis]
                     r = np.arange(lo // 2, hi // 2 + 1)
-                    rows.append(r % n if not metallic[axis] else np.clip(r, 0, n - 1))
+                    rows.append(r % n if wraps[axis] else np.clip(r, 0, n - 1))
                 if not np.any(sigma[np.ix_(*rows)] != 0):
                     continue
                 sel = [(c > lo) & (c <= hi) for c, (lo, hi) in zip(coords, (bx, by, bz))]
@@ -226,7 +236,9 @@ def problem_from_driver(driver) -> Problem:
                    faces=tuple(pml.faces) if pml is not None else ((0.0, 0.0),) * 3,
                    mirror=tuple(grid.mirror_phase(a) or 0 for a in range(3)),
                    full=tuple(grid.shape_full),
-                   bloch=tuple(None if grid.bloch_phase(a) is None else grid.eikna(a) for a in range(3)))
+                   bloch=tuple(None if grid.bloch_phase(a) is None else grid.eikna(a) for a in range(3)),
+                   owned=tuple(grid.owned_cells(a) for a in range(3)),
+                   wraps=tuple(grid.axis_wraps(a) for a in range(3)))
 
 
 class Oracle:
@@ -328,7 +340,8 @@ class Oracle:
             s.condfac[side][q] = self._ptr(np.ascontiguousarray(fac, dtype=dtype))
             s.condinv[side][q] = self._ptr(np.ascontiguousarray(inv, dtype=dtype))
             if problem.pml:
-                keeps = keeps_volume(shape, problem.metallic, problem.faces, YEE[name], sigma)
+                keeps = keeps_volume(shape, problem.metallic, problem.faces, YEE[name], sigma,
+                                     problem.owned, problem.wraps)
                 s.keeps[side][q] = self._ptr(np.ascontiguousarray(keeps, dtype=np.uint8))
                 self.fcond[name] = z()
                 s.fcond[side][q] = self.fcond[name].ctypes.data

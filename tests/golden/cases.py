@@ -77,6 +77,11 @@ CASES = {
     "mirror_periodic_pml": dict(n=(16, 12, 13), pml={"z": {"high": 3}, "x": 2}, steps=50,
                                 symmetry=(("Z", -1),), boundaries=("metallic", "periodic", "periodic"),
                                 mirror_sources=True),
+    # A conductivity under a PML on a folded periodic axis (its chunks cut MEEP's window,
+    # the far ghost slot taking the top one).
+    "mirror_periodic_lossy": dict(n=(14, 16, 12), pml={"y": {"high": 3}, "x": 2}, steps=50,
+                                  symmetry=(("Y", 1),), boundaries=("metallic", "periodic", "metallic"),
+                                  mirror_sources=True, conductivity="band"),
 }
 
 # The 80^3 sphere-under-PML workload (resolution 10, 10-cell PML, eps 4 sphere of radius

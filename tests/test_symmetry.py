@@ -44,10 +44,6 @@ def test_folded_counts_origin_and_coordinates():
 
 
 def test_folds_that_are_not_stepped_are_refused():
-    d = FdtdDriver((1.4, 1.4, 1.4), 10, force_complex_fields=False, boundaries="periodic",
-                   symmetry=("X",))
-    with pytest.raises(Unsupported, match="periodic"):
-        d.set_conductivity(0.1)
     with pytest.raises(Unsupported, match="k_point"):
         Grid((2.0, 2.0, 2.0), 10, boundaries=("metallic", "periodic", "periodic"),
              k_point=(0, 0.2, 0), symmetry=("X",))

@@ -28,7 +28,7 @@ import numpy as np
 
 from . import conductivity as cond
 from .conductivity import AbsorberLayer
-from .dft import (DFTMonitor, FluxMonitor, absorbing_cells, automatic_decimation,
+from .dft import (DFTMonitor, FluxMonitor, absorbing_cells, automatic_decimation, folded_site,
                   normalize_frequencies)
 from .dispersion import Susceptibility
 from .grid import AXIS_NAMES, IYEE, Grid, Unsupported
@@ -500,7 +500,19 @@ class FdtdDriver:
         for axis in axes:
             pad = [(0, 0)] * 3
             pad[axis] = (0, 1)
-            if self.grid.is_metallic(axis):
+            if self.grid.is_mirrored(axis):
+                # one past the stored rows of a folded axis: the metallic wall's zero, or on
+                # a periodic fold the image about the second mirror (dft.folded_site)
+                site = folded_site(self.grid, axis, 0, self.grid.shape[axis])
+                if isinstance(site, tuple):
+                    row, flipped = site
+                    image = np.take(padded, [row], axis=axis)
+                    if flipped:
+                        image = image * self.grid.parity(component, axis)
+                    padded = np.concatenate([padded, image.astype(padded.dtype)], axis=axis)
+                else:
+                    padded = np.pad(padded, pad)
+            elif self.grid.is_metallic(axis):
                 padded = np.pad(padded, pad)
             else:
                 padded = np.pad(padded, pad, mode="wrap")

@@ -258,3 +258,34 @@ def test_the_batch_refuses_a_folded_plan(gpu):
     assert "mirror" in _lib.last_error(lib) or "magnetic" in _lib.last_error(lib)
     lib.mgb_batch_destroy(handle)
     driver.close()
+
+
+def test_cell_centred_read_takes_the_image_past_a_periodic_fold():
+    """The centred value on the last stored row of a folded periodic axis averages with
+    the word one past it: its image about the second mirror, with the parity."""
+    import torch
+
+    d = FdtdDriver((1.4, 1.2, 1.2), 10, force_complex_fields=False, boundaries="periodic",
+                   symmetry=(Mirror("X", -1),))
+    rng = np.random.default_rng(3)
+    words = {c: torch.from_numpy(rng.standard_normal(d.grid.shape).astype(np.float32))
+             for c in ("Ex", "Ey", "Hx")}
+
+    class Stub:
+        def field(self, name):
+            return words[name]
+
+    d.engine = Stub()
+    n = d.grid.shape[0]
+    row = d.grid.far_reflect_row(0)
+    hx = words["Hx"].numpy()
+    # Hx has Yee shift 0 on x alone: the word past the top row n-1 sits at doubled
+    # -2 + 2n, whose image about the second mirror is the far reflect row (reference
+    # stepping.py:2361)
+    from meep_gpu_gb300.dft import folded_site
+    assert folded_site(d.grid, 0, 0, n) == (row, True)
+    centred = d.get_field("Hx")
+    sign = d.grid.parity("Hx", 0)
+    expected_top = np.float32(0.5) * (hx[n - 1] + np.float32(sign) * hx[row])
+    assert np.array_equal(centred[n - 1], expected_top)
+    d.engine = None

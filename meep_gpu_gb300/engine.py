@@ -813,10 +813,9 @@ class ComplexEngine:
         self.re.write_accumulator(monitor, q, values)
         self.im.write_accumulator(monitor, q, None)
 
-    def flux_spectrum(self, monitor: FluxMonitor) -> np.ndarray:
-        """``sum w * Re(Ea conj(Hb) - Eb conj(Ha)) * dA * weight`` of the complex transforms,
-        summed in float64 on the device."""
-        self.flush_dft()
+    def _device_flux(self, monitor: FluxMonitor) -> torch.Tensor:
+        """``sum w * Re(Ea conj(Hb) - Eb conj(Ha)) * dA`` of the complex transforms, summed
+        in float64 on the device (the current stream)."""
         index = self.monitors.index(monitor)
         parts = []
         for engine in (self.re, self.im):
@@ -825,8 +824,25 @@ class ComplexEngine:
         total = parts[0] + 1j * parts[1]
         ea, eb, ha, hb = total[0], total[1], total[2], total[3]
         weights = self.re.monitor_tensors[index][2].to(torch.float64)
-        flux = torch.real(ea * torch.conj(hb) - eb * torch.conj(ha)) @ weights
-        return flux.cpu().numpy() * monitor.measure * monitor.weight
+        return torch.real(ea * torch.conj(hb) - eb * torch.conj(ha)) @ weights
+
+    def flux_spectrum(self, monitor: FluxMonitor) -> np.ndarray:
+        self.flush_dft()
+        return self._device_flux(monitor).cpu().numpy() * monitor.measure * monitor.weight
+
+    def queue_flux_spectrum(self, monitor: FluxMonitor):
+        """The complex flux reduction and its read-back into pinned host memory, queued on
+        the engines' stream; returns ``(host, event)`` as ``Engine.queue_flux_spectrum``."""
+        stream = self.re.stream if self.re.stream is not None else torch.cuda.current_stream(self.device)
+        with torch.cuda.stream(stream):
+            for engine in (self.re, self.im):
+                _lib.check(self.lib, self.lib.mgb_dft_flush(engine.handle, stream.cuda_stream))
+            flux = self._device_flux(monitor)
+            host = torch.empty(monitor.num_frequencies, dtype=torch.float64, pin_memory=True)
+            host.copy_(flux, non_blocking=True)
+            event = torch.cuda.Event()
+            event.record(stream)
+        return host, event
 
     def field(self, name: str) -> torch.Tensor:
         return torch.complex(self.re.field(name), self.im.field(name))

@@ -106,7 +106,8 @@ def footprint_bytes(driver) -> int:
     for monitor in list(driver._flux_monitors) + list(driver._dft_monitors):
         total += 4 * len(monitor.components) * monitor.num_frequencies * 2 * monitor.cells
     total += 8 * sum(len(s.cells) for s in driver._sources) * 4096
-    return total
+    # a complex run keeps two parts (the material tables are shared, counted twice here)
+    return 2 * total if driver.complex_fields else total
 
 
 @dataclass
@@ -117,6 +118,13 @@ class _Job:
     bytes: int
     slot: int = -1
     engine: object = None
+    slots: Tuple[int, ...] = ()  # every slot the job holds (two for a complex run)
+
+    @property
+    def slots_needed(self) -> int:
+        """Slots the job steps in: one, or two for complex fields (its real and imaginary
+        parts, which at k = 0 step independently)."""
+        return 2 if getattr(self.driver, "complex_fields", False) else 1
     words: Optional[torch.Tensor] = None
     admitted: float = 0.0
     readback: object = None  # (pinned host spectrum, event) once its reduction is queued
@@ -258,32 +266,47 @@ class BatchServer:
     # --- slots --------------------------------------------------------------------------
     @property
     def active(self) -> int:
+        """Slots in use (a complex job holds two)."""
         return sum(job is not None for job in self.slots)
 
-    def fits(self, nbytes: int) -> bool:
-        """A free slot, and room in the HBM budget (slots still draining count)."""
-        return (self.active < self.max_slots
+    def fits(self, nbytes: int, slots: int = 1) -> bool:
+        """Free slots, and room in the HBM budget (slots still draining count)."""
+        return (self.active + slots <= self.max_slots
                 and (self.resident_bytes == 0 or self.resident_bytes + nbytes <= self.budget_bytes))
 
     def admit(self, job: _Job, now: float) -> None:
-        """Make a job's device state (on the setup stream) and put it in a free slot."""
-        slot = self.slots.index(None)
-        if job.driver.complex_fields:
-            raise Unsupported("a batched slot steps real fields (force_complex_fields=False)")
+        """Make a job's device state (on the setup stream) and put it in free slots: one,
+        or for complex fields (k = 0) two, its real and imaginary parts, each driven by
+        its part of the currents; the spectrum combines the two parts' transforms."""
+        if job.driver.grid.has_bloch:
+            raise Unsupported("a batched slot does not carry Bloch phases (its two parts meet across "
+                              "the phased faces)")
         if job.driver.grid.has_symmetry:
             raise Unsupported("a batched slot does not carry mirror symmetry")
+        free = [i for i, held in enumerate(self.slots) if held is None]
+        if len(free) < job.slots_needed:
+            raise RuntimeError("admit() needs free slots: check fits() first")
         with torch.cuda.stream(self.setup_stream):
             # the batch accumulates its monitors step by step (dft_batched)
             job.engine = job.driver.freeze(stream=self.stream, autotune=False, dft_accumulation="direct")
-            if job.driver.sources:
-                host = deposit_words(job.driver.sources, 0, job.request.steps, job.driver.grid.dt)
-                job.words = torch.from_numpy(host).to(self.device)
-        words = job.words.data_ptr() if job.words is not None else None
-        _lib.check(self.lib, self.lib.mgb_batch_set_slot(self.handle, slot, job.engine.handle,
-                                                         job.request.steps, words))
-        job.slot = slot
+            plans = [job.engine.re, job.engine.im] if job.slots_needed == 2 else [job.engine]
+            words = []
+            for plan, part in zip(plans, ("real", "imag")):
+                if job.driver.sources:
+                    host = deposit_words(job.driver.sources, 0, job.request.steps, job.driver.grid.dt,
+                                         part=part)
+                    words.append(torch.from_numpy(host).to(self.device))
+                else:
+                    words.append(None)
+        job.words = words
+        for slot, plan, table in zip(free, plans, words):
+            _lib.check(self.lib, self.lib.mgb_batch_set_slot(
+                self.handle, slot, plan.handle, job.request.steps,
+                table.data_ptr() if table is not None else None))
+            self.slots[slot] = job
+        job.slots = tuple(free[:len(plans)])
+        job.slot = job.slots[0]
         job.admitted = now
-        self.slots[slot] = job
         self.resident_bytes += job.bytes
 
     def commit(self) -> None:
@@ -315,11 +338,12 @@ class BatchServer:
         steps = self.steps()
         count = 0
         for slot, job in enumerate(self.slots):
-            if job is None or steps[slot] < job.request.steps:
+            if job is None or slot != job.slot or any(steps[s] < job.request.steps for s in job.slots):
                 continue
             job.readback = job.engine.queue_flux_spectrum(job.flux)
-            _lib.check(self.lib, self.lib.mgb_batch_clear_slot(self.handle, slot))
-            self.slots[slot] = None
+            for held in job.slots:
+                _lib.check(self.lib, self.lib.mgb_batch_clear_slot(self.handle, held))
+                self.slots[held] = None
             self.draining.append(job)
             count += 1
         return count
@@ -421,7 +445,7 @@ def serve(server: BatchServer, requests: Sequence[Request], realtime: bool = Tru
             if server.active >= server.max_slots:
                 break
             job = job_for(request)
-            if server.fits(job.bytes):
+            if server.fits(job.bytes, job.slots_needed):
                 server.admit(job, now())
                 waiting.remove(request)
             else:

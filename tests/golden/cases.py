@@ -48,6 +48,9 @@ CASES = {
                           boundaries=("metallic", "periodic", "metallic")),
     "complex_cond": dict(n=(14, 12, 16), pml=3, steps=50, conductivity="band", magnetic=True,
                          complex=True),
+    # Complex fields on the sphere case (a complex source amplitude): the case the serving
+    # batch's complex slots are checked on (at most two monitors).
+    "complex_sphere": dict(n=(14, 12, 16), pml=3, steps=60, complex=True, complex_amplitude=True),
     # Bloch-periodic fields (complex, k != 0): phased x and y with an interior point
     # source, a DFT volume and a flux plane spanning the whole y-z cross-section; and
     # a phased x axis under a z PML with a line source wrapping the phased axis, odd
@@ -146,7 +149,8 @@ def build_case(driver_cls, susceptibility_cls, case: dict, reference: bool = Fal
     else:
         d.add_source({"source_type": "gaussian", "component": "Ez",
                       "center": (source_x, 0.03, 0.0), "size": (0, 0, 0),
-                      "frequency": fcen, "fwidth": fwidth})
+                      "frequency": fcen, "fwidth": fwidth,
+                      "amplitude": (0.6 - 0.8j) if case.get("complex_amplitude") else 1.0})
     if case.get("bloch_line"):
         d.add_source({"source_type": "gaussian", "component": "Ey", "center": (0.0, -0.1, 0.1),
                       "size": (lengths[0], 0, 0), "frequency": fcen, "fwidth": fwidth,

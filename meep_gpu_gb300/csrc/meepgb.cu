@@ -2557,6 +2557,10 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
   if (d.nx < 2 || d.ny < 2 || d.nz < 2) {
     return fail(MGB_ERR_UNSUPPORTED, "every axis needs at least 2 cells (reduced-dimension runs are refused)");
   }
+  // the step kernels index a volume with 32-bit cell offsets
+  if ((long long)d.nx * d.ny * d.nz >= (1LL << 31)) {
+    return fail(MGB_ERR_UNSUPPORTED, "a grid of 2^31 cells or more is not stepped (32-bit cell offsets)");
+  }
   const int n[3] = {d.nx, d.ny, d.nz};
   for (int q = 0; q < 3; ++q) {
     if (d.E[q] == nullptr || d.D[q] == nullptr || d.H[q] == nullptr || d.inv_eps[q] == nullptr) {

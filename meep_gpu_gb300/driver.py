@@ -380,6 +380,9 @@ class FdtdDriver:
         import torch
 
         from .engine import ComplexEngine, Engine
+        if self.grid.total_cells >= 1 << 31:
+            raise Unsupported(f"a grid of {self.grid.total_cells} cells (2^31 or more) is not stepped by "
+                              "this engine (32-bit cell offsets)")
         self.prepare()
         device = torch.device("cuda", self.gpu_id)
         engine_cls = ComplexEngine if self.complex_fields else Engine

@@ -40,6 +40,9 @@ def test_create_refuses_bad_descriptors_without_a_gpu():
     desc.nx, desc.ny, desc.nz = 1, 8, 8
     assert lib.mgb_create(ctypes.byref(desc), ctypes.byref(handle)) == -3
     assert "at least 2 cells" in _lib.last_error(lib)
+    desc.nx, desc.ny, desc.nz = 1300, 1300, 1300  # 2.2e9 cells: past 32-bit offsets
+    assert lib.mgb_create(ctypes.byref(desc), ctypes.byref(handle)) == -3
+    assert "2^31" in _lib.last_error(lib)
 
 
 def test_batch_entry_points_refuse_bad_arguments_without_a_gpu():

@@ -1925,6 +1925,19 @@ __global__ void __launch_bounds__(256, GEN ? 5 : 4) step_batched(const __grid_co
   const int i1 = min(i0 + tb.xchunk, sp.nx);
   const int axes = sp.pml ? cta_axes(sp, i0, i1, w.z * (int)blockDim.y, (int)blockDim.y,
                                       w.y * (int)blockDim.x, (int)blockDim.x) : 0;
+  // a Bloch-phased slot (one part of a complex run, its other part in another slot of the
+  // same batch step): the CTAs at index 0 of a phased axis read the other part there
+  if (cta_bloch(sp, i0, w.z * (int)blockDim.y, w.y * (int)blockDim.x)) {
+    if (PART == 0) {
+      if (sp.pml) h_march<true, false, -1, false, true>(sp, j, k, i0, i1, n == 0);
+      else h_march<false, false, -1, false, true>(sp, j, k, i0, i1, n == 0);
+    } else {
+      const double* words = st.words + n * sp.nsrc;
+      if (sp.pml) e_march<true, false, -1, true>(sp, j, k, i0, i1, (int)(n & 1), words);
+      else e_march<false, false, -1, true>(sp, j, k, i0, i1, (int)(n & 1), words);
+    }
+    return;
+  }
   if (PART == 0) {
     const int first = n == 0;
     if (GEN) {
@@ -3436,7 +3449,6 @@ int mgb_batch_set_slot(mgb_batch* b, int32_t slot, mgb_sim* sim, int64_t end_ste
   if (sim->step.nsrc > 0 && words == nullptr) return fail(MGB_ERR_ARGUMENT, "the slot's sources need deposit words");
   if (sim->has_cond) return fail(MGB_ERR_UNSUPPORTED, "a batched slot does not carry a conductivity");
   if (sim->step.nsrc_h > 0) return fail(MGB_ERR_UNSUPPORTED, "a batched slot does not carry magnetic sources");
-  if (sim->step.bloch) return fail(MGB_ERR_UNSUPPORTED, "a batched slot does not carry Bloch phases");
   if (sim->folded) return fail(MGB_ERR_UNSUPPORTED, "a batched slot does not carry mirror folds");
   if (sim->desc.nmonitors > kSlotMonitors)
     return fail(MGB_ERR_UNSUPPORTED, "a batched slot holds at most " + std::to_string(kSlotMonitors) + " monitors");
@@ -3462,6 +3474,12 @@ int mgb_batch_set_slot(mgb_batch* b, int32_t slot, mgb_sim* sim, int64_t end_ste
     for (int a = 0; a < 3; ++a) q.met[a] = sim->step.met[a];
     for (int c = 0; c < 3; ++c) { q.E[c] = sim->step.E[c]; q.H[c] = sim->step.H[c]; }
     q.mon = sim->desc.monitors[m];
+    q.bloch = sim->step.bloch;
+    q.part = sim->step.part;
+    for (int a = 0; a < 3; ++a) {
+      q.bmode[a] = sim->step.bmode[a]; q.bre[a] = sim->step.bre[a]; q.bim[a] = sim->step.bim[a];
+      q.pE[a] = sim->step.pE[a]; q.pH[a] = sim->step.pH[a];
+    }
   }
   b->dirty[slot] = 1;
   b->work_dirty = true;

@@ -276,11 +276,10 @@ class BatchServer:
 
     def admit(self, job: _Job, now: float) -> None:
         """Make a job's device state (on the setup stream) and put it in free slots: one,
-        or for complex fields (k = 0) two, its real and imaginary parts, each driven by
-        its part of the currents; the spectrum combines the two parts' transforms."""
-        if job.driver.grid.has_bloch:
-            raise Unsupported("a batched slot does not carry Bloch phases (its two parts meet across "
-                              "the phased faces)")
+        or for complex fields two, its real and imaginary parts, each driven by its part
+        of the currents (with a Bloch phase the two read each other across the phased
+        faces, which a batch step allows: every slot's H half, then every slot's E half);
+        the spectrum combines the two parts' transforms."""
         if job.driver.grid.has_symmetry:
             raise Unsupported("a batched slot does not carry mirror symmetry")
         free = [i for i, held in enumerate(self.slots) if held is None]

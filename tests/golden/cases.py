@@ -51,6 +51,10 @@ CASES = {
     # Complex fields on the sphere case (a complex source amplitude): the case the serving
     # batch's complex slots are checked on (at most two monitors).
     "complex_sphere": dict(n=(14, 12, 16), pml=3, steps=60, complex=True, complex_amplitude=True),
+    # The sphere case on a Bloch lattice (periodic x and y, k = (0.3, -0.2, 0), a z PML):
+    # the case the serving batch's Bloch slots are checked on (one monitor).
+    "bloch_sphere": dict(n=(14, 12, 16), pml={"z": 3}, steps=60, complex=True, boundaries=("periodic", "periodic", "metallic"),
+                         k_point=(0.3, -0.2, 0.0)),
     # Bloch-periodic fields (complex, k != 0): phased x and y with an interior point
     # source, a DFT volume and a flux plane spanning the whole y-z cross-section; and
     # a phased x axis under a z PML with a line source wrapping the phased axis, odd

@@ -1905,6 +1905,20 @@ __device__ __forceinline__ void copy_to_shared(T* dst, const T* src) {
 // GEN false: the prefetching marches (family 2, 64 registers); true: the generic marches
 // with each item's x chunk prefetched into L2 (family 4, 48 registers). `t` is the
 // launch's step within the batch step call.
+// The phased march of a batched Bloch slot's CTA (one half of step n).
+template <int PART>
+__device__ __noinline__ void batched_bloch_march(const StepParams& sp, int j, int k, int i0, int i1, long long n,
+                                                 const double* slot_words) {
+  if (PART == 0) {
+    if (sp.pml) h_march<true, false, -1, false, true>(sp, j, k, i0, i1, n == 0);
+    else h_march<false, false, -1, false, true>(sp, j, k, i0, i1, n == 0);
+  } else {
+    const double* words = slot_words + n * sp.nsrc;
+    if (sp.pml) e_march<true, false, -1, true>(sp, j, k, i0, i1, (int)(n & 1), words);
+    else e_march<false, false, -1, true>(sp, j, k, i0, i1, (int)(n & 1), words);
+  }
+}
+
 template <int PART, bool GEN>
 __global__ void __launch_bounds__(256, GEN ? 5 : 4) step_batched(const __grid_constant__ BatchTables tb, int t) {
   __shared__ StepParams sp;
@@ -1927,15 +1941,9 @@ __global__ void __launch_bounds__(256, GEN ? 5 : 4) step_batched(const __grid_co
                                       w.y * (int)blockDim.x, (int)blockDim.x) : 0;
   // a Bloch-phased slot (one part of a complex run, its other part in another slot of the
   // same batch step): the CTAs at index 0 of a phased axis read the other part there
+  // (out of line, so the other marches keep their register allocation)
   if (cta_bloch(sp, i0, w.z * (int)blockDim.y, w.y * (int)blockDim.x)) {
-    if (PART == 0) {
-      if (sp.pml) h_march<true, false, -1, false, true>(sp, j, k, i0, i1, n == 0);
-      else h_march<false, false, -1, false, true>(sp, j, k, i0, i1, n == 0);
-    } else {
-      const double* words = st.words + n * sp.nsrc;
-      if (sp.pml) e_march<true, false, -1, true>(sp, j, k, i0, i1, (int)(n & 1), words);
-      else e_march<false, false, -1, true>(sp, j, k, i0, i1, (int)(n & 1), words);
-    }
+    batched_bloch_march<PART>(sp, j, k, i0, i1, n, st.words);
     return;
   }
   if (PART == 0) {

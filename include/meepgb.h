@@ -170,7 +170,7 @@ typedef struct mgb_sim_desc {
    * batch and the adjoint entry points. */
   const mgb_conductivity* conductivity;
   /* magnetic source points: the last nsrc_magnetic of the nsrc, and their bounding box
-   * (half-open). A run with magnetic sources is refused by the batch. */
+   * (half-open). */
   int32_t nsrc_magnetic;
   int32_t src_box_magnetic[6];
   /* Bloch-periodic complex runs (k_point != 0): a complex run is two plans, one over the
@@ -397,9 +397,11 @@ int mgb_batch_set_shape(mgb_batch* batch, int32_t block_z, int32_t block_y, int3
 int mgb_batch_set_family(mgb_batch* batch, int32_t family);
 
 /* Put a plan in a slot, to run steps 0 .. end_step-1 from its arrays' current words
- * (normally zero). words: device float64 [end_step][points] deposit words of its electric
- * sources from step 0 (NULL if it has none); the plan's own mgb_set_source_words table is
- * not used. At most 2 monitors of at most 512 frequencies. Takes effect at the next
+ * (normally zero). words: device float64 [end_step][points] deposit words of its sources
+ * (electric and magnetic points, the plan's order) from step 0 (NULL if it has none); the
+ * plan's own mgb_set_source_words table is not used. At most 2 monitors of at most 512
+ * frequencies. The two parts of a Bloch-phased complex run go in two slots of the same
+ * batch. Refused: a conductivity, mirror folds. Takes effect at the next
  * mgb_batch_commit; the plan and its arrays must outlive the slot's last queued step. */
 int mgb_batch_set_slot(mgb_batch* batch, int32_t slot, mgb_sim* sim, int64_t end_step,
                        const double* words);

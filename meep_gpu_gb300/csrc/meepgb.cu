@@ -1910,13 +1910,20 @@ template <int PART>
 __device__ __noinline__ void batched_bloch_march(const StepParams& sp, int j, int k, int i0, int i1, long long n,
                                                  const double* slot_words) {
   if (PART == 0) {
-    if (sp.pml) h_march<true, false, -1, false, true>(sp, j, k, i0, i1, n == 0);
-    else h_march<false, false, -1, false, true>(sp, j, k, i0, i1, n == 0);
+    if (sp.pml) h_march<true, false, -1, true, true>(sp, j, k, i0, i1, n == 0);
+    else h_march<false, false, -1, true, true>(sp, j, k, i0, i1, n == 0);
   } else {
     const double* words = slot_words + n * sp.nsrc;
     if (sp.pml) e_march<true, false, -1, true>(sp, j, k, i0, i1, (int)(n & 1), words);
     else e_march<false, false, -1, true>(sp, j, k, i0, i1, (int)(n & 1), words);
   }
+}
+
+// The H march of a batched slot's CTA that holds magnetic source points (step n's row of
+// the slot's words is in the shared parameters).
+__device__ __noinline__ void batched_msrc_march(const StepParams& sp, int j, int k, int i0, int i1, long long n) {
+  if (sp.pml) h_march<true, false, -1, true>(sp, j, k, i0, i1, n == 0);
+  else h_march<false, false, -1, true>(sp, j, k, i0, i1, n == 0);
 }
 
 template <int PART, bool GEN>
@@ -1930,7 +1937,10 @@ __global__ void __launch_bounds__(256, GEN ? 5 : 4) step_batched(const __grid_co
   const long long n = tb.n0[w.x] + t;
   if (!st.active || n >= st.end) return;  // uniform over the CTA
   __syncthreads();
-  if (threadIdx.x == 0 && threadIdx.y == 0) sp.l2pf = GEN ? 1 : 0;
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    sp.l2pf = GEN ? 1 : 0;
+    sp.src_words = st.words != nullptr ? st.words + n * sp.nsrc : nullptr;  // step n's row
+  }
   __syncthreads();
   const int k = w.y * (int)blockDim.x + (int)threadIdx.x;
   const int j = w.z * (int)blockDim.y + (int)threadIdx.y;
@@ -1944,6 +1954,12 @@ __global__ void __launch_bounds__(256, GEN ? 5 : 4) step_batched(const __grid_co
   // (out of line, so the other marches keep their register allocation)
   if (cta_bloch(sp, i0, w.z * (int)blockDim.y, w.y * (int)blockDim.x)) {
     batched_bloch_march<PART>(sp, j, k, i0, i1, n, st.words);
+    return;
+  }
+  // a slot with magnetic sources: the CTAs that hold its magnetic points deposit them
+  if (PART == 0 && cta_msrc(sp, i0, i1, w.z * (int)blockDim.y, (int)blockDim.y, w.y * (int)blockDim.x,
+                            (int)blockDim.x)) {
+    batched_msrc_march(sp, j, k, i0, i1, n);
     return;
   }
   if (PART == 0) {
@@ -3456,7 +3472,6 @@ int mgb_batch_set_slot(mgb_batch* b, int32_t slot, mgb_sim* sim, int64_t end_ste
   if (end_step < 1) return fail(MGB_ERR_ARGUMENT, "a slot needs at least one step");
   if (sim->step.nsrc > 0 && words == nullptr) return fail(MGB_ERR_ARGUMENT, "the slot's sources need deposit words");
   if (sim->has_cond) return fail(MGB_ERR_UNSUPPORTED, "a batched slot does not carry a conductivity");
-  if (sim->step.nsrc_h > 0) return fail(MGB_ERR_UNSUPPORTED, "a batched slot does not carry magnetic sources");
   if (sim->folded) return fail(MGB_ERR_UNSUPPORTED, "a batched slot does not carry mirror folds");
   if (sim->desc.nmonitors > kSlotMonitors)
     return fail(MGB_ERR_UNSUPPORTED, "a batched slot holds at most " + std::to_string(kSlotMonitors) + " monitors");

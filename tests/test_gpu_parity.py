@@ -191,24 +191,3 @@ def test_nonfinite_detector_raises(gpu):
     with pytest.raises(FdtdDivergence):
         driver.run(num_steps=40, progress_interval=10)
     driver.close()
-
-
-def test_batch_refuses_magnetic_sources(gpu):
-    import ctypes
-
-    import torch
-
-    from meep_gpu_gb300 import _lib
-
-    driver, _, _ = build_case(FdtdDriver, Susceptibility, CASES["magnetic"])
-    engine = driver.freeze(autotune=False)
-    lib = engine.lib
-    nbytes = lib.mgb_batch_bytes(2, 64, 64)
-    buf = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
-    handle = ctypes.c_void_p()
-    _lib.check(lib, lib.mgb_batch_create(2, 64, 64, buf.data_ptr(), nbytes, ctypes.byref(handle)))
-    engine.ensure_source_words(0, 10)
-    assert lib.mgb_batch_set_slot(handle, 0, engine.handle, 10, engine._words.data_ptr()) == -3
-    assert "magnetic" in _lib.last_error(lib)
-    lib.mgb_batch_destroy(handle)
-    driver.close()

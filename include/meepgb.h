@@ -210,6 +210,16 @@ int mgb_step_pair(mgb_sim* real, mgb_sim* imag, int64_t first_step, int32_t nste
 /* Version of this ABI (MGB_ABI_VERSION). */
 int mgb_abi_version(void);
 
+/* Test hook: the limit, in nanoseconds, of the FIRST bounded wait of later launches of the
+ * TMA tile kernels (which = 0: their first shared-memory stage; family 1) or of the
+ * tensor-core contraction (which = 1: its first phase tile's MMAs); 0 makes that wait give
+ * up at once, a negative value restores the normal limit (the default). A wait that runs
+ * out sets its status bit (2 for the tile kernels in the plan's status word, 4 for the
+ * contraction) and the kernel leaves; every later wait, including the one that lets the
+ * kernel's own copies or MMAs finish before it exits or frees tensor memory, keeps its
+ * normal bound. Process-wide. No reference counterpart. */
+int mgb_set_test_wait_limit(int32_t which, int64_t nanoseconds);
+
 /* Validate a descriptor and make a plan from a copy of it. Replaces plan_fast_path
  * (meep_gpu/fastpath.py:6986); refusals return MGB_ERR_UNSUPPORTED with the reason. */
 int mgb_create(const mgb_sim_desc* desc, mgb_sim** out);
@@ -245,6 +255,13 @@ int mgb_launch(mgb_sim* sim, int64_t step, int32_t part, void* stream);
  * (meep_gpu/dft.py:3107) without the dA * weight scale, which the host applies. */
 int mgb_flux_spectrum(mgb_sim* sim, int32_t monitor, const float* weights, double* out,
                       void* stream);
+
+/* Add the field energy sum |E|^2 eps + |B|^2 over the grid (eps = 1 / inv_eps of each E
+ * component; B the stored B word on each H component's own-axis membership, H's word
+ * elsewhere) to *out (device double), in float64, on `stream`. Replaces
+ * FdtdDriver._field_energy (meep_gpu/driver.py:3634), the scalar of the divergence guard
+ * _DivergenceGuard (driver.py:747-792). Asynchronous. */
+int mgb_field_energy(mgb_sim* sim, double* out, void* stream);
 
 /* 1 when the plan steps with the TMA tile kernels, 0 when with the generic kernels (a z
  * extent that is not a multiple of 4, or MEEPGB_TILES=0 in the environment). */
@@ -325,12 +342,22 @@ int mgb_dft_contract(const float* samples, int64_t ld, int64_t ncols, int32_t ns
 
 /* mgb_dft_contract with no scratch argument and no allocation: the phase table lives in
  * a device array of the library sized for MGB_DFT_MAX_FREQ frequencies (looked up once
- * per device). Sizes beyond the maximum are refused before the device is touched. Calls
+ * per device). Every refusal (sizes beyond the maximum, ld < ncols, a null argument), and
+ * a call with no work (nsamples or ncols 0), returns before the device is touched. Calls
  * that overlap on the device share that table and race: order them on one stream. */
 int mgb_dft_contract_noalloc(const float* samples, int64_t ld, int64_t ncols, int32_t nsamples,
                              const double* omega, int32_t nfreq, int64_t first_step,
                              int32_t step_stride, double dt, int32_t half_step_back, double scale,
                              float* acc, void* stream);
+
+/* Status word of the standalone contractions (mgb_dft_contract, mgb_dft_contract_noalloc)
+ * on the current device: a device int of the library, ORed with 4 when a contraction's
+ * tensor-core wait ran out (that call left the accumulators as they were, or added only
+ * the phase tiles before the one that timed out). It stays set until cleared. Queues a
+ * copy of the word into dst (device memory, or page-locked host memory; 4 bytes) on
+ * `stream` and, when clear is nonzero, a reset to zero after it. Asynchronous; allocates
+ * nothing. No reference counterpart (the reference's kernels report no wait). */
+int mgb_dft_contract_status(int32_t* dst, int32_t clear, void* stream);
 
 /* ---- Adjoint (reverse-time) stepping ------------------------------------------------
  * No reference counterpart (the reference has no adjoint). The adjoint state is a second

@@ -138,6 +138,7 @@ SIGNATURES = {
     "mgb_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p]),
     "mgb_flux_spectrum": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.c_void_p]),
+    "mgb_field_energy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "mgb_uses_tiles": (ctypes.c_int, [ctypes.c_void_p]),
     "mgb_select_kernels": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "mgb_select_half": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
@@ -160,6 +161,8 @@ SIGNATURES = {
                                                 ctypes.c_int64, ctypes.c_int32, ctypes.c_double,
                                                 ctypes.c_int32, ctypes.c_double, ctypes.c_void_p,
                                                 ctypes.c_void_p]),
+    "mgb_dft_contract_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
+    "mgb_set_test_wait_limit": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64]),
     "mgb_adjoint_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(MgbAdjoint), ctypes.c_int64,
                                         ctypes.c_void_p]),
     "mgb_adjoint_inject": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p]),

@@ -128,8 +128,13 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
   return ok != 0;
 }
 
-// Wait for phase `parity` of the MMA barrier for at most ~1 s of wall time.
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // ~1 s of wall time
+
+// Wait for phase `parity` of the MMA barrier for at most limit_ns of wall time; a limit
+// of 0 gives up without looking (the test hook that makes a wait run out).
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity,
+                                                  unsigned long long limit_ns = kWaitLimitNs) {
+  if (limit_ns == 0) return false;
   if (mbar_try_wait(bar, parity)) return true;
   unsigned long long start, now;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(start));
@@ -137,7 +142,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsig
     for (int spin = 0; spin < 256; ++spin)
       if (mbar_try_wait(bar, parity)) return true;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
-    if (now - start > 1000000000ull) return false;
+    if (now - start > limit_ns) return false;
   }
 }
 
@@ -227,11 +232,14 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const __grid_cons
       }
       mma_commit(bar);
     }
-    bool ok = mbar_wait_bounded(bar, parity);
+    const unsigned long long limit =
+        (mt == 0 && c.first_wait_ns >= 0) ? (unsigned long long)c.first_wait_ns : kWaitLimitNs;
+    bool ok = mbar_wait_bounded(bar, parity, limit);
     ok = __syncthreads_and(ok) != 0;
     if (!ok) {
-      // The MMAs did not complete in time: report, give them one more bounded wait, and
-      // leave without touching the accumulators.
+      // The MMAs did not complete in time: report, give them one more wait with the
+      // normal bound (tensor memory is freed only once they have completed, or that wait
+      // has run out too), and leave without touching the accumulators.
       if (tid == 0 && c.status != nullptr) atomicOr(c.status, 4);
       mbar_wait_bounded(bar, parity);
       __syncthreads();

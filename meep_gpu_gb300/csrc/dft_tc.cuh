@@ -31,6 +31,8 @@ struct Contraction {
   int nfreq;
   const float* table;                   // [mpad][kDepth] phase rows (see launch_table)
   int* status;                          // ORed with 4 when a tensor-core wait times out
+  long long first_wait_ns;              // limit of the first tile's wait; negative: the normal
+                                        // limit (a test hook: 0 gives up before waiting)
 };
 
 // Rows of the phase table: 2 * nfreq rounded up to the 128-row tile.

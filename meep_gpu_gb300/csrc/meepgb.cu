@@ -41,6 +41,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <atomic>
 #include <utility>
 #include <mutex>
 #include <cstdio>
@@ -57,6 +58,15 @@ int fail(int code, const std::string& message) {
   g_error = message;
   return code;
 }
+
+// Test hook (mgb_set_test_wait_limit): the limit, in nanoseconds, of the first bounded
+// wait of the next launches of the tile kernels (index 0: their first shared-memory stage)
+// and of the tensor-core contraction (index 1: its first tile's MMAs); negative keeps the
+// normal limit. Every later wait of those kernels, the drains included, keeps its normal
+// bound.
+std::atomic<long long> g_test_wait_limit[2] = {{-1}, {-1}};
+
+long long test_wait_limit(int which) { return g_test_wait_limit[which].load(std::memory_order_relaxed); }
 
 constexpr int kInteger = 0;
 constexpr int kHalf = 1;
@@ -127,6 +137,8 @@ struct TileMaps {
   int ninv;             // distinct inverse-epsilon volumes (1 or 3)
   int inv_of[3];        // which of inv[] serves each component
   int stages;
+  long long first_wait_ns;  // limit of the first stage wait; negative: the normal limit
+                            // (a test hook: 0 gives up before waiting)
 };
 
 struct BoxArgs {
@@ -1241,15 +1253,24 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
-// Wait for phase `parity` of a stage barrier, for at most ~2 s of wall time.
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+constexpr unsigned long long kStageWaitNs = 2000000000ull;  // ~2 s of wall time
+
+// Wait for phase `parity` of a stage barrier, for at most limit_ns of wall time; a limit
+// of 0 gives up without looking (the test hook that makes a wait run out).
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity,
+                                          unsigned long long limit_ns = kStageWaitNs) {
+  if (limit_ns == 0) return false;
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long start = global_ns();
   for (;;) {
     for (int spin = 0; spin < 256; ++spin)
       if (mbar_try_wait(bar, parity)) return true;
-    if (global_ns() - start > 2000000000ull) return false;
+    if (global_ns() - start > limit_ns) return false;
   }
+}
+
+__device__ __forceinline__ unsigned long long first_stage_limit(const TileMaps& maps) {
+  return maps.first_wait_ns >= 0 ? (unsigned long long)maps.first_wait_ns : kStageWaitNs;
 }
 
 __device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* map,
@@ -1262,7 +1283,9 @@ __device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* map,
 }
 
 // After an aborted wait: thread 0 lets this CTA's copies still in flight land (each
-// wait bounded) before the CTA exits and its shared memory is reused.
+// wait bounded) before the CTA exits and its shared memory is reused. `from` is the
+// oldest chain not yet known to have landed in every thread; waiting again on a chain
+// that has landed returns at once (its stage's phase has completed).
 __device__ __noinline__ void drain_copies(unsigned long long* full, int S, int from, int issued,
                                           int tid) {
   if (tid != 0) return;
@@ -1334,7 +1357,7 @@ __global__ void __launch_bounds__(kThreads, 2) h_tile(const __grid_constant__ St
   const int e = ty * kHaloZ + tz;  // this cell in an E box
   const int o = ty * kTileZ + tz;  // this cell in an own box
   const float dtdx = p.dtdx;
-  bool ok = mbar_wait(&full[0], 0);
+  bool ok = mbar_wait(&full[0], 0, first_stage_limit(maps));
   for (int i = i0; i < i1; ++i) {
     const int chain = i - i0;
     ok = ok && mbar_wait(&full[(chain + 1) % S], (unsigned)(((chain + 1) / S) & 1));
@@ -1374,8 +1397,10 @@ __global__ void __launch_bounds__(kThreads, 2) h_tile(const __grid_constant__ St
     }
     __syncthreads();  // the stage of plane i is read by everyone
     if (abort_flag) {
+      // chains chain .. issued - 1 may still be in flight (chain itself when the wait
+      // that failed was the first one)
       if (p.status != nullptr && tid == 0) atomicOr(p.status, 2);
-      drain_copies(full, S, chain + 1, issued, tid);
+      drain_copies(full, S, chain, issued, tid);
       return;
     }
     if (tid == 0 && chain + S < nchain) {
@@ -1450,7 +1475,7 @@ __global__ void __launch_bounds__(kThreads, 2) e_tile(const __grid_constant__ St
   const int o = ty * kTileZ + tz;            // this cell in an own box
   const int inv0 = 3 + maps.inv_of[0], inv1 = 3 + maps.inv_of[1], inv2 = 3 + maps.inv_of[2];
   const float dtdx = p.dtdx;
-  bool ok = mbar_wait(&full[0], 0);
+  bool ok = mbar_wait(&full[0], 0, first_stage_limit(maps));
   for (int i = i0; i < i1; ++i) {
     const int chain = i - i0 + 1;
     ok = ok && mbar_wait(&full[chain % S], (unsigned)((chain / S) & 1));
@@ -1488,8 +1513,10 @@ __global__ void __launch_bounds__(kThreads, 2) e_tile(const __grid_constant__ St
     }
     __syncthreads();  // the stage of plane i - 1 is read by everyone
     if (abort_flag) {
+      // chains chain - 1 .. issued - 1 may still be in flight (chain - 1 when the wait
+      // that failed was the first one)
       if (p.status != nullptr && tid == 0) atomicOr(p.status, 2);
-      drain_copies(full, S, chain, issued, tid);
+      drain_copies(full, S, chain - 1, issued, tid);
       return;
     }
     if (tid == 0 && chain - 1 + S < nchain) {
@@ -2487,6 +2514,12 @@ int launch_error(const char* what) {
   return MGB_OK;
 }
 
+// A CUDA call that returned `err` (already taken off the sticky-free error state).
+int cuda_error(cudaError_t err, const char* what) {
+  cudaGetLastError();
+  return fail(MGB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(err));
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   if (fn == nullptr) {
@@ -2531,6 +2564,7 @@ void setup_tiles(mgb_sim* sim) {
       return;
   TileMaps& m = sim->maps;
   memset(&m, 0, sizeof m);
+  m.first_wait_ns = -1;
   bool ok = true;
   for (int q = 0; q < 3; ++q) {
     ok = ok && make_map(&m.E[q], p.E[q], p.nx, p.ny, p.nz, kHaloZ, kHaloY);
@@ -2573,6 +2607,12 @@ void setup_tiles(mgb_sim* sim) {
 extern "C" {
 
 int mgb_abi_version(void) { return MGB_ABI_VERSION; }
+
+int mgb_set_test_wait_limit(int32_t which, int64_t nanoseconds) {
+  if (which < 0 || which > 1) return fail(MGB_ERR_ARGUMENT, "which must be 0 (tile stages) or 1 (contraction)");
+  g_test_wait_limit[which].store(nanoseconds < 0 ? -1 : (long long)nanoseconds, std::memory_order_relaxed);
+  return MGB_OK;
+}
 
 int mgb_last_error(char* buf, size_t size) {
   if (buf == nullptr || size == 0) return MGB_ERR_ARGUMENT;
@@ -2889,10 +2929,11 @@ int flush_monitor(mgb_sim* sim, int m, cudaStream_t s) {
       ++c.ncomp;
     }
     if (c.ncomp == 0) continue;
-    if (mgbdft::launch_table(mon.omega, mon.nfreq, buf.first_post, mon.decimation, mon.dt, half_back,
-                             mon.scale, buf.count, buf.table, s) != cudaSuccess ||
-        mgbdft::launch_contract(c, s) != cudaSuccess)
-      return launch_error("tensor-core DFT contraction");
+    c.first_wait_ns = test_wait_limit(1);
+    cudaError_t err = mgbdft::launch_table(mon.omega, mon.nfreq, buf.first_post, mon.decimation, mon.dt, half_back,
+                                           mon.scale, buf.count, buf.table, s);
+    if (err == cudaSuccess) err = mgbdft::launch_contract(c, s);
+    if (err != cudaSuccess) return cuda_error(err, "tensor-core DFT contraction");
   }
   buf.count = 0;
   return MGB_OK;
@@ -2909,6 +2950,7 @@ int launch_part_kernels(mgb_sim* sim, long long n, int part, cudaStream_t s) {
       const int xc = hc.tile_xchunk;
       const dim3 grid((p.nz + kTileZ - 1) / kTileZ, (p.ny + kTileY - 1) / kTileY,
                       (p.nx + xc - 1) / xc);
+      sim->maps.first_wait_ns = test_wait_limit(0);  // the launch takes the maps by value
       if (part == 0) {
         if (pml) launch_step(sim, h_tile<true>, grid, dim3(kThreads), sim->h_smem, s, p, sim->maps, (int)(n == 0), xc);
         else launch_step(sim, h_tile<false>, grid, dim3(kThreads), sim->h_smem, s, p, sim->maps, (int)(n == 0), xc);
@@ -3602,28 +3644,63 @@ void mgb_batch_destroy(mgb_batch* b) {
 
 // ======================================================================================
 // Tensor-core DFT contraction ABI
-extern "C" {
+//
+// The standalone contractions (mgb_dft_contract and its allocation-free twin) report a
+// tensor-core wait that ran out in a status word of the library: a file-scope device int
+// beside the allocation-free entry point's phase table, so neither entry point needs a
+// caller buffer for it. Both device addresses are looked up once per device
+// (cudaGetSymbolAddress with that device current) and cached. The status word is sticky
+// until mgb_dft_contract_status clears it.
+namespace {
 
-size_t mgb_dft_scratch_bytes(int32_t nfreq) {
-  if (nfreq < 1 || nfreq > mgbdft::kMaxFreq) return 0;
-  return mgbdft::table_bytes(nfreq);
+static __device__ __align__(256) float g_dft_table[2 * mgbdft::kMaxFreq * mgbdft::kDepth];
+static __device__ int g_contract_status;
+
+struct StaticWords {
+  void* table = nullptr;
+  int* status = nullptr;
+};
+
+std::mutex g_static_mutex;
+std::vector<StaticWords> g_static_words;  // per device, empty until looked up
+
+int static_words(StaticWords* out) {
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess) return launch_error("current device");
+  std::lock_guard<std::mutex> lock(g_static_mutex);
+  if ((int)g_static_words.size() <= device) g_static_words.resize(device + 1);
+  StaticWords& words = g_static_words[device];
+  if (words.table == nullptr) {
+    void* table = nullptr;
+    void* status = nullptr;
+    cudaError_t err = cudaGetSymbolAddress(&table, g_dft_table);
+    if (err != cudaSuccess) return cuda_error(err, "static DFT table address");
+    err = cudaGetSymbolAddress(&status, g_contract_status);
+    if (err != cudaSuccess) return cuda_error(err, "contraction status address");
+    words.table = table;
+    words.status = static_cast<int*>(status);
+  }
+  *out = words;
+  return MGB_OK;
 }
 
-int mgb_dft_contract(const float* samples, int64_t ld, int64_t ncols, int32_t nsamples, const double* omega,
-                     int32_t nfreq, int64_t first_step, int32_t step_stride, double dt, int32_t half_step_back,
-                     double scale, float* acc, void* scratch, size_t scratch_bytes, void* stream) {
-  if (samples == nullptr || omega == nullptr || acc == nullptr || scratch == nullptr)
-    return fail(MGB_ERR_ARGUMENT, "null argument");
+// Arguments every contraction entry point checks before it touches the device; returns
+// MGB_OK, or the refusal. *nothing is set when the call has no work.
+int check_contract(const float* samples, int64_t ld, int64_t ncols, int32_t nsamples, const double* omega,
+                   int32_t nfreq, const float* acc, bool* nothing) {
   if (nfreq < 1 || nfreq > mgbdft::kMaxFreq)
     return fail(MGB_ERR_ARGUMENT, "nfreq must be 1.." + std::to_string(mgbdft::kMaxFreq));
   if (nsamples < 0 || nsamples > mgbdft::kDepth)
     return fail(MGB_ERR_ARGUMENT, "nsamples must be 0.." + std::to_string(mgbdft::kDepth));
   if (ncols < 0 || ld < ncols) return fail(MGB_ERR_ARGUMENT, "ld must be at least ncols");
-  if (scratch_bytes < mgbdft::table_bytes(nfreq))
-    return fail(MGB_ERR_ARGUMENT, "scratch is smaller than mgb_dft_scratch_bytes(nfreq)");
-  if (nsamples == 0 || ncols == 0) return MGB_OK;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  float* table = static_cast<float*>(scratch);
+  if (samples == nullptr || omega == nullptr || acc == nullptr) return fail(MGB_ERR_ARGUMENT, "null argument");
+  *nothing = (nsamples == 0 || ncols == 0);
+  return MGB_OK;
+}
+
+int contract_with_table(const float* samples, int64_t ld, int64_t ncols, int32_t nsamples, const double* omega,
+                        int32_t nfreq, int64_t first_step, int32_t step_stride, double dt, int32_t half_step_back,
+                        double scale, float* acc, float* table, int* status, cudaStream_t s) {
   mgbdft::Contraction c = {};
   c.samples = samples;
   c.ld = ld;
@@ -3634,42 +3711,12 @@ int mgb_dft_contract(const float* samples, int64_t ld, int64_t ncols, int32_t ns
   c.acc_ld = ncols;
   c.nfreq = nfreq;
   c.table = table;
-  if (mgbdft::launch_table(omega, nfreq, first_step, step_stride, dt, half_step_back ? 1 : 0, scale, nsamples,
-                           table, s) != cudaSuccess ||
-      mgbdft::launch_contract(c, s) != cudaSuccess)
-    return launch_error("tensor-core DFT contraction");
-  return MGB_OK;
-}
-
-}  // extern "C"
-
-// ======================================================================================
-// Tensor-core DFT contraction without caller scratch
-//
-// The phase table lives in a file-scope device array sized for the largest contraction
-// (2 * MGB_DFT_MAX_FREQ rows of MGB_DFT_DEPTH words). Its address is looked up once per
-// device (cudaGetSymbolAddress with that device current) and cached. No word of it must
-// start at zero: the table kernel writes every word the contraction then reads. Calls
-// that overlap on the device (different streams, or threads without ordering) share the
-// one table and race.
-namespace {
-
-static __device__ __align__(256) float g_dft_table[2 * mgbdft::kMaxFreq * mgbdft::kDepth];
-
-std::mutex g_table_mutex;
-std::vector<void*> g_table_address;  // per device, null until looked up
-
-int static_table(void** out) {
-  int device = 0;
-  if (cudaGetDevice(&device) != cudaSuccess) return launch_error("current device");
-  std::lock_guard<std::mutex> lock(g_table_mutex);
-  if ((int)g_table_address.size() <= device) g_table_address.resize(device + 1, nullptr);
-  if (g_table_address[device] == nullptr) {
-    void* address = nullptr;
-    if (cudaGetSymbolAddress(&address, g_dft_table) != cudaSuccess) return launch_error("static DFT table address");
-    g_table_address[device] = address;
-  }
-  *out = g_table_address[device];
+  c.status = status;
+  c.first_wait_ns = test_wait_limit(1);
+  cudaError_t err = mgbdft::launch_table(omega, nfreq, first_step, step_stride, dt, half_step_back ? 1 : 0, scale,
+                                         nsamples, table, s);
+  if (err == cudaSuccess) err = mgbdft::launch_contract(c, s);
+  if (err != cudaSuccess) return cuda_error(err, "tensor-core DFT contraction");
   return MGB_OK;
 }
 
@@ -3677,22 +3724,159 @@ int static_table(void** out) {
 
 extern "C" {
 
+size_t mgb_dft_scratch_bytes(int32_t nfreq) {
+  if (nfreq < 1 || nfreq > mgbdft::kMaxFreq) return 0;
+  return mgbdft::table_bytes(nfreq);
+}
+
+int mgb_dft_contract(const float* samples, int64_t ld, int64_t ncols, int32_t nsamples, const double* omega,
+                     int32_t nfreq, int64_t first_step, int32_t step_stride, double dt, int32_t half_step_back,
+                     double scale, float* acc, void* scratch, size_t scratch_bytes, void* stream) {
+  bool nothing = false;
+  const int rc = check_contract(samples, ld, ncols, nsamples, omega, nfreq, acc, &nothing);
+  if (rc != MGB_OK) return rc;
+  if (scratch == nullptr) return fail(MGB_ERR_ARGUMENT, "null argument");
+  if (scratch_bytes < mgbdft::table_bytes(nfreq))
+    return fail(MGB_ERR_ARGUMENT, "scratch is smaller than mgb_dft_scratch_bytes(nfreq)");
+  if (nothing) return MGB_OK;
+  StaticWords words;
+  const int found = static_words(&words);
+  if (found != MGB_OK) return found;
+  return contract_with_table(samples, ld, ncols, nsamples, omega, nfreq, first_step, step_stride, dt,
+                             half_step_back, scale, acc, static_cast<float*>(scratch), words.status,
+                             static_cast<cudaStream_t>(stream));
+}
+
+// The phase table of this entry point is g_dft_table (2 * MGB_DFT_MAX_FREQ rows of
+// MGB_DFT_DEPTH words). No word of it must start at zero: the table kernel writes every
+// word the contraction then reads. Calls that overlap on the device (different streams,
+// or threads without ordering) share the one table and race.
 int mgb_dft_contract_noalloc(const float* samples, int64_t ld, int64_t ncols, int32_t nsamples,
                              const double* omega, int32_t nfreq, int64_t first_step, int32_t step_stride,
                              double dt, int32_t half_step_back, double scale, float* acc, void* stream) {
-  // the sizes are checked before the device is touched
-  if (nfreq < 1 || nfreq > mgbdft::kMaxFreq)
-    return fail(MGB_ERR_ARGUMENT, "nfreq must be 1.." + std::to_string(mgbdft::kMaxFreq));
-  if (nsamples < 0 || nsamples > mgbdft::kDepth)
-    return fail(MGB_ERR_ARGUMENT, "nsamples must be 0.." + std::to_string(mgbdft::kDepth));
   static_assert(sizeof(g_dft_table) >= (size_t)2 * mgbdft::kMaxFreq * mgbdft::kDepth * sizeof(float),
                 "static table holds the largest contraction");
-  if (samples == nullptr || omega == nullptr || acc == nullptr) return fail(MGB_ERR_ARGUMENT, "null argument");
-  void* table = nullptr;
-  const int rc = static_table(&table);
+  // every refusal, and a call with no work, returns before the device is touched
+  bool nothing = false;
+  const int rc = check_contract(samples, ld, ncols, nsamples, omega, nfreq, acc, &nothing);
   if (rc != MGB_OK) return rc;
-  return mgb_dft_contract(samples, ld, ncols, nsamples, omega, nfreq, first_step, step_stride, dt,
-                          half_step_back, scale, acc, table, sizeof(g_dft_table), stream);
+  if (nothing) return MGB_OK;
+  StaticWords words;
+  const int found = static_words(&words);
+  if (found != MGB_OK) return found;
+  return contract_with_table(samples, ld, ncols, nsamples, omega, nfreq, first_step, step_stride, dt,
+                             half_step_back, scale, acc, static_cast<float*>(words.table), words.status,
+                             static_cast<cudaStream_t>(stream));
+}
+
+int mgb_dft_contract_status(int32_t* dst, int32_t clear, void* stream) {
+  if (dst == nullptr) return fail(MGB_ERR_ARGUMENT, "null argument");
+  StaticWords words;
+  const int found = static_words(&words);
+  if (found != MGB_OK) return found;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t err = cudaMemcpyAsync(dst, words.status, sizeof(int32_t), cudaMemcpyDefault, s);
+  if (err != cudaSuccess) return cuda_error(err, "contraction status read");
+  if (clear != 0) {
+    err = cudaMemsetAsync(words.status, 0, sizeof(int32_t), s);
+    if (err != cudaSuccess) return cuda_error(err, "contraction status reset");
+  }
+  return MGB_OK;
+}
+
+}  // extern "C"
+
+// ======================================================================================
+// Field energy (the divergence guard's scalar)
+//
+// sum over the grid of |E|^2 eps + |B|^2 (eps = 1 / inverse permittivity of each E
+// component; B is the H half's B word: the auxiliary's on its own-axis membership, H's
+// elsewhere, where MEEP's H is B's word). Each cell's terms are formed in float32 and
+// summed in float64 per thread, then per block, then into one device double.
+namespace {
+
+struct EnergyArgs {
+  const float* E[3];
+  const float* inv[3];
+  const float* H[3];
+  const float* B[3];  // NULL: no own-axis membership (H is B everywhere)
+  int axis[3], a0[3], a1[3], b0[3], b1[3];
+  int ny, nz;
+  long long cells;
+  double* out;
+};
+
+__global__ void __launch_bounds__(256) energy_kernel(const __grid_constant__ EnergyArgs a) {
+  double sum = 0.0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long plane = (long long)a.ny * a.nz;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < a.cells; c += stride) {
+    const int i = (int)(c / plane);
+    const int rem = (int)(c - (long long)i * plane);
+    const int at[3] = {i, rem / a.nz, rem % a.nz};
+    float cell = 0.f;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const float e = a.E[q][c];
+      cell += (e * e) / a.inv[q][c];
+      float b = a.H[q][c];
+      if (a.B[q] != nullptr) {
+        const int r = at[a.axis[q]];
+        if ((r >= a.a0[q] && r < a.a1[q]) || (r >= a.b0[q] && r < a.b1[q])) b = a.B[q][c];
+      }
+      cell += b * b;
+    }
+    sum += (double)cell;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, off);
+  __shared__ double warp_sums[8];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) warp_sums[warp] = sum;
+  __syncthreads();
+  if (warp == 0) {
+    sum = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0.0;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, off);
+    if (lane == 0) atomicAdd(a.out, sum);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int mgb_field_energy(mgb_sim* sim, double* out, void* stream) {
+  if (sim == nullptr || out == nullptr) return fail(MGB_ERR_ARGUMENT, "null argument");
+  const mgb_sim_desc& d = sim->desc;
+  EnergyArgs a = {};
+  for (int q = 0; q < 3; ++q) {
+    a.E[q] = d.E[q];
+    a.inv[q] = d.inv_eps[q];
+    a.H[q] = d.H[q];
+    const mgb_aux& b = d.B[q];
+    if (d.pml_active && b.data != nullptr && (b.a1 > b.a0 || b.b1 > b.b0)) {
+      a.B[q] = b.data;
+      a.axis[q] = b.axis;
+      a.a0[q] = b.a0;
+      a.a1[q] = b.a1;
+      a.b0[q] = b.b0;
+      a.b1[q] = b.b1;
+    }
+  }
+  a.ny = d.ny;
+  a.nz = d.nz;
+  a.cells = (long long)d.nx * d.ny * d.nz;
+  a.out = out;
+  int device = 0, sms = 0;
+  if (cudaGetDevice(&device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+    return launch_error("device query");
+  const long long blocks = std::min<long long>((long long)sms * 8, (a.cells + 255) / 256);
+  energy_kernel<<<(unsigned)std::max<long long>(blocks, 1), 256, 0, static_cast<cudaStream_t>(stream)>>>(a);
+  const cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return cuda_error(err, "field energy");
+  return MGB_OK;
 }
 
 }  // extern "C"

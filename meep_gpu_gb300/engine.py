@@ -659,6 +659,23 @@ class Engine:
         """Whether a non-finite E has been written (raises on a device timeout)."""
         return bool(self.device_status() & self.STATUS_NONFINITE)
 
+    def queue_field_energy(self, out: torch.Tensor) -> None:
+        """Add this plan's sum |E|^2 eps + |B|^2 (float64, on the device) into ``out``."""
+        _lib.check(self.lib, self.lib.mgb_field_energy(self.handle, out.data_ptr(), self._stream_handle()))
+
+    def energy_word(self) -> torch.Tensor:
+        """A zeroed device double, zeroed on the stream the plan steps on."""
+        stream = self.stream if self.stream is not None else torch.cuda.current_stream(self.device)
+        with torch.cuda.stream(stream):
+            return torch.zeros(1, dtype=torch.float64, device=self.device)
+
+    def field_energy(self) -> float:
+        """The divergence guard's scalar (reference ``FdtdDriver._field_energy``,
+        driver.py:3634): one device reduction and one 8-byte read."""
+        out = self.energy_word()
+        self.queue_field_energy(out)
+        return float(out.item())
+
     # --- read-out -----------------------------------------------------------------------
     def field(self, name: str) -> torch.Tensor:
         """Device tensor of one component's stored Yee words (H composed from B and slab)."""
@@ -852,6 +869,13 @@ class ComplexEngine:
 
     def nonfinite(self) -> bool:
         return self.re.nonfinite() or self.im.nonfinite()
+
+    def field_energy(self) -> float:
+        """|E|^2 eps + |B|^2 over both parts: re^2 + im^2 of every word."""
+        out = self.re.energy_word()
+        self.re.queue_field_energy(out)
+        self.im.queue_field_energy(out)
+        return float(out.item())
 
     def algorithmic_bytes(self) -> Dict[str, int]:
         a, b = self.re.algorithmic_bytes(), self.im.algorithmic_bytes()

@@ -1,13 +1,19 @@
 """The allocation-free contraction entry point (static phase-table scratch) against the
-entry point that takes caller scratch: identical words, twice in a row, across sizes."""
+entry point that takes caller scratch: identical words, twice in a row, across sizes,
+with no device memory taken by the calls."""
+
+import re
+from pathlib import Path
 
 import numpy as np
 import pytest
 
 from meep_gpu_gb300 import _lib
 
+SOURCE = Path(__file__).resolve().parent.parent / "meep_gpu_gb300" / "csrc" / "meepgb.cu"
 
-def test_noalloc_refuses_sizes_beyond_the_maximum_before_touching_the_device():
+
+def test_noalloc_refuses_bad_arguments_before_touching_the_device():
     lib = _lib.load()
     assert lib.mgb_dft_contract_noalloc(None, 4, 4, 1, None, _lib.MGB_DFT_MAX_FREQ + 1, 0, 1, 0.1, 0,
                                         1.0, None, None) == -1
@@ -15,6 +21,31 @@ def test_noalloc_refuses_sizes_beyond_the_maximum_before_touching_the_device():
     assert lib.mgb_dft_contract_noalloc(None, 4, 4, _lib.MGB_DFT_DEPTH + 1, None, 4, 0, 1, 0.1, 0,
                                         1.0, None, None) == -1
     assert "nsamples" in _lib.last_error(lib)
+    assert lib.mgb_dft_contract_noalloc(None, 3, 4, 1, None, 4, 0, 1, 0.1, 0, 1.0, None, None) == -1
+    assert "ld" in _lib.last_error(lib)
+    assert lib.mgb_dft_contract_noalloc(None, 4, 4, 1, None, 4, 0, 1, 0.1, 0, 1.0, None, None) == -1
+    assert "null" in _lib.last_error(lib)
+    assert lib.mgb_dft_contract_status(None, 0, None) == -1
+
+
+def _function_body(text: str, name: str) -> str:
+    start = text.index(f"int {name}(")
+    depth, i = 0, text.index("{", start)
+    for j in range(i, len(text)):
+        depth += {"{": 1, "}": -1}.get(text[j], 0)
+        if depth == 0:
+            return text[start:j + 1]
+    raise AssertionError(f"no body for {name}")
+
+
+def test_noalloc_path_names_no_allocating_call():
+    """The entry point and the helpers it calls name no allocating CUDA routine."""
+    text = SOURCE.read_text()
+    body = "".join(_function_body(text, name) for name in
+                   ("mgb_dft_contract_noalloc", "static_words", "check_contract", "contract_with_table",
+                    "mgb_dft_contract_status"))
+    assert not re.search(r"cuda(Malloc|Free|HostAlloc|MallocAsync|MallocManaged|MallocHost)\w*", body)
+    assert "g_dft_table" in body and "cudaGetSymbolAddress" in body
 
 
 @pytest.mark.gpu
@@ -24,6 +55,8 @@ def test_noalloc_equals_the_scratch_entry_point_twice_in_a_row(gpu):
     lib = _lib.load()
     stream = torch.cuda.current_stream().cuda_stream
     rng = np.random.default_rng(7)
+    status = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    _lib.check(lib, lib.mgb_dft_contract_status(status.data_ptr(), 1, stream))
     for nfreq, ncols, nsamples in ((64, 700, 32), (512, 300, 17), (3, 1, 1)):
         ld = ncols + 5
         samples = torch.from_numpy(rng.standard_normal((32, ld)).astype(np.float32)).cuda()
@@ -34,9 +67,19 @@ def test_noalloc_equals_the_scratch_entry_point_twice_in_a_row(gpu):
         expected = acc0.clone()
         _lib.check(lib, lib.mgb_dft_contract(samples.data_ptr(), *args, expected.data_ptr(), scratch.data_ptr(),
                                              scratch.numel() * 4, stream))
-        for _ in range(2):
-            got = acc0.clone()
+        outputs = [acc0.clone(), acc0.clone()]
+        # one call first (its device's table address is looked up), then two more with
+        # the caching allocator's counters unchanged across them
+        _lib.check(lib, lib.mgb_dft_contract_noalloc(samples.data_ptr(), *args, acc0.clone().data_ptr(), stream))
+        torch.cuda.synchronize()
+        allocated, reserved = torch.cuda.memory_allocated(), torch.cuda.memory_reserved()
+        for got in outputs:
             _lib.check(lib, lib.mgb_dft_contract_noalloc(samples.data_ptr(), *args, got.data_ptr(), stream))
-            torch.cuda.synchronize()
+        torch.cuda.synchronize()
+        assert (torch.cuda.memory_allocated(), torch.cuda.memory_reserved()) == (allocated, reserved)
+        for got in outputs:
             assert torch.equal(got, expected), (nfreq, ncols, nsamples)
         assert not torch.equal(expected, acc0)
+    _lib.check(lib, lib.mgb_dft_contract_status(status.data_ptr(), 0, stream))
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0, "a contraction reported a tensor-core wait that ran out"

@@ -55,6 +55,11 @@ CASES = {
     # the case the serving batch's Bloch slots are checked on (one monitor).
     "bloch_sphere": dict(n=(14, 12, 16), pml={"z": 3}, steps=60, complex=True, boundaries=("periodic", "periodic", "metallic"),
                          k_point=(0.3, -0.2, 0.0)),
+    # The Bloch sphere case with magnetic sources (a Gaussian Hx point, a CW Hz sheet):
+    # the magnetic deposit of the batch's phased (index-0) CTAs.
+    "bloch_magnetic": dict(n=(14, 12, 16), pml={"z": 3}, steps=60, complex=True,
+                           boundaries=("periodic", "periodic", "metallic"), k_point=(0.3, -0.2, 0.0),
+                           magnetic=True),
     # Bloch-periodic fields (complex, k != 0): phased x and y with an interior point
     # source, a DFT volume and a flux plane spanning the whole y-z cross-section; and
     # a phased x axis under a z PML with a line source wrapping the phased axis, odd
@@ -94,6 +99,8 @@ CASES = {
 # The 80^3 sphere-under-PML workload (resolution 10, 10-cell PML, eps 4 sphere of radius
 # 2, Ez Gaussian at x = -2, one 50-frequency x-normal flux plane at x = 2.5).
 SPHERE80 = dict(n=(80, 80, 80), pml=10, steps=200, sphere80=True)
+# The same workload over its full 2000 steps.
+SPHERE80_FULL = dict(SPHERE80, steps=2000)
 
 
 def build_case(driver_cls, susceptibility_cls, case: dict, reference: bool = False):

@@ -1,14 +1,16 @@
 """Record golden vectors from the reference implementation (run in the build container).
 
 Imports the reference's NumPy array path (``meep_gpu.FdtdDriver`` with
-``prefer_gpu=False``) from ``$MEEPGB_REFERENCE`` (default: the reference checkout
-beside the repository) and writes small fixtures into this directory:
+``prefer_gpu=False``) from ``$MEEPGB_REFERENCE`` (default: a ``reference`` checkout in
+the directory that holds this repository) and writes small fixtures into this directory:
 
 * ``fields_<case>.npz``: every stored float32 field word (E, D, B, H and, for a
   dispersive case, P) after N steps of a small seeded case, plus its flux spectra and
   DFT accumulators;
 * ``digest_sphere80.json``: SHA-256 of every field component after 200 steps of the
   80^3 sphere-under-PML workload (the full-size configuration), plus its flux spectrum;
+  ``digest_sphere80_2000.json``: the same after the workload's full 2000 steps
+  (``python make_golden.py digest2000``);
 * ``tables.npz``: PML coefficient vectors, source deposition tables, flux-plane
   regions and weights and automatic decimation factors for a sweep of requests;
 * ``conductivity_tables.npz``: ``mp.Absorber`` sigma volumes, conductivity
@@ -36,14 +38,17 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-REFERENCE = os.environ.get("MEEPGB_REFERENCE", "/root/reference")
+REFERENCE = os.environ.get("MEEPGB_REFERENCE", str(HERE.parent.parent.parent / "reference"))
+if not (Path(REFERENCE) / "meep_gpu").is_dir():
+    raise SystemExit(f"no reference checkout at {REFERENCE}: set MEEPGB_REFERENCE to the directory "
+                     "that holds the meep_gpu package")
 sys.path.insert(0, REFERENCE)
 
 from meep_gpu import FdtdDriver  # noqa: E402
 from meep_gpu.dispersion import Susceptibility  # noqa: E402
 
 sys.path.insert(0, str(HERE.parent.parent))
-from tests.golden.cases import CASES, SPHERE80, build_case  # noqa: E402
+from tests.golden.cases import CASES, SPHERE80, SPHERE80_FULL, build_case  # noqa: E402
 
 COMPONENTS = ("Ex", "Ey", "Ez", "Dx", "Dy", "Dz", "Bx", "By", "Bz", "Hx", "Hy", "Hz")
 
@@ -71,17 +76,17 @@ def record_fields(name: str, case: dict) -> None:
     print(name, "written")
 
 
-def record_digest() -> None:
-    driver, flux, _ = reference_driver(SPHERE80)
-    driver.run(num_steps=SPHERE80["steps"])
+def record_digest(case=SPHERE80, filename="digest_sphere80.json") -> None:
+    driver, flux, _ = reference_driver(case)
+    driver.run(num_steps=case["steps"])
     digests = {}
     for c in COMPONENTS:
         words = np.ascontiguousarray(driver.get_field(c, cell_centered=False), dtype=np.float32)
         digests[c] = hashlib.sha256(words.tobytes()).hexdigest()
-    payload = {"case": "sphere80", "steps": SPHERE80["steps"], "sha256": digests,
+    payload = {"case": "sphere80", "steps": case["steps"], "sha256": digests,
                "flux": [float(v) for v in flux[0].get_flux_spectrum()],
                "decimation": int(flux[0].decimation_factor)}
-    (HERE / "digest_sphere80.json").write_text(json.dumps(payload, indent=1) + "\n")
+    (HERE / filename).write_text(json.dumps(payload, indent=1) + "\n")
     print("digest written")
 
 
@@ -259,6 +264,8 @@ if __name__ == "__main__":
         record_tables()
     if "digest" in which:
         record_digest()
+    if "digest2000" in which:
+        record_digest(SPHERE80_FULL, "digest_sphere80_2000.json")
     if "conductivity" in which:
         record_conductivity_tables()
     if "flux_norm" in which:

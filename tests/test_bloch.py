@@ -52,7 +52,7 @@ def test_src_vol_entries_are_the_reference_entries(tables, t):
         assert np.array_equal(np.asarray(source.amps, dtype=np.complex128), tables[f"c{t}_s{m}_amps"]), (t, m)
 
 
-@pytest.mark.parametrize("name", ["bloch", "bloch_pml", "bloch_sphere"])
+@pytest.mark.parametrize("name", ["bloch", "bloch_pml", "bloch_sphere", "bloch_magnetic"])
 def test_oracle_bloch_pair_matches_reference_words(name):
     """The float32 oracle's two parts, stepped together, are the reference's complex words
     bit for bit; its transforms and spectra match to float32 rounding."""

@@ -244,7 +244,7 @@ def test_batch_steps_every_golden_configuration_to_the_reference_words(gpu):
     names = [n for n in sorted(CASES) if n not in ("mixed", "tile_mixed", "complex_mixed")
              and not CASES[n].get("conductivity") and not CASES[n].get("bloch_monitors")
              and not CASES[n].get("symmetry")]
-    assert {"complex_sphere", "bloch_sphere", "magnetic"} <= set(names)
+    assert {"complex_sphere", "bloch_sphere", "bloch_magnetic", "magnetic"} <= set(names)
     slots = sum(2 if CASES[n].get("complex") else 1 for n in names)
     server = serving.BatchServer(gpu, max_slots=slots, steps_per_replay=16, max_side=72)
     jobs = []

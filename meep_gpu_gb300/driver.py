@@ -37,10 +37,62 @@ from .sources import Source, bind_src_vols, make_waveform
 
 FIELD_COMPONENTS = ("Ex", "Ey", "Ez", "Dx", "Dy", "Dz", "Hx", "Hy", "Hz", "Bx", "By", "Bz")
 STEP_TOLERANCE = 1e-9
+# How often run() samples the field energy of a dispersive run, and how far above the peak
+# reached while the sources still emit it may climb afterwards (reference driver.py:319-320).
+STABILITY_CHECK_INTERVAL = 20
+STABILITY_GROWTH_LIMIT = 1e3
 
 
 class FdtdDivergence(RuntimeError):
-    """A non-finite field was written: the run diverged."""
+    """The run diverged: a non-finite field was written, or a dispersive run's field
+    energy ran away after its sources stopped."""
+
+
+class DivergenceGuard:
+    """The field-energy watch of a dispersive run (reference ``_DivergenceGuard``,
+    driver.py:747-792).
+
+    A dispersive run can diverge smoothly, staying finite for thousands of steps. In a
+    passive medium under periodic or absorbing boundaries the field energy is
+    non-increasing once the last source has stopped, so every ``interval`` steps the
+    energy ``sum |E|^2 eps + |B|^2`` is read: a non-finite value raises, while the
+    sources emit the peak is tracked, and afterwards a value above ``growth_limit``
+    times that peak raises :class:`FdtdDivergence`.
+
+    ``energy`` is the scalar's source (default: the driver's device reduction).
+    """
+
+    def __init__(self, driver: "FdtdDriver", interval: int = STABILITY_CHECK_INTERVAL,
+                 growth_limit: float = STABILITY_GROWTH_LIMIT,
+                 energy: Optional[Callable[[], float]] = None):
+        self._driver = driver
+        self.interval = max(1, int(interval))
+        self._growth_limit = float(growth_limit)
+        self._source_end = driver.last_source_time()
+        self._energy = energy if energy is not None else driver.field_energy
+        self.peak = 0.0
+        self.samples = 0
+
+    def update(self) -> None:
+        """Sample when the step count is a multiple of the interval; raise on divergence."""
+        driver = self._driver
+        if driver.step_count % self.interval:
+            return
+        energy = float(self._energy())
+        self.samples += 1
+        if not math.isfinite(energy):
+            raise FdtdDivergence(f"field energy is not finite ({energy}) after {driver.step_count} steps of "
+                                 f"a dispersive run")
+        if driver.time <= self._source_end:
+            self.peak = max(self.peak, energy)
+            return
+        if self.peak > 0.0 and energy > self._growth_limit * self.peak:
+            raise FdtdDivergence(
+                f"field energy grew to {energy:.3e} after {driver.step_count} steps, {energy / self.peak:.3e} "
+                f"times the peak {self.peak:.3e} reached while the sources emitted (they stopped at "
+                f"t={self._source_end:g}, it is now t={driver.time:g}); a passive medium cannot gain energy "
+                f"after its drive stops, so the run is diverging")
+        self.peak = max(self.peak, energy)
 
 
 class FdtdCancelled(RuntimeError):
@@ -425,6 +477,30 @@ class FdtdDriver:
         self.engine.step(self.step_count, int(nsteps))
         self.step_count += int(nsteps)
 
+    @property
+    def has_polarizations(self) -> bool:
+        return any(any(v is not None for v in volumes) for _, volumes in self._poles)
+
+    def field_energy(self) -> float:
+        """``sum |E|^2 eps + |B|^2`` over the grid in float64, reduced on the device
+        (reference ``_field_energy``, driver.py:3634); 0 before the first step."""
+        if self.engine is None:
+            return 0.0
+        return self.engine.field_energy()
+
+    def last_source_time(self) -> float:
+        """The latest time any source emits (reference ``_last_source_time``,
+        driver.py:3918): a Gaussian's peak plus cutoff times width, a continuous
+        source's end time."""
+        latest = 0.0
+        for source in self._sources:
+            waveform = source.waveform
+            if hasattr(waveform, "peak_time"):
+                latest = max(latest, waveform.peak_time + waveform.cutoff * waveform.width)
+            elif getattr(waveform, "end_time", None) is not None:
+                latest = max(latest, float(waveform.end_time))
+        return latest
+
     def sources_end_time(self) -> float:
         """Last time any source is on (Gaussian: peak + cutoff), MEEP's ``last_source_time``."""
         latest = 0.0
@@ -444,7 +520,9 @@ class FdtdDriver:
 
         Steps are queued in chunks of ``progress_interval``; between chunks the
         non-finite detector is read (one small device-to-host read) and the cancel
-        and progress callbacks run. Returns the number of steps taken.
+        and progress callbacks run. A dispersive run also stops at every multiple of
+        ``STABILITY_CHECK_INTERVAL`` steps for the divergence guard's field energy
+        (:class:`DivergenceGuard`). Returns the number of steps taken.
         """
         if unsupported:
             raise Unsupported(f"run options {sorted(unsupported)} are not supported by this engine")
@@ -463,12 +541,22 @@ class FdtdDriver:
             if total != num_steps or total < 1:
                 raise ValueError(f"num_steps must be a positive whole number, got {num_steps!r}")
         interval = max(1, int(progress_interval))
+        guard = DivergenceGuard(self) if (check_finite and self.has_polarizations) else None
         started = time_module.perf_counter()
         completed = 0
+        since_report = 0
         while completed < total:
-            chunk = min(interval, total - completed)
+            chunk = min(interval - since_report, total - completed)
+            if guard is not None:
+                chunk = min(chunk, guard.interval - self.step_count % guard.interval)
             self.step_many(chunk)
             completed += chunk
+            since_report += chunk
+            if guard is not None:
+                guard.update()
+            if since_report < interval and completed < total:
+                continue
+            since_report = 0
             if check_finite and self.engine.nonfinite():
                 raise FdtdDivergence(f"a non-finite E was written by step {self.step_count}")
             if cancel_check is not None and cancel_check():

@@ -18,7 +18,14 @@ decimated steps).
 * ``cpu_baseline``: the float32 oracle (the C restatement of the reference's array
   path, OpenMP over every host core) on a bounded sample of the same workload.
 * ``error``: relative L2 of the fields and flux against the float64 oracle on bounded
-  samples.
+  samples, the timed 192^3 eight-DFT workload's own (600 steps) among them.
+* ``configs``: the other configurations (the 80^3 sphere, the 192^3 Lorentz slab)
+  device-resident over ``--config-steps`` steps, each with its per-half roofline and clocks.
+* ``full_run``: each configuration's whole run at its stated step count (80^3: 2000,
+  192^3 eight-DFT: 5000, Lorentz: 10,000) with every DFT sample, contraction and spectrum
+  read inside the window, device-resident and end to end through ``FdtdDriver``.
+* ``adjoint``: the 96^3 adjoint gradient (forward with checkpoints, backward) and its
+  agreement with the float64 finite differences of ``tests/golden/adjoint96_fd.json``.
 * ``lossy``: the lossy kernels (D and B conductivity) on two 192^3 workloads, an
   absorber in place of the PML and a conductivity under the PML, each with its per-half
   roofline, and their float64 error on a 40^3 lossy case.
@@ -80,6 +87,11 @@ def parse_args():
     p.add_argument("--serving-replay", type=int, default=128, help="steps per captured replay")
     p.add_argument("--serving-budget-gb", type=float, default=16.0)
     p.add_argument("--no-plain", action="store_true", help="skip the one-at-a-time solve")
+    p.add_argument("--config-steps", type=int, default=200,
+                   help="steps timed on the other configurations (80^3 sphere, 192^3 Lorentz slab); 0 skips")
+    p.add_argument("--no-full-run", action="store_true",
+                   help="skip the whole runs of the three configurations at their stated step counts")
+    p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint section of the default line")
     p.add_argument("--adjoint", action="store_true",
                    help="instead of the step line: the 96^3 adjoint-gradient workload")
     p.add_argument("--dft", action="store_true",
@@ -228,6 +240,12 @@ def time_oracle(workload: str, steps: int, budget_s: float = 20.0, warmup: int =
     return cells * sample / elapsed / 1e6, sample, cells
 
 
+def workload_config(workload: str, cells: int, world: int) -> dict:
+    """The ``config`` object both arms print (the same keys and values)."""
+    return {"workload": workload, "cells": cells, "parallelism": f"replicas{world}",
+            "l2": "inputs larger than L2 (no flush needed)"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -238,7 +256,7 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(cells / (value * 1e6) * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "cells": cells},
+        "config": workload_config(args.workload, cells, args.gpus),
         "cpu_baseline": {"value": round(value, 3), "unit": "Mcell-steps/s", "cores": cpu_threads(),
                          "kind": "port",
                          "sample": f"{sample} full-grid steps of {args.workload} on the float32 C oracle "
@@ -389,6 +407,15 @@ def main():
     error = None
     if not args.no_validate:
         error = validate(device)
+    configs = None
+    if args.config_steps > 0:
+        configs = {name: measure_workload(device, name, args.config_steps) for name in ("sphere80", "lorentz192")}
+    full_run = None
+    if not args.no_full_run:
+        full_run = {name: bench_full_run(device, name) for name in ("sphere80", "sphere192_8dft", "lorentz192")}
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = adjoint_section(args)
     served = None
     if args.serving > 0:
         served = bench_serving(device, args)
@@ -406,15 +433,15 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 5),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": args.workload, "cells": cells, "parallelism": f"replicas{world}",
-                   "l2": "inputs larger than L2 (no flush needed)",
-                   "kernels": {"h_half": family_name(choice[0]) if choice else None,
-                               "e_half": family_name(choice[1]) if choice else None,
-                               "choice": choice, "chosen_by": "argument" if kernels else "autotuner"},
-                   "monitors": {"flux_planes": len(flux), "dft_volumes": len(dft),
-                                "decimation": [m.decimation_factor for m in list(flux) + list(dft)][:1]}},
+        "config": workload_config(args.workload, cells, world),
+        "kernels": {"h_half": family_name(choice[0]) if choice else None,
+                    "e_half": family_name(choice[1]) if choice else None,
+                    "choice": choice, "chosen_by": "argument" if kernels else "autotuner"},
+        "monitors": {"flux_planes": len(flux), "dft_volumes": len(dft),
+                     "decimation": [m.decimation_factor for m in list(flux) + list(dft)][:1]},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-        "clocks": clocks.summary(), "error": error, "serving": served, "lossy": lossy, "mirror": mirror, "complex": complex_,
+        "clocks": clocks.summary(), "error": error, "configs": configs, "full_run": full_run,
+        "adjoint": adjoint, "serving": served, "lossy": lossy, "mirror": mirror, "complex": complex_,
     }
     print(json.dumps(line), flush=True)
 
@@ -472,11 +499,17 @@ def bench_serving(device, args):
 
 
 def bench_adjoint(args):
+    """``--adjoint``: the adjoint section alone, as one JSON line."""
+    print(json.dumps(adjoint_section(args)), flush=True)
+
+
+def adjoint_section(args) -> dict:
     """96^3 adjoint gradient: forward with checkpoints, backward, float64 finite differences.
 
-    Prints one JSON line: the objective, the timing of forward and backward (CUDA events
-    around each), and the agreement with central differences (h = 1e-3) of the float64
-    oracle on ``--fd-voxels`` seeded voxels and along one seeded direction over the box.
+    The objective, the timing of forward and backward (CUDA events around each), and the
+    agreement with central differences (h = 1e-3) of the float64 oracle on seeded voxels
+    and along one seeded direction over the box (read from the committed fixture when
+    present, else computed with ``--fd-voxels`` voxels).
     """
     import torch
 
@@ -559,8 +592,8 @@ def bench_adjoint(args):
         "data": "synthetic (seeded eps ~ U[1,12])",
         "reference_adjoint": "unavailable: the reference has no adjoint gradient",
     }
-    print(json.dumps(line), flush=True)
     problem.close()
+    return line
 
 
 def bench_dft(args):
@@ -619,6 +652,116 @@ def bench_dft(args):
     print(json.dumps(line), flush=True)
 
 
+def measure_workload(device, name: str, steps: int, kernel_steps: int = 20) -> dict:
+    """One workload device-resident: ``steps`` steps timed with CUDA events on the
+    launching stream after 3 warm-up steps, then each half timed launch by launch over
+    ``kernel_steps`` steps; per-half and whole-step roofline against the measured HBM
+    peak, with the clocks sampled during the timed steps."""
+    import torch
+
+    from meep_gpu_gb300 import FdtdDriver, workloads
+
+    peak, _ = measured_peaks()
+    stream = torch.cuda.current_stream(device)
+    driver, _, _ = workloads.build(name, FdtdDriver)
+    driver.step_many(3)
+    engine = driver.engine
+    first = driver.step_count
+    engine.ensure_source_words(first, steps + kernel_steps)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(device)
+    with ClockSampler(device.index or 0) as clocks:
+        start.record(stream)
+        engine.step(first, steps)
+        end.record(stream)
+        torch.cuda.synchronize(device)
+    ms = start.elapsed_time(end) / steps
+    n0 = first + steps
+    events = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(kernel_steps)]
+    for t, ev in enumerate(events):
+        ev[0].record(stream)
+        engine.launch(n0 + t, 0, stream)
+        ev[1].record(stream)
+        engine.launch(n0 + t, 1, stream)
+        ev[2].record(stream)
+    torch.cuda.synchronize(device)
+    nbytes = engine.algorithmic_bytes()
+    halves = {}
+    for part, key in enumerate(("h_half", "e_half")):
+        half_ms = float(np.mean([ev[part].elapsed_time(ev[part + 1]) for ev in events]))
+        gbs = nbytes[key] / (half_ms / 1e3) / 1e9
+        halves[key] = {"ms": round(half_ms, 4), "GB/s": round(gbs, 1), "frac": round(gbs / peak, 4)}
+    cells = driver.grid.total_cells
+    step_bytes = nbytes["h_half"] + nbytes["e_half"]
+    out = {"value": round(cells / (ms / 1e3) / 1e6, 3), "unit": "Mcell-steps/s", "cells": cells,
+           "ms_per_step": round(ms, 5), "steps": steps, "step_bytes_per_cell": round(step_bytes / cells, 2),
+           "step_frac": round(step_bytes / (ms / 1e3) / 1e9 / peak, 4), "per_kernel": halves,
+           "kernels": [list(c) for c in engine.choice] if engine.choice is not None else None,
+           "clocks": clocks.summary()}
+    if engine.nonfinite():
+        raise RuntimeError(f"the {name} run wrote a non-finite field")
+    driver.close()
+    del driver, engine
+    torch.cuda.empty_cache()
+    return out
+
+
+def bench_full_run(device, name: str) -> dict:
+    """A configuration's whole run at its stated step count, every monitor included.
+
+    ``device``: steps 0 .. N-1 of a fresh driver (kernels chosen at the freeze on a
+    scratch copy) timed with CUDA events, with every DFT sample, contraction and the
+    final read of every spectrum inside the window. ``e2e``: the same run through the
+    public API from host arrays (``FdtdDriver``: configure, ``run(num_steps=N)`` with its
+    default checks, read every flux spectrum and DFT array), on the wall clock.
+    """
+    import torch
+
+    from meep_gpu_gb300 import FdtdDriver, workloads
+
+    total = workloads.STEPS[name]
+    stream = torch.cuda.current_stream(device)
+    driver, flux, dft = workloads.build(name, FdtdDriver)
+    engine = driver.freeze()
+    engine.ensure_source_words(0, total)
+    launches = step_launches(engine, 0, total)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(device)
+    with ClockSampler(device.index or 0) as clocks:
+        start.record(stream)
+        engine.step(0, total)
+        driver.step_count = total
+        spectra = [engine.queue_flux_spectrum(m) for m in flux]
+        arrays = [engine.device_accumulator(m, q) for m in dft for q in range(len(m.components))]
+        end.record(stream)
+        torch.cuda.synchronize(device)
+    ms = start.elapsed_time(end)
+    cells = driver.grid.total_cells
+    finite = all(bool(torch.isfinite(a).all()) for a in arrays)
+    driver.close()
+    del driver, engine, spectra, arrays
+    torch.cuda.empty_cache()
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    d2, f2, v2 = workloads.build(name, FdtdDriver)
+    d2.run(num_steps=total)
+    results = [m.get_flux_spectrum() for m in f2]
+    host = [m.raw(c) for m in v2 for c in m.components]
+    wall = time.perf_counter() - t0
+    d2h = sum(r.nbytes for r in results) + sum(a.nbytes for a in host)
+    d2.close()
+    del d2
+    torch.cuda.empty_cache()
+    return {"steps": total, "cells": cells, "ms": round(ms, 2),
+            "value": round(cells * total / (ms / 1e3) / 1e6, 1), "unit": "Mcell-steps/s",
+            "gpu_launches": launches, "monitors": {"flux_planes": len(flux), "dft_volumes": len(dft)},
+            "finite": finite, "clocks": clocks.summary(),
+            "e2e": {"value": round(cells * total / wall / 1e6, 1), "unit": "Mcell-steps/s", "wall_s": round(wall, 3),
+                    "d2h_bytes": d2h,
+                    "what": "FdtdDriver from host arrays: configure, run(num_steps) with its default checks, "
+                            "read every spectrum and DFT array"}}
+
+
 def bench_lossy(device, args):
     """The lossy kernels on the 192^3 absorber and lossy-PML workloads: device-resident
     throughput over K steps, each half's roofline, and the float64 error of the 40^3
@@ -628,51 +771,7 @@ def bench_lossy(device, args):
     from meep_gpu_gb300 import FdtdDriver, workloads
     from oracle.oracle import Oracle, problem_from_driver
 
-    out = {}
-    peak, _ = measured_peaks()
-    stream = torch.cuda.current_stream(device)
-    for name in ("absorber192", "lossy_pml192"):
-        driver, _, _ = workloads.build(name, FdtdDriver)
-        driver.step_many(3)
-        engine = driver.engine
-        first, steps = driver.step_count, args.lossy_steps
-        engine.ensure_source_words(first, steps + 20)
-        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize(device)
-        with ClockSampler(device.index or 0) as clocks:
-            start.record(stream)
-            engine.step(first, steps)
-            end.record(stream)
-            torch.cuda.synchronize(device)
-        ms = start.elapsed_time(end) / steps
-        n0 = first + steps
-        events = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(20)]
-        for t, ev in enumerate(events):
-            ev[0].record(stream)
-            engine.launch(n0 + t, 0, stream)
-            ev[1].record(stream)
-            engine.launch(n0 + t, 1, stream)
-            ev[2].record(stream)
-        torch.cuda.synchronize(device)
-        nbytes = engine.algorithmic_bytes()
-        halves = {}
-        for part, key in enumerate(("h_half", "e_half")):
-            half_ms = float(np.mean([ev[part].elapsed_time(ev[part + 1]) for ev in events]))
-            gbs = nbytes[key] / (half_ms / 1e3) / 1e9
-            halves[key] = {"ms": round(half_ms, 4), "GB/s": round(gbs, 1), "frac": round(gbs / peak, 4)}
-        cells = driver.grid.total_cells
-        step_bytes = nbytes["h_half"] + nbytes["e_half"]
-        out[name] = {"value": round(cells / (ms / 1e3) / 1e6, 3), "unit": "Mcell-steps/s",
-                     "ms_per_step": round(ms, 5), "steps": steps,
-                     "step_bytes_per_cell": round(step_bytes / cells, 2),
-                     "step_frac": round(step_bytes / (ms / 1e3) / 1e9 / peak, 4),
-                     "per_kernel": halves, "kernels": [list(c) for c in engine.choice],
-                     "clocks": clocks.summary()}
-        if engine.nonfinite():
-            raise RuntimeError(f"the {name} run wrote a non-finite field")
-        driver.close()
-        del driver, engine
-        torch.cuda.empty_cache()
+    out = {name: measure_workload(device, name, args.lossy_steps) for name in ("absorber192", "lossy_pml192")}
     steps = workloads.STEPS["lossy40"]
     gpu, flux, _ = workloads.build("lossy40", FdtdDriver)
     gpu.run(num_steps=steps, progress_interval=steps)
@@ -892,7 +991,48 @@ def validate(device):
         "fields_rel_l2_vs_f64": float(math.sqrt(num / den)),
         "flux_rel_vs_f64": float(np.max(np.abs(got - expected)) / np.max(np.abs(expected)))}
     gpu.close()
+    out["sphere192_8dft_600_steps"] = headline_error(600)
     return out
+
+
+def headline_error(steps: int) -> dict:
+    """The timed workload's own error: the 192^3 eight-DFT case after ``steps`` steps
+    against the float64 oracle (fields relative L2 over E and H; each flux plane's
+    largest deviation relative to its peak; each DFT volume's relative L2)."""
+    from meep_gpu_gb300 import FdtdDriver, workloads
+    from oracle.oracle import Oracle, problem_from_driver
+
+    os.environ.setdefault("OMP_NUM_THREADS", str(cpu_threads()))
+    gpu, flux, dft = workloads.build("sphere192_8dft", FdtdDriver)
+    gpu.run(num_steps=steps, progress_interval=steps)
+    ref, _, _ = workloads.build("sphere192_8dft", FdtdDriver)
+    t0 = time.perf_counter()
+    o64 = Oracle(problem_from_driver(ref), "f64")
+    o64.run(steps)
+    oracle_s = time.perf_counter() - t0
+    num = den = 0.0
+    for c in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz"):
+        a = gpu.get_field(c, cell_centered=False).astype(np.float64)
+        b = o64.field(c)
+        num += float(np.sum((a - b) ** 2))
+        den += float(np.sum(b ** 2))
+    flux_err = []
+    for index, monitor in enumerate(flux):
+        expected = o64.flux_spectrum(index)
+        flux_err.append(float(np.max(np.abs(monitor.get_flux_spectrum() - expected)) / np.max(np.abs(expected))))
+    dft_err = []
+    for index, monitor in enumerate(dft):
+        n2 = d2 = 0.0
+        for c in monitor.components:
+            expected = o64.dft(len(flux) + index, c)
+            got = monitor.raw(c).reshape(expected.shape).astype(np.complex128)
+            n2 += float(np.sum(np.abs(got - expected) ** 2))
+            d2 += float(np.sum(np.abs(expected) ** 2))
+        dft_err.append(float(math.sqrt(n2 / d2)) if d2 > 0 else 0.0)
+    gpu.close()
+    return {"fields_rel_l2_vs_f64": float(math.sqrt(num / den)), "flux_rel_vs_f64_max": max(flux_err),
+            "flux_rel_vs_f64": flux_err, "dft_rel_l2_vs_f64": dft_err,
+            "oracle_seconds": round(oracle_s, 1), "oracle_threads": cpu_threads()}
 
 
 if __name__ == "__main__":

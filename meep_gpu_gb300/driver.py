@@ -320,8 +320,10 @@ class FdtdDriver:
                 volumes.append(None)
                 continue
             volume = np.ascontiguousarray(self._volume(value, "sigma").astype(np.float32))
-            if not np.all(np.isfinite(volume)):
-                raise ValueError("sigma must be finite")
+            if not np.all(np.isfinite(volume)) or np.any(volume < 0):
+                # reference dispersion.py:623: a negative sigma is gain
+                raise ValueError("sigma must be finite and >= 0 in every cell: a negative sigma is gain, which "
+                                 "grows the field while every magnitude still looks reasonable")
             volumes.append(volume if np.any(volume != 0) else None)
         radius = susceptibility.stability_radius(self.grid.dt)
         if radius > 1.0 + 1e-12:

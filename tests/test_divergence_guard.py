@@ -2,9 +2,14 @@
 meep_gpu/driver.py:747-792; energy ``_field_energy`` :3634; interval 20 and limit 1e3,
 :319-320).
 
-On the host the guard is fed energy sequences; on the GPU a Lorentz slab with gain
-(negative sigma) grows smoothly while staying finite and is stopped by the guard, a
-passive one is not, and the device reduction equals the same sum formed on the host.
+On the host the guard is fed energy sequences (growth while the sources emit, a runaway
+after they stop, decay, non-finite values). The reference's guard compares each sample
+after the sources with the running maximum of every sample before it, so it stops a
+jump of more than 1e3 times within one interval and an energy that is no longer finite.
+On the GPU a driven Lorentz slab whose energy overflows float32 while every field word is
+still finite is stopped at the guard's first sample, a passive one runs through, and the
+device reduction equals the same sum formed on the host. Gain (negative sigma) is refused
+as the reference refuses it.
 """
 
 import math
@@ -82,33 +87,42 @@ def test_guard_samples_only_at_multiples_of_the_interval():
     assert calls == [20, 40, 60]
 
 
-def gain_slab(sigma):
+def lorentz_slab(sigma=1.5, amplitude=1.0, continuous=False):
     d = FdtdDriver((1.6, 1.4, 1.5), 10, force_complex_fields=False, boundaries="metallic")
     d.setup_pml(3)
     x, y, z = d.grid.meshgrid()
     slab = np.abs(x) < 0.2
     d.set_epsilon(np.where(slab, 2.25, 1.0))
     d.add_susceptibility(Susceptibility(frequency=1.1, gamma=0.05), np.where(slab, sigma, 0.0))
-    d.add_source({"source_type": "gaussian", "component": "Ez", "center": (-0.4, 0.0, 0.0),
-                  "size": (0, 0, 0), "frequency": 0.8, "fwidth": 1.0})
+    spec = {"component": "Ez", "center": (-0.4, 0.0, 0.0), "size": (0, 0, 0), "frequency": 0.8,
+            "amplitude": amplitude}
+    spec.update({"source_type": "continuous"} if continuous else {"source_type": "gaussian", "fwidth": 1.0})
+    d.add_source(spec)
     return d
 
 
+def test_gain_is_refused_as_the_reference_refuses_it():
+    d = FdtdDriver((1.6, 1.4, 1.5), 10, force_complex_fields=False, boundaries="metallic")
+    with pytest.raises(ValueError, match="negative sigma is gain"):
+        d.add_susceptibility(Susceptibility(frequency=1.1, gamma=0.05), -0.2)
+
+
 @pytest.mark.gpu
-def test_gain_slab_is_stopped_while_finite(gpu):
-    d = gain_slab(-0.2)
-    with pytest.raises(FdtdDivergence, match="grew"):
-        d.run(num_steps=2000)
-    # the sources stop at t = 10 (step 200); the float32 oracle's energy passes 1e3 times
-    # the peak at t = 20
-    assert d.step_count == 400
+def test_energy_overflow_is_stopped_while_the_field_is_finite(gpu):
+    """A field driven past 1.8e19 overflows its float32 energy terms while every E word
+    is still finite: the guard raises at its first sample, the E detector would not."""
+    d = lorentz_slab(amplitude=1e24, continuous=True)
+    with pytest.raises(FdtdDivergence, match="not finite"):
+        d.run(num_steps=400)
+    assert d.step_count == STABILITY_CHECK_INTERVAL
     assert not d.engine.nonfinite()
+    assert np.isfinite(d.get_field("Ez", cell_centered=False)).all()
     d.close()
 
 
 @pytest.mark.gpu
 def test_passive_slab_runs_through(gpu):
-    d = gain_slab(1.5)
+    d = lorentz_slab()
     d.run(num_steps=1000, progress_interval=300)
     assert d.step_count == 1000
     d.close()
@@ -116,7 +130,7 @@ def test_passive_slab_runs_through(gpu):
 
 @pytest.mark.gpu
 def test_device_energy_is_the_host_sum(gpu):
-    d = gain_slab(1.5)
+    d = lorentz_slab()
     d.run(num_steps=150)
     energy = d.field_energy()
     eps = 1.0 / d.engine.inv_eps[0].cpu().numpy().astype(np.float64)

@@ -2,6 +2,7 @@
 entry point that takes caller scratch: identical words, twice in a row, across sizes,
 with no device memory taken by the calls."""
 
+import gc
 import re
 from pathlib import Path
 
@@ -69,14 +70,22 @@ def test_noalloc_equals_the_scratch_entry_point_twice_in_a_row(gpu):
                                              scratch.numel() * 4, stream))
         outputs = [acc0.clone(), acc0.clone()]
         # one call first (its device's table address is looked up), then two more with
-        # the caching allocator's counters unchanged across them
-        _lib.check(lib, lib.mgb_dft_contract_noalloc(samples.data_ptr(), *args, acc0.clone().data_ptr(), stream))
+        # the caching allocator's counters unchanged across them (the garbage collector
+        # held off, so no tensor of an earlier test is freed in between)
+        warm = acc0.clone()
+        _lib.check(lib, lib.mgb_dft_contract_noalloc(samples.data_ptr(), *args, warm.data_ptr(), stream))
         torch.cuda.synchronize()
-        allocated, reserved = torch.cuda.memory_allocated(), torch.cuda.memory_reserved()
-        for got in outputs:
-            _lib.check(lib, lib.mgb_dft_contract_noalloc(samples.data_ptr(), *args, got.data_ptr(), stream))
-        torch.cuda.synchronize()
-        assert (torch.cuda.memory_allocated(), torch.cuda.memory_reserved()) == (allocated, reserved)
+        gc.collect()
+        gc.disable()
+        try:
+            allocated, reserved = torch.cuda.memory_allocated(), torch.cuda.memory_reserved()
+            for got in outputs:
+                _lib.check(lib, lib.mgb_dft_contract_noalloc(samples.data_ptr(), *args, got.data_ptr(), stream))
+            torch.cuda.synchronize()
+            after = (torch.cuda.memory_allocated(), torch.cuda.memory_reserved())
+        finally:
+            gc.enable()
+        assert after == (allocated, reserved)
         for got in outputs:
             assert torch.equal(got, expected), (nfreq, ncols, nsamples)
         assert not torch.equal(expected, acc0)

@@ -163,7 +163,9 @@ typedef struct mgb_sim_desc {
   mgb_monitor monitors[MGB_MAX_MONITORS];
   /* status word: the E half ORs 1 into it when it writes a NaN/Inf E; a tile kernel ORs
    * 2 when a wait for its own shared-memory copies exceeds its time limit (the kernel
-   * then stops stepping instead of spinning). */
+   * then stops stepping instead of spinning); a contraction ORs 4 when its tensor-core
+   * wait runs out; the wavefront kernel ORs 8 when a wait for the chunks it reads runs
+   * out (every later item of that launch is skipped). */
   int32_t* status; /* device, may be NULL */
   /* D and B conductivity, NULL for a lossless run; the library keeps a copy. A run with
    * a conductivity steps with the generic kernels (family 0 or 4) and is refused by the
@@ -286,6 +288,27 @@ int mgb_select_kernels(mgb_sim* sim, int32_t family);
  * pair computes the same words. No reference counterpart. */
 int mgb_select_half(mgb_sim* sim, int32_t part, int32_t family, int32_t block_z, int32_t block_y,
                     int32_t x_chunk);
+
+/* ---- Wavefront stepping --------------------------------------------------------------
+ * Runs of steps in one persistent launch: resident CTAs take (step, half, x chunk, (y, z)
+ * tile) items in a skewed order that lets `window` consecutive steps pass over a chunk
+ * while its neighbourhood is in L2, each item starting when the chunks it reads are done
+ * (per-chunk completion counters; every wait is bounded, status bit 8 when one runs out).
+ * The words are those of the launch-per-half kernels. Runs end after each step on which a
+ * monitor is due (the monitor kernels run between launches). For runs without mirror
+ * folds, Bloch phases or a conductivity, on a metallic x axis. No reference counterpart:
+ * the reference launches one kernel per slot and step. */
+
+/* Bytes of the caller's wave buffer for chunks of x_chunk planes, blocks of `window`
+ * steps (1..16) and runs of at most max_steps steps (0 for bad arguments). */
+size_t mgb_wave_bytes(mgb_sim* sim, int32_t x_chunk, int32_t window, int32_t max_steps);
+
+/* Step with the wavefront path from now on: block_z (a multiple of 32) x block_y columns per
+ * tile, x_chunk planes per chunk; buffer (device, 256-byte aligned, at least
+ * mgb_wave_bytes() bytes, owned by the caller and used by every later mgb_step). Its item
+ * table is written on `stream`. buffer NULL switches the path off. */
+int mgb_set_wave(mgb_sim* sim, int32_t block_z, int32_t block_y, int32_t x_chunk, int32_t window,
+                 int32_t max_steps, void* buffer, size_t bytes, void* stream);
 
 /* Release the plan (never the caller's arrays). */
 void mgb_destroy(mgb_sim* sim);

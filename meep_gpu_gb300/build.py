@@ -1,8 +1,11 @@
 """Build recipe of the CUDA library ``libmeepgb.so`` (sm_103a, in-tree).
 
-Two translation units (the stepping library and the tensor-core DFT contraction)
-compiled by nvcc straight into a shared object next to this file. ``-fmad=false`` is part of the numerics contract: no multiply-add may be
-contracted, so every float32 word matches the reference's separately rounded
+Three translation units compiled by nvcc in parallel and linked into a shared object next
+to this file: the stepping library, the tensor-core DFT contraction and the wavefront
+step kernel. The wavefront unit caches every global load in L2 only (``-dlcm=cg``): its
+persistent CTAs read words other SMs rewrote during the same launch, and L1 is not
+coherent with them. ``-fmad=false`` is part of the numerics contract: no multiply-add may
+be contracted, so every float32 word matches the reference's separately rounded
 operations.
 """
 
@@ -16,10 +19,13 @@ from pathlib import Path
 
 PACKAGE = Path(__file__).resolve().parent
 ROOT = PACKAGE.parent
-SOURCES = [PACKAGE / "csrc" / "meepgb.cu", PACKAGE / "csrc" / "dft_tc.cu"]
-HEADERS = [PACKAGE / "csrc" / "dft_tc.cuh"]
+CSRC = PACKAGE / "csrc"
+SOURCES = [CSRC / "meepgb.cu", CSRC / "dft_tc.cu", CSRC / "wave.cu"]
+HEADERS = [CSRC / "dft_tc.cuh", CSRC / "step_device.cuh", CSRC / "wave.cuh"]
 LIBRARY = PACKAGE / "libmeepgb.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# extra flags per translation unit
+UNIT_FLAGS = {"wave.cu": ["-Xptxas", "-dlcm=cg"]}
 
 
 def nvcc() -> str:
@@ -44,14 +50,28 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     """Compile ``libmeepgb.so`` unless it is newer than every input."""
     if not force and not stale():
         return LIBRARY
-    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-fmad=false", "-std=c++17",
-           "-Xcompiler", "-fPIC", "-shared", "-I", str(ROOT / "include"),
-           "-o", str(LIBRARY) + ".tmp", *map(str, SOURCES)]
+    common = [*ARCH, "-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
+              "-I", str(ROOT / "include")]
     if verbose:
-        cmd.insert(1, "-Xptxas=-v")
-        print(" ".join(cmd), file=sys.stderr)
-    subprocess.run(cmd, check=True)
+        common.append("-Xptxas=-v")
+    objects, procs = [], []
+    for source in SOURCES:
+        obj = PACKAGE / (source.stem + ".o")
+        cmd = [nvcc(), *common, *UNIT_FLAGS.get(source.name, []), "-c", str(source), "-o", str(obj) + ".tmp"]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        procs.append((subprocess.Popen(cmd), cmd))
+        objects.append(obj)
+    failed = [cmd for proc, cmd in procs if proc.wait() != 0]
+    if failed:
+        raise subprocess.CalledProcessError(1, failed[0])
+    for obj in objects:
+        os.replace(str(obj) + ".tmp", obj)
+    link = [nvcc(), *ARCH, "-shared", "-Xcompiler", "-fPIC", "-o", str(LIBRARY) + ".tmp", *map(str, objects)]
+    subprocess.run(link, check=True)
     os.replace(str(LIBRARY) + ".tmp", LIBRARY)
+    for obj in objects:
+        obj.unlink()
     return LIBRARY
 
 

@@ -54,6 +54,13 @@ AUTOTUNE_CANDIDATES = ((0, 32, 4, 4), (0, 32, 8, 4), (0, 32, 4, 8), (0, 64, 2, 8
                        (4, 32, 8, 2), (4, 32, 8, 8), (4, 64, 4, 4), (4, 16, 16, 4), (4, 32, 2, 4),
                        (5, 32, 4, 4), (5, 16, 8, 4), (5, 32, 4, 8), (5, 32, 2, 8), (5, 32, 4, 2))
 _AUTOTUNE_CACHE: Dict[tuple, Tuple[int, int, int, int]] = {}
+# Wavefront choices the autotuner times against the best pair of per-half kernels:
+# (block_z, block_y, x_chunk, window), as kernel choice (6, block_z, block_y, x_chunk, window).
+WAVE_CANDIDATES = ((32, 4, 4, 3), (32, 4, 4, 4), (32, 8, 4, 3), (32, 4, 2, 4), (32, 4, 2, 6), (64, 4, 4, 3),
+                   (32, 4, 8, 2))
+WAVE_FAMILY = 6
+# Steps one wavefront launch may hold (the length of the counter table).
+WAVE_MAX_STEPS = 256
 
 
 def autotune_key(grid: Grid, pml: Optional[PML], npoles: int, ninv: int, lossy: bool = False) -> tuple:
@@ -207,6 +214,8 @@ class Engine:
         self._setup_monitors()
         self._pole_specs = list(poles)
         self.choice = None
+        self.wave = None
+        self.wave_buffer = None
         self.handle = None
         self._words: Optional[torch.Tensor] = None
         self._words_first = 0
@@ -529,9 +538,46 @@ class Engine:
         """Whether the plan steps with the TMA tile kernels (else the generic ones)."""
         return bool(self.lib.mgb_uses_tiles(self.handle))
 
+    @property
+    def wave_eligible(self) -> bool:
+        """Whether the wavefront path can step this plan (metallic x, no folds, no Bloch
+        phase, no conductivity)."""
+        grid = self.grid
+        return (grid.is_metallic(0) and not grid.has_symmetry and not grid.has_bloch
+                and not self.conductivity)
+
+    def set_wave(self, choice: Optional[Tuple[int, int, int, int]]) -> None:
+        """Step with the wavefront path, (block_z, block_y, x_chunk, window), or leave it
+        (None). The counter buffer is this engine's (a torch allocation)."""
+        stream = self._stream_handle()
+        if choice is None:
+            _lib.check(self.lib, self.lib.mgb_set_wave(self.handle, 32, 4, 4, 1, 1, None, 0, stream))
+            self.wave = None
+            self.wave_buffer = None
+            return
+        bz, by, xc, window = (int(v) for v in choice)
+        nbytes = self.lib.mgb_wave_bytes(self.handle, xc, window, WAVE_MAX_STEPS)
+        if nbytes == 0:
+            raise ValueError(f"bad wavefront choice {choice}")
+        buffer = torch.empty(nbytes + 256, dtype=torch.uint8, device=self.device)
+        offset = (-buffer.data_ptr()) % 256
+        _lib.check(self.lib, self.lib.mgb_set_wave(self.handle, bz, by, xc, window, WAVE_MAX_STEPS,
+                                                   buffer.data_ptr() + offset, nbytes, stream))
+        self.wave = (bz, by, xc, window)
+        self.wave_buffer = buffer
+
     def select(self, choice) -> None:
         """Apply a kernel choice: one (family, block_z, block_y, x_chunk) for both halves,
-        or a pair of them (H half, E half)."""
+        or a pair of them (H half, E half); (6, block_z, block_y, x_chunk, window) steps
+        with the wavefront path (the halves keep their choice for single launches)."""
+        if len(choice) == 5 and int(choice[0]) == WAVE_FAMILY:
+            self.set_wave(tuple(int(v) for v in choice[1:]))
+            return
+        if len(choice) == 3 and isinstance(choice[0], (tuple, list)):
+            # (H half, E half, wavefront choice or None): an autotuned result
+            self.select((choice[0], choice[1]))
+            self.set_wave(choice[2])
+            return
         if len(choice) == 2 and isinstance(choice[0], (tuple, list)):
             h, e = (tuple(int(v) for v in c) for c in choice)
         else:
@@ -595,12 +641,46 @@ class Engine:
                 ms = float(np.min([ev[part].elapsed_time(ev[part + 1]) for ev in marks]))
                 if ms < best_ms[part]:
                     best[part], best_ms[part] = choice, ms
+        wave = None
+        if self.wave_eligible and os.environ.get("MEEPGB_WAVE", "1") != "0":
+            wave = self._tune_wave(scratch, (best[0], best[1]), stream)
         scratch.close()
         del scratch
-        _AUTOTUNE_CACHE[key] = (best[0], best[1])
-        self.select((best[0], best[1]))
+        _AUTOTUNE_CACHE[key] = (best[0], best[1], wave)
+        self.select((best[0], best[1], wave))
         self.autotune_ms = best_ms[0] + best_ms[1]
         return self.choice
+
+    def _tune_wave(self, scratch: "Engine", halves, stream, steps: int = 24):
+        """The fastest wavefront choice, if it steps a run of ``steps`` steps faster than
+        the chosen pair of per-half kernels (whole steps timed with CUDA events)."""
+        def run_ms() -> float:
+            scratch.step(0, 4)
+            start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            best_ms = float("inf")
+            for _ in range(2):
+                start.record(stream)
+                scratch.step(4, steps)
+                end.record(stream)
+                end.synchronize()
+                best_ms = min(best_ms, start.elapsed_time(end))
+            return best_ms
+
+        scratch.select(halves)
+        scratch.set_wave(None)
+        best, best_ms = None, run_ms()
+        for choice in WAVE_CANDIDATES:
+            try:
+                scratch.set_wave(choice)
+            except (_lib.MeepGBError, ValueError):
+                continue
+            ms = run_ms()
+            if scratch.device_status_word() & self.STATUS_WAVE_TIMEOUT:
+                raise RuntimeError("a wavefront wait ran out on the device while the autotuner timed it")
+            if ms < best_ms:
+                best, best_ms = choice, ms
+        scratch.set_wave(None)
+        return best
 
     def launch(self, step: int, part: int, stream=None) -> None:
         """Launch one kernel of one step: 0 the H half, 1 the E half, 2 the monitors."""
@@ -639,18 +719,26 @@ class Engine:
         return {"h_half": word * h, "e_half": word * e}
 
     # status bits the kernels set: 1 a non-finite E was written; 2 a tile kernel's wait
-    # for its shared-memory copies timed out; 4 a tensor-core contraction's wait timed out
-    STATUS_NONFINITE, STATUS_TILE_TIMEOUT, STATUS_MMA_TIMEOUT = 1, 2, 4
+    # for its shared-memory copies timed out; 4 a tensor-core contraction's wait timed out;
+    # 8 a wavefront kernel's wait for the chunks it reads timed out
+    STATUS_NONFINITE, STATUS_TILE_TIMEOUT, STATUS_MMA_TIMEOUT, STATUS_WAVE_TIMEOUT = 1, 2, 4, 8
+
+    def device_status_word(self) -> int:
+        """The raw status word (one small device-to-host read)."""
+        return int(self.status.item())
 
     def device_status(self) -> int:
         """The status word (one small device-to-host read); raises if a kernel timed out."""
         word = int(self.status.item())
-        if word & (self.STATUS_TILE_TIMEOUT | self.STATUS_MMA_TIMEOUT):
+        timeouts = self.STATUS_TILE_TIMEOUT | self.STATUS_MMA_TIMEOUT | self.STATUS_WAVE_TIMEOUT
+        if word & timeouts:
             what = []
             if word & self.STATUS_TILE_TIMEOUT:
                 what.append("a tile kernel's wait for its staged planes")
             if word & self.STATUS_MMA_TIMEOUT:
                 what.append("a tensor-core contraction's wait for its MMAs")
+            if word & self.STATUS_WAVE_TIMEOUT:
+                what.append("a wavefront kernel's wait for the chunks it reads")
             raise RuntimeError(f"{' and '.join(what)} timed out on the device; the results of "
                                "the steps since the last check are not valid")
         return word
@@ -771,9 +859,10 @@ class ComplexEngine:
                     engine.desc.partner_E[q] = partner.fields["E" + axis].data_ptr()
                     engine.desc.partner_H[q] = partner.fields["H" + axis].data_ptr()
         self.re.finish()
-        self.im._finish_args = (self.im._finish_args[0],
-                                self.re.choice if self.re.choice is not None else kernels,
-                                launch_shape, False)
+        im_choice = kernels
+        if self.re.choice is not None:
+            im_choice = (self.re.choice[0], self.re.choice[1], self.re.wave)
+        self.im._finish_args = (self.im._finish_args[0], im_choice, launch_shape, False)
         self.im.finish()
         self.grid = grid
         self.device = self.re.device

@@ -30,8 +30,17 @@ GENERIC = (0, 32, 8, 4)
 PREFETCH = (2, 32, 4, 4)
 WARP_SPECIALIZED = ((2, 16, 8, 4), (3, 64, 8, 8))  # H prefetching, E warp-specialized tiles
 L2_PREFETCH = ((4, 32, 4, 4), (5, 16, 8, 4))  # families 0 / 2 with the x chunk prefetched into L2
+WAVE = (6, 32, 4, 4, 3)  # the wavefront path: 32 x 4 tiles, 4-plane chunks, 3-step blocks
 MODES = {"tiles": TILES, "generic": GENERIC, "prefetch": PREFETCH, "ws": WARP_SPECIALIZED,
-         "l2": L2_PREFETCH}
+         "l2": L2_PREFETCH, "wave": WAVE}
+
+
+def wave_steps(case) -> bool:
+    """Whether the wavefront path takes a case (metallic x, no folds, Bloch or conductivity)."""
+    boundaries = case.get("boundaries", "metallic")
+    x = boundaries if isinstance(boundaries, str) else boundaries[0]
+    return (x == "metallic" and not case.get("symmetry") and not case.get("k_point")
+            and not case.get("conductivity"))
 
 
 def gpu_case(case, steps=None, kernels=None, chunks=None):
@@ -58,7 +67,9 @@ def test_fields_are_the_reference_words(gpu, name, mode):
     case = CASES[name]
     gold = golden_io.fields(name)
     tileable = case["n"][2] % 4 == 0
-    if (case.get("conductivity") or case.get("k_point")) and mode not in ("generic", "l2"):
+    if mode == "wave" and not wave_steps(case):
+        pytest.skip("the wavefront path steps metallic-x runs without folds, Bloch phases or conductivity")
+    if (case.get("conductivity") or case.get("k_point")) and mode not in ("generic", "l2", "wave"):
         pytest.skip("lossy and Bloch-phased runs step with the generic kernels only (the others are refused)")
     if mode in ("tiles", "ws") and not tileable:
         mode = "generic"
@@ -67,6 +78,9 @@ def test_fields_are_the_reference_words(gpu, name, mode):
         kernels = (4, 32, 4, 4)  # lossy and Bloch-phased runs take families 0 and 4
     driver, flux, dft = gpu_case(case, kernels=kernels)
     assert driver.engine.uses_tiles == (mode in ("tiles", "ws"))
+    if mode == "wave":
+        engines = [driver.engine.re, driver.engine.im] if case.get("complex") else [driver.engine]
+        assert all(e.wave == WAVE[1:] for e in engines)
     for c in FIELDS:
         got = driver.get_field(c, cell_centered=False)
         mismatched = int(np.sum(got != gold[c]))
@@ -144,6 +158,7 @@ def test_sphere80_words_after_200_steps(gpu, mode):
     gold = golden_io.digest()
     driver, flux, _ = gpu_case(SPHERE80, steps=gold["steps"], kernels=MODES[mode])
     assert driver.engine.uses_tiles == (mode in ("tiles", "ws"))
+    assert (driver.engine.wave is not None) == (mode == "wave")
     for c, expected in gold["sha256"].items():
         words = np.ascontiguousarray(driver.get_field(c, cell_centered=False), dtype=np.float32)
         assert hashlib.sha256(words.tobytes()).hexdigest() == expected, c

@@ -92,6 +92,7 @@ def test_device_status_word_is_decoded():
     def fake(word):
         return types.SimpleNamespace(status=torch.tensor([word], dtype=torch.int32),
                                      STATUS_NONFINITE=1, STATUS_TILE_TIMEOUT=2, STATUS_MMA_TIMEOUT=4,
+                                     STATUS_WAVE_TIMEOUT=8,
                                      device_status=lambda: Engine.device_status(fake_obj[0]))
 
     fake_obj = [None]
@@ -99,10 +100,13 @@ def test_device_status_word_is_decoded():
         fake_obj[0] = fake(word)
         assert Engine.device_status(fake_obj[0]) == word
         assert Engine.nonfinite(fake_obj[0]) is diverged
-    for word in (2, 4, 6, 3):
+    for word in (2, 4, 6, 3, 8, 9):
         fake_obj[0] = fake(word)
         with pytest.raises(RuntimeError, match="timed out"):
             Engine.device_status(fake_obj[0])
+    fake_obj[0] = fake(8)
+    with pytest.raises(RuntimeError, match="wavefront"):
+        Engine.device_status(fake_obj[0])
 
 
 def test_magnetic_sources_take_their_current_at_the_whole_step():

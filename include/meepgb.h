@@ -303,12 +303,13 @@ int mgb_select_half(mgb_sim* sim, int32_t part, int32_t family, int32_t block_z,
  * steps (1..16) and runs of at most max_steps steps (0 for bad arguments). */
 size_t mgb_wave_bytes(mgb_sim* sim, int32_t x_chunk, int32_t window, int32_t max_steps);
 
-/* Step with the wavefront path from now on: block_z (a multiple of 32) x block_y columns per
+/* Step with the wavefront path from now on: the column marches of family 0 (plain loads) or
+ * 2 (the next plane's loads issued ahead), block_z (a multiple of 32) x block_y columns per
  * tile, x_chunk planes per chunk; buffer (device, 256-byte aligned, at least
  * mgb_wave_bytes() bytes, owned by the caller and used by every later mgb_step). Its item
  * table is written on `stream`. buffer NULL switches the path off. */
-int mgb_set_wave(mgb_sim* sim, int32_t block_z, int32_t block_y, int32_t x_chunk, int32_t window,
-                 int32_t max_steps, void* buffer, size_t bytes, void* stream);
+int mgb_set_wave(mgb_sim* sim, int32_t family, int32_t block_z, int32_t block_y, int32_t x_chunk,
+                 int32_t window, int32_t max_steps, void* buffer, size_t bytes, void* stream);
 
 /* Release the plan (never the caller's arrays). */
 void mgb_destroy(mgb_sim* sim);

@@ -145,8 +145,8 @@ SIGNATURES = {
                                        ctypes.c_int32, ctypes.c_int32]),
     "mgb_wave_bytes": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     "mgb_set_wave": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
-                                    ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_size_t,
-                                    ctypes.c_void_p]),
+                                    ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+                                    ctypes.c_size_t, ctypes.c_void_p]),
     "mgb_destroy": (None, [ctypes.c_void_p]),
     "mgb_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
     "mgb_dft_scratch_bytes": (ctypes.c_size_t, [ctypes.c_int32]),

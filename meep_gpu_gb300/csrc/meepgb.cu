@@ -1515,6 +1515,7 @@ struct mgb_sim {
     bool on = false;
     int bz = 32, by = 4, xchunk = 4, window = 4, max_steps = 0;
     int chunks = 0, tiles_z = 0, tiles_y = 0, blocks = 0;
+    int family = 0;  // 0 the plain column marches, 2 the prefetching ones
     unsigned* control = nullptr;
     unsigned* table = nullptr;
     unsigned* done = nullptr;
@@ -2145,7 +2146,7 @@ int step_wave(mgb_sim* sim, long long first, int nsteps, cudaStream_t s) {
     StepParams p = sim->step;
     p.l2pf = 0;
     p.src_words = nullptr;
-    err = mgbwave::launch_wave(p, w, wv.blocks, dim3(wv.bz, wv.by, 1), pml, msrc, s);
+    err = mgbwave::launch_wave(p, w, wv.blocks, dim3(wv.bz, wv.by, 1), wv.family, pml, msrc, s);
     if (err != cudaSuccess) return cuda_error(err, "wavefront step launch");
     const int rc = launch_part(sim, stop - 1, 2, s);  // the monitors due after the run's last step
     if (rc != MGB_OK) return rc;
@@ -2194,7 +2195,7 @@ size_t mgb_wave_bytes(mgb_sim* sim, int32_t x_chunk, int32_t window, int32_t max
   return wave_done_offset(window, chunks) + (size_t)max_steps * 2 * chunks * sizeof(unsigned);
 }
 
-int mgb_set_wave(mgb_sim* sim, int32_t block_z, int32_t block_y, int32_t x_chunk, int32_t window,
+int mgb_set_wave(mgb_sim* sim, int32_t family, int32_t block_z, int32_t block_y, int32_t x_chunk, int32_t window,
                  int32_t max_steps, void* buffer, size_t bytes, void* stream) {
   if (sim == nullptr) return fail(MGB_ERR_ARGUMENT, "null plan");
   if (buffer == nullptr) {
@@ -2207,6 +2208,7 @@ int mgb_set_wave(mgb_sim* sim, int32_t block_z, int32_t block_y, int32_t x_chunk
   if (!sim->desc.metallic[0])
     return fail(MGB_ERR_UNSUPPORTED, "the wavefront path needs a metallic x axis (a periodic x would make the "
                                      "first chunk wait on the last)");
+  if (family != 0 && family != 2) return fail(MGB_ERR_ARGUMENT, "the wavefront marches are family 0 or 2");
   if (block_z < 32 || block_z % 32 != 0 || block_y < 1 || block_z * block_y > 256)
     return fail(MGB_ERR_ARGUMENT, "block_z must be a multiple of 32 and block_z * block_y at most 256");
   const size_t need = mgb_wave_bytes(sim, x_chunk, window, max_steps);
@@ -2218,13 +2220,14 @@ int mgb_set_wave(mgb_sim* sim, int32_t block_z, int32_t block_y, int32_t x_chunk
   if (chunks >= (1 << 16)) return fail(MGB_ERR_ARGUMENT, "too many x chunks for the item table");
   const bool pml = sim->desc.pml_active != 0;
   const bool msrc = sim->step.nsrc_h > 0;
-  const int per_sm = mgbwave::wave_blocks_per_sm(block_z * block_y, pml, msrc);
+  const int per_sm = mgbwave::wave_blocks_per_sm(block_z * block_y, family, pml, msrc);
   int device = 0, sms = 0;
   if (per_sm <= 0 || cudaGetDevice(&device) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
     return launch_error("wavefront occupancy");
   mgb_sim::Wave& wv = sim->wave;
   unsigned char* base = static_cast<unsigned char*>(buffer);
+  wv.family = family;
   wv.bz = block_z;
   wv.by = block_y;
   wv.xchunk = x_chunk;

@@ -23,6 +23,13 @@ __device__ __forceinline__ unsigned load_acquire(const unsigned* at) {
   return v;
 }
 
+// Publish one completed tile: a release reduction, so the tile's stores (every thread's,
+// ordered before it by the CTA barrier) are visible to whoever reads the new count with
+// acquire semantics.
+__device__ __forceinline__ void add_release(unsigned* counter, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(counter), "r"(v) : "memory");
+}
+
 __device__ __forceinline__ unsigned long long now_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -48,40 +55,60 @@ __device__ __forceinline__ unsigned* done_at(const WaveArgs& w, int t, int half,
   return w.done + ((long long)t * 2 + half) * w.chunks + c;
 }
 
-template <bool PML, bool MSRC>
+// A tile's columns of one half: the plain marches (PF false) or the prefetching ones
+// (the next plane's loads issued ahead, z neighbours by shuffle), compiled for the axes
+// whose memberships the tile reaches, as the launch-per-half kernels do.
+template <bool PML, bool MSRC, bool PF>
 __device__ __forceinline__ void h_tile_march(const StepParams& p, int j, int k, int i0, int i1, int j0, int by,
                                              int k0, int bz, int first_step) {
   if (MSRC && cta_msrc(p, i0, i1, j0, by, k0, bz)) {
-    h_march<PML, false, -1, true>(p, j, k, i0, i1, first_step);
+    if (PF) h_march_pf<PML, -1, true>(p, j, k, i0, i1, first_step);
+    else h_march<PML, false, -1, true>(p, j, k, i0, i1, first_step);
     return;
   }
   if (!PML) {
-    h_march<false>(p, j, k, i0, i1, first_step);
+    if (PF) h_march_pf<false>(p, j, k, i0, i1, first_step);
+    else h_march<false>(p, j, k, i0, i1, first_step);
     return;
   }
-#define MGB_MARCH(AXV, PMLV) h_march<PMLV, false, AXV>(p, j, k, i0, i1, first_step)
-  MGB_AXES_SWITCH(cta_axes(p, i0, i1, j0, by, k0, bz), MGB_MARCH)
+  if (PF) {
+#define MGB_MARCH(AXV, PMLV) h_march_pf<PMLV, AXV>(p, j, k, i0, i1, first_step)
+    MGB_AXES_SWITCH(cta_axes(p, i0, i1, j0, by, k0, bz), MGB_MARCH)
 #undef MGB_MARCH
+  } else {
+#define MGB_MARCH(AXV, PMLV) h_march<PMLV, false, AXV>(p, j, k, i0, i1, first_step)
+    MGB_AXES_SWITCH(cta_axes(p, i0, i1, j0, by, k0, bz), MGB_MARCH)
+#undef MGB_MARCH
+  }
 }
 
-template <bool PML>
+template <bool PML, bool PF>
 __device__ __forceinline__ void e_tile_march(const StepParams& p, int j, int k, int i0, int i1, int j0, int by,
                                              int k0, int bz, int parity, const double* words) {
   if (!PML) {
-    e_march<false>(p, j, k, i0, i1, parity, words);
+    if (PF) e_march_pf<false>(p, j, k, i0, i1, parity, words);
+    else e_march<false>(p, j, k, i0, i1, parity, words);
     return;
   }
-#define MGB_MARCH(AXV, PMLV) e_march<PMLV, false, AXV>(p, j, k, i0, i1, parity, words)
-  MGB_AXES_SWITCH(cta_axes(p, i0, i1, j0, by, k0, bz), MGB_MARCH)
+  if (PF) {
+#define MGB_MARCH(AXV, PMLV) e_march_pf<PMLV, AXV>(p, j, k, i0, i1, parity, words)
+    MGB_AXES_SWITCH(cta_axes(p, i0, i1, j0, by, k0, bz), MGB_MARCH)
 #undef MGB_MARCH
+  } else {
+#define MGB_MARCH(AXV, PMLV) e_march<PMLV, false, AXV>(p, j, k, i0, i1, parity, words)
+    MGB_AXES_SWITCH(cta_axes(p, i0, i1, j0, by, k0, bz), MGB_MARCH)
+#undef MGB_MARCH
+  }
 }
 
-template <bool PML, bool MSRC>
-__global__ void __launch_bounds__(256, 4) wave_step(const __grid_constant__ StepParams params,
-                                                    const __grid_constant__ WaveArgs w) {
+template <bool PML, bool MSRC, bool PF>
+__global__ void __launch_bounds__(256, PF ? 3 : 4) wave_step(const __grid_constant__ StepParams params,
+                                                             const __grid_constant__ WaveArgs w) {
   // the parameters in shared memory: the source-word row changes with each item's step
   __shared__ StepParams sp;
-  __shared__ unsigned long long s_item;
+  // the next item, taken while the current one is worked on (two slots, alternating, so
+  // thread 0 never overwrites the one the other threads are still reading)
+  __shared__ unsigned long long s_item[2];
   __shared__ int s_go;
   const int tid = threadIdx.y * blockDim.x + threadIdx.x;
   const int nthreads = blockDim.x * blockDim.y;
@@ -90,19 +117,18 @@ __global__ void __launch_bounds__(256, 4) wave_step(const __grid_constant__ Step
     int* dst = reinterpret_cast<int*>(&sp);
     for (int at = tid; at < (int)(sizeof(StepParams) / sizeof(int)); at += nthreads) dst[at] = src[at];
   }
-  __syncthreads();
   const int bz = blockDim.x, by = blockDim.y;
   const int tiles = w.tiles_z * w.tiles_y;
   const unsigned long long per_block = (unsigned long long)w.window * 2 * w.chunks * tiles;
+  unsigned long long* queue = reinterpret_cast<unsigned long long*>(w.control);
   const unsigned* abort_flag = w.control + 2;
-  for (;;) {
-    if (tid == 0) {
-      // after a wait has run out anywhere, every CTA leaves at its next item
-      s_item = load_acquire(abort_flag) != 0 ? w.total
-                                            : atomicAdd(reinterpret_cast<unsigned long long*>(w.control), 1ull);
-    }
-    __syncthreads();
-    const unsigned long long v = s_item;
+  if (tid == 0) {
+    // after a wait has run out anywhere, every CTA leaves at its next item
+    s_item[0] = load_acquire(abort_flag) != 0 ? w.total : atomicAdd(queue, 1ull);
+  }
+  __syncthreads();
+  for (int turn = 0;; turn ^= 1) {
+    const unsigned long long v = s_item[turn];
     if (v >= w.total) return;
     const int block = (int)(v / per_block);
     const unsigned long long r = v - (unsigned long long)block * per_block;
@@ -111,78 +137,85 @@ __global__ void __launch_bounds__(256, 4) wave_step(const __grid_constant__ Step
     const unsigned code = w.table[entry];
     const int k_step = (int)(code >> 20), half = (int)((code >> 16) & 15u), c = (int)(code & 0xffffu);
     const int t = block * w.window + k_step;
-    if (t < w.steps) {
-      const long long n = w.first + t;
-      if (tid == 0) {
-        bool ok = true;
-        if (half == 0) {
-          if (t > 0) {
-            ok = wait_count(done_at(w, t - 1, 1, c), tiles, abort_flag);
-            if (ok && c + 1 < w.chunks) ok = wait_count(done_at(w, t - 1, 1, c + 1), tiles, abort_flag);
-          }
-        } else {
-          ok = wait_count(done_at(w, t, 0, c), tiles, abort_flag);
-          if (ok && c > 0) ok = wait_count(done_at(w, t, 0, c - 1), tiles, abort_flag);
+    const bool live = t < w.steps;  // uniform over the CTA
+    const long long n = w.first + t;
+    if (tid == 0) {
+      bool ok = live && load_acquire(abort_flag) == 0;
+      if (ok && half == 0) {
+        if (t > 0) {
+          ok = wait_count(done_at(w, t - 1, 1, c), tiles, abort_flag);
+          if (ok && c + 1 < w.chunks) ok = wait_count(done_at(w, t - 1, 1, c + 1), tiles, abort_flag);
         }
-        if (!ok) {
-          if (sp.status != nullptr) atomicOr(sp.status, 8);
-          atomicExch(w.control + 2, 1u);
-        }
-        s_go = ok ? 1 : 0;
-        sp.src_words = sp.nsrc > 0 ? w.words + (n - w.words_first) * sp.nsrc : nullptr;
+      } else if (ok) {
+        ok = wait_count(done_at(w, t, 0, c), tiles, abort_flag);
+        if (ok && c > 0) ok = wait_count(done_at(w, t, 0, c - 1), tiles, abort_flag);
       }
-      __syncthreads();
-      if (s_go) {
-        const int tz = tile % w.tiles_z, ty = tile / w.tiles_z;
-        const int k0 = tz * bz, j0 = ty * by;
-        const int k = k0 + threadIdx.x, j = j0 + threadIdx.y;
-        const int i0 = c * w.xchunk, i1 = min(i0 + w.xchunk, sp.nx);
-        if (k < sp.nz && j < sp.ny) {
-          if (half == 0)
-            h_tile_march<PML, MSRC>(sp, j, k, i0, i1, j0, by, k0, bz, (int)(n == 0));
-          else
-            e_tile_march<PML>(sp, j, k, i0, i1, j0, by, k0, bz, (int)(n & 1), sp.src_words);
-        }
+      if (live && !ok) {
+        if (sp.status != nullptr) atomicOr(sp.status, 8);
+        atomicExch(w.control + 2, 1u);
       }
-      __syncthreads();  // every thread's stores of the item are issued
-      if (tid == 0) {
-        __threadfence();
-        atomicAdd(done_at(w, t, half, c), 1u);
-      }
-    } else {
-      __syncthreads();
+      s_go = ok ? 1 : 0;
+      sp.src_words = (sp.nsrc > 0 && live) ? w.words + (n - w.words_first) * sp.nsrc : nullptr;
+      // the next item, while this one is worked on: its dependencies are earlier items,
+      // this one's among them at most, which this CTA finishes first
+      s_item[turn ^ 1] = load_acquire(abort_flag) != 0 ? w.total : atomicAdd(queue, 1ull);
     }
+    __syncthreads();
+    if (s_go) {
+      const int tz = tile % w.tiles_z, ty = tile / w.tiles_z;
+      const int k0 = tz * bz, j0 = ty * by;
+      const int k = k0 + threadIdx.x, j = j0 + threadIdx.y;
+      const int i0 = c * w.xchunk, i1 = min(i0 + w.xchunk, sp.nx);
+      if (k < sp.nz && j < sp.ny) {
+        if (half == 0)
+          h_tile_march<PML, MSRC, PF>(sp, j, k, i0, i1, j0, by, k0, bz, (int)(n == 0));
+        else
+          e_tile_march<PML, PF>(sp, j, k, i0, i1, j0, by, k0, bz, (int)(n & 1), sp.src_words);
+      }
+    }
+    __syncthreads();  // every thread's stores of the item are issued; sp is free again
+    if (tid == 0 && live) add_release(done_at(w, t, half, c), 1u);
   }
 }
 
-// One block's chunk items in sequence order (one thread: a few thousand entries).
+// One block's chunk items in sequence order (one thread: a few thousand entries). At
+// position pos, for each step k of the block: the H half of chunk pos - skew k, then the
+// E half of chunk pos - skew k - 1, so every item's dependencies lie at least one whole
+// position earlier in the sequence.
 __global__ void wave_table(unsigned* table, int window, int chunks) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
   int at = 0;
-  const int positions = chunks + kSkew * (window - 1);
+  const int positions = chunks + 1 + kSkew * (window - 1);
   for (int pos = 0; pos < positions; ++pos) {
     for (int k = 0; k < window; ++k) {
-      const int c = pos - kSkew * k;
-      if (c < 0 || c >= chunks) continue;
-      table[at++] = ((unsigned)k << 20) | (0u << 16) | (unsigned)c;
-      table[at++] = ((unsigned)k << 20) | (1u << 16) | (unsigned)c;
+      const int ch = pos - kSkew * k;
+      if (ch >= 0 && ch < chunks) table[at++] = ((unsigned)k << 20) | (0u << 16) | (unsigned)ch;
+      const int ce = ch - 1;
+      if (ce >= 0 && ce < chunks) table[at++] = ((unsigned)k << 20) | (1u << 16) | (unsigned)ce;
     }
   }
 }
 
-template <bool PML, bool MSRC>
+template <bool PML, bool MSRC, bool PF>
 const void* wave_kernel() {
-  return reinterpret_cast<const void*>(wave_step<PML, MSRC>);
+  return reinterpret_cast<const void*>(wave_step<PML, MSRC, PF>);
+}
+
+template <bool PF>
+void launch_family(const StepParams& p, const WaveArgs& w, int blocks, dim3 block, bool pml, bool msrc,
+                   cudaStream_t s) {
+  if (pml && msrc) wave_step<true, true, PF><<<blocks, block, 0, s>>>(p, w);
+  else if (pml) wave_step<true, false, PF><<<blocks, block, 0, s>>>(p, w);
+  else if (msrc) wave_step<false, true, PF><<<blocks, block, 0, s>>>(p, w);
+  else wave_step<false, false, PF><<<blocks, block, 0, s>>>(p, w);
 }
 
 }  // namespace
 
-cudaError_t launch_wave(const StepParams& p, const WaveArgs& w, int blocks, dim3 block, bool pml, bool msrc,
-                        cudaStream_t s) {
-  if (pml && msrc) wave_step<true, true><<<blocks, block, 0, s>>>(p, w);
-  else if (pml) wave_step<true, false><<<blocks, block, 0, s>>>(p, w);
-  else if (msrc) wave_step<false, true><<<blocks, block, 0, s>>>(p, w);
-  else wave_step<false, false><<<blocks, block, 0, s>>>(p, w);
+cudaError_t launch_wave(const StepParams& p, const WaveArgs& w, int blocks, dim3 block, int family, bool pml,
+                        bool msrc, cudaStream_t s) {
+  if (family == 2) launch_family<true>(p, w, blocks, block, pml, msrc, s);
+  else launch_family<false>(p, w, blocks, block, pml, msrc, s);
   return cudaGetLastError();
 }
 
@@ -191,9 +224,12 @@ cudaError_t launch_wave_table(unsigned* table, int window, int chunks, cudaStrea
   return cudaGetLastError();
 }
 
-int wave_blocks_per_sm(int threads, bool pml, bool msrc) {
-  const void* fn = pml ? (msrc ? wave_kernel<true, true>() : wave_kernel<true, false>())
-                       : (msrc ? wave_kernel<false, true>() : wave_kernel<false, false>());
+int wave_blocks_per_sm(int threads, int family, bool pml, bool msrc) {
+  const bool pf = family == 2;
+  const void* fn = pf ? (pml ? (msrc ? wave_kernel<true, true, true>() : wave_kernel<true, false, true>())
+                             : (msrc ? wave_kernel<false, true, true>() : wave_kernel<false, false, true>()))
+                      : (pml ? (msrc ? wave_kernel<true, true, false>() : wave_kernel<true, false, false>())
+                             : (msrc ? wave_kernel<false, true, false>() : wave_kernel<false, false, false>()));
   int blocks = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, threads, 0) != cudaSuccess) {
     cudaGetLastError();

@@ -4,9 +4,11 @@
 // (step t, half, x chunk c, (y, z) tile) that resident CTAs take in order from a global
 // counter. The sequence is cut into blocks of `window` steps; within a block it sweeps the
 // chunks by position, and at position pos it holds, for k = 0 .. window - 1, every tile of
-// the H half and then of the E half of step k at chunk pos - skew * k. So a chunk is
-// visited by the block's steps one after the other while its neighbourhood is still in
-// L2, and each word is brought from HBM about once per window instead of once per step.
+// the H half of step k at chunk pos - skew * k and then of its E half one chunk behind.
+// So a chunk is visited by the block's steps one after the other while its neighbourhood
+// is still in L2, and each word is brought from HBM about once per window instead of
+// once per step; every dependency of an item lies at least one position earlier, which
+// leaves the CTAs a position's worth of items to work on while it completes.
 //
 // Dependencies are per chunk, on completion counters (tiles done) that an item waits on
 // before it starts (bounded; see wave.cu): H(t, c) after E(t-1, c) and E(t-1, c+1) (the
@@ -22,7 +24,7 @@
 namespace mgbwave {
 
 constexpr int kMaxWindow = 16;
-constexpr int kSkew = 2;
+constexpr int kSkew = 3;
 constexpr int kControlWords = 64;  // queue counter, abort flag (256 bytes)
 
 struct WaveArgs {
@@ -43,10 +45,11 @@ struct WaveArgs {
 // Entries of one block's table: window * 2 * chunks.
 inline int table_entries(int window, int chunks) { return window * 2 * chunks; }
 
-cudaError_t launch_wave(const mgbstep::StepParams& p, const WaveArgs& w, int blocks, dim3 block, bool pml,
-                        bool msrc, cudaStream_t s);
+// family 0: the plain column marches; 2: the prefetching ones.
+cudaError_t launch_wave(const mgbstep::StepParams& p, const WaveArgs& w, int blocks, dim3 block, int family,
+                        bool pml, bool msrc, cudaStream_t s);
 cudaError_t launch_wave_table(unsigned* table, int window, int chunks, cudaStream_t s);
 // Resident CTAs of `threads` threads per SM for the kernel variant (0 on error).
-int wave_blocks_per_sm(int threads, bool pml, bool msrc);
+int wave_blocks_per_sm(int threads, int family, bool pml, bool msrc);
 
 }  // namespace mgbwave

@@ -55,9 +55,11 @@ AUTOTUNE_CANDIDATES = ((0, 32, 4, 4), (0, 32, 8, 4), (0, 32, 4, 8), (0, 64, 2, 8
                        (5, 32, 4, 4), (5, 16, 8, 4), (5, 32, 4, 8), (5, 32, 2, 8), (5, 32, 4, 2))
 _AUTOTUNE_CACHE: Dict[tuple, Tuple[int, int, int, int]] = {}
 # Wavefront choices the autotuner times against the best pair of per-half kernels:
-# (block_z, block_y, x_chunk, window), as kernel choice (6, block_z, block_y, x_chunk, window).
-WAVE_CANDIDATES = ((32, 4, 4, 3), (32, 4, 4, 4), (32, 8, 4, 3), (32, 4, 2, 4), (32, 4, 2, 6), (64, 4, 4, 3),
-                   (32, 4, 8, 2))
+# (march family, block_z, block_y, x_chunk, window), as kernel choice
+# (6, family, block_z, block_y, x_chunk, window); family 0 the plain column marches, 2 the
+# prefetching ones.
+WAVE_CANDIDATES = ((2, 32, 4, 4, 3), (2, 32, 4, 4, 4), (2, 32, 8, 4, 3), (0, 32, 8, 4, 3), (0, 32, 4, 4, 3),
+                   (2, 32, 4, 8, 2), (2, 64, 4, 4, 3))
 WAVE_FAMILY = 6
 # Steps one wavefront launch may hold (the length of the counter table).
 WAVE_MAX_STEPS = 256
@@ -546,31 +548,31 @@ class Engine:
         return (grid.is_metallic(0) and not grid.has_symmetry and not grid.has_bloch
                 and not self.conductivity)
 
-    def set_wave(self, choice: Optional[Tuple[int, int, int, int]]) -> None:
-        """Step with the wavefront path, (block_z, block_y, x_chunk, window), or leave it
-        (None). The counter buffer is this engine's (a torch allocation)."""
+    def set_wave(self, choice: Optional[Tuple[int, int, int, int, int]]) -> None:
+        """Step with the wavefront path, (march family, block_z, block_y, x_chunk, window),
+        or leave it (None). The counter buffer is this engine's (a torch allocation)."""
         stream = self._stream_handle()
         if choice is None:
-            _lib.check(self.lib, self.lib.mgb_set_wave(self.handle, 32, 4, 4, 1, 1, None, 0, stream))
+            _lib.check(self.lib, self.lib.mgb_set_wave(self.handle, 0, 32, 4, 4, 1, 1, None, 0, stream))
             self.wave = None
             self.wave_buffer = None
             return
-        bz, by, xc, window = (int(v) for v in choice)
+        family, bz, by, xc, window = (int(v) for v in choice)
         nbytes = self.lib.mgb_wave_bytes(self.handle, xc, window, WAVE_MAX_STEPS)
         if nbytes == 0:
             raise ValueError(f"bad wavefront choice {choice}")
         buffer = torch.empty(nbytes + 256, dtype=torch.uint8, device=self.device)
         offset = (-buffer.data_ptr()) % 256
-        _lib.check(self.lib, self.lib.mgb_set_wave(self.handle, bz, by, xc, window, WAVE_MAX_STEPS,
+        _lib.check(self.lib, self.lib.mgb_set_wave(self.handle, family, bz, by, xc, window, WAVE_MAX_STEPS,
                                                    buffer.data_ptr() + offset, nbytes, stream))
-        self.wave = (bz, by, xc, window)
+        self.wave = (family, bz, by, xc, window)
         self.wave_buffer = buffer
 
     def select(self, choice) -> None:
         """Apply a kernel choice: one (family, block_z, block_y, x_chunk) for both halves,
-        or a pair of them (H half, E half); (6, block_z, block_y, x_chunk, window) steps
-        with the wavefront path (the halves keep their choice for single launches)."""
-        if len(choice) == 5 and int(choice[0]) == WAVE_FAMILY:
+        or a pair of them (H half, E half); (6, family, block_z, block_y, x_chunk, window)
+        steps with the wavefront path (the halves keep their choice for single launches)."""
+        if len(choice) == 6 and int(choice[0]) == WAVE_FAMILY:
             self.set_wave(tuple(int(v) for v in choice[1:]))
             return
         if len(choice) == 3 and isinstance(choice[0], (tuple, list)):

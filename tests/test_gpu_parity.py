@@ -30,7 +30,8 @@ GENERIC = (0, 32, 8, 4)
 PREFETCH = (2, 32, 4, 4)
 WARP_SPECIALIZED = ((2, 16, 8, 4), (3, 64, 8, 8))  # H prefetching, E warp-specialized tiles
 L2_PREFETCH = ((4, 32, 4, 4), (5, 16, 8, 4))  # families 0 / 2 with the x chunk prefetched into L2
-WAVE = (6, 32, 4, 4, 3)  # the wavefront path: 32 x 4 tiles, 4-plane chunks, 3-step blocks
+WAVE = (6, 2, 32, 4, 4, 3)  # the wavefront path: prefetching marches, 32 x 4 tiles, 4-plane chunks,
+# 3-step blocks
 MODES = {"tiles": TILES, "generic": GENERIC, "prefetch": PREFETCH, "ws": WARP_SPECIALIZED,
          "l2": L2_PREFETCH, "wave": WAVE}
 
@@ -77,8 +78,9 @@ def test_fields_are_the_reference_words(gpu, name, mode):
     if (case.get("conductivity") or case.get("k_point")) and mode == "l2":
         kernels = (4, 32, 4, 4)  # lossy and Bloch-phased runs take families 0 and 4
     driver, flux, dft = gpu_case(case, kernels=kernels)
-    assert driver.engine.uses_tiles == (mode in ("tiles", "ws"))
-    if mode == "wave":
+    if mode != "wave":  # the wavefront path leaves the per-half choice at its default
+        assert driver.engine.uses_tiles == (mode in ("tiles", "ws"))
+    else:
         engines = [driver.engine.re, driver.engine.im] if case.get("complex") else [driver.engine]
         assert all(e.wave == WAVE[1:] for e in engines)
     for c in FIELDS:
@@ -157,7 +159,9 @@ def test_chunked_runs_equal_one_run(gpu):
 def test_sphere80_words_after_200_steps(gpu, mode):
     gold = golden_io.digest()
     driver, flux, _ = gpu_case(SPHERE80, steps=gold["steps"], kernels=MODES[mode])
-    assert driver.engine.uses_tiles == (mode in ("tiles", "ws"))
+    if mode != "wave":
+        assert driver.engine.uses_tiles == (mode in ("tiles", "ws"))
+    assert (driver.engine.wave is not None) == (mode == "wave")
     assert (driver.engine.wave is not None) == (mode == "wave")
     for c, expected in gold["sha256"].items():
         words = np.ascontiguousarray(driver.get_field(c, cell_centered=False), dtype=np.float32)

@@ -17,9 +17,10 @@ because every coefficient outside the membership is exactly 1.0 (checked here).
 
 The membership on each (lattice, axis) is at most two runs ``[a0, a1) U [b0, b1)``,
 the same four words per (lattice, axis) as the reference's ``chunk_bounds_record``
-(``chunk_map.py:897``). The device stores every auxiliary array compactly over its
-runs only: position ``i`` of the axis maps to slab row ``i - a0`` in the low run and
-``(a1 - a0) + (i - b0)`` in the high run.
+(``chunk_map.py:897``). The device stores every auxiliary array as a full grid volume
+of which only the cells whose coordinate along the array's axis lies in those runs are
+ever read or written: a cell's auxiliary word sits at the cell's own offset, and the
+untouched cells move no bytes.
 """
 
 from __future__ import annotations

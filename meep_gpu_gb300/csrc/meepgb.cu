@@ -1516,6 +1516,7 @@ struct mgb_sim {
     int bz = 32, by = 4, xchunk = 4, window = 4, max_steps = 0;
     int chunks = 0, tiles_z = 0, tiles_y = 0, blocks = 0;
     int family = 0;  // 0 the plain column marches, 2 the prefetching ones
+    int l2pf = 1;    // each tile's chunk planes prefetched into L2 before its march
     unsigned* control = nullptr;
     unsigned* table = nullptr;
     unsigned* done = nullptr;
@@ -2144,7 +2145,7 @@ int step_wave(mgb_sim* sim, long long first, int nsteps, cudaStream_t s) {
     const long long blocks = (steps + wv.window - 1) / wv.window;
     w.total = (unsigned long long)blocks * wv.window * 2 * wv.chunks * wv.tiles_z * wv.tiles_y;
     StepParams p = sim->step;
-    p.l2pf = 0;
+    p.l2pf = wv.l2pf;
     p.src_words = nullptr;
     err = mgbwave::launch_wave(p, w, wv.blocks, dim3(wv.bz, wv.by, 1), wv.family, pml, msrc, s);
     if (err != cudaSuccess) return cuda_error(err, "wavefront step launch");
@@ -2228,6 +2229,8 @@ int mgb_set_wave(mgb_sim* sim, int32_t family, int32_t block_z, int32_t block_y,
   mgb_sim::Wave& wv = sim->wave;
   unsigned char* base = static_cast<unsigned char*>(buffer);
   wv.family = family;
+  const char* l2pf = getenv("MEEPGB_WAVE_L2PF");
+  wv.l2pf = (l2pf != nullptr && l2pf[0] == '0') ? 0 : 1;
   wv.bz = block_z;
   wv.by = block_y;
   wv.xchunk = x_chunk;

@@ -102,7 +102,7 @@ __device__ __forceinline__ void e_tile_march(const StepParams& p, int j, int k, 
 }
 
 template <bool PML, bool MSRC, bool PF>
-__global__ void __launch_bounds__(256, PF ? 3 : 4) wave_step(const __grid_constant__ StepParams params,
+__global__ void __launch_bounds__(256, PF ? 3 : 5) wave_step(const __grid_constant__ StepParams params,
                                                              const __grid_constant__ WaveArgs w) {
   // the parameters in shared memory: the source-word row changes with each item's step
   __shared__ StepParams sp;

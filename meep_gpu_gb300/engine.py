@@ -644,7 +644,9 @@ class Engine:
                 if ms < best_ms[part]:
                     best[part], best_ms[part] = choice, ms
         wave = None
-        if self.wave_eligible and os.environ.get("MEEPGB_WAVE", "1") != "0":
+        # the wavefront path is timed only on request: on the benchmarked grids it steps
+        # slower than the best pair of per-half kernels
+        if self.wave_eligible and os.environ.get("MEEPGB_WAVE", "0") == "1":
             wave = self._tune_wave(scratch, (best[0], best[1]), stream)
         scratch.close()
         del scratch

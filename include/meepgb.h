@@ -289,6 +289,22 @@ int mgb_select_kernels(mgb_sim* sim, int32_t family);
 int mgb_select_half(mgb_sim* sim, int32_t part, int32_t family, int32_t block_z, int32_t block_y,
                     int32_t x_chunk);
 
+/* ---- X-range split stepping ----------------------------------------------------------
+ * Each half launched as `ranges` launches over consecutive ranges of x planes, on streams
+ * of the plan (created here, released by mgb_destroy) ordered by events: the H half of a
+ * range after the E half of the step before on it and the range above, the E half of a
+ * range after the H half on it and the range below. The GPU then fills one launch's tail
+ * with the next ready range and begins a step on the low ranges while the previous one
+ * finishes the high ones. mgb_step forks the streams from its stream and joins them back
+ * (monitor kernels run on it, joined before and forked after). Generic kernel families
+ * only (the tile kernels step every plane in one launch); refused for mirror folds, Bloch
+ * phases or a periodic x axis. No reference counterpart. */
+#define MGB_MAX_SPLIT 16
+
+/* Split each half into `ranges` (2..MGB_MAX_SPLIT) x-range launches; 0 or 1 switches the
+ * split off. */
+int mgb_set_split(mgb_sim* sim, int32_t ranges);
+
 /* ---- Wavefront stepping --------------------------------------------------------------
  * Runs of steps in one persistent launch: resident CTAs take (step, half, x chunk, (y, z)
  * tile) items in a skewed order that lets `window` consecutive steps pass over a chunk

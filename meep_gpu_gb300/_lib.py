@@ -143,6 +143,7 @@ SIGNATURES = {
     "mgb_select_kernels": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "mgb_select_half": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                        ctypes.c_int32, ctypes.c_int32]),
+    "mgb_set_split": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "mgb_wave_bytes": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     "mgb_set_wave": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                     ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,

@@ -22,7 +22,7 @@ namespace mgbdft {
 namespace {
 
 constexpr int kRows = 128;           // M per tile = tensor-memory lanes
-constexpr int kCols = 256;           // N per tile = tensor-memory columns
+constexpr int kCols = 128;           // N per tile = tensor-memory columns (3 CTAs per SM)
 constexpr int kThreads = 256;        // warp w reads lanes 32(w % 4) .. + 31, columns half w / 4
 constexpr int kSlices = kDepth / 8;  // kind::tf32 takes K = 8 per MMA
 // K-major without swizzle: core matrices of 8 rows x 16 bytes (4 elements). In one K
@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(256) table_kernel(const double* __restrict__ o
   table[idx] = v;
 }
 
-__global__ void __launch_bounds__(kThreads, 1) contract_kernel(const __grid_constant__ Contraction c) {
+__global__ void __launch_bounds__(kThreads, 3) contract_kernel(const __grid_constant__ Contraction c) {
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* b_hi = smem;
   unsigned char* b_lo = smem + kTileB;

@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(256, 4) h_generic_pf(const __grid_constant__ S
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
-  const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  const int i0 = (blockIdx.z + p.xbase) * xchunk, i1 = min(i0 + xchunk, p.nx);
   // a run with magnetic sources: the CTAs that hold source points deposit them
   if (MSRC && cta_msrc(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x)) {
     h_march_pf<PML, -1, true>(p, j, k, i0, i1, first_step);
@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(256, 4) e_generic_pf(const __grid_constant__ S
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
-  const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  const int i0 = (blockIdx.z + p.xbase) * xchunk, i1 = min(i0 + xchunk, p.nx);
   if (!PML) {
     e_march_pf<false>(p, j, k, i0, i1, parity, p.src_words);
     return;
@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(256, 5) h_generic(const __grid_constant__ Step
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
-  const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  const int i0 = (blockIdx.z + p.xbase) * xchunk, i1 = min(i0 + xchunk, p.nx);
   // a Bloch-phased run: the CTAs at index 0 of a phased axis read the other part there
   if (cta_bloch(p, i0, blockIdx.y * blockDim.y, blockIdx.x * blockDim.x)) {
     h_march<PML, false, -1, true, true>(p, j, k, i0, i1, first_step);
@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(256, 5) e_generic(const __grid_constant__ Step
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
-  const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  const int i0 = (blockIdx.z + p.xbase) * xchunk, i1 = min(i0 + xchunk, p.nx);
   // a Bloch-phased run: the CTAs at index 0 of a phased axis read the other part there
   if (cta_bloch(p, i0, blockIdx.y * blockDim.y, blockIdx.x * blockDim.x)) {
     e_march<PML, false, -1, true>(p, j, k, i0, i1, parity, p.src_words);
@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(256, 4) h_generic_cond(const __grid_constant__
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
-  const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  const int i0 = (blockIdx.z + p.xbase) * xchunk, i1 = min(i0 + xchunk, p.nx);
   // a Bloch-phased run: the CTAs at index 0 of a phased axis read the other part there
   if (cta_bloch(p, i0, blockIdx.y * blockDim.y, blockIdx.x * blockDim.x)) {
     h_march<PML, true, -1, true, true>(p, j, k, i0, i1, first_step, &cp);
@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(256, 4) e_generic_cond(const __grid_constant__
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
-  const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  const int i0 = (blockIdx.z + p.xbase) * xchunk, i1 = min(i0 + xchunk, p.nx);
   // a Bloch-phased run: the CTAs at index 0 of a phased axis read the other part there
   if (cta_bloch(p, i0, blockIdx.y * blockDim.y, blockIdx.x * blockDim.x)) {
     e_march<PML, true, -1, true>(p, j, k, i0, i1, parity, p.src_words, &cp);
@@ -1510,6 +1510,15 @@ struct mgb_sim {
     int count = 0;              // samples buffered since the last contraction
     long long first_post = 0;   // the step after which sample 0 was taken
   } dbuf[MGB_MAX_MONITORS];
+  // The x-range split (mgb_set_split): each half launched as `ranges` launches over ranges
+  // of planes on the plan's own streams, ordered by events instead of by one stream.
+  struct Split {
+    int ranges = 0;  // 0 or 1: off
+    cudaStream_t streams[MGB_MAX_SPLIT] = {};
+    cudaEvent_t h_done[2][MGB_MAX_SPLIT] = {};  // by step parity
+    cudaEvent_t e_done[2][MGB_MAX_SPLIT] = {};
+    cudaEvent_t fork = nullptr;
+  } split;
   // The wavefront path (mgb_set_wave): runs of steps in one persistent launch.
   struct Wave {
     bool on = false;
@@ -1971,7 +1980,10 @@ int flush_monitor(mgb_sim* sim, int m, cudaStream_t s) {
 }
 
 // Launches of one step, split by part so mgb_step and mgb_launch share them.
-int launch_part_kernels(mgb_sim* sim, long long n, int part, cudaStream_t s) {
+// plane0 / plane1: the planes [plane0, plane1) a generic-kernel half covers (plane0 a
+// multiple of the half's x chunk; plane1 -1 for the last plane); the tile kernels always
+// cover every plane.
+int launch_part_kernels(mgb_sim* sim, long long n, int part, cudaStream_t s, int plane0 = 0, int plane1 = -1) {
   StepParams& p = sim->step;
   const bool pml = sim->desc.pml_active != 0;
   if (part == 0 || part == 1) {
@@ -1999,8 +2011,10 @@ int launch_part_kernels(mgb_sim* sim, long long n, int part, cudaStream_t s) {
     }
     const dim3 block(hc.block_z, hc.block_y, 1);
     const int xc = hc.xchunk;
-    const dim3 grid((p.nz + block.x - 1) / block.x, (p.ny + block.y - 1) / block.y, (p.nx + xc - 1) / xc);
+    const int last = plane1 < 0 ? p.nx : plane1;
+    const dim3 grid((p.nz + block.x - 1) / block.x, (p.ny + block.y - 1) / block.y, (last - plane0 + xc - 1) / xc);
     p.l2pf = hc.l2pf ? 1 : 0;  // per half; the launch takes the parameters by value
+    p.xbase = plane0 / xc;     // ditto: the first chunk of this launch's planes
     const bool msrc = p.nsrc_h > 0;  // the H kernels with the magnetic deposit compiled in
     if (sim->has_cond) {
       if (part == 0) {
@@ -2156,6 +2170,100 @@ int step_wave(mgb_sim* sim, long long first, int nsteps, cudaStream_t s) {
   return MGB_OK;
 }
 
+// Planes per range of the x-range split: a multiple of both halves' x chunks.
+int split_planes(const mgb_sim* sim) {
+  const int a = sim->half[0].xchunk, b = sim->half[1].xchunk;
+  int g = a, h = b;
+  while (h != 0) { const int t = g % h; g = h; h = t; }
+  const int unit = a / g * b;
+  const int per = (sim->step.nx + sim->split.ranges - 1) / sim->split.ranges;
+  return ((per + unit - 1) / unit) * unit;
+}
+
+// Steps [first, first + nsteps) with each half split into x ranges on the plan's streams:
+// H(n, r) after E(n-1, r) and E(n-1, r+1) (it reads E one plane above and overwrites the H
+// that E(n-1, r+1) read), E(n, r) after H(n, r) and H(n, r-1) (it reads H one plane below
+// and overwrites the E that H(n, r-1) read). So the GPU fills a range's tail with the next
+// ready range and starts step n+1 on the low ranges while step n finishes the high ones.
+// The monitors due after a step run on the caller's stream, joined before and forked
+// after; the caller's stream waits for every range at the end.
+int step_split(mgb_sim* sim, long long first, int nsteps, cudaStream_t origin) {
+  mgb_sim::Split& sp = sim->split;
+  const int R = sp.ranges;
+  const int planes = split_planes(sim);
+  int ranges_used = 0;
+  int lo[MGB_MAX_SPLIT], hi[MGB_MAX_SPLIT];
+  for (int r = 0; r < R; ++r) {
+    lo[r] = r * planes;
+    hi[r] = std::min((r + 1) * planes, sim->step.nx);
+    if (lo[r] < hi[r]) ranges_used = r + 1;
+  }
+  auto fork = [&]() -> cudaError_t {
+    cudaError_t err = cudaEventRecord(sp.fork, origin);
+    for (int r = 0; r < ranges_used && err == cudaSuccess; ++r) err = cudaStreamWaitEvent(sp.streams[r], sp.fork, 0);
+    return err;
+  };
+  auto join = [&](int b) -> cudaError_t {
+    cudaError_t err = cudaSuccess;
+    for (int r = 0; r < ranges_used && err == cudaSuccess; ++r) err = cudaStreamWaitEvent(origin, sp.e_done[b][r], 0);
+    return err;
+  };
+  cudaError_t err = fork();
+  if (err != cudaSuccess) return cuda_error(err, "split fork");
+  for (int t = 0; t < nsteps; ++t) {
+    const long long n = first + t;
+    const int b = (int)(n & 1), pb = b ^ 1;
+    for (int r = 0; r < ranges_used; ++r) {
+      if (t > 0 && r + 1 < ranges_used) {
+        err = cudaStreamWaitEvent(sp.streams[r], sp.e_done[pb][r + 1], 0);
+        if (err != cudaSuccess) return cuda_error(err, "split wait");
+      }
+      const int rc = launch_part_kernels(sim, n, 0, sp.streams[r], lo[r], hi[r]);
+      if (rc != MGB_OK) return rc;
+      err = cudaEventRecord(sp.h_done[b][r], sp.streams[r]);
+      if (err != cudaSuccess) return cuda_error(err, "split record");
+    }
+    for (int r = 0; r < ranges_used; ++r) {
+      if (r > 0) {
+        err = cudaStreamWaitEvent(sp.streams[r], sp.h_done[b][r - 1], 0);
+        if (err != cudaSuccess) return cuda_error(err, "split wait");
+      }
+      const int rc = launch_part_kernels(sim, n, 1, sp.streams[r], lo[r], hi[r]);
+      if (rc != MGB_OK) return rc;
+      err = cudaEventRecord(sp.e_done[b][r], sp.streams[r]);
+      if (err != cudaSuccess) return cuda_error(err, "split record");
+    }
+    bool due = false;
+    for (int m = 0; m < sim->desc.nmonitors; ++m)
+      if ((n + 1) % sim->desc.monitors[m].decimation == 0) due = true;
+    if (due) {
+      err = join(b);
+      if (err != cudaSuccess) return cuda_error(err, "split join");
+      const int rc = launch_part(sim, n, 2, origin);
+      if (rc != MGB_OK) return rc;
+      err = fork();
+      if (err != cudaSuccess) return cuda_error(err, "split fork");
+    }
+  }
+  sim->step.xbase = 0;
+  err = join((int)((first + nsteps - 1) & 1));
+  if (err != cudaSuccess) return cuda_error(err, "split join");
+  return launch_error("split step launch");
+}
+
+void free_split(mgb_sim* sim) {
+  mgb_sim::Split& sp = sim->split;
+  for (int r = 0; r < MGB_MAX_SPLIT; ++r) {
+    if (sp.streams[r] != nullptr) cudaStreamDestroy(sp.streams[r]);
+    for (int b = 0; b < 2; ++b) {
+      if (sp.h_done[b][r] != nullptr) cudaEventDestroy(sp.h_done[b][r]);
+      if (sp.e_done[b][r] != nullptr) cudaEventDestroy(sp.e_done[b][r]);
+    }
+  }
+  if (sp.fork != nullptr) cudaEventDestroy(sp.fork);
+  sp = mgb_sim::Split();
+}
+
 int check_words(mgb_sim* sim, long long first, long long count) {
   if (sim->step.nsrc > 0 &&
       (first < sim->words_first || first + count > sim->words_first + sim->words_steps)) {
@@ -2179,6 +2287,8 @@ int mgb_step(mgb_sim* sim, int64_t first_step, int32_t nsteps, void* stream) {
   if (rc != MGB_OK) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (sim->wave.on) return step_wave(sim, first_step, nsteps, s);
+  if (sim->split.ranges > 1 && !sim->half[0].tiles && !sim->half[1].tiles)
+    return step_split(sim, first_step, nsteps, s);
   for (int32_t t = 0; t < nsteps; ++t) {
     const long long n = first_step + t;
     for (int part = 0; part < 3; ++part) launch_part(sim, n, part, s);
@@ -2188,6 +2298,36 @@ int mgb_step(mgb_sim* sim, int64_t first_step, int32_t nsteps, void* stream) {
     }
   }
   return launch_error("step launch");
+}
+
+int mgb_set_split(mgb_sim* sim, int32_t ranges) {
+  if (sim == nullptr) return fail(MGB_ERR_ARGUMENT, "null plan");
+  if (ranges < 0 || ranges > MGB_MAX_SPLIT)
+    return fail(MGB_ERR_ARGUMENT, "ranges must be 0.." + std::to_string(MGB_MAX_SPLIT));
+  if (ranges > 1 && (sim->folded || sim->step.bloch || !sim->desc.metallic[0]))
+    return fail(MGB_ERR_UNSUPPORTED, "the x-range split steps runs without mirror folds or Bloch phases, on a "
+                                     "metallic x axis");
+  free_split(sim);
+  if (ranges <= 1) return MGB_OK;
+  mgb_sim::Split& sp = sim->split;
+  for (int r = 0; r < ranges; ++r) {
+    cudaError_t err = cudaStreamCreateWithFlags(&sp.streams[r], cudaStreamNonBlocking);
+    for (int b = 0; b < 2 && err == cudaSuccess; ++b) {
+      err = cudaEventCreateWithFlags(&sp.h_done[b][r], cudaEventDisableTiming);
+      if (err == cudaSuccess) err = cudaEventCreateWithFlags(&sp.e_done[b][r], cudaEventDisableTiming);
+    }
+    if (err != cudaSuccess) {
+      free_split(sim);
+      return cuda_error(err, "split streams");
+    }
+  }
+  const cudaError_t err = cudaEventCreateWithFlags(&sp.fork, cudaEventDisableTiming);
+  if (err != cudaSuccess) {
+    free_split(sim);
+    return cuda_error(err, "split streams");
+  }
+  sp.ranges = ranges;
+  return MGB_OK;
 }
 
 size_t mgb_wave_bytes(mgb_sim* sim, int32_t x_chunk, int32_t window, int32_t max_steps) {
@@ -2423,7 +2563,11 @@ int mgb_select_half(mgb_sim* sim, int32_t part, int32_t family, int32_t block_z,
   return MGB_OK;
 }
 
-void mgb_destroy(mgb_sim* sim) { delete sim; }
+void mgb_destroy(mgb_sim* sim) {
+  if (sim == nullptr) return;
+  free_split(sim);
+  delete sim;
+}
 
 }  // extern "C"
 

@@ -43,6 +43,7 @@ struct StepParams {
   int src_box_h[6];         // box of the magnetic points
   int32_t* status;
   int l2pf;  // 1: each thread prefetches its x chunk's field planes into L2 before marching
+  int xbase; // first x chunk of a launch that covers a range of the planes (0: from plane 0)
   // Bloch phases (complex runs with k != 0): per axis 0 none, 1 copy, 2 negate, 3 the
   // phase (re, im) rounded to float32; `part` 0 steps real parts, 1 imaginary parts;
   // pE / pH the other part's E and H

@@ -61,6 +61,8 @@ _AUTOTUNE_CACHE: Dict[tuple, Tuple[int, int, int, int]] = {}
 WAVE_CANDIDATES = ((2, 32, 4, 4, 3), (2, 32, 4, 4, 4), (2, 32, 8, 4, 3), (0, 32, 8, 4, 3), (0, 32, 4, 4, 3),
                    (2, 32, 4, 8, 2), (2, 64, 4, 4, 3))
 WAVE_FAMILY = 6
+# X-range splits (launches per half) the autotuner times against the unsplit halves.
+SPLIT_CANDIDATES = (2, 3, 4, 6)
 # Steps one wavefront launch may hold (the length of the counter table).
 WAVE_MAX_STEPS = 256
 
@@ -216,6 +218,7 @@ class Engine:
         self._setup_monitors()
         self._pole_specs = list(poles)
         self.choice = None
+        self.split = 0
         self.wave = None
         self.wave_buffer = None
         self.handle = None
@@ -548,6 +551,20 @@ class Engine:
         return (grid.is_metallic(0) and not grid.has_symmetry and not grid.has_bloch
                 and not self.conductivity)
 
+    @property
+    def split_eligible(self) -> bool:
+        """Whether the halves can be split into x-range launches (metallic x, no folds, no
+        Bloch phase, generic kernel families)."""
+        grid = self.grid
+        return (grid.is_metallic(0) and not grid.has_symmetry and not grid.has_bloch
+                and not self.uses_tiles)
+
+    def set_split(self, ranges: int) -> None:
+        """Launch each half as ``ranges`` x-range launches on the plan's streams (0 or 1:
+        one launch per half)."""
+        _lib.check(self.lib, self.lib.mgb_set_split(self.handle, int(ranges)))
+        self.split = int(ranges) if ranges > 1 else 0
+
     def set_wave(self, choice: Optional[Tuple[int, int, int, int, int]]) -> None:
         """Step with the wavefront path, (march family, block_z, block_y, x_chunk, window),
         or leave it (None). The counter buffer is this engine's (a torch allocation)."""
@@ -575,10 +592,12 @@ class Engine:
         if len(choice) == 6 and int(choice[0]) == WAVE_FAMILY:
             self.set_wave(tuple(int(v) for v in choice[1:]))
             return
-        if len(choice) == 3 and isinstance(choice[0], (tuple, list)):
-            # (H half, E half, wavefront choice or None): an autotuned result
+        if len(choice) in (3, 4) and isinstance(choice[0], (tuple, list)):
+            # (H half, E half, wavefront choice or None[, x-range split]): an autotuned result
             self.select((choice[0], choice[1]))
             self.set_wave(choice[2])
+            if len(choice) == 4:
+                self.set_split(choice[3])
             return
         if len(choice) == 2 and isinstance(choice[0], (tuple, list)):
             h, e = (tuple(int(v) for v in c) for c in choice)
@@ -648,12 +667,45 @@ class Engine:
         # slower than the best pair of per-half kernels
         if self.wave_eligible and os.environ.get("MEEPGB_WAVE", "0") == "1":
             wave = self._tune_wave(scratch, (best[0], best[1]), stream)
+        split = 0
+        if wave is None and os.environ.get("MEEPGB_SPLIT", "1") != "0":
+            split = self._tune_split(scratch, (best[0], best[1]), stream)
         scratch.close()
         del scratch
-        _AUTOTUNE_CACHE[key] = (best[0], best[1], wave)
-        self.select((best[0], best[1], wave))
+        _AUTOTUNE_CACHE[key] = (best[0], best[1], wave, split)
+        self.select((best[0], best[1], wave, split))
         self.autotune_ms = best_ms[0] + best_ms[1]
         return self.choice
+
+    def _run_ms(self, scratch: "Engine", stream, steps: int = 24) -> float:
+        """The fastest of two timed runs of ``steps`` whole steps on the scratch engine."""
+        scratch.step(0, 4)
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        best_ms = float("inf")
+        for _ in range(2):
+            start.record(stream)
+            scratch.step(4, steps)
+            end.record(stream)
+            end.synchronize()
+            best_ms = min(best_ms, start.elapsed_time(end))
+        return best_ms
+
+    def _tune_split(self, scratch: "Engine", halves, stream) -> int:
+        """The x-range split that steps fastest (0: none), whole steps timed."""
+        scratch.select(halves)
+        if not scratch.split_eligible:
+            return 0
+        scratch.set_split(0)
+        best, best_ms = 0, self._run_ms(scratch, stream)
+        for ranges in SPLIT_CANDIDATES:
+            if ranges * 2 > self.grid.shape[0]:
+                continue
+            scratch.set_split(ranges)
+            ms = self._run_ms(scratch, stream)
+            if ms < best_ms:
+                best, best_ms = ranges, ms
+        scratch.set_split(0)
+        return best
 
     def _tune_wave(self, scratch: "Engine", halves, stream, steps: int = 24):
         """The fastest wavefront choice, if it steps a run of ``steps`` steps faster than
@@ -865,7 +917,7 @@ class ComplexEngine:
         self.re.finish()
         im_choice = kernels
         if self.re.choice is not None:
-            im_choice = (self.re.choice[0], self.re.choice[1], self.re.wave)
+            im_choice = (self.re.choice[0], self.re.choice[1], self.re.wave, self.re.split)
         self.im._finish_args = (self.im._finish_args[0], im_choice, launch_shape, False)
         self.im.finish()
         self.grid = grid

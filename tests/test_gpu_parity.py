@@ -32,8 +32,9 @@ WARP_SPECIALIZED = ((2, 16, 8, 4), (3, 64, 8, 8))  # H prefetching, E warp-speci
 L2_PREFETCH = ((4, 32, 4, 4), (5, 16, 8, 4))  # families 0 / 2 with the x chunk prefetched into L2
 WAVE = (6, 2, 32, 4, 4, 3)  # the wavefront path: prefetching marches, 32 x 4 tiles, 4-plane chunks,
 # 3-step blocks
+SPLIT = ((4, 32, 4, 4), (2, 32, 4, 2), None, 3)  # each half as three x-range launches on three streams
 MODES = {"tiles": TILES, "generic": GENERIC, "prefetch": PREFETCH, "ws": WARP_SPECIALIZED,
-         "l2": L2_PREFETCH, "wave": WAVE}
+         "l2": L2_PREFETCH, "wave": WAVE, "split": SPLIT}
 
 
 def wave_steps(case) -> bool:
@@ -70,15 +71,23 @@ def test_fields_are_the_reference_words(gpu, name, mode):
     tileable = case["n"][2] % 4 == 0
     if mode == "wave" and not wave_steps(case):
         pytest.skip("the wavefront path steps metallic-x runs without folds, Bloch phases or conductivity")
-    if (case.get("conductivity") or case.get("k_point")) and mode not in ("generic", "l2", "wave"):
+    if mode == "split" and not (wave_steps(case) or (case.get("conductivity") and not case.get("symmetry")
+                                                     and wave_steps(dict(case, conductivity=None)))):
+        pytest.skip("the x-range split steps metallic-x runs without folds or Bloch phases")
+    if (case.get("conductivity") or case.get("k_point")) and mode not in ("generic", "l2", "wave", "split"):
         pytest.skip("lossy and Bloch-phased runs step with the generic kernels only (the others are refused)")
     if mode in ("tiles", "ws") and not tileable:
         mode = "generic"
     kernels = MODES[mode]
     if (case.get("conductivity") or case.get("k_point")) and mode == "l2":
         kernels = (4, 32, 4, 4)  # lossy and Bloch-phased runs take families 0 and 4
+    if case.get("conductivity") and mode == "split":
+        kernels = ((4, 32, 4, 4), (0, 32, 4, 2), None, 3)
     driver, flux, dft = gpu_case(case, kernels=kernels)
-    if mode != "wave":  # the wavefront path leaves the per-half choice at its default
+    if mode == "split":
+        engines = [driver.engine.re, driver.engine.im] if case.get("complex") else [driver.engine]
+        assert all(e.split == 3 for e in engines)
+    elif mode != "wave":  # the wavefront path leaves the per-half choice at its default
         assert driver.engine.uses_tiles == (mode in ("tiles", "ws"))
     else:
         engines = [driver.engine.re, driver.engine.im] if case.get("complex") else [driver.engine]
@@ -159,9 +168,10 @@ def test_chunked_runs_equal_one_run(gpu):
 def test_sphere80_words_after_200_steps(gpu, mode):
     gold = golden_io.digest()
     driver, flux, _ = gpu_case(SPHERE80, steps=gold["steps"], kernels=MODES[mode])
-    if mode != "wave":
+    if mode not in ("wave", "split"):
         assert driver.engine.uses_tiles == (mode in ("tiles", "ws"))
     assert (driver.engine.wave is not None) == (mode == "wave")
+    assert (driver.engine.split == 3) == (mode == "split")
     assert (driver.engine.wave is not None) == (mode == "wave")
     for c, expected in gold["sha256"].items():
         words = np.ascontiguousarray(driver.get_field(c, cell_centered=False), dtype=np.float32)

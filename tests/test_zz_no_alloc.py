@@ -75,19 +75,20 @@ def test_noalloc_equals_the_scratch_entry_point_twice_in_a_row(gpu):
         warm = acc0.clone()
         _lib.check(lib, lib.mgb_dft_contract_noalloc(samples.data_ptr(), *args, warm.data_ptr(), stream))
         torch.cuda.synchronize()
+        pointers = [out.data_ptr() for out in outputs]
         gc.collect()
         gc.disable()
         try:
             allocated, reserved = torch.cuda.memory_allocated(), torch.cuda.memory_reserved()
-            for got in outputs:
-                _lib.check(lib, lib.mgb_dft_contract_noalloc(samples.data_ptr(), *args, got.data_ptr(), stream))
+            for ptr in pointers:
+                _lib.check(lib, lib.mgb_dft_contract_noalloc(samples.data_ptr(), *args, ptr, stream))
             torch.cuda.synchronize()
             after = (torch.cuda.memory_allocated(), torch.cuda.memory_reserved())
         finally:
             gc.enable()
         assert after == (allocated, reserved)
-        for got in outputs:
-            assert torch.equal(got, expected), (nfreq, ncols, nsamples)
+        for out in outputs:
+            assert torch.equal(out, expected), (nfreq, ncols, nsamples)
         assert not torch.equal(expected, acc0)
     _lib.check(lib, lib.mgb_dft_contract_status(status.data_ptr(), 0, stream))
     torch.cuda.synchronize()

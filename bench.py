@@ -116,7 +116,8 @@ def step_launches(engine, first: int, steps: int) -> int:
     monitor due after a step either its accumulation (step by step) or its sample plus,
     every MGB_DFT_DEPTH samples, a phase table and a contraction per time group (E, H)."""
     from meep_gpu_gb300 import _lib
-    count = 2 * steps
+    # the two halves, each as one launch or as one launch per x range
+    count = 2 * steps * max(1, getattr(engine, "split", 0) or 1)
     for index, m in enumerate(engine.monitors):
         due = sum(1 for n in range(first, first + steps) if (n + 1) % m.decimation_factor == 0)
         if engine.dft_samples[index] is None:
@@ -303,6 +304,7 @@ def main():
     driver.step_many(args.warmup)  # freezes the configuration and warms the kernels
     engine = driver.engine
     choice = list(engine.choice) if engine.choice is not None else None
+    split, wave = getattr(engine, "split", 0), getattr(engine, "wave", None)
     cells = driver.grid.total_cells
     first = driver.step_count
     engine.ensure_source_words(first, args.steps)
@@ -436,7 +438,8 @@ def main():
         "config": workload_config(args.workload, cells, world),
         "kernels": {"h_half": family_name(choice[0]) if choice else None,
                     "e_half": family_name(choice[1]) if choice else None,
-                    "choice": choice, "chosen_by": "argument" if kernels else "autotuner"},
+                    "choice": choice, "x_range_split": split, "wave": wave,
+                    "chosen_by": "argument" if kernels else "autotuner"},
         "monitors": {"flux_planes": len(flux), "dft_volumes": len(dft),
                      "decimation": [m.decimation_factor for m in list(flux) + list(dft)][:1]},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,

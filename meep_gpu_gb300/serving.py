@@ -385,6 +385,115 @@ class BatchServer:
             pass
 
 
+class _Marks:
+    """Events at the end of the work queued on several batch streams."""
+
+    def __init__(self, events):
+        self.events = events
+
+    def synchronize(self) -> None:
+        for event in self.events:
+            event.synchronize()
+
+    def query(self) -> bool:
+        return all(event.query() for event in self.events)
+
+
+class MultiBatchServer:
+    """Several batches, each on its own stream and CUDA graph, behind one server's calls.
+
+    The slots of different batches are independent simulations, so nothing orders one
+    batch's launches after another's: the GPU fills the tail of one batch's step launch
+    with the other batches' work instead of idling SMs at every half. A request goes to
+    the batch with the fewest resident cells that has room for it (both slots of a
+    complex request to the same batch: with a Bloch phase its parts read each other).
+    """
+
+    def __init__(self, device: Optional[torch.device] = None, groups: int = 2, max_slots: int = 32,
+                 budget_bytes: Optional[int] = None, steps_per_replay: int = 64, use_graph: bool = True,
+                 shape: Optional[Tuple[int, int, int]] = None, max_side: int = max(SIDES),
+                 max_monitor_cells: Optional[int] = None):
+        groups = max(1, int(groups))
+        if budget_bytes is None:
+            free, _total = torch.cuda.mem_get_info(device)
+            budget_bytes = int(0.5 * free)
+        per_slots = max(2, -(-int(max_slots) // groups))
+        self.servers = [BatchServer(device, max_slots=per_slots, budget_bytes=int(budget_bytes) // groups,
+                                    steps_per_replay=steps_per_replay, use_graph=use_graph, shape=shape,
+                                    max_side=max_side, max_monitor_cells=max_monitor_cells)
+                        for _ in range(groups)]
+        self.max_slots = per_slots * groups
+        self.cells: List[int] = [0] * groups
+        self.owner: Dict[int, int] = {}
+
+    @property
+    def active(self) -> int:
+        return sum(server.active for server in self.servers)
+
+    @property
+    def draining(self) -> list:
+        return [job for server in self.servers for job in server.draining]
+
+    @property
+    def replays(self) -> int:
+        return sum(server.replays for server in self.servers)
+
+    @property
+    def shape(self):
+        return self.servers[0].shape
+
+    def autotune(self, sides: Sequence[int] = SIDES, steps: int = 8):
+        shape = self.servers[0].autotune(sides, steps)
+        for server in self.servers[1:]:
+            server.set_shape(shape)
+        return shape
+
+    def fits(self, nbytes: int, slots: int = 1) -> bool:
+        return any(server.fits(nbytes, slots) for server in self.servers)
+
+    def admit(self, job: _Job, now: float) -> None:
+        room = [g for g, server in enumerate(self.servers) if server.fits(job.bytes, job.slots_needed)]
+        if not room:
+            raise RuntimeError("admit() needs room in some batch: check fits() first")
+        g = min(room, key=lambda at: self.cells[at])
+        self.servers[g].admit(job, now)
+        self.cells[g] += job.request.side ** 3
+        self.owner[id(job)] = g
+
+    def commit(self) -> None:
+        for server in self.servers:
+            if server.active:
+                server.commit()
+
+    def launch(self, steps: Optional[int] = None) -> None:
+        for server in self.servers:
+            if server.active:
+                server.launch(steps)
+
+    def mark(self) -> _Marks:
+        return _Marks([server.mark() for server in self.servers])
+
+    def finish(self) -> int:
+        count = 0
+        for g, server in enumerate(self.servers):
+            before = set(id(job) for job in server.draining)
+            count += server.finish()
+            for job in server.draining:
+                if id(job) not in before:
+                    self.cells[g] -= job.request.side ** 3
+        return count
+
+    def collect(self, now_fn: Callable[[], float], wait: bool = False) -> List["Result"]:
+        results = []
+        for server in self.servers:
+            results.extend(server.collect(now_fn, wait=wait))
+        return results
+
+    def close(self) -> None:
+        for server in self.servers:
+            server.close()
+
+
 @dataclass
 class Report:
     """Outcome of serving a stream: per-request results and the stream's throughput."""

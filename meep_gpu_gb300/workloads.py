@@ -234,11 +234,16 @@ def main(argv=None) -> None:
     parser.add_argument("--kernels", default=None,
                         help="fixed kernel choice: 4 numbers (family, block_z, block_y, x_chunk) "
                              "or 8 (the H half's, then the E half's); default: autotuned")
+    parser.add_argument("--split", type=int, default=0,
+                        help="with --kernels: launch each half over this many x ranges")
     args = parser.parse_args(argv)
     kernels = None
     if args.kernels:
         values = tuple(int(v) for v in args.kernels.split(","))
         kernels = values if len(values) == 4 else (values[:4], values[4:])
+        if args.split > 1:
+            pair = kernels if len(values) == 8 else (kernels, kernels)
+            kernels = (pair[0], pair[1], None, args.split)
     driver, _, _ = build(args.name, FdtdDriver, kernels=kernels)
     driver.step_many(3)
     torch.cuda.synchronize()
@@ -246,7 +251,7 @@ def main(argv=None) -> None:
     driver.engine.step(driver.step_count, args.steps)
     torch.cuda.synchronize()
     elapsed = time.perf_counter() - start
-    print(f"{args.name}: {driver.grid}, kernels {driver.engine.choice}, "
+    print(f"{args.name}: {driver.grid}, kernels {driver.engine.choice}, split {driver.engine.split}, "
           f"{1e3 * elapsed / max(args.steps, 1):.4f} ms/step over {args.steps} steps")
     driver.close()
 

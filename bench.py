@@ -84,6 +84,8 @@ def parse_args():
     p.add_argument("--serving", type=int, default=512,
                    help="requests in the served stream (0: skip the serving measurement)")
     p.add_argument("--serving-slots", type=int, default=48)
+    p.add_argument("--serving-groups", type=int, default=4,
+                   help="independent batches (own stream and graph each) the slots are spread over")
     p.add_argument("--serving-replay", type=int, default=128, help="steps per captured replay")
     p.add_argument("--serving-budget-gb", type=float, default=16.0)
     p.add_argument("--no-plain", action="store_true", help="skip the one-at-a-time solve")
@@ -461,9 +463,9 @@ def bench_serving(device, args):
     from meep_gpu_gb300 import serving
     requests = serving.make_stream(args.serving, rate=40.0, seed=0)
     warm = [serving.Request(-1 - i, s, 4.0, 0.3 * s, 70, 0.0) for i, s in enumerate(serving.SIDES)]
-    server = serving.BatchServer(device, max_slots=args.serving_slots,
-                                 steps_per_replay=args.serving_replay,
-                                 budget_bytes=int(args.serving_budget_gb * 1e9))
+    server = serving.MultiBatchServer(device, groups=args.serving_groups, max_slots=args.serving_slots,
+                                      steps_per_replay=args.serving_replay,
+                                      budget_bytes=int(args.serving_budget_gb * 1e9))
     shape = server.autotune()
     serving.serve(server, warm, realtime=False)
     torch.cuda.synchronize(device)
@@ -474,7 +476,8 @@ def bench_serving(device, args):
     out = {
         "requests": len(requests), "arrivals": "Poisson 40/s, seed 0",
         "sides": list(serving.SIDES), "steps": "U[1000,4000]", "pml_cells": serving.PML_CELLS,
-        "nfreq": serving.NFREQ, "slots": args.serving_slots, "steps_per_replay": args.serving_replay,
+        "nfreq": serving.NFREQ, "slots": args.serving_slots, "groups": args.serving_groups,
+        "steps_per_replay": args.serving_replay,
         "budget_gb": args.serving_budget_gb, "shape": list(shape), "graph": True,
         "sims_per_s": round(report.sims_per_second, 3),
         "p50_s": round(report.latency_percentile(50), 4),

@@ -174,6 +174,21 @@ def test_served_spectra_equal_the_plain_solve(gpu, use_graph):
 
 
 @pytest.mark.gpu
+def test_grouped_batches_serve_the_plain_spectra(gpu):
+    """Three independent batches on their own streams (one slot each, six requests):
+    every spectrum equals the one-at-a-time solve's."""
+    server = serving.MultiBatchServer(gpu, groups=3, max_slots=3, steps_per_replay=16)
+    assert len(server.servers) == 3 and server.max_slots >= 3
+    report = serving.serve(server, SMALL, realtime=False)
+    server.close()
+    got = report.spectra()
+    assert sorted(got) == [r.index for r in SMALL]
+    for request in SMALL:
+        expected, _ = plain(request, (0, 32, 4, 4))
+        assert np.array_equal(got[request.index], expected), request.index
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("shape", [(32, 4, 4), (64, 2, 8), (32, 8, 2), (64, 4, 1)])
 def test_served_fields_equal_the_plain_solve(gpu, shape):
     """All slots at once under another launch shape: every field word equals the alone run."""

@@ -110,8 +110,11 @@ typedef struct mgb_conductivity {
  * [0]: the B ghosts (H half), [1]: the D ghosts (E half). Entry t of a list: the ghost's
  * cell offset, the offset of the stored word it images, and a code (bits 0-1 the
  * component 0..2, bit 2 negate, bit 3 zero: the ghost sits on a metallic wall of
- * another axis). saved[h]: device scratch of MGB_FOLD_WORDS * count[h] floats, zeroed
- * by the caller, where the library keeps each ghost's state from before its half. */
+ * another axis). Entries are independent (any order steps the same words); lists in
+ * x-plane order of the ghost offsets let the x-range split fold each range's ghosts
+ * with the range (mgb_set_split). saved[h]: device scratch of MGB_FOLD_WORDS * count[h]
+ * floats, zeroed by the caller, where the library keeps each ghost's state from before
+ * its half. */
 #define MGB_FOLD_WORDS (2 + MGB_MAX_POLES)
 typedef struct mgb_fold {
   int32_t count[2];
@@ -297,8 +300,12 @@ int mgb_select_half(mgb_sim* sim, int32_t part, int32_t family, int32_t block_z,
  * with the next ready range and begins a step on the low ranges while the previous one
  * finishes the high ones. mgb_step forks the streams from its stream and joins them back
  * (monitor kernels run on it, joined before and forked after). Generic kernel families
- * only (the tile kernels step every plane in one launch); refused for mirror folds, Bloch
- * phases or a periodic x axis. No reference counterpart. */
+ * only (the tile kernels step every plane in one launch); refused for Bloch phases or a
+ * periodic x axis. On a folded run each range's half is followed on its stream by the
+ * fold of the range's ghosts, which needs ghost lists in x-plane order with every image
+ * in its ghost's plane (plane 2 for plane 0's ghosts of a folded x axis; mgb_create
+ * records whether they are, mgb_set_split refuses them otherwise); with a folded x axis
+ * and ranges under 3 planes mgb_step steps unsplit. No reference counterpart. */
 #define MGB_MAX_SPLIT 16
 
 /* Split each half into `ranges` (2..MGB_MAX_SPLIT) x-range launches; 0 or 1 switches the

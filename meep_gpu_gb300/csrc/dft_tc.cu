@@ -7,13 +7,16 @@
 // accumulator word at each decimated step; here K such steps are buffered and added in
 // one pass, so the accumulators are read and written once per K samples.
 //
-// One CTA (eight warps) owns a 256-column tile of one component: it stages the samples
-// (K = 32 rows) in shared memory as TF32 high and low parts, then for each 128-row tile
-// of phases stages the phase rows the same way, one thread issues the 12 MMAs
-// (4 K-slices x 3 products) into a 128 x 256 float32 accumulator in tensor memory, and
-// every warp reads its 32 lanes back (tcgen05.ld) and adds them to the accumulators in
-// global memory through a shared-memory transpose (coalesced rows). Operands use the
-// canonical K-major layout without swizzle.
+// The table kernel writes the phase rows already split into TF32 high and low parts, in
+// the shared-memory image the MMAs read (canonical K-major layout without swizzle), one
+// 32 KB image per 128-row tile. One CTA (eight warps) owns a 128-column tile of one
+// component: it loads its samples (K = 32 rows), asks L2 for the accumulator rows it
+// will add to, stages the samples in shared memory as TF32 high and low parts, then for
+// each 128-row tile of phases copies the tile's image into shared memory with one bulk
+// asynchronous copy (cp.async.bulk, completing on an mbarrier), one thread issues the 12
+// MMAs (4 K-slices x 3 products) into a 128 x 128 float32 accumulator in tensor memory,
+// and every warp reads its 32 lanes back (tcgen05.ld) and adds them to the accumulators
+// in global memory through a shared-memory transpose (coalesced rows).
 #include "dft_tc.cuh"
 
 #include <cstdint>
@@ -36,6 +39,7 @@ constexpr int kSliceB = kCols * 32;
 constexpr int kTileA = kSliceA * kSlices;  // 16 KB
 constexpr int kTileB = kSliceB * kSlices;  // 32 KB
 constexpr int kSmemBytes = 2 * kTileB + 2 * kTileA + 64;
+constexpr int kTableTile = 2 * kTileA;  // bytes of one 128-row tile's phase image (high, low)
 // Instruction descriptor: D float32 (bits 4-5 = 1), A and B TF32 (bits 7-9, 10-12 = 2),
 // both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28.
 constexpr unsigned kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((unsigned)(kCols >> 3) << 17) |
@@ -117,6 +121,22 @@ __device__ __forceinline__ void mbar_init(unsigned long long* bar) {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
+// Arm the barrier's phase for `bytes` of asynchronous copies (this thread's arrival).
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+// One bulk copy global -> shared (both 16-byte aligned, bytes a multiple of 16), counted
+// on the barrier's transaction bytes.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
   unsigned ok;
   asm volatile(
@@ -148,16 +168,32 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsig
 
 __device__ __forceinline__ int rows_of(int nfreq) { return ((2 * nfreq + kRows - 1) / kRows) * kRows; }
 
-__global__ void __launch_bounds__(256) table_kernel(const double* __restrict__ omega, int nfreq,
-                                                    long long first_post, int stride, double dt,
-                                                    int half_back, double scale, int nsamples,
-                                                    float* __restrict__ table) {
-  const int mpad = rows_of(nfreq);
+// Row m, sample k of the phase table as its tile's shared-memory image: the TF32 high
+// part at the K-major offset of (m mod 128, k) in the tile's first 16 KB, the low part
+// (the TF32 rounding of what the high part leaves) at the same offset in the second.
+__device__ __forceinline__ void put_phase(float* table, int m, int k, float v) {
+  const float h = to_tf32(v);
+  const float l = to_tf32(v - h);
+  unsigned char* tile = reinterpret_cast<unsigned char*>(table) + (size_t)(m / kRows) * kTableTile;
+  const int off = kmajor_offset(m % kRows, k, kSliceA);
+  *reinterpret_cast<float*>(tile + off) = h;
+  *reinterpret_cast<float*>(tile + kTileA + off) = l;
+}
+
+// One thread per (frequency, sample): the cosine and sine rows of one angle (rows 2f and
+// 2f + 1), zero in the padding rows and past nsamples.
+__global__ void __launch_bounds__(64) table_kernel(const double* __restrict__ omega, int nfreq,
+                                                   long long first_post, int stride, double dt,
+                                                   int half_back, double scale, int nsamples,
+                                                   float* __restrict__ table) {
+  // the contraction that follows may start now: it reads this table only after
+  // griddepcontrol.wait, which waits for this grid to complete
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  const int pairs = rows_of(nfreq) / 2;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= mpad * kDepth) return;
-  const int m = idx / kDepth, k = idx % kDepth;
-  const int f = m >> 1;
-  float v = 0.f;
+  if (idx >= pairs * kDepth) return;
+  const int f = idx / kDepth, k = idx % kDepth;
+  float vc = 0.f, vs = 0.f;
   if (f < nfreq && k < nsamples) {
     // the same float64 expressions as the step-by-step phases
     const long long post = first_post + (long long)k * stride;
@@ -165,9 +201,11 @@ __global__ void __launch_bounds__(256) table_kernel(const double* __restrict__ o
     const double t = half_back ? t_e - 0.5 * dt : t_e;
     double s, co;
     sincos(t * omega[f], &s, &co);
-    v = (m & 1) ? (float)(s * scale) : (float)(co * scale);
+    vc = (float)(co * scale);
+    vs = (float)(s * scale);
   }
-  table[idx] = v;
+  put_phase(table, 2 * f, k, vc);
+  put_phase(table, 2 * f + 1, k, vs);
 }
 
 __global__ void __launch_bounds__(kThreads, 3) contract_kernel(const __grid_constant__ Contraction c) {
@@ -176,23 +214,56 @@ __global__ void __launch_bounds__(kThreads, 3) contract_kernel(const __grid_cons
   unsigned char* b_lo = smem + kTileB;
   unsigned char* a_hi = smem + 2 * kTileB;
   unsigned char* a_lo = a_hi + kTileA;
-  unsigned long long* bar = reinterpret_cast<unsigned long long*>(a_lo + kTileA);
-  unsigned* tmem_slot = reinterpret_cast<unsigned*>(bar + 1);
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(a_lo + kTileA);  // MMA commits
+  unsigned long long* tbar = bar + 1;                                               // phase copies
+  unsigned* tmem_slot = reinterpret_cast<unsigned*>(bar + 2);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int q = blockIdx.y;
   static_assert(kThreads == 256, "two warps per 32 tensor-memory lanes");
   const long long n0 = (long long)blockIdx.x * kCols;
 
-  if (warp == 0) tmem_alloc(tmem_slot, kCols);
-  if (tid == 0) mbar_init(bar);
-  // Samples: rows k < nsamples of this component's columns [n0, n0 + 256), zero beyond.
+  const int mpad = rows_of(c.nfreq);
+  const int mrows = 2 * c.nfreq;
+  float* acc = c.acc + c.acc_off[q];
+  // Samples: rows k < nsamples of this component's columns [n0, n0 + 128), zero beyond,
+  // loaded first (all in flight together): the staging waits for them.
   const float* src = c.samples + c.sample_off[q];
-  for (int idx = tid; idx < kDepth * kCols; idx += kThreads) {
+  constexpr int kPerThread = kDepth * kCols / kThreads;
+  float v[kPerThread];
+#pragma unroll
+  for (int u = 0; u < kPerThread; ++u) {
+    const int idx = tid + u * kThreads;
     const int k = idx / kCols, n = idx % kCols;
-    float v = 0.f;
-    if (k < c.nsamples && n0 + n < c.ncols) v = src[(long long)k * c.ld + n0 + n];
-    const float h = to_tf32(v);
-    const float l = to_tf32(v - h);
+    v[u] = (k < c.nsamples && n0 + n < c.ncols) ? __ldcs(src + (long long)k * c.ld + n0 + n) : 0.f;
+  }
+  // Then the accumulator rows of this tile (2 nfreq rows of 128 columns, 512 bytes each)
+  // requested into L2: their DRAM reads overlap the staging and the MMAs instead of
+  // waiting in the epilogue. (The memory clobber keeps the sample loads issued first.)
+  for (int at = tid; at < mrows * (kCols / 32); at += kThreads) {
+    const int r = at / (kCols / 32);
+    const long long n = n0 + (at % (kCols / 32)) * 32;
+    if (n < c.ncols)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(acc + (long long)r * c.acc_ld + n) : "memory");
+  }
+  if (warp == 0) tmem_alloc(tmem_slot, kCols);
+  const int tiles = mpad / kRows;
+  const unsigned char* table = reinterpret_cast<const unsigned char*>(c.table);
+  if (tid == 0) {
+    mbar_init(bar);
+    mbar_init(tbar);
+    // the first phase tile's image, in flight while the samples are staged, once the
+    // table kernel this launch depends on has completed (everything else this kernel
+    // reads was written before that kernel began)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    mbar_expect_tx(tbar, kTableTile);
+    bulk_load(a_hi, table, kTableTile, tbar);
+  }
+#pragma unroll
+  for (int u = 0; u < kPerThread; ++u) {
+    const int idx = tid + u * kThreads;
+    const int k = idx / kCols, n = idx % kCols;
+    const float h = to_tf32(v[u]);
+    const float l = to_tf32(v[u] - h);
     const int off = kmajor_offset(n, k, kSliceB);
     *reinterpret_cast<float*>(b_hi + off) = h;
     *reinterpret_cast<float*>(b_lo + off) = l;
@@ -201,37 +272,38 @@ __global__ void __launch_bounds__(kThreads, 3) contract_kernel(const __grid_cons
   __syncthreads();
   fence_after_sync();
   const unsigned tmem = *tmem_slot;
-  const int mpad = rows_of(c.nfreq);
-  const int mrows = 2 * c.nfreq;
-  float* acc = c.acc + c.acc_off[q];
-  unsigned parity = 0;
-  for (int mt = 0; mt < mpad / kRows; ++mt) {
-    for (int idx = tid; idx < kRows * kDepth; idx += kThreads) {
-      const int r = idx / kDepth, k = idx % kDepth;
-      const float v = c.table[(long long)(mt * kRows + r) * kDepth + k];
-      const float h = to_tf32(v);
-      const float l = to_tf32(v - h);
-      const int off = kmajor_offset(r, k, kSliceA);
-      *reinterpret_cast<float*>(a_hi + off) = h;
-      *reinterpret_cast<float*>(a_lo + off) = l;
-    }
-    // the generic-proxy stores must be visible to the tensor core's reads
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    fence_after_sync();
+  unsigned parity = 0, tparity = 0;
+  for (int mt = 0; mt < tiles; ++mt) {
+    // thread 0: the tile's phase image has landed (bounded wait), then the MMAs
+    bool landed = true;
     if (tid == 0) {
+      landed = mbar_wait_bounded(tbar, tparity);
+      if (landed) {
 #pragma unroll
-      for (int j = 0; j < kSlices; ++j) {
-        const unsigned long long ah = smem_desc(smem_u32(a_hi + j * kSliceA));
-        const unsigned long long al = smem_desc(smem_u32(a_lo + j * kSliceA));
-        const unsigned long long bh = smem_desc(smem_u32(b_hi + j * kSliceB));
-        const unsigned long long bl = smem_desc(smem_u32(b_lo + j * kSliceB));
-        mma_tf32(tmem, ah, bh, j > 0 ? 1u : 0u);
-        mma_tf32(tmem, ah, bl, 1u);
-        mma_tf32(tmem, al, bh, 1u);
+        for (int j = 0; j < kSlices; ++j) {
+          const unsigned long long ah = smem_desc(smem_u32(a_hi + j * kSliceA));
+          const unsigned long long al = smem_desc(smem_u32(a_lo + j * kSliceA));
+          const unsigned long long bh = smem_desc(smem_u32(b_hi + j * kSliceB));
+          const unsigned long long bl = smem_desc(smem_u32(b_lo + j * kSliceB));
+          mma_tf32(tmem, ah, bh, j > 0 ? 1u : 0u);
+          mma_tf32(tmem, ah, bl, 1u);
+          mma_tf32(tmem, al, bh, 1u);
+        }
+        mma_commit(bar);
       }
-      mma_commit(bar);
     }
+    if (__syncthreads_or(!landed)) {
+      // The copy did not land in time: report, give it one more wait with the normal
+      // bound (shared memory is released only once it has landed, or that wait has run
+      // out too), and leave without an MMA.
+      if (tid == 0) {
+        if (c.status != nullptr) atomicOr(c.status, 4);
+        mbar_wait_bounded(tbar, tparity);
+      }
+      __syncthreads();
+      break;
+    }
+    tparity ^= 1u;
     const unsigned long long limit =
         (mt == 0 && c.first_wait_ns >= 0) ? (unsigned long long)c.first_wait_ns : kWaitLimitNs;
     bool ok = mbar_wait_bounded(bar, parity, limit);
@@ -276,8 +348,14 @@ __global__ void __launch_bounds__(kThreads, 3) contract_kernel(const __grid_cons
       }
       __syncwarp();
     }
+    // the staging's generic-proxy accesses ordered before the next image's bulk copy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     fence_before_sync();
     __syncthreads();  // tensor memory and the phase tile are free for the next tile
+    if (tid == 0 && mt + 1 < tiles) {
+      mbar_expect_tx(tbar, kTableTile);
+      bulk_load(a_hi, table + (size_t)(mt + 1) * kTableTile, kTableTile, tbar);
+    }
   }
   fence_after_sync();
   if (warp == 0) tmem_dealloc(tmem, kCols);
@@ -287,25 +365,39 @@ __global__ void __launch_bounds__(kThreads, 3) contract_kernel(const __grid_cons
 
 int table_rows(int nfreq) { return ((2 * nfreq + kRows - 1) / kRows) * kRows; }
 
-size_t table_bytes(int nfreq) { return (size_t)table_rows(nfreq) * kDepth * sizeof(float); }
+size_t table_bytes(int nfreq) { return (size_t)(table_rows(nfreq) / kRows) * kTableTile; }
 
-cudaError_t launch_table(const double* omega, int nfreq, long long first_post, int stride, double dt,
-                         int half_back, double scale, int nsamples, float* table, cudaStream_t stream) {
-  const int total = table_rows(nfreq) * kDepth;
-  table_kernel<<<(total + 255) / 256, 256, 0, stream>>>(omega, nfreq, first_post, stride, dt, half_back,
-                                                        scale, nsamples, table);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_contract(const Contraction& c, cudaStream_t stream) {
+cudaError_t launch_contraction(const double* omega, long long first_post, int stride, double dt, int half_back,
+                               double scale, const Contraction& c, cudaStream_t stream) {
+  static_assert(kTableTile == kRows * kDepth * 2 * sizeof(float), "a tile image holds its rows' two parts");
+  static_assert(kMaxTableBytes == (size_t)(2 * kMaxFreq / kRows) * kTableTile, "the largest table");
+  // the bulk copies of the phase images start 16-byte aligned
+  if ((reinterpret_cast<uintptr_t>(c.table) & 15u) != 0) return cudaErrorInvalidValue;
   if (c.ncols <= 0 || c.ncomp <= 0) return cudaSuccess;
   // per device, so set at every launch (contractions are rare: one per kDepth samples)
-  const cudaError_t err =
-      cudaFuncSetAttribute(contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+  cudaError_t err = cudaFuncSetAttribute(contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
   if (err != cudaSuccess) return err;
-  const dim3 grid((unsigned)((c.ncols + kCols - 1) / kCols), (unsigned)c.ncomp, 1);
-  contract_kernel<<<grid, kThreads, kSmemBytes, stream>>>(c);
-  return cudaGetLastError();
+  // the table: one (cosine, sine) pair a thread, in blocks of 64 so the float64 work
+  // spreads over many SMs
+  const int total = table_rows(c.nfreq) / 2 * kDepth;
+  table_kernel<<<(total + 63) / 64, 64, 0, stream>>>(omega, c.nfreq, first_post, stride, dt, half_back, scale,
+                                                     c.nsamples, const_cast<float*>(c.table));
+  err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  // the contraction as the table kernel's programmatic dependent: its CTAs start while
+  // the table is formed, load their samples and request their accumulators, and wait
+  // for the table grid (griddepcontrol.wait) only before the first phase copy
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)((c.ncols + kCols - 1) / kCols), (unsigned)c.ncomp, 1);
+  cfg.blockDim = dim3(kThreads, 1, 1);
+  cfg.dynamicSmemBytes = kSmemBytes;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, contract_kernel, c);
 }
 
 }  // namespace mgbdft

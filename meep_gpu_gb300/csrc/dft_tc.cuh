@@ -17,6 +17,9 @@ namespace mgbdft {
 constexpr int kDepth = 32;     // samples per contraction (K)
 constexpr int kMaxFreq = 512;  // 2 * kMaxFreq phase rows at most
 constexpr int kMaxComps = 6;
+// Bytes of the largest phase table: 2 * kMaxFreq rows (a multiple of the 128-row tile),
+// each word as its TF32 high and low parts.
+constexpr size_t kMaxTableBytes = (size_t)2 * kMaxFreq * kDepth * 2 * sizeof(float);
 
 struct Contraction {
   const float* samples;                 // rows k < kDepth, row stride ld
@@ -29,7 +32,8 @@ struct Contraction {
   long long acc_off[kMaxComps];
   long long acc_ld;
   int nfreq;
-  const float* table;                   // [mpad][kDepth] phase rows (see launch_table)
+  const float* table;                   // phase tiles' shared-memory images (launch_contraction),
+                                        // 16-byte aligned
   int* status;                          // ORed with 4 when a tensor-core wait times out
   long long first_wait_ns;              // limit of the first tile's wait; negative: the normal
                                         // limit (a test hook: 0 gives up before waiting)
@@ -40,14 +44,14 @@ int table_rows(int nfreq);
 // Bytes of the phase table for nfreq frequencies.
 size_t table_bytes(int nfreq);
 
-// Phase rows for samples taken after steps first_post + k * stride (k < nsamples) at
-// t = post * dt, less dt / 2 when half_back; rows 2f, 2f + 1 = cos, sin times scale;
-// every other entry of the [table_rows][kDepth] table is written as zero.
-cudaError_t launch_table(const double* omega, int nfreq, long long first_post, int stride,
-                         double dt, int half_back, double scale, int nsamples, float* table,
-                         cudaStream_t stream);
-
-// acc += P . S for every component of the contraction (one launch).
-cudaError_t launch_contract(const Contraction& c, cudaStream_t stream);
+// One contraction: the phase table into c.table, then acc += P . S for every component
+// of c (one launch each). Phase rows for samples taken after steps first_post + k *
+// stride (k < c.nsamples) at t = post * dt, less dt / 2 when half_back; rows 2f, 2f + 1 =
+// cos, sin times scale; every other entry of the table_rows x kDepth phases is zero. The
+// table is written as each 128-row tile's shared-memory image for the MMAs: the TF32
+// high parts in the canonical K-major layout (16 KB), then the low parts (16 KB). The
+// contraction kernel is launched as the table kernel's programmatic dependent.
+cudaError_t launch_contraction(const double* omega, long long first_post, int stride, double dt,
+                               int half_back, double scale, const Contraction& c, cudaStream_t stream);
 
 }  // namespace mgbdft

@@ -1448,26 +1448,27 @@ __device__ __forceinline__ void fold_e_ghost(const StepParams& p, const FoldArgs
   if (!isfinite(e) && p.status != nullptr) atomicOr(p.status, 1);
 }
 
-// After the H half: the B ghosts, and the D ghosts' state for the E half of this step.
+// After the H half: the B ghosts, and the D ghosts' state for the E half of this step
+// (entries [lo, hi) of each list; thread u takes entry lo + u of both).
 __global__ void __launch_bounds__(256) fold_h(const __grid_constant__ StepParams p, const __grid_constant__ FoldArgs f,
                                               int first_step, int parity) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < f.count[0]) fold_h_ghost(p, f, t, first_step);
-  if (t < f.count[1]) fold_keep_e(p, f, t, parity);
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f.lo[0] + u < f.hi[0]) fold_h_ghost(p, f, f.lo[0] + u, first_step);
+  if (f.lo[1] + u < f.hi[1]) fold_keep_e(p, f, f.lo[1] + u, parity);
 }
 
 // After the E half: the D ghosts, and the B ghosts' state for the next step's H half.
 __global__ void __launch_bounds__(256) fold_e(const __grid_constant__ StepParams p, const __grid_constant__ FoldArgs f,
                                               int parity) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < f.count[1]) fold_e_ghost(p, f, t, parity);
-  if (t < f.count[0]) fold_keep_h(p, f, t);
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f.lo[1] + u < f.hi[1]) fold_e_ghost(p, f, f.lo[1] + u, parity);
+  if (f.lo[0] + u < f.hi[0]) fold_keep_h(p, f, f.lo[0] + u);
 }
 
 // The B ghosts' state, when a step is launched without the E fold of the step before.
 __global__ void __launch_bounds__(256) fold_keep(const __grid_constant__ StepParams p, const __grid_constant__ FoldArgs f) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < f.count[0]) fold_keep_h(p, f, t);
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f.lo[0] + u < f.hi[0]) fold_keep_h(p, f, f.lo[0] + u);
 }
 
 }  // namespace
@@ -1498,6 +1499,11 @@ struct mgb_sim {
   bool folded = false;
   FoldArgs fold = {};
   long long fold_kept = -1;
+  // The first entry of each x plane in each ghost list (nx + 1 entries), kept when every
+  // list runs in x-plane order and every ghost's image lies in the ghost's own plane or,
+  // on a folded x axis, two planes above plane 0: the x-range split then folds each
+  // range's ghosts on the range's stream. Empty otherwise.
+  std::vector<int> fold_plane[2];
   size_t h_smem = 0, e_smem = 0, e_ws_smem = 0;
   const double* words = nullptr;
   long long words_first = 0;
@@ -1796,6 +1802,7 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
                                     "(at least 4)");
     fold_mask |= 1 << a;
   }
+  std::vector<int> fold_plane[2];
   if (fold_mask != 0) {
     if (d.bloch_axes != 0) return fail(MGB_ERR_UNSUPPORTED, "a folded run carries no Bloch phase");
     const long long cells = (long long)n[0] * n[1] * n[2];
@@ -1818,6 +1825,19 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
         if (ghost[t] < 0 || ghost[t] >= cells || image[t] < 0 || image[t] >= cells || (code[t] & 3) == 3 ||
             (code[t] & ~15) != 0)
           return fail(MGB_ERR_ARGUMENT, "a mirror-fold ghost entry lies outside the volume");
+      // x-plane offsets of the list, for the x-range split
+      const long long plane_cells = (long long)n[1] * n[2];
+      bool ordered = true;
+      for (int t = 0; t < count && ordered; ++t) {
+        const int gx = (int)(ghost[t] / plane_cells), ix = (int)(image[t] / plane_cells);
+        ordered = (t == 0 || ghost[t - 1] / plane_cells <= gx) && (ix == gx || (gx == 0 && ix == 2));
+      }
+      fold_plane[h].clear();
+      if (ordered) {
+        fold_plane[h].assign(n[0] + 1, count);
+        for (int t = count - 1; t >= 0; --t) fold_plane[h][ghost[t] / plane_cells] = t;
+        for (int x = n[0] - 1; x >= 0; --x) fold_plane[h][x] = std::min(fold_plane[h][x], fold_plane[h][x + 1]);
+      }
     }
   } else if (d.fold.count[0] != 0 || d.fold.count[1] != 0) {
     return fail(MGB_ERR_ARGUMENT, "mirror-fold ghost lists without a mirror plane");
@@ -1899,6 +1919,14 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
       sim->fold.image[h] = d.fold.image[h];
       sim->fold.code[h] = d.fold.code[h];
       sim->fold.saved[h] = d.fold.saved[h];
+      sim->fold.lo[h] = 0;
+      sim->fold.hi[h] = d.fold.count[h];
+    }
+    const bool planes_known = (d.fold.count[0] == 0 || !fold_plane[0].empty()) &&
+                              (d.fold.count[1] == 0 || !fold_plane[1].empty());
+    for (int h = 0; h < 2 && planes_known; ++h) {
+      if (fold_plane[h].empty()) fold_plane[h].assign(n[0] + 1, 0);
+      sim->fold_plane[h] = std::move(fold_plane[h]);
     }
   }
   setup_tiles(sim);
@@ -1970,9 +1998,8 @@ int flush_monitor(mgb_sim* sim, int m, cudaStream_t s) {
     }
     if (c.ncomp == 0) continue;
     c.first_wait_ns = test_wait_limit(1);
-    cudaError_t err = mgbdft::launch_table(mon.omega, mon.nfreq, buf.first_post, mon.decimation, mon.dt, half_back,
-                                           mon.scale, buf.count, buf.table, s);
-    if (err == cudaSuccess) err = mgbdft::launch_contract(c, s);
+    const cudaError_t err =
+        mgbdft::launch_contraction(mon.omega, buf.first_post, mon.decimation, mon.dt, half_back, mon.scale, c, s);
     if (err != cudaSuccess) return cuda_error(err, "tensor-core DFT contraction");
   }
   buf.count = 0;
@@ -2097,22 +2124,31 @@ int launch_part_kernels(mgb_sim* sim, long long n, int part, cudaStream_t s, int
   return MGB_OK;
 }
 
-// One part of step n, with the mirror folds after each half of a folded run.
-int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s) {
-  if (!sim->folded || part == 2) return launch_part_kernels(sim, n, part, s);
-  const StepParams& p = sim->step;
-  const int count = std::max(sim->fold.count[0], sim->fold.count[1]);
-  const unsigned blocks = (unsigned)((count + 255) / 256);
-  if (part == 0 && sim->fold_kept != n && sim->fold.count[0] > 0)
-    fold_keep<<<(unsigned)((sim->fold.count[0] + 255) / 256), 256, 0, s>>>(p, sim->fold);
-  const int rc = launch_part_kernels(sim, n, part, s);
+// One part of step n over x planes [plane0, plane1) (plane1 < 0: every plane), with the
+// mirror folds of those planes' ghosts after each half of a folded run. A ranged call
+// leaves the kept-state step to its caller, which sets it once every range's E half is
+// queued.
+int launch_part(mgb_sim* sim, long long n, int part, cudaStream_t s, int plane0 = 0, int plane1 = -1) {
+  if (!sim->folded || part == 2) return launch_part_kernels(sim, n, part, s, plane0, plane1);
+  FoldArgs f = sim->fold;
+  if (plane1 >= 0) {
+    for (int h = 0; h < 2; ++h) {
+      f.lo[h] = sim->fold_plane[h][plane0];
+      f.hi[h] = sim->fold_plane[h][plane1];
+    }
+  }
+  const int c0 = f.hi[0] - f.lo[0], c1 = f.hi[1] - f.lo[1];
+  const unsigned blocks = (unsigned)((std::max(c0, c1) + 255) / 256);
+  if (part == 0 && sim->fold_kept != n && c0 > 0)
+    fold_keep<<<(unsigned)((c0 + 255) / 256), 256, 0, s>>>(sim->step, f);
+  const int rc = launch_part_kernels(sim, n, part, s, plane0, plane1);
   if (rc != MGB_OK) return rc;
   if (blocks == 0) return MGB_OK;
   if (part == 0) {
-    fold_h<<<blocks, 256, 0, s>>>(sim->step, sim->fold, (int)(n == 0), (int)(n & 1));
+    fold_h<<<blocks, 256, 0, s>>>(sim->step, f, (int)(n == 0), (int)(n & 1));
   } else {
-    fold_e<<<blocks, 256, 0, s>>>(sim->step, sim->fold, (int)(n & 1));
-    sim->fold_kept = n + 1;
+    fold_e<<<blocks, 256, 0, s>>>(sim->step, f, (int)(n & 1));
+    if (plane1 < 0) sim->fold_kept = n + 1;
   }
   return MGB_OK;
 }
@@ -2185,8 +2221,11 @@ int split_planes(const mgb_sim* sim) {
 // that E(n-1, r+1) read), E(n, r) after H(n, r) and H(n, r-1) (it reads H one plane below
 // and overwrites the E that H(n, r-1) read). So the GPU fills a range's tail with the next
 // ready range and starts step n+1 on the low ranges while step n finishes the high ones.
-// The monitors due after a step run on the caller's stream, joined before and forked
-// after; the caller's stream waits for every range at the end.
+// On a folded run each half of a range is followed, on the range's stream, by the fold of
+// the range's ghosts (their images lie in the range: the same plane, or plane 2 for the
+// ghosts of a folded x axis, which the first range holds), so the events above cover the
+// ghost words too. The monitors due after a step run on the caller's stream, joined
+// before and forked after; the caller's stream waits for every range at the end.
 int step_split(mgb_sim* sim, long long first, int nsteps, cudaStream_t origin) {
   mgb_sim::Split& sp = sim->split;
   const int R = sp.ranges;
@@ -2218,7 +2257,7 @@ int step_split(mgb_sim* sim, long long first, int nsteps, cudaStream_t origin) {
         err = cudaStreamWaitEvent(sp.streams[r], sp.e_done[pb][r + 1], 0);
         if (err != cudaSuccess) return cuda_error(err, "split wait");
       }
-      const int rc = launch_part_kernels(sim, n, 0, sp.streams[r], lo[r], hi[r]);
+      const int rc = launch_part(sim, n, 0, sp.streams[r], lo[r], hi[r]);
       if (rc != MGB_OK) return rc;
       err = cudaEventRecord(sp.h_done[b][r], sp.streams[r]);
       if (err != cudaSuccess) return cuda_error(err, "split record");
@@ -2228,11 +2267,12 @@ int step_split(mgb_sim* sim, long long first, int nsteps, cudaStream_t origin) {
         err = cudaStreamWaitEvent(sp.streams[r], sp.h_done[b][r - 1], 0);
         if (err != cudaSuccess) return cuda_error(err, "split wait");
       }
-      const int rc = launch_part_kernels(sim, n, 1, sp.streams[r], lo[r], hi[r]);
+      const int rc = launch_part(sim, n, 1, sp.streams[r], lo[r], hi[r]);
       if (rc != MGB_OK) return rc;
       err = cudaEventRecord(sp.e_done[b][r], sp.streams[r]);
       if (err != cudaSuccess) return cuda_error(err, "split record");
     }
+    sim->fold_kept = n + 1;  // every range's B ghosts' state is kept for step n + 1
     bool due = false;
     for (int m = 0; m < sim->desc.nmonitors; ++m)
       if ((n + 1) % sim->desc.monitors[m].decimation == 0) due = true;
@@ -2287,7 +2327,9 @@ int mgb_step(mgb_sim* sim, int64_t first_step, int32_t nsteps, void* stream) {
   if (rc != MGB_OK) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (sim->wave.on) return step_wave(sim, first_step, nsteps, s);
-  if (sim->split.ranges > 1 && !sim->half[0].tiles && !sim->half[1].tiles)
+  // (a folded x axis images plane 2 onto plane 0: the first range must hold both)
+  if (sim->split.ranges > 1 && !sim->half[0].tiles && !sim->half[1].tiles &&
+      (!sim->folded || sim->desc.mirror[0] == 0 || split_planes(sim) >= 3))
     return step_split(sim, first_step, nsteps, s);
   for (int32_t t = 0; t < nsteps; ++t) {
     const long long n = first_step + t;
@@ -2304,9 +2346,12 @@ int mgb_set_split(mgb_sim* sim, int32_t ranges) {
   if (sim == nullptr) return fail(MGB_ERR_ARGUMENT, "null plan");
   if (ranges < 0 || ranges > MGB_MAX_SPLIT)
     return fail(MGB_ERR_ARGUMENT, "ranges must be 0.." + std::to_string(MGB_MAX_SPLIT));
-  if (ranges > 1 && (sim->folded || sim->step.bloch || !sim->desc.metallic[0]))
-    return fail(MGB_ERR_UNSUPPORTED, "the x-range split steps runs without mirror folds or Bloch phases, on a "
-                                     "metallic x axis");
+  if (ranges > 1 && (sim->step.bloch || !sim->desc.metallic[0]))
+    return fail(MGB_ERR_UNSUPPORTED, "the x-range split steps runs without Bloch phases, on a metallic x axis");
+  if (ranges > 1 && sim->folded && sim->fold_plane[0].empty())
+    return fail(MGB_ERR_UNSUPPORTED, "the x-range split folds each range's ghosts: the ghost lists must run in "
+                                     "x-plane order with each image in its ghost's plane (or plane 2 of a "
+                                     "folded x axis)");
   free_split(sim);
   if (ranges <= 1) return MGB_OK;
   mgb_sim::Split& sp = sim->split;
@@ -2941,7 +2986,7 @@ void mgb_batch_destroy(mgb_batch* b) {
 // until mgb_dft_contract_status clears it.
 namespace {
 
-static __device__ __align__(256) float g_dft_table[2 * mgbdft::kMaxFreq * mgbdft::kDepth];
+static __device__ __align__(256) float g_dft_table[mgbdft::kMaxTableBytes / sizeof(float)];
 static __device__ int g_contract_status;
 
 struct StaticWords {
@@ -3001,9 +3046,8 @@ int contract_with_table(const float* samples, int64_t ld, int64_t ncols, int32_t
   c.table = table;
   c.status = status;
   c.first_wait_ns = test_wait_limit(1);
-  cudaError_t err = mgbdft::launch_table(omega, nfreq, first_step, step_stride, dt, half_step_back ? 1 : 0, scale,
-                                         nsamples, table, s);
-  if (err == cudaSuccess) err = mgbdft::launch_contract(c, s);
+  const cudaError_t err =
+      mgbdft::launch_contraction(omega, first_step, step_stride, dt, half_step_back ? 1 : 0, scale, c, s);
   if (err != cudaSuccess) return cuda_error(err, "tensor-core DFT contraction");
   return MGB_OK;
 }
@@ -3026,6 +3070,7 @@ int mgb_dft_contract(const float* samples, int64_t ld, int64_t ncols, int32_t ns
   if (scratch == nullptr) return fail(MGB_ERR_ARGUMENT, "null argument");
   if (scratch_bytes < mgbdft::table_bytes(nfreq))
     return fail(MGB_ERR_ARGUMENT, "scratch is smaller than mgb_dft_scratch_bytes(nfreq)");
+  if ((reinterpret_cast<uintptr_t>(scratch) & 15u) != 0) return fail(MGB_ERR_ARGUMENT, "scratch must be 16-byte aligned");
   if (nothing) return MGB_OK;
   StaticWords words;
   const int found = static_words(&words);
@@ -3035,15 +3080,14 @@ int mgb_dft_contract(const float* samples, int64_t ld, int64_t ncols, int32_t ns
                              static_cast<cudaStream_t>(stream));
 }
 
-// The phase table of this entry point is g_dft_table (2 * MGB_DFT_MAX_FREQ rows of
-// MGB_DFT_DEPTH words). No word of it must start at zero: the table kernel writes every
+// The phase table of this entry point is g_dft_table (the tile images of 2 *
+// MGB_DFT_MAX_FREQ rows of MGB_DFT_DEPTH words, each word's two TF32 parts: 256 KB). No word of it must start at zero: the table kernel writes every
 // word the contraction then reads. Calls that overlap on the device (different streams,
 // or threads without ordering) share the one table and race.
 int mgb_dft_contract_noalloc(const float* samples, int64_t ld, int64_t ncols, int32_t nsamples,
                              const double* omega, int32_t nfreq, int64_t first_step, int32_t step_stride,
                              double dt, int32_t half_step_back, double scale, float* acc, void* stream) {
-  static_assert(sizeof(g_dft_table) >= (size_t)2 * mgbdft::kMaxFreq * mgbdft::kDepth * sizeof(float),
-                "static table holds the largest contraction");
+  static_assert(sizeof(g_dft_table) >= mgbdft::kMaxTableBytes, "static table holds the largest contraction");
   // every refusal, and a call with no work, returns before the device is touched
   bool nothing = false;
   const int rc = check_contract(samples, ld, ncols, nsamples, omega, nfreq, acc, &nothing);

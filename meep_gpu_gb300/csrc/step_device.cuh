@@ -62,6 +62,9 @@ struct FoldArgs {
   const int32_t* image[2];
   const uint8_t* code[2];
   float* saved[2];
+  // the entries [lo, hi) of each list a launch takes (the whole lists, or one x range's)
+  int lo[2];
+  int hi[2];
 };
 
 // Tensor maps of the tile kernels (each 64-byte aligned, passed as __grid_constant__).

@@ -94,7 +94,9 @@ def fold_ghosts(grid: Grid, family: str) -> Dict[str, np.ndarray]:
     reflect row; each with the product of the component's parities over those axes (the
     near passes, ``zero_metal`` and the far passes compose to that), zero where it sits
     on a metallic wall of an unfolded axis. ``ghost`` / ``image``: int32 cell offsets;
-    ``code``: component | 4 negate | 8 zero."""
+    ``code``: component | 4 negate | 8 zero. Entries run in cell-offset order (x plane
+    first, the components of one cell in turn), so each x plane's ghosts are one run of
+    the list: the x-range split folds a range's ghosts with the range."""
     nx, ny, nz = grid.shape
     strides = (ny * nz, nz, 1)
     ghosts, images, codes = [], [], []
@@ -130,9 +132,11 @@ def fold_ghosts(grid: Grid, family: str) -> Dict[str, np.ndarray]:
         codes.append(q | np.where(sign < 0, 4, 0) | np.where(zero, 8, 0))
     if not ghosts:
         return {"ghost": np.zeros(0, np.int32), "image": np.zeros(0, np.int32), "code": np.zeros(0, np.uint8)}
-    return {"ghost": np.concatenate(ghosts).astype(np.int32),
-            "image": np.concatenate(images).astype(np.int32),
-            "code": np.concatenate(codes).astype(np.uint8)}
+    ghost = np.concatenate(ghosts)
+    order = np.argsort(ghost, kind="stable")
+    return {"ghost": ghost[order].astype(np.int32),
+            "image": np.concatenate(images)[order].astype(np.int32),
+            "code": np.concatenate(codes)[order].astype(np.uint8)}
 
 
 class Engine:
@@ -553,11 +557,10 @@ class Engine:
 
     @property
     def split_eligible(self) -> bool:
-        """Whether the halves can be split into x-range launches (metallic x, no folds, no
-        Bloch phase, generic kernel families)."""
+        """Whether the halves can be split into x-range launches (metallic x, no Bloch
+        phase, generic kernel families; a folded run folds each range's ghosts with it)."""
         grid = self.grid
-        return (grid.is_metallic(0) and not grid.has_symmetry and not grid.has_bloch
-                and not self.uses_tiles)
+        return grid.is_metallic(0) and not grid.has_bloch and not self.uses_tiles
 
     def set_split(self, ranges: int) -> None:
         """Launch each half as ``ranges`` x-range launches on the plan's streams (0 or 1:

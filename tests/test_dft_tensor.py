@@ -88,7 +88,11 @@ def test_contraction_refuses_bad_sizes(gpu):
     assert lib.mgb_dft_contract(ptr, 4, 4, 33, ptr, 1, 0, 1, 0.1, 0, 1.0, ptr, ptr, 4096, stream) == -1
     assert lib.mgb_dft_contract(ptr, 4, 4, 1, ptr, 513, 0, 1, 0.1, 0, 1.0, ptr, ptr, 1 << 30, stream) == -1
     assert lib.mgb_dft_contract(ptr, 4, 4, 1, ptr, 8, 0, 1, 0.1, 0, 1.0, ptr, ptr, 16, stream) == -1
-    assert lib.mgb_dft_scratch_bytes(0) == 0 and lib.mgb_dft_scratch_bytes(64) == 128 * 32 * 4
+    # one 128-row tile of 32 samples, each phase as its two TF32 parts
+    assert lib.mgb_dft_scratch_bytes(0) == 0 and lib.mgb_dft_scratch_bytes(64) == 128 * 32 * 4 * 2
+    assert lib.mgb_dft_scratch_bytes(65) == 2 * 128 * 32 * 4 * 2
+    # a scratch that is not 16-byte aligned is refused before the device is touched
+    assert lib.mgb_dft_contract(ptr, 4, 4, 1, ptr, 8, 0, 1, 0.1, 0, 1.0, ptr, ptr + 4, 1 << 20, stream) == -1
 
 
 def sphere(dft_accumulation, steps):

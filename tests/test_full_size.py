@@ -98,3 +98,39 @@ def test_192_cube_workloads_are_the_oracle_words(gpu, name, steps):
             scale = max(float(np.max(np.abs(expected))), 1e-300)
             assert np.max(np.abs(got - expected)) <= 1e-5 * scale, f"dft {index} {c}"
     driver.close()
+
+
+def test_folded_192_split_is_the_oracle_words(gpu):
+    """The folded 192^3 case (the eight-DFT sphere under an even Y and an odd Z plane,
+    192 x 97 x 97 stored cells) with each half split into three x ranges, each range's
+    ghosts folded on the range's stream: every word equal to the float32 oracle's after
+    120 steps run as 1 + 39 + 80 (each call starts without the step before's E fold, so
+    every range keeps its B ghosts' state first), every monitor's transforms within 1e-5
+    of their peak."""
+    chunks = (1, 39, 80)
+    driver, flux, dft = workloads.build("mirror192", FdtdDriver)
+    driver.kernels = ((4, 32, 4, 4), (4, 16, 16, 4), None, 3)
+    for chunk in chunks:
+        driver.run(num_steps=chunk, progress_interval=chunk)
+    assert driver.engine.split == 3
+    _oracle_threads()
+    mine, _, _ = workloads.build("mirror192", FdtdDriver)
+    oracle = Oracle(problem_from_driver(mine), "f32")
+    oracle.run(sum(chunks))
+    for c in FIELDS:
+        bad = int(np.sum(driver.get_field(c, cell_centered=False) != oracle.field(c)))
+        assert bad == 0, f"mirror192 {c}: {bad} words differ from the float32 oracle"
+    for index, monitor in enumerate(flux):
+        expected = oracle.flux_spectrum(index)
+        got = monitor.get_flux_spectrum()
+        assert np.max(np.abs(got - expected)) <= 1e-5 * max(np.max(np.abs(expected)), 1e-300), f"flux {index}"
+    for index, monitor in enumerate(dft):
+        for c in monitor.components:
+            expected = oracle.dft(len(flux) + index, c)
+            got = monitor.raw(c).reshape(expected.shape)
+            # (after 120 steps the pulse has not reached every DFT volume: a transform
+            # still below float32's normal range is compared at that floor)
+            scale = max(float(np.max(np.abs(expected))), 1.2e-38)
+            assert np.max(np.abs(got - expected)) <= 1e-5 * scale, f"dft {index} {c}"
+    assert driver.engine.status.item() == 0
+    driver.close()

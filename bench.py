@@ -584,6 +584,7 @@ def adjoint_section(args) -> dict:
         fd_source = "float64 oracle, this run"
     ad = [float(grad[v]) for v in picks]
     ad_dir = float(np.sum(grad * direction))
+    reverse = adjoint_reverse_roofline(problem, steps)
     line = {
         "metric": "adjoint gradient (96^3, 4000 steps, checkpoints every 200)",
         "objective": float(value.item()), "objective_f64": j64,
@@ -595,11 +596,61 @@ def adjoint_section(args) -> dict:
         "fd_rel_l2": float(np.linalg.norm(np.array(ad) - np.array(fd)) / np.linalg.norm(fd)) if fd else None,
         "directional": {"adjoint": ad_dir, "fd_f64": fd_dir, "rel_err": abs(ad_dir - fd_dir) / abs(fd_dir)},
         "h": h, "fd_source": fd_source, "box": [list(b) for b in box],
+        "reverse_step": reverse,
         "data": "synthetic (seeded eps ~ U[1,12])",
         "reference_adjoint": "unavailable: the reference has no adjoint gradient",
     }
     problem.close()
     return line
+
+
+def adjoint_reverse_roofline(problem, steps: int, reps: int = 60) -> dict:
+    """The reverse step alone (``mgb_adjoint_step``: the transposed E half, then the
+    transposed H half), timed with CUDA events over ``reps`` reversals of the last step
+    after the gradient has been read (the words it leaves are not used), against its
+    algorithmic bytes: per cell, the transposed E half reads the adjoint E, D and mu_B (3
+    volumes each) and each distinct inverse-epsilon volume and writes E, D and mu_D (3
+    each); the transposed H half reads H and mu_D and writes H and mu_B (3 each); on the
+    PML slabs each auxiliary the forward half touches is read and written once
+    (``fu``/``f_w`` of D and E; ``fu`` of B, the slab B and ``f_w`` of H); over the
+    gradient box the saved D (3 words) is read and the gradient read and written."""
+    import ctypes
+
+    import torch
+
+    engine = problem.engine
+    lib = engine.lib
+    stream = problem.stream
+    word = 4
+    cells = engine.grid.total_cells
+    aux = lambda name: sum(engine.aux_cells[f"{name}{a}"] for a in "xyz") if engine.pml is not None else 0  # noqa: E731
+    distinct_inv = len({t.data_ptr() for t in engine.inv_eps})
+    box_cells = int(np.prod([b1 - b0 for b0, b1 in problem.box]))
+    e_bytes = word * ((18 + distinct_inv) * cells + 2 * aux("fuD") + 2 * aux("fwE") + 5 * box_cells)
+    h_bytes = word * (12 * cells + 2 * aux("fuB") + 2 * aux("B") + 2 * aux("fwH"))
+    args = ctypes.byref(problem.adj)
+    handle = stream.cuda_stream
+    for _ in range(3):
+        _lib_check(lib, lib.mgb_adjoint_step(problem.adj_handle, args, steps - 1, handle))
+    marks = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    torch.cuda.synchronize()
+    marks[0].record(stream)
+    for _ in range(reps):
+        _lib_check(lib, lib.mgb_adjoint_step(problem.adj_handle, args, steps - 1, handle))
+    marks[1].record(stream)
+    torch.cuda.synchronize()
+    ms = marks[0].elapsed_time(marks[1]) / reps
+    peak, source = measured_peaks()
+    gbs = (e_bytes + h_bytes) / (ms / 1e3) / 1e9
+    return {"ms": round(ms, 4), "algorithmic_bytes": e_bytes + h_bytes,
+            "bytes_e": e_bytes, "bytes_h": h_bytes, "gbs": round(gbs, 1),
+            "hbm_frac": round(gbs / peak, 3), "peak_gbs": peak, "peak_source": source,
+            "note": f"{reps} reversals of the last step, CUDA events; two launches each"}
+
+
+def _lib_check(lib, rc):
+    from meep_gpu_gb300 import _lib
+    _lib.check(lib, rc)
 
 
 def bench_dft(args):

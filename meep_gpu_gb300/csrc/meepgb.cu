@@ -1085,14 +1085,19 @@ __device__ __forceinline__ float coef(const float* table, bool pml, int at) {
   return pml ? __ldg(table + at) : 1.f;
 }
 
-// Reverse of the E half: gather mu_B, transposed D/E update, mu_D, gradient.
-template <bool PML>
-__global__ void __launch_bounds__(256) adj_e(const __grid_constant__ StepParams p,
-                                             const __grid_constant__ AdjParams a, int xchunk) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  if (k >= p.nz || j >= p.ny) return;
-  const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+__device__ __forceinline__ constexpr bool axis_on(int ax, int a) { return ax >= 0 && ((ax >> a) & 1) != 0; }
+
+// The reverse marches below are compiled per CTA for the axes whose memberships the CTA
+// reaches (AX, as the forward kernels are; -1 with PML false: none): along any other axis
+// every membership is empty and every coefficient exactly 1 for the CTA's cells, so those
+// loads and tests drop out and the words are those of the general form. The x
+// neighbours of mu carry from plane to plane in registers, and the chunk's planes are
+// requested into L2 before the march.
+
+// One thread's column (j, k) of the reverse E half over planes [i0, i1): gather mu_B,
+// transposed D/E update, mu_D, gradient.
+template <bool PML, int AX>
+__device__ __forceinline__ void adj_e_march(const StepParams& p, const AdjParams& a, int j, int k, int i0, int i1) {
   const int sx = p.ny * p.nz, sy = p.nz;
   const float dtdx = p.dtdx;
   // "c - y": the cell whose forward (+y) neighbour is this one: none on a metallic
@@ -1102,20 +1107,36 @@ __global__ void __launch_bounds__(256) adj_e(const __grid_constant__ StepParams 
   const int box_ny = a.box[3] - a.box[2], box_nz = a.box[5] - a.box[4];
   const bool jk_in_box = j >= a.box[2] && j < a.box[3] && k >= a.box[4] && k < a.box[5];
   const long long box_cells = (long long)(a.box[1] - a.box[0]) * box_ny * box_nz;
+  const int col = j * sy + k;
+  {
+    const float* vols[12] = {p.E[0], p.E[1], p.E[2], p.D[0], p.D[1], p.D[2],
+                             a.mu_b[0], a.mu_b[1], a.mu_b[2], p.inv_eps[0], p.inv_eps[1], p.inv_eps[2]};
+    prefetch_planes(vols, p.inv_eps[1] == p.inv_eps[0] ? 10 : 12, i0 * sx + col, sx, i1 - i0);
+  }
+  // mu_B of y and z components one plane below (x neighbours), carried
+  float mb1_xm = 0.f, mb2_xm = 0.f;
+  {
+    const int im = i0 > 0 ? i0 - 1 : (p.met[0] ? -1 : p.nx - 1);
+    if (im >= 0) {
+      mb1_xm = a.mu_b[1][im * sx + col];
+      mb2_xm = a.mu_b[2][im * sx + col];
+    }
+  }
   for (int i = i0; i < i1; ++i) {
-    const int im = i > 0 ? i - 1 : (p.met[0] ? -1 : p.nx - 1);
-    const int c = i * sx + j * sy + k;
+    const int c = i * sx + col;
     const int cym = jm >= 0 ? i * sx + jm * sy + k : -1;
     const int czm = km >= 0 ? i * sx + j * sy + km : -1;
-    const int cxm = im >= 0 ? im * sx + j * sy + k : -1;
     auto mb = [&](int q, int at) { return at >= 0 ? a.mu_b[q][at] : 0.f; };
+    const float mb0 = a.mu_b[0][c], mb1 = a.mu_b[1][c], mb2 = a.mu_b[2][c];
     // Transpose of the H half's curls (forward differences):
     //   cx = dtdx*((Ez[+y] - Ez) + Ey - Ey[+z]), cy = dtdx*((Ex[+z] - Ex) + Ez - Ez[+x]),
     //   cz = dtdx*((Ey[+x] - Ey) + Ex - Ex[+y]).
     float le[3];
-    le[0] = p.E[0][c] + dtdx * ((mb(1, czm) - mb(1, c)) + (mb(2, c) - mb(2, cym)));
-    le[1] = p.E[1][c] + dtdx * ((mb(0, c) - mb(0, czm)) + (mb(2, cxm) - mb(2, c)));
-    le[2] = p.E[2][c] + dtdx * ((mb(0, cym) - mb(0, c)) + (mb(1, c) - mb(1, cxm)));
+    le[0] = p.E[0][c] + dtdx * ((mb(1, czm) - mb1) + (mb2 - mb(2, cym)));
+    le[1] = p.E[1][c] + dtdx * ((mb0 - mb(0, czm)) + (mb2_xm - mb2));
+    le[2] = p.E[2][c] + dtdx * ((mb(0, cym) - mb0) + (mb1 - mb1_xm));
+    mb1_xm = mb1;
+    mb2_xm = mb2;
     const bool wx = p.met[0] && i == 0, wy = p.met[1] && j == 0, wz = p.met[2] && k == 0;
     const int coord[3] = {i, j, k};
     float grad = 0.f;
@@ -1126,12 +1147,13 @@ __global__ void __launch_bounds__(256) adj_e(const __grid_constant__ StepParams 
     for (int q = 0; q < 3; ++q) {
       const int a1 = (q + 1) % 3, a2 = (q + 2) % 3;
       const bool masked = q == 0 ? (wy || wz) : q == 1 ? (wx || wz) : (wx || wy);
-      const bool own = PML && in_runs(p.fwE[q], coord[q]);
-      const bool f = PML && in_runs(p.fuD[q], coord[a2]);
-      const float k1 = coef(p.kms[kInteger][a1], PML, coord[a1]);
-      const float s1 = coef(p.sinv[kInteger][a1], PML, coord[a1]);
-      const float k2 = coef(p.kms[kInteger][a2], PML, coord[a2]);
-      const float s2 = coef(p.sinv[kInteger][a2], PML, coord[a2]);
+      const bool own = PML && axis_on(AX, q) && in_runs(p.fwE[q], coord[q]);
+      const bool f = PML && axis_on(AX, a2) && in_runs(p.fuD[q], coord[a2]);
+      const bool c1 = PML && axis_on(AX, a1), c2 = PML && axis_on(AX, a2);
+      const float k1 = coef(p.kms[kInteger][a1], c1, coord[a1]);
+      const float s1 = coef(p.sinv[kInteger][a1], c1, coord[a1]);
+      const float k2 = coef(p.kms[kInteger][a2], c2, coord[a2]);
+      const float s2 = coef(p.sinv[kInteger][a2], c2, coord[a2]);
       // E' = E + (kps*w - kms*fw), fw' = w on the own membership; E' = w elsewhere.
       float lw = le[q], le_in = 0.f;
       if (own) {
@@ -1165,34 +1187,41 @@ __global__ void __launch_bounds__(256) adj_e(const __grid_constant__ StepParams 
   }
 }
 
-// Reverse of the H half: gather mu_D, transposed B/H update, mu_B.
-template <bool PML>
-__global__ void __launch_bounds__(256) adj_h(const __grid_constant__ StepParams p,
-                                             const __grid_constant__ AdjParams a, int xchunk) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  if (k >= p.nz || j >= p.ny) return;
-  const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+// One thread's column (j, k) of the reverse H half over planes [i0, i1): gather mu_D,
+// transposed B/H update, mu_B.
+template <bool PML, int AX>
+__device__ __forceinline__ void adj_h_march(const StepParams& p, const AdjParams& a, int j, int k, int i0, int i1) {
   const int sx = p.ny * p.nz, sy = p.nz;
   const float dtdx = p.dtdx;
   // "c + y": the cell whose backward (-y) neighbour is this one: none on a metallic axis
   // at the top, row 0 on a periodic one.
   const int jp = j + 1 < p.ny ? j + 1 : (p.met[1] ? -1 : 0);
   const int kp = k + 1 < p.nz ? k + 1 : (p.met[2] ? -1 : 0);
+  const int col = j * sy + k;
+  {
+    const float* vols[6] = {p.H[0], p.H[1], p.H[2], a.mu_d[0], a.mu_d[1], a.mu_d[2]};
+    prefetch_planes(vols, 6, i0 * sx + col, sx, i1 - i0);
+  }
+  // mu_D of y and z components at this plane, carried from the plane below's x neighbour
+  float md1 = a.mu_d[1][i0 * sx + col], md2 = a.mu_d[2][i0 * sx + col];
   for (int i = i0; i < i1; ++i) {
     const int ip = i + 1 < p.nx ? i + 1 : (p.met[0] ? -1 : 0);
-    const int c = i * sx + j * sy + k;
+    const int c = i * sx + col;
     const int cyp = jp >= 0 ? i * sx + jp * sy + k : -1;
     const int czp = kp >= 0 ? i * sx + j * sy + kp : -1;
-    const int cxp = ip >= 0 ? ip * sx + j * sy + k : -1;
+    const int cxp = ip >= 0 ? ip * sx + col : -1;
     auto md = [&](int q, int at) { return at >= 0 ? a.mu_d[q][at] : 0.f; };
+    const float md0 = a.mu_d[0][c];
+    const float md1_xp = md(1, cxp), md2_xp = md(2, cxp);
     // Transpose of the E half's curls (backward differences):
     //   cx = dtdx*((Hz[-y] - Hz) + Hy - Hy[-z]), cy = dtdx*((Hx[-z] - Hx) + Hz - Hz[-x]),
     //   cz = dtdx*((Hy[-x] - Hy) + Hx - Hx[-y]).
     float lh[3];
-    lh[0] = p.H[0][c] + dtdx * ((md(1, czp) - md(1, c)) + (md(2, c) - md(2, cyp)));
-    lh[1] = p.H[1][c] + dtdx * ((md(0, c) - md(0, czp)) + (md(2, cxp) - md(2, c)));
-    lh[2] = p.H[2][c] + dtdx * ((md(0, cyp) - md(0, c)) + (md(1, c) - md(1, cxp)));
+    lh[0] = p.H[0][c] + dtdx * ((md(1, czp) - md1) + (md2 - md(2, cyp)));
+    lh[1] = p.H[1][c] + dtdx * ((md0 - md(0, czp)) + (md2_xp - md2));
+    lh[2] = p.H[2][c] + dtdx * ((md(0, cyp) - md0) + (md1 - md1_xp));
+    md1 = md1_xp;
+    md2 = md2_xp;
     const int coord[3] = {i, j, k};
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
@@ -1200,12 +1229,13 @@ __global__ void __launch_bounds__(256) adj_h(const __grid_constant__ StepParams 
       // zero_metal_B: the curl and the new word of B_q are 0 at index 0 of a metallic
       // own axis (never an own-axis membership cell).
       const bool wall = p.met[q] && coord[q] == 0;
-      const bool own = PML && in_runs(p.B[q], coord[q]);
-      const bool f = PML && in_runs(p.fuB[q], coord[a2]);
-      const float k1 = coef(p.kms[kHalf][a1], PML, coord[a1]);
-      const float s1 = coef(p.sinv[kHalf][a1], PML, coord[a1]);
-      const float k2 = coef(p.kms[kHalf][a2], PML, coord[a2]);
-      const float s2 = coef(p.sinv[kHalf][a2], PML, coord[a2]);
+      const bool own = PML && axis_on(AX, q) && in_runs(p.B[q], coord[q]);
+      const bool f = PML && axis_on(AX, a2) && in_runs(p.fuB[q], coord[a2]);
+      const bool c1 = PML && axis_on(AX, a1), c2 = PML && axis_on(AX, a2);
+      const float k1 = coef(p.kms[kHalf][a1], c1, coord[a1]);
+      const float s1 = coef(p.sinv[kHalf][a1], c1, coord[a1]);
+      const float k2 = coef(p.kms[kHalf][a2], c2, coord[a2]);
+      const float s2 = coef(p.sinv[kHalf][a2], c2, coord[a2]);
       // H' = H + (kps*b' - kms*fw) (step 0: b' + (kps*b' - kms*b')), fw' = b', B' = b' on
       // the own membership; elsewhere H' = b' and H's storage is B's word.
       float lb;
@@ -1245,6 +1275,42 @@ __global__ void __launch_bounds__(256) adj_h(const __grid_constant__ StepParams 
       a.mu_b[q][c] = wall ? 0.f : mu;
     }
   }
+}
+
+// Reverse of the E half, one CTA per (z, y) tile and x chunk.
+template <bool PML>
+__global__ void __launch_bounds__(256) adj_e(const __grid_constant__ StepParams p,
+                                             const __grid_constant__ AdjParams a, int xchunk) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (k >= p.nz || j >= p.ny) return;
+  const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  if (!PML) {
+    adj_e_march<false, -1>(p, a, j, k, i0, i1);
+    return;
+  }
+#define MGB_MARCH(AXV, PMLV) adj_e_march<PMLV, AXV>(p, a, j, k, i0, i1)
+  MGB_AXES_SWITCH(cta_axes(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x),
+                  MGB_MARCH)
+#undef MGB_MARCH
+}
+
+// Reverse of the H half.
+template <bool PML>
+__global__ void __launch_bounds__(256) adj_h(const __grid_constant__ StepParams p,
+                                             const __grid_constant__ AdjParams a, int xchunk) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (k >= p.nz || j >= p.ny) return;
+  const int i0 = blockIdx.z * xchunk, i1 = min(i0 + xchunk, p.nx);
+  if (!PML) {
+    adj_h_march<false, -1>(p, a, j, k, i0, i1);
+    return;
+  }
+#define MGB_MARCH(AXV, PMLV) adj_h_march<PMLV, AXV>(p, a, j, k, i0, i1)
+  MGB_AXES_SWITCH(cta_axes(p, i0, i1, blockIdx.y * blockDim.y, blockDim.y, blockIdx.x * blockDim.x, blockDim.x),
+                  MGB_MARCH)
+#undef MGB_MARCH
 }
 
 // Adjoint of one DFT sample taken after step post - 1: the sample's adjoint

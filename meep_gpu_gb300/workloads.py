@@ -220,7 +220,9 @@ def adjoint96(eps_box=None, driver_cls=None, seed: int = 0, **driver_kwargs):
 
 def main(argv=None) -> None:
     """Build one workload on the GPU and step it: ``python -m meep_gpu_gb300.workloads NAME
-    [--steps K]`` (three steps to make the plan and choose its kernels, then K timed)."""
+    [--steps K]`` (three steps to make the plan and choose its kernels, then K timed).
+    ``adjoint96``: the adjoint gradient over K steps (checkpoints every min(200, K)),
+    forward and backward once to make the plans, then once timed."""
     import argparse
     import time
 
@@ -229,7 +231,7 @@ def main(argv=None) -> None:
     from .driver import FdtdDriver
 
     parser = argparse.ArgumentParser(description=main.__doc__)
-    parser.add_argument("name", choices=WORKLOADS)
+    parser.add_argument("name", choices=tuple(WORKLOADS) + ("adjoint96",))
     parser.add_argument("--steps", type=int, default=10)
     parser.add_argument("--kernels", default=None,
                         help="fixed kernel choice: 4 numbers (family, block_z, block_y, x_chunk) "
@@ -237,6 +239,26 @@ def main(argv=None) -> None:
     parser.add_argument("--split", type=int, default=0,
                         help="with --kernels: launch each half over this many x ranges")
     args = parser.parse_args(argv)
+    if args.name == "adjoint96":
+        from .adjoint import FluxAdjoint
+
+        driver, flux, box, eps_box = adjoint96()
+        problem = FluxAdjoint(driver, flux, box, args.steps, checkpoint_every=min(200, args.steps))
+        eps = torch.from_numpy(eps_box)
+        problem.forward(eps)
+        problem.backward()
+        torch.cuda.synchronize()
+        start = time.perf_counter()
+        problem.forward(eps)
+        middle = time.perf_counter()
+        problem.backward()
+        torch.cuda.synchronize()
+        stop = time.perf_counter()
+        print(f"adjoint96: {driver.grid}, {args.steps} steps, forward {1e3 * (middle - start):.2f} ms, "
+              f"backward {1e3 * (stop - middle):.2f} ms")
+        problem.close()
+        driver.close()
+        return
     kernels = None
     if args.kernels:
         values = tuple(int(v) for v in args.kernels.split(","))

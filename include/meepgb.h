@@ -126,7 +126,8 @@ typedef struct mgb_fold {
 
 typedef struct mgb_sim_desc {
   int32_t abi_version; /* MGB_ABI_VERSION */
-  int32_t nx, ny, nz;  /* at least 2 each, fewer than 2^31 cells in all */
+  int32_t nx, ny, nz;  /* at least 1 each (an axis of one cell is periodic: MEEP's unit
+                        * direction, the invariant z of a 2-D run), fewer than 2^31 cells */
   int32_t metallic[3]; /* 1: PEC walls on that axis; 0: periodic wrap */
   float dtdx;          /* float32(dt / dx) */
   int32_t pml_active;

@@ -1126,29 +1126,48 @@ __device__ __forceinline__ void adj_e_march(const StepParams& p, const AdjParams
     const int c = i * sx + col;
     const int cym = jm >= 0 ? i * sx + jm * sy + k : -1;
     const int czm = km >= 0 ? i * sx + j * sy + km : -1;
+    const int coord[3] = {i, j, k};
+    const bool in_box = jk_in_box && i >= a.box[0] && i < a.box[1];
+    const long long bcell =
+        in_box ? ((long long)(i - a.box[0]) * box_ny + (j - a.box[2])) * box_nz + (k - a.box[4]) : 0;
+    // Every word the cell reads, before any store: the stores of one component could
+    // alias the next one's loads for all the compiler knows, so loads placed between
+    // them would each wait a round trip; gathered here they are one.
+    bool own[3], fm[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      own[q] = PML && axis_on(AX, q) && in_runs(p.fwE[q], coord[q]);
+      fm[q] = PML && axis_on(AX, (q + 2) % 3) && in_runs(p.fuD[q], coord[(q + 2) % 3]);
+    }
     auto mb = [&](int q, int at) { return at >= 0 ? a.mu_b[q][at] : 0.f; };
     const float mb0 = a.mu_b[0][c], mb1 = a.mu_b[1][c], mb2 = a.mu_b[2][c];
+    const float mb1_zm = mb(1, czm), mb2_ym = mb(2, cym), mb0_zm = mb(0, czm), mb0_ym = mb(0, cym);
+    float e_old[3], d_old[3], inv[3], fw_old[3], fu_old[3], d_after[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      e_old[q] = p.E[q][c];
+      d_old[q] = p.D[q][c];
+      inv[q] = p.inv_eps[q][c];
+      fw_old[q] = own[q] ? p.fwE[q].data[c] : 0.f;
+      fu_old[q] = fm[q] ? p.fuD[q].data[c] : 0.f;
+      d_after[q] = in_box ? a.d_after[(long long)q * box_cells + bcell] : 0.f;
+    }
+    const float grad_old = in_box ? a.grad_inv[bcell] : 0.f;
     // Transpose of the H half's curls (forward differences):
     //   cx = dtdx*((Ez[+y] - Ez) + Ey - Ey[+z]), cy = dtdx*((Ex[+z] - Ex) + Ez - Ez[+x]),
     //   cz = dtdx*((Ey[+x] - Ey) + Ex - Ex[+y]).
     float le[3];
-    le[0] = p.E[0][c] + dtdx * ((mb(1, czm) - mb1) + (mb2 - mb(2, cym)));
-    le[1] = p.E[1][c] + dtdx * ((mb0 - mb(0, czm)) + (mb2_xm - mb2));
-    le[2] = p.E[2][c] + dtdx * ((mb(0, cym) - mb0) + (mb1 - mb1_xm));
+    le[0] = e_old[0] + dtdx * ((mb1_zm - mb1) + (mb2 - mb2_ym));
+    le[1] = e_old[1] + dtdx * ((mb0 - mb0_zm) + (mb2_xm - mb2));
+    le[2] = e_old[2] + dtdx * ((mb0_ym - mb0) + (mb1 - mb1_xm));
     mb1_xm = mb1;
     mb2_xm = mb2;
     const bool wx = p.met[0] && i == 0, wy = p.met[1] && j == 0, wz = p.met[2] && k == 0;
-    const int coord[3] = {i, j, k};
     float grad = 0.f;
-    const bool in_box = jk_in_box && i >= a.box[0] && i < a.box[1];
-    const long long bcell =
-        in_box ? ((long long)(i - a.box[0]) * box_ny + (j - a.box[2])) * box_nz + (k - a.box[4]) : 0;
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
       const int a1 = (q + 1) % 3, a2 = (q + 2) % 3;
       const bool masked = q == 0 ? (wy || wz) : q == 1 ? (wx || wz) : (wx || wy);
-      const bool own = PML && axis_on(AX, q) && in_runs(p.fwE[q], coord[q]);
-      const bool f = PML && axis_on(AX, a2) && in_runs(p.fuD[q], coord[a2]);
       const bool c1 = PML && axis_on(AX, a1), c2 = PML && axis_on(AX, a2);
       const float k1 = coef(p.kms[kInteger][a1], c1, coord[a1]);
       const float s1 = coef(p.sinv[kInteger][a1], c1, coord[a1]);
@@ -1156,22 +1175,21 @@ __device__ __forceinline__ void adj_e_march(const StepParams& p, const AdjParams
       const float s2 = coef(p.sinv[kInteger][a2], c2, coord[a2]);
       // E' = E + (kps*w - kms*fw), fw' = w on the own membership; E' = w elsewhere.
       float lw = le[q], le_in = 0.f;
-      if (own) {
+      if (own[q]) {
         const float kps = __ldg(p.kps[kHalf][q] + coord[q]);
         const float kms = __ldg(p.kms[kHalf][q] + coord[q]);
-        lw = kps * le[q] + p.fwE[q].data[c];
+        lw = kps * le[q] + fw_old[q];
         le_in = le[q];
         p.fwE[q].data[c] = -kms * le[q];
       }
-      if (in_box) grad += lw * a.d_after[(long long)q * box_cells + bcell];
+      if (in_box) grad += lw * d_after[q];
       // w = inv * d'; D' = d'; d' is forced to 0 on the masked wall cells.
-      const float ld = masked ? 0.f : p.D[q][c] + p.inv_eps[q][c] * lw;
+      const float ld = masked ? 0.f : d_old[q] + inv[q] * lw;
       // d' from the curl: split-field recurrence on the dsigu membership, else
       // d' = (k1*d - curl)*s1. fu' is stored even on masked cells (curl 0 there).
       float ld_in, mu;
-      if (f) {
-        const float lu_out = p.fuD[q].data[c];
-        const float ln = s2 * ld + lu_out;
+      if (fm[q]) {
+        const float ln = s2 * ld + fu_old[q];
         ld_in = k2 * s2 * ld;
         p.fuD[q].data[c] = -s2 * ld + k1 * s1 * ln;
         mu = -s1 * ln;
@@ -1183,7 +1201,7 @@ __device__ __forceinline__ void adj_e_march(const StepParams& p, const AdjParams
       p.E[q][c] = le_in;
       a.mu_d[q][c] = masked ? 0.f : mu;
     }
-    if (in_box) a.grad_inv[bcell] += grad;
+    if (in_box) a.grad_inv[bcell] = grad_old + grad;
   }
 }
 
@@ -1210,27 +1228,41 @@ __device__ __forceinline__ void adj_h_march(const StepParams& p, const AdjParams
     const int cyp = jp >= 0 ? i * sx + jp * sy + k : -1;
     const int czp = kp >= 0 ? i * sx + j * sy + kp : -1;
     const int cxp = ip >= 0 ? ip * sx + col : -1;
+    const int coord[3] = {i, j, k};
+    // every word the cell reads, before any store (one round trip, as in the E half)
+    bool own[3], fm[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      own[q] = PML && axis_on(AX, q) && in_runs(p.B[q], coord[q]);
+      fm[q] = PML && axis_on(AX, (q + 2) % 3) && in_runs(p.fuB[q], coord[(q + 2) % 3]);
+    }
     auto md = [&](int q, int at) { return at >= 0 ? a.mu_d[q][at] : 0.f; };
     const float md0 = a.mu_d[0][c];
     const float md1_xp = md(1, cxp), md2_xp = md(2, cxp);
+    const float md1_zp = md(1, czp), md2_yp = md(2, cyp), md0_zp = md(0, czp), md0_yp = md(0, cyp);
+    float h_old[3], fw_old[3], b_old[3], fu_old[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      h_old[q] = p.H[q][c];
+      fw_old[q] = own[q] ? p.fwH[q].data[c] : 0.f;
+      b_old[q] = own[q] ? p.B[q].data[c] : 0.f;
+      fu_old[q] = fm[q] ? p.fuB[q].data[c] : 0.f;
+    }
     // Transpose of the E half's curls (backward differences):
     //   cx = dtdx*((Hz[-y] - Hz) + Hy - Hy[-z]), cy = dtdx*((Hx[-z] - Hx) + Hz - Hz[-x]),
     //   cz = dtdx*((Hy[-x] - Hy) + Hx - Hx[-y]).
     float lh[3];
-    lh[0] = p.H[0][c] + dtdx * ((md(1, czp) - md1) + (md2 - md(2, cyp)));
-    lh[1] = p.H[1][c] + dtdx * ((md0 - md(0, czp)) + (md2_xp - md2));
-    lh[2] = p.H[2][c] + dtdx * ((md(0, cyp) - md0) + (md1 - md1_xp));
+    lh[0] = h_old[0] + dtdx * ((md1_zp - md1) + (md2 - md2_yp));
+    lh[1] = h_old[1] + dtdx * ((md0 - md0_zp) + (md2_xp - md2));
+    lh[2] = h_old[2] + dtdx * ((md0_yp - md0) + (md1 - md1_xp));
     md1 = md1_xp;
     md2 = md2_xp;
-    const int coord[3] = {i, j, k};
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
       const int a1 = (q + 1) % 3, a2 = (q + 2) % 3;
       // zero_metal_B: the curl and the new word of B_q are 0 at index 0 of a metallic
       // own axis (never an own-axis membership cell).
       const bool wall = p.met[q] && coord[q] == 0;
-      const bool own = PML && axis_on(AX, q) && in_runs(p.B[q], coord[q]);
-      const bool f = PML && axis_on(AX, a2) && in_runs(p.fuB[q], coord[a2]);
       const bool c1 = PML && axis_on(AX, a1), c2 = PML && axis_on(AX, a2);
       const float k1 = coef(p.kms[kHalf][a1], c1, coord[a1]);
       const float s1 = coef(p.sinv[kHalf][a1], c1, coord[a1]);
@@ -1240,10 +1272,10 @@ __device__ __forceinline__ void adj_h_march(const StepParams& p, const AdjParams
       // the own membership; elsewhere H' = b' and H's storage is B's word.
       float lb;
       float lh_in = 0.f, lw_in = 0.f;
-      if (own) {
+      if (own[q]) {
         const float kps = __ldg(p.kps[kInteger][q] + coord[q]);
         const float kms = __ldg(p.kms[kInteger][q] + coord[q]);
-        const float extra = p.fwH[q].data[c] + p.B[q].data[c];
+        const float extra = fw_old[q] + b_old[q];
         if (a.first_step) {
           lb = ((1.f + kps) - kms) * lh[q] + extra;
         } else {
@@ -1255,9 +1287,8 @@ __device__ __forceinline__ void adj_h_march(const StepParams& p, const AdjParams
         lb = wall ? 0.f : lh[q];
       }
       float lb_in, mu;
-      if (f) {
-        const float lu_out = p.fuB[q].data[c];
-        const float ln = s2 * lb + lu_out;
+      if (fm[q]) {
+        const float ln = s2 * lb + fu_old[q];
         lb_in = k2 * s2 * lb;
         p.fuB[q].data[c] = -s2 * lb + k1 * s1 * ln;
         mu = -s1 * ln;
@@ -1265,7 +1296,7 @@ __device__ __forceinline__ void adj_h_march(const StepParams& p, const AdjParams
         lb_in = k1 * s1 * lb;
         mu = -s1 * lb;
       }
-      if (own) {
+      if (own[q]) {
         p.B[q].data[c] = lb_in;
         p.H[q][c] = lh_in;
         p.fwH[q].data[c] = lw_in;
@@ -1743,8 +1774,14 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
                                       " does not match the library's " +
                                       std::to_string(MGB_ABI_VERSION));
   }
-  if (d.nx < 2 || d.ny < 2 || d.nz < 2) {
-    return fail(MGB_ERR_UNSUPPORTED, "every axis needs at least 2 cells (reduced-dimension runs are refused)");
+  if (d.nx < 1 || d.ny < 1 || d.nz < 1) return fail(MGB_ERR_ARGUMENT, "every axis needs at least one cell");
+  // a one-cell axis is periodic (MEEP's unit directions; a 2-D run's invariant z): its
+  // differences read the same sample twice, the exact zero of an invariant axis
+  {
+    const int counts[3] = {d.nx, d.ny, d.nz};
+    for (int a = 0; a < 3; ++a)
+      if (counts[a] == 1 && (d.metallic[a] || d.mirror[a] != 0))
+        return fail(MGB_ERR_UNSUPPORTED, "an axis of one cell must be periodic (not metallic, not folded)");
   }
   // the step kernels index a volume with 32-bit cell offsets
   if ((long long)d.nx * d.ny * d.nz >= (1LL << 31)) {

@@ -99,6 +99,14 @@ class FdtdCancelled(RuntimeError):
     """``cancel_check`` asked the run to stop."""
 
 
+class _null_context:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        return False
+
+
 def _as_xyz(name: str, value: Any) -> Tuple[float, float, float]:
     values = tuple(float(v) for v in value)
     if len(values) != 3:
@@ -118,12 +126,13 @@ class FdtdDriver:
                  gpu_id: int = 0, launch_shape: Optional[Tuple[int, int, int]] = None,
                  kernels: Optional[Tuple[int, int, int, int]] = None,
                  dft_accumulation: Optional[str] = None):
-        if dimensions != 3 or cylindrical:
-            raise Unsupported("only 3-D Cartesian runs are stepped by this engine")
+        if dimensions not in (2, 3) or cylindrical:
+            raise Unsupported("3-D and 2-D (z invariant) Cartesian runs are stepped by this engine; "
+                              "1-D and cylindrical ones are not")
         if beta != 0.0 or any(float(k) != 0.0 for k in bfast_scaled_k):
             raise Unsupported("out-of-plane beta and BFAST are not stepped by this engine")
         del m, accurate_fields_near_cylorigin, prefer_gpu
-        self.grid = Grid(cell_size, resolution, courant, boundaries, k_point, symmetry)
+        self.grid = Grid(cell_size, resolution, courant, boundaries, k_point, symmetry, dimensions=dimensions)
         # complex64 fields (the reference's default): at k = 0 the real and imaginary
         # parts step as two real runs (engine.ComplexEngine)
         self.complex_fields = bool(force_complex_fields)
@@ -151,6 +160,8 @@ class FdtdDriver:
         self._absorber_layers: Tuple[AbsorberLayer, ...] = ()
         self._absorber_sigma: Dict[str, np.ndarray] = {}
         self._conductivity: Dict[str, Optional[np.ndarray]] = {}
+        # components MEEP allocated no array for (a 2-D run's other polarization)
+        self._absent: Tuple[str, ...] = ()
         self._flux_monitors: List[FluxMonitor] = []
         self._dft_monitors: List[DFTMonitor] = []
         self._automatic: List[Any] = []
@@ -200,12 +211,29 @@ class FdtdDriver:
         self._eps = (epsilon, epsilon, epsilon)
         self._inv_eps = (inverse, inverse, inverse)
 
-    def set_epsilon_components(self, eps_x: Any, eps_y: Any, eps_z: Any) -> None:
-        """Diagonal permittivity, one volume per E component (MEEP's chi1inv[c][c])."""
+    def set_epsilon_components(self, epsilon: Any, eps_y: Any = None, eps_z: Any = None,
+                               chi1inv_offdiagonal: Any = None) -> None:
+        """Diagonal permittivity, one volume per E component (MEEP's chi1inv[c][c]):
+        the reference's form, a mapping with exactly ``Ex``, ``Ey`` and ``Ez`` (reference
+        ``driver.py:1220``), or the three volumes in order. Off-diagonal chi1inv rows are
+        refused unless every one is identically zero."""
         self._require_unfrozen("set_epsilon_components")
+        if chi1inv_offdiagonal:
+            for row in dict(chi1inv_offdiagonal).values():
+                for volume in dict(row).values():
+                    if np.any(np.asarray(volume) != 0):
+                        raise Unsupported("off-diagonal chi1inv is not stepped by this engine")
+        if isinstance(epsilon, Mapping):
+            if set(epsilon) != {"Ex", "Ey", "Ez"} or eps_y is not None or eps_z is not None:
+                raise ValueError("set_epsilon_components takes a mapping of exactly Ex, Ey and Ez")
+            values = (epsilon["Ex"], epsilon["Ey"], epsilon["Ez"])
+        else:
+            if eps_y is None or eps_z is None:
+                raise ValueError("set_epsilon_components takes a mapping or three volumes")
+            values = (epsilon, eps_y, eps_z)
         eps = []
         inv = []
-        for label, value in (("eps_x", eps_x), ("eps_y", eps_y), ("eps_z", eps_z)):
+        for label, value in zip(("eps_x", "eps_y", "eps_z"), values):
             epsilon, inverse = self._epsilon_and_inverse(value, label)
             eps.append(epsilon)
             inv.append(inverse)
@@ -331,6 +359,55 @@ class FdtdDriver:
                              f"(root modulus {radius:.6f})")
         self._poles.append((susceptibility, volumes))
 
+    # MEEP allocates a component with every component "like" it (fields.cpp:458-474): in a
+    # 2-D cell its own polarization, in 3-D every component.
+    _POLARIZATIONS = (("Ez", "Dz", "Hx", "Hy", "Bx", "By"), ("Ex", "Ey", "Dx", "Dy", "Hz", "Bz"))
+
+    def _allocated_with(self, component: str) -> Tuple[str, ...]:
+        if self.grid.dimensions == 2:
+            for family in self._POLARIZATIONS:
+                if component in family:
+                    return family
+        return FIELD_COMPONENTS
+
+    def set_absent_components(self, names: Any) -> None:
+        """Record the components MEEP allocated no array for (reference ``driver.py:2344``,
+        ``fields.py:1088``): a 2-D run's other polarization, whose E MEEP never steps and
+        reads as +0. Every component is stepped here; with no source on them and nothing
+        coupling them in they hold zeros, +0 through the curls and the PML forms (their
+        coefficients are positive) and through the positive inverse permittivity. The one
+        form that can leave a -0 is a mirror fold's odd-parity ghost, so on a folded run
+        the absent E words are reset to +0 after every step. Refused: a component a source
+        drives, and any change after the first step. An empty ``names`` steps everything."""
+        self._require_unfrozen("set_absent_components")
+        names = tuple(names)
+        unknown = sorted(set(names) - set(FIELD_COMPONENTS))
+        if unknown:
+            raise ValueError(f"set_absent_components: {unknown} are not field components "
+                             f"(the twelve are {FIELD_COMPONENTS})")
+        driven = sorted({source.component for source in self._sources} & set(names))
+        if driven:
+            raise ValueError(f"set_absent_components: {driven} carry a source, and MEEP allocates "
+                             "every component a source requires")
+        self._absent = tuple(name for name in FIELD_COMPONENTS if name in names)
+
+    @property
+    def absent_components(self) -> Tuple[str, ...]:
+        return self._absent
+
+    def _clear_absent(self) -> None:
+        """Reset the absent E components to +0 (folded runs only: see
+        :meth:`set_absent_components`)."""
+        import torch
+
+        engine = self.engine
+        parts = (engine.re, engine.im) if hasattr(engine, "re") else (engine,)
+        for part in parts:
+            with torch.cuda.stream(part.stream) if part.stream is not None else _null_context():
+                for name in self._absent:
+                    if name[0] == "E":
+                        part.fields[name].zero_()
+
     def add_source(self, source_data: Mapping[str, Any]) -> Source:
         """A source from the reference's boundary-protocol dict (driver.py:2567)."""
         self._require_unfrozen("add_source")
@@ -350,8 +427,18 @@ class FdtdDriver:
             raise Unsupported("a complex source amplitude needs complex fields")
         if self.pml is not None and self.has_conductivity:
             self._require_source_clear_of_conductive_pml(source.center, source.size, self.pml.faces)
+        # MEEP's require_component: a sourced component, and every one allocated with it,
+        # is present
+        if source.component in self._absent:
+            allocated = self._allocated_with(source.component)
+            self._absent = tuple(name for name in self._absent if name not in allocated)
         self._sources.append(source)
         return source
+
+    def _require_3d_monitor(self) -> None:
+        if self.grid.dimensions != 3:
+            raise Unsupported("flux and DFT monitors of a 2-D run (lines and areas on an invariant z) "
+                              "are not registered by this engine")
 
     def _decimation(self, request: int, frequencies) -> int:
         request = int(request)
@@ -367,6 +454,7 @@ class FdtdDriver:
                          nfreq: Optional[int] = None, decimation_factor: int = 1,
                          weight: float = 1.0) -> FluxMonitor:
         self._require_unfrozen("add_flux_monitor")
+        self._require_3d_monitor()
         freqs = normalize_frequencies(frequencies, frequency, fcen, df, nfreq)
         if center is None or size is None:
             raise ValueError("a flux monitor needs a center and a size")
@@ -382,6 +470,7 @@ class FdtdDriver:
                         *, frequency: Any = None, fcen: Optional[float] = None, df: Optional[float] = None,
                         nfreq: Optional[int] = None, decimation_factor: int = 1) -> DFTMonitor:
         self._require_unfrozen("add_dft_monitor")
+        self._require_3d_monitor()
         freqs = normalize_frequencies(frequencies, frequency, fcen, df, nfreq)
         monitor = DFTMonitor(self.grid, freqs, tuple(components), self._decimation(decimation_factor, freqs))
         if int(decimation_factor) == 0:
@@ -476,6 +565,12 @@ class FdtdDriver:
     def step_many(self, nsteps: int) -> None:
         if self.engine is None:
             self._freeze()
+        if any(name[0] == "E" for name in self._absent) and self.grid.has_symmetry:
+            for _ in range(int(nsteps)):
+                self.engine.step(self.step_count, 1)
+                self._clear_absent()
+                self.step_count += 1
+            return
         self.engine.step(self.step_count, int(nsteps))
         self.step_count += int(nsteps)
 

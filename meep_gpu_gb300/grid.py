@@ -178,11 +178,14 @@ def normalize_boundaries(boundaries: Any) -> Tuple[str, str, str]:
 
 
 class Grid:
-    """Cell counts, spacing, dt and registration of one 3-D simulation."""
+    """Cell counts, spacing, dt and registration of one simulation: 3-D, or 2-D with z
+    translationally invariant (reference ``grid.py:337``): MEEP leaves z out of its
+    loops, so every z difference reads the same sample twice; here that is one stored
+    cell on z with a periodic wrap, whose difference is the same exact zero."""
 
     def __init__(self, cell_size: Sequence[float], resolution: float, courant: float = 0.5,
                  boundaries: Any = None, k_point: Sequence[float] = (0.0, 0.0, 0.0),
-                 symmetry: Any = ()):
+                 symmetry: Any = (), dimensions: int = 3):
         if len(tuple(cell_size)) != 3:
             raise ValueError(f"cell_size needs three lengths, got {cell_size!r}")
         self.cell_size = tuple(float(v) for v in cell_size)
@@ -192,15 +195,38 @@ class Grid:
         self.courant = float(courant)
         self.dx = 1.0 / self.resolution
         self.dt = self.courant / self.resolution
-        counts = tuple(cell_count(length, self.resolution) for length in self.cell_size)
-        if min(counts) < 2:
-            raise Unsupported(
-                f"every axis needs at least 2 cells (got {counts}); reduced-dimension runs "
-                "are not stepped by this engine")
+        if dimensions not in (2, 3) or isinstance(dimensions, bool):
+            raise Unsupported(f"dimensions {dimensions!r}: 3-D and 2-D (z invariant) runs are stepped "
+                              "by this engine, 1-D and cylindrical ones are not")
+        self.dimensions = int(dimensions)
+        # the axes MEEP's loops carry (reference sources.py:770 _meep_directions): 2-D drops z
+        self.directions = (0, 1, 2) if self.dimensions == 3 else (0, 1)
+        self.invariant_axes = tuple(a not in self.directions for a in range(3))
+        if self.invariant_axes[2] and self.cell_size[2] != 0.0:
+            raise ValueError(f"dimensions=2 makes z translationally invariant: its cell_size must be 0 "
+                             f"(an invariant axis has no extent), got {self.cell_size[2]!r}")
+        counts = tuple(1 if self.invariant_axes[a] else cell_count(self.cell_size[a], self.resolution)
+                       for a in range(3))
         self.shape_full = counts
         self.nx_full, self.ny_full, self.nz_full = counts
         self.boundaries = normalize_boundaries(boundaries)
+        for axis in range(3):
+            if self.boundaries[axis] != METALLIC:
+                continue
+            if self.invariant_axes[axis]:
+                raise ValueError(f"the {AXIS_NAMES[axis]} axis is invariant at dimensions={self.dimensions}: "
+                                 "it has no outer face, so it cannot be metallic (a wall there zeroes the "
+                                 "components whose Yee shift on it is 0); leave it periodic")
+            if counts[axis] < 2:
+                raise ValueError(f"the {AXIS_NAMES[axis]} axis is metallic and holds {counts[axis]} cell(s): "
+                                 "MEEP makes a one-cell direction periodic (fields.cpp, unit directions); "
+                                 "declare it periodic or give it more cells")
+        if min(counts) < 1:
+            raise ValueError(f"every carried axis needs at least one cell, got {counts}")
         self.mirrors = normalize_mirrors(symmetry)
+        for axis in range(3):
+            if self.mirrors[axis] is not None and self.invariant_axes[axis]:
+                raise ValueError(f"a mirror plane normal to the invariant {AXIS_NAMES[axis]} axis")
         # MEEP's halve(): n - n//2 + 1 owned cells on a folded axis, from one cell below the
         # plane (reference grid.py:604, vec.cpp halve); a folded periodic axis stores one
         # more, MEEP's big_corner plane and the far ghost slot past it
@@ -244,6 +270,16 @@ class Grid:
 
     def axis_wraps(self, axis: int) -> bool:
         return self.boundaries[axis] == PERIODIC and self.mirrors[axis] is None
+
+    def is_invariant(self, axis: int) -> bool:
+        """Whether the axis is translationally invariant (z of a 2-D run)."""
+        return self.invariant_axes[axis]
+
+    def nosize_direction(self, axis: int) -> bool:
+        """MEEP's ``fields::nosize_direction`` (reference ``grid.py:1237``): a one-cell
+        periodic axis stands for the whole direction, so a zero-extent source request
+        there is not a delta function (its amplitude is not scaled by the resolution)."""
+        return self.axis_wraps(axis) and self.shape_full[axis] == 1
 
     @property
     def has_symmetry(self) -> bool:

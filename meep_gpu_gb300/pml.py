@@ -168,7 +168,8 @@ class PML:
         self.grid = grid
         self.order = int(order)
         self.R_asymptotic = float(R_asymptotic)
-        self.faces: Faces = self._resolve_mirror_faces(normalize_thickness(thickness), thickness)
+        self.faces: Faces = self._resolve_invariant_faces(
+            self._resolve_mirror_faces(normalize_thickness(thickness), thickness), thickness)
         for axis, n in enumerate(grid.shape):
             low, high = self.faces[axis]
             if low + high > n:
@@ -184,6 +185,21 @@ class PML:
                                      grid.axis_wraps(axis))
                 self.records[(lattice, axis)] = runs_of(line)
                 self._check_unit_outside(axis, lattice, line)
+
+    def _resolve_invariant_faces(self, faces: Faces, request: Any) -> Faces:
+        """No layer on an invariant axis (z of a 2-D run: it has no faces). A scalar
+        request means the faces of the axes the run carries; one naming an invariant
+        axis's face is refused."""
+        uniform = not isinstance(request, (dict, tuple, list))
+        resolved = list(faces)
+        for axis in range(3):
+            if not self.grid.is_invariant(axis) or faces[axis] == (0.0, 0.0):
+                continue
+            if not uniform:
+                raise ValueError(f"PML requested on the {AXIS_NAMES[axis]} axis, which is invariant at "
+                                 f"dimensions={self.grid.dimensions}: it has no faces to absorb at")
+            resolved[axis] = (0.0, 0.0)
+        return tuple(resolved)  # type: ignore[return-value]
 
     def _resolve_mirror_faces(self, faces: Faces, request: Any) -> Faces:
         """No layer on the low face of a folded axis: its cell 0 straddles the mirror plane,

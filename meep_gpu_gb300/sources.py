@@ -257,10 +257,14 @@ def deposition_pieces(grid: Grid, component: str, center: Sequence[float], size:
         raise Unsupported(f"source component {component!r} is not one of Ex..Ez, Hx..Hz")
     a = grid.resolution
     inva = grid.dx
+    # the axes MEEP's loops carry: an invariant one (z of a 2-D run) is one point of
+    # weight 1 at stored cell 0, with no bounds, tapers, lattice shifts or amplitude scale
+    directions = grid.directions
+    resolved = [d in directions for d in range(3)]
     where_min = [float(center[d]) - float(size[d]) / 2 for d in range(3)]
     where_max = [float(center[d]) + float(size[d]) / 2 for d in range(3)]
     lengths = tuple(n * grid.dx for n in grid.shape_full)  # the snapped cell (reference Grid.Lx/Ly/Lz)
-    for d in range(3):
+    for d in directions:
         span = where_max[d] - where_min[d]
         if span > lengths[d] + inva:
             raise ValueError(f"source size {size[d]} exceeds the cell length {lengths[d]} by more than one cell")
@@ -268,20 +272,22 @@ def deposition_pieces(grid: Grid, component: str, center: Sequence[float], size:
             excess = span - lengths[d]
             where_min[d] = where_min[d] - excess * 0.5
             where_max[d] = where_min[d] + lengths[d]
+    # amp * a per zero-extent carried direction, except a one-cell periodic one (MEEP's
+    # nosize_direction: a zero extent there means the whole direction)
     amp = (float(complex(amplitude).real), float(complex(amplitude).imag))
-    for d in range(3):
-        if where_max[d] - where_min[d] == 0.0:
+    for d in directions:
+        if where_max[d] - where_min[d] == 0.0 and not grid.nosize_direction(d):
             amp = (amp[0] * a, amp[1] * a)
     iyee = IYEE[comp]
     iyee_c = [1 - iyee[d] for d in range(3)]
     is_ = [0, 0, 0]
     ie = [0, 0, 0]
-    tapers = []
-    for d in range(3):
+    tapers = [(1.0, 1.0, 1.0, 1.0)] * 3
+    for d in directions:
         yee_c = iyee_c[d] * 0.5 * inva
         is_[d] = vec2diel_floor(where_min[d] + yee_c, a) - iyee_c[d]
         ie[d] = vec2diel_ceil(where_max[d] + yee_c, a) - iyee_c[d]
-        tapers.append(boundary_weights(where_min[d], where_max[d], is_[d], ie[d], a))
+        tapers[d] = boundary_weights(where_min[d], where_max[d], is_[d], ie[d], a)
     io = [grid.origin_doubled(d) for d in range(3)]
     counts = grid.shape
     # the window top is MEEP's big corner, owned cells up: a folded periodic axis's far
@@ -295,7 +301,8 @@ def deposition_pieces(grid: Grid, component: str, center: Sequence[float], size:
     # MEEP loops lattice shifts on every axis with a periodic outer face, a folded one
     # included (its second mirror is a lattice image; reference sources.py:925), by the
     # full cell's lattice vector
-    periodic = [wraps[d] or (grid.is_mirrored(d) and not grid.is_metallic(d)) for d in range(3)]
+    periodic = [resolved[d] and (wraps[d] or (grid.is_mirrored(d) and not grid.is_metallic(d)))
+                for d in range(3)]
     half_inva = 0.5 * inva
     min_shift = [0, 0, 0]
     max_shift = [0, 0, 0]
@@ -323,6 +330,9 @@ def deposition_pieces(grid: Grid, component: str, center: Sequence[float], size:
             pass_amp = cmul(amp, (ph[0], -ph[1]))
         ranges = []
         for d in range(3):
+            if not resolved[d]:
+                ranges.append([None])
+                continue
             low = max(is_[d] - shifted[d], window_low[d])
             high = min(ie[d] - shifted[d], window_high[d])
             ranges.append(list(range(low, high + 1, 2)) if low <= high else [])
@@ -336,6 +346,12 @@ def deposition_pieces(grid: Grid, component: str, center: Sequence[float], size:
                         inert = False
                         rel = []
                         for d in range(3):
+                            if not resolved[d]:
+                                # an amplitude function is handed 0 on an axis the run
+                                # does not carry (MEEP's vec2py)
+                                rel.append(0.0)
+                                cell.append(0)
+                                continue
                             loc = (0.5 * coords[d]) * inva + shifted[d] * half_inva
                             rel.append(loc - centre[d])
                             ladder = (coords[d] - io[d]) // 2
@@ -358,6 +374,9 @@ def deposition_pieces(grid: Grid, component: str, center: Sequence[float], size:
             weights = []
             empty = False
             for d in range(3):
+                if not resolved[d]:
+                    weights.append(None)
+                    continue
                 isc[d] = max(is_[d] - shifted[d], window_low[d], lo[d] + 2 - iyee[d])
                 iec[d] = min(ie[d] - shifted[d], hi[d] - iyee[d])
                 if isc[d] > iec[d]:
@@ -370,10 +389,13 @@ def deposition_pieces(grid: Grid, component: str, center: Sequence[float], size:
             cells: List[Tuple[int, int, int]] = []
             amps: List[complex] = []
             for coords, cell, value in points:
-                if any(not isc[d] <= coords[d] <= iec[d] for d in range(3)):
+                if any(not isc[d] <= coords[d] <= iec[d] for d in directions):
                     continue
                 factors = []
                 for d in range(3):
+                    if weights[d] is None:
+                        factors.append(1.0)
+                        continue
                     ws0, ws1, we0, we1, n = weights[d]
                     factors.append(loop_weight((coords[d] - isc[d]) // 2, n, ws0, ws1, we0, we1))
                 weight = factors[2] * (factors[1] * (1.0 * factors[0]))

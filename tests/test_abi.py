@@ -37,9 +37,14 @@ def test_create_refuses_bad_descriptors_without_a_gpu():
     code = lib.mgb_create(ctypes.byref(desc), ctypes.byref(handle))
     assert code == -1 and "ABI version" in _lib.last_error(lib)
     desc.abi_version = _lib.MGB_ABI_VERSION
-    desc.nx, desc.ny, desc.nz = 1, 8, 8
+    desc.nx, desc.ny, desc.nz = 0, 8, 8
+    assert lib.mgb_create(ctypes.byref(desc), ctypes.byref(handle)) == -1
+    assert "at least one cell" in _lib.last_error(lib)
+    desc.nx = 1  # a one-cell axis must be periodic
+    desc.metallic[0] = 1
     assert lib.mgb_create(ctypes.byref(desc), ctypes.byref(handle)) == -3
-    assert "at least 2 cells" in _lib.last_error(lib)
+    assert "one cell must be periodic" in _lib.last_error(lib)
+    desc.metallic[0] = 0
     desc.nx, desc.ny, desc.nz = 1300, 1300, 1300  # 2.2e9 cells: past 32-bit offsets
     assert lib.mgb_create(ctypes.byref(desc), ctypes.byref(handle)) == -3
     assert "2^31" in _lib.last_error(lib)

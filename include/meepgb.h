@@ -38,8 +38,8 @@
 extern "C" {
 #endif
 
-#define MGB_ABI_VERSION 3
-#define MGB_MAX_POLES 4
+#define MGB_ABI_VERSION 4
+#define MGB_MAX_POLES 8
 #define MGB_MAX_MONITORS 16
 #define MGB_MAX_MONITOR_COMPONENTS 6
 

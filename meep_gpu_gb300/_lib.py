@@ -14,8 +14,8 @@ from typing import Optional
 
 PACKAGE = Path(__file__).resolve().parent
 
-MGB_ABI_VERSION = 3
-MGB_MAX_POLES = 4
+MGB_ABI_VERSION = 4
+MGB_MAX_POLES = 8
 MGB_MAX_MONITORS = 16
 MGB_MAX_MONITOR_COMPONENTS = 6
 MGB_DFT_DEPTH = 32

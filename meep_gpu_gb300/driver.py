@@ -126,9 +126,9 @@ class FdtdDriver:
                  gpu_id: int = 0, launch_shape: Optional[Tuple[int, int, int]] = None,
                  kernels: Optional[Tuple[int, int, int, int]] = None,
                  dft_accumulation: Optional[str] = None):
-        if dimensions not in (2, 3) or cylindrical:
-            raise Unsupported("3-D and 2-D (z invariant) Cartesian runs are stepped by this engine; "
-                              "1-D and cylindrical ones are not")
+        if dimensions not in (1, 2, 3) or cylindrical:
+            raise Unsupported("3-D, 2-D (z invariant) and 1-D (along z) Cartesian runs are stepped by "
+                              "this engine; cylindrical ones are not")
         if beta != 0.0 or any(float(k) != 0.0 for k in bfast_scaled_k):
             raise Unsupported("out-of-plane beta and BFAST are not stepped by this engine")
         del m, accurate_fields_near_cylorigin, prefer_gpu
@@ -360,15 +360,17 @@ class FdtdDriver:
         self._poles.append((susceptibility, volumes))
 
     # MEEP allocates a component with every component "like" it (fields.cpp:458-474): in a
-    # 2-D cell its own polarization, in 3-D every component.
-    _POLARIZATIONS = (("Ez", "Dz", "Hx", "Hy", "Bx", "By"), ("Ex", "Ey", "Dx", "Dy", "Hz", "Bz"))
+    # 2-D cell its own polarization, in 1-D the pair it couples to, in 3-D every component.
+    _POLARIZATIONS = {2: (("Ez", "Dz", "Hx", "Hy", "Bx", "By"), ("Ex", "Ey", "Dx", "Dy", "Hz", "Bz")),
+                      1: (("Ex", "Dx", "Hy", "By"), ("Ey", "Dy", "Hx", "Bx"))}
 
     def _allocated_with(self, component: str) -> Tuple[str, ...]:
-        if self.grid.dimensions == 2:
-            for family in self._POLARIZATIONS:
-                if component in family:
-                    return family
-        return FIELD_COMPONENTS
+        if self.grid.dimensions == 3:
+            return FIELD_COMPONENTS
+        for family in self._POLARIZATIONS[self.grid.dimensions]:
+            if component in family:
+                return family
+        return (component,)
 
     def set_absent_components(self, names: Any) -> None:
         """Record the components MEEP allocated no array for (reference ``driver.py:2344``,
@@ -437,8 +439,8 @@ class FdtdDriver:
 
     def _require_3d_monitor(self) -> None:
         if self.grid.dimensions != 3:
-            raise Unsupported("flux and DFT monitors of a 2-D run (lines and areas on an invariant z) "
-                              "are not registered by this engine")
+            raise Unsupported(f"flux and DFT monitors of a {self.grid.dimensions}-D run (regions on "
+                              "invariant axes) are not registered by this engine")
 
     def _decimation(self, request: int, frequencies) -> int:
         request = int(request)

@@ -178,10 +178,11 @@ def normalize_boundaries(boundaries: Any) -> Tuple[str, str, str]:
 
 
 class Grid:
-    """Cell counts, spacing, dt and registration of one simulation: 3-D, or 2-D with z
-    translationally invariant (reference ``grid.py:337``): MEEP leaves z out of its
-    loops, so every z difference reads the same sample twice; here that is one stored
-    cell on z with a periodic wrap, whose difference is the same exact zero."""
+    """Cell counts, spacing, dt and registration of one simulation: 3-D, 2-D with z
+    translationally invariant, or 1-D along z with x and y invariant (reference
+    ``grid.py:337``): MEEP leaves an invariant axis out of its loops, so every difference
+    along it reads the same sample twice; here that is one stored cell with a periodic
+    wrap, whose difference is the same exact zero."""
 
     def __init__(self, cell_size: Sequence[float], resolution: float, courant: float = 0.5,
                  boundaries: Any = None, k_point: Sequence[float] = (0.0, 0.0, 0.0),
@@ -195,16 +196,19 @@ class Grid:
         self.courant = float(courant)
         self.dx = 1.0 / self.resolution
         self.dt = self.courant / self.resolution
-        if dimensions not in (2, 3) or isinstance(dimensions, bool):
-            raise Unsupported(f"dimensions {dimensions!r}: 3-D and 2-D (z invariant) runs are stepped "
-                              "by this engine, 1-D and cylindrical ones are not")
+        if dimensions not in (1, 2, 3) or isinstance(dimensions, bool):
+            raise Unsupported(f"dimensions {dimensions!r}: 3-D, 2-D (z invariant) and 1-D (along z) "
+                              "runs are stepped by this engine")
         self.dimensions = int(dimensions)
-        # the axes MEEP's loops carry (reference sources.py:770 _meep_directions): 2-D drops z
-        self.directions = (0, 1, 2) if self.dimensions == 3 else (0, 1)
+        # the axes MEEP's loops carry (reference sources.py:770 _meep_directions): 2-D
+        # drops z, 1-D keeps z alone
+        self.directions = {3: (0, 1, 2), 2: (0, 1), 1: (2,)}[self.dimensions]
         self.invariant_axes = tuple(a not in self.directions for a in range(3))
-        if self.invariant_axes[2] and self.cell_size[2] != 0.0:
-            raise ValueError(f"dimensions=2 makes z translationally invariant: its cell_size must be 0 "
-                             f"(an invariant axis has no extent), got {self.cell_size[2]!r}")
+        for axis in range(3):
+            if self.invariant_axes[axis] and self.cell_size[axis] != 0.0:
+                raise ValueError(f"dimensions={self.dimensions} makes {AXIS_NAMES[axis]} translationally "
+                                 f"invariant: its cell_size must be 0 (an invariant axis has no extent), "
+                                 f"got {self.cell_size[axis]!r}")
         counts = tuple(1 if self.invariant_axes[a] else cell_count(self.cell_size[a], self.resolution)
                        for a in range(3))
         self.shape_full = counts

@@ -187,7 +187,8 @@ class PML:
                 self._check_unit_outside(axis, lattice, line)
 
     def _resolve_invariant_faces(self, faces: Faces, request: Any) -> Faces:
-        """No layer on an invariant axis (z of a 2-D run: it has no faces). A scalar
+        """No layer on an invariant axis (z of a 2-D run, x and y of a 1-D one: it has no
+        faces). A scalar
         request means the faces of the axes the run carries; one naming an invariant
         axis's face is refused."""
         uniform = not isinstance(request, (dict, tuple, list))

@@ -57,7 +57,7 @@ typedef struct SUF(oracle_state) {
   REAL* scratch; /* one volume, the curl */
   REAL* drive[3]; /* W of each component, formed by update_E for update_P */
   int npoles;
-  SUF(oracle_pole) poles[4];
+  SUF(oracle_pole) poles[8];
   int nsrc;
   const long long* src_cell;
   const int* src_comp;

@@ -64,7 +64,7 @@ def _state_type(real) -> type:
                     ("E", P * 3), ("D", P * 3), ("B", P * 3), ("H", P * 3),
                     ("fwH", P * 3), ("fwE", P * 3), ("fuB", P * 3), ("fuD", P * 3),
                     ("inv_eps", P * 3), ("scratch", P), ("drive", P * 3),
-                    ("npoles", ctypes.c_int), ("poles", Pole * 4),
+                    ("npoles", ctypes.c_int), ("poles", Pole * 8),
                     ("nsrc", ctypes.c_int), ("src_cell", P), ("src_comp", P),
                     ("h_separated", ctypes.c_int),
                     ("condfac", (P * 3) * 2), ("condinv", (P * 3) * 2), ("keeps", (P * 3) * 2),

@@ -34,13 +34,13 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-# c and c_prime: 3-D, odd Y and Z mirror planes, a PML of 7.5 cells, an Hx source. Not
-# recorded: ex.absorber-1d (a 1-D run with five poles: this engine steps 3-D and 2-D runs
-# and four poles), the holey-waveguide band case (its digests need MEEP's recorded chunk
+# c and c_prime: 3-D, odd Y and Z mirror planes, a PML of 7.5 cells, an Hx source;
+# ex.absorber-1d: 1-D, a Drude and four Lorentz poles, absorber layers at both z faces.
+# Not recorded: the holey-waveguide band case (its digests need MEEP's recorded chunk
 # layout and currents even on the reference) and the cylindrical ring.
-CASES = ("a", "b", "c", "c_prime", "ex.material-dispersion")
+CASES = ("a", "b", "c", "c_prime", "ex.material-dispersion", "ex.absorber-1d")
 KEPT_CALLS = ("set_epsilon", "set_epsilon_components", "setup_pml", "add_source", "add_susceptibility",
-              "set_absent_components")
+              "set_absorber", "set_absent_components")
 
 
 def _plain(value, arrays, label):
@@ -63,6 +63,9 @@ def _plain(value, arrays, label):
     kind = type(value).__name__
     if kind == "Mirror":
         return {"mirror": [str(value.axis), int(value.phase)]}
+    if kind == "AbsorberLayer":
+        return {"absorber": {"thickness": float(value.thickness), "axis": int(value.axis),
+                             "side": str(value.side), "R_asymptotic": float(value.R_asymptotic)}}
     if kind == "Susceptibility":
         return {"susceptibility": {"frequency": float(value.frequency), "gamma": float(value.gamma),
                                    "kind": str(value.kind)}}

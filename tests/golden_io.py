@@ -37,6 +37,9 @@ def _identity_value(node, arrays):
         if set(node) == {"mirror"}:
             from meep_gpu_gb300 import Mirror
             return Mirror(node["mirror"][0], node["mirror"][1])
+        if set(node) == {"absorber"}:
+            from meep_gpu_gb300.conductivity import AbsorberLayer
+            return AbsorberLayer(**node["absorber"])
         return {k: _identity_value(v, arrays) for k, v in node.items()}
     if isinstance(node, list):
         return [_identity_value(v, arrays) for v in node]

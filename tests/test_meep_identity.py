@@ -1,10 +1,12 @@
 """MEEP's own words: the MEEP-identity cases.
 
-For five runs minted on MEEP itself — ``a`` (a 200 x 200 2-D cell, vacuum, PML, a
+For six runs minted on MEEP itself — ``a`` (a 200 x 200 2-D cell, vacuum, PML, a
 Gaussian Ez point source), ``b`` (the same with a per-component permittivity up to 12),
 ``c`` and ``c_prime`` (3-D, 39 x 18 x 19 stored cells under odd Y and Z mirror planes, a
 PML of 7.5 cells, a dielectric block, a Gaussian Hx point source) and
-``ex.material-dispersion`` (one periodic 2-D cell, eps 2.25 and two Lorentz poles) — the
+``ex.material-dispersion`` (one periodic 2-D cell, eps 2.25 and two Lorentz poles) and
+``ex.absorber-1d`` (a 1-D run of 400 cells along z, a Drude and four Lorentz poles,
+absorber layers at both faces, an Ex source) — the
 reference keeps the SHA-256 of every stored float32 word (mirror ghosts excepted) of all
 twelve components at 30 or 31 compared steps (``parity/meep_gpu/fixtures/meep_identity/
 keep``, replayed by ``meep_gpu/meep_identity.py:680``). ``tests/golden/
@@ -30,7 +32,7 @@ from meep_gpu_gb300.grid import IYEE, Grid, Unsupported
 from oracle.oracle import Oracle, problem_from_driver
 from tests import golden_io
 
-CASES = ("a", "b", "c", "c_prime", "ex.material-dispersion")
+CASES = ("a", "b", "c", "c_prime", "ex.material-dispersion", "ex.absorber-1d")
 
 
 def _mismatches(case, entry, field_at, advance):
@@ -87,8 +89,12 @@ def test_2d_grid_rules():
         Grid((1.0, 2.0, 0.0), 10, boundaries="metallic", dimensions=2)
     with pytest.raises(ValueError, match="one-cell direction periodic"):
         Grid((0.1, 2.0, 2.0), 10, boundaries={"x": "metallic"})
-    with pytest.raises(Unsupported, match="1-D"):
+    line = Grid((0.0, 0.0, 3.0), 10, boundaries={"z": "metallic"}, dimensions=1)
+    assert line.shape == (1, 1, 30) and line.is_invariant(0) and line.is_invariant(1)
+    with pytest.raises(ValueError, match="must be 0"):
         Grid((1.0, 1.0, 1.0), 10, dimensions=1)
+    with pytest.raises(Unsupported, match="cylindrical"):
+        FdtdDriver((1.0, 1.0, 1.0), 10, cylindrical=True)
     # a scalar PML thickness covers the carried axes only; naming z is refused
     d = FdtdDriver((2.0, 2.0, 0.0), 10, boundaries={"x": "metallic", "y": "metallic"}, dimensions=2,
                    force_complex_fields=False)
@@ -141,6 +147,8 @@ def test_engine_reproduces_meeps_words(gpu, case, mode):
     driver, entry = golden_io.build_identity(case, FdtdDriver, Susceptibility)
     if mode == "split" and driver.grid.shape[0] < 6:
         pytest.skip("the x-range split needs an x axis of several ranges")
+    if mode == "prefetch" and driver.has_conductivity:
+        pytest.skip("a run with a conductivity steps with the generic families 0 and 4 only")
     driver.kernels = MODES[mode]
     bad = _mismatches(case, entry, lambda c: driver.get_field(c, cell_centered=False), driver.step_many)
     if mode == "split":

@@ -273,7 +273,8 @@ def main(argv=None) -> None:
     driver.engine.step(driver.step_count, args.steps)
     torch.cuda.synchronize()
     elapsed = time.perf_counter() - start
-    print(f"{args.name}: {driver.grid}, kernels {driver.engine.choice}, split {driver.engine.split}, "
+    engine = driver.engine.re if hasattr(driver.engine, "re") else driver.engine
+    print(f"{args.name}: {driver.grid}, kernels {engine.choice}, split {engine.split}, wave {engine.wave}, "
           f"{1e3 * elapsed / max(args.steps, 1):.4f} ms/step over {args.steps} steps")
     driver.close()
 

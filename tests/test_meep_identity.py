@@ -156,3 +156,33 @@ def test_engine_reproduces_meeps_words(gpu, case, mode):
     assert bad == [], f"{case} ({mode}): digests differ from MEEP's at {bad[:6]}"
     assert driver.engine.device_status_word() == 0
     driver.close()
+
+
+@pytest.mark.gpu
+def test_absent_e_components_stay_plus_zero_on_a_folded_2d_run(gpu):
+    """MEEP never steps an absent E component, so it reads +0. On a folded run the odd-
+    parity ghost of D (here Dy under an odd X plane) is -0 where its image is +0, and
+    E = inv * D would carry that -0: the driver resets the absent E words after every
+    step. The present components are the same words as without the absent set."""
+    from meep_gpu_gb300 import Mirror
+
+    def run(absent):
+        d = FdtdDriver((2.0, 2.0, 0.0), 10, dimensions=2, force_complex_fields=False,
+                       boundaries={"x": "metallic", "y": "metallic"}, symmetry=(Mirror("X", -1),))
+        d.setup_pml({"y": (3, 3)})
+        d.add_source({"component": "Ez", "center": (0.5, 0, 0), "size": (0, 0, 0),
+                      "source_type": "gaussian", "frequency": 1.0, "fwidth": 1.0})
+        if absent:
+            d.set_absent_components(["Ex", "Ey", "Dx", "Dy", "Hz", "Bz"])
+        d.run(num_steps=40)
+        return d
+
+    plain, marked = run(False), run(True)
+    for c in ("Ex", "Ey"):
+        words = marked.get_field(c, cell_centered=False)
+        assert not np.any(words) and not np.any(np.signbit(words)), c
+    assert np.any(np.signbit(plain.get_field("Ey", cell_centered=False))), "the -0 this test guards against"
+    for c in ("Ez", "Dz", "Hx", "Hy", "Bx", "By"):
+        assert np.array_equal(plain.get_field(c, cell_centered=False), marked.get_field(c, cell_centered=False)), c
+    plain.close()
+    marked.close()

@@ -997,8 +997,9 @@ def bench_mirror(device, args):
         "stored_cells": cells, "unfolded_cells": full, "ms_per_step": round(ms, 5), "steps": steps,
         "step_frac": round(step_bytes / (ms / 1e3) / 1e9 / peak, 4), "per_kernel": halves,
         "ghosts": [int(engine.desc.fold.count[0]), int(engine.desc.fold.count[1])],
-        "kernels": [list(c) for c in engine.choice], "clocks": clocks.summary(),
-        "note": "each half's time includes its fold kernel (ghost words and their E/H)"}}
+        "kernels": [list(c) for c in engine.choice], "x_range_split": engine.split, "clocks": clocks.summary(),
+        "note": "each half's time includes its fold kernel (ghost words and their E/H); the per-half "
+                "times are single launches, the step takes the x-range split"}}
     if engine.nonfinite():
         raise RuntimeError("the mirror192 run wrote a non-finite field")
     driver.close()

@@ -633,6 +633,7 @@ class Engine:
         stream = torch.cuda.current_stream(self.device)
         best = [None, None]
         best_ms = [float("inf"), float("inf")]
+        timed: List[Dict[tuple, float]] = [{}, {}]  # every candidate's time, per half
         for choice in AUTOTUNE_CANDIDATES:
             if choice[0] not in self.allowed_families:
                 continue
@@ -663,6 +664,7 @@ class Engine:
             for part in applies:
                 # the fastest of the timed launches: the least disturbed by anything else
                 ms = float(np.min([ev[part].elapsed_time(ev[part + 1]) for ev in marks]))
+                timed[part][choice] = ms
                 if ms < best_ms[part]:
                     best[part], best_ms[part] = choice, ms
         wave = None
@@ -671,8 +673,18 @@ class Engine:
         if self.wave_eligible and os.environ.get("MEEPGB_WAVE", "0") == "1":
             wave = self._tune_wave(scratch, (best[0], best[1]), stream)
         split = 0
-        if wave is None and os.environ.get("MEEPGB_SPLIT", "1") != "0":
-            split = self._tune_split(scratch, (best[0], best[1]), stream)
+        if (wave is None and os.environ.get("MEEPGB_SPLIT", "1") != "0" and self.grid.is_metallic(0)
+                and not self.grid.has_bloch):
+            # the two fastest single launches of each half, paired and timed on whole steps
+            # with every split: the fastest launch alone is not always the fastest when the
+            # ranges of both halves overlap
+            tops = [sorted(timed[part], key=timed[part].get)[:2] or [best[part]] for part in (0, 1)]
+            best_step = float("inf")
+            for h in tops[0]:
+                for e in tops[1]:
+                    ranges, ms = self._tune_split(scratch, (h, e), stream, with_time=True)
+                    if ms < best_step:
+                        best_step, best[0], best[1], split = ms, h, e, ranges
         scratch.close()
         del scratch
         _AUTOTUNE_CACHE[key] = (best[0], best[1], wave, split)
@@ -680,12 +692,13 @@ class Engine:
         self.autotune_ms = best_ms[0] + best_ms[1]
         return self.choice
 
-    def _run_ms(self, scratch: "Engine", stream, steps: int = 24) -> float:
-        """The fastest of two timed runs of ``steps`` whole steps on the scratch engine."""
+    def _run_ms(self, scratch: "Engine", stream, steps: int = 48) -> float:
+        """The fastest of three timed runs of ``steps`` whole steps on the scratch engine
+        (long enough that candidates a few per cent apart are told apart)."""
         scratch.step(0, 4)
         start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         best_ms = float("inf")
-        for _ in range(2):
+        for _ in range(3):
             start.record(stream)
             scratch.step(4, steps)
             end.record(stream)
@@ -693,22 +706,21 @@ class Engine:
             best_ms = min(best_ms, start.elapsed_time(end))
         return best_ms
 
-    def _tune_split(self, scratch: "Engine", halves, stream) -> int:
-        """The x-range split that steps fastest (0: none), whole steps timed."""
+    def _tune_split(self, scratch: "Engine", halves, stream, with_time: bool = False):
+        """The x-range split that steps fastest (0: none), whole steps timed; with
+        ``with_time`` also that split's time (ms per timed run)."""
         scratch.select(halves)
-        if not scratch.split_eligible:
-            return 0
         scratch.set_split(0)
         best, best_ms = 0, self._run_ms(scratch, stream)
         for ranges in SPLIT_CANDIDATES:
-            if ranges * 2 > self.grid.shape[0]:
+            if ranges * 2 > self.grid.shape[0] or not scratch.split_eligible:
                 continue
             scratch.set_split(ranges)
             ms = self._run_ms(scratch, stream)
             if ms < best_ms:
                 best, best_ms = ranges, ms
         scratch.set_split(0)
-        return best
+        return (best, best_ms) if with_time else best
 
     def _tune_wave(self, scratch: "Engine", halves, stream, steps: int = 24):
         """The fastest wavefront choice, if it steps a run of ``steps`` steps faster than

@@ -203,6 +203,12 @@ typedef struct mgb_sim_desc {
   int32_t mirror[3];
   int32_t full[3];
   mgb_fold fold;
+  /* bit a: axis a is translationally invariant (z of a 2-D run, x and y of a 1-D one;
+   * one periodic cell each). A curl partner whose derivative lies along such an axis is
+   * absent, as MEEP's step plan drops it (fields.cpp figure_out_step_plan): the curl is
+   * dtdx * (g1s - g1) or (-dtdx) * (g2s - g2) instead of the full bracket. Such runs
+   * step on the generic kernel families and are refused by the batch and the adjoint. */
+  int32_t invariant;
 } mgb_sim_desc;
 
 typedef struct mgb_sim mgb_sim;

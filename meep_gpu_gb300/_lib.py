@@ -116,6 +116,7 @@ class MgbSimDesc(ctypes.Structure):
         ("mirror", ctypes.c_int32 * 3),
         ("full", ctypes.c_int32 * 3),
         ("fold", MgbFold),
+        ("invariant", ctypes.c_int32),
     ]
 
 

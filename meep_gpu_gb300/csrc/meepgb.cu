@@ -1699,7 +1699,7 @@ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) ==
 void setup_tiles(mgb_sim* sim) {
   const char* env = getenv("MEEPGB_TILES");
   if (env != nullptr && env[0] == '0') return;
-  if (sim->has_cond || sim->step.bloch) return;
+  if (sim->has_cond || sim->step.bloch || sim->step.inv) return;
   const StepParams& p = sim->step;
   if (p.nz % 4 != 0) return;
   for (int q = 0; q < 3; ++q)
@@ -1782,6 +1782,10 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
     for (int a = 0; a < 3; ++a)
       if (counts[a] == 1 && (d.metallic[a] || d.mirror[a] != 0))
         return fail(MGB_ERR_UNSUPPORTED, "an axis of one cell must be periodic (not metallic, not folded)");
+    if ((d.invariant & ~7) != 0) return fail(MGB_ERR_ARGUMENT, "invariant is a bit mask of the three axes");
+    for (int a = 0; a < 3; ++a)
+      if (((d.invariant >> a) & 1) && (counts[a] != 1 || ((d.bloch_axes >> a) & 1)))
+        return fail(MGB_ERR_ARGUMENT, "an invariant axis holds one periodic cell without a Bloch phase");
   }
   // the step kernels index a volume with 32-bit cell offsets
   if ((long long)d.nx * d.ny * d.nz >= (1LL << 31)) {
@@ -1977,6 +1981,7 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
   // whatever its outer face: past a periodic one the readers are the far ghost slot,
   // which the fold writes too
   for (int a = 0; a < 3; ++a) p.met[a] = (d.metallic[a] || d.mirror[a] != 0) ? 1 : 0;
+  p.inv = d.invariant & 7;
   p.dtdx = d.dtdx;
   for (int l = 0; l < 2; ++l)
     for (int a = 0; a < 3; ++a) {
@@ -2662,6 +2667,8 @@ int choose_family(mgb_sim* sim, mgb_sim::HalfChoice& h, int family, int part) {
     return fail(MGB_ERR_UNSUPPORTED, "a run with a conductivity steps with the generic kernels (family 0 or 4)");
   if (sim->step.bloch && family != 0 && family != 4)
     return fail(MGB_ERR_UNSUPPORTED, "a Bloch-phased run steps with the generic kernels (family 0 or 4)");
+  if (sim->step.inv && (family == 1 || family == 3))
+    return fail(MGB_ERR_UNSUPPORTED, "a reduced-dimension run steps with the generic kernel families (0, 2, 4, 5)");
   if (family == 0 || family == 2 || family == 4 || family == 5) {
     h.tiles = false;
     h.ws = false;
@@ -2951,6 +2958,7 @@ int mgb_batch_set_slot(mgb_batch* b, int32_t slot, mgb_sim* sim, int64_t end_ste
   if (sim->step.nsrc > 0 && words == nullptr) return fail(MGB_ERR_ARGUMENT, "the slot's sources need deposit words");
   if (sim->has_cond) return fail(MGB_ERR_UNSUPPORTED, "a batched slot does not carry a conductivity");
   if (sim->folded) return fail(MGB_ERR_UNSUPPORTED, "a batched slot does not carry mirror folds");
+  if (sim->step.inv) return fail(MGB_ERR_UNSUPPORTED, "a batched slot is a 3-D run");
   if (sim->desc.nmonitors > kSlotMonitors)
     return fail(MGB_ERR_UNSUPPORTED, "a batched slot holds at most " + std::to_string(kSlotMonitors) + " monitors");
   for (int m = 0; m < sim->desc.nmonitors; ++m) {
@@ -3326,6 +3334,7 @@ int mgb_adjoint_step(mgb_sim* adj, const mgb_adjoint* a, int64_t step, void* str
   if (adj->step.npoles != 0) return fail(MGB_ERR_UNSUPPORTED, "the adjoint step does not carry susceptibility poles");
   if (adj->has_cond) return fail(MGB_ERR_UNSUPPORTED, "the adjoint step does not carry a conductivity");
   if (adj->folded) return fail(MGB_ERR_UNSUPPORTED, "the adjoint step does not carry mirror folds");
+  if (adj->step.inv) return fail(MGB_ERR_UNSUPPORTED, "the adjoint step is for 3-D runs");
   for (int q = 0; q < 3; ++q)
     if (a->mu_b[q] == nullptr || a->mu_d[q] == nullptr) return fail(MGB_ERR_ARGUMENT, "missing mu volume");
   const StepParams& p = adj->step;
@@ -3407,6 +3416,7 @@ int mgb_adjoint_segment(mgb_sim* fwd, mgb_sim* adj, const mgb_adjoint* a, int64_
   if (monitor < 0 || monitor >= adj->desc.nmonitors) return fail(MGB_ERR_ARGUMENT, "no such monitor");
   if (fwd->has_cond || adj->has_cond) return fail(MGB_ERR_UNSUPPORTED, "the adjoint step does not carry a conductivity");
   if (fwd->folded || adj->folded) return fail(MGB_ERR_UNSUPPORTED, "the adjoint step does not carry mirror folds");
+  if (fwd->step.inv || adj->step.inv) return fail(MGB_ERR_UNSUPPORTED, "the adjoint step is for 3-D runs");
   int rc = check_words(fwd, first_step, nsteps);
   if (rc != MGB_OK) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -53,7 +53,27 @@ struct StepParams {
   int part;
   const float* pE[3];
   const float* pH[3];
+  // bit a: axis a is translationally invariant (a 2-D or 1-D run): curl partners whose
+  // derivative lies along it are absent (curl_term)
+  int inv;
 };
+
+// One curl bracket, dtdx * (((S1 - A1) + A2) - S2) (S the shifted operand, A the one at
+// the cell, the partners in MEEP's order), with MEEP's step plan on a reduced-dimension
+// run (fields.cpp figure_out_step_plan, step_generic.cpp step_curl): a partner whose
+// derivative axis the run does not resolve is absent, and the one-partner forms are
+// dtdx * (S1 - A1) and (-dtdx) * (S2 - A2) rather than the full bracket, which rounds
+// differently where the absent partner is nonzero. axis1 / axis2: the partners'
+// derivative axes.
+__device__ __forceinline__ float curl_term(const StepParams& p, float s1, float a1, float a2, float s2,
+                                           int axis1, int axis2) {
+  if (p.inv == 0) return p.dtdx * (((s1 - a1) + a2) - s2);
+  const bool have1 = ((p.inv >> axis1) & 1) == 0, have2 = ((p.inv >> axis2) & 1) == 0;
+  if (have1 && have2) return p.dtdx * (((s1 - a1) + a2) - s2);
+  if (have1) return p.dtdx * (s1 - a1);
+  if (have2) return (-p.dtdx) * (s2 - a2);
+  return 0.f;
+}
 
 // The ghost lists of mirror-folded axes (mgb_fold), passed to the fold kernels.
 struct FoldArgs {
@@ -656,7 +676,6 @@ __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i
   const float* Ex = p.E[0];
   const float* Ey = p.E[1];
   const float* Ez = p.E[2];
-  const float dtdx = p.dtdx;
   const bool ytop = (j + 1 == p.ny), ztop = (k + 1 == p.nz);
   const bool ywall = ytop && p.met[1], zwall = ztop && p.met[2];
   const int oy = ytop ? -(p.ny - 1) * sy : sy;
@@ -717,9 +736,9 @@ __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i
       if (k == 0) { gx2 = bloch_word(p, 2, true, ey, p.pE[1], c); gy1 = bloch_word(p, 2, true, ex, p.pE[0], c); }
       if (i == 0) { gy2 = bloch_word(p, 0, true, ez, p.pE[2], c); gz1 = bloch_word(p, 0, true, ey, p.pE[1], c); }
     }
-    const float cx = dtdx * (((ez_yp - gx1) + gx2) - ey_zp);
-    const float cy = dtdx * (((ex_zp - gy1) + gy2) - ez_xp);
-    const float cz = dtdx * (((ey_xp - gz1) + gz2) - ex_yp);
+    const float cx = curl_term(p, ez_yp, gx1, gx2, ey_zp, 1, 2);
+    const float cy = curl_term(p, ex_zp, gy1, gy2, ez_xp, 2, 0);
+    const float cz = curl_term(p, ey_xp, gz1, gz2, ex_yp, 0, 1);
     float h_new[3];
     h_cell<PML, COND, AX, MSRC>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, h_old, ax, h_new, cp);
     p.H[0][c] = h_new[0];
@@ -737,7 +756,6 @@ __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i
                                         const mgb_conductivity* cp = nullptr) {
   const int sx = p.ny * p.nz;
   const int sy = p.nz;
-  const float dtdx = p.dtdx;
   const float* Hx = p.H[0];
   const float* Hy = p.H[1];
   const float* Hz = p.H[2];
@@ -801,9 +819,9 @@ __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i
       if (k == 0) { gx2 = bloch_word(p, 2, false, hy, p.pH[1], c); gy1 = bloch_word(p, 2, false, hx, p.pH[0], c); }
       if (i == 0) { gy2 = bloch_word(p, 0, false, hz, p.pH[2], c); gz1 = bloch_word(p, 0, false, hy, p.pH[1], c); }
     }
-    const float cx = dtdx * (((hz_ym - gx1) + gx2) - hy_zm);
-    const float cy = dtdx * (((hx_zm - gy1) + gy2) - hz_xm);
-    const float cz = dtdx * (((hy_xm - gz1) + gz2) - hx_ym);
+    const float cx = curl_term(p, hz_ym, gx1, gx2, hy_zm, 1, 2);
+    const float cy = curl_term(p, hx_zm, gy1, gy2, hz_xm, 2, 0);
+    const float cz = curl_term(p, hy_xm, gz1, gz2, hx_ym, 0, 1);
     e_cell<PML, COND, AX>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, d, inv, words, ax, cp);
     hy_xm = hy;
     hz_xm = hz;
@@ -848,7 +866,6 @@ __device__ __forceinline__ void h_march_pf(const StepParams& p, int j, int k, in
                                            int first_step) {
   const int sx = p.ny * p.nz;
   const int sy = p.nz;
-  const float dtdx = p.dtdx;
   const bool ytop = (j + 1 == p.ny), ztop = (k + 1 == p.nz);
   const bool ywall = ytop && p.met[1], zwall = ztop && p.met[2];
   const int oy = ytop ? -(p.ny - 1) * sy : sy;
@@ -896,9 +913,9 @@ __device__ __forceinline__ void h_march_pf(const StepParams& p, int j, int k, in
     }
     HAux ax = {};
     if (PML && axes != 0) h_aux_load(p, hcol, pl, c, ax);
-    const float cx = dtdx * (((cur.ez_yp - ez) + ey) - cur.ey_zp);
-    const float cy = dtdx * (((cur.ex_zp - cur.ex) + ez) - cur.ez_xp);
-    const float cz = dtdx * (((cur.ey_xp - ey) + cur.ex) - cur.ex_yp);
+    const float cx = curl_term(p, cur.ez_yp, ez, ey, cur.ey_zp, 1, 2);
+    const float cy = curl_term(p, cur.ex_zp, cur.ex, ez, cur.ez_xp, 2, 0);
+    const float cz = curl_term(p, cur.ey_xp, ey, cur.ex, cur.ex_yp, 0, 1);
     float h_new[3];
     h_cell<PML, false, AX, MSRC>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, cur.h, ax, h_new);
     p.H[0][c] = h_new[0];
@@ -944,7 +961,6 @@ __device__ __forceinline__ void e_march_pf(const StepParams& p, int j, int k, in
                                            int parity, const double* words) {
   const int sx = p.ny * p.nz;
   const int sy = p.nz;
-  const float dtdx = p.dtdx;
   const int jm = j == 0 ? (p.met[1] ? -1 : p.ny - 1) : j - 1;
   const int km = k == 0 ? (p.met[2] ? -1 : p.nz - 1) : k - 1;
   const int col = j * sy + k;
@@ -996,9 +1012,9 @@ __device__ __forceinline__ void e_march_pf(const StepParams& p, int j, int k, in
     }
     EAux ax = {};
     if (PML && axes != 0) e_aux_load(p, ecol, pl, c, ax);
-    const float cx = dtdx * (((cur.hz_ym - cur.hz) + cur.hy) - cur.hy_zm);
-    const float cy = dtdx * (((cur.hx_zm - cur.hx) + cur.hz) - hz_xm);
-    const float cz = dtdx * (((hy_xm - cur.hy) + cur.hx) - cur.hx_ym);
+    const float cx = curl_term(p, cur.hz_ym, cur.hz, cur.hy, cur.hy_zm, 1, 2);
+    const float cy = curl_term(p, cur.hx_zm, cur.hx, cur.hz, hz_xm, 2, 0);
+    const float cz = curl_term(p, hy_xm, cur.hy, cur.hx, cur.hx_ym, 0, 1);
     e_cell<PML, false, AX>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, cur.d, cur.inv, words, ax);
     hy_xm = cur.hy;
     hz_xm = cur.hz;

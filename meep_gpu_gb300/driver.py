@@ -437,10 +437,14 @@ class FdtdDriver:
         self._sources.append(source)
         return source
 
-    def _require_3d_monitor(self) -> None:
-        if self.grid.dimensions != 3:
-            raise Unsupported(f"flux and DFT monitors of a {self.grid.dimensions}-D run (regions on "
-                              "invariant axes) are not registered by this engine")
+    def _require_flat_on_invariant_axes(self, size, what: str) -> None:
+        """A monitor region has no extent on an invariant axis (reference ``driver.py:3270``):
+        the measure takes one dx per extended axis, so an extent there would scale the
+        result by dx."""
+        offenders = [AXIS_NAMES[a] for a in range(3) if self.grid.is_invariant(a) and float(size[a]) != 0.0]
+        if offenders:
+            raise ValueError(f"{what} size {tuple(size)} claims an extent along the invariant axes {offenders} "
+                             f"of a {self.grid.dimensions}-D run; give those axes 0")
 
     def _decimation(self, request: int, frequencies) -> int:
         request = int(request)
@@ -456,11 +460,25 @@ class FdtdDriver:
                          nfreq: Optional[int] = None, decimation_factor: int = 1,
                          weight: float = 1.0) -> FluxMonitor:
         self._require_unfrozen("add_flux_monitor")
-        self._require_3d_monitor()
         freqs = normalize_frequencies(frequencies, frequency, fcen, df, nfreq)
         if center is None or size is None:
             raise ValueError("a flux monitor needs a center and a size")
-        monitor = FluxMonitor(self.grid, freqs, _as_xyz("center", center), _as_xyz("size", size),
+        plane_size = _as_xyz("size", size)
+        self._require_flat_on_invariant_axes(plane_size, "flux plane")
+        if self.grid.dimensions != 3:
+            # an invariant axis is flat by construction and never the normal (no power
+            # crosses it): the normal is the first flat axis the run resolves (reference
+            # driver.py:3037-3058)
+            if direction is None:
+                flat = [a for a in self.grid.directions if plane_size[a] < self.grid.dx]
+                if not flat:
+                    raise ValueError(f"flux plane size {plane_size} has no flat axis among the axes this "
+                                     "run resolves; give a size below one cell on the normal axis")
+                direction = flat[0]
+            elif self.grid.is_invariant(int(direction)):
+                raise ValueError(f"a flux plane normal to the invariant {AXIS_NAMES[int(direction)]} axis "
+                                 "measures a power that is identically zero")
+        monitor = FluxMonitor(self.grid, freqs, _as_xyz("center", center), plane_size,
                               direction, weight, self._decimation(decimation_factor, freqs))
         if int(decimation_factor) == 0:
             self._automatic.append(monitor)
@@ -472,7 +490,8 @@ class FdtdDriver:
                         *, frequency: Any = None, fcen: Optional[float] = None, df: Optional[float] = None,
                         nfreq: Optional[int] = None, decimation_factor: int = 1) -> DFTMonitor:
         self._require_unfrozen("add_dft_monitor")
-        self._require_3d_monitor()
+        if size is not None:
+            self._require_flat_on_invariant_axes(_as_xyz("size", size), "DFT region")
         freqs = normalize_frequencies(frequencies, frequency, fcen, df, nfreq)
         monitor = DFTMonitor(self.grid, freqs, tuple(components), self._decimation(decimation_factor, freqs))
         if int(decimation_factor) == 0:

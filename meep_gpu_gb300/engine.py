@@ -188,6 +188,7 @@ class Engine:
         for axis in range(3):
             d.metallic[axis] = 1 if grid.is_metallic(axis) else 0
         d.dtdx = float(np.float32(grid.dt / grid.dx))
+        d.invariant = sum(1 << a for a in range(3) if grid.is_invariant(a))
         for q, axis in enumerate("xyz"):
             d.E[q] = self.fields["E" + axis].data_ptr()
             d.D[q] = self.fields["D" + axis].data_ptr()
@@ -231,7 +232,8 @@ class Engine:
         self._words_steps = 0
         # kernel families the plan may take: the generic ones only when a conductivity or
         # a Bloch phase is stepped (the library refuses the others for such a plan)
-        self.allowed_families = (0, 4) if (self.conductivity or grid.has_bloch) else (0, 1, 2, 3, 4, 5)
+        self.allowed_families = ((0, 4) if (self.conductivity or grid.has_bloch)
+                                 else (0, 2, 4, 5) if grid.dimensions != 3 else (0, 1, 2, 3, 4, 5))
         self._finish_args = (dft_accumulation, kernels, launch_shape, autotune)
         if create:
             self.finish()

@@ -262,11 +262,12 @@ def driver_for(fields, pml, grid, sources, gpu_id: int = 0):
 
     if getattr(fields, "has_nonlinearity", False) or getattr(fields, "has_offdiagonal_epsilon", False):
         raise Unsupported("nonlinear or off-diagonal-epsilon runs are not stepped by this engine")
-    if getattr(grid, "dimensions", 3) != 3 or getattr(grid, "cylindrical", False):
-        raise Unsupported("only 3-D Cartesian runs are stepped by this engine")
+    if getattr(grid, "cylindrical", False):
+        raise Unsupported("cylindrical runs are not stepped by this engine")
     driver = FdtdDriver(tuple(grid.cell_size), grid.resolution, courant=grid.courant,
                         force_complex_fields=bool(fields.force_complex_fields), symmetry=_mirrors(grid),
-                        k_point=tuple(grid.k_point), boundaries=_boundaries(grid), gpu_id=gpu_id)
+                        k_point=tuple(grid.k_point), boundaries=_boundaries(grid), gpu_id=gpu_id,
+                        dimensions=int(getattr(grid, "dimensions", 3)))
     driver.set_epsilon_components(*(np.asarray(_host(fields.epsilon_for(c)), dtype=np.float32) for c in E_NAMES))
     if pml is not None and getattr(pml, "is_active", True):
         driver.setup_pml(tuple(tuple(pair) for pair in pml.thickness_by_face), order=int(pml.order))
@@ -281,6 +282,9 @@ def driver_for(fields, pml, grid, sources, gpu_id: int = 0):
         driver.set_b_conductivity({c: volumes[c] for c in ("Bx", "By", "Bz")})
     for source in sources or ():
         driver.add_source(_source_spec(source))
+    absent = tuple(getattr(fields, "absent_components", ()) or ())
+    if absent:
+        driver.set_absent_components(absent)
     return driver
 
 

@@ -188,19 +188,14 @@ class PML:
 
     def _resolve_invariant_faces(self, faces: Faces, request: Any) -> Faces:
         """No layer on an invariant axis (z of a 2-D run, x and y of a 1-D one: it has no
-        faces). A scalar
-        request means the faces of the axes the run carries; one naming an invariant
-        axis's face is refused."""
-        uniform = not isinstance(request, (dict, tuple, list))
-        resolved = list(faces)
+        faces). A request that puts one there, a scalar thickness included, is refused as
+        the reference refuses it (``driver.py:2248``): name the axes the run resolves."""
         for axis in range(3):
-            if not self.grid.is_invariant(axis) or faces[axis] == (0.0, 0.0):
-                continue
-            if not uniform:
-                raise ValueError(f"PML requested on the {AXIS_NAMES[axis]} axis, which is invariant at "
-                                 f"dimensions={self.grid.dimensions}: it has no faces to absorb at")
-            resolved[axis] = (0.0, 0.0)
-        return tuple(resolved)  # type: ignore[return-value]
+            if self.grid.is_invariant(axis) and faces[axis] != (0.0, 0.0):
+                raise ValueError(f"the PML puts {faces[axis]} cells on the {AXIS_NAMES[axis]} axis, which "
+                                 f"dimensions={self.grid.dimensions} makes translationally invariant: it has "
+                                 "no face to absorb at; request the layers on the axes the run resolves")
+        return faces
 
     def _resolve_mirror_faces(self, faces: Faces, request: Any) -> Faces:
         """No layer on the low face of a folded axis: its cell 0 straddles the mirror plane,

@@ -83,6 +83,11 @@ typedef struct SUF(oracle_state) {
   int part;
   REAL* pE[3];
   REAL* pH[3];
+  /* bit a: axis a is translationally invariant (a 2-D or 1-D run, one periodic cell):
+   * a curl partner differenced along it is absent (reference stepping.py:2189
+   * curl_presence), and the one-partner forms are dtdx * (g1s - g1) and
+   * (-dtdx) * (g2s - g2). */
+  int invariant;
 } SUF(oracle_state);
 
 /* A curl operand read across a Bloch-phased face at the same stored index (reference
@@ -153,10 +158,20 @@ static void SUF(curl_family)(SUF(oracle_state)* s, REAL* const target[3], REAL* 
             if (at0[a1] == 0 && s->bmode[a1]) g1c = SUF(bloch_word)(s, a1, !backward, g1c, partner[a2][c]);
             if (at0[a2] == 0 && s->bmode[a2]) g2c = SUF(bloch_word)(s, a2, !backward, g2c, partner[a1][c]);
           }
-          REAL bracket = g1s - g1c;
-          bracket = bracket + g2c;
-          bracket = bracket - g2s;
-          REAL curl = s->dtdx * bracket;
+          const int have1 = !((s->invariant >> a1) & 1), have2 = !((s->invariant >> a2) & 1);
+          REAL curl;
+          if (have1 && have2) {
+            REAL bracket = g1s - g1c;
+            bracket = bracket + g2c;
+            bracket = bracket - g2s;
+            curl = s->dtdx * bracket;
+          } else if (have1) {
+            curl = s->dtdx * (g1s - g1c);
+          } else if (have2) {
+            curl = (-s->dtdx) * (g2s - g2c);
+          } else {
+            curl = (REAL)0;
+          }
           /* mask: cell 0 of every metallic axis where the target's Yee shift is 0 (the
            * wall, or on a folded axis the plane's ghost: reference stepping.py:2589).
            * B (shift 1 on the two transverse axes) has shift 0 only on its own axis q;

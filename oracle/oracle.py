@@ -71,7 +71,7 @@ def _state_type(real) -> type:
                     ("fcond", (P * 3) * 2), ("fold", ctypes.c_int * 3),
                     ("full", ctypes.c_int * 3), ("bloch", ctypes.c_int), ("bmode", ctypes.c_int * 3),
                     ("bre", real * 3), ("bim", real * 3), ("part", ctypes.c_int),
-                    ("pE", P * 3), ("pH", P * 3)]
+                    ("pE", P * 3), ("pH", P * 3), ("invariant", ctypes.c_int)]
     return State
 
 
@@ -123,6 +123,8 @@ class Problem:
     # counts, and every non-metallic axis)
     owned: Optional[Tuple[int, int, int]] = None
     wraps: Optional[Tuple[bool, bool, bool]] = None
+    # bit a: axis a is translationally invariant (a 2-D or 1-D run)
+    invariant: int = 0
 
 
 YEE = {"Dx": (1, 0, 0), "Dy": (0, 1, 0), "Dz": (0, 0, 1),
@@ -238,7 +240,8 @@ def problem_from_driver(driver) -> Problem:
                    full=tuple(grid.shape_full),
                    bloch=tuple(None if grid.bloch_phase(a) is None else grid.eikna(a) for a in range(3)),
                    owned=tuple(grid.owned_cells(a) for a in range(3)),
-                   wraps=tuple(grid.axis_wraps(a) for a in range(3)))
+                   wraps=tuple(grid.axis_wraps(a) for a in range(3)),
+                   invariant=sum(1 << a for a in range(3) if getattr(grid, "is_invariant", lambda _: False)(a)))
 
 
 class Oracle:
@@ -272,6 +275,7 @@ class Oracle:
         s.nx, s.ny, s.nz = shape
         s.metallic[:] = list(problem.metallic)
         s.fold[:] = list(problem.mirror)
+        s.invariant = int(problem.invariant)
         s.full[:] = list(problem.full) if any(problem.mirror) else list(shape)
         s.part = 1 if part == "imag" else 0
         s.bloch = 1 if any(b is not None for b in problem.bloch) else 0

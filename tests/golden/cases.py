@@ -94,6 +94,13 @@ CASES = {
     "mirror_periodic_lossy": dict(n=(14, 16, 12), pml={"y": {"high": 3}, "x": 2}, steps=50,
                                   symmetry=(("Y", 1),), boundaries=("metallic", "periodic", "metallic"),
                                   mirror_sources=True, conductivity="band"),
+    # A 2-D run (z invariant: one periodic cell): a dielectric cylinder, a Lorentz block,
+    # both polarizations driven (an Ez and an Hz Gaussian point), PML on x and y, flux
+    # lines normal to x and y and a DFT area.
+    "two_d": dict(n=(16, 14, 0), pml=3, steps=60, dims=2),
+    # A 1-D run along z (x and y invariant): an absorber-free PML line, an Ex Gaussian
+    # point, a Drude pole, a z-normal flux point and a DFT segment.
+    "one_d": dict(n=(0, 0, 40), pml=4, steps=80, dims=1),
 }
 
 # The 80^3 sphere-under-PML workload (resolution 10, 10-cell PML, eps 4 sphere of radius
@@ -103,8 +110,50 @@ SPHERE80 = dict(n=(80, 80, 80), pml=10, steps=200, sphere80=True)
 SPHERE80_FULL = dict(SPHERE80, steps=2000)
 
 
+def _build_reduced(driver_cls, susceptibility_cls, case: dict, reference: bool):
+    """A 2-D (z invariant) or 1-D (along z) case: MEEP's spelling, a zero extent on each
+    invariant axis."""
+    res = 10
+    dims = case["dims"]
+    lengths = tuple(v / res for v in case["n"])
+    boundaries = {"x": "metallic", "y": "metallic"} if dims == 2 else {"z": "metallic"}
+    d = driver_cls(cell_size=lengths, resolution=res, courant=0.5, force_complex_fields=False,
+                   boundaries=boundaries, dimensions=dims, **({"prefer_gpu": False} if reference else {}))
+    d.setup_pml({"x": case["pml"], "y": case["pml"]} if dims == 2 else {"z": case["pml"]})
+    x, y, z = d.grid.meshgrid()
+    flux, dft = [], []
+    if dims == 2:
+        d.set_epsilon(np.where(x ** 2 + y ** 2 < 0.3 ** 2, 4.0, 1.0).astype(np.float32))
+        block = (np.abs(x - 0.3) < 0.15) & (np.abs(y) < 0.3)
+        d.add_susceptibility(susceptibility_cls(frequency=0.9, gamma=0.1),
+                             np.where(block, 0.8, 0.0).astype(np.float32))
+        d.add_source({"source_type": "gaussian", "component": "Ez", "center": (-0.4, 0.03, 0.0),
+                      "size": (0, 0, 0), "frequency": 0.6, "fwidth": 0.5})
+        d.add_source({"source_type": "gaussian", "component": "Hz", "center": (-0.35, -0.1, 0.0),
+                      "size": (0, 0, 0), "frequency": 0.5, "fwidth": 0.4, "amplitude": 0.7})
+        flux.append(d.add_flux_monitor(fcen=0.6, df=0.3, nfreq=4, center=(0.45, 0.0, 0.0),
+                                       size=(0, 0.8, 0), decimation_factor=1))
+        flux.append(d.add_flux_monitor(frequencies=[0.4, 0.55], center=(0.0, 0.35, 0.0),
+                                       size=(0.9, 0, 0), decimation_factor=2))
+        dft.append(d.add_dft_monitor(frequencies=[0.5, 0.7], components=("Ez", "Hx", "Hz"),
+                                     center=(0.1, 0.0, 0.0), size=(0.6, 0.5, 0), decimation_factor=1))
+    else:
+        d.set_epsilon(np.where(np.abs(z) < 0.5, 2.5, 1.0).astype(np.float32))
+        d.add_susceptibility(susceptibility_cls(frequency=0.6, gamma=0.2, kind="drude"),
+                             np.where(np.abs(z) < 0.5, 0.4, 0.0).astype(np.float32))
+        d.add_source({"source_type": "gaussian", "component": "Ex", "center": (0.0, 0.0, -1.0),
+                      "size": (0, 0, 0), "frequency": 0.7, "fwidth": 0.6})
+        flux.append(d.add_flux_monitor(fcen=0.7, df=0.4, nfreq=5, center=(0.0, 0.0, 1.0),
+                                       size=(0, 0, 0), decimation_factor=1))
+        dft.append(d.add_dft_monitor(frequencies=[0.6, 0.8], components=("Ex", "Hy"),
+                                     center=(0.0, 0.0, 0.2), size=(0, 0, 0.6), decimation_factor=1))
+    return d, flux, dft
+
+
 def build_case(driver_cls, susceptibility_cls, case: dict, reference: bool = False):
     """Configure one case; returns (driver, flux monitors, DFT monitors)."""
+    if case.get("dims"):
+        return _build_reduced(driver_cls, susceptibility_cls, case, reference)
     res = 10
     n = case["n"]
     lengths = tuple(v / res for v in n)

@@ -254,11 +254,11 @@ def test_batch_steps_every_golden_configuration_to_the_reference_words(gpu):
     from tests import golden_io
     from tests.golden.cases import CASES, build_case
 
-    # <= 2 monitors a slot; lossy runs and folds are not batched (refused by name); a
-    # complex run takes two slots (its two parts), Bloch-phased or not
+    # <= 2 monitors a slot; lossy runs, folds and 2-D / 1-D runs are not batched (refused
+    # by name); a complex run takes two slots (its two parts), Bloch-phased or not
     names = [n for n in sorted(CASES) if n not in ("mixed", "tile_mixed", "complex_mixed")
              and not CASES[n].get("conductivity") and not CASES[n].get("bloch_monitors")
-             and not CASES[n].get("symmetry")]
+             and not CASES[n].get("symmetry") and not CASES[n].get("dims")]
     assert {"complex_sphere", "bloch_sphere", "bloch_magnetic", "magnetic"} <= set(names)
     slots = sum(2 if CASES[n].get("complex") else 1 for n in names)
     server = serving.BatchServer(gpu, max_slots=slots, steps_per_replay=16, max_side=72)

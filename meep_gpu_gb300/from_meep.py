@@ -100,6 +100,41 @@ def _side_names(mp, side) -> Tuple[str, ...]:
 
 
 # --- compatibility ---------------------------------------------------------------------
+def lifted_dimensions(sim) -> Optional[int]:
+    """MEEP's dimensions of ``sim``: its ``dimensions``, or 2 / 1 inferred from a zero
+    cell extent on z / on x and y (MEEP's ``Simulation._infer_dimensions``); None for a
+    combination this engine does not step. MEEP ignores an invariant axis's extent, so
+    the lift passes 0 there."""
+    dims = int(getattr(sim, "dimensions", 3) or 3)
+    cell = _vector3(sim.cell_size)
+    if dims == 3 and cell[2] == 0.0 and cell[0] > 0.0 and cell[1] > 0.0:
+        dims = 2
+    elif dims == 3 and cell[0] == 0.0 and cell[1] == 0.0 and cell[2] > 0.0:
+        dims = 1
+    resolved = {3: (0, 1, 2), 2: (0, 1), 1: (2,)}.get(dims)
+    if resolved is None or any(cell[a] <= 0.0 for a in resolved):
+        return None
+    return dims
+
+
+def _lifted_cell(sim, dims: int) -> Tuple[float, float, float]:
+    cell = list(_vector3(sim.cell_size))
+    for axis in {3: (), 2: (2,), 1: (0, 1)}[dims]:
+        cell[axis] = 0.0
+    return tuple(cell)  # type: ignore[return-value]
+
+
+def _lifted_boundaries(sim, dims: int, kind: str) -> Dict[str, str]:
+    """The boundary of every axis the run resolves; a one-cell axis is periodic whatever
+    the k_point (MEEP's unit directions, fields.cpp)."""
+    cell = _vector3(sim.cell_size)
+    out = {}
+    for axis in {3: (0, 1, 2), 2: (0, 1), 1: (2,)}[dims]:
+        one_cell = int(cell[axis] * float(sim.resolution) + 0.5) == 1
+        out["xyz"[axis]] = "periodic" if one_cell else kind
+    return out
+
+
 def _materials(sim) -> List[Any]:
     materials = [getattr(sim, "default_material", None)]
     materials += [getattr(obj, "material", None) for obj in (getattr(sim, "geometry", None) or ())]
@@ -110,12 +145,12 @@ def gpu_compatibility(mp, sim) -> List[str]:
     """Every reason this engine refuses ``sim`` (empty: it can be lifted); reference
     ``gpu_compatibility`` (from_meep.py) for the configurations stepped here."""
     reasons: List[str] = []
-    dims = getattr(sim, "dimensions", 3)
-    if dims != 3 or getattr(sim, "is_cylindrical", False):
-        reasons.append(f"only 3-D Cartesian cells are stepped (dimensions={dims!r})")
-    cell = _vector3(sim.cell_size)
-    if any(v <= 0 for v in cell):
-        reasons.append(f"a cell with a zero extent {cell} is a reduced-dimension run")
+    if getattr(sim, "is_cylindrical", False):
+        reasons.append("cylindrical cells are not stepped")
+    dims = lifted_dimensions(sim)
+    if dims is None:
+        reasons.append(f"dimensions={getattr(sim, 'dimensions', 3)!r} on a cell of size "
+                       f"{_vector3(sim.cell_size)}: 3-D, 2-D (z invariant) and 1-D (along z) cells are stepped")
     if getattr(sim, "special_kz", False):
         reasons.append("special_kz (an out-of-plane beta) is not stepped")
     if getattr(sim, "material_function", None) is not None or getattr(sim, "epsilon_input_file", ""):
@@ -216,6 +251,10 @@ def yee_points(grid, component: str) -> Tuple[np.ndarray, np.ndarray, np.ndarray
     tics = []
     for axis in range(3):
         n = grid.shape[axis]
+        if grid.is_invariant(axis):
+            # MEEP hands 0 on an axis the run does not carry (vec2py)
+            tics.append(np.zeros(1))
+            continue
         doubled = grid.origin_doubled(axis) + 2 * np.arange(n) + shifts[axis]
         tics.append(doubled * (grid.dx / 2.0))
     return tuple(tics)  # type: ignore[return-value]
@@ -336,7 +375,8 @@ def _lift_layers(mp, sim, driver) -> None:
     for layer in getattr(sim, "boundary_layers", None) or ():
         thickness = float(layer.thickness)
         axis = _direction_axis(mp, getattr(layer, "direction", getattr(mp, "ALL", -1)))
-        axes = range(3) if axis is None else (axis,)
+        # a layer on an invariant axis is dropped, as MEEP drops it (it has no face)
+        axes = [a for a in (range(3) if axis is None else (axis,)) if not driver.grid.is_invariant(a)]
         sides = _side_names(mp, getattr(layer, "side", getattr(mp, "ALL", -1)))
         kind = type(layer).__name__
         for a in axes:
@@ -359,6 +399,19 @@ def _lift_layers(mp, sim, driver) -> None:
         driver.setup_pml(faces, order=order or 2)
     if absorbers:
         driver.set_absorber(absorbers)
+
+
+def _lift_absent_components(mp, sim, driver) -> None:
+    """The components MEEP allocated no array for (``fields::have_component``, read once
+    the sources are in; reference ``driver.py:2344``): a reduced-dimension run's other
+    polarization. A fields object without that query leaves every component stepped."""
+    have = getattr(sim.fields, "have_component", None)
+    if not callable(have) or driver.grid.dimensions == 3:
+        return
+    absent = [name for name in ("Ex", "Ey", "Ez", "Dx", "Dy", "Dz", "Hx", "Hy", "Hz", "Bx", "By", "Bz")
+              if hasattr(mp, name) and not have(getattr(mp, name))]
+    if absent:
+        driver.set_absent_components(absent)
 
 
 def _lift_source(mp, source) -> Dict[str, Any]:
@@ -460,13 +513,15 @@ def lift_simulation(sim, *, prefer_gpu: bool = True, gpu_id: int = 0, epsilon_ro
     started = time.perf_counter()
     sim.init_sim()
     k_point = getattr(sim, "k_point", False)
+    dims = lifted_dimensions(sim)
     driver = FdtdDriver(
-        cell_size=_vector3(sim.cell_size), resolution=float(sim.resolution), courant=float(sim.Courant),
+        cell_size=_lifted_cell(sim, dims), resolution=float(sim.resolution), courant=float(sim.Courant),
         force_complex_fields=not bool(sim.fields.is_real),
         symmetry=tuple(Mirror("XYZ"[_direction_axis(mp, s.direction)], int(complex(s.phase).real))
                        for s in getattr(sim, "symmetries", None) or ()),
         k_point=_vector3(k_point) if k_point else (0.0, 0.0, 0.0),
-        boundaries="periodic" if k_point else "metallic", gpu_id=gpu_id)
+        boundaries=_lifted_boundaries(sim, dims, "periodic" if k_point else "metallic"),
+        dimensions=dims, gpu_id=gpu_id)
     try:
         route = epsilon_route
         if route == "auto":
@@ -477,6 +532,7 @@ def lift_simulation(sim, *, prefer_gpu: bool = True, gpu_id: int = 0, epsilon_ro
         _lift_layers(mp, sim, driver)
         for source in getattr(sim, "sources", None) or ():
             driver.add_source(_lift_source(mp, source))
+        _lift_absent_components(mp, sim, driver)
         driver.migrated_monitors = migrate_monitors(mp, sim, driver)
     except Exception:
         driver.close()

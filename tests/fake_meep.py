@@ -154,6 +154,18 @@ class _Fields:
     def last_source_time(self):
         return max([s.src.last_time() for s in self._sim.sources] + [0.0])
 
+    def have_component(self, component):
+        """MEEP allocates a component with every one "like" it: in a 2-D cell (zero z
+        extent) the polarization of some source, in 3-D everything."""
+        cell = self._sim.cell_size
+        if cell.z != 0:
+            return True
+        names = {Ex: "Ex", Ey: "Ey", Ez: "Ez", Hx: "Hx", Hy: "Hy", Hz: "Hz",
+                 Dx: "Dx", Dy: "Dy", Dz: "Dz", Bx: "Bx", By: "By", Bz: "Bz"}
+        families = (("Ez", "Dz", "Hx", "Hy", "Bx", "By"), ("Ex", "Ey", "Dx", "Dy", "Hz", "Bz"))
+        sourced = {names.get(src.component) for src in self._sim.sources}
+        return any(names.get(component) in family and sourced & set(family) for family in families)
+
     def get_chi1inv(self, component, direction, loc, frequency=0.0):
         assert frequency == 0
         eps = self._sim.get_epsilon_grid(np.array([loc.x]), np.array([loc.y]), np.array([loc.z]))

@@ -146,8 +146,11 @@ def test_periodic_and_complex_and_symmetric_cells():
 def test_lift_refuses_what_the_engine_does_not_step_by_name():
     cases = []
     sim, _, _ = standin()
-    sim.dimensions = 2
-    cases.append((sim, "3-D"))
+    sim.is_cylindrical = True
+    cases.append((sim, "cylindrical"))
+    sim, _, _ = standin()
+    sim.cell_size = mp.Vector3(2.4, 0, 0)  # a zero extent on y with x resolved
+    cases.append((sim, "dimensions"))
     sim, _, _ = standin()
     sim.dft_objects.append(mp.DftForce([0.5], [mp.FluxRegion(mp.Vector3(), mp.Vector3(0, 1, 1))], 0))
     cases.append((sim, "DftForce"))
@@ -243,3 +246,39 @@ def test_two_run_normalisation_through_minus_flux_data(gpu):
     second.close()
     d1.close()
     d2.close()
+
+
+def test_a_2d_simulation_lifts_to_the_hand_built_2d_run():
+    """A cell with no z extent is MEEP's 2-D run: one periodic cell on the invariant z, a
+    PML on the two resolved axes only, the other polarization recorded as absent, and a
+    flux line; the lifted run's float32 oracle words equal the hand-built run's."""
+    from oracle.oracle import Oracle, problem_from_driver
+
+    disk = mp.Medium(epsilon=4.0)
+    sim = mp.Simulation(mp.Vector3(2.0, 1.6, 0), 10, geometry=[mp.Cylinder(0.3, material=disk)],
+                        boundary_layers=[mp.PML(0.3)],
+                        sources=[mp.Source(mp.GaussianSource(0.8, fwidth=1.0), component=mp.Ez,
+                                           center=mp.Vector3(-0.5, 0.03, 0))])
+    sim.add_flux(0.8, 0.5, 4, mp.FluxRegion(mp.Vector3(0.5, 0, 0), mp.Vector3(0, 1.0, 0)))
+    lifted = lift_simulation(sim)
+    assert lifted.grid.dimensions == 2 and lifted.grid.shape == (20, 16, 1)
+    assert lifted.pml.faces[2] == (0.0, 0.0)
+    assert set(lifted.absent_components) == {"Ex", "Ey", "Dx", "Dy", "Hz", "Bz"}
+    d = FdtdDriver((2.0, 1.6, 0.0), 10, force_complex_fields=False, dimensions=2,
+                   boundaries={"x": "metallic", "y": "metallic"})
+    xs, ys, _ = yee_points(d.grid, "Ez")
+    eps = np.where((xs[:, None, None] ** 2 + ys[None, :, None] ** 2) <= 0.3 ** 2, 4.0, 1.0)
+    d.set_epsilon(np.broadcast_to(eps, d.grid.shape))
+    d.setup_pml({"x": 3.0, "y": 3.0})
+    d.add_source({"source_type": "gaussian", "component": "Ez", "center": (-0.5, 0.03, 0.0), "size": (0, 0, 0),
+                  "frequency": 0.8, "fwidth": 1.0})
+    d.add_flux_monitor(list(np.linspace(0.55, 1.05, 4)), center=(0.5, 0, 0), size=(0, 1.0, 0),
+                       decimation_factor=0)
+    runs = []
+    for driver in (lifted, d):
+        oracle = Oracle(problem_from_driver(driver), "f32")
+        oracle.run(40)
+        runs.append(oracle)
+    for c in FIELDS:
+        assert np.array_equal(runs[0].field(c), runs[1].field(c)), c
+    assert np.array_equal(runs[0].flux_spectrum(0), runs[1].flux_spectrum(0))

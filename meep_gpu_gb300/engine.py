@@ -54,6 +54,18 @@ AUTOTUNE_CANDIDATES = ((0, 32, 4, 4), (0, 32, 8, 4), (0, 32, 4, 8), (0, 64, 2, 8
                        (4, 32, 8, 2), (4, 32, 8, 8), (4, 64, 4, 4), (4, 16, 16, 4), (4, 32, 2, 4),
                        (5, 32, 4, 4), (5, 16, 8, 4), (5, 32, 4, 8), (5, 32, 2, 8), (5, 32, 4, 2))
 _AUTOTUNE_CACHE: Dict[tuple, Tuple[int, int, int, int]] = {}
+
+
+def autotune_candidates(grid: Grid) -> Tuple[Tuple[int, int, int, int], ...]:
+    """The launch shapes timed for a grid. The marches put z on a warp's lanes, so a grid
+    one cell deep in z (a 2-D run) also takes CTAs one cell wide in z with y on the lanes,
+    and one a single cell wide in y (a 1-D run) CTAs one row high with z on the lanes."""
+    extra = []
+    if grid.shape[2] == 1:
+        extra += [(f, 1, by, xc) for f in (0, 2, 4, 5) for by in (64, 128) for xc in (2, 4, 8)]
+    if grid.shape[1] == 1:
+        extra += [(f, bz, 1, xc) for f in (0, 2, 4, 5) for bz in (64, 128) for xc in (1, 2, 4)]
+    return AUTOTUNE_CANDIDATES + tuple(extra)
 # Wavefront choices the autotuner times against the best pair of per-half kernels:
 # (march family, block_z, block_y, x_chunk, window), as kernel choice
 # (6, family, block_z, block_y, x_chunk, window); family 0 the plain column marches, 2 the
@@ -636,7 +648,7 @@ class Engine:
         best = [None, None]
         best_ms = [float("inf"), float("inf")]
         timed: List[Dict[tuple, float]] = [{}, {}]  # every candidate's time, per half
-        for choice in AUTOTUNE_CANDIDATES:
+        for choice in autotune_candidates(self.grid):
             if choice[0] not in self.allowed_families:
                 continue
             # a candidate one half refuses is timed on the other half only

@@ -57,11 +57,11 @@ import numpy as np
 
 WORKLOADS = ("sphere80", "sphere192_8dft", "lorentz192", "sphere128", "sphere192", "absorber192",
              "lossy_pml192", "lossy40", "mirror192", "mirror80", "sphere192_nopml", "bloch192",
-             "complex80", "bloch48")
+             "complex80", "bloch48", "tm2d_4096")
 STEPS = {"sphere80": 2000, "sphere192_8dft": 5000, "lorentz192": 10000, "sphere128": 1000,
          "sphere192": 5000, "absorber192": 5000, "lossy_pml192": 5000, "lossy40": 300,
          "mirror192": 5000, "mirror80": 600, "sphere192_nopml": 5000, "bloch192": 5000,
-         "complex80": 600, "bloch48": 600}
+         "complex80": 600, "bloch48": 600, "tm2d_4096": 4000}
 
 
 def _axes(grid):
@@ -171,6 +171,20 @@ def build(name: str, driver_cls=None, susceptibility_cls=None, **driver_kwargs):
                       "size": (0, 0.6, 0.4), "frequency": 0.4, "fwidth": 0.3})
         flux = [d.add_flux_monitor(fcen=0.4, df=0.3, nfreq=20, center=(0.9, 0, 0), size=(0, 2.0, 2.0),
                                    decimation_factor=2)]
+        return d, flux, []
+    if name == "tm2d_4096":
+        # a 2-D run (z invariant): 4096 x 4096 cells at resolution 20, a 20-cell PML on x
+        # and y, an eps-4 disk of radius 40, an Ez Gaussian point and two flux lines
+        d = driver_cls(cell_size=(204.8, 204.8, 0.0), resolution=20, courant=0.5, dimensions=2,
+                       force_complex_fields=False, boundaries={"x": "metallic", "y": "metallic"},
+                       **driver_kwargs)
+        d.setup_pml({"x": 20, "y": 20})
+        x, y, _ = _axes(d.grid)
+        d.set_epsilon(np.where(x ** 2 + y ** 2 < 40.0 ** 2, np.float32(4.0), np.float32(1.0)))
+        d.add_source({"source_type": "gaussian", "component": "Ez", "center": (-60.0, 0.0, 0.0),
+                      "size": (0, 0, 0), "frequency": 0.5, "fwidth": 0.3})
+        flux = [d.add_flux_monitor(fcen=0.5, df=0.3, nfreq=50, center=(sign * 60.0, 0, 0),
+                                   size=(0, 150.0, 0), decimation_factor=0) for sign in (1.0, -1.0)]
         return d, flux, []
     if name == "lorentz192":
         res = 20

@@ -33,8 +33,9 @@ L2_PREFETCH = ((4, 32, 4, 4), (5, 16, 8, 4))  # families 0 / 2 with the x chunk 
 WAVE = (6, 2, 32, 4, 4, 3)  # the wavefront path: prefetching marches, 32 x 4 tiles, 4-plane chunks,
 # 3-step blocks
 SPLIT = ((4, 32, 4, 4), (2, 32, 4, 2), None, 3)  # each half as three x-range launches on three streams
+YLANES = ((0, 1, 128, 4), (4, 1, 64, 2))  # y on the lanes: CTAs one cell wide in z
 MODES = {"tiles": TILES, "generic": GENERIC, "prefetch": PREFETCH, "ws": WARP_SPECIALIZED,
-         "l2": L2_PREFETCH, "wave": WAVE, "split": SPLIT}
+         "l2": L2_PREFETCH, "wave": WAVE, "split": SPLIT, "ylanes": YLANES}
 
 
 def x_metallic(case) -> bool:
@@ -87,7 +88,7 @@ def test_fields_are_the_reference_words(gpu, name, mode):
         pytest.skip("the wavefront path steps metallic-x runs without folds, Bloch phases or conductivity")
     if mode == "split" and not split_steps(case):
         pytest.skip("the x-range split steps metallic-x runs without Bloch phases")
-    if (case.get("conductivity") or case.get("k_point")) and mode not in ("generic", "l2", "wave", "split"):
+    if (case.get("conductivity") or case.get("k_point")) and mode not in ("generic", "l2", "wave", "split", "ylanes"):
         pytest.skip("lossy and Bloch-phased runs step with the generic kernels only (the others are refused)")
     if mode in ("tiles", "ws") and not tileable:
         mode = "generic"

@@ -137,7 +137,10 @@ def test_absent_components_are_recorded_and_refused_when_driven():
 
 
 MODES = {"autotuned": None, "generic": (0, 32, 4, 4), "prefetch": (2, 32, 4, 4), "l2": (4, 32, 4, 4),
-         "split": ((4, 32, 4, 4), (2, 32, 4, 2), None, 3)}
+         "split": ((4, 32, 4, 4), (2, 32, 4, 2), None, 3),
+         # y on the warp's lanes (CTAs one cell wide in z) and z rows one cell high in y:
+         # the shapes the autotuner adds for 2-D and 1-D grids
+         "ylanes": ((0, 1, 128, 4), (4, 1, 64, 2)), "zrows": ((2, 128, 1, 2), (4, 64, 1, 4))}
 
 
 @pytest.mark.gpu
@@ -147,7 +150,7 @@ def test_engine_reproduces_meeps_words(gpu, case, mode):
     driver, entry = golden_io.build_identity(case, FdtdDriver, Susceptibility)
     if mode == "split" and driver.grid.shape[0] < 6:
         pytest.skip("the x-range split needs an x axis of several ranges")
-    if mode == "prefetch" and driver.has_conductivity:
+    if mode in ("prefetch", "zrows") and driver.has_conductivity:
         pytest.skip("a run with a conductivity steps with the generic families 0 and 4 only")
     driver.kernels = MODES[mode]
     bad = _mismatches(case, entry, lambda c: driver.get_field(c, cell_centered=False), driver.step_many)

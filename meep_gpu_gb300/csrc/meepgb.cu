@@ -1464,7 +1464,7 @@ __device__ __forceinline__ void fold_keep_h(const StepParams& p, const FoldArgs&
   cell_of(p, g, i, j, k);
   const bool sb = p.pml && in_runs(p.B[q], coord_along(q, i, j, k));
   f.saved[0][t] = p.H[q][g];
-  f.saved[0][n + t] = sb ? p.fwH[q].data[g] : 0.f;
+  f.saved[0][n + t] = sb ? p.B[q].data[g] : 0.f;  // f_w of H is B's word there
 }
 
 // The D ghosts' E, f_w and the polarization the E half overwrites, before the E half.
@@ -1501,7 +1501,6 @@ __device__ __forceinline__ void fold_h_ghost(const StepParams& p, const FoldArgs
     const float kps = ldgf(p.kps[kInteger][q], cq), kms = ldgf(p.kms[kInteger][q], cq);
     h = (first_step ? b : h_old) + (kps * b - kms * (first_step ? b : w_old));
     p.B[q].data[g] = b;
-    p.fwH[q].data[g] = b;
   }
   p.H[q][g] = h;
 }

@@ -293,7 +293,7 @@ __device__ __forceinline__ float cond_curl(const mgb_conductivity& cp, int side,
 // Every auxiliary word an H cell reads, loaded from the membership flags alone, so the
 // caller issues these loads together with the field loads (one round trip per plane).
 struct HAux {
-  float b[3], w[3], u[3];
+  float b[3], u[3];
 };
 
 __device__ __forceinline__ void h_aux_load(const StepParams& p, const HColumn& col, const HPlane& pl, int c,
@@ -303,7 +303,6 @@ __device__ __forceinline__ void h_aux_load(const StepParams& p, const HColumn& c
 #pragma unroll
   for (int q = 0; q < 3; ++q) {
     a.b[q] = sb[q] ? p.B[q].data[c] : 0.f;
-    a.w[q] = sb[q] ? p.fwH[q].data[c] : 0.f;
     a.u[q] = sf[q] ? p.fuB[q].data[c] : 0.f;
   }
 }
@@ -320,7 +319,10 @@ __device__ __forceinline__ void h_cell_v(const StepParams& p, const HColumn& col
   float b0 = sb0 ? a.b[0] : h_old[0];
   float b1 = sb1 ? a.b[1] : h_old[1];
   float b2 = sb2 ? a.b[2] : h_old[2];
-  const float w0 = a.w[0], w1 = a.w[1], w2 = a.w[2];
+  // f_w of H: MEEP's update_H stores B's new word in it on the own-axis membership, where
+  // B itself is stored too, so after step 0 (which reads neither) it is always B's old
+  // word: read once, as B, and not stored separately
+  const float w0 = a.b[0], w1 = a.b[1], w2 = a.b[2];
   const float u0 = a.u[0], u1 = a.u[1], u2 = a.u[2];
   // Bx: dsig y, dsigu z; By: dsig z, dsigu x; Bz: dsig x, dsigu y.
   float n0 = 0.f, n1 = 0.f, n2 = 0.f;
@@ -358,9 +360,9 @@ __device__ __forceinline__ void h_cell_v(const StepParams& p, const HColumn& col
   if (sf0) p.fuB[0].data[c] = n0;
   if (sf1) p.fuB[1].data[c] = n1;
   if (sf2) p.fuB[2].data[c] = n2;
-  if (sb0) { p.B[0].data[c] = b0; p.fwH[0].data[c] = b0; }
-  if (sb1) { p.B[1].data[c] = b1; p.fwH[1].data[c] = b1; }
-  if (sb2) { p.B[2].data[c] = b2; p.fwH[2].data[c] = b2; }
+  if (sb0) p.B[0].data[c] = b0;
+  if (sb1) p.B[1].data[c] = b1;
+  if (sb2) p.B[2].data[c] = b2;
 }
 
 // Whether the H variant chosen for `axes` reads the plane's x coefficients (every
@@ -471,10 +473,7 @@ __device__ __forceinline__ void h_aux_prefetch(const StepParams& p, const HColum
     const bool f[3] = {col.f0, in_runs(p.fuB[1], i), col.f2};
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
-      if (b[q]) {
-        l2_prefetch(p.B[q].data + c);
-        l2_prefetch(p.fwH[q].data + c);
-      }
+      if (b[q]) l2_prefetch(p.B[q].data + c);
       if (f[q]) l2_prefetch(p.fuB[q].data + c);
     }
   }

@@ -779,7 +779,7 @@ class Engine:
         """Minimum HBM bytes one launch of each step kernel must move.
 
         H half: read E (3 volumes) and H (3), write H (3); on the PML slabs read and
-        write ``fu`` of B, and read and write the slab B and ``f_w`` of H.
+        write ``fu`` of B and the slab B (``f_w`` of H is B's old word there: no bytes).
         E half: read H (3 volumes: the slab word or B's) and D (3) and each distinct
         inverse-epsilon volume, write D (3) and E (3); on the slabs read and write ``fu``
         of D, read and write ``f_w`` of E and read E; per pole and driven component read
@@ -788,7 +788,7 @@ class Engine:
         cells = self.grid.total_cells
         word = 4
         aux = lambda name: sum(self.aux_cells[f"{name}{a}"] for a in "xyz") if self.pml is not None else 0  # noqa: E731
-        h = 9 * cells + 2 * aux("fuB") + 2 * aux("B") + 2 * aux("fwH")
+        h = 9 * cells + 2 * aux("fuB") + 2 * aux("B")
         distinct_inv = len({t.data_ptr() for t in self.inv_eps})
         e = (12 + distinct_inv) * cells + 2 * aux("fuD") + 3 * aux("fwE")
         for kept in getattr(self, "pole_tensors", []):

@@ -1474,14 +1474,19 @@ __device__ __forceinline__ void fold_keep_e(const StepParams& p, const FoldArgs&
   cell_of(p, g, i, j, k);
   const bool sw = p.pml && in_runs(p.fwE[q], coord_along(q, i, j, k));
   f.saved[1][t] = p.E[q][g];
-  f.saved[1][n + t] = sw ? p.fwE[q].data[g] : 0.f;
   bool in_box;
   const long long pb = pole_index(p, i, j, k, in_box);
+  // f_w of E: chi1inv (D - sum of P) of the old D and of the polarization the E half
+  // overwrites, as the step kernels recompute it
+  float fw = p.D[q][g];
   for (int m = 0; m < p.npoles; ++m) {
     const mgb_pole& pole = p.poles[m];
     const float* prv = parity ? pole.p[q][0] : pole.p[q][1];
-    f.saved[1][(2 + m) * n + t] = (in_box && pole.sigma[q] != nullptr) ? prv[pb] : 0.f;
+    const float pp = (in_box && pole.sigma[q] != nullptr) ? prv[pb] : 0.f;
+    f.saved[1][(2 + m) * n + t] = pp;
+    if (in_box && pole.sigma[q] != nullptr) fw = fw - pp;
   }
+  f.saved[1][n + t] = sw ? __ldg(p.inv_eps[q] + g) * fw : 0.f;
 }
 
 // One B ghost: B from its image, zero_metal_B, then update_H on its own-axis membership.
@@ -1528,7 +1533,6 @@ __device__ __forceinline__ void fold_e_ghost(const StepParams& p, const FoldArgs
   if (p.pml && in_runs(p.fwE[q], cq)) {
     const float e_old = f.saved[1][t], fw_old = f.saved[1][n + t];
     e = e_old + (ldgf(p.kps[kHalf][q], cq) * w - ldgf(p.kms[kHalf][q], cq) * fw_old);
-    p.fwE[q].data[g] = w;
   }
   p.E[q][g] = e;
   if (in_box)

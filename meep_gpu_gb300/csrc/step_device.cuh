@@ -446,10 +446,11 @@ __device__ __forceinline__ void e_plane_coefficients(const StepParams& p, int i,
 // for one cell at offset c, for a warp that may touch the x (SX), y (SY) and z (SZ)
 // memberships (x: Dx own, Dy dsigu, Dz dsig; y: Dx dsig, Dy own, Dz dsigu; z: Dx dsigu,
 // Dy dsig, Dz own). <false, false, false> is the plain update.
-// Every auxiliary word an E cell reads (split-field fu of D, f_w of E, and the old E on
-// the own-axis membership), loaded from the flags alone with the field loads.
+// Every auxiliary word an E cell reads (split-field fu of D and the old E on the
+// own-axis membership), loaded from the flags alone with the field loads. f_w of E is
+// not among them: its old word is recomputed from the old D (see e_cell_v).
 struct EAux {
-  float u[3], fw[3], e[3];
+  float u[3], e[3];
 };
 
 __device__ __forceinline__ void e_aux_load(const StepParams& p, const EColumn& col, const EPlane& pl, int c,
@@ -459,7 +460,6 @@ __device__ __forceinline__ void e_aux_load(const StepParams& p, const EColumn& c
 #pragma unroll
   for (int q = 0; q < 3; ++q) {
     a.u[q] = sf[q] ? p.fuD[q].data[c] : 0.f;
-    a.fw[q] = sw[q] ? p.fwE[q].data[c] : 0.f;
     a.e[q] = sw[q] ? p.E[q][c] : 0.f;
   }
 }
@@ -487,10 +487,7 @@ __device__ __forceinline__ void e_aux_prefetch(const StepParams& p, const EColum
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
       if (f[q]) l2_prefetch(p.fuD[q].data + c);
-      if (w[q]) {
-        l2_prefetch(p.fwE[q].data + c);
-        l2_prefetch(p.E[q] + c);
-      }
+      if (w[q]) l2_prefetch(p.E[q] + c);
     }
   }
 }
@@ -509,8 +506,33 @@ __device__ __forceinline__ void e_cell_v(const StepParams& p, const EColumn& col
   const bool sw0 = SX && pl.w0, sw1 = SY && col.w1, sw2 = SZ && col.w2;
   // The cell's auxiliary words (loaded by the caller, before any store).
   const float u0 = a.u[0], u1 = a.u[1], u2 = a.u[2];
-  const float fw0 = a.fw[0], fw1 = a.fw[1], fw2 = a.fw[2];
   const float e0 = a.e[0], e1 = a.e[1], e2 = a.e[2];
+  const bool in_box = p.npoles > 0 && i >= p.pbox[0] && i < p.pbox[1] && j >= p.pbox[2] &&
+                      j < p.pbox[3] && k >= p.pbox[4] && k < p.pbox[5];
+  long long pb = 0;
+  if (in_box) {
+    const int bny = p.pbox[3] - p.pbox[2], bnz = p.pbox[5] - p.pbox[4];
+    pb = ((long long)(i - p.pbox[0]) * bny + (j - p.pbox[2])) * bnz + (k - p.pbox[4]);
+  }
+  // f_w of E: MEEP's update_E stores w = chi1inv (D - sum of P) in it on the own-axis
+  // membership, so its old word is that expression of the old D (this cell's stored D)
+  // and of the polarization the previous step subtracted (the buffer this step writes
+  // P' over), in the same order of operations: recomputed here instead of stored.
+  float fw[3] = {0.f, 0.f, 0.f};
+  if (sw0 || sw1 || sw2) {
+    fw[0] = d[0]; fw[1] = d[1]; fw[2] = d[2];
+    if (in_box)
+      for (int m = 0; m < p.npoles; ++m) {
+        const mgb_pole& pole = p.poles[m];
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+          if (pole.sigma[q] != nullptr) fw[q] = fw[q] - (parity ? pole.p[q][0] : pole.p[q][1])[pb];
+      }
+    fw[0] = inv[0] * fw[0];
+    fw[1] = inv[1] * fw[1];
+    fw[2] = inv[2] * fw[2];
+  }
+  const float fw0 = fw[0], fw1 = fw[1], fw2 = fw[2];
   // Dx: dsig y, dsigu z; Dy: dsig z, dsigu x; Dz: dsig x, dsigu y.
   float n0 = 0.f, n1 = 0.f, n2 = 0.f;
   if (COND) {
@@ -540,13 +562,8 @@ __device__ __forceinline__ void e_cell_v(const StepParams& p, const EColumn& col
   if (wy || wz) d[0] = 0.f;
   if (wx || wz) d[1] = 0.f;
   if (wx || wy) d[2] = 0.f;
-  const bool in_box = p.npoles > 0 && i >= p.pbox[0] && i < p.pbox[1] && j >= p.pbox[2] &&
-                      j < p.pbox[3] && k >= p.pbox[4] && k < p.pbox[5];
-  long long pb = 0;
   float w[3] = {d[0], d[1], d[2]};
   if (in_box) {
-    const int bny = p.pbox[3] - p.pbox[2], bnz = p.pbox[5] - p.pbox[4];
-    pb = ((long long)(i - p.pbox[0]) * bny + (j - p.pbox[2])) * bnz + (k - p.pbox[4]);
     for (int m = 0; m < p.npoles; ++m) {
       const mgb_pole& pole = p.poles[m];
 #pragma unroll
@@ -564,9 +581,6 @@ __device__ __forceinline__ void e_cell_v(const StepParams& p, const EColumn& col
   if (sf0) p.fuD[0].data[c] = n0;
   if (sf1) p.fuD[1].data[c] = n1;
   if (sf2) p.fuD[2].data[c] = n2;
-  if (sw0) p.fwE[0].data[c] = w[0];
-  if (sw1) p.fwE[1].data[c] = w[1];
-  if (sw2) p.fwE[2].data[c] = w[2];
   p.D[0][c] = d[0];
   p.D[1][c] = d[1];
   p.D[2][c] = d[2];

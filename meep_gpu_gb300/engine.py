@@ -7,12 +7,14 @@ and drives ``mgb_step``. Layout in HBM, all float32 and C-ordered ``(nx, ny, nz)
 * E, D, H: three full volumes each; one inverse-epsilon volume per distinct array
   (the isotropic case aliases one volume for all three components). Outside each H
   component's own-axis integer PML runs MEEP's H is B's word, so H carries B there;
-* PML auxiliaries, read and written only on their membership runs: B and the ``f_w`` of
-  H on each H component's own-axis integer runs, ``f_w`` of E on the own-axis half
-  runs, and the split-field ``fu`` of B (half lattice) and D (integer lattice) on the
-  dsigu runs. Each is allocated as a full volume (HBM is plentiful) so a cell's
-  auxiliary word sits at the cell's own offset and needs no index arithmetic; the cells
-  outside the runs are never touched and move no bytes;
+* PML auxiliaries, read and written only on their membership runs: B on each H
+  component's own-axis integer runs and the split-field ``fu`` of B (half lattice) and
+  D (integer lattice) on the dsigu runs. Each is allocated as a full volume (HBM is
+  plentiful) so a cell's auxiliary word sits at the cell's own offset and needs no index
+  arithmetic; the cells outside the runs are never touched and move no bytes. The
+  ``f_w`` of H and E volumes are allocated too (the adjoint keeps its multipliers of
+  them there) but the forward step moves neither: ``f_w`` of H is B's old word and
+  ``f_w`` of E is recomputed from the old D;
 * polarization: two rotating buffers per pole and driven component, over the bounding
   box of the cells where any pole's sigma is nonzero (P stays zero elsewhere);
 * DFT accumulators ``[ncomp][nfreq][re, im][cells]`` per monitor.
@@ -689,10 +691,12 @@ class Engine:
         split = 0
         if (wave is None and os.environ.get("MEEPGB_SPLIT", "1") != "0" and self.grid.is_metallic(0)
                 and not self.grid.has_bloch):
-            # the two fastest single launches of each half, paired and timed on whole steps
-            # with every split: the fastest launch alone is not always the fastest when the
-            # ranges of both halves overlap
-            tops = [sorted(timed[part], key=timed[part].get)[:2] or [best[part]] for part in (0, 1)]
+            # the three fastest single launches of each half, paired and timed on whole
+            # steps with every split: the fastest launch alone is not always the fastest
+            # when the ranges of both halves overlap, and single launches a few per cent
+            # apart can swap places (on the 192^3 sphere the E half that steps fastest
+            # split came third alone)
+            tops = [sorted(timed[part], key=timed[part].get)[:3] or [best[part]] for part in (0, 1)]
             best_step = float("inf")
             for h in tops[0]:
                 for e in tops[1]:
@@ -782,7 +786,8 @@ class Engine:
         write ``fu`` of B and the slab B (``f_w`` of H is B's old word there: no bytes).
         E half: read H (3 volumes: the slab word or B's) and D (3) and each distinct
         inverse-epsilon volume, write D (3) and E (3); on the slabs read and write ``fu``
-        of D, read and write ``f_w`` of E and read E; per pole and driven component read
+        of D and read E (``f_w`` of E is recomputed from the old D); per pole and driven
+        component read
         P, P_prev and sigma and write P' over the polarization box.
         """
         cells = self.grid.total_cells
@@ -790,7 +795,7 @@ class Engine:
         aux = lambda name: sum(self.aux_cells[f"{name}{a}"] for a in "xyz") if self.pml is not None else 0  # noqa: E731
         h = 9 * cells + 2 * aux("fuB") + 2 * aux("B")
         distinct_inv = len({t.data_ptr() for t in self.inv_eps})
-        e = (12 + distinct_inv) * cells + 2 * aux("fuD") + 3 * aux("fwE")
+        e = (12 + distinct_inv) * cells + 2 * aux("fuD") + aux("fwE")
         for kept in getattr(self, "pole_tensors", []):
             for _, (s, p0, _p1) in kept.items():
                 e += 4 * int(p0.numel())

@@ -643,7 +643,12 @@ class Engine:
         if key in _AUTOTUNE_CACHE:
             self.select(_AUTOTUNE_CACHE[key])
             return self.choice
-        scratch = Engine(self.grid, self.pml, [t.cpu().numpy() for t in self.inv_eps],
+        # one host array per distinct volume, so the scratch aliases the same components
+        # (an isotropic run's E half reads one inverse-epsilon volume, not three)
+        host: Dict[int, np.ndarray] = {}
+        for t in self.inv_eps:
+            host.setdefault(t.data_ptr(), t.cpu().numpy())
+        scratch = Engine(self.grid, self.pml, [host[t.data_ptr()] for t in self.inv_eps],
                          self._pole_specs, [], [], device=self.device, autotune=False,
                          conductivity=self.conductivity)
         stream = torch.cuda.current_stream(self.device)
@@ -726,7 +731,10 @@ class Engine:
 
     def _tune_split(self, scratch: "Engine", halves, stream, with_time: bool = False):
         """The x-range split that steps fastest (0: none), whole steps timed; with
-        ``with_time`` also that split's time (ms per timed run)."""
+        ``with_time`` also that split's time (ms per timed run). More ranges are kept
+        only when they step at least 1 % faster than fewer: on the scratch engine 3 and 4
+        ranges of the 192^3 sphere time within 0.3 % of each other, while on the
+        simulation itself 4 ranges stepped up to 3 % slower."""
         scratch.select(halves)
         scratch.set_split(0)
         best, best_ms = 0, self._run_ms(scratch, stream)
@@ -735,7 +743,7 @@ class Engine:
                 continue
             scratch.set_split(ranges)
             ms = self._run_ms(scratch, stream)
-            if ms < best_ms:
+            if ms < 0.99 * best_ms:
                 best, best_ms = ranges, ms
         scratch.set_split(0)
         return (best, best_ms) if with_time else best

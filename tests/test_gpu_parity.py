@@ -225,6 +225,27 @@ def test_autotuned_choice_steps_the_same_words(gpu):
     driver.close()
 
 
+def test_autotuner_times_the_same_volumes(gpu, monkeypatch):
+    """The autotuner's scratch engine aliases the inverse-epsilon volumes as the run does
+    (an isotropic run's E half reads one volume; a scratch with three would time another
+    workload and rank the launch shapes differently)."""
+    from meep_gpu_gb300 import engine as engine_mod
+
+    engine_mod._AUTOTUNE_CACHE.clear()
+    distinct = []
+    original = engine_mod.Engine.finish
+
+    def recording(self):
+        distinct.append(len({t.data_ptr() for t in self.inv_eps}))
+        return original(self)
+
+    monkeypatch.setattr(engine_mod.Engine, "finish", recording)
+    driver, _, _ = gpu_case(CASES["tile_lorentz"])
+    assert len(distinct) >= 2, "the autotuner built no scratch engine"
+    assert set(distinct) == {1}, distinct
+    driver.close()
+
+
 def test_nonfinite_detector_raises(gpu):
     """A current large enough to overflow float32 is reported by the run, not returned."""
     from meep_gpu_gb300 import FdtdDivergence

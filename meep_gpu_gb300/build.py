@@ -1,8 +1,8 @@
 """Build recipe of the CUDA library ``libmeepgb.so`` (sm_103a, in-tree).
 
-Three translation units compiled by nvcc in parallel and linked into a shared object next
-to this file: the stepping library, the tensor-core DFT contraction and the wavefront
-step kernel. The wavefront unit caches every global load in L2 only (``-dlcm=cg``): its
+Four translation units compiled by nvcc in parallel and linked into a shared object next
+to this file: the stepping library, the tensor-core DFT contraction, the wavefront step
+kernel and the reduced-dimension step kernels. The wavefront unit caches every global load in L2 only (``-dlcm=cg``): its
 persistent CTAs read words other SMs rewrote during the same launch, and L1 is not
 coherent with them. ``-fmad=false`` is part of the numerics contract: no multiply-add may
 be contracted, so every float32 word matches the reference's separately rounded
@@ -20,8 +20,8 @@ from pathlib import Path
 PACKAGE = Path(__file__).resolve().parent
 ROOT = PACKAGE.parent
 CSRC = PACKAGE / "csrc"
-SOURCES = [CSRC / "meepgb.cu", CSRC / "dft_tc.cu", CSRC / "wave.cu"]
-HEADERS = [CSRC / "dft_tc.cuh", CSRC / "step_device.cuh", CSRC / "wave.cuh"]
+SOURCES = [CSRC / "meepgb.cu", CSRC / "dft_tc.cu", CSRC / "wave.cu", CSRC / "reduced.cu"]
+HEADERS = [CSRC / "dft_tc.cuh", CSRC / "step_device.cuh", CSRC / "wave.cuh", CSRC / "reduced.cuh"]
 LIBRARY = PACKAGE / "libmeepgb.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # extra flags per translation unit

@@ -35,6 +35,7 @@
 
 #include "meepgb.h"
 #include "dft_tc.cuh"
+#include "reduced.cuh"
 #include "wave.cuh"
 
 #include <cuda.h>
@@ -89,6 +90,7 @@ namespace {
 template <bool PML, bool MSRC>
 __global__ void __launch_bounds__(256, 4) h_generic_pf(const __grid_constant__ StepParams p,
                                                        int first_step, int xchunk) {
+  step_entry();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
@@ -111,6 +113,7 @@ __global__ void __launch_bounds__(256, 4) h_generic_pf(const __grid_constant__ S
 template <bool PML>
 __global__ void __launch_bounds__(256, 4) e_generic_pf(const __grid_constant__ StepParams p, int parity,
                                                        int xchunk) {
+  step_entry();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
@@ -129,6 +132,7 @@ __global__ void __launch_bounds__(256, 4) e_generic_pf(const __grid_constant__ S
 template <bool PML, bool MSRC>
 __global__ void __launch_bounds__(256, 5) h_generic(const __grid_constant__ StepParams p,
                                                     int first_step, int xchunk) {
+  step_entry();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
@@ -157,6 +161,7 @@ __global__ void __launch_bounds__(256, 5) h_generic(const __grid_constant__ Step
 template <bool PML>
 __global__ void __launch_bounds__(256, 5) e_generic(const __grid_constant__ StepParams p, int parity,
                                                     int xchunk) {
+  step_entry();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
@@ -184,6 +189,7 @@ template <bool PML, bool MSRC>
 __global__ void __launch_bounds__(256, 4) h_generic_cond(const __grid_constant__ StepParams p,
                                                       const __grid_constant__ mgb_conductivity cp,
                                                       int first_step, int xchunk) {
+  step_entry();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
@@ -212,6 +218,7 @@ template <bool PML>
 __global__ void __launch_bounds__(256, 4) e_generic_cond(const __grid_constant__ StepParams p,
                                                       const __grid_constant__ mgb_conductivity cp,
                                                       int parity, int xchunk) {
+  step_entry();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
@@ -329,6 +336,7 @@ template <bool PML>
 __global__ void __launch_bounds__(kThreads, 2) h_tile(const __grid_constant__ StepParams p,
                                                      const __grid_constant__ TileMaps maps,
                                                      int first_step, int xchunk) {
+  step_entry();
   extern __shared__ __align__(128) unsigned char smem[];
   const int S = maps.stages;
   const int stage_bytes = 3 * kBoxHalo + 3 * kBoxOwn;
@@ -442,6 +450,7 @@ template <bool PML>
 __global__ void __launch_bounds__(kThreads, 2) e_tile(const __grid_constant__ StepParams p,
                                                      const __grid_constant__ TileMaps maps,
                                                      int parity, int xchunk) {
+  step_entry();
   extern __shared__ __align__(128) unsigned char smem[];
   const int S = maps.stages;
   const int stage_bytes = 3 * kBoxHalo + (3 + maps.ninv) * kBoxOwn;
@@ -566,6 +575,7 @@ template <bool PML>
 __global__ void __launch_bounds__(kWsThreads, 2) e_ws(const __grid_constant__ StepParams p,
                                                      const __grid_constant__ TileMaps maps,
                                                      int parity, int xchunk) {
+  step_entry();
   extern __shared__ __align__(128) unsigned char smem[];
   const int S = maps.stages;
   const int stage_bytes = 3 * kBoxHalo + (3 + maps.ninv) * kBoxOwn;
@@ -1597,6 +1607,9 @@ struct mgb_sim {
   // Mirror folds: the ghost lists, and the step whose H half the B ghosts' kept state is
   // for (-1: none kept yet).
   bool folded = false;
+  // step kernels of an unsplit plan launched as programmatic dependents (MEEPGB_PDL=0 at
+  // mgb_create: plain launches)
+  bool pdl = true;
   FoldArgs fold = {};
   long long fold_kept = -1;
   // The first entry of each x plane in each ghost list (nx + 1 entries), kept when every
@@ -1956,6 +1969,8 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
   if (sim == nullptr) return fail(MGB_ERR_ARGUMENT, "host allocation of the plan failed");
   sim->desc = d;
   sim->desc.conductivity = nullptr;  // the caller's struct need not outlive this call
+  const char* pdl = getenv("MEEPGB_PDL");
+  sim->pdl = !(pdl != nullptr && pdl[0] == '0');
   if (lossy) {
     sim->has_cond = true;
     sim->cond = *d.conductivity;
@@ -2074,11 +2089,34 @@ int mgb_set_source_words(mgb_sim* sim, const double* words, int64_t first_step, 
 
 namespace {
 
-// Launch a step kernel.
+// Whether step kernels launch as programmatic dependents: in an unsplit plan the next
+// half's CTAs then take the SMs the last wave of the half before frees (192^3 sphere:
+// 0.1542 -> 0.1485 ms a step); across the x-range split's streams their waiting CTAs
+// would hold slots the other ranges' kernels fill (0.1400 -> 0.1509), so a split plan
+// launches plainly, as does a plan made with MEEPGB_PDL=0.
+bool step_pdl(const mgb_sim* sim) { return sim->pdl && sim->split.ranges <= 1; }
+
+// Launch a step kernel, as a programmatic dependent of the kernel before it in the
+// stream when step_pdl (every step kernel begins with step_entry, which waits for that
+// kernel before touching memory).
 template <typename... KArgs, typename... Args>
-void launch_step(const mgb_sim*, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+void launch_step(const mgb_sim* sim, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
                  Args&&... args) {
-  kernel<<<grid, block, smem, s>>>(std::forward<Args>(args)...);
+  if (!step_pdl(sim)) {
+    kernel<<<grid, block, smem, s>>>(std::forward<Args>(args)...);
+    return;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);  // errors: launch_error
 }
 
 // Add a monitor's buffered samples to its accumulators: one phase table and one
@@ -2154,6 +2192,13 @@ int launch_part_kernels(mgb_sim* sim, long long n, int part, cudaStream_t s, int
     p.l2pf = hc.l2pf ? 1 : 0;  // per half; the launch takes the parameters by value
     p.xbase = plane0 / xc;     // ditto: the first chunk of this launch's planes
     const bool msrc = p.nsrc_h > 0;  // the H kernels with the magnetic deposit compiled in
+    if (p.inv != 0) {  // a 2-D or 1-D run: its own kernels, whatever the generic family
+      const cudaError_t err = mgbred::launch_half(p, sim->cond, sim->has_cond, msrc, pml, part,
+                                                  part == 0 ? (int)(n == 0) : (int)(n & 1), grid, block, xc,
+                                                  step_pdl(sim), s);
+      if (err != cudaSuccess) return cuda_error(err, "reduced-dimension step launch");
+      return MGB_OK;
+    }
     if (sim->has_cond) {
       if (part == 0) {
         if (pml && msrc) launch_step(sim, h_generic_cond<true, true>, grid, block, 0, s, p, sim->cond, (int)(n == 0), xc);
@@ -2502,6 +2547,8 @@ int mgb_set_wave(mgb_sim* sim, int32_t family, int32_t block_z, int32_t block_y,
   if (sim->folded || sim->step.bloch || sim->has_cond)
     return fail(MGB_ERR_UNSUPPORTED, "the wavefront path steps runs without mirror folds, Bloch phases or a "
                                      "conductivity");
+  if (sim->step.inv != 0)
+    return fail(MGB_ERR_UNSUPPORTED, "the wavefront path steps 3-D runs");
   if (!sim->desc.metallic[0])
     return fail(MGB_ERR_UNSUPPORTED, "the wavefront path needs a metallic x axis (a periodic x would make the "
                                      "first chunk wait on the last)");

@@ -65,9 +65,14 @@ struct StepParams {
 // dtdx * (S1 - A1) and (-dtdx) * (S2 - A2) rather than the full bracket, which rounds
 // differently where the absent partner is nonzero. axis1 / axis2: the partners'
 // derivative axes.
+// RED: the march of a reduced-dimension run (the kernels send such runs to one general
+// march compiled with it); the 3-D marches compile the full bracket alone, since the
+// branches below, inlined into every march, cost them registers (the H march spilled
+// 128 bytes a thread instead of 4).
+template <bool RED>
 __device__ __forceinline__ float curl_term(const StepParams& p, float s1, float a1, float a2, float s2,
                                            int axis1, int axis2) {
-  if (p.inv == 0) return p.dtdx * (((s1 - a1) + a2) - s2);
+  if (!RED || p.inv == 0) return p.dtdx * (((s1 - a1) + a2) - s2);
   const bool have1 = ((p.inv >> axis1) & 1) == 0, have2 = ((p.inv >> axis2) & 1) == 0;
   if (have1 && have2) return p.dtdx * (((s1 - a1) + a2) - s2);
   if (have1) return p.dtdx * (s1 - a1);
@@ -150,6 +155,16 @@ __device__ __forceinline__ float bloch_word(const P& p, int axis, bool conj, flo
   const float b = conj ? -p.bim[axis] : p.bim[axis];
   const float other = partner[c];
   return p.part ? (a * own) + (b * other) : (a * own) - (b * other);
+}
+
+// Entry of a step kernel launched as its stream predecessor's programmatic dependent:
+// let this grid's own dependent be scheduled once every CTA here has started (its CTAs
+// then take the SM slots this grid's last wave frees, and wait), then wait for the
+// predecessor grid to complete with its memory visible, before any global access. In a
+// launch without the programmatic attribute both instructions do nothing.
+__device__ __forceinline__ void step_entry() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
 __device__ __forceinline__ void l2_prefetch(const float* p) {
@@ -681,7 +696,7 @@ __device__ __forceinline__ int cta_axes(const StepParams& p, int i0, int i1, int
 // ------------------------------------------------------------------------------------
 // Generic kernels: plain loads, one thread per (y, z) column marching over x.
 // One thread's column (j, k) of the H half over planes [i0, i1).
-template <bool PML, bool COND = false, int AX = -1, bool MSRC = false, bool BLOCH = false>
+template <bool PML, bool COND = false, int AX = -1, bool MSRC = false, bool BLOCH = false, bool RED = false>
 __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i0, int i1,
                                         int first_step, const mgb_conductivity* cp = nullptr) {
   const int sx = p.ny * p.nz;
@@ -749,9 +764,9 @@ __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i
       if (k == 0) { gx2 = bloch_word(p, 2, true, ey, p.pE[1], c); gy1 = bloch_word(p, 2, true, ex, p.pE[0], c); }
       if (i == 0) { gy2 = bloch_word(p, 0, true, ez, p.pE[2], c); gz1 = bloch_word(p, 0, true, ey, p.pE[1], c); }
     }
-    const float cx = curl_term(p, ez_yp, gx1, gx2, ey_zp, 1, 2);
-    const float cy = curl_term(p, ex_zp, gy1, gy2, ez_xp, 2, 0);
-    const float cz = curl_term(p, ey_xp, gz1, gz2, ex_yp, 0, 1);
+    const float cx = curl_term<RED>(p, ez_yp, gx1, gx2, ey_zp, 1, 2);
+    const float cy = curl_term<RED>(p, ex_zp, gy1, gy2, ez_xp, 2, 0);
+    const float cz = curl_term<RED>(p, ey_xp, gz1, gz2, ex_yp, 0, 1);
     float h_new[3];
     h_cell<PML, COND, AX, MSRC>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, h_old, ax, h_new, cp);
     p.H[0][c] = h_new[0];
@@ -763,7 +778,7 @@ __device__ __forceinline__ void h_march(const StepParams& p, int j, int k, int i
 }
 
 // One thread's column (j, k) of the E half over planes [i0, i1).
-template <bool PML, bool COND = false, int AX = -1, bool BLOCH = false>
+template <bool PML, bool COND = false, int AX = -1, bool BLOCH = false, bool RED = false>
 __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i0, int i1,
                                         int parity, const double* words,
                                         const mgb_conductivity* cp = nullptr) {
@@ -832,9 +847,9 @@ __device__ __forceinline__ void e_march(const StepParams& p, int j, int k, int i
       if (k == 0) { gx2 = bloch_word(p, 2, false, hy, p.pH[1], c); gy1 = bloch_word(p, 2, false, hx, p.pH[0], c); }
       if (i == 0) { gy2 = bloch_word(p, 0, false, hz, p.pH[2], c); gz1 = bloch_word(p, 0, false, hy, p.pH[1], c); }
     }
-    const float cx = curl_term(p, hz_ym, gx1, gx2, hy_zm, 1, 2);
-    const float cy = curl_term(p, hx_zm, gy1, gy2, hz_xm, 2, 0);
-    const float cz = curl_term(p, hy_xm, gz1, gz2, hx_ym, 0, 1);
+    const float cx = curl_term<RED>(p, hz_ym, gx1, gx2, hy_zm, 1, 2);
+    const float cy = curl_term<RED>(p, hx_zm, gy1, gy2, hz_xm, 2, 0);
+    const float cz = curl_term<RED>(p, hy_xm, gz1, gz2, hx_ym, 0, 1);
     e_cell<PML, COND, AX>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, d, inv, words, ax, cp);
     hy_xm = hy;
     hz_xm = hz;
@@ -874,7 +889,7 @@ __device__ __forceinline__ void h_loads(const StepParams& p, HLoads& L, int i, i
   L.h[2] = p.H[2][c];
 }
 
-template <bool PML, int AX = -1, bool MSRC = false>
+template <bool PML, int AX = -1, bool MSRC = false, bool RED = false>
 __device__ __forceinline__ void h_march_pf(const StepParams& p, int j, int k, int i0, int i1,
                                            int first_step) {
   const int sx = p.ny * p.nz;
@@ -926,9 +941,9 @@ __device__ __forceinline__ void h_march_pf(const StepParams& p, int j, int k, in
     }
     HAux ax = {};
     if (PML && axes != 0) h_aux_load(p, hcol, pl, c, ax);
-    const float cx = curl_term(p, cur.ez_yp, ez, ey, cur.ey_zp, 1, 2);
-    const float cy = curl_term(p, cur.ex_zp, cur.ex, ez, cur.ez_xp, 2, 0);
-    const float cz = curl_term(p, cur.ey_xp, ey, cur.ex, cur.ex_yp, 0, 1);
+    const float cx = curl_term<RED>(p, cur.ez_yp, ez, ey, cur.ey_zp, 1, 2);
+    const float cy = curl_term<RED>(p, cur.ex_zp, cur.ex, ez, cur.ez_xp, 2, 0);
+    const float cz = curl_term<RED>(p, cur.ey_xp, ey, cur.ex, cur.ex_yp, 0, 1);
     float h_new[3];
     h_cell<PML, false, AX, MSRC>(p, hcol, pl, axes, first_step, i, j, k, c, cx, cy, cz, cur.h, ax, h_new);
     p.H[0][c] = h_new[0];
@@ -969,7 +984,7 @@ __device__ __forceinline__ void e_loads(const StepParams& p, ELoads& L, int i, i
   L.inv[2] = __ldg(p.inv_eps[2] + c);
 }
 
-template <bool PML, int AX = -1>
+template <bool PML, int AX = -1, bool RED = false>
 __device__ __forceinline__ void e_march_pf(const StepParams& p, int j, int k, int i0, int i1,
                                            int parity, const double* words) {
   const int sx = p.ny * p.nz;
@@ -1025,9 +1040,9 @@ __device__ __forceinline__ void e_march_pf(const StepParams& p, int j, int k, in
     }
     EAux ax = {};
     if (PML && axes != 0) e_aux_load(p, ecol, pl, c, ax);
-    const float cx = curl_term(p, cur.hz_ym, cur.hz, cur.hy, cur.hy_zm, 1, 2);
-    const float cy = curl_term(p, cur.hx_zm, cur.hx, cur.hz, hz_xm, 2, 0);
-    const float cz = curl_term(p, hy_xm, cur.hy, cur.hx, cur.hx_ym, 0, 1);
+    const float cx = curl_term<RED>(p, cur.hz_ym, cur.hz, cur.hy, cur.hy_zm, 1, 2);
+    const float cy = curl_term<RED>(p, cur.hx_zm, cur.hx, cur.hz, hz_xm, 2, 0);
+    const float cz = curl_term<RED>(p, hy_xm, cur.hy, cur.hx, cur.hx_ym, 0, 1);
     e_cell<PML, false, AX>(p, ecol, pl, axes, parity, i, j, k, c, cx, cy, cz, cur.d, cur.inv, words, ax);
     hy_xm = cur.hy;
     hz_xm = cur.hz;

@@ -565,11 +565,11 @@ class Engine:
 
     @property
     def wave_eligible(self) -> bool:
-        """Whether the wavefront path can step this plan (metallic x, no folds, no Bloch
-        phase, no conductivity)."""
+        """Whether the wavefront path can step this plan (a 3-D run, metallic x, no folds,
+        no Bloch phase, no conductivity)."""
         grid = self.grid
         return (grid.is_metallic(0) and not grid.has_symmetry and not grid.has_bloch
-                and not self.conductivity)
+                and not self.conductivity and grid.dimensions == 3)
 
     @property
     def split_eligible(self) -> bool:

@@ -48,9 +48,10 @@ def x_metallic(case) -> bool:
 
 
 def wave_steps(case) -> bool:
-    """Whether the wavefront path takes a case (metallic x, no folds, Bloch or conductivity)."""
+    """Whether the wavefront path takes a case (a 3-D run, metallic x, no folds, Bloch or
+    conductivity)."""
     return (x_metallic(case) and not case.get("symmetry") and not case.get("k_point")
-            and not case.get("conductivity"))
+            and not case.get("conductivity") and not case.get("dims"))
 
 
 def split_steps(case) -> bool:
@@ -85,7 +86,7 @@ def test_fields_are_the_reference_words(gpu, name, mode):
     # the tile kernels step 3-D runs whose z extent is a multiple of 4
     tileable = case["n"][2] % 4 == 0 and not case.get("dims")
     if mode == "wave" and not wave_steps(case):
-        pytest.skip("the wavefront path steps metallic-x runs without folds, Bloch phases or conductivity")
+        pytest.skip("the wavefront path steps 3-D metallic-x runs without folds, Bloch phases or conductivity")
     if mode == "split" and not split_steps(case):
         pytest.skip("the x-range split steps metallic-x runs without Bloch phases")
     if (case.get("conductivity") or case.get("k_point")) and mode not in ("generic", "l2", "wave", "split", "ylanes"):

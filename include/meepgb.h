@@ -207,7 +207,8 @@ typedef struct mgb_sim_desc {
    * one periodic cell each). A curl partner whose derivative lies along such an axis is
    * absent, as MEEP's step plan drops it (fields.cpp figure_out_step_plan): the curl is
    * dtdx * (g1s - g1) or (-dtdx) * (g2s - g2) instead of the full bracket. Such runs
-   * step on the generic kernel families and are refused by the batch and the adjoint. */
+   * take a generic kernel family (their own kernels, with the chosen launch shape) and are
+   * refused by the tile kernels, the wavefront path, the batch and the adjoint. */
   int32_t invariant;
 } mgb_sim_desc;
 

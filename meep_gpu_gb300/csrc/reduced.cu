@@ -13,7 +13,7 @@ using namespace mgbstep;
 namespace {
 
 template <bool PML, bool COND, bool MSRC>
-__global__ void __launch_bounds__(256, 4) h_reduced(const __grid_constant__ StepParams p,
+__global__ void __launch_bounds__(256, COND ? 4 : 5) h_reduced(const __grid_constant__ StepParams p,
                                                     const __grid_constant__ mgb_conductivity cp, int first_step,
                                                     int xchunk) {
   step_entry();
@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(256, 4) h_reduced(const __grid_constant__ Step
 }
 
 template <bool PML, bool COND>
-__global__ void __launch_bounds__(256, 4) e_reduced(const __grid_constant__ StepParams p,
+__global__ void __launch_bounds__(256, COND ? 4 : 5) e_reduced(const __grid_constant__ StepParams p,
                                                     const __grid_constant__ mgb_conductivity cp, int parity,
                                                     int xchunk) {
   step_entry();

@@ -170,6 +170,23 @@ def test_ring_depth_does_not_change_a_word(gpu, stages, kernels, monkeypatch):
     driver.close()
 
 
+@pytest.mark.parametrize("pdl", ["0", "1"])
+@pytest.mark.parametrize("kernels", [GENERIC, PREFETCH, L2_PREFETCH, TILES, WARP_SPECIALIZED])
+def test_programmatic_launches_change_no_word(gpu, kernels, pdl, monkeypatch):
+    """An unsplit plan launches each half as its predecessor's programmatic dependent
+    (every step kernel waits for it before touching memory); with MEEPGB_PDL=0 the
+    launches are plain. Both step the reference's words, with every kernel family."""
+    monkeypatch.setenv("MEEPGB_PDL", pdl)
+    case = CASES["tile_lorentz"]
+    gold = golden_io.fields("tile_lorentz")
+    driver, _, _ = gpu_case(case, kernels=kernels)
+    assert driver.engine.split == 0
+    for c in FIELDS:
+        assert np.array_equal(driver.get_field(c, cell_centered=False), gold[c]), (kernels, pdl, c)
+    assert driver.engine.status.item() == 0
+    driver.close()
+
+
 def test_chunked_runs_equal_one_run(gpu):
     case = CASES["lorentz_slab"]
     gold = golden_io.fields("lorentz_slab")

@@ -54,7 +54,9 @@ AUTOTUNE_CANDIDATES = ((0, 32, 4, 4), (0, 32, 8, 4), (0, 32, 4, 8), (0, 64, 2, 8
                        (2, 32, 4, 2), (2, 32, 2, 4), (3, 64, 8, 4), (3, 64, 8, 8), (3, 64, 8, 16),
                        (4, 32, 4, 4), (4, 16, 8, 4), (4, 32, 4, 8), (4, 32, 8, 4), (4, 32, 4, 2),
                        (4, 32, 8, 2), (4, 32, 8, 8), (4, 64, 4, 4), (4, 16, 16, 4), (4, 32, 2, 4),
-                       (5, 32, 4, 4), (5, 16, 8, 4), (5, 32, 4, 8), (5, 32, 2, 8), (5, 32, 4, 2))
+                       (5, 32, 4, 4), (5, 16, 8, 4), (5, 32, 4, 8), (5, 32, 2, 8), (5, 32, 4, 2),
+                       # short x chunks: more CTAs for grids too small to fill the SMs
+                       (0, 16, 16, 2), (4, 16, 16, 2), (0, 16, 16, 1), (0, 16, 8, 1))
 _AUTOTUNE_CACHE: Dict[tuple, Tuple[int, int, int, int]] = {}
 
 

@@ -1444,8 +1444,9 @@ __global__ void __launch_bounds__(256) copy_box(const __grid_constant__ StepPara
 // and after the half's sources it becomes the parity-signed word of stored row 2 (the
 // product of the parities at a corner), then zero_metal of the other axes' walls, and
 // its E (H) is stepped from that word with the ghost's own coefficients. The step
-// kernels have by then overwritten the ghost's E, f_w and P (H, f_w) from the wall word,
-// so each ghost's state from before the half is kept in `saved` (words [w * count + t]):
+// kernels have by then overwritten the ghost's E, D and P (H and B) from the wall word,
+// so each ghost's state from before the half is kept in `saved` (words [w * count + t]:
+// E, its f_w formed from the old D and P, and P; H and B's old word as its f_w):
 // the H fold kernel keeps the D ghosts' state for the E half that follows, the E fold
 // kernel the B ghosts' state for the next step's H half.
 

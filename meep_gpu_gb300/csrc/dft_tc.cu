@@ -367,6 +367,13 @@ int table_rows(int nfreq) { return ((2 * nfreq + kRows - 1) / kRows) * kRows; }
 
 size_t table_bytes(int nfreq) { return (size_t)(table_rows(nfreq) / kRows) * kTableTile; }
 
+cudaError_t preload_kernels() {
+  cudaFuncAttributes attr;
+  cudaError_t err = cudaFuncGetAttributes(&attr, reinterpret_cast<const void*>(table_kernel));
+  if (err == cudaSuccess) err = cudaFuncGetAttributes(&attr, reinterpret_cast<const void*>(contract_kernel));
+  return err;
+}
+
 cudaError_t launch_contraction(const double* omega, long long first_post, int stride, double dt, int half_back,
                                double scale, const Contraction& c, cudaStream_t stream) {
   static_assert(kTableTile == kRows * kDepth * 2 * sizeof(float), "a tile image holds its rows' two parts");

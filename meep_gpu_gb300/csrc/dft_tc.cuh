@@ -54,4 +54,8 @@ size_t table_bytes(int nfreq);
 cudaError_t launch_contraction(const double* omega, long long first_post, int stride, double dt,
                                int half_back, double scale, const Contraction& c, cudaStream_t stream);
 
+// Load the table and contraction kernels now (a plan's creation) rather than at a run's
+// first flush, which under lazy module loading can fall inside its timed steps.
+cudaError_t preload_kernels();
+
 }  // namespace mgbdft

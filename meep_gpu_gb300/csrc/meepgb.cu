@@ -1966,6 +1966,21 @@ int mgb_create(const mgb_sim_desc* desc, mgb_sim** out) {
   } else if (d.fold.count[0] != 0 || d.fold.count[1] != 0) {
     return fail(MGB_ERR_ARGUMENT, "mirror-fold ghost lists without a mirror plane");
   }
+  {
+    // Load the kernels a run may first launch only after its first steps (the monitors'
+    // samples and contractions, and a reduced-dimension run's step kernels) now: under
+    // lazy module loading a first launch loads its whole module, which cost a 2-D run's
+    // first timed call about 11 ms when its first sample was this module's first launch.
+    cudaFuncAttributes attr;
+    const void* monitors[] = {reinterpret_cast<const void*>(dft_sample), reinterpret_cast<const void*>(dft_accumulate),
+                              reinterpret_cast<const void*>(flux_reduce)};
+    cudaError_t err = cudaSuccess;
+    for (const void* k : monitors)
+      if (err == cudaSuccess) err = cudaFuncGetAttributes(&attr, k);
+    if (err == cudaSuccess) err = mgbdft::preload_kernels();
+    if (err == cudaSuccess && (d.invariant & 7) != 0) err = mgbred::preload_kernels();
+    if (err != cudaSuccess) return cuda_error(err, "loading the monitor and step kernels");
+  }
   mgb_sim* sim = new (std::nothrow) mgb_sim();
   if (sim == nullptr) return fail(MGB_ERR_ARGUMENT, "host allocation of the plan failed");
   sim->desc = d;

@@ -81,6 +81,22 @@ cudaError_t launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, bool pdl, cu
 
 }  // namespace
 
+cudaError_t preload_kernels() {
+  const void* kernels[] = {
+      reinterpret_cast<const void*>(h_reduced<true, true, true>), reinterpret_cast<const void*>(h_reduced<true, true, false>),
+      reinterpret_cast<const void*>(h_reduced<false, true, true>), reinterpret_cast<const void*>(h_reduced<false, true, false>),
+      reinterpret_cast<const void*>(h_reduced<true, false, true>), reinterpret_cast<const void*>(h_reduced<true, false, false>),
+      reinterpret_cast<const void*>(h_reduced<false, false, true>), reinterpret_cast<const void*>(h_reduced<false, false, false>),
+      reinterpret_cast<const void*>(e_reduced<true, true>), reinterpret_cast<const void*>(e_reduced<false, true>),
+      reinterpret_cast<const void*>(e_reduced<true, false>), reinterpret_cast<const void*>(e_reduced<false, false>)};
+  for (const void* k : kernels) {
+    cudaFuncAttributes attr;
+    const cudaError_t err = cudaFuncGetAttributes(&attr, k);
+    if (err != cudaSuccess) return err;
+  }
+  return cudaSuccess;
+}
+
 cudaError_t launch_half(const StepParams& p, const mgb_conductivity& cp, bool cond, bool msrc, bool pml, int part,
                         int flag, dim3 grid, dim3 block, int xchunk, bool pdl, cudaStream_t s) {
   if (part == 0) {

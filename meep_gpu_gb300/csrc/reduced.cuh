@@ -19,4 +19,9 @@ namespace mgbred {
 cudaError_t launch_half(const mgbstep::StepParams& p, const mgb_conductivity& cp, bool cond, bool msrc, bool pml,
                         int part, int flag, dim3 grid, dim3 block, int xchunk, bool pdl, cudaStream_t s);
 
+// Load every reduced-dimension kernel now (a plan's creation) rather than at its first
+// launch: under lazy module loading that first launch fell inside a run's first timed
+// call and cost it about 11 ms.
+cudaError_t preload_kernels();
+
 }  // namespace mgbred

@@ -88,6 +88,22 @@ def autotune_key(grid: Grid, pml: Optional[PML], npoles: int, ninv: int, lossy: 
     return (grid.shape, grid.boundaries, faces, npoles, ninv, lossy)
 
 
+def host_volumes(volumes: Sequence[torch.Tensor]) -> List[np.ndarray]:
+    """Host copies of device volumes, one array per distinct volume: components that share
+    a device volume share the host array, so an engine built from them (which keeps one
+    device volume per distinct host array) aliases the same components. The autotuner's
+    scratch engine is built this way: with three copies of an isotropic run's one
+    inverse-epsilon volume its E half would read two more words a cell than the run's."""
+    host: Dict[int, np.ndarray] = {}
+    out = []
+    for t in volumes:
+        key = t.data_ptr()
+        if key not in host:
+            host[key] = t.cpu().numpy()
+        out.append(host[key])
+    return out
+
+
 def _ptr(t: Optional[torch.Tensor]) -> Optional[int]:
     return None if t is None else t.data_ptr()
 
@@ -645,12 +661,7 @@ class Engine:
         if key in _AUTOTUNE_CACHE:
             self.select(_AUTOTUNE_CACHE[key])
             return self.choice
-        # one host array per distinct volume, so the scratch aliases the same components
-        # (an isotropic run's E half reads one inverse-epsilon volume, not three)
-        host: Dict[int, np.ndarray] = {}
-        for t in self.inv_eps:
-            host.setdefault(t.data_ptr(), t.cpu().numpy())
-        scratch = Engine(self.grid, self.pml, [host[t.data_ptr()] for t in self.inv_eps],
+        scratch = Engine(self.grid, self.pml, host_volumes(self.inv_eps),
                          self._pole_specs, [], [], device=self.device, autotune=False,
                          conductivity=self.conductivity)
         stream = torch.cuda.current_stream(self.device)

@@ -29,6 +29,16 @@ def test_library_loads_and_exports_every_declared_symbol():
     assert lib.mgb_abi_version() == _lib.MGB_ABI_VERSION
 
 
+def test_build_compiles_every_translation_unit():
+    """The GPU machine has only what build() compiles: every CUDA source and header of the
+    package is in the recipe (a unit left out would leave its kernels unresolved there)."""
+    from meep_gpu_gb300 import build
+
+    csrc = ROOT / "meep_gpu_gb300" / "csrc"
+    assert {p.name for p in csrc.glob("*.cu")} == {p.name for p in build.SOURCES}
+    assert {p.name for p in csrc.glob("*.cuh")} == {p.name for p in build.HEADERS}
+
+
 def test_create_refuses_bad_descriptors_without_a_gpu():
     lib = _lib.load()
     desc = _lib.MgbSimDesc()

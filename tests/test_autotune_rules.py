@@ -1,6 +1,7 @@
 """The autotuner's host-side rules, without a GPU: the scratch engine it times candidates
 on aliases the run's inverse-epsilon volumes as the run does, and the x-range split it
-keeps takes more ranges only when they step at least 1 % faster than fewer."""
+keeps takes more ranges only when they step at least 1 % faster than fewer, and the
+wavefront path is offered to 3-D runs only."""
 
 from types import SimpleNamespace
 
@@ -61,3 +62,23 @@ def test_split_skips_ranges_thinner_than_two_planes(monkeypatch):
     times = {r: 10.0 - r for r in (0,) + SPLIT_CANDIDATES}  # every split faster
     ranges, _ = _tuned(times, monkeypatch, nx=8)
     assert ranges == 4  # 6 ranges of an 8-plane grid are refused before they are timed
+
+
+def _engine_on(grid, conductivity=None):
+    engine = Engine.__new__(Engine)
+    engine.grid = grid
+    engine.conductivity = conductivity or {}
+    return engine
+
+
+def test_wavefront_path_takes_3d_runs_only():
+    """The wavefront marches compile the 3-D curl alone: a 2-D or 1-D run never takes
+    them (the library refuses it too), while a plain 3-D metallic-x run may."""
+    from meep_gpu_gb300.grid import Grid
+
+    assert _engine_on(Grid((4.0, 4.0, 4.0), 10, 0.5, "metallic")).wave_eligible
+    two_d = Grid((4.0, 4.0, 0.0), 10, 0.5, {"x": "metallic", "y": "metallic"}, dimensions=2)
+    assert two_d.dimensions == 2 and two_d.is_metallic(0)
+    assert not _engine_on(two_d).wave_eligible
+    lossy = _engine_on(Grid((4.0, 4.0, 4.0), 10, 0.5, "metallic"), conductivity={"Dz": object()})
+    assert not lossy.wave_eligible

@@ -367,7 +367,9 @@ def main():
                 "per_kernel": {k: {"ms": round(v["ms"], 4), "GB/s": round(v["gbs"], 1),
                                    "frac": round(v["gbs"] / peak, 4)} for k, v in timed.items()},
                 "step_bytes_per_cell": round(step_bytes / cells, 2),
-                "step_frac": round(step_bytes / ((ms / args.steps) / 1e3) / 1e9 / peak, 4)}
+                "step_frac": round(step_bytes / ((ms / args.steps) / 1e3) / 1e9 / peak, 4),
+                "bytes_counted": "words the step moves; the f_w words of H and E, which the "
+                                 "reference also moves, are formed in registers and not counted"}
     driver.close()
     del driver, engine
     torch.cuda.empty_cache()
